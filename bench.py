@@ -1,0 +1,294 @@
+"""Benchmark of the GB300 pair-counting engines.
+
+One JSON line on stdout (rank 0).  Metric: in-range ordered pair evaluations
+per second (pairs whose separation passes the outermost bin, read exactly
+from the counts), on the configuration named in ``config.workload``:
+
+  xyz2m   (default) npairs_xy_z, 2,000,000 clustered points, L = 1000,
+          20 log rp bins 0.1-30 x 40 linear pi bins 0-40
+  3d100k  npairs_3d, 100,000 uniform points, L = 250, 15 log bins 0.1-20
+  3d10m   npairs_3d, 10,000,000 clustered points, L = 2000, 30 log bins 0.5-50
+
+A step is one full engine call (cell-list build + count + readback) on
+device-resident inputs; L2 is flushed (256 MiB write) between steps outside
+the timed events.  ``e2e`` repeats the step through the public drop-in API
+from pinned host memory.  ``--impl reference`` times the CPU oracle (a C
+restatement of the reference engines, all host threads) on a bounded sample.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    "xyz2m": dict(kind="xyz", n=2_000_000, L=1000.0, ncen=200_000, logm=(11.0, 15.0),
+                  bins=np.logspace(-1, np.log10(30), 20), bins2=np.linspace(0, 40, 40)),
+    "3d100k": dict(kind="3d", n=100_000, L=250.0, ncen=0, bins=np.logspace(-1, np.log10(20), 15)),
+    "3d10m": dict(kind="3d", n=10_000_000, L=2000.0, ncen=1_000_000, logm=(11.0, 15.5),
+                  bins=np.logspace(np.log10(0.5), np.log10(50), 30)),
+}
+
+
+def make_points(w, seed=2):
+    from halotools_gb300 import mocks
+    if w["ncen"] == 0:
+        return np.random.default_rng(0).uniform(0, w["L"], (w["n"], 3))
+    return mocks.clustered_points(w["n"], w["L"], w["ncen"], logm_range=w["logm"], seed=seed)
+
+
+def in_range(kind, out):
+    return int(out[-1] if kind == "3d" else out[-1, -1])
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 7:
+                continue
+            try:
+                sm.append(float(p[0]))
+                smax = float(p[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[3:7]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def call_device(plan, kind, xd, n, w, box, out):
+    """One engine call on device-resident positions (sample2 is sample1)."""
+    from halotools_gb300 import _native as N
+    ptr = xd.data_ptr()
+    if kind == "3d":
+        rc = plan.lib.gbp_npairs_3d(plan.handle, ptr, n, ptr, n, N.pd(w["bins"]), len(w["bins"]),
+                                    N.pd(box), 1, N.GBP_MEM_DEVICE, N.pi64(out))
+    else:
+        rc = plan.lib.gbp_npairs_xy_z(plan.handle, ptr, n, ptr, n, N.pd(w["bins"]),
+                                      len(w["bins"]), N.pd(w["bins2"]), len(w["bins2"]),
+                                      N.pd(box), 1, N.GBP_MEM_DEVICE, N.pi64(out))
+    plan.check(rc)
+
+
+def cpu_sample(x, w, frac_side):
+    """Points inside the sub-cube [0, frac_side*L)^3, counted non-periodically."""
+    sub = x[np.all(x < frac_side * w["L"], axis=1)]
+    return np.ascontiguousarray(sub)
+
+
+def run_cpu(w, x, steps, warmup, frac_side, threads):
+    from oracle import oracle
+    sub = cpu_sample(x, w, frac_side)
+    f = (lambda: oracle.npairs_3d(sub, sub, w["bins"], num_threads=threads)) if w["kind"] == "3d" \
+        else (lambda: oracle.npairs_xy_z(sub, sub, w["bins"], w["bins2"], num_threads=threads))
+    for _ in range(warmup):
+        f()
+    t0 = time.perf_counter()
+    pairs = 0
+    for _ in range(steps):
+        pairs += in_range(w["kind"], f())
+    dt = time.perf_counter() - t0
+    return pairs / dt, dt, len(sub)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="xyz2m", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    w = WORKLOADS[args.workload]
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    cfg = {"workload": args.workload, "engine": "npairs_" + ("3d" if w["kind"] == "3d" else "xy_z"),
+           "points": w["n"], "box": w["L"], "bins": len(w["bins"]),
+           "bins2": len(w["bins2"]) if "bins2" in w else None, "autocorr": True,
+           "l2": "flushed between steps (256 MiB write, outside the timed events)"}
+    metric = "pair evals/s (in-range ordered pairs, exact counts)"
+    threads = os.cpu_count() or 1
+    # CPU sample: a sub-cube holding about 1/8 (xyz2m, 3d100k) or 1/64 (3d10m) of the box
+    frac_side = {"xyz2m": 0.5, "3d100k": 1.0, "3d10m": 0.25}[args.workload]
+
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        x = make_points(w)
+        value, dt, nsub = run_cpu(w, x, args.steps, args.warmup, frac_side, threads)
+        sample = ("%d points in the sub-cube [0, %.0f)^3 of the workload, non-periodic, "
+                  "%d steps" % (nsub, frac_side * w["L"], args.steps))
+        line = {"impl": "reference", "metric": metric, "value": value, "unit": "pairs/s",
+                "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": cfg,
+                "cpu_baseline": {"value": value, "unit": "pairs/s", "cores": threads,
+                                 "kind": "port", "sample": sample},
+                "e2e": {"value": value, "unit": "pairs/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return 0
+
+    import torch
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    dev = local
+    torch.cuda.set_device(dev)
+    import halotools_gb300 as H
+    from halotools_gb300 import _native as N
+
+    x = make_points(w)
+    box = np.array([w["L"]] * 3)
+    n = len(x)
+    xd = torch.from_numpy(x).to(f"cuda:{dev}")
+    plan = N.Plan(dev)
+    stream = torch.cuda.current_stream(dev)
+    plan.set_stream(stream.cuda_stream)
+    out = np.zeros(len(w["bins"]) if w["kind"] == "3d" else (len(w["bins"]), len(w["bins2"])),
+                   dtype=np.int64)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{dev}")
+    for _ in range(args.warmup):
+        call_device(plan, w["kind"], xd, n, w, box, out)
+    pairs_step = in_range(w["kind"], out)
+    st0 = plan.stats()
+    fp32_peak = plan.fp32_peak_tflops()
+
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    count_ms = []
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(dev) as clk:
+        for k in range(args.steps):
+            flush.zero_()
+            ev[k][0].record(stream)
+            call_device(plan, w["kind"], xd, n, w, box, out)
+            ev[k][1].record(stream)
+            count_ms.append(plan.stats()["ms_count"])
+        torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    total_s = sum(step_ms) / 1e3
+    if world > 1:
+        t = torch.tensor([total_s], device=f"cuda:{dev}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_s = float(t.item())
+    value = pairs_step * args.steps * world / total_s
+    st = plan.stats()
+
+    # e2e: public drop-in API from pinned host memory, result back on the host
+    xp = torch.from_numpy(x).pin_memory().numpy()
+    f = (lambda: H.npairs_3d(xp, xp, w["bins"], period=w["L"])) if w["kind"] == "3d" else \
+        (lambda: H.npairs_xy_z(xp, xp, w["bins"], w["bins2"], period=w["L"]))
+    for _ in range(2):
+        f()
+    e2e_t = []
+    for _ in range(max(3, args.steps // 2)):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = f()
+        e2e_t.append(time.perf_counter() - t0)
+    assert in_range(w["kind"], r) == pairs_step
+    st_e2e = H.default_plan(dev).stats()
+    e2e = {"value": pairs_step / float(np.mean(e2e_t)), "unit": "pairs/s",
+           "h2d_bytes_per_step": int(st_e2e["h2d_bytes"]),
+           "d2h_bytes_per_step": int(st_e2e["d2h_bytes"]),
+           "ms_per_step": float(np.mean(e2e_t)) * 1e3}
+
+    cnt_ms = float(np.mean(count_ms))
+    achieved = 8.0 * pairs_step / (cnt_ms * 1e-3) / 1e12
+    roofline = {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                "frac": achieved / fp32_peak if fp32_peak else None, "traffic": None,
+                "kernel": "k_count<%d>" % (0 if w["kind"] == "3d" else 1),
+                "flops_per_unit": 8, "unit_of_work": "in-range ordered pair",
+                "peak_source": "measured live: FFMA-chain probe kernel (gbp_measure_fp32_peak)",
+                "count_ms": cnt_ms,
+                "candidate_pairs": st["candidate_pairs"], "recheck_pairs": st["recheck_pairs"],
+                "grid_cells": st["cells"], "reach": st["reach"],
+                "stencil_cells": st["stencil_cells"]}
+    tf = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tf):
+        try:
+            roofline["traffic"] = json.load(open(tf)).get(args.workload)
+        except Exception:
+            pass
+
+    line = {"metric": metric, "value": value, "unit": "pairs/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_s / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+            "data": "synthetic (seeded; shapes of the named configuration)", "config": cfg,
+            "roofline": roofline, "e2e": e2e, "clocks": clk.summary(),
+            "gpu_launches": int(st["kernel_launches"]) * args.steps,
+            "ms_build": st["ms_build"], "ms_count": cnt_ms, "pairs_per_step": pairs_step}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        v, dt, nsub = run_cpu(w, x, 1, 0, frac_side, threads)
+        line["cpu_baseline"] = {"value": v, "unit": "pairs/s", "cores": threads, "kind": "port",
+                                "sample": "%d points in the sub-cube [0, %.0f)^3, non-periodic, "
+                                          "C oracle cell walk, %.1f s" % (nsub, frac_side * w["L"], dt)}
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

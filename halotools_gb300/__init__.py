@@ -1,0 +1,51 @@
+"""GB300-native pair-counting engines for halotools' mock observables.
+
+``npairs_3d``, ``npairs_xy_z``, ``npairs_s_mu`` and ``marked_npairs_3d`` keep
+the halotools signatures (mock_observables/pair_counters/__init__.py:3-18) and
+run on hand-written sm_103a CUDA kernels through the C ABI declared in
+``include/gbpairs.h``.  ``install_into_halotools()`` rebinds the names that
+halotools' estimators bound at import time, so ``tpcf``, ``wp``,
+``rp_pi_tpcf``, ``s_mu_tpcf`` and ``marked_tpcf`` pick them up as drop-ins.
+"""
+from .pair_counters import (HalotoolsError, marked_npairs_3d, npairs_3d, npairs_s_mu,
+                            npairs_xy_z)
+from ._native import GBPairsError, GBPairsUnavailable, Plan, default_plan
+
+__all__ = ("npairs_3d", "npairs_xy_z", "npairs_s_mu", "marked_npairs_3d", "HalotoolsError",
+           "GBPairsError", "GBPairsUnavailable", "Plan", "default_plan",
+           "install_into_halotools")
+
+# module attribute -> our function, for every place halotools binds a counter
+_BINDINGS = (
+    ("halotools.mock_observables.pair_counters", "npairs_3d", npairs_3d),
+    ("halotools.mock_observables.pair_counters", "npairs_xy_z", npairs_xy_z),
+    ("halotools.mock_observables.pair_counters", "npairs_s_mu", npairs_s_mu),
+    ("halotools.mock_observables.pair_counters", "marked_npairs_3d", marked_npairs_3d),
+    ("halotools.mock_observables", "npairs_3d", npairs_3d),
+    ("halotools.mock_observables", "npairs_xy_z", npairs_xy_z),
+    ("halotools.mock_observables", "npairs_s_mu", npairs_s_mu),
+    ("halotools.mock_observables", "marked_npairs_3d", marked_npairs_3d),
+    ("halotools.mock_observables.two_point_clustering.tpcf", "npairs_3d", npairs_3d),
+    ("halotools.mock_observables.two_point_clustering.rp_pi_tpcf", "npairs_xy_z", npairs_xy_z),
+    ("halotools.mock_observables.two_point_clustering.s_mu_tpcf", "npairs_s_mu", npairs_s_mu),
+    ("halotools.mock_observables.two_point_clustering.marked_tpcf", "marked_npairs_3d",
+     marked_npairs_3d),
+)
+
+
+def install_into_halotools():
+    """Point halotools' estimators at the GB300 counters; returns the rebound names.
+
+    Modules that are not importable (halotools absent) are skipped.
+    """
+    import importlib
+    done = []
+    for mod_name, attr, fn in _BINDINGS:
+        try:
+            mod = importlib.import_module(mod_name)
+        except Exception:
+            continue
+        if hasattr(mod, attr):
+            setattr(mod, attr, fn)
+            done.append("%s.%s" % (mod_name, attr))
+    return done

@@ -1,0 +1,184 @@
+"""ctypes binding of ``libgbpairs.so`` (declared in ``include/gbpairs.h``).
+
+The library is the only compute path: if it cannot be loaded, or no CUDA
+device is present, every counting call raises ``GBPairsUnavailable``.  There
+is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+import numpy as np
+
+from . import build as _build
+
+GBP_OK = 0
+GBP_ERR_INVALID = -1
+GBP_ERR_CUDA = -2
+GBP_ERR_NOMEM = -3
+GBP_ERR_RANGE = -4
+GBP_ERR_NODEVICE = -5
+GBP_MEM_HOST = 0
+GBP_MEM_DEVICE = 1
+
+EXPORTED = (
+    "gbp_plan_create", "gbp_plan_destroy", "gbp_plan_set_stream", "gbp_plan_set_reach",
+    "gbp_plan_last_error", "gbp_plan_stats", "gbp_npairs_3d", "gbp_npairs_xy_z",
+    "gbp_npairs_s_mu", "gbp_marked_npairs_3d", "gbp_measure_fp32_peak",
+)
+
+
+class GBPairsUnavailable(RuntimeError):
+    """The CUDA library or a GPU is missing; no fallback exists."""
+
+
+class GBPairsError(RuntimeError):
+    """A CUDA-side failure reported by the library."""
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [
+        ("candidate_pairs", ctypes.c_int64),
+        ("recheck_pairs", ctypes.c_int64),
+        ("cells", ctypes.c_int64 * 3),
+        ("reach", ctypes.c_int32),
+        ("stencil_cells", ctypes.c_int32),
+        ("work_items", ctypes.c_int64),
+        ("ms_build", ctypes.c_float),
+        ("ms_count", ctypes.c_float),
+        ("ms_total", ctypes.c_float),
+        ("count_launches", ctypes.c_int32),
+        ("kernel_launches", ctypes.c_int32),
+        ("h2d_bytes", ctypes.c_int64),
+        ("d2h_bytes", ctypes.c_int64),
+    ]
+
+    def as_dict(self):
+        d = {f: getattr(self, f) for f, _ in self._fields_}
+        d["cells"] = list(self.cells)
+        return d
+
+
+_lib = None
+_lock = threading.Lock()
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True):
+    """Load (building first if needed) and type the C-ABI."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = _build.LIB
+        if not os.path.exists(path):
+            if not build_if_missing:
+                raise GBPairsUnavailable("libgbpairs.so not built: run halotools_gb300.build")
+            try:
+                path = _build.build()
+            except Exception as exc:  # nvcc missing, compile error ...
+                raise GBPairsUnavailable("cannot build libgbpairs.so: %s" % exc) from exc
+        try:
+            L = ctypes.CDLL(path)
+        except OSError as exc:
+            raise GBPairsUnavailable("cannot load %s: %s" % (path, exc)) from exc
+        P = ctypes.POINTER
+        pd, pi64 = P(ctypes.c_double), P(ctypes.c_int64)
+        vp, i32, i64 = ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64
+        L.gbp_plan_create.argtypes = [ctypes.c_int, P(vp)]
+        L.gbp_plan_destroy.argtypes = [vp]
+        L.gbp_plan_set_stream.argtypes = [vp, vp]
+        L.gbp_plan_set_reach.argtypes = [vp, ctypes.c_int]
+        L.gbp_plan_last_error.argtypes = [vp]
+        L.gbp_plan_last_error.restype = ctypes.c_char_p
+        L.gbp_plan_stats.argtypes = [vp, P(Stats)]
+        L.gbp_npairs_3d.argtypes = [vp, vp, i64, vp, i64, pd, i32, pd, i32, i32, pi64]
+        L.gbp_npairs_xy_z.argtypes = [vp, vp, i64, vp, i64, pd, i32, pd, i32, pd, i32, i32, pi64]
+        L.gbp_npairs_s_mu.argtypes = [vp, vp, i64, vp, i64, pd, i32, pd, i32, pd, i32, i32, pi64]
+        L.gbp_marked_npairs_3d.argtypes = [vp, vp, i64, vp, i64, vp, vp, i32, i32, pd, i32, pd,
+                                           i32, i32, pd]
+        L.gbp_measure_fp32_peak.argtypes = [vp, pd]
+        _lib = L
+        return L
+
+
+class Plan:
+    """Owns one ``gbp_plan`` (stream + device workspace) on one GPU."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load()
+        h = ctypes.c_void_p()
+        rc = self.lib.gbp_plan_create(int(device), ctypes.byref(h))
+        if rc == GBP_ERR_NODEVICE:
+            raise GBPairsUnavailable("no CUDA device visible: the gbpairs engines need a GPU")
+        if rc != GBP_OK:
+            raise GBPairsError("gbp_plan_create failed with status %d" % rc)
+        self.handle = h
+        self.device = device
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.gbp_plan_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def check(self, rc: int):
+        if rc == GBP_OK:
+            return
+        msg = self.lib.gbp_plan_last_error(self.handle).decode(errors="replace")
+        if rc == GBP_ERR_RANGE:
+            raise ValueError(msg)
+        if rc == GBP_ERR_INVALID:
+            raise ValueError(msg)
+        raise GBPairsError("gbpairs failure %d: %s" % (rc, msg))
+
+    def stats(self) -> dict:
+        s = Stats()
+        self.check(self.lib.gbp_plan_stats(self.handle, ctypes.byref(s)))
+        return s.as_dict()
+
+    def set_stream(self, stream_ptr):
+        self.check(self.lib.gbp_plan_set_stream(self.handle, ctypes.c_void_p(stream_ptr)))
+
+    def fp32_peak_tflops(self) -> float:
+        v = ctypes.c_double()
+        self.check(self.lib.gbp_measure_fp32_peak(self.handle, ctypes.byref(v)))
+        return v.value
+
+    def set_reach(self, reach: int):
+        self.check(self.lib.gbp_plan_set_reach(self.handle, int(reach)))
+
+
+_plans = {}
+
+
+def default_plan(device: int = 0) -> Plan:
+    with _lock:
+        p = _plans.get(device)
+    if p is None:
+        p = Plan(device)
+        with _lock:
+            _plans[device] = p
+    return p
+
+
+def dptr(a: np.ndarray):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+def pd(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def pi64(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))

@@ -1,0 +1,896 @@
+// C-ABI of the gbpairs library: plans, argument checks, grid and stencil
+// choice, edge thresholds, device workspace and the per-call pipeline
+//   H2D positions -> cell lists (gbp_mesh.cu) -> work items -> count kernel
+//   (gbp_count.cu) -> D2H differential histogram -> cumulative counts.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <string>
+#include <vector>
+
+#include "../../include/gbpairs.h"
+#include "gbp_internal.cuh"
+
+namespace {
+
+const double INF = std::numeric_limits<double>::infinity();
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+};
+
+}  // namespace
+
+struct gbp_plan {
+    int device = 0;
+    cudaStream_t own = nullptr;
+    cudaStream_t stream = nullptr;
+    int reach = 0;
+    int nsm = 0;
+    DevBuf work;           // device workspace, grow-only
+    void *pinned = nullptr;
+    size_t pinned_bytes = 0;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    gbp_stats stats;
+    std::string err;
+};
+
+namespace {
+
+int fail(gbp_plan *p, int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    if (p) p->err = buf;
+    return code;
+}
+
+#define CK(expr)                                                                          \
+    do {                                                                                  \
+        cudaError_t e_ = (expr);                                                          \
+        if (e_ != cudaSuccess)                                                            \
+            return fail(plan, e_ == cudaErrorMemoryAllocation ? GBP_ERR_NOMEM : GBP_ERR_CUDA, \
+                        "%s: %s", #expr, cudaGetErrorString(e_));                         \
+    } while (0)
+
+// ---------------- edges ----------------
+// Walk-from-the-top semantics of npairs_3d / npairs_xy_z / marked engines:
+// counts[k] is incremented iff v <= E[m] for every m >= k; a NaN edge stops
+// the walk, so it and every edge below it are never satisfied.
+std::vector<double> edges_top_walk(const double *r, int n) {
+    std::vector<double> E(n);
+    double m = INF;
+    bool dead = false;
+    for (int k = n - 1; k >= 0; k--) {
+        double e = r[k] * r[k];
+        if (std::isnan(e)) dead = true;
+        if (dead) {
+            E[k] = -INF;
+        } else {
+            m = std::min(m, e);
+            E[k] = m;
+        }
+    }
+    return E;
+}
+
+// npairs_s_mu_engine.pyx:198-226 semantics: a value is skipped when it exceeds
+// max(E) (NaN max: never skipped); otherwise its index is 1 + the first k
+// (walking down from n-2) with v > E[k].  Returns non-decreasing E' with
+// bin(v) = smallest m such that v <= E'[m].
+std::vector<double> edges_smu(const std::vector<double> &E) {
+    int n = (int)E.size();
+    std::vector<double> Ep(n);
+    double gate = -INF;
+    bool nan = false;
+    for (double e : E) {
+        if (std::isnan(e)) nan = true;
+        else gate = std::max(gate, e);
+    }
+    Ep[n - 1] = nan ? INF : gate;
+    double m = INF;
+    for (int k = n - 2; k >= 0; k--) {
+        if (!std::isnan(E[k])) m = std::min(m, E[k]);
+        Ep[k] = m;
+    }
+    // keep E' non-decreasing at the top (the gate is >= every finite edge)
+    for (int k = n - 2; k >= 0; k--) Ep[k] = std::min(Ep[k], Ep[k + 1]);
+    return Ep;
+}
+
+float f_down(double x) {
+    if (std::isnan(x)) return -std::numeric_limits<float>::infinity();
+    float f = (float)x;
+    if ((double)f > x) f = std::nextafter(f, -std::numeric_limits<float>::infinity());
+    return f;
+}
+
+float f_up(double x) {
+    if (std::isnan(x)) return std::numeric_limits<float>::infinity();
+    float f = (float)x;
+    if ((double)f < x) f = std::nextafter(f, std::numeric_limits<float>::infinity());
+    return f;
+}
+
+struct AxisHost {
+    int nb = 0;
+    std::vector<double> E;
+    std::vector<float> hi, lo;
+    std::vector<float4> lut;
+    int T = 0, S = 0, B = 0;
+    float vlo = 0, vhi = 0;
+};
+
+// Error model.  Coordinates are FP32 offsets from a cell corner, |u| <= c, the
+// stencil offset o*c is rounded to FP32 and added, and dx is formed in FP32:
+// |dx32 - dx| <= delta with delta = 2^-24 (c + c + K c + (K+1) c + |dx|) plus
+// the FP64 rounding of the corner and of the reference's own dx (~2^-50 L).
+struct ErrModel {
+    double cmax = 0, K = 1, Lmax = 0;
+    double delta(double Ebound) const {
+        double dxmax = std::sqrt(std::max(Ebound, 0.0));
+        return std::ldexp(1.0, -24) * (2 * cmax + K * cmax + (K + 1) * cmax + dxmax) * 1.02 +
+               std::ldexp(1.0, -50) * Lmax;
+    }
+    // bound on |v32 - v64| for v a sum of m squares near E
+    double band(double E, int m) const {
+        double E1 = E * (1.0 + std::ldexp(1.0, -10)) + 1e-300;
+        double d = delta(E1);
+        return 2.0 * d * std::sqrt((double)m) * std::sqrt(E1) + m * d * d +
+               (m + 1) * std::ldexp(1.0, -24) * E1 + m * std::ldexp(1.0, -50) * E1;
+    }
+};
+
+void axis_thresholds(AxisHost &ax, const std::vector<double> &E, const ErrModel *em, int m) {
+    ax.nb = (int)E.size();
+    ax.E = E;
+    ax.hi.resize(ax.nb);
+    ax.lo.resize(ax.nb);
+    for (int k = 0; k < ax.nb; k++) {
+        double e = E[k];
+        if (std::isinf(e)) {
+            ax.hi[k] = ax.lo[k] = (float)e;
+            continue;
+        }
+        double b = em ? 2.0 * em->band(e, m) : 0.0;
+        ax.lo[k] = f_down(e - b);
+        ax.hi[k] = f_up(e + b);
+    }
+    // hi must be non-decreasing for the table's start bins
+    for (int k = 1; k < ax.nb; k++) ax.hi[k] = std::max(ax.hi[k], ax.hi[k - 1]);
+}
+
+uint32_t fbits(float f) {
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    return u;
+}
+float bitsf(uint32_t u) {
+    float f;
+    std::memcpy(&f, &u, 4);
+    return f;
+}
+
+// Float-bit lookup table: slot s covers the FP32 values whose bits, shifted
+// right by S, equal B + s; values below/above the covered octaves clamp into
+// the first/last slot.  Each slot stores the first bin not provably exceeded
+// by every value of the slot (b0) and, if at most one edge can be crossed in
+// the slot, that edge's thresholds; otherwise (thr, lo) = (+inf, -inf) which
+// sends the pair to the walk.  qband(a) (optional) is stored in .w.
+template <class QB>
+void axis_lut(AxisHost &ax, QB qband) {
+    const float finf = std::numeric_limits<float>::infinity();
+    double hmax = 0, pmin = INF;
+    for (int k = 0; k < ax.nb; k++) {
+        for (float t : {ax.hi[k], ax.lo[k]}) {
+            if (std::isfinite(t) && t > 0) {
+                hmax = std::max(hmax, (double)t);
+                pmin = std::min(pmin, (double)t);
+            }
+        }
+    }
+    int emax = hmax > 0 ? std::ilogb(hmax) + 1 : 0;
+    emax = std::min(emax, 126);
+    int emin = std::isfinite(pmin) ? std::ilogb(pmin) - 1 : emax - 1;
+    emin = std::max(emin, std::max(emax - 40, -126));
+    int O = emax - emin + 1;
+    int m = 0;
+    while (m < 10 && (O << (m + 1)) <= GBP_LUT_MAX) m++;
+    ax.S = 23 - m;
+    ax.T = O << m;
+    ax.B = (emin + 127) << m;
+    ax.vlo = std::ldexp(1.0f, emin);
+    ax.vhi = std::nextafter(std::ldexp(1.0f, emax + 1), 0.0f);
+    ax.lut.resize(ax.T);
+    for (int s = 0; s < ax.T; s++) {
+        float a = s == 0 ? 0.0f : bitsf((uint32_t)(ax.B + s) << ax.S);
+        float bnext = s == ax.T - 1 ? finf : bitsf((uint32_t)(ax.B + s + 1) << ax.S);
+        float pred = std::nextafter(bnext, 0.0f);
+        int b0 = 0;
+        while (b0 < ax.nb && ax.hi[b0] < a) b0++;
+        float4 e;
+        int bi = b0;
+        std::memcpy(&e.x, &bi, 4);
+        if (b0 == ax.nb) {
+            e.y = finf;
+            e.z = finf;
+        } else {
+            bool simple = (b0 + 1 == ax.nb) || (pred <= ax.lo[b0 + 1]);
+            e.y = simple ? ax.hi[b0] : finf;
+            e.z = simple ? ax.lo[b0] : -finf;
+        }
+        e.w = qband(a);
+        ax.lut[s] = e;
+    }
+}
+
+// ---------------- grid & stencil ----------------
+struct Geometry {
+    int n[3];
+    double c[3], L[3];
+    int K;
+    int pbc;
+    int64_t ncells;
+    std::vector<int> sten;
+    std::vector<float4> stenD;
+    int nself;
+};
+
+const int64_t MAX_CELLS = 1ll << 24;
+const int64_t MAX_CELLS_PER_DIM = 256;
+
+// Cells per dimension for reach K: as many as keep K*c >= search, capped;
+// with periodic wrap every offset in [-K, K] must reach a distinct cell.
+bool grid_for_reach(int K, const double L[3], const double search[3], int pbc, int64_t n[3]) {
+    for (int d = 0; d < 3; d++) {
+        int64_t m = (int64_t)std::floor(L[d] * K / search[d]);
+        m = std::min<int64_t>(std::max<int64_t>(m, 1), MAX_CELLS_PER_DIM);
+        // search <= L/3, so three cells of size L/3 always cover it for K = 1
+        if (pbc && K == 1) m = std::max<int64_t>(m, 3);
+        if (pbc && m < 2 * K + 1) return false;
+        n[d] = m;
+    }
+    return true;
+}
+
+void choose_grid(Geometry &g, const double L[3], const double search[3], int pbc, int64_t n2,
+                 int reach_hint) {
+    for (int d = 0; d < 3; d++) g.L[d] = L[d];
+    g.pbc = pbc;
+    double vol = L[0] * L[1] * L[2];
+    double rho = vol > 0 ? (double)n2 / vol : 0;
+    int best = 1;
+    for (int K = 2; K <= 4; K++) {
+        int64_t n[3];
+        if (!grid_for_reach(K, L, search, pbc, n)) break;
+        double cvol = (L[0] / n[0]) * (L[1] / n[1]) * (L[2] / n[2]);
+        if (reach_hint > 0) {
+            if (K <= reach_hint) best = K;
+            continue;
+        }
+        // autotune: finer cells prune more of the cube stencil, but each work
+        // item then streams fewer points per i; keep ~28+ points per cell.
+        if (rho * cvol >= 28.0) best = K;
+    }
+    int64_t n[3];
+    grid_for_reach(best, L, search, pbc, n);
+    g.K = best;
+    g.ncells = 1;
+    for (int d = 0; d < 3; d++) {
+        g.n[d] = (int)n[d];
+        g.c[d] = L[d] / (double)n[d];
+        g.ncells *= n[d];
+    }
+}
+
+// kind 0: sphere of radius search[0]; kind 1: cylinder (rp, pi).
+void build_stencil(Geometry &g, const double search[3], int kind, bool autocorr) {
+    int K = g.K;
+    g.sten.clear();
+    g.stenD.clear();
+    auto push = [&](int ox, int oy, int oz) {
+        g.sten.push_back((ox + 64) | ((oy + 64) << 8) | ((oz + 64) << 16));
+        g.stenD.push_back(make_float4((float)(ox * g.c[0]), (float)(oy * g.c[1]),
+                                      (float)(oz * g.c[2]), 0.f));
+    };
+    auto keep = [&](int ox, int oy, int oz) {
+        double gx = std::max(std::abs(ox) - 1, 0) * g.c[0];
+        double gy = std::max(std::abs(oy) - 1, 0) * g.c[1];
+        double gz = std::max(std::abs(oz) - 1, 0) * g.c[2];
+        const double slack = 1.0 + 1e-9;
+        if (kind == 0) return gx * gx + gy * gy + gz * gz <= search[0] * search[0] * slack;
+        return gx * gx + gy * gy <= search[0] * search[0] * slack && gz <= search[2] * slack;
+    };
+    int Kx = std::min(K, g.pbc ? K : g.n[0] - 1);
+    int Ky = std::min(K, g.pbc ? K : g.n[1] - 1);
+    int Kz = std::min(K, g.pbc ? K : g.n[2] - 1);
+    push(0, 0, 0);
+    for (int ox = -Kx; ox <= Kx; ox++)
+        for (int oy = -Ky; oy <= Ky; oy++)
+            for (int oz = -Kz; oz <= Kz; oz++) {
+                if (ox == 0 && oy == 0 && oz == 0) continue;
+                if (autocorr) {
+                    bool pos = ox > 0 || (ox == 0 && (oy > 0 || (oy == 0 && oz > 0)));
+                    if (!pos) continue;
+                }
+                if (keep(ox, oy, oz)) push(ox, oy, oz);
+            }
+    g.nself = autocorr ? 1 : 0;
+}
+
+// ---------------- workspace ----------------
+struct Carve {
+    size_t off = 0;
+    template <class T>
+    size_t take(size_t count) {
+        off = (off + 255) & ~(size_t)255;
+        size_t o = off;
+        off += count * sizeof(T);
+        return o;
+    }
+};
+
+int ensure_work(gbp_plan *plan, size_t bytes) {
+    if (plan->work.bytes >= bytes) return GBP_OK;
+    if (plan->work.p) cudaFree(plan->work.p);
+    plan->work.p = nullptr;
+    plan->work.bytes = 0;
+    size_t want = std::max(bytes, plan->work.bytes + plan->work.bytes / 4);
+    CK(cudaMalloc(&plan->work.p, want));
+    plan->work.bytes = want;
+    return GBP_OK;
+}
+
+int ensure_pinned(gbp_plan *plan, size_t bytes) {
+    if (plan->pinned_bytes >= bytes) return GBP_OK;
+    if (plan->pinned) cudaFreeHost(plan->pinned);
+    plan->pinned = nullptr;
+    plan->pinned_bytes = 0;
+    CK(cudaMallocHost(&plan->pinned, bytes));
+    plan->pinned_bytes = bytes;
+    return GBP_OK;
+}
+
+struct SampleDev {
+    const double *xyz = nullptr;
+    int *cellid, *rank, *count, *start, *orig;
+    float4 *pos32;
+    double *pos64;
+    float *w32 = nullptr;
+    double *w64 = nullptr;
+};
+
+struct Call {
+    int mode;
+    const double *xyz1, *xyz2;
+    int64_t n1, n2;
+    bool autocorr;
+    int mem;
+    const double *w1 = nullptr, *w2 = nullptr;
+    int nw = 0, wfunc = 0;
+    AxisHost ax[2];
+    int naxes;
+    Geometry g;
+};
+
+template <class T>
+T *at(void *base, size_t off) {
+    return reinterpret_cast<T *>(static_cast<char *>(base) + off);
+}
+
+// Runs the pipeline; fills hist_host with the differential histogram
+// ((nb0+1) x (nb1+1) u64).
+int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host) {
+    CK(cudaSetDevice(plan->device));
+    cudaStream_t st = plan->stream;
+    std::memset(&plan->stats, 0, sizeof(plan->stats));
+    const int64_t ncells = c.g.ncells;
+    const int nb0 = c.ax[0].nb, nb1 = c.naxes > 1 ? c.ax[1].nb : 0;
+    const int T0 = c.ax[0].T, T1 = c.naxes > 1 ? c.ax[1].T : 0;
+    const int nsten = (int)c.g.sten.size();
+    const size_t nhist = (size_t)(nb0 + 1) * (size_t)(c.naxes > 1 ? nb1 + 1 : 1);
+    const int nsamp = c.autocorr ? 1 : 2;
+    const int64_t ns[2] = {c.n1, c.n2};
+
+    // ---- carve the workspace ----
+    Carve cv;
+    size_t o_xyz[2] = {0, 0}, o_cellid[2], o_rank[2], o_count[2], o_start[2], o_orig[2],
+           o_pos32[2], o_pos64[2], o_w32[2] = {0, 0}, o_w64[2] = {0, 0}, o_win[2] = {0, 0};
+    for (int s = 0; s < nsamp; s++) {
+        size_t n = (size_t)std::max<int64_t>(ns[s], 1);
+        if (c.mem == GBP_MEM_HOST) o_xyz[s] = cv.take<double>(3 * n);
+        o_cellid[s] = cv.take<int>(n);
+        o_rank[s] = cv.take<int>(n);
+        o_count[s] = cv.take<int>((size_t)ncells + 1);
+        o_start[s] = cv.take<int>((size_t)ncells + 1);
+        o_orig[s] = cv.take<int>(n);
+        o_pos32[s] = cv.take<float4>(2 * n);
+        o_pos64[s] = cv.take<double>(3 * n);
+        if (c.nw > 0) {
+            if (c.mem == GBP_MEM_HOST) o_win[s] = cv.take<double>(n * c.nw);
+            o_w32[s] = cv.take<float>(n * c.nw);
+            o_w64[s] = cv.take<double>(n * c.nw);
+        }
+    }
+    size_t scan_ints = gbp_scan_tmp_ints(ncells + 1);
+    size_t o_scan = cv.take<int>(scan_ints);
+    size_t max_items = (size_t)ncells + (size_t)(c.n1 / GBP_TI) + 16;
+    size_t o_items = cv.take<int4>(max_items);
+    size_t o_itmp = cv.take<int>(2 * ((size_t)ncells + 2));
+    size_t o_lut0 = cv.take<float4>(T0), o_lut1 = cv.take<float4>(std::max(T1, 1));
+    size_t o_E0 = cv.take<double>(nb0), o_E1 = cv.take<double>(std::max(nb1, 1));
+    size_t o_hi0 = cv.take<float>(nb0), o_lo0 = cv.take<float>(nb0);
+    size_t o_hi1 = cv.take<float>(std::max(nb1, 1)), o_lo1 = cv.take<float>(std::max(nb1, 1));
+    size_t o_sten = cv.take<int>(nsten), o_stenD = cv.take<float4>(nsten);
+    size_t o_hist = cv.take<unsigned long long>(nhist);
+    size_t o_histd = cv.take<double>(nhist);
+    size_t o_misc = cv.take<unsigned long long>(8);  // counter, nitems, err, recheck, cand
+    size_t total = cv.take<char>(0) + 256;
+    int rc = ensure_work(plan, total);
+    if (rc) return rc;
+    void *W = plan->work.p;
+
+    // ---- small tables through one pinned upload ----
+    Carve hv;
+    size_t h_lut0 = hv.take<float4>(T0), h_lut1 = hv.take<float4>(std::max(T1, 1));
+    size_t h_E0 = hv.take<double>(nb0), h_E1 = hv.take<double>(std::max(nb1, 1));
+    size_t h_hi0 = hv.take<float>(nb0), h_lo0 = hv.take<float>(nb0);
+    size_t h_hi1 = hv.take<float>(std::max(nb1, 1)), h_lo1 = hv.take<float>(std::max(nb1, 1));
+    size_t h_sten = hv.take<int>(nsten), h_stenD = hv.take<float4>(nsten);
+    size_t h_end = hv.take<char>(0);
+    size_t h_hist = hv.take<unsigned long long>(nhist);
+    size_t h_histd = hv.take<double>(nhist);
+    size_t h_misc = hv.take<unsigned long long>(8);
+    rc = ensure_pinned(plan, hv.take<char>(0) + 256);
+    if (rc) return rc;
+    void *H = plan->pinned;
+    std::memcpy(at<char>(H, h_lut0), c.ax[0].lut.data(), sizeof(float4) * T0);
+    std::memcpy(at<char>(H, h_E0), c.ax[0].E.data(), sizeof(double) * nb0);
+    std::memcpy(at<char>(H, h_hi0), c.ax[0].hi.data(), sizeof(float) * nb0);
+    std::memcpy(at<char>(H, h_lo0), c.ax[0].lo.data(), sizeof(float) * nb0);
+    if (c.naxes > 1) {
+        std::memcpy(at<char>(H, h_lut1), c.ax[1].lut.data(), sizeof(float4) * T1);
+        std::memcpy(at<char>(H, h_E1), c.ax[1].E.data(), sizeof(double) * nb1);
+        std::memcpy(at<char>(H, h_hi1), c.ax[1].hi.data(), sizeof(float) * nb1);
+        std::memcpy(at<char>(H, h_lo1), c.ax[1].lo.data(), sizeof(float) * nb1);
+    }
+    std::memcpy(at<char>(H, h_sten), c.g.sten.data(), sizeof(int) * nsten);
+    std::memcpy(at<char>(H, h_stenD), c.g.stenD.data(), sizeof(float4) * nsten);
+
+    CK(cudaEventRecord(plan->ev[0], st));
+    int64_t h2d = 0, d2h = 0;
+    h2d += (int64_t)(sizeof(float4) * (T0 + T1) + sizeof(double) * (nb0 + nb1) +
+                     sizeof(float) * 2 * (nb0 + nb1) + (sizeof(int) + sizeof(float4)) * nsten);
+    CK(cudaMemcpyAsync(at<char>(W, o_lut0), at<char>(H, h_lut0), sizeof(float4) * T0, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(at<char>(W, o_E0), at<char>(H, h_E0), sizeof(double) * nb0, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(at<char>(W, o_hi0), at<char>(H, h_hi0), sizeof(float) * nb0, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(at<char>(W, o_lo0), at<char>(H, h_lo0), sizeof(float) * nb0, cudaMemcpyHostToDevice, st));
+    if (c.naxes > 1) {
+        CK(cudaMemcpyAsync(at<char>(W, o_lut1), at<char>(H, h_lut1), sizeof(float4) * T1, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(at<char>(W, o_E1), at<char>(H, h_E1), sizeof(double) * nb1, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(at<char>(W, o_hi1), at<char>(H, h_hi1), sizeof(float) * nb1, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(at<char>(W, o_lo1), at<char>(H, h_lo1), sizeof(float) * nb1, cudaMemcpyHostToDevice, st));
+    }
+    CK(cudaMemcpyAsync(at<char>(W, o_sten), at<char>(H, h_sten), sizeof(int) * nsten, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(at<char>(W, o_stenD), at<char>(H, h_stenD), sizeof(float4) * nsten, cudaMemcpyHostToDevice, st));
+    (void)h_end;
+
+    // ---- positions and weights ----
+    SampleDev sd[2];
+    for (int s = 0; s < nsamp; s++) {
+        const double *src = s == 0 ? c.xyz1 : c.xyz2;
+        const double *wsrc = s == 0 ? c.w1 : c.w2;
+        size_t n = (size_t)ns[s];
+        if (c.mem == GBP_MEM_HOST) {
+            sd[s].xyz = at<double>(W, o_xyz[s]);
+            if (n) CK(cudaMemcpyAsync((void *)sd[s].xyz, src, 3 * n * sizeof(double), cudaMemcpyHostToDevice, st));
+            h2d += (int64_t)(3 * n * sizeof(double));
+        } else {
+            sd[s].xyz = src;
+        }
+        sd[s].cellid = at<int>(W, o_cellid[s]);
+        sd[s].rank = at<int>(W, o_rank[s]);
+        sd[s].count = at<int>(W, o_count[s]);
+        sd[s].start = at<int>(W, o_start[s]);
+        sd[s].orig = at<int>(W, o_orig[s]);
+        sd[s].pos32 = at<float4>(W, o_pos32[s]);
+        sd[s].pos64 = at<double>(W, o_pos64[s]);
+        if (c.nw > 0) {
+            const double *wd = wsrc;
+            if (c.mem == GBP_MEM_HOST) {
+                wd = at<double>(W, o_win[s]);
+                if (n) CK(cudaMemcpyAsync((void *)wd, wsrc, n * c.nw * sizeof(double), cudaMemcpyHostToDevice, st));
+                h2d += (int64_t)(n * c.nw * sizeof(double));
+            }
+            sd[s].w32 = at<float>(W, o_w32[s]);
+            sd[s].w64 = at<double>(W, o_w64[s]);
+            wsrc = wd;
+        }
+        if (s == 0) c.w1 = wsrc; else c.w2 = wsrc;
+    }
+    unsigned long long *misc = at<unsigned long long>(W, o_misc);
+    CK(cudaMemsetAsync(misc, 0, 8 * sizeof(unsigned long long), st));
+    int *d_counter = reinterpret_cast<int *>(misc);
+    int *d_nitems = reinterpret_cast<int *>(misc) + 1;
+    int *d_err = reinterpret_cast<int *>(misc) + 2;
+    unsigned long long *d_stat = misc + 2;  // [0] rechecks, [1] candidate pairs
+
+    MeshDev md;
+    for (int d = 0; d < 3; d++) {
+        md.n[d] = c.g.n[d];
+        md.c[d] = c.g.c[d];
+        md.L[d] = c.g.L[d];
+    }
+    md.ncells = ncells;
+    int launches = 0;
+    for (int s = 0; s < nsamp; s++) {
+        const double *wsrc = s == 0 ? c.w1 : c.w2;
+        cudaError_t e = gbp_build_cells(sd[s].xyz, ns[s], md, sd[s].cellid, sd[s].rank, sd[s].count,
+                                        sd[s].start, at<int>(W, o_scan), sd[s].pos32, sd[s].pos64,
+                                        sd[s].orig, c.nw > 0 ? wsrc : nullptr, c.nw, sd[s].w32,
+                                        sd[s].w64, d_err, st, &launches);
+        CK(e);
+    }
+    CK(gbp_build_items(sd[0].start, ncells, at<int4>(W, o_items), d_nitems, at<int>(W, o_itmp),
+                       at<int>(W, o_scan), st, &launches));
+    CK(cudaMemsetAsync(at<char>(W, o_hist), 0, nhist * sizeof(unsigned long long), st));
+    CK(cudaMemsetAsync(at<char>(W, o_histd), 0, nhist * sizeof(double), st));
+    CK(cudaEventRecord(plan->ev[1], st));
+
+    const SampleDev &s2 = c.autocorr ? sd[0] : sd[1];
+    CountArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.pos1 = sd[0].pos32;
+    a.pos2 = s2.pos32;
+    a.x64_1 = sd[0].pos64;
+    a.x64_2 = s2.pos64;
+    a.start2 = s2.start;
+    a.items = at<int4>(W, o_items);
+    a.nitems = d_nitems;
+    a.counter = d_counter;
+    a.sten = at<int>(W, o_sten);
+    a.stenD = at<float4>(W, o_stenD);
+    a.nsten = nsten;
+    a.nself = c.g.nself;
+    for (int d = 0; d < 3; d++) {
+        a.n[d] = c.g.n[d];
+        a.L[d] = c.g.L[d];
+    }
+    a.pbc = c.g.pbc;
+    for (int x = 0; x < c.naxes; x++) {
+        AxisDev &ad = a.ax[x];
+        const AxisHost &ah = c.ax[x];
+        ad.lut = at<float4>(W, x == 0 ? o_lut0 : o_lut1);
+        ad.E = at<double>(W, x == 0 ? o_E0 : o_E1);
+        ad.hi = at<float>(W, x == 0 ? o_hi0 : o_hi1);
+        ad.lo = at<float>(W, x == 0 ? o_lo0 : o_lo1);
+        ad.nb = ah.nb;
+        ad.T = ah.T;
+        ad.S = ah.S;
+        ad.B = ah.B;
+        ad.vlo = ah.vlo;
+        ad.vhi = ah.vhi;
+    }
+    a.hist_stride = c.naxes > 1 ? nb1 + 1 : 1;
+    a.hist = at<unsigned long long>(W, o_hist);
+    a.histd = at<double>(W, o_histd);
+    a.nrecheck = d_stat;
+    a.w1 = sd[0].w32;
+    a.w2 = s2.w32;
+    a.w64_1 = sd[0].w64;
+    a.w64_2 = s2.w64;
+    a.nw = c.nw;
+    a.wfunc = c.wfunc;
+
+    SmemLayout L = gbp_smem_layout(c.mode, T0, T1, nb0, nb1, nsten);
+    size_t smem = (size_t)L.total;
+    int occ = gbp_count_occupancy(c.mode, smem);
+    if (occ <= 0) return fail(plan, GBP_ERR_INVALID, "count kernel does not fit (smem %zu B)", smem);
+    int grid = plan->nsm * occ;
+    CK(gbp_launch_count(c.mode, a, grid, smem, st));
+    launches += 1;
+    CK(cudaEventRecord(plan->ev[2], st));
+    CK(cudaMemcpyAsync(at<char>(H, h_hist), a.hist, nhist * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(at<char>(H, h_histd), a.histd, nhist * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(at<char>(H, h_misc), misc, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+    CK(cudaEventRecord(plan->ev[3], st));
+    d2h += (int64_t)(nhist * (sizeof(unsigned long long) + sizeof(double)) + 8 * sizeof(unsigned long long));
+    CK(cudaStreamSynchronize(st));
+
+    const unsigned long long *hm = at<unsigned long long>(H, h_misc);
+    int err_word = reinterpret_cast<const int *>(hm)[2];
+    if (err_word) return fail(plan, GBP_ERR_RANGE, "positions outside [0, period] or not finite");
+    hist_host.assign(at<unsigned long long>(H, h_hist), at<unsigned long long>(H, h_hist) + nhist);
+    gbp_stats &S = plan->stats;
+    S.recheck_pairs = (int64_t)hm[2];
+    S.candidate_pairs = (int64_t)hm[3];
+    for (int d = 0; d < 3; d++) S.cells[d] = c.g.n[d];
+    S.reach = c.g.K;
+    S.stencil_cells = nsten;
+    int nit = reinterpret_cast<const int *>(hm)[1];
+    S.work_items = nit;
+    cudaEventElapsedTime(&S.ms_build, plan->ev[0], plan->ev[1]);
+    cudaEventElapsedTime(&S.ms_count, plan->ev[1], plan->ev[2]);
+    cudaEventElapsedTime(&S.ms_total, plan->ev[0], plan->ev[3]);
+    S.count_launches = 1;
+    S.kernel_launches = launches;
+    S.h2d_bytes = h2d;
+    S.d2h_bytes = d2h;
+    return GBP_OK;
+}
+
+int check_common(gbp_plan *plan, const double *xyz1, int64_t n1, const double *xyz2, int64_t n2,
+                 const double *period3, int pbc, int mem) {
+    if (!plan) return GBP_ERR_INVALID;
+    if (n1 < 0 || n2 < 0) return fail(plan, GBP_ERR_INVALID, "negative point count");
+    if ((n1 > 0 && !xyz1) || (n2 > 0 && !xyz2)) return fail(plan, GBP_ERR_INVALID, "null positions");
+    if (n1 >= (1ll << 30) || n2 >= (1ll << 30)) return fail(plan, GBP_ERR_INVALID, "too many points (limit 2^30)");
+    if (!period3) return fail(plan, GBP_ERR_INVALID, "null period");
+    for (int d = 0; d < 3; d++)
+        if (!(period3[d] > 0) || !std::isfinite(period3[d]))
+            return fail(plan, GBP_ERR_INVALID, "period must be finite and positive");
+    if (pbc != 0 && pbc != 1) return fail(plan, GBP_ERR_INVALID, "pbc must be 0 or 1");
+    if (mem != GBP_MEM_HOST && mem != GBP_MEM_DEVICE) return fail(plan, GBP_ERR_INVALID, "bad mem kind");
+    return GBP_OK;
+}
+
+int check_search(gbp_plan *plan, const double search[3], const double period3[3]) {
+    for (int d = 0; d < 3; d++) {
+        // rectangular_mesh.py:376-417
+        if (!(search[d] <= period3[d] / 3.0))
+            return fail(plan, GBP_ERR_RANGE,
+                        "search length %.6g cannot be larger than Lbox/3 (period %.6g)", search[d], period3[d]);
+        if (!(search[d] > 0))
+            return fail(plan, GBP_ERR_INVALID, "the largest bin edge must be positive");
+    }
+    return GBP_OK;
+}
+
+double max_nan(const double *r, int n) {
+    double m = r[0];
+    for (int k = 0; k < n; k++) {
+        if (std::isnan(r[k]) || std::isnan(m)) m = NAN;
+        else m = std::max(m, r[k]);
+    }
+    return m;
+}
+
+ErrModel err_model(const Geometry &g) {
+    ErrModel em;
+    em.cmax = std::max(g.c[0], std::max(g.c[1], g.c[2]));
+    em.K = g.K;
+    em.Lmax = std::max(g.L[0], std::max(g.L[1], g.L[2]));
+    return em;
+}
+
+}  // namespace
+
+// ======================= C ABI =======================
+extern "C" {
+
+int gbp_plan_create(int device, gbp_plan **out) {
+    if (!out) return GBP_ERR_INVALID;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) return GBP_ERR_NODEVICE;
+    if (device < 0 || device >= ndev) return GBP_ERR_INVALID;
+    gbp_plan *plan = new gbp_plan();
+    plan->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&plan->own, cudaStreamNonBlocking);
+    for (int i = 0; i < 4 && e == cudaSuccess; i++) e = cudaEventCreate(&plan->ev[i]);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&plan->nsm, cudaDevAttrMultiProcessorCount, device);
+    if (e != cudaSuccess) {
+        gbp_plan_destroy(plan);
+        return GBP_ERR_CUDA;
+    }
+    plan->stream = plan->own;
+    *out = plan;
+    return GBP_OK;
+}
+
+int gbp_plan_destroy(gbp_plan *plan) {
+    if (!plan) return GBP_OK;
+    cudaSetDevice(plan->device);
+    if (plan->stream) cudaStreamSynchronize(plan->stream);
+    if (plan->work.p) cudaFree(plan->work.p);
+    if (plan->pinned) cudaFreeHost(plan->pinned);
+    for (int i = 0; i < 4; i++)
+        if (plan->ev[i]) cudaEventDestroy(plan->ev[i]);
+    if (plan->own) cudaStreamDestroy(plan->own);
+    delete plan;
+    return GBP_OK;
+}
+
+int gbp_plan_set_stream(gbp_plan *plan, void *s) {
+    if (!plan) return GBP_ERR_INVALID;
+    plan->stream = s ? static_cast<cudaStream_t>(s) : plan->own;
+    return GBP_OK;
+}
+
+int gbp_plan_set_reach(gbp_plan *plan, int reach) {
+    if (!plan || reach < 0 || reach > 4) return GBP_ERR_INVALID;
+    plan->reach = reach;
+    return GBP_OK;
+}
+
+const char *gbp_plan_last_error(const gbp_plan *plan) { return plan ? plan->err.c_str() : "null plan"; }
+
+int gbp_plan_stats(const gbp_plan *plan, gbp_stats *st) {
+    if (!plan || !st) return GBP_ERR_INVALID;
+    *st = plan->stats;
+    return GBP_OK;
+}
+
+int gbp_npairs_3d(gbp_plan *plan, const double *xyz1, int64_t n1, const double *xyz2, int64_t n2,
+                  const double *rbins, int32_t nb, const double *period3, int32_t pbc, int32_t mem,
+                  int64_t *counts) {
+    int rc = check_common(plan, xyz1, n1, xyz2, n2, period3, pbc, mem);
+    if (rc) return rc;
+    if (!rbins || nb < 2 || nb > GBP_NB_MAX || !counts)
+        return fail(plan, GBP_ERR_INVALID, "rbins must have 2..%d entries", GBP_NB_MAX);
+    double rmax = max_nan(rbins, nb);
+    double search[3] = {rmax, rmax, rmax};
+    if ((rc = check_search(plan, search, period3))) return rc;
+    Call c;
+    c.mode = MODE_3D;
+    c.xyz1 = xyz1;
+    c.xyz2 = xyz2;
+    c.n1 = n1;
+    c.n2 = n2;
+    c.autocorr = (xyz1 == xyz2 && n1 == n2);
+    c.mem = mem;
+    c.naxes = 1;
+    choose_grid(c.g, period3, search, pbc, n2, plan->reach);
+    build_stencil(c.g, search, 0, c.autocorr);
+    ErrModel em = err_model(c.g);
+    axis_thresholds(c.ax[0], edges_top_walk(rbins, nb), &em, 3);
+    axis_lut(c.ax[0], [](float) { return 0.0f; });
+    std::vector<unsigned long long> h;
+    if (n1 == 0 || n2 == 0) {
+        for (int k = 0; k < nb; k++) counts[k] = 0;
+        return GBP_OK;
+    }
+    if ((rc = run_call(plan, c, h))) return rc;
+    unsigned long long run = 0;
+    for (int k = 0; k < nb; k++) {
+        run += h[k];
+        counts[k] = (int64_t)run;
+    }
+    return GBP_OK;
+}
+
+int gbp_npairs_xy_z(gbp_plan *plan, const double *xyz1, int64_t n1, const double *xyz2, int64_t n2,
+                    const double *rp_bins, int32_t n_rp, const double *pi_bins, int32_t n_pi,
+                    const double *period3, int32_t pbc, int32_t mem, int64_t *counts) {
+    int rc = check_common(plan, xyz1, n1, xyz2, n2, period3, pbc, mem);
+    if (rc) return rc;
+    if (!rp_bins || !pi_bins || n_rp < 2 || n_pi < 2 || n_rp > GBP_NB_MAX || n_pi > GBP_NB_MAX || !counts)
+        return fail(plan, GBP_ERR_INVALID, "bin arrays must have 2..%d entries", GBP_NB_MAX);
+    double rpm = max_nan(rp_bins, n_rp), pim = max_nan(pi_bins, n_pi);
+    double search[3] = {rpm, rpm, pim};
+    if ((rc = check_search(plan, search, period3))) return rc;
+    Call c;
+    c.mode = MODE_XYZ;
+    c.xyz1 = xyz1;
+    c.xyz2 = xyz2;
+    c.n1 = n1;
+    c.n2 = n2;
+    c.autocorr = (xyz1 == xyz2 && n1 == n2);
+    c.mem = mem;
+    c.naxes = 2;
+    choose_grid(c.g, period3, search, pbc, n2, plan->reach);
+    build_stencil(c.g, search, 1, c.autocorr);
+    ErrModel em = err_model(c.g);
+    axis_thresholds(c.ax[0], edges_top_walk(rp_bins, n_rp), &em, 2);
+    axis_thresholds(c.ax[1], edges_top_walk(pi_bins, n_pi), &em, 1);
+    axis_lut(c.ax[0], [](float) { return 0.0f; });
+    axis_lut(c.ax[1], [](float) { return 0.0f; });
+    if (n1 == 0 || n2 == 0) {
+        for (int k = 0; k < n_rp * n_pi; k++) counts[k] = 0;
+        return GBP_OK;
+    }
+    std::vector<unsigned long long> h;
+    if ((rc = run_call(plan, c, h))) return rc;
+    // counts[k][g] = sum over differential bins a <= k, b <= g
+    const int st = n_pi + 1;
+    for (int k = 0; k < n_rp; k++)
+        for (int g2 = 0; g2 < n_pi; g2++) {
+            int64_t v = (int64_t)h[(size_t)k * st + g2];
+            if (k > 0) v += counts[(k - 1) * n_pi + g2];
+            if (g2 > 0) v += counts[k * n_pi + g2 - 1];
+            if (k > 0 && g2 > 0) v -= counts[(k - 1) * n_pi + g2 - 1];
+            counts[k * n_pi + g2] = v;
+        }
+    return GBP_OK;
+}
+
+int gbp_npairs_s_mu(gbp_plan *plan, const double *xyz1, int64_t n1, const double *xyz2, int64_t n2,
+                    const double *s_bins, int32_t n_s, const double *mu_prime, int32_t n_mu,
+                    const double *period3, int32_t pbc, int32_t mem, int64_t *counts) {
+    int rc = check_common(plan, xyz1, n1, xyz2, n2, period3, pbc, mem);
+    if (rc) return rc;
+    if (!s_bins || !mu_prime || n_s < 2 || n_mu < 2 || n_s > GBP_NB_MAX || n_mu > GBP_NB_MAX || !counts)
+        return fail(plan, GBP_ERR_INVALID, "bin arrays must have 2..%d entries", GBP_NB_MAX);
+    double smax = max_nan(s_bins, n_s);
+    double search[3] = {smax, smax, smax};
+    if ((rc = check_search(plan, search, period3))) return rc;
+    Call c;
+    c.mode = MODE_SMU;
+    c.xyz1 = xyz1;
+    c.xyz2 = xyz2;
+    c.n1 = n1;
+    c.n2 = n2;
+    c.autocorr = (xyz1 == xyz2 && n1 == n2);
+    c.mem = mem;
+    c.naxes = 2;
+    choose_grid(c.g, period3, search, pbc, n2, plan->reach);
+    build_stencil(c.g, search, 0, c.autocorr);
+    ErrModel em = err_model(c.g);
+    std::vector<double> Es(n_s), Em(n_mu);
+    for (int k = 0; k < n_s; k++) Es[k] = s_bins[k] * s_bins[k];
+    for (int k = 0; k < n_mu; k++) Em[k] = mu_prime[k] * mu_prime[k];
+    std::vector<double> Eps = edges_smu(Es), Epm = edges_smu(Em);
+    axis_thresholds(c.ax[0], Eps, &em, 3);
+    axis_thresholds(c.ax[1], Epm, nullptr, 0);
+    // q = dxy/s^2 error bound for pairs with s^2 >= a (FP32 value), factor 2 margin
+    double dtop = em.delta(smax * smax);
+    double Lm = em.Lmax;
+    ErrModel emc = em;
+    axis_lut(c.ax[0], [&](float a) -> float {
+        double s2lo = (double)a - 2.0 * emc.band((double)a, 3);
+        if (!(s2lo > 0)) return 3.0e38f;
+        double s = std::sqrt(s2lo);
+        double qb = 9.0 * std::ldexp(1.0, -24) + 4.6 * dtop / s + 5.0 * dtop * dtop / (s * s) +
+                    std::ldexp(1.0, -48) * Lm / s;
+        return f_up(2.0 * qb);
+    });
+    axis_lut(c.ax[1], [](float) { return 0.0f; });
+    if (n1 == 0 || n2 == 0) {
+        for (int k = 0; k < n_s * n_mu; k++) counts[k] = 0;
+        return GBP_OK;
+    }
+    std::vector<unsigned long long> h;
+    if ((rc = run_call(plan, c, h))) return rc;
+    // npairs_s_mu_engine.pyx:232-234
+    const int st = n_mu + 1;
+    for (int k = 0; k < n_s; k++)
+        for (int g2 = 0; g2 < n_mu; g2++) {
+            int64_t v = (int64_t)h[(size_t)k * st + g2];
+            if (k > 0) v += counts[(k - 1) * n_mu + g2];
+            if (g2 > 0) v += counts[k * n_mu + g2 - 1];
+            if (k > 0 && g2 > 0) v -= counts[(k - 1) * n_mu + g2 - 1];
+            counts[k * n_mu + g2] = v;
+        }
+    return GBP_OK;
+}
+
+int gbp_marked_npairs_3d(gbp_plan *plan, const double *xyz1, int64_t n1, const double *xyz2,
+                         int64_t n2, const double *w1, const double *w2, int32_t nw,
+                         int32_t wfunc_id, const double *rbins, int32_t nb, const double *period3,
+                         int32_t pbc, int32_t mem, double *out) {
+    (void)xyz1; (void)n1; (void)xyz2; (void)n2; (void)w1; (void)w2; (void)nw; (void)wfunc_id;
+    (void)rbins; (void)nb; (void)period3; (void)pbc; (void)mem; (void)out;
+    return fail(plan, GBP_ERR_INVALID, "marked counts not built yet");
+}
+
+int gbp_measure_fp32_peak(gbp_plan *plan, double *tflops) {
+    if (!plan || !tflops) return GBP_ERR_INVALID;
+    CK(cudaSetDevice(plan->device));
+    float ms = 0;
+    double flops = 0;
+    CK(gbp_run_ffma_probe(plan->nsm, plan->stream, &ms, &flops));
+    *tflops = ms > 0 ? flops / (ms * 1e-3) / 1e12 : 0.0;
+    return GBP_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,138 @@
+// Internal definitions shared by the gbpairs CUDA translation units.
+//
+// Data layout in HBM (one sample; the auto-correlation path sorts once):
+//   pos32[N]  float4  cell-relative FP32 coordinates (x - ix*cx, ...) in
+//                     cell-sorted order, .w = sorted index (int bits)
+//   pos64[3N] double  the FP64 positions in the same order (edge recheck)
+//   orig[N]   int     sorted position -> caller's index
+//   start[ncells+1]   CSR offsets of each cell's points
+// A count kernel walks work items (cell, first point, point count) and, per
+// item, streams the stencil cells' points through shared memory.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#define GBP_BLOCK 256
+#define GBP_WARPS (GBP_BLOCK / 32)
+#define GBP_TI 256          // max i-points per work item (one per thread)
+#define GBP_JCAP 1024       // staged j-points per chunk
+#define GBP_LUT_MAX 2048    // float-bit lookup slots per axis
+#define GBP_NB_MAX 64       // edges per axis
+#define GBP_SMAX 512        // stencil cells
+#define GBP_FAR 1.0e18f     // coordinate of an idle lane: far outside every edge
+
+enum { MODE_3D = 0, MODE_XYZ = 1, MODE_SMU = 2, MODE_MARK = 3, MODE_ADJ = 4 };
+
+// One binning axis: squared quantity v compared with edges E'[0..nb-1]
+// (non-decreasing); bin(v) = smallest k with v <= E'[k], nb if none.
+// hi/lo are FP32 thresholds: v32 > hi[k] proves v64 > E'[k]; v32 <= lo[k]
+// proves v64 <= E'[k].  lut[s] = {b0 (int bits), thr, lo, qband}.
+struct AxisDev {
+    const float4 *lut;
+    const float *hi;
+    const float *lo;
+    const double *E;
+    int nb;
+    int T;      // lut slots
+    int S;      // right shift of the float bits
+    int B;      // first slot's shifted-bits value
+    float vlo;  // clamp range of v before the lookup
+    float vhi;
+};
+
+struct CountArgs {
+    const float4 *pos1;
+    const float4 *pos2;
+    const double *x64_1;
+    const double *x64_2;
+    const int *start2;
+    const int4 *items;
+    const int *nitems;      // device scalar (written by the item builder)
+    int *counter;           // work-item cursor, zero before launch
+    const int *sten;        // packed (ox+64) | (oy+64)<<8 | (oz+64)<<16
+    const float4 *stenD;    // FP32 cell offsets o*c per stencil cell
+    int nsten;
+    int nself;              // 1 if stencil[0] is the own cell counted once (auto mode), else 0
+    int n[3];
+    int pbc;
+    double L[3];
+    AxisDev ax[2];
+    int hist_stride;        // bins per histogram copy
+    unsigned long long *hist;   // global differential histogram(s)
+    unsigned long long *nrecheck;
+    // marked / adjoint
+    const float *w1;        // sorted weights, (N1, nw) FP32
+    const float *w2;
+    const double *w64_1;    // sorted FP64 weights (marking-function conditions)
+    const double *w64_2;
+    int nw;
+    int wfunc;
+    double *histd;          // FP64 weighted histogram (marked)
+};
+
+// Shared-memory layout of the count kernel, identical on host and device.
+struct SmemLayout {
+    int off_lut0, off_lut1, off_j, off_D, off_E0, off_E1, off_hi0, off_lo0, off_hi1, off_lo1,
+        off_off, off_cstart, off_pre, off_hist, total;
+};
+
+__host__ __device__ inline int gbp_align(int x, int a) { return (x + a - 1) / a * a; }
+
+__host__ __device__ inline SmemLayout gbp_smem_layout(int mode, int T0, int T1, int nb0, int nb1,
+                                                      int nsten) {
+    SmemLayout L;
+    int o = 0;
+    L.off_lut0 = o; o += T0 * 16;
+    L.off_lut1 = o; o += T1 * 16;
+    L.off_j = o; o += GBP_JCAP * 16;
+    L.off_D = o; o += nsten * 16;
+    L.off_E0 = o; o += gbp_align(nb0 * 8, 16);
+    L.off_E1 = o; o += gbp_align(nb1 * 8, 16);
+    L.off_hi0 = o; o += gbp_align(nb0 * 4, 16);
+    L.off_lo0 = o; o += gbp_align(nb0 * 4, 16);
+    L.off_hi1 = o; o += gbp_align(nb1 * 4, 16);
+    L.off_lo1 = o; o += gbp_align(nb1 * 4, 16);
+    L.off_off = o; o += gbp_align(nsten * 4, 16);
+    L.off_cstart = o; o += gbp_align(nsten * 4, 16);
+    L.off_pre = o; o += gbp_align((nsten + 1) * 4, 16);
+    L.off_hist = o;
+    int hist_bytes;
+    if (mode == MODE_3D) {
+        hist_bytes = GBP_WARPS * (nb0 + 1) * 32 * 4;          // lane-private u32
+    } else if (mode == MODE_MARK) {
+        hist_bytes = GBP_WARPS * (nb0 + 1) * 32 * 4 * 2;      // lane-private FP32 sum + compensation
+    } else if (mode == MODE_ADJ) {
+        hist_bytes = GBP_BLOCK * 8 + 16;                      // per-thread partial gradients
+    } else {
+        hist_bytes = GBP_WARPS * (nb0 + 1) * (nb1 + 1) * 4;   // per-warp shared u32 (2-D)
+    }
+    o += gbp_align(hist_bytes, 16);
+    L.total = o;
+    return L;
+}
+
+// ---- launchers (defined in the .cu files) ----
+struct MeshDev {
+    int n[3];
+    double c[3];
+    double L[3];
+    int64_t ncells;
+};
+
+// Digitise, count, scan and scatter one sample into the cell-sorted layout.
+cudaError_t gbp_build_cells(const double *d_xyz, int64_t npts, const MeshDev &m, int *d_cellid,
+                            int *d_rank, int *d_count, int *d_start, int *d_scan_tmp,
+                            float4 *d_pos32, double *d_pos64, int *d_orig, const double *d_w,
+                            int nw, float *d_w32, double *d_w64, int *d_err, cudaStream_t st,
+                            int *launches);
+// Work items (cell, first, count) for every non-empty cell of a sorted sample.
+cudaError_t gbp_build_items(const int *d_start, int64_t ncells, int4 *d_items, int *d_nitems,
+                            int *d_tmp, int *d_scan_tmp, cudaStream_t st, int *launches);
+cudaError_t gbp_scan_exclusive(const int *d_in, int *d_out, int64_t n, int *d_tmp,
+                               cudaStream_t st, int *launches);
+size_t gbp_scan_tmp_ints(int64_t n);
+
+cudaError_t gbp_launch_count(int mode, const CountArgs &a, int grid, size_t smem, cudaStream_t st);
+int gbp_count_occupancy(int mode, size_t smem);
+cudaError_t gbp_count_set_smem(size_t smem);
+cudaError_t gbp_run_ffma_probe(int nsm, cudaStream_t st, float *ms_out, double *flops_out);

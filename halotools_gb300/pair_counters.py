@@ -1,0 +1,315 @@
+"""Drop-in front-ends for halotools' pair counters, running on the GB300 engines.
+
+Signatures, defaults, argument checks and error messages follow the
+reference front-ends:
+
+* ``npairs_3d``        halotools mock_observables/pair_counters/npairs_3d.py:20-213
+* ``npairs_xy_z``      npairs_xy_z.py:20-237
+* ``npairs_s_mu``      npairs_s_mu.py:20-209
+* ``marked_npairs_3d`` marked_npairs_3d.py:25-326
+
+``num_threads`` is validated as the reference does and then ignored (the GPU
+is the parallel engine).  ``approx_cell1_size`` / ``approx_cell2_size`` are
+validated and used only as hints: the GPU chooses its own cell grid, and the
+counts do not depend on it.
+
+Two deliberate differences, both for inputs the reference does not define:
+periodic positions outside ``[0, period]`` and non-finite positions raise
+``ValueError`` (the reference's mesh silently drops or mis-files them), and
+bin edges must be non-negative with a positive maximum.
+"""
+from __future__ import annotations
+
+import multiprocessing
+
+import numpy as np
+
+from . import _native
+from ._native import GBP_MEM_HOST
+
+__all__ = ("npairs_3d", "npairs_xy_z", "npairs_s_mu", "marked_npairs_3d", "HalotoolsError")
+
+
+class HalotoolsError(Exception):
+    """Raised for weight-shape errors, as halotools.custom_exceptions.HalotoolsError."""
+
+
+_NUM_THREADS_MSG = "Input ``num_threads`` argument must be an integer or the string 'max'"
+_PERIOD_MSG = "Input ``period`` must be a bounded positive number in all dimensions"
+
+
+def _check_num_threads(num_threads):
+    # npairs_3d.py:157-162
+    if num_threads != 1 or not isinstance(num_threads, int):
+        if isinstance(num_threads, str) and num_threads == "max":
+            return multiprocessing.cpu_count()
+        if not isinstance(num_threads, int):
+            raise ValueError(_NUM_THREADS_MSG)
+    return num_threads
+
+
+def _is_strictly_increasing(a):
+    # array_is_monotonic(a, strict=True) == 1 (utils/array_utils.py)
+    return bool(np.all(np.diff(a) > 0))
+
+
+def _bins(b, msg):
+    b = np.atleast_1d(b).astype("f8")
+    if not (b.ndim == 1 and len(b) > 1 and (len(b) <= 2 or _is_strictly_increasing(b))):
+        raise ValueError(msg)
+    return b
+
+
+def _columns(sample):
+    s = np.asarray(sample)
+    if s.ndim != 2 or s.shape[1] < 3:
+        raise ValueError("Input sample of points must be a Numpy ndarray of shape (Npts, 3).")
+    return s
+
+
+def _enclose_in_box(s1, s2, min_size):
+    # mesh_helpers.py:17-64: shift by the smallest coordinate over both samples
+    # and all three dimensions, in the input dtype; box = largest extent,
+    # padded to min_size.
+    x1, x2 = s1[:, :3], s2[:, :3]
+    xyzmin = np.min([np.min(x1[:, 0]), np.min(x2[:, 0]), np.min(x1[:, 1]), np.min(x2[:, 1]),
+                     np.min(x1[:, 2]), np.min(x2[:, 2])])
+    xyzmax = np.max([np.max(x1[:, 0]), np.max(x2[:, 0]), np.max(x1[:, 1]), np.max(x2[:, 1]),
+                     np.max(x1[:, 2]), np.max(x2[:, 2])]) - xyzmin
+    x1 = x1 - xyzmin
+    x2 = x2 - xyzmin
+    lbox = np.array([xyzmax, xyzmax, xyzmax])
+    min_size = np.atleast_1d(min_size)
+    if np.any(lbox < min_size):
+        lbox[(lbox < min_size)] = min_size[(lbox < min_size)]
+    return x1, x2, lbox.astype(np.float64)
+
+
+def _period(period):
+    p = np.atleast_1d(period).astype(float)
+    if len(p) == 1:
+        p = np.array([p[0]] * 3)
+    if len(p) != 3 or not (np.all(p < np.inf) and np.all(p > 0)):
+        raise ValueError(_PERIOD_MSG)
+    return p
+
+
+def _approx_cells(a, default, name):
+    # npairs_3d.py:202-209 then mesh_helpers._set_approximate_cell_sizes
+    if a is None:
+        a = default
+    elif np.size(a) == 1:
+        a = [a, a, a]
+    a = np.atleast_1d(a)
+    if len(a) != 3 or a.ndim != 1:
+        raise ValueError("Input ``%s`` must be a length-3 sequence" % name)
+    return a
+
+
+def _search_check(search, period):
+    # rectangular_mesh.py:376-417
+    for d, ax in enumerate("xyz"):
+        if not (search[d] <= period[d] / 3.0):
+            msg = ("\n The maximum length over which you search for pairs of points \n"
+                   "cannot be larger than Lbox/3 in any dimension. \n"
+                   "You tried to search for pairs out to a length of search_%slength = %.2f,\n"
+                   "but the size of your box in this dimension is %speriod = %.2f.\n"
+                   "If you need to count pairs on these length scales, \n"
+                   "you should use a larger simulation.\n" % (ax, search[d], ax, period[d]))
+            raise ValueError(msg)
+
+
+def _positions(sample1, sample2, period, search, pbc_min_size):
+    """Return contiguous float64 (N,3) arrays, box, pbc flag, auto flag."""
+    s1 = _columns(sample1)
+    same = sample2 is sample1
+    s2 = s1 if same else _columns(sample2)
+    if period is None:
+        pbc = 0
+        x1, x2, box = _enclose_in_box(s1, s2, pbc_min_size)
+    else:
+        pbc = 1
+        box = _period(period)
+        x1, x2 = s1[:, :3], s2[:, :3]
+    x1 = np.ascontiguousarray(x1, dtype=np.float64)
+    x2 = x1 if same else np.ascontiguousarray(x2, dtype=np.float64)
+    for x in (x1,) if same else (x1, x2):
+        if x.size and not np.all(np.isfinite(x)):
+            raise ValueError("Input sample contains non-finite positions")
+        if pbc and x.size and (np.any(x < 0) or np.any(x > box)):
+            raise ValueError("Periodic positions must lie in [0, period] in every dimension")
+    if not same and x1.shape == x2.shape and np.array_equal(x1, x2):
+        x2 = x1  # identical samples: the auto-correlation path gives the same counts
+    _search_check(search, box)
+    return x1, x2, np.ascontiguousarray(box, dtype=np.float64), pbc
+
+
+def _nonneg(b, what):
+    if np.any(b < 0) or not np.max(b) > 0:
+        raise ValueError("Input ``%s`` must be non-negative with a positive maximum" % what)
+
+
+def npairs_3d(sample1, sample2, rbins, period=None, num_threads=1, approx_cell1_size=None,
+              approx_cell2_size=None):
+    """Cumulative pair counts ``counts[k] = #(i, j)`` with separation ``<= rbins[k]``.
+
+    Same inputs and output as halotools ``npairs_3d`` (npairs_3d.py:20): an
+    int64 array of length ``len(rbins)``; ordered pairs, so auto-counts are
+    doubled and include self-pairs.
+    """
+    _check_num_threads(num_threads)
+    rbins = _bins(rbins, "Input ``rbins`` must be a monotonically increasing 1D array with at "
+                         "least two entries")
+    rmax = np.max(rbins)
+    _approx_cells(approx_cell1_size, [rmax] * 3, "approx_cell1_size")
+    _approx_cells(approx_cell2_size, [rmax] * 3, "approx_cell2_size")
+    _nonneg(rbins, "rbins")
+    x1, x2, box, pbc = _positions(sample1, sample2, period, [rmax] * 3, [rmax * 3.0] * 3)
+    plan = _native.default_plan()
+    out = np.zeros(len(rbins), dtype=np.int64)
+    plan.check(plan.lib.gbp_npairs_3d(plan.handle, _native.dptr(x1), len(x1), _native.dptr(x2),
+                                      len(x2), _native.pd(rbins), len(rbins), _native.pd(box),
+                                      pbc, GBP_MEM_HOST, _native.pi64(out)))
+    return out
+
+
+def npairs_xy_z(sample1, sample2, rp_bins, pi_bins, period=None, num_threads=1,
+                approx_cell1_size=None, approx_cell2_size=None):
+    """Cumulative (r_p, pi) pair counts, shape ``(len(rp_bins), len(pi_bins))``.
+
+    Same inputs and output as halotools ``npairs_xy_z`` (npairs_xy_z.py:20);
+    z is the line of sight.
+    """
+    _check_num_threads(num_threads)
+    rp_bins = _bins(rp_bins, "Input ``rp_bins`` must be a monotonically increasing 1D array "
+                             "with at least two entries")
+    pi_bins = _bins(pi_bins, "Input ``pi_bins`` must be a monotonically increasing 1D array "
+                             "with at least two entries")
+    rpm, pim = np.max(rp_bins), np.max(pi_bins)
+    _approx_cells(approx_cell1_size, [rpm, rpm, pim], "approx_cell1_size")
+    _approx_cells(approx_cell2_size, [rpm, rpm, pim], "approx_cell2_size")
+    _nonneg(rp_bins, "rp_bins")
+    _nonneg(pi_bins, "pi_bins")
+    x1, x2, box, pbc = _positions(sample1, sample2, period, [rpm, rpm, pim],
+                                  [rpm * 3.0, rpm * 3.0, pim * 3.0])
+    plan = _native.default_plan()
+    out = np.zeros((len(rp_bins), len(pi_bins)), dtype=np.int64)
+    plan.check(plan.lib.gbp_npairs_xy_z(plan.handle, _native.dptr(x1), len(x1), _native.dptr(x2),
+                                        len(x2), _native.pd(rp_bins), len(rp_bins),
+                                        _native.pd(pi_bins), len(pi_bins), _native.pd(box), pbc,
+                                        GBP_MEM_HOST, _native.pi64(out)))
+    return out
+
+
+def npairs_s_mu(sample1, sample2, s_bins, mu_bins, period=None, num_threads=1,
+                approx_cell1_size=None, approx_cell2_size=None):
+    """Cumulative (s, mu) pair counts, shape ``(len(s_bins), len(mu_bins))``.
+
+    Same inputs and output as halotools ``npairs_s_mu`` (npairs_s_mu.py:20):
+    the second axis runs over ``sort(sin(arccos(mu_bins)))``
+    (npairs_s_mu.py:174-175), i.e. increasing angle from the line of sight z.
+    """
+    _check_num_threads(num_threads)
+    s_bins = _bins(s_bins, "Input ``rbins`` must be a monotonically increasing 1D array with at "
+                           "least two entries")
+    smax = np.max(s_bins)
+    mu_bins = np.atleast_1d(mu_bins)
+    if not (mu_bins.ndim == 1 and len(mu_bins) > 1 and
+            (len(mu_bins) <= 2 or _is_strictly_increasing(mu_bins))):
+        raise ValueError("\n Input `mu_bins` must be a monotonically increasing \n"
+                         "1D array with at least two entries")
+    _approx_cells(approx_cell1_size, [smax] * 3, "approx_cell1_size")
+    _approx_cells(approx_cell2_size, [smax] * 3, "approx_cell2_size")
+    _nonneg(s_bins, "s_bins")
+    mu_prime = np.ascontiguousarray(np.sort(np.sin(np.arccos(mu_bins))), dtype=np.float64)
+    x1, x2, box, pbc = _positions(sample1, sample2, period, [smax] * 3, [smax * 3.0] * 3)
+    plan = _native.default_plan()
+    out = np.zeros((len(s_bins), len(mu_prime)), dtype=np.int64)
+    plan.check(plan.lib.gbp_npairs_s_mu(plan.handle, _native.dptr(x1), len(x1), _native.dptr(x2),
+                                        len(x2), _native.pd(s_bins), len(s_bins),
+                                        _native.pd(mu_prime), len(mu_prime), _native.pd(box),
+                                        pbc, GBP_MEM_HOST, _native.pi64(out)))
+    return out
+
+
+# marked_npairs_3d.py:281-326
+_NUM_WEIGHTS = {1: 1, 2: 1, 3: 2, 4: 2, 5: 2, 6: 2, 7: 2, 8: 2, 9: 2, 10: 2, 11: 2,
+                12: 4, 13: 4, 14: 3, 15: 3, 16: 5, 17: 5}
+
+
+def _func_signature_int_from_wfunc(weight_func_id):
+    if type(weight_func_id) != int:
+        raise ValueError("\n weight_func_id parameter must be an integer ID of a weighting function.")
+    if weight_func_id not in _NUM_WEIGHTS:
+        raise HalotoolsError("The value ``weight_func_id`` = %i is not recognized" % weight_func_id)
+    return _NUM_WEIGHTS[weight_func_id]
+
+
+def _process_weights(sample1, sample2, weights1, weights2, weight_func_id):
+    """marked_npairs_3d.py:186-276: shape checks and float64 (N, n_w) arrays."""
+    nw = _func_signature_int_from_wfunc(weight_func_id)
+    out = []
+    for which, sample, w in ((1, sample1, weights1), (2, sample2, weights2)):
+        npts = np.shape(sample)[0]
+        shape = (npts, nw)
+        conv = False
+        if w is None:
+            w = np.ones(shape, dtype=np.float64)
+        else:
+            w = np.atleast_1d(w).astype("float64")
+            if w.ndim == 1:
+                conv = True
+                w = w.reshape((len(w), 1))
+            elif w.ndim != 2:
+                raise HalotoolsError("\n You must either pass in a 1-D or 2-D array \n"
+                                     "for the input `weights%d`. Instead, an array of \n"
+                                     "dimension %i was received." % (which, w.ndim))
+        if np.shape(w) != shape:
+            if conv:
+                raise HalotoolsError("\n You passed in a 1-D array for `weights%d` that \n"
+                                     "does not have the correct length. The number of \n"
+                                     "points in `sample%d` = %i, while the number of points \n"
+                                     "in your input 1-D `weights%d` array = %i"
+                                     % (which, which, npts, which, np.shape(w)[0]))
+            raise HalotoolsError("\n You passed in a 2-D array for `weights%d` that \n"
+                                 "does not have a consistent shape with `sample%d`. \n"
+                                 "`sample%d` has length %i. The input value of `weight_func_id` = %i \n"
+                                 "For this value of `weight_func_id`, there should be %i weights \n"
+                                 "per point. The shape of your input `weights%d` is (%i, %i)\n"
+                                 % (which, which, which, npts, weight_func_id, nw, which,
+                                    np.shape(w)[0], np.shape(w)[1]))
+        out.append(np.ascontiguousarray(w, dtype=np.float64))
+    return out[0], out[1], nw
+
+
+def marked_npairs_3d(sample1, sample2, rbins, weight_func_id, period=None, weights1=None,
+                     weights2=None, num_threads=1, approx_cell1_size=None,
+                     approx_cell2_size=None):
+    """Cumulative weighted pair counts ``W(<r)`` (float64, length ``len(rbins)``).
+
+    Same inputs and output as halotools ``marked_npairs_3d``
+    (marked_npairs_3d.py:25); weights accumulate in FP32 with compensated
+    (Kahan) partial sums, within 1e-6 relative of the FP64 reference for
+    non-negative marks.
+    """
+    _check_num_threads(num_threads)
+    rbins = _bins(rbins, "Input ``rbins`` must be a monotonically increasing 1D array with at "
+                         "least two entries")
+    rmax = np.max(rbins)
+    _approx_cells(approx_cell1_size, [rmax] * 3, "approx_cell1_size")
+    _approx_cells(approx_cell2_size, [rmax] * 3, "approx_cell2_size")
+    x1, x2, box, pbc = _positions(sample1, sample2, period, [rmax] * 3, [rmax * 3.0] * 3)
+    w1, w2, nw = _process_weights(sample1, sample2, weights1, weights2, weight_func_id)
+    _nonneg(rbins, "rbins")
+    if x2 is x1 and not (weights2 is weights1 or np.array_equal(w1, w2)):
+        x2 = x1.copy()  # same points, different marks: count as a cross-correlation
+    if x2 is x1:
+        w2 = w1
+    plan = _native.default_plan()
+    out = np.zeros(len(rbins), dtype=np.float64)
+    plan.check(plan.lib.gbp_marked_npairs_3d(plan.handle, _native.dptr(x1), len(x1),
+                                             _native.dptr(x2), len(x2), _native.dptr(w1),
+                                             _native.dptr(w2), nw, int(weight_func_id),
+                                             _native.pd(rbins), len(rbins), _native.pd(box), pbc,
+                                             GBP_MEM_HOST, _native.pd(out)))
+    return out

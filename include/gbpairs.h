@@ -1,0 +1,122 @@
+/*
+ * gbpairs — GB300 (sm_103a) pair-counting engines behind a plain C ABI.
+ *
+ * Drop-in replacement for the engines behind halotools'
+ * mock_observables.pair_counters front-ends.  Every entry point takes plain
+ * pointers and sizes, writes into caller-owned output buffers, keeps no
+ * pointer after it returns, and reports failure through an int status
+ * (GBP_OK == 0); gbp_plan_last_error() gives the message.
+ *
+ * Positions are (N, 3) row-major float64.  For non-periodic counts the caller
+ * passes positions already shifted into their enclosing box together with that
+ * box as `period` and pbc = 0 (halotools mesh_helpers.py:17-64 does this shift
+ * in the front-end before any engine runs).  `mem` says where the position,
+ * weight and output arrays live: GBP_MEM_HOST (pageable or pinned host memory)
+ * or GBP_MEM_DEVICE (device pointers on the plan's GPU).  Bin edges are always
+ * host arrays.  Passing the same pointer (and count) for sample 2 as for
+ * sample 1 selects the auto-correlation path, which visits each unordered
+ * pair once and counts it for both orders, exactly as the reference counts
+ * ordered pairs (npairs_3d.py:26-29).
+ */
+#ifndef GBPAIRS_H
+#define GBPAIRS_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBP_OK 0
+#define GBP_ERR_INVALID (-1)   /* bad argument (null pointer, size, edge array) */
+#define GBP_ERR_CUDA (-2)      /* CUDA runtime error (launch, copy, device) */
+#define GBP_ERR_NOMEM (-3)     /* device or host allocation failed */
+#define GBP_ERR_RANGE (-4)     /* search length exceeds period/3, or positions out of the box */
+#define GBP_ERR_NODEVICE (-5)  /* no CUDA device / wrong architecture */
+
+#define GBP_MEM_HOST 0
+#define GBP_MEM_DEVICE 1
+
+typedef struct gbp_plan gbp_plan;
+
+/* Execution statistics of the most recent call on a plan. */
+typedef struct {
+    int64_t candidate_pairs;  /* pairs whose FP32 distance was evaluated */
+    int64_t recheck_pairs;    /* pairs re-evaluated in FP64 near a bin edge */
+    int64_t cells[3];         /* grid the call used */
+    int32_t reach;            /* stencil reach in cells */
+    int32_t stencil_cells;    /* cells in the (pruned) stencil */
+    int64_t work_items;       /* (cell, point-chunk) items of the count kernel */
+    float ms_build;           /* device time of the cell-list build */
+    float ms_count;           /* device time of the pair-count kernel */
+    float ms_total;           /* device time of the whole call incl. copies */
+    int32_t count_launches;   /* launches of the pair-count kernel in the call */
+    int32_t kernel_launches;  /* all kernel launches of the call */
+    int64_t h2d_bytes;        /* host-to-device bytes copied by the call */
+    int64_t d2h_bytes;        /* device-to-host bytes copied by the call */
+} gbp_stats;
+
+/* Plan: a CUDA stream, cached device workspace and statistics. Not
+ * thread-safe; distinct plans may be used from distinct host threads. */
+int gbp_plan_create(int device, gbp_plan **plan);
+int gbp_plan_destroy(gbp_plan *plan);
+/* Use an existing cudaStream_t (NULL = the plan's own stream). */
+int gbp_plan_set_stream(gbp_plan *plan, void *cuda_stream);
+/* Force the stencil reach (1..4 cells per search length); 0 = automatic. */
+int gbp_plan_set_reach(gbp_plan *plan, int reach);
+const char *gbp_plan_last_error(const gbp_plan *plan);
+int gbp_plan_stats(const gbp_plan *plan, gbp_stats *stats);
+
+/*
+ * Cumulative 3-D pair counts: counts[k] = #ordered pairs (i, j) whose FP64
+ * squared separation satisfies the reference's walk from the top edge down,
+ * i.e. dsq <= rbins[m]^2 for every m >= k.
+ * Replaces npairs_3d_engine (cpairs/npairs_3d_engine.pyx:17-184) and the
+ * mesh/Pool fan-out of npairs_3d (npairs_3d.py:112-150).
+ */
+int gbp_npairs_3d(gbp_plan *plan, const double *xyz1, int64_t n1, const double *xyz2,
+                  int64_t n2, const double *rbins, int32_t nbins, const double *period3,
+                  int32_t pbc, int32_t mem, int64_t *counts);
+
+/*
+ * Cumulative (r_p, pi) counts, row-major [n_rp][n_pi].
+ * Replaces npairs_xy_z_engine (cpairs/npairs_xy_z_engine.pyx:17-196) and
+ * npairs_xy_z (npairs_xy_z.py:124-163).
+ */
+int gbp_npairs_xy_z(gbp_plan *plan, const double *xyz1, int64_t n1, const double *xyz2,
+                    int64_t n2, const double *rp_bins, int32_t n_rp, const double *pi_bins,
+                    int32_t n_pi, const double *period3, int32_t pbc, int32_t mem,
+                    int64_t *counts);
+
+/*
+ * Cumulative (s, mu') counts, row-major [n_s][n_mu], where mu_prime is
+ * sort(sin(arccos(mu_bins))) as prepared by npairs_s_mu.py:174-175.
+ * Replaces npairs_s_mu_engine (cpairs/npairs_s_mu_engine.pyx:18-236).
+ */
+int gbp_npairs_s_mu(gbp_plan *plan, const double *xyz1, int64_t n1, const double *xyz2,
+                    int64_t n2, const double *s_bins, int32_t n_s, const double *mu_prime,
+                    int32_t n_mu, const double *period3, int32_t pbc, int32_t mem,
+                    int64_t *counts);
+
+/*
+ * Cumulative weighted counts for marking function `wfunc_id` (1..17) with
+ * `nw` weights per point, weights as (N, nw) row-major float64.
+ * Replaces marked_npairs_3d_engine (marked_cpairs/marked_npairs_3d_engine.pyx:22-218).
+ */
+int gbp_marked_npairs_3d(gbp_plan *plan, const double *xyz1, int64_t n1, const double *xyz2,
+                         int64_t n2, const double *w1, const double *w2, int32_t nw,
+                         int32_t wfunc_id, const double *rbins, int32_t nbins,
+                         const double *period3, int32_t pbc, int32_t mem, double *out);
+
+/*
+ * Measurement utility with no counterpart in the reference: runs a dependent-
+ * chain FFMA kernel on the plan's GPU and returns the FP32 FMA throughput in
+ * TFLOP/s (2 flops per FFMA), the ceiling of the count kernels' FP32 pipe.
+ */
+int gbp_measure_fp32_peak(gbp_plan *plan, double *tflops);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBPAIRS_H */

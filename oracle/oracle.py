@@ -1,0 +1,178 @@
+"""ctypes front-end of the C oracle (``oracle/pairs_oracle.c``).
+
+TEST INFRASTRUCTURE: only the tests, the smoke check and the benchmark's CPU
+baseline leg use this module.  It restates the argument processing of the
+reference front-ends (halotools mock_observables/pair_counters/npairs_3d.py:153-213,
+npairs_xy_z.py:166-237, npairs_s_mu.py:154-175, marked_npairs_3d.py:186-326)
+just far enough to drive the C cell walks with the same inputs the reference
+engines see, without validating user errors (the product's front-end does that).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SRC = os.path.join(HERE, "pairs_oracle.c")
+LIB = os.path.join(HERE, "liboracle.so")
+
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    """Compile the C oracle (unfused, left-to-right FP64) into ``oracle/liboracle.so``."""
+    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(SRC):
+        tmp = LIB + ".tmp%d" % os.getpid()
+        subprocess.run(["gcc", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
+                        "-pthread", SRC, "-o", tmp, "-lm"], check=True)
+        os.replace(tmp, LIB)
+    return LIB
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB)
+        P = ctypes.POINTER
+        d, i64, i = ctypes.c_double, ctypes.c_int64, ctypes.c_int
+        pd, pi64 = P(d), P(i64)
+        L.orc_npairs_3d.argtypes = [pd, i64, pd, i64, pd, i, pd, i, pd, pd, i, pi64]
+        L.orc_npairs_xy_z.argtypes = [pd, i64, pd, i64, pd, i, pd, i, pd, i, pd, pd, i, pi64]
+        L.orc_npairs_s_mu.argtypes = [pd, i64, pd, i64, pd, i, pd, i, pd, i, pd, pd, i, pi64]
+        L.orc_marked_npairs_3d.argtypes = [pd, i64, pd, i64, pd, pd, i, i, pd, i, pd, i, pd, pd, i, pd]
+        L.orc_bf_npairs_3d.argtypes = [pd, i64, pd, i64, pd, i, pd, i, pi64]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _pi(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
+
+
+def _geometry(sample1, sample2, search_max, period):
+    """Columns, optional enclosing box (mesh_helpers.py:17-64), period array."""
+    s1 = np.asarray(sample1)
+    s2 = np.asarray(sample2)
+    if period is None:
+        pbc = 0
+        x1, x2 = s1[:, :3], s2[:, :3]
+        xyzmin = np.min([np.min(x1[:, 0]), np.min(x2[:, 0]), np.min(x1[:, 1]), np.min(x2[:, 1]),
+                         np.min(x1[:, 2]), np.min(x2[:, 2])])
+        xyzmax = np.max([np.max(x1), np.max(x2)]) - xyzmin
+        x1 = x1 - xyzmin
+        x2 = x2 - xyzmin
+        lbox = np.array([xyzmax] * 3, dtype=np.float64)
+        mins = np.asarray(search_max, dtype=np.float64) * 3.0
+        lbox = np.where(lbox < mins, mins, lbox)
+    else:
+        pbc = 1
+        x1, x2 = s1[:, :3], s2[:, :3]
+        lbox = np.atleast_1d(period).astype(np.float64)
+        if len(lbox) == 1:
+            lbox = np.array([lbox[0]] * 3)
+    x1 = np.ascontiguousarray(x1, dtype=np.float64)
+    x2 = np.ascontiguousarray(x2, dtype=np.float64)
+    return x1, x2, np.ascontiguousarray(lbox, dtype=np.float64), pbc
+
+
+def _approx(a, default):
+    if a is None:
+        return np.asarray(default, dtype=np.float64)
+    a = np.atleast_1d(a).astype(np.float64)
+    if len(a) == 1:
+        a = np.array([a[0]] * 3)
+    return np.ascontiguousarray(a)
+
+
+def _check(rc):
+    if rc == -2:
+        raise ValueError("cannot be larger than Lbox/3")
+    if rc != 0:
+        raise RuntimeError("oracle failure %d" % rc)
+
+
+def npairs_3d(sample1, sample2, rbins, period=None, num_threads=1,
+              approx_cell1_size=None, approx_cell2_size=None):
+    rbins = np.ascontiguousarray(np.atleast_1d(rbins), dtype=np.float64)
+    rmax = np.max(rbins)
+    x1, x2, lbox, pbc = _geometry(sample1, sample2, [rmax] * 3, period)
+    a1 = _approx(approx_cell1_size, [rmax] * 3)
+    a2 = _approx(approx_cell2_size, [rmax] * 3)
+    out = np.zeros(len(rbins), dtype=np.int64)
+    _check(lib().orc_npairs_3d(_p(x1), len(x1), _p(x2), len(x2), _p(rbins), len(rbins),
+                               _p(lbox), pbc, _p(a1), _p(a2), int(num_threads), _pi(out)))
+    return out
+
+
+def npairs_xy_z(sample1, sample2, rp_bins, pi_bins, period=None, num_threads=1,
+                approx_cell1_size=None, approx_cell2_size=None):
+    rp = np.ascontiguousarray(np.atleast_1d(rp_bins), dtype=np.float64)
+    pi = np.ascontiguousarray(np.atleast_1d(pi_bins), dtype=np.float64)
+    rpm, pim = np.max(rp), np.max(pi)
+    x1, x2, lbox, pbc = _geometry(sample1, sample2, [rpm, rpm, pim], period)
+    a1 = _approx(approx_cell1_size, [rpm, rpm, pim])
+    a2 = _approx(approx_cell2_size, [rpm, rpm, pim])
+    out = np.zeros((len(rp), len(pi)), dtype=np.int64)
+    _check(lib().orc_npairs_xy_z(_p(x1), len(x1), _p(x2), len(x2), _p(rp), len(rp), _p(pi),
+                                 len(pi), _p(lbox), pbc, _p(a1), _p(a2), int(num_threads),
+                                 _pi(out)))
+    return out
+
+
+def npairs_s_mu(sample1, sample2, s_bins, mu_bins, period=None, num_threads=1,
+                approx_cell1_size=None, approx_cell2_size=None):
+    s = np.ascontiguousarray(np.atleast_1d(s_bins), dtype=np.float64)
+    smax = np.max(s)
+    mu_prime = np.ascontiguousarray(np.sort(np.sin(np.arccos(np.atleast_1d(mu_bins)))),
+                                    dtype=np.float64)
+    x1, x2, lbox, pbc = _geometry(sample1, sample2, [smax] * 3, period)
+    a1 = _approx(approx_cell1_size, [smax] * 3)
+    a2 = _approx(approx_cell2_size, [smax] * 3)
+    out = np.zeros((len(s), len(mu_prime)), dtype=np.int64)
+    _check(lib().orc_npairs_s_mu(_p(x1), len(x1), _p(x2), len(x2), _p(s), len(s), _p(mu_prime),
+                                 len(mu_prime), _p(lbox), pbc, _p(a1), _p(a2), int(num_threads),
+                                 _pi(out)))
+    return out
+
+
+NUM_WEIGHTS = {1: 1, 2: 1, 3: 2, 4: 2, 5: 2, 6: 2, 7: 2, 8: 2, 9: 2, 10: 2, 11: 2,
+               12: 4, 13: 4, 14: 3, 15: 3, 16: 5, 17: 5}
+
+
+def marked_npairs_3d(sample1, sample2, rbins, weight_func_id, period=None, weights1=None,
+                     weights2=None, num_threads=1, approx_cell1_size=None, approx_cell2_size=None):
+    rbins = np.ascontiguousarray(np.atleast_1d(rbins), dtype=np.float64)
+    rmax = np.max(rbins)
+    nw = NUM_WEIGHTS[weight_func_id]
+    n1, n2 = len(sample1), len(sample2)
+    w1 = np.ones((n1, nw)) if weights1 is None else np.asarray(weights1, dtype=np.float64).reshape(n1, nw)
+    w2 = np.ones((n2, nw)) if weights2 is None else np.asarray(weights2, dtype=np.float64).reshape(n2, nw)
+    w1 = np.ascontiguousarray(w1)
+    w2 = np.ascontiguousarray(w2)
+    x1, x2, lbox, pbc = _geometry(sample1, sample2, [rmax] * 3, period)
+    a1 = _approx(approx_cell1_size, [rmax] * 3)
+    a2 = _approx(approx_cell2_size, [rmax] * 3)
+    out = np.zeros(len(rbins), dtype=np.float64)
+    _check(lib().orc_marked_npairs_3d(_p(x1), n1, _p(x2), n2, _p(w1), _p(w2), nw,
+                                      int(weight_func_id), _p(rbins), len(rbins), _p(lbox), pbc,
+                                      _p(a1), _p(a2), int(num_threads), _p(out)))
+    return out
+
+
+def brute_force_npairs_3d(sample1, sample2, rbins, period=None):
+    """Mesh-free O(N1*N2) count; small inputs only."""
+    rbins = np.ascontiguousarray(np.atleast_1d(rbins), dtype=np.float64)
+    rmax = np.max(rbins)
+    x1, x2, lbox, pbc = _geometry(sample1, sample2, [rmax] * 3, period)
+    out = np.zeros(len(rbins), dtype=np.int64)
+    _check(lib().orc_bf_npairs_3d(_p(x1), len(x1), _p(x2), len(x2), _p(rbins), len(rbins),
+                                  _p(lbox), pbc, _pi(out)))
+    return out

@@ -1,0 +1,520 @@
+/*
+ * CPU restatement of halotools' pair-counting engines.
+ *
+ * TEST INFRASTRUCTURE: this is the oracle the CUDA path is checked against and
+ * the CPU baseline that the benchmark times beside it.  It is never linked
+ * into, or called by, the library's product path.
+ *
+ * It restates, in plain C, the reference's double mesh and its cell walks:
+ *   - sample1_cell_size / sample2_cell_sizes / RectangularMesh
+ *     (halotools mock_observables/pair_counters/rectangular_mesh.py:19-225)
+ *   - npairs_3d_engine     (cpairs/npairs_3d_engine.pyx:103-184)
+ *   - npairs_xy_z_engine   (cpairs/npairs_xy_z_engine.pyx:143-196)
+ *   - npairs_s_mu_engine   (cpairs/npairs_s_mu_engine.pyx:150-236)
+ *   - marked_npairs_3d_engine and the 17 marking functions
+ *     (marked_cpairs/marked_npairs_3d_engine.pyx:150-218,
+ *      marked_cpairs/marking_functions.pyx:21-218)
+ * The outer cell1 loop is split into contiguous ranges over POSIX threads,
+ * as the reference splits it over processes (mesh_helpers.py:183-221).
+ *
+ * Arithmetic: every squared distance is evaluated left to right and unfused,
+ * ((dx*dx + dy*dy) + dz*dz) with dx = (x1 - shift) - x2, which is what the
+ * reference's -Ofast build does on x86-64 (checked against its golden
+ * vectors).  Build with -ffp-contract=off so no FMA is formed.
+ */
+#include <math.h>
+#include <pthread.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define MAXCELLS_PER_DIM 50 /* rectangular_mesh.py:15-16 */
+
+/* numpy's float floor_divide (npy_divmod), used by digitized_position. */
+static double npy_floor_divide(double a, double b) {
+    double mod = fmod(a, b);
+    if (b == 0.0) return a / b;
+    double div = (a - mod) / b;
+    if (mod != 0.0) {
+        if ((b < 0) != (mod < 0)) div -= 1.0;
+    }
+    double floordiv;
+    if (div != 0.0) {
+        floordiv = floor(div);
+        if (div - floordiv > 0.5) floordiv += 1.0;
+    } else {
+        floordiv = copysign(0.0, a / b);
+    }
+    return floordiv;
+}
+
+/* rectangular_mesh.py:25-55 */
+static double sample1_cell_size(double period, double search, double approx) {
+    long ndivs = (long)floor(period / approx);
+    if (ndivs < 1) ndivs = 1;
+    if (ndivs > MAXCELLS_PER_DIM) ndivs = MAXCELLS_PER_DIM;
+    long nsearch = (long)floor(period / search);
+    if (nsearch < 1) nsearch = 1;
+    if (nsearch < ndivs) ndivs = nsearch;
+    if (ndivs < 3) ndivs = 3;
+    return period / (double)ndivs;
+}
+
+/* rectangular_mesh.py:58-82; np.round rounds half to even, as nearbyint does */
+static double sample2_cell_sizes(double period, double cell1, double approx) {
+    long n1 = (long)nearbyint(period / cell1);
+    long d = (long)nearbyint(cell1 / approx);
+    if (d < 1) d = 1;
+    if (d > MAXCELLS_PER_DIM) d = MAXCELLS_PER_DIM;
+    long n2 = n1 * d;
+    if (n2 > MAXCELLS_PER_DIM) {
+        long per = MAXCELLS_PER_DIM / n1;
+        n2 = per * n1;
+    }
+    return period / (double)n2;
+}
+
+typedef struct {
+    int n[3];
+    double cell[3];
+    int64_t ncells;
+    int64_t *start;   /* CSR offsets, ncells+1 */
+    int64_t *order;   /* sorted position -> original index */
+} mesh_t;
+
+/* RectangularMesh.__init__ (rectangular_mesh.py:118-222); a stable counting
+ * sort stands in for argsort, which changes only the order within a cell. */
+static int mesh_build(mesh_t *m, const double *xyz, int64_t npts,
+                      const double period[3], const double approx[3]) {
+    for (int d = 0; d < 3; d++) {
+        long nd = (long)nearbyint(period[d] / approx[d]);
+        if (nd < 1) nd = 1;
+        m->n[d] = (int)nd;
+        m->cell[d] = period[d] / (double)nd;
+    }
+    m->ncells = (int64_t)m->n[0] * m->n[1] * m->n[2];
+    m->start = (int64_t *)calloc((size_t)m->ncells + 1, sizeof(int64_t));
+    m->order = (int64_t *)malloc((size_t)(npts > 0 ? npts : 1) * sizeof(int64_t));
+    int64_t *cid = (int64_t *)malloc((size_t)(npts > 0 ? npts : 1) * sizeof(int64_t));
+    if (!m->start || !m->order || !cid) { free(cid); return -1; }
+    for (int64_t i = 0; i < npts; i++) {
+        int64_t ip[3];
+        for (int d = 0; d < 3; d++) {
+            double q = floor(npy_floor_divide(xyz[3 * i + d], m->cell[d]));
+            int64_t v = (int64_t)q;
+            if (v >= m->n[d]) v = m->n[d] - 1;
+            ip[d] = v;
+        }
+        int64_t c = ip[0] * ((int64_t)m->n[1] * m->n[2]) + ip[1] * m->n[2] + ip[2];
+        /* ids outside [0, ncells) fall outside every CSR range, as with searchsorted */
+        cid[i] = c;
+        if (c >= 0 && c < m->ncells) m->start[c + 1]++;
+    }
+    for (int64_t c = 0; c < m->ncells; c++) m->start[c + 1] += m->start[c];
+    int64_t *fill = (int64_t *)malloc((size_t)m->ncells * sizeof(int64_t) + 8);
+    if (!fill) { free(cid); return -1; }
+    memcpy(fill, m->start, (size_t)m->ncells * sizeof(int64_t));
+    for (int64_t i = 0; i < npts; i++) {
+        int64_t c = cid[i];
+        if (c >= 0 && c < m->ncells) m->order[fill[c]++] = i;
+    }
+    free(fill);
+    free(cid);
+    return 0;
+}
+
+static void mesh_free(mesh_t *m) {
+    free(m->start);
+    free(m->order);
+}
+
+enum { K_3D = 0, K_XYZ = 1, K_SMU = 2, K_MARKED = 3 };
+
+typedef struct {
+    int kind;
+    mesh_t m1, m2;
+    int steps[3], per[3];
+    double period[3];
+    int pbc;
+    /* sorted SoA copies (npairs_3d_engine.pyx:58-63) */
+    double *x1, *y1, *z1, *x2, *y2, *z2;
+    double *w1, *w2;
+    int nw, wfunc;
+    /* squared bin edges */
+    const double *e1;
+    int n1e;
+    const double *e2;
+    int n2e;
+    double smax2, mumax2;
+} walk_t;
+
+typedef struct {
+    const walk_t *w;
+    int64_t c0, c1;
+    int64_t *icounts;
+    double *dcounts;
+} job_t;
+
+/* marking_functions.pyx:21-218 (ids 1-17); id 0 is the custom hook, zero. */
+static double wfunc_eval(int id, const double *a, const double *b) {
+    switch (id) {
+    case 1: return a[0] * b[0];
+    case 2: return a[0] + b[0];
+    case 3: return (a[0] == b[0]) ? a[1] * b[1] : 0.0;
+    case 4: return (a[0] != b[0]) ? a[1] * b[1] : 0.0;
+    case 5: return (b[0] > a[0]) ? a[1] * b[1] : 0.0;
+    case 6: return (b[0] < a[0]) ? a[1] * b[1] : 0.0;
+    case 7: return (b[0] > (a[0] + a[1])) ? b[1] : 0.0;
+    case 8: return (b[0] < (a[0] + a[1])) ? b[1] : 0.0;
+    case 9: return (fabs(a[0] - b[0]) < a[1]) ? b[1] : 0.0;
+    case 10: return (fabs(a[0] - b[0]) > a[1]) ? b[1] : 0.0;
+    case 11: return (b[0] > a[0] * a[1]) ? b[1] : 0.0;
+    case 12: return a[0] * b[0] * (a[1] * b[1] + a[2] * b[2] + a[3] * b[3]);
+    case 13: {
+        double d = (a[1] * b[1] + a[2] * b[2] + a[3] * b[3]);
+        return a[0] * b[0] * d * d;
+    }
+    case 14: return a[0] * b[0] * (a[1] * b[1] + a[2] * b[2]);
+    case 15: {
+        double d = (a[1] * b[1] + a[2] * b[2]);
+        return a[0] * b[0] * d * d;
+    }
+    case 16:
+        if (a[4] == b[4]) {
+            double d = (a[1] * b[1] + a[2] * b[2] + a[3] * b[3]);
+            return a[0] * b[0] * d * d;
+        }
+        return 0.0;
+    case 17:
+        if (a[4] != b[4]) {
+            double d = (a[1] * b[1] + a[2] * b[2] + a[3] * b[3]);
+            return a[0] * b[0] * d * d;
+        }
+        return 0.0;
+    default: return 0.0;
+    }
+}
+
+static void walk_range(const walk_t *w, int64_t c0, int64_t c1, int64_t *ic, double *dc) {
+    const mesh_t *m1 = &w->m1, *m2 = &w->m2;
+    const int n1y = m1->n[1], n1z = m1->n[2];
+    const int n2x = m2->n[0], n2y = m2->n[1], n2z = m2->n[2];
+    int64_t *diff = NULL;
+    if (w->kind == K_SMU) diff = ic; /* differential counts, summed by the caller */
+    for (int64_t icell1 = c0; icell1 < c1; icell1++) {
+        int64_t if1 = m1->start[icell1], il1 = m1->start[icell1 + 1];
+        int64_t Ni = il1 - if1;
+        if (Ni <= 0) continue;
+        int ix1 = (int)(icell1 / ((int64_t)n1y * n1z));
+        int iy1 = (int)((icell1 - (int64_t)ix1 * n1y * n1z) / n1z);
+        int iz1 = (int)(icell1 - (int64_t)ix1 * n1y * n1z - (int64_t)iy1 * n1z);
+        int lx = ix1 * w->per[0] - w->steps[0], rx = (ix1 + 1) * w->per[0] + w->steps[0];
+        int ly = iy1 * w->per[1] - w->steps[1], ry = (iy1 + 1) * w->per[1] + w->steps[1];
+        int lz = iz1 * w->per[2] - w->steps[2], rz = (iz1 + 1) * w->per[2] + w->steps[2];
+        for (int nx = lx; nx < rx; nx++) {
+            double xs = nx < 0 ? -w->period[0] * w->pbc : (nx >= n2x ? w->period[0] * w->pbc : 0.0);
+            int ix2 = ((nx % n2x) + n2x) % n2x;
+            for (int ny = ly; ny < ry; ny++) {
+                double ys = ny < 0 ? -w->period[1] * w->pbc : (ny >= n2y ? w->period[1] * w->pbc : 0.0);
+                int iy2 = ((ny % n2y) + n2y) % n2y;
+                for (int nz = lz; nz < rz; nz++) {
+                    double zs = nz < 0 ? -w->period[2] * w->pbc : (nz >= n2z ? w->period[2] * w->pbc : 0.0);
+                    int iz2 = ((nz % n2z) + n2z) % n2z;
+                    int64_t icell2 = (int64_t)ix2 * n2y * n2z + (int64_t)iy2 * n2z + iz2;
+                    int64_t if2 = m2->start[icell2], il2 = m2->start[icell2 + 1];
+                    if (il2 <= if2) continue;
+                    for (int64_t i = if1; i < il1; i++) {
+                        double x1t = w->x1[i] - xs, y1t = w->y1[i] - ys, z1t = w->z1[i] - zs;
+                        for (int64_t j = if2; j < il2; j++) {
+                            double dx = x1t - w->x2[j];
+                            double dy = y1t - w->y2[j];
+                            double dz = z1t - w->z2[j];
+                            if (w->kind == K_3D) {
+                                double dsq = dx * dx + dy * dy + dz * dz;
+                                int k = w->n1e - 1;
+                                while (dsq <= w->e1[k]) {
+                                    ic[k] += 1;
+                                    k--;
+                                    if (k < 0) break;
+                                }
+                            } else if (w->kind == K_MARKED) {
+                                double dsq = dx * dx + dy * dy + dz * dz;
+                                double wt = wfunc_eval(w->wfunc, w->w1 + i * w->nw, w->w2 + j * w->nw);
+                                int k = w->n1e - 1;
+                                while (dsq <= w->e1[k]) {
+                                    dc[k] += wt;
+                                    k--;
+                                    if (k < 0) break;
+                                }
+                            } else if (w->kind == K_XYZ) {
+                                double dxy = dx * dx + dy * dy;
+                                double dzz = dz * dz;
+                                int k = w->n1e - 1;
+                                while (dxy <= w->e1[k]) {
+                                    int g = w->n2e - 1;
+                                    while (dzz <= w->e2[g]) {
+                                        ic[(int64_t)k * w->n2e + g] += 1;
+                                        g--;
+                                        if (g < 0) break;
+                                    }
+                                    k--;
+                                    if (k < 0) break;
+                                }
+                            } else { /* K_SMU */
+                                double dxy = dx * dx + dy * dy;
+                                double dzz = dz * dz;
+                                double s2 = dzz + dxy;
+                                if (s2 > w->smax2) continue;
+                                double mu2 = (s2 > 0.0) ? dxy / s2 : 0.0;
+                                if (mu2 > w->mumax2) continue;
+                                int k = w->n1e - 2;
+                                while (k != -1) {
+                                    if (s2 > w->e1[k]) break;
+                                    k--;
+                                }
+                                int g = w->n2e - 2;
+                                while (g != -1) {
+                                    if (mu2 > w->e2[g]) break;
+                                    g--;
+                                }
+                                diff[(int64_t)(k + 1) * w->n2e + (g + 1)] += 1;
+                            }
+                        }
+                    }
+                }
+            }
+        }
+    }
+}
+
+static void *walk_thread(void *arg) {
+    job_t *j = (job_t *)arg;
+    walk_range(j->w, j->c0, j->c1, j->icounts, j->dcounts);
+    return NULL;
+}
+
+/*
+ * Common driver.  xyz arrays are (N, 3) row-major float64.  period holds the
+ * box lengths (the enclosing box when pbc == 0).  search[3] are the search
+ * lengths, approx1/approx2 the approximate cell sizes.  Returns 0, or a
+ * negative code: -1 allocation failure, -2 search longer than period/3.
+ */
+static int run_walk(int kind, const double *xyz1, int64_t n1, const double *xyz2, int64_t n2,
+                    const double *w1, const double *w2, int nw, int wfunc,
+                    const double *e1, int n1e, const double *e2, int n2e,
+                    double smax2, double mumax2,
+                    const double period[3], int pbc, const double search[3],
+                    const double approx1[3], const double approx2[3], int nthreads,
+                    int64_t *icounts, double *dcounts) {
+    walk_t w;
+    memset(&w, 0, sizeof(w));
+    w.kind = kind;
+    w.pbc = pbc;
+    for (int d = 0; d < 3; d++) {
+        w.period[d] = period[d];
+        if (!(search[d] <= period[d] / 3.0)) return -2; /* rectangular_mesh.py:376-417 */
+    }
+    double c1[3], c2[3];
+    for (int d = 0; d < 3; d++) c1[d] = sample1_cell_size(period[d], search[d], approx1[d]);
+    if (mesh_build(&w.m1, xyz1, n1, period, c1) != 0) return -1;
+    for (int d = 0; d < 3; d++) c2[d] = sample2_cell_sizes(period[d], w.m1.cell[d], approx2[d]);
+    if (mesh_build(&w.m2, xyz2, n2, period, c2) != 0) { mesh_free(&w.m1); return -1; }
+    for (int d = 0; d < 3; d++) {
+        w.steps[d] = (int)ceil(search[d] / w.m2.cell[d]);
+        w.per[d] = w.m2.n[d] / w.m1.n[d];
+    }
+    size_t s1 = (size_t)(n1 > 0 ? n1 : 1), s2 = (size_t)(n2 > 0 ? n2 : 1);
+    double *buf = (double *)malloc(sizeof(double) * 3 * (s1 + s2));
+    if (!buf) { mesh_free(&w.m1); mesh_free(&w.m2); return -1; }
+    w.x1 = buf; w.y1 = buf + s1; w.z1 = buf + 2 * s1;
+    w.x2 = buf + 3 * s1; w.y2 = w.x2 + s2; w.z2 = w.x2 + 2 * s2;
+    for (int64_t k = 0; k < n1; k++) {
+        int64_t i = w.m1.order[k];
+        w.x1[k] = xyz1[3 * i]; w.y1[k] = xyz1[3 * i + 1]; w.z1[k] = xyz1[3 * i + 2];
+    }
+    for (int64_t k = 0; k < n2; k++) {
+        int64_t i = w.m2.order[k];
+        w.x2[k] = xyz2[3 * i]; w.y2[k] = xyz2[3 * i + 1]; w.z2[k] = xyz2[3 * i + 2];
+    }
+    double *wb = NULL;
+    if (kind == K_MARKED) {
+        wb = (double *)malloc(sizeof(double) * (size_t)nw * (s1 + s2));
+        if (!wb) { free(buf); mesh_free(&w.m1); mesh_free(&w.m2); return -1; }
+        w.w1 = wb; w.w2 = wb + (size_t)nw * s1;
+        for (int64_t k = 0; k < n1; k++)
+            memcpy(w.w1 + k * nw, w1 + w.m1.order[k] * nw, sizeof(double) * nw);
+        for (int64_t k = 0; k < n2; k++)
+            memcpy(w.w2 + k * nw, w2 + w.m2.order[k] * nw, sizeof(double) * nw);
+        w.nw = nw;
+        w.wfunc = wfunc;
+    }
+    w.e1 = e1; w.n1e = n1e; w.e2 = e2; w.n2e = n2e;
+    w.smax2 = smax2; w.mumax2 = mumax2;
+
+    int64_t nout = (kind == K_3D || kind == K_MARKED) ? n1e : (int64_t)n1e * n2e;
+    if (nthreads < 1) nthreads = 1;
+    if (nthreads > w.m1.ncells) nthreads = (int)w.m1.ncells;
+    job_t *jobs = (job_t *)calloc((size_t)nthreads, sizeof(job_t));
+    pthread_t *th = (pthread_t *)calloc((size_t)nthreads, sizeof(pthread_t));
+    int64_t *ipart = (int64_t *)calloc((size_t)nthreads * nout, sizeof(int64_t));
+    double *dpart = (double *)calloc((size_t)nthreads * nout, sizeof(double));
+    int rc = 0;
+    if (!jobs || !th || !ipart || !dpart) { rc = -1; goto done; }
+    /* contiguous cell1 ranges, as np.array_split (mesh_helpers.py:218-220) */
+    {
+        int64_t base = w.m1.ncells / nthreads, extra = w.m1.ncells % nthreads, c = 0;
+        for (int t = 0; t < nthreads; t++) {
+            int64_t len = base + (t < extra ? 1 : 0);
+            jobs[t].w = &w;
+            jobs[t].c0 = c;
+            jobs[t].c1 = c + len;
+            jobs[t].icounts = ipart + (size_t)t * nout;
+            jobs[t].dcounts = dpart + (size_t)t * nout;
+            c += len;
+        }
+    }
+    if (nthreads == 1) {
+        walk_thread(&jobs[0]);
+    } else {
+        int started = 0;
+        for (int t = 0; t < nthreads; t++) {
+            if (pthread_create(&th[t], NULL, walk_thread, &jobs[t]) != 0) break;
+            started++;
+        }
+        for (int t = 0; t < started; t++) pthread_join(th[t], NULL);
+        for (int t = started; t < nthreads; t++) walk_thread(&jobs[t]);
+    }
+    for (int64_t k = 0; k < nout; k++) {
+        int64_t si = 0;
+        double sd = 0.0;
+        for (int t = 0; t < nthreads; t++) {
+            si += ipart[(size_t)t * nout + k];
+            sd += dpart[(size_t)t * nout + k];
+        }
+        if (icounts) icounts[k] = si;
+        if (dcounts) dcounts[k] = sd;
+    }
+    if (kind == K_SMU && icounts) {
+        /* npairs_s_mu_engine.pyx:232-234: 2-D cumulative sum of the differential counts */
+        for (int k = 0; k < n1e; k++)
+            for (int g = 0; g < n2e; g++) {
+                int64_t v = icounts[(int64_t)k * n2e + g];
+                if (k > 0) v += icounts[(int64_t)(k - 1) * n2e + g];
+                if (g > 0) v += icounts[(int64_t)k * n2e + g - 1];
+                if (k > 0 && g > 0) v -= icounts[(int64_t)(k - 1) * n2e + g - 1];
+                icounts[(int64_t)k * n2e + g] = v;
+            }
+    }
+done:
+    free(jobs); free(th); free(ipart); free(dpart);
+    free(wb); free(buf);
+    mesh_free(&w.m1); mesh_free(&w.m2);
+    return rc;
+}
+
+/* ---------------- public oracle entry points ---------------- */
+
+/* npairs_3d_engine: counts[k] = #ordered pairs with dsq <= rbins[k]^2 (walked from the top) */
+int orc_npairs_3d(const double *xyz1, int64_t n1, const double *xyz2, int64_t n2,
+                  const double *rbins, int nb, const double period[3], int pbc,
+                  const double approx1[3], const double approx2[3], int nthreads, int64_t *out) {
+    double *e = (double *)malloc(sizeof(double) * (size_t)nb);
+    if (!e) return -1;
+    double rmax = rbins[0];
+    for (int k = 0; k < nb; k++) { e[k] = rbins[k] * rbins[k]; if (rbins[k] > rmax) rmax = rbins[k]; }
+    double search[3] = {rmax, rmax, rmax};
+    int rc = run_walk(K_3D, xyz1, n1, xyz2, n2, NULL, NULL, 0, 0, e, nb, NULL, 0, 0, 0,
+                      period, pbc, search, approx1, approx2, nthreads, out, NULL);
+    free(e);
+    return rc;
+}
+
+int orc_npairs_xy_z(const double *xyz1, int64_t n1, const double *xyz2, int64_t n2,
+                    const double *rp_bins, int nrp, const double *pi_bins, int npi,
+                    const double period[3], int pbc, const double approx1[3],
+                    const double approx2[3], int nthreads, int64_t *out) {
+    double *e1 = (double *)malloc(sizeof(double) * (size_t)(nrp + npi));
+    if (!e1) return -1;
+    double *e2 = e1 + nrp;
+    double rpmax = rp_bins[0], pimax = pi_bins[0];
+    for (int k = 0; k < nrp; k++) { e1[k] = rp_bins[k] * rp_bins[k]; if (rp_bins[k] > rpmax) rpmax = rp_bins[k]; }
+    for (int k = 0; k < npi; k++) { e2[k] = pi_bins[k] * pi_bins[k]; if (pi_bins[k] > pimax) pimax = pi_bins[k]; }
+    double search[3] = {rpmax, rpmax, pimax};
+    int rc = run_walk(K_XYZ, xyz1, n1, xyz2, n2, NULL, NULL, 0, 0, e1, nrp, e2, npi, 0, 0,
+                      period, pbc, search, approx1, approx2, nthreads, out, NULL);
+    free(e1);
+    return rc;
+}
+
+/* mu_prime = sort(sin(arccos(mu_bins))) is prepared by the caller (npairs_s_mu.py:174-175) */
+int orc_npairs_s_mu(const double *xyz1, int64_t n1, const double *xyz2, int64_t n2,
+                    const double *s_bins, int ns, const double *mu_prime, int nmu,
+                    const double period[3], int pbc, const double approx1[3],
+                    const double approx2[3], int nthreads, int64_t *out) {
+    double *e1 = (double *)malloc(sizeof(double) * (size_t)(ns + nmu));
+    if (!e1) return -1;
+    double *e2 = e1 + ns;
+    double smax = s_bins[0];
+    for (int k = 0; k < ns; k++) { e1[k] = s_bins[k] * s_bins[k]; if (s_bins[k] > smax) smax = s_bins[k]; }
+    for (int k = 0; k < nmu; k++) e2[k] = mu_prime[k] * mu_prime[k];
+    /* np.max propagates NaN */
+    double smax2 = e1[0], mumax2 = e2[0];
+    for (int k = 0; k < ns; k++) { if (isnan(e1[k]) || isnan(smax2)) smax2 = NAN; else if (e1[k] > smax2) smax2 = e1[k]; }
+    for (int k = 0; k < nmu; k++) { if (isnan(e2[k]) || isnan(mumax2)) mumax2 = NAN; else if (e2[k] > mumax2) mumax2 = e2[k]; }
+    double search[3] = {smax, smax, smax};
+    int rc = run_walk(K_SMU, xyz1, n1, xyz2, n2, NULL, NULL, 0, 0, e1, ns, e2, nmu, smax2, mumax2,
+                      period, pbc, search, approx1, approx2, nthreads, out, NULL);
+    free(e1);
+    return rc;
+}
+
+int orc_marked_npairs_3d(const double *xyz1, int64_t n1, const double *xyz2, int64_t n2,
+                         const double *w1, const double *w2, int nw, int wfunc,
+                         const double *rbins, int nb, const double period[3], int pbc,
+                         const double approx1[3], const double approx2[3], int nthreads,
+                         double *out) {
+    double *e = (double *)malloc(sizeof(double) * (size_t)nb);
+    if (!e) return -1;
+    double rmax = rbins[0];
+    for (int k = 0; k < nb; k++) { e[k] = rbins[k] * rbins[k]; if (rbins[k] > rmax) rmax = rbins[k]; }
+    double search[3] = {rmax, rmax, rmax};
+    int rc = run_walk(K_MARKED, xyz1, n1, xyz2, n2, w1, w2, nw, wfunc, e, nb, NULL, 0, 0, 0,
+                      period, pbc, search, approx1, approx2, nthreads, NULL, out);
+    free(e);
+    return rc;
+}
+
+/*
+ * Brute force over all N1*N2 ordered pairs, choosing per dimension the one
+ * shift in {-L, 0, +L} that gives the smallest |dx| (for in-range pairs this
+ * is the shift the cell walk uses), then the npairs_3d bin walk.  A second,
+ * mesh-free oracle used to cross-check the cell walk on small inputs.
+ */
+static double shifted_delta(double a, double b, double L, int pbc) {
+    double d0 = a - b;
+    if (!pbc) return d0;
+    double dp = (a - L) - b;   /* x2shift = +L */
+    double dm = (a + L) - b;   /* x2shift = -L, x1 - (-L) */
+    double best = d0;
+    if (fabs(dp) < fabs(best)) best = dp;
+    if (fabs(dm) < fabs(best)) best = dm;
+    return best;
+}
+
+int orc_bf_npairs_3d(const double *xyz1, int64_t n1, const double *xyz2, int64_t n2,
+                     const double *rbins, int nb, const double period[3], int pbc, int64_t *out) {
+    double *e = (double *)malloc(sizeof(double) * (size_t)nb);
+    if (!e) return -1;
+    for (int k = 0; k < nb; k++) { e[k] = rbins[k] * rbins[k]; out[k] = 0; }
+    for (int64_t i = 0; i < n1; i++)
+        for (int64_t j = 0; j < n2; j++) {
+            double dx = shifted_delta(xyz1[3 * i], xyz2[3 * j], period[0], pbc);
+            double dy = shifted_delta(xyz1[3 * i + 1], xyz2[3 * j + 1], period[1], pbc);
+            double dz = shifted_delta(xyz1[3 * i + 2], xyz2[3 * j + 2], period[2], pbc);
+            double dsq = dx * dx + dy * dy + dz * dz;
+            int k = nb - 1;
+            while (dsq <= e[k]) { out[k]++; k--; if (k < 0) break; }
+        }
+    free(e);
+    return 0;
+}

@@ -1,0 +1,96 @@
+"""Import the reference's own pair-counter front-ends with the engines built by
+``oracle/build_ref.py``.
+
+Test infrastructure only (golden-vector generation, oracle pinning).  Nothing
+is copied: stub package objects point ``__path__`` at the read-only halotools
+tree (for the ``.py`` front-ends) and at ``oracle/_ref`` (for the compiled
+engines), so ``halotools/__init__.py`` and its astropy/h5py imports never run.
+The one astropy symbol the front-ends import, ``NumpyRNGContext``
+(halotools ``utils/array_utils.py:6``), is replaced by a small stand-in that
+seeds and restores numpy's legacy global RNG.
+"""
+from __future__ import annotations
+
+import importlib
+import os
+import sys
+import types
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_ref")
+DEFAULT_SRC = "/root/reference"
+
+
+class NumpyRNGContext:
+    """Seed numpy's legacy global RNG inside a ``with`` block, then restore it."""
+
+    def __init__(self, seed):
+        self.seed = seed
+
+    def __enter__(self):
+        self._state = np.random.get_state()
+        np.random.seed(self.seed)
+
+    def __exit__(self, *exc):
+        np.random.set_state(self._state)
+
+
+def _pkg(name: str, paths):
+    mod = types.ModuleType(name)
+    mod.__path__ = [p for p in paths if os.path.isdir(p)]
+    mod.__package__ = name
+    sys.modules[name] = mod
+    return mod
+
+
+def load(src_root: str = DEFAULT_SRC):
+    """Return a namespace with the reference ``npairs_3d``, ``npairs_xy_z``,
+    ``npairs_s_mu``, ``marked_npairs_3d`` and the brute-force ``pairs`` module."""
+    if "halotools.mock_observables.pair_counters.npairs_3d" in sys.modules:
+        return _namespace()
+    from oracle import build_ref
+    if not build_ref.build(src_root):
+        raise RuntimeError("reference engines cannot be built here")
+
+    if "astropy" not in sys.modules:
+        astropy = types.ModuleType("astropy")
+        utils = types.ModuleType("astropy.utils")
+        misc = types.ModuleType("astropy.utils.misc")
+        misc.NumpyRNGContext = NumpyRNGContext
+        astropy.utils = utils
+        utils.misc = misc
+        sys.modules.update({"astropy": astropy, "astropy.utils": utils,
+                            "astropy.utils.misc": misc})
+
+    ht = os.path.join(src_root, "halotools")
+    bt = os.path.join(BUILD, "halotools")
+    pc = os.path.join("mock_observables", "pair_counters")
+    _pkg("halotools", [ht])
+    _pkg("halotools.utils", [os.path.join(ht, "utils")])
+    _pkg("halotools.mock_observables", [os.path.join(ht, "mock_observables")])
+    _pkg("halotools.mock_observables.pair_counters", [os.path.join(ht, pc)])
+    cp = _pkg("halotools.mock_observables.pair_counters.cpairs",
+              [os.path.join(ht, pc, "cpairs"), os.path.join(bt, pc, "cpairs")])
+    mcp = _pkg("halotools.mock_observables.pair_counters.marked_cpairs",
+               [os.path.join(ht, pc, "marked_cpairs"), os.path.join(bt, pc, "marked_cpairs")])
+    base = "halotools.mock_observables.pair_counters"
+    for name in ("npairs_3d_engine", "npairs_xy_z_engine", "npairs_s_mu_engine"):
+        m = importlib.import_module(base + ".cpairs." + name)
+        setattr(cp, name, getattr(m, name))
+    m = importlib.import_module(base + ".marked_cpairs.marked_npairs_3d_engine")
+    mcp.marked_npairs_3d_engine = m.marked_npairs_3d_engine
+    return _namespace()
+
+
+def _namespace():
+    base = "halotools.mock_observables.pair_counters"
+    ns = types.SimpleNamespace()
+    ns.npairs_3d = importlib.import_module(base + ".npairs_3d").npairs_3d
+    ns.npairs_xy_z = importlib.import_module(base + ".npairs_xy_z").npairs_xy_z
+    ns.npairs_s_mu = importlib.import_module(base + ".npairs_s_mu").npairs_s_mu
+    ns.marked_npairs_3d = importlib.import_module(base + ".marked_npairs_3d").marked_npairs_3d
+    ns.pairs = importlib.import_module(base + ".pairs")
+    ns.HalotoolsError = importlib.import_module("halotools.custom_exceptions").HalotoolsError
+    return ns

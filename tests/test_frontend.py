@@ -1,0 +1,90 @@
+"""Argument handling of the drop-in front-ends; mirrors the reference's own
+error-message tests (test_npairs_3d.py:270-304, test_npairs_xy_z.py:267-341,
+test_marked_npairs_3d.py:181-232).  Every case raises before any GPU work."""
+import numpy as np
+import pytest
+
+import halotools_gb300 as h
+
+rng = np.random.default_rng(3)
+S = rng.uniform(0, 1, (50, 3))
+
+
+def test_sensible_num_threads():
+    with pytest.raises(ValueError) as err:
+        h.npairs_3d(S, S, [0.1, 0.2], period=1, num_threads="Cuba Gooding Jr.")
+    assert "Input ``num_threads`` argument must be an integer or the string 'max'" in str(err.value)
+
+
+def test_sensible_rbins():
+    with pytest.raises(ValueError) as err:
+        h.npairs_3d(S, S, 0.1, period=1)
+    assert "Input ``rbins`` must be a monotonically increasing 1D array with at least two entries" in str(err.value)
+    with pytest.raises(ValueError):
+        h.npairs_3d(S, S, [0.1, 0.3, 0.2], period=1)
+
+
+def test_sensible_period():
+    with pytest.raises(ValueError) as err:
+        h.npairs_3d(S, S, [0.1, 0.2], period=np.inf)
+    assert "Input ``period`` must be a bounded positive number in all dimensions" in str(err.value)
+
+
+def test_search_longer_than_third_of_box():
+    with pytest.raises(ValueError) as err:
+        h.npairs_3d(S, S, [0.1, 0.4], period=1)
+    assert "cannot be larger than Lbox/3" in str(err.value)
+
+
+def test_rp_pi_bins_messages():
+    with pytest.raises(ValueError) as err:
+        h.npairs_xy_z(S, S, 0.1, [0.1, 0.2], period=1)
+    assert "Input ``rp_bins`` must be a monotonically increasing 1D array" in str(err.value)
+    with pytest.raises(ValueError) as err:
+        h.npairs_xy_z(S, S, [0.1, 0.2], [0.3, 0.2, 0.1], period=1)
+    assert "Input ``pi_bins`` must be a monotonically increasing 1D array" in str(err.value)
+
+
+def test_mu_bins_message():
+    with pytest.raises(ValueError) as err:
+        h.npairs_s_mu(S, S, [0.1, 0.2], [0.5, 0.2, 0.1], period=1)
+    assert "Input `mu_bins` must be a monotonically increasing" in str(err.value)
+
+
+def test_approx_cell_size_shape():
+    with pytest.raises(ValueError) as err:
+        h.npairs_3d(S, S, [0.1, 0.2], period=1, approx_cell1_size=[0.1, 0.1])
+    assert "must be a length-3 sequence" in str(err.value)
+
+
+def test_out_of_box_and_nonfinite_positions_rejected():
+    bad = S.copy()
+    bad[0, 0] = 1.5
+    with pytest.raises(ValueError):
+        h.npairs_3d(bad, S, [0.1, 0.2], period=1)
+    bad[0, 0] = np.nan
+    with pytest.raises(ValueError):
+        h.npairs_3d(bad, S, [0.1, 0.2], period=1)
+
+
+@pytest.mark.parametrize("wid", list(range(1, 18)))
+def test_marked_weight_shapes(wid):
+    nw = {1: 1, 2: 1, 3: 2, 4: 2, 5: 2, 6: 2, 7: 2, 8: 2, 9: 2, 10: 2, 11: 2,
+          12: 4, 13: 4, 14: 3, 15: 3, 16: 5, 17: 5}[wid]
+    with pytest.raises(h.HalotoolsError):
+        h.marked_npairs_3d(S, S, [0.1, 0.2], wid, period=1, weights1=np.ones((50, nw + 1)),
+                           weights2=np.ones((50, nw + 1)))
+    with pytest.raises(h.HalotoolsError):
+        h.marked_npairs_3d(S, S, [0.1, 0.2], wid, period=1, weights1=np.ones(49),
+                           weights2=np.ones((50, nw)))
+
+
+def test_marked_bad_ids():
+    with pytest.raises(h.HalotoolsError):
+        h.marked_npairs_3d(S, S, [0.1, 0.2], 18, period=1)
+    with pytest.raises(ValueError):
+        h.marked_npairs_3d(S, S, [0.1, 0.2], 1.0, period=1)
+
+
+def test_install_into_halotools_without_halotools_is_a_noop():
+    assert isinstance(h.install_into_halotools(), list)

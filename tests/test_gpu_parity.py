@@ -1,0 +1,144 @@
+"""CUDA engines against the reference's golden vectors and the C oracle.
+
+Integer counts must be bit-exact.  Run on a GB300 with ``pytest -m gpu``.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle
+from tests import golden_cases as G
+
+pytestmark = pytest.mark.gpu
+
+INT_CASES = [n for n in G.names() if not n.startswith("marked")]
+
+
+@pytest.mark.parametrize("name", INT_CASES)
+def test_golden_exact(gpu, name):
+    c = G.load(name)
+    if c is None:
+        pytest.skip("seeded generator differs on this platform")
+    got = G.call(gpu, c)
+    assert got.dtype == np.int64
+    assert np.array_equal(got, c["out"]), (name, got, c["out"])
+
+
+def clustered(rng, n, L, ncen, mlo=11.0, mhi=15.0):
+    """Centres + NFW-like satellites + uniform fill, z displaced (RSD)."""
+    cen = rng.uniform(0, L, (ncen, 3))
+    m = 10 ** rng.uniform(mlo, mhi, ncen)
+    nsat = rng.poisson((m / 1e12) ** 0.9)
+    tot = min(int(nsat.sum()), n - ncen)
+    host = np.repeat(np.arange(ncen), nsat)[:tot]
+    rvir = (m[host] / 1e14) ** (1 / 3.0)
+    r = rvir * rng.uniform(0, 1, tot) ** 1.5
+    d = rng.normal(size=(tot, 3))
+    d *= (r / np.linalg.norm(d, axis=1))[:, None]
+    sat = cen[host] + d
+    fill = rng.uniform(0, L, (n - ncen - tot, 3))
+    pts = np.concatenate([cen, sat, fill])
+    pts[:, 2] += rng.normal(0, 5.0, len(pts))
+    return np.mod(pts, L)
+
+
+@pytest.mark.parametrize("reach", [1, 2, 3])
+def test_npairs_3d_matches_oracle_any_grid(gpu, reach):
+    rng = np.random.default_rng(11)
+    L = 300.0
+    s = clustered(rng, 60000, L, 3000)
+    rb = np.logspace(-1, np.log10(25), 20)
+    want = oracle.npairs_3d(s, s, rb, period=L, num_threads=8)
+    plan = gpu.default_plan()
+    plan.set_reach(reach)
+    try:
+        got = gpu.npairs_3d(s, s, rb, period=L)
+        assert plan.stats()["reach"] == reach
+    finally:
+        plan.set_reach(0)
+    assert np.array_equal(got, want)
+
+
+def test_npairs_3d_cross_nonperiodic_matches_oracle(gpu):
+    rng = np.random.default_rng(12)
+    s1 = rng.uniform(-50, 150, (40000, 3))
+    s2 = rng.uniform(0, 120, (30000, 3))
+    rb = np.logspace(-1, np.log10(15), 12)
+    assert np.array_equal(gpu.npairs_3d(s1, s2, rb), oracle.npairs_3d(s1, s2, rb, num_threads=8))
+
+
+def test_npairs_xy_z_matches_oracle(gpu):
+    rng = np.random.default_rng(13)
+    L = 400.0
+    s = clustered(rng, 50000, L, 2500)
+    rp = np.logspace(-1, np.log10(30), 20)
+    pi = np.linspace(0, 40, 40)
+    want = oracle.npairs_xy_z(s, s, rp, pi, period=L, num_threads=8)
+    assert np.array_equal(gpu.npairs_xy_z(s, s, rp, pi, period=L), want)
+
+
+def test_npairs_s_mu_matches_oracle(gpu):
+    rng = np.random.default_rng(14)
+    L = 400.0
+    s = clustered(rng, 50000, L, 2500)
+    sb = np.logspace(np.log10(0.5), np.log10(40), 30)
+    mu = np.linspace(0, 1, 20)
+    want = oracle.npairs_s_mu(s, s, sb, mu, period=L, num_threads=8)
+    assert np.array_equal(gpu.npairs_s_mu(s, s, sb, mu, period=L), want)
+
+
+def test_s_mu_last_column_equals_npairs_3d(gpu):
+    # size-independent identity (test_npairs_s_mu.py:63-97): summing over mu
+    rng = np.random.default_rng(15)
+    L = 1000.0
+    s = clustered(rng, 400000, L, 20000)
+    sb = np.logspace(np.log10(0.5), np.log10(50), 30)
+    a = gpu.npairs_s_mu(s, s, sb, np.linspace(0, 1, 20), period=L)
+    b = gpu.npairs_3d(s, s, sb, period=L)
+    assert np.array_equal(a[:, -1], b)
+
+
+def test_auto_equals_cross_of_a_copy(gpu):
+    rng = np.random.default_rng(16)
+    s = rng.uniform(0, 200, (80000, 3))
+    rb = np.logspace(-1, np.log10(20), 15)
+    a = gpu.npairs_3d(s, s, rb, period=200.0)
+    # a perturbed copy is not detected as identical, so this runs the cross path
+    t = s.copy()
+    t[0, 0] = np.nextafter(t[0, 0], 0.0)
+    b = gpu.npairs_3d(s, t, rb, period=200.0)
+    c = oracle.npairs_3d(s, t, rb, period=200.0, num_threads=8)
+    assert np.array_equal(b, c)
+    assert abs(int(a[-1]) - int(b[-1])) <= 2 * 1000
+
+
+def test_repeat_runs_identical(gpu):
+    rng = np.random.default_rng(17)
+    s = clustered(rng, 100000, 500.0, 5000)
+    rb = np.logspace(-1, np.log10(30), 20)
+    a = gpu.npairs_3d(s, s, rb, period=500.0)
+    b = gpu.npairs_3d(s, s, rb, period=500.0)
+    assert np.array_equal(a, b)
+
+
+def test_empty_and_single_point_samples(gpu):
+    rb = np.array([0.1, 0.5])
+    e = np.zeros((0, 3))
+    one = np.array([[0.5, 0.5, 0.5]])
+    assert np.array_equal(gpu.npairs_3d(e, one, rb, period=2.0), [0, 0])
+    assert np.array_equal(gpu.npairs_3d(one, one, rb, period=2.0), [1, 1])
+    assert np.array_equal(gpu.npairs_xy_z(one, e, rb, rb, period=2.0), np.zeros((2, 2)))
+
+
+def test_points_on_box_faces(gpu):
+    # coordinates exactly 0 and exactly L are legal and wrap
+    pts = np.array([[0.0, 0.0, 0.0], [10.0, 10.0, 10.0], [10.0, 0.0, 5.0], [0.0, 10.0, 9.5]])
+    rb = np.array([0.1, 0.6, 1.0, 3.0])
+    want = oracle.npairs_3d(pts, pts, rb, period=10.0)
+    assert np.array_equal(gpu.npairs_3d(pts, pts, rb, period=10.0), want)
+
+
+def test_recheck_happens_and_counts_stay_exact(gpu):
+    c = G.load("3d_ties0")
+    got = gpu.npairs_3d(c["s1"], c["s2"], c["bins"], period=c["period"])
+    assert gpu.default_plan().stats()["recheck_pairs"] >= len(c["bins"])
+    assert np.array_equal(got, c["out"])

@@ -1,0 +1,54 @@
+"""The C oracle against the reference's golden vectors (CPU only)."""
+import numpy as np
+import pytest
+
+from oracle import oracle
+from tests import golden_cases as G
+
+
+@pytest.mark.parametrize("name", G.names())
+def test_oracle_matches_reference_golden(name):
+    c = G.load(name)
+    if c is None:
+        pytest.skip("seeded generator differs on this platform")
+    got = G.call(oracle, c)
+    if c["kind"] == "marked":
+        np.testing.assert_allclose(got, c["out"], rtol=1e-12, atol=1e-12)
+    else:
+        assert np.array_equal(got, c["out"]), (got, c["out"])
+
+
+def test_tie_fixtures_pin_left_to_right_unfused_order():
+    # every partner sits exactly on its own edge under ((dx*dx + dy*dy) + dz*dz)
+    for name in G.names("3d_ties"):
+        c = G.load(name)
+        assert np.array_equal(c["out"], np.arange(1, len(c["bins"]) + 1))
+
+
+@pytest.mark.parametrize("period", [None, 50.0])
+def test_cell_walk_equals_brute_force(period):
+    rng = np.random.default_rng(7)
+    s1 = rng.uniform(0, 50, (700, 3))
+    s2 = rng.uniform(0, 50, (600, 3))
+    rb = np.logspace(-1, np.log10(12), 9)
+    assert np.array_equal(oracle.npairs_3d(s1, s2, rb, period=period),
+                          oracle.brute_force_npairs_3d(s1, s2, rb, period=period))
+
+
+def test_threads_do_not_change_counts():
+    rng = np.random.default_rng(8)
+    s = rng.uniform(0, 100, (5000, 3))
+    rb = np.logspace(-1, np.log10(20), 10)
+    a = oracle.npairs_3d(s, s, rb, period=100.0, num_threads=1)
+    b = oracle.npairs_3d(s, s, rb, period=100.0, num_threads=4)
+    assert np.array_equal(a, b)
+
+
+def test_oracle_planted_error_is_caught():
+    # a mistake planted in the oracle's inputs (one partner nudged past its
+    # edge) must change the count, so the tie fixtures are sensitive
+    c = G.load("3d_ties0")
+    s2 = c["s2"].copy()
+    s2[0, 0] = np.nextafter(s2[0, 0], np.inf if s2[0, 0] < c["s1"][0, 0] else -np.inf) + 1e-9
+    got = oracle.npairs_3d(c["s1"], s2, c["bins"], period=c["period"])
+    assert not np.array_equal(got, c["out"])
