@@ -76,13 +76,16 @@ def load(build_if_missing: bool = True):
         if _lib is not None:
             return _lib
         path = _build.LIB
-        if not os.path.exists(path):
-            if not build_if_missing:
-                raise GBPairsUnavailable("libgbpairs.so not built: run halotools_gb300.build")
+        if build_if_missing:
+            # rebuilds only when a source changed (fingerprint stamp)
             try:
                 path = _build.build()
             except Exception as exc:  # nvcc missing, compile error ...
-                raise GBPairsUnavailable("cannot build libgbpairs.so: %s" % exc) from exc
+                if not os.path.exists(path):
+                    raise GBPairsUnavailable("cannot build libgbpairs.so: %s" % exc) from exc
+                raise
+        elif not os.path.exists(path):
+            raise GBPairsUnavailable("libgbpairs.so not built: run halotools_gb300.build")
         try:
             L = ctypes.CDLL(path)
         except OSError as exc:

@@ -387,6 +387,28 @@ T *at(void *base, size_t off) {
     return reinterpret_cast<T *>(static_cast<char *>(base) + off);
 }
 
+// bin of an exactly known FP64 value (self-pairs: every separation is 0)
+int host_bin(const AxisHost &ax, double v) {
+    int k = 0;
+    while (k < ax.nb && !(v <= ax.E[k])) k++;
+    return k;
+}
+
+// The count kernels skip (i, i) in auto mode; the reference computes
+// dx = (x - 0) - x = 0 for it, so it lands in the bins of v = 0.
+void add_self_pairs(const Call &c, std::vector<unsigned long long> &h) {
+    if (!c.autocorr) return;
+    int a = host_bin(c.ax[0], 0.0);
+    if (a >= c.ax[0].nb) return;
+    if (c.naxes == 1) {
+        h[a] += (unsigned long long)c.n1;
+        return;
+    }
+    int b = host_bin(c.ax[1], 0.0);
+    if (b >= c.ax[1].nb) return;
+    h[(size_t)a * (c.ax[1].nb + 1) + b] += (unsigned long long)c.n1;
+}
+
 // Runs the pipeline; fills hist_host with the differential histogram
 // ((nb0+1) x (nb1+1) u64).
 int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host) {
@@ -591,8 +613,17 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
     a.nw = c.nw;
     a.wfunc = c.wfunc;
 
-    SmemLayout L = gbp_smem_layout(c.mode, T0, T1, nb0, nb1, nsten);
+    // shared histogram copies: one per warp while they stay small, else one per CTA
+    int copies = 1;
+    if (c.mode != MODE_3D) {
+        size_t one = (size_t)(nb0 + 1) * (size_t)(c.naxes > 1 ? nb1 + 1 : 1) * 4;
+        copies = one * GBP_WARPS <= (64u << 10) ? GBP_WARPS : 1;
+    }
+    a.hist_copies = copies;
+    SmemLayout L = gbp_smem_layout(c.mode, T0, T1, nb0, nb1, nsten, copies);
     size_t smem = (size_t)L.total;
+    if (smem > (size_t)(227u << 10))
+        return fail(plan, GBP_ERR_INVALID, "too many bins for one shared-memory histogram (%zu B)", smem);
     int occ = gbp_count_occupancy(c.mode, smem);
     if (occ <= 0) return fail(plan, GBP_ERR_INVALID, "count kernel does not fit (smem %zu B)", smem);
     int grid = plan->nsm * occ;
@@ -610,6 +641,7 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
     int err_word = reinterpret_cast<const int *>(hm)[2];
     if (err_word) return fail(plan, GBP_ERR_RANGE, "positions outside [0, period] or not finite");
     hist_host.assign(at<unsigned long long>(H, h_hist), at<unsigned long long>(H, h_hist) + nhist);
+    add_self_pairs(c, hist_host);
     gbp_stats &S = plan->stats;
     S.recheck_pairs = (int64_t)hm[2];
     S.candidate_pairs = (int64_t)hm[3];
@@ -742,7 +774,7 @@ int gbp_npairs_3d(gbp_plan *plan, const double *xyz1, int64_t n1, const double *
     double search[3] = {rmax, rmax, rmax};
     if ((rc = check_search(plan, search, period3))) return rc;
     Call c;
-    c.mode = MODE_3D;
+    c.mode = nb <= GBP_NB_LANE ? MODE_3D : MODE_3DS;
     c.xyz1 = xyz1;
     c.xyz2 = xyz2;
     c.n1 = n1;

@@ -83,8 +83,10 @@ __device__ __forceinline__ Exact3 exact_pair(const double *p, const double *q, c
 }
 
 // ---------------- 3-D ----------------
+// lane_stride 32: lane-private bins; 0: shared copy updated with atomics.
 __device__ __noinline__ int slow_3d(float v, int b0, int is, int js, unsigned w,
-                                    unsigned *hl, const AxisSm &A, const CountArgs &a) {
+                                    unsigned *hl, int lane_stride, const AxisSm &A,
+                                    const CountArgs &a) {
     int k = walk_bin(v, b0, A);
     if (k >= 0) return k;
     atomicAdd(a.nrecheck, 1ull);
@@ -93,11 +95,19 @@ __device__ __noinline__ int slow_3d(float v, int b0, int is, int js, unsigned w,
     int k1 = exact_bin(exact_pair(p, q, a).s2, b0, A);
     if (w == 1) return k1;
     int k2 = exact_bin(exact_pair(q, p, a).s2, b0, A);
-    hl[k1 * 32] += 1u;
-    hl[k2 * 32] += 1u;
+    if (lane_stride) {
+        hl[k1 * lane_stride] += 1u;
+        hl[k2 * lane_stride] += 1u;
+    } else {
+        if (k1 < A.nb) atomicAdd(&hl[k1], 1u);
+        if (k2 < A.nb) atomicAdd(&hl[k2], 1u);
+    }
     return -1;
 }
 
+// LANE: lane-private bins (stride 32 words per bin); otherwise a shared copy
+// updated with atomics (wide histograms).
+template <bool LANE>
 __device__ __forceinline__ void pair_3d(const float4 &ui, const float4 &t, unsigned w,
                                         unsigned *hl, const AxisSm &A, const CountArgs &a) {
     float dx = ui.x - t.x, dy = ui.y - t.y, dz = ui.z - t.z;
@@ -105,10 +115,12 @@ __device__ __forceinline__ void pair_3d(const float4 &ui, const float4 &t, unsig
     float4 e = lut_entry(v, A);
     int b = __float_as_int(e.x) + (v > e.y ? 1 : 0);
     if ((v > e.z) & !(v > e.y)) {
-        b = slow_3d(v, __float_as_int(e.x), __float_as_int(ui.w), __float_as_int(t.w), w, hl, A, a);
+        b = slow_3d(v, __float_as_int(e.x), __float_as_int(ui.w), __float_as_int(t.w), w, hl,
+                    LANE ? 32 : 0, A, a);
         if (b < 0) return;
     }
-    hl[b * 32] += w;
+    if (LANE) hl[b * 32] += w;
+    else if (b < A.nb) atomicAdd(&hl[b], w);
 }
 
 // ---------------- (rp, pi) ----------------
@@ -222,7 +234,8 @@ __global__ void __launch_bounds__(GBP_BLOCK) k_count(const CountArgs a) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nb0 = a.ax[0].nb, nb1 = TWO ? a.ax[1].nb : 0;
     const int T0 = a.ax[0].T, T1 = TWO ? a.ax[1].T : 0;
-    const SmemLayout L = gbp_smem_layout(MODE, T0, T1, nb0, nb1, a.nsten);
+    const int copies = a.hist_copies;
+    const SmemLayout L = gbp_smem_layout(MODE, T0, T1, nb0, nb1, a.nsten, copies);
     float4 *s_lut0 = (float4 *)(smem + L.off_lut0);
     float4 *s_lut1 = (float4 *)(smem + L.off_lut1);
     float4 *s_j = (float4 *)(smem + L.off_j);
@@ -256,8 +269,8 @@ __global__ void __launch_bounds__(GBP_BLOCK) k_count(const CountArgs a) {
         s_off[i] = a.sten[i];
         s_D[i] = a.stenD[i];
     }
-    const int hist_words = (MODE == MODE_3D) ? GBP_WARPS * (nb0 + 1) * 32
-                                             : GBP_WARPS * (nb0 + 1) * (nb1 + 1);
+    const int nbin = (nb0 + 1) * (TWO ? nb1 + 1 : 1);
+    const int hist_words = (MODE == MODE_3D) ? GBP_WARPS * (nb0 + 1) * 32 : copies * nbin;
     for (int i = tid; i < hist_words; i += GBP_BLOCK) s_hist[i] = 0u;
     if (tid == 0) s_nitems = *a.nitems;
 
@@ -266,7 +279,7 @@ __global__ void __launch_bounds__(GBP_BLOCK) k_count(const CountArgs a) {
               TWO ? a.ax[1].vlo : 0.f, TWO ? a.ax[1].vhi : 0.f};
     const int stride2 = nb1 + 1;
     unsigned *hl = s_hist + warp * (nb0 + 1) * 32 + lane;          // 3-D: lane-private column
-    unsigned *hw = s_hist + warp * (nb0 + 1) * (nb1 + 1);          // 2-D: this warp's copy
+    unsigned *hw = s_hist + (warp % copies) * nbin;                // shared copy of this warp
     const int n0 = a.n[0], n1 = a.n[1], n2 = a.n[2];
     unsigned long long since_flush = 0, cand = 0;
     __syncthreads();
@@ -348,19 +361,31 @@ __global__ void __launch_bounds__(GBP_BLOCK) k_count(const CountArgs a) {
                 const int split = min(max(nselfj - base, 0), len);
                 const unsigned wrest = a.nself ? 2u : 1u;
                 int jj = grp;
+                // own-cell segment: every ordered pair once, except (i, i), whose
+                // FP64 separation is exactly 0 and is added on the host
+                const int iself = __float_as_int(ui.w);
                 if (MODE == MODE_3D) {
 #pragma unroll 4
-                    for (; jj < split; jj += G) pair_3d(ui, s_j[jj], 1u, hl, A0, a);
+                    for (; jj < split; jj += G)
+                        if (__float_as_int(s_j[jj].w) != iself) pair_3d<true>(ui, s_j[jj], 1u, hl, A0, a);
 #pragma unroll 4
-                    for (; jj < len; jj += G) pair_3d(ui, s_j[jj], wrest, hl, A0, a);
+                    for (; jj < len; jj += G) pair_3d<true>(ui, s_j[jj], wrest, hl, A0, a);
+                } else if (MODE == MODE_3DS) {
+#pragma unroll 4
+                    for (; jj < split; jj += G)
+                        if (__float_as_int(s_j[jj].w) != iself) pair_3d<false>(ui, s_j[jj], 1u, hw, A0, a);
+#pragma unroll 4
+                    for (; jj < len; jj += G) pair_3d<false>(ui, s_j[jj], wrest, hw, A0, a);
                 } else if (MODE == MODE_XYZ) {
 #pragma unroll 2
-                    for (; jj < split; jj += G) pair_xyz(ui, s_j[jj], 1u, hw, stride2, A0, A1, a);
+                    for (; jj < split; jj += G)
+                        if (__float_as_int(s_j[jj].w) != iself) pair_xyz(ui, s_j[jj], 1u, hw, stride2, A0, A1, a);
 #pragma unroll 2
                     for (; jj < len; jj += G) pair_xyz(ui, s_j[jj], wrest, hw, stride2, A0, A1, a);
                 } else if (MODE == MODE_SMU) {
 #pragma unroll 2
-                    for (; jj < split; jj += G) pair_smu(ui, s_j[jj], 1u, hw, stride2, A0, A1, a);
+                    for (; jj < split; jj += G)
+                        if (__float_as_int(s_j[jj].w) != iself) pair_smu(ui, s_j[jj], 1u, hw, stride2, A0, A1, a);
 #pragma unroll 2
                     for (; jj < len; jj += G) pair_smu(ui, s_j[jj], wrest, hw, stride2, A0, A1, a);
                 }
@@ -368,12 +393,13 @@ __global__ void __launch_bounds__(GBP_BLOCK) k_count(const CountArgs a) {
             __syncthreads();
         }
         // a lane adds at most 2 per staged j it visits; flush long before u32 overflow
-        since_flush += 2ull * (unsigned long long)total * (MODE == MODE_3D ? 1ull : 32ull);
+        since_flush += 2ull * (unsigned long long)total *
+                       (MODE == MODE_3D ? 1ull : (unsigned long long)(GBP_BLOCK / copies));
         if (since_flush > (1ull << 31)) {
             for (int i = tid; i < hist_words; i += GBP_BLOCK) {
                 unsigned v = s_hist[i];
                 if (v) {
-                    int bin = (MODE == MODE_3D) ? (i / 32) % (nb0 + 1) : i % ((nb0 + 1) * (nb1 + 1));
+                    int bin = (MODE == MODE_3D) ? (i / 32) % (nb0 + 1) : i % nbin;
                     atomicAdd(&a.hist[bin], (unsigned long long)v);
                     s_hist[i] = 0u;
                 }
@@ -393,10 +419,9 @@ __global__ void __launch_bounds__(GBP_BLOCK) k_count(const CountArgs a) {
             if (lane == 0 && s) atomicAdd(&a.hist[b], s);
         }
     } else {
-        const int nbin = (nb0 + 1) * (nb1 + 1);
         for (int b = tid; b < nbin; b += GBP_BLOCK) {
             unsigned long long s = 0;
-            for (int w = 0; w < GBP_WARPS; w++) s += s_hist[w * nbin + b];
+            for (int w = 0; w < copies; w++) s += s_hist[w * nbin + b];
             if (s) atomicAdd(&a.hist[b], s);
         }
     }
@@ -424,6 +449,10 @@ cudaError_t gbp_launch_count(int mode, const CountArgs &a, int grid, size_t smem
         e = set_smem_attr<MODE_SMU>(smem);
         if (e == cudaSuccess) k_count<MODE_SMU><<<grid, GBP_BLOCK, smem, st>>>(a);
         break;
+    case MODE_3DS:
+        e = set_smem_attr<MODE_3DS>(smem);
+        if (e == cudaSuccess) k_count<MODE_3DS><<<grid, GBP_BLOCK, smem, st>>>(a);
+        break;
     default:
         return cudaErrorInvalidValue;
     }
@@ -446,6 +475,10 @@ int gbp_count_occupancy(int mode, size_t smem) {
     case MODE_SMU:
         set_smem_attr<MODE_SMU>(smem);
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nblk, k_count<MODE_SMU>, GBP_BLOCK, smem);
+        break;
+    case MODE_3DS:
+        set_smem_attr<MODE_3DS>(smem);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nblk, k_count<MODE_3DS>, GBP_BLOCK, smem);
         break;
     default:
         return 0;

@@ -17,11 +17,12 @@
 #define GBP_TI 256          // max i-points per work item (one per thread)
 #define GBP_JCAP 1024       // staged j-points per chunk
 #define GBP_LUT_MAX 2048    // float-bit lookup slots per axis
-#define GBP_NB_MAX 64       // edges per axis
+#define GBP_NB_MAX 1024     // edges per axis
+#define GBP_NB_LANE 64      // 1-D histograms up to this size use lane-private bins
 #define GBP_SMAX 512        // stencil cells
 #define GBP_FAR 1.0e18f     // coordinate of an idle lane: far outside every edge
 
-enum { MODE_3D = 0, MODE_XYZ = 1, MODE_SMU = 2, MODE_MARK = 3, MODE_ADJ = 4 };
+enum { MODE_3D = 0, MODE_XYZ = 1, MODE_SMU = 2, MODE_MARK = 3, MODE_ADJ = 4, MODE_3DS = 5 };
 
 // One binning axis: squared quantity v compared with edges E'[0..nb-1]
 // (non-decreasing); bin(v) = smallest k with v <= E'[k], nb if none.
@@ -58,6 +59,7 @@ struct CountArgs {
     double L[3];
     AxisDev ax[2];
     int hist_stride;        // bins per histogram copy
+    int hist_copies;        // shared histogram copies (2-D and wide 1-D): 8 = one per warp, or 1
     unsigned long long *hist;   // global differential histogram(s)
     unsigned long long *nrecheck;
     // marked / adjoint
@@ -79,7 +81,7 @@ struct SmemLayout {
 __host__ __device__ inline int gbp_align(int x, int a) { return (x + a - 1) / a * a; }
 
 __host__ __device__ inline SmemLayout gbp_smem_layout(int mode, int T0, int T1, int nb0, int nb1,
-                                                      int nsten) {
+                                                      int nsten, int copies) {
     SmemLayout L;
     int o = 0;
     L.off_lut0 = o; o += T0 * 16;
@@ -103,8 +105,10 @@ __host__ __device__ inline SmemLayout gbp_smem_layout(int mode, int T0, int T1, 
         hist_bytes = GBP_WARPS * (nb0 + 1) * 32 * 4 * 2;      // lane-private FP32 sum + compensation
     } else if (mode == MODE_ADJ) {
         hist_bytes = GBP_BLOCK * 8 + 16;                      // per-thread partial gradients
+    } else if (mode == MODE_3DS) {
+        hist_bytes = copies * (nb0 + 1) * 4;                  // shared u32 copies (wide 1-D)
     } else {
-        hist_bytes = GBP_WARPS * (nb0 + 1) * (nb1 + 1) * 4;   // per-warp shared u32 (2-D)
+        hist_bytes = copies * (nb0 + 1) * (nb1 + 1) * 4;      // shared u32 copies (2-D)
     }
     o += gbp_align(hist_bytes, 16);
     L.total = o;

@@ -133,11 +133,6 @@ def _positions(sample1, sample2, period, search, pbc_min_size):
         x1, x2 = s1[:, :3], s2[:, :3]
     x1 = np.ascontiguousarray(x1, dtype=np.float64)
     x2 = x1 if same else np.ascontiguousarray(x2, dtype=np.float64)
-    for x in (x1,) if same else (x1, x2):
-        if x.size and not np.all(np.isfinite(x)):
-            raise ValueError("Input sample contains non-finite positions")
-        if pbc and x.size and (np.any(x < 0) or np.any(x > box)):
-            raise ValueError("Periodic positions must lie in [0, period] in every dimension")
     if not same and x1.shape == x2.shape and np.array_equal(x1, x2):
         x2 = x1  # identical samples: the auto-correlation path gives the same counts
     _search_check(search, box)

@@ -57,16 +57,6 @@ def test_approx_cell_size_shape():
     assert "must be a length-3 sequence" in str(err.value)
 
 
-def test_out_of_box_and_nonfinite_positions_rejected():
-    bad = S.copy()
-    bad[0, 0] = 1.5
-    with pytest.raises(ValueError):
-        h.npairs_3d(bad, S, [0.1, 0.2], period=1)
-    bad[0, 0] = np.nan
-    with pytest.raises(ValueError):
-        h.npairs_3d(bad, S, [0.1, 0.2], period=1)
-
-
 @pytest.mark.parametrize("wid", list(range(1, 18)))
 def test_marked_weight_shapes(wid):
     nw = {1: 1, 2: 1, 3: 2, 4: 2, 5: 2, 6: 2, 7: 2, 8: 2, 9: 2, 10: 2, 11: 2,

@@ -142,3 +142,37 @@ def test_recheck_happens_and_counts_stay_exact(gpu):
     got = gpu.npairs_3d(c["s1"], c["s2"], c["bins"], period=c["period"])
     assert gpu.default_plan().stats()["recheck_pairs"] >= len(c["bins"])
     assert np.array_equal(got, c["out"])
+
+
+def test_wide_histogram_npairs_3d(gpu):
+    # more edges than the lane-private histogram holds: shared-atomic variant
+    rng = np.random.default_rng(18)
+    s = rng.uniform(0, 100, (30000, 3))
+    rb = np.linspace(0.05, 12.0, 150)
+    assert np.array_equal(gpu.npairs_3d(s, s, rb, period=100.0),
+                          oracle.npairs_3d(s, s, rb, period=100.0, num_threads=8))
+
+
+def test_wide_2d_histogram_single_copy(gpu):
+    rng = np.random.default_rng(19)
+    s = rng.uniform(0, 100, (20000, 3))
+    rp = np.linspace(0.1, 10.0, 60)
+    pi = np.linspace(0.0, 12.0, 90)
+    assert np.array_equal(gpu.npairs_xy_z(s, s, rp, pi, period=100.0),
+                          oracle.npairs_xy_z(s, s, rp, pi, period=100.0, num_threads=8))
+
+
+def test_out_of_box_and_nonfinite_positions_rejected(gpu):
+    # the device digitiser flags them; the call raises instead of miscounting
+    s = np.random.default_rng(20).uniform(0, 1, (500, 3))
+    bad = s.copy()
+    bad[0, 0] = 1.5
+    with pytest.raises(ValueError):
+        gpu.npairs_3d(bad, s, [0.1, 0.2], period=1)
+    bad[0, 0] = np.nan
+    with pytest.raises(ValueError):
+        gpu.npairs_3d(bad, s, [0.1, 0.2], period=1)
+    with pytest.raises(ValueError):
+        gpu.npairs_3d(bad, s, [0.1, 0.2])
+    # the plan stays usable after a rejected call
+    assert gpu.npairs_3d(s, s, [0.1, 0.2], period=1)[-1] >= 500
