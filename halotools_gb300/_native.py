@@ -27,6 +27,7 @@ EXPORTED = (
     "gbp_plan_create", "gbp_plan_destroy", "gbp_plan_set_stream", "gbp_plan_set_reach",
     "gbp_plan_last_error", "gbp_plan_stats", "gbp_npairs_3d", "gbp_npairs_xy_z",
     "gbp_npairs_s_mu", "gbp_marked_npairs_3d", "gbp_measure_fp32_peak",
+    "gbp_npairs_3d_static",
 )
 
 
@@ -106,6 +107,7 @@ def load(build_if_missing: bool = True):
         L.gbp_marked_npairs_3d.argtypes = [vp, vp, i64, vp, i64, vp, vp, i32, i32, pd, i32, pd,
                                            i32, i32, pd]
         L.gbp_measure_fp32_peak.argtypes = [vp, pd]
+        L.gbp_npairs_3d_static.argtypes = [vp, i64, pd, i32, pd, i32, vp, vp]
         _lib = L
         return L
 

@@ -15,11 +15,12 @@
 #include <vector>
 
 #include "../../include/gbpairs.h"
+#include "gbp_host.h"
 #include "gbp_internal.cuh"
 
-namespace {
+using namespace gbp;
 
-const double INF = std::numeric_limits<double>::infinity();
+namespace {
 
 struct DevBuf {
     void *p = nullptr;
@@ -62,271 +63,6 @@ int fail(gbp_plan *p, int code, const char *fmt, ...) {
                         "%s: %s", #expr, cudaGetErrorString(e_));                         \
     } while (0)
 
-// ---------------- edges ----------------
-// Walk-from-the-top semantics of npairs_3d / npairs_xy_z / marked engines:
-// counts[k] is incremented iff v <= E[m] for every m >= k; a NaN edge stops
-// the walk, so it and every edge below it are never satisfied.
-std::vector<double> edges_top_walk(const double *r, int n) {
-    std::vector<double> E(n);
-    double m = INF;
-    bool dead = false;
-    for (int k = n - 1; k >= 0; k--) {
-        double e = r[k] * r[k];
-        if (std::isnan(e)) dead = true;
-        if (dead) {
-            E[k] = -INF;
-        } else {
-            m = std::min(m, e);
-            E[k] = m;
-        }
-    }
-    return E;
-}
-
-// npairs_s_mu_engine.pyx:198-226 semantics: a value is skipped when it exceeds
-// max(E) (NaN max: never skipped); otherwise its index is 1 + the first k
-// (walking down from n-2) with v > E[k].  Returns non-decreasing E' with
-// bin(v) = smallest m such that v <= E'[m].
-std::vector<double> edges_smu(const std::vector<double> &E) {
-    int n = (int)E.size();
-    std::vector<double> Ep(n);
-    double gate = -INF;
-    bool nan = false;
-    for (double e : E) {
-        if (std::isnan(e)) nan = true;
-        else gate = std::max(gate, e);
-    }
-    Ep[n - 1] = nan ? INF : gate;
-    double m = INF;
-    for (int k = n - 2; k >= 0; k--) {
-        if (!std::isnan(E[k])) m = std::min(m, E[k]);
-        Ep[k] = m;
-    }
-    // keep E' non-decreasing at the top (the gate is >= every finite edge)
-    for (int k = n - 2; k >= 0; k--) Ep[k] = std::min(Ep[k], Ep[k + 1]);
-    return Ep;
-}
-
-float f_down(double x) {
-    if (std::isnan(x)) return -std::numeric_limits<float>::infinity();
-    float f = (float)x;
-    if ((double)f > x) f = std::nextafter(f, -std::numeric_limits<float>::infinity());
-    return f;
-}
-
-float f_up(double x) {
-    if (std::isnan(x)) return std::numeric_limits<float>::infinity();
-    float f = (float)x;
-    if ((double)f < x) f = std::nextafter(f, std::numeric_limits<float>::infinity());
-    return f;
-}
-
-struct AxisHost {
-    int nb = 0;
-    std::vector<double> E;
-    std::vector<float> hi, lo;
-    std::vector<float4> lut;
-    int T = 0, S = 0, B = 0;
-    float vlo = 0, vhi = 0;
-};
-
-// Error model.  Coordinates are FP32 offsets from a cell corner, |u| <= c, the
-// stencil offset o*c is rounded to FP32 and added, and dx is formed in FP32:
-// |dx32 - dx| <= delta with delta = 2^-24 (c + c + K c + (K+1) c + |dx|) plus
-// the FP64 rounding of the corner and of the reference's own dx (~2^-50 L).
-struct ErrModel {
-    double cmax = 0, K = 1, Lmax = 0;
-    double delta(double Ebound) const {
-        double dxmax = std::sqrt(std::max(Ebound, 0.0));
-        return std::ldexp(1.0, -24) * (2 * cmax + K * cmax + (K + 1) * cmax + dxmax) * 1.02 +
-               std::ldexp(1.0, -50) * Lmax;
-    }
-    // bound on |v32 - v64| for v a sum of m squares near E
-    double band(double E, int m) const {
-        double E1 = E * (1.0 + std::ldexp(1.0, -10)) + 1e-300;
-        double d = delta(E1);
-        return 2.0 * d * std::sqrt((double)m) * std::sqrt(E1) + m * d * d +
-               (m + 1) * std::ldexp(1.0, -24) * E1 + m * std::ldexp(1.0, -50) * E1;
-    }
-};
-
-void axis_thresholds(AxisHost &ax, const std::vector<double> &E, const ErrModel *em, int m) {
-    ax.nb = (int)E.size();
-    ax.E = E;
-    ax.hi.resize(ax.nb);
-    ax.lo.resize(ax.nb);
-    for (int k = 0; k < ax.nb; k++) {
-        double e = E[k];
-        if (std::isinf(e)) {
-            ax.hi[k] = ax.lo[k] = (float)e;
-            continue;
-        }
-        double b = em ? 2.0 * em->band(e, m) : 0.0;
-        ax.lo[k] = f_down(e - b);
-        ax.hi[k] = f_up(e + b);
-    }
-    // hi must be non-decreasing for the table's start bins
-    for (int k = 1; k < ax.nb; k++) ax.hi[k] = std::max(ax.hi[k], ax.hi[k - 1]);
-}
-
-uint32_t fbits(float f) {
-    uint32_t u;
-    std::memcpy(&u, &f, 4);
-    return u;
-}
-float bitsf(uint32_t u) {
-    float f;
-    std::memcpy(&f, &u, 4);
-    return f;
-}
-
-// Float-bit lookup table: slot s covers the FP32 values whose bits, shifted
-// right by S, equal B + s; values below/above the covered octaves clamp into
-// the first/last slot.  Each slot stores the first bin not provably exceeded
-// by every value of the slot (b0) and, if at most one edge can be crossed in
-// the slot, that edge's thresholds; otherwise (thr, lo) = (+inf, -inf) which
-// sends the pair to the walk.  qband(a) (optional) is stored in .w.
-template <class QB>
-void axis_lut(AxisHost &ax, QB qband) {
-    const float finf = std::numeric_limits<float>::infinity();
-    double hmax = 0, pmin = INF;
-    for (int k = 0; k < ax.nb; k++) {
-        for (float t : {ax.hi[k], ax.lo[k]}) {
-            if (std::isfinite(t) && t > 0) {
-                hmax = std::max(hmax, (double)t);
-                pmin = std::min(pmin, (double)t);
-            }
-        }
-    }
-    int emax = hmax > 0 ? std::ilogb(hmax) + 1 : 0;
-    emax = std::min(emax, 126);
-    int emin = std::isfinite(pmin) ? std::ilogb(pmin) - 1 : emax - 1;
-    emin = std::max(emin, std::max(emax - 40, -126));
-    int O = emax - emin + 1;
-    int m = 0;
-    while (m < 10 && (O << (m + 1)) <= GBP_LUT_MAX) m++;
-    ax.S = 23 - m;
-    ax.T = O << m;
-    ax.B = (emin + 127) << m;
-    ax.vlo = std::ldexp(1.0f, emin);
-    ax.vhi = std::nextafter(std::ldexp(1.0f, emax + 1), 0.0f);
-    ax.lut.resize(ax.T);
-    for (int s = 0; s < ax.T; s++) {
-        float a = s == 0 ? 0.0f : bitsf((uint32_t)(ax.B + s) << ax.S);
-        float bnext = s == ax.T - 1 ? finf : bitsf((uint32_t)(ax.B + s + 1) << ax.S);
-        float pred = std::nextafter(bnext, 0.0f);
-        int b0 = 0;
-        while (b0 < ax.nb && ax.hi[b0] < a) b0++;
-        float4 e;
-        int bi = b0;
-        std::memcpy(&e.x, &bi, 4);
-        if (b0 == ax.nb) {
-            e.y = finf;
-            e.z = finf;
-        } else {
-            bool simple = (b0 + 1 == ax.nb) || (pred <= ax.lo[b0 + 1]);
-            e.y = simple ? ax.hi[b0] : finf;
-            e.z = simple ? ax.lo[b0] : -finf;
-        }
-        e.w = qband(a);
-        ax.lut[s] = e;
-    }
-}
-
-// ---------------- grid & stencil ----------------
-struct Geometry {
-    int n[3];
-    double c[3], L[3];
-    int K;
-    int pbc;
-    int64_t ncells;
-    std::vector<int> sten;
-    std::vector<float4> stenD;
-    int nself;
-};
-
-const int64_t MAX_CELLS = 1ll << 24;
-const int64_t MAX_CELLS_PER_DIM = 256;
-
-// Cells per dimension for reach K: as many as keep K*c >= search, capped;
-// with periodic wrap every offset in [-K, K] must reach a distinct cell.
-bool grid_for_reach(int K, const double L[3], const double search[3], int pbc, int64_t n[3]) {
-    for (int d = 0; d < 3; d++) {
-        int64_t m = (int64_t)std::floor(L[d] * K / search[d]);
-        m = std::min<int64_t>(std::max<int64_t>(m, 1), MAX_CELLS_PER_DIM);
-        // search <= L/3, so three cells of size L/3 always cover it for K = 1
-        if (pbc && K == 1) m = std::max<int64_t>(m, 3);
-        if (pbc && m < 2 * K + 1) return false;
-        n[d] = m;
-    }
-    return true;
-}
-
-void choose_grid(Geometry &g, const double L[3], const double search[3], int pbc, int64_t n2,
-                 int reach_hint) {
-    for (int d = 0; d < 3; d++) g.L[d] = L[d];
-    g.pbc = pbc;
-    double vol = L[0] * L[1] * L[2];
-    double rho = vol > 0 ? (double)n2 / vol : 0;
-    int best = 1;
-    for (int K = 2; K <= 4; K++) {
-        int64_t n[3];
-        if (!grid_for_reach(K, L, search, pbc, n)) break;
-        double cvol = (L[0] / n[0]) * (L[1] / n[1]) * (L[2] / n[2]);
-        if (reach_hint > 0) {
-            if (K <= reach_hint) best = K;
-            continue;
-        }
-        // autotune: finer cells prune more of the cube stencil, but each work
-        // item then streams fewer points per i; keep ~28+ points per cell.
-        if (rho * cvol >= 28.0) best = K;
-    }
-    int64_t n[3];
-    grid_for_reach(best, L, search, pbc, n);
-    g.K = best;
-    g.ncells = 1;
-    for (int d = 0; d < 3; d++) {
-        g.n[d] = (int)n[d];
-        g.c[d] = L[d] / (double)n[d];
-        g.ncells *= n[d];
-    }
-}
-
-// kind 0: sphere of radius search[0]; kind 1: cylinder (rp, pi).
-void build_stencil(Geometry &g, const double search[3], int kind, bool autocorr) {
-    int K = g.K;
-    g.sten.clear();
-    g.stenD.clear();
-    auto push = [&](int ox, int oy, int oz) {
-        g.sten.push_back((ox + 64) | ((oy + 64) << 8) | ((oz + 64) << 16));
-        g.stenD.push_back(make_float4((float)(ox * g.c[0]), (float)(oy * g.c[1]),
-                                      (float)(oz * g.c[2]), 0.f));
-    };
-    auto keep = [&](int ox, int oy, int oz) {
-        double gx = std::max(std::abs(ox) - 1, 0) * g.c[0];
-        double gy = std::max(std::abs(oy) - 1, 0) * g.c[1];
-        double gz = std::max(std::abs(oz) - 1, 0) * g.c[2];
-        const double slack = 1.0 + 1e-9;
-        if (kind == 0) return gx * gx + gy * gy + gz * gz <= search[0] * search[0] * slack;
-        return gx * gx + gy * gy <= search[0] * search[0] * slack && gz <= search[2] * slack;
-    };
-    int Kx = std::min(K, g.pbc ? K : g.n[0] - 1);
-    int Ky = std::min(K, g.pbc ? K : g.n[1] - 1);
-    int Kz = std::min(K, g.pbc ? K : g.n[2] - 1);
-    push(0, 0, 0);
-    for (int ox = -Kx; ox <= Kx; ox++)
-        for (int oy = -Ky; oy <= Ky; oy++)
-            for (int oz = -Kz; oz <= Kz; oz++) {
-                if (ox == 0 && oy == 0 && oz == 0) continue;
-                if (autocorr) {
-                    bool pos = ox > 0 || (ox == 0 && (oy > 0 || (oy == 0 && oz > 0)));
-                    if (!pos) continue;
-                }
-                if (keep(ox, oy, oz)) push(ox, oy, oz);
-            }
-    g.nself = autocorr ? 1 : 0;
-}
-
 // ---------------- workspace ----------------
 struct Carve {
     size_t off = 0;
@@ -360,6 +96,34 @@ int ensure_pinned(gbp_plan *plan, size_t bytes) {
     return GBP_OK;
 }
 
+// one binning axis, vector-backed (up to GBP_NB_MAX edges)
+struct AxisHost {
+    int nb = 0;
+    std::vector<double> E;
+    std::vector<float> hi, lo;
+    std::vector<float4> lut;
+    int T = 0, S = 0, B = 0;
+    float vlo = 0, vhi = 0;
+    void set(const std::vector<double> &Ein, const ErrModel *em, int m) {
+        nb = (int)Ein.size();
+        E = Ein;
+        hi.assign(nb, 0.f);
+        lo.assign(nb, 0.f);
+        thresholds(nb, E.data(), em, m, hi.data(), lo.data());
+    }
+    template <class QB>
+    void make_lut(QB q) {
+        lut.resize(GBP_LUT_MAX);
+        LutInfo i = build_lut(nb, hi.data(), lo.data(), q, lut.data());
+        T = i.T;
+        S = i.S;
+        B = i.B;
+        vlo = i.vlo;
+        vhi = i.vhi;
+        lut.resize(T);
+    }
+};
+
 struct SampleDev {
     const double *xyz = nullptr;
     int *cellid, *rank, *count, *start, *orig;
@@ -387,24 +151,17 @@ T *at(void *base, size_t off) {
     return reinterpret_cast<T *>(static_cast<char *>(base) + off);
 }
 
-// bin of an exactly known FP64 value (self-pairs: every separation is 0)
-int host_bin(const AxisHost &ax, double v) {
-    int k = 0;
-    while (k < ax.nb && !(v <= ax.E[k])) k++;
-    return k;
-}
-
 // The count kernels skip (i, i) in auto mode; the reference computes
 // dx = (x - 0) - x = 0 for it, so it lands in the bins of v = 0.
 void add_self_pairs(const Call &c, std::vector<unsigned long long> &h) {
     if (!c.autocorr) return;
-    int a = host_bin(c.ax[0], 0.0);
+    int a = host_bin(c.ax[0].nb, c.ax[0].E.data(), 0.0);
     if (a >= c.ax[0].nb) return;
     if (c.naxes == 1) {
         h[a] += (unsigned long long)c.n1;
         return;
     }
-    int b = host_bin(c.ax[1], 0.0);
+    int b = host_bin(c.ax[1].nb, c.ax[1].E.data(), 0.0);
     if (b >= c.ax[1].nb) return;
     h[(size_t)a * (c.ax[1].nb + 1) + b] += (unsigned long long)c.n1;
 }
@@ -418,7 +175,7 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
     const int64_t ncells = c.g.ncells;
     const int nb0 = c.ax[0].nb, nb1 = c.naxes > 1 ? c.ax[1].nb : 0;
     const int T0 = c.ax[0].T, T1 = c.naxes > 1 ? c.ax[1].T : 0;
-    const int nsten = (int)c.g.sten.size();
+    const int nsten = c.g.nsten;
     const size_t nhist = (size_t)(nb0 + 1) * (size_t)(c.naxes > 1 ? nb1 + 1 : 1);
     const int nsamp = c.autocorr ? 1 : 2;
     const int64_t ns[2] = {c.n1, c.n2};
@@ -485,8 +242,8 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
         std::memcpy(at<char>(H, h_hi1), c.ax[1].hi.data(), sizeof(float) * nb1);
         std::memcpy(at<char>(H, h_lo1), c.ax[1].lo.data(), sizeof(float) * nb1);
     }
-    std::memcpy(at<char>(H, h_sten), c.g.sten.data(), sizeof(int) * nsten);
-    std::memcpy(at<char>(H, h_stenD), c.g.stenD.data(), sizeof(float4) * nsten);
+    std::memcpy(at<char>(H, h_sten), c.g.sten, sizeof(int) * nsten);
+    std::memcpy(at<char>(H, h_stenD), c.g.stenD, sizeof(float4) * nsten);
 
     CK(cudaEventRecord(plan->ev[0], st));
     int64_t h2d = 0, d2h = 0;
@@ -687,22 +444,7 @@ int check_search(gbp_plan *plan, const double search[3], const double period3[3]
     return GBP_OK;
 }
 
-double max_nan(const double *r, int n) {
-    double m = r[0];
-    for (int k = 0; k < n; k++) {
-        if (std::isnan(r[k]) || std::isnan(m)) m = NAN;
-        else m = std::max(m, r[k]);
-    }
-    return m;
-}
 
-ErrModel err_model(const Geometry &g) {
-    ErrModel em;
-    em.cmax = std::max(g.c[0], std::max(g.c[1], g.c[2]));
-    em.K = g.K;
-    em.Lmax = std::max(g.L[0], std::max(g.L[1], g.L[2]));
-    return em;
-}
 
 }  // namespace
 
@@ -782,11 +524,13 @@ int gbp_npairs_3d(gbp_plan *plan, const double *xyz1, int64_t n1, const double *
     c.autocorr = (xyz1 == xyz2 && n1 == n2);
     c.mem = mem;
     c.naxes = 1;
-    choose_grid(c.g, period3, search, pbc, n2, plan->reach);
+    choose_grid(c.g, period3, search, pbc, n2, plan->reach, MAX_CELLS_PER_DIM);
     build_stencil(c.g, search, 0, c.autocorr);
     ErrModel em = err_model(c.g);
-    axis_thresholds(c.ax[0], edges_top_walk(rbins, nb), &em, 3);
-    axis_lut(c.ax[0], [](float) { return 0.0f; });
+    std::vector<double> E(nb);
+    edges_top_walk(rbins, nb, E.data());
+    c.ax[0].set(E, &em, 3);
+    c.ax[0].make_lut(no_qband);
     std::vector<unsigned long long> h;
     if (n1 == 0 || n2 == 0) {
         for (int k = 0; k < nb; k++) counts[k] = 0;
@@ -820,13 +564,16 @@ int gbp_npairs_xy_z(gbp_plan *plan, const double *xyz1, int64_t n1, const double
     c.autocorr = (xyz1 == xyz2 && n1 == n2);
     c.mem = mem;
     c.naxes = 2;
-    choose_grid(c.g, period3, search, pbc, n2, plan->reach);
+    choose_grid(c.g, period3, search, pbc, n2, plan->reach, MAX_CELLS_PER_DIM);
     build_stencil(c.g, search, 1, c.autocorr);
     ErrModel em = err_model(c.g);
-    axis_thresholds(c.ax[0], edges_top_walk(rp_bins, n_rp), &em, 2);
-    axis_thresholds(c.ax[1], edges_top_walk(pi_bins, n_pi), &em, 1);
-    axis_lut(c.ax[0], [](float) { return 0.0f; });
-    axis_lut(c.ax[1], [](float) { return 0.0f; });
+    std::vector<double> E0(n_rp), E1(n_pi);
+    edges_top_walk(rp_bins, n_rp, E0.data());
+    edges_top_walk(pi_bins, n_pi, E1.data());
+    c.ax[0].set(E0, &em, 2);
+    c.ax[1].set(E1, &em, 1);
+    c.ax[0].make_lut(no_qband);
+    c.ax[1].make_lut(no_qband);
     if (n1 == 0 || n2 == 0) {
         for (int k = 0; k < n_rp * n_pi; k++) counts[k] = 0;
         return GBP_OK;
@@ -865,20 +612,21 @@ int gbp_npairs_s_mu(gbp_plan *plan, const double *xyz1, int64_t n1, const double
     c.autocorr = (xyz1 == xyz2 && n1 == n2);
     c.mem = mem;
     c.naxes = 2;
-    choose_grid(c.g, period3, search, pbc, n2, plan->reach);
+    choose_grid(c.g, period3, search, pbc, n2, plan->reach, MAX_CELLS_PER_DIM);
     build_stencil(c.g, search, 0, c.autocorr);
     ErrModel em = err_model(c.g);
-    std::vector<double> Es(n_s), Em(n_mu);
+    std::vector<double> Es(n_s), Em(n_mu), Eps(n_s), Epm(n_mu);
     for (int k = 0; k < n_s; k++) Es[k] = s_bins[k] * s_bins[k];
     for (int k = 0; k < n_mu; k++) Em[k] = mu_prime[k] * mu_prime[k];
-    std::vector<double> Eps = edges_smu(Es), Epm = edges_smu(Em);
-    axis_thresholds(c.ax[0], Eps, &em, 3);
-    axis_thresholds(c.ax[1], Epm, nullptr, 0);
+    edges_smu(Es.data(), n_s, Eps.data());
+    edges_smu(Em.data(), n_mu, Epm.data());
+    c.ax[0].set(Eps, &em, 3);
+    c.ax[1].set(Epm, nullptr, 0);
     // q = dxy/s^2 error bound for pairs with s^2 >= a (FP32 value), factor 2 margin
     double dtop = em.delta(smax * smax);
     double Lm = em.Lmax;
     ErrModel emc = em;
-    axis_lut(c.ax[0], [&](float a) -> float {
+    c.ax[0].make_lut([&](float a) -> float {
         double s2lo = (double)a - 2.0 * emc.band((double)a, 3);
         if (!(s2lo > 0)) return 3.0e38f;
         double s = std::sqrt(s2lo);
@@ -886,7 +634,7 @@ int gbp_npairs_s_mu(gbp_plan *plan, const double *xyz1, int64_t n1, const double
                     std::ldexp(1.0, -48) * Lm / s;
         return f_up(2.0 * qb);
     });
-    axis_lut(c.ax[1], [](float) { return 0.0f; });
+    c.ax[1].make_lut(no_qband);
     if (n1 == 0 || n2 == 0) {
         for (int k = 0; k < n_s * n_mu; k++) counts[k] = 0;
         return GBP_OK;

@@ -1,0 +1,301 @@
+// Host-side planning shared by the plan API (gbp_api.cu) and the
+// allocation-free entry point (gbp_static.cu): the reference's bin-edge
+// semantics, FP32 thresholds with a rigorous error band, float-bit lookup
+// tables, grid choice and the cell stencil.  Everything works on fixed-size
+// storage supplied by the caller; nothing here allocates.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <limits>
+
+#include "gbp_internal.cuh"
+
+#define GBP_STEN_CAP 729  // (2*4+1)^3 cells for reach <= 4
+
+namespace gbp {
+
+const double INF = std::numeric_limits<double>::infinity();
+const float FINF = std::numeric_limits<float>::infinity();
+
+// Walk-from-the-top semantics of npairs_3d / npairs_xy_z / marked engines
+// (npairs_3d_engine.pyx:178-182): counts[k] is incremented iff v <= r[m]^2 for
+// every m >= k; a NaN edge stops the walk.  E'[k] = min(r[k..]^2), -inf once a
+// NaN was met, so bin(v) = smallest k with v <= E'[k].
+inline void edges_top_walk(const double *r, int n, double *E) {
+    double m = INF;
+    bool dead = false;
+    for (int k = n - 1; k >= 0; k--) {
+        double e = r[k] * r[k];
+        if (std::isnan(e)) dead = true;
+        if (dead) {
+            E[k] = -INF;
+        } else {
+            m = std::min(m, e);
+            E[k] = m;
+        }
+    }
+}
+
+// npairs_s_mu_engine.pyx:198-226 semantics for squared edges Ein: a value is
+// skipped when it exceeds max(Ein) (a NaN max never skips); otherwise its index
+// is 1 + the first k (walking down from n-2) with v > Ein[k].  Writes
+// non-decreasing E' with bin(v) = smallest m such that v <= E'[m].
+inline void edges_smu(const double *Ein, int n, double *Ep) {
+    double gate = -INF;
+    bool nan = false;
+    for (int k = 0; k < n; k++) {
+        if (std::isnan(Ein[k])) nan = true;
+        else gate = std::max(gate, Ein[k]);
+    }
+    Ep[n - 1] = nan ? INF : gate;
+    double m = INF;
+    for (int k = n - 2; k >= 0; k--) {
+        if (!std::isnan(Ein[k])) m = std::min(m, Ein[k]);
+        Ep[k] = m;
+    }
+    for (int k = n - 2; k >= 0; k--) Ep[k] = std::min(Ep[k], Ep[k + 1]);
+}
+
+inline float f_down(double x) {
+    if (std::isnan(x)) return -FINF;
+    float f = (float)x;
+    if ((double)f > x) f = std::nextafter(f, -FINF);
+    return f;
+}
+
+inline float f_up(double x) {
+    if (std::isnan(x)) return FINF;
+    float f = (float)x;
+    if ((double)f < x) f = std::nextafter(f, FINF);
+    return f;
+}
+
+inline float bitsf(uint32_t u) {
+    float f;
+    std::memcpy(&f, &u, 4);
+    return f;
+}
+
+// Error model.  Coordinates are FP32 offsets from a cell corner, |u| <= c, the
+// stencil offset o*c is rounded to FP32 and added, and dx is formed in FP32:
+// |dx32 - dx| <= delta = 2^-24 (c + c + K c + (K+1) c + |dx|) plus the FP64
+// rounding of the corner and of the reference's own dx (~2^-50 L).
+struct ErrModel {
+    double cmax = 0, K = 1, Lmax = 0;
+    double delta(double Ebound) const {
+        double dxmax = std::sqrt(std::max(Ebound, 0.0));
+        return std::ldexp(1.0, -24) * (2 * cmax + K * cmax + (K + 1) * cmax + dxmax) * 1.02 +
+               std::ldexp(1.0, -50) * Lmax;
+    }
+    // bound on |v32 - v64| for v a sum of m squares near E
+    double band(double E, int m) const {
+        double E1 = E * (1.0 + std::ldexp(1.0, -10)) + 1e-300;
+        double d = delta(E1);
+        return 2.0 * d * std::sqrt((double)m) * std::sqrt(E1) + m * d * d +
+               (m + 1) * std::ldexp(1.0, -24) * E1 + m * std::ldexp(1.0, -50) * E1;
+    }
+};
+
+// FP32 thresholds: v32 <= lo[k] proves v64 <= E[k]; v32 > hi[k] proves
+// v64 > E[k] (twice the error bound on each side).  em == nullptr gives the
+// tight FP32 bracket of E (used for the mu' axis, whose band is per pair).
+inline void thresholds(int nb, const double *E, const ErrModel *em, int m, float *hi, float *lo) {
+    for (int k = 0; k < nb; k++) {
+        double e = E[k];
+        if (std::isinf(e)) {
+            hi[k] = lo[k] = (float)e;
+            continue;
+        }
+        double b = em ? 2.0 * em->band(e, m) : 0.0;
+        lo[k] = f_down(e - b);
+        hi[k] = f_up(e + b);
+    }
+    for (int k = 1; k < nb; k++) hi[k] = std::max(hi[k], hi[k - 1]);
+}
+
+struct LutInfo {
+    int T = 0, S = 0, B = 0;
+    float vlo = 0, vhi = 0;
+};
+
+// Float-bit lookup table: slot s covers the FP32 values whose bits, shifted
+// right by S, equal B + s; values below/above the covered octaves clamp into
+// the first/last slot.  Each slot stores the first bin not provably exceeded
+// by every value of the slot (b0) and, if at most one edge can be crossed in
+// the slot, that edge's thresholds; otherwise (thr, lo) = (+inf, -inf), which
+// sends the pair to the per-edge walk.  qband(a) goes to .w.  The octaves run
+// from just below the smallest positive lower threshold (an edge at 0 lives in
+// slot 0) to just above the largest finite upper threshold.
+template <class QB>
+LutInfo build_lut(int nb, const float *hi, const float *lo, QB qband, float4 *lut) {
+    LutInfo L;
+    double hmax = 0, pmin = INF;
+    for (int k = 0; k < nb; k++) {
+        if (std::isfinite(hi[k]) && hi[k] > 0) hmax = std::max(hmax, (double)hi[k]);
+        if (std::isfinite(lo[k]) && lo[k] > 0) pmin = std::min(pmin, (double)lo[k]);
+    }
+    int emax = hmax > 0 ? std::ilogb(hmax) + 1 : 0;
+    emax = std::min(emax, 126);
+    int emin = std::isfinite(pmin) ? std::ilogb(pmin) - 1 : emax - 1;
+    emin = std::min(emin, emax - 1);
+    emin = std::max(emin, std::max(emax - 40, -126));
+    int O = emax - emin + 1;
+    int m = 0;
+    while (m < 10 && (O << (m + 1)) <= GBP_LUT_MAX) m++;
+    L.S = 23 - m;
+    L.T = O << m;
+    L.B = (emin + 127) << m;
+    L.vlo = std::ldexp(1.0f, emin);
+    L.vhi = std::nextafter(std::ldexp(1.0f, emax + 1), 0.0f);
+    for (int s = 0; s < L.T; s++) {
+        float a = s == 0 ? 0.0f : bitsf((uint32_t)(L.B + s) << L.S);
+        float bnext = s == L.T - 1 ? FINF : bitsf((uint32_t)(L.B + s + 1) << L.S);
+        float pred = std::nextafter(bnext, 0.0f);
+        int b0 = 0;
+        while (b0 < nb && hi[b0] < a) b0++;
+        float4 e;
+        std::memcpy(&e.x, &b0, 4);
+        if (b0 == nb) {
+            e.y = FINF;
+            e.z = FINF;
+        } else {
+            bool simple = (b0 + 1 == nb) || (pred <= lo[b0 + 1]);
+            e.y = simple ? hi[b0] : FINF;
+            e.z = simple ? lo[b0] : -FINF;
+        }
+        e.w = qband(a);
+        lut[s] = e;
+    }
+    return L;
+}
+
+inline float no_qband(float) { return 0.0f; }
+
+// bin of an exactly known FP64 value (self-pairs: every separation is 0)
+inline int host_bin(int nb, const double *E, double v) {
+    int k = 0;
+    while (k < nb && !(v <= E[k])) k++;
+    return k;
+}
+
+// ---------------- grid & stencil ----------------
+struct Geometry {
+    int n[3];
+    double c[3], L[3];
+    int K;
+    int pbc;
+    int64_t ncells;
+    int nsten;
+    int nself;
+    int sten[GBP_STEN_CAP];
+    float4 stenD[GBP_STEN_CAP];
+};
+
+const int64_t MAX_CELLS_PER_DIM = 256;
+
+// Cells per dimension for reach K: as many as keep K*c >= search, capped;
+// with periodic wrap every offset in [-K, K] must reach a distinct cell.
+inline bool grid_for_reach(int K, const double L[3], const double search[3], int pbc,
+                           int64_t n[3], int64_t cap) {
+    for (int d = 0; d < 3; d++) {
+        int64_t m = (int64_t)std::floor(L[d] * K / search[d]);
+        m = std::min<int64_t>(std::max<int64_t>(m, 1), cap);
+        // search <= L/3, so three cells of size L/3 always cover it for K = 1
+        if (pbc && K == 1) m = std::max<int64_t>(m, 3);
+        if (pbc && m < 2 * K + 1) return false;
+        n[d] = m;
+    }
+    return true;
+}
+
+// Reach K in 1..4 (hint > 0 forces it when feasible); the automatic choice
+// keeps about 28+ points of sample 2 per cell: finer cells prune more of the
+// cube stencil, but each work item then streams fewer points per i-point.
+inline void choose_grid(Geometry &g, const double L[3], const double search[3], int pbc,
+                        int64_t n2, int reach_hint, int64_t cap_per_dim) {
+    for (int d = 0; d < 3; d++) g.L[d] = L[d];
+    g.pbc = pbc;
+    double vol = L[0] * L[1] * L[2];
+    double rho = vol > 0 ? (double)n2 / vol : 0;
+    int best = 1;
+    for (int K = 2; K <= 4; K++) {
+        int64_t n[3];
+        if (!grid_for_reach(K, L, search, pbc, n, cap_per_dim)) break;
+        double cvol = (L[0] / n[0]) * (L[1] / n[1]) * (L[2] / n[2]);
+        if (reach_hint > 0) {
+            if (K <= reach_hint) best = K;
+            continue;
+        }
+        if (rho * cvol >= 28.0) best = K;
+    }
+    int64_t n[3];
+    grid_for_reach(best, L, search, pbc, n, cap_per_dim);
+    g.K = best;
+    g.ncells = 1;
+    for (int d = 0; d < 3; d++) {
+        g.n[d] = (int)n[d];
+        g.c[d] = L[d] / (double)n[d];
+        g.ncells *= n[d];
+    }
+}
+
+// kind 0: sphere of radius search[0]; kind 1: cylinder (rp = search[0], pi = search[2]).
+// Offsets whose cell boxes are farther apart than the search are dropped.  In
+// auto mode the own cell comes first and only the lexicographically positive
+// half of the other offsets is kept (each unordered cell pair once).
+inline void build_stencil(Geometry &g, const double search[3], int kind, bool autocorr) {
+    int K = g.K;
+    g.nsten = 0;
+    auto push = [&](int ox, int oy, int oz) {
+        g.sten[g.nsten] = (ox + 64) | ((oy + 64) << 8) | ((oz + 64) << 16);
+        g.stenD[g.nsten] = make_float4((float)(ox * g.c[0]), (float)(oy * g.c[1]),
+                                       (float)(oz * g.c[2]), 0.f);
+        g.nsten++;
+    };
+    auto keep = [&](int ox, int oy, int oz) {
+        double gx = std::max(std::abs(ox) - 1, 0) * g.c[0];
+        double gy = std::max(std::abs(oy) - 1, 0) * g.c[1];
+        double gz = std::max(std::abs(oz) - 1, 0) * g.c[2];
+        const double slack = 1.0 + 1e-9;
+        if (kind == 0) return gx * gx + gy * gy + gz * gz <= search[0] * search[0] * slack;
+        return gx * gx + gy * gy <= search[0] * search[0] * slack && gz <= search[2] * slack;
+    };
+    int Kx = std::min(K, g.pbc ? K : g.n[0] - 1);
+    int Ky = std::min(K, g.pbc ? K : g.n[1] - 1);
+    int Kz = std::min(K, g.pbc ? K : g.n[2] - 1);
+    push(0, 0, 0);
+    for (int ox = -Kx; ox <= Kx; ox++)
+        for (int oy = -Ky; oy <= Ky; oy++)
+            for (int oz = -Kz; oz <= Kz; oz++) {
+                if (ox == 0 && oy == 0 && oz == 0) continue;
+                if (autocorr) {
+                    bool pos = ox > 0 || (ox == 0 && (oy > 0 || (oy == 0 && oz > 0)));
+                    if (!pos) continue;
+                }
+                if (keep(ox, oy, oz)) push(ox, oy, oz);
+            }
+    g.nself = autocorr ? 1 : 0;
+}
+
+inline ErrModel err_model(const Geometry &g) {
+    ErrModel em;
+    em.cmax = std::max(g.c[0], std::max(g.c[1], g.c[2]));
+    em.K = g.K;
+    em.Lmax = std::max(g.L[0], std::max(g.L[1], g.L[2]));
+    return em;
+}
+
+inline double max_nan(const double *r, int n) {
+    double m = r[0];
+    for (int k = 0; k < n; k++) {
+        if (std::isnan(r[k]) || std::isnan(m)) m = NAN;
+        else m = std::max(m, r[k]);
+    }
+    return m;
+}
+
+}  // namespace gbp

@@ -109,6 +109,33 @@ int gbp_marked_npairs_3d(gbp_plan *plan, const double *xyz1, int64_t n1, const d
                          const double *period3, int32_t pbc, int32_t mem, double *out);
 
 /*
+ * Allocation-free npairs_3d.  No counterpart in the reference: it exists for
+ * callers that cannot allocate device memory while they count (a process
+ * whose device memory belongs to another framework's caching allocator, or a
+ * latency-critical loop where cudaMalloc/cudaFree would synchronise the
+ * device).  Same counts as gbp_npairs_3d for an auto-correlation
+ * (sample 2 == sample 1), but every scratch buffer lives in one static
+ * device array of GBP_STATIC_SCRATCH_BYTES that each GPU loading this
+ * library holds until exit; the call allocates nothing, device or host.
+ *   xyz     device pointer, (n, 3) row-major float64, 1 <= n <= GBP_STATIC_MAX_POINTS
+ *   rbins   host array of 2..64 edges; period3 host array; pbc 0 or 1
+ *   counts  device pointer to n_bins int64, written by the last kernel of the
+ *           call (all -1 if a position lies outside [0, period] or is not
+ *           finite)
+ *   stream  cudaStream_t (NULL = legacy default stream); the call does not
+ *           synchronise it
+ * Larger inputs return GBP_ERR_INVALID.  The first call on a device looks up
+ * the array's device address (cudaGetSymbolAddress) with that device
+ * current; make that first call before any stream capture.  All calls share
+ * the array: calls that overlap on the GPU race and must be serialised.
+ */
+#define GBP_STATIC_MAX_POINTS 131072
+#define GBP_STATIC_MAX_CELLS 131072
+#define GBP_STATIC_SCRATCH_BYTES (13u << 20)
+int gbp_npairs_3d_static(const double *xyz, int64_t n, const double *rbins, int32_t nbins,
+                         const double *period3, int32_t pbc, int64_t *counts, void *stream);
+
+/*
  * Measurement utility with no counterpart in the reference: runs a dependent-
  * chain FFMA kernel on the plan's GPU and returns the FP32 FMA throughput in
  * TFLOP/s (2 flops per FFMA), the ceiling of the count kernels' FP32 pipe.

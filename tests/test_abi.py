@@ -29,7 +29,7 @@ def test_library_exports_every_declared_symbol():
 
 def test_binding_covers_header():
     from halotools_gb300 import _native
-    assert set(declared_symbols()) <= set(_native.EXPORTED) | {"gbp_npairs_3d_static"}
+    assert set(declared_symbols()) <= set(_native.EXPORTED)
 
 
 def test_plan_create_without_gpu_reports_no_device():
