@@ -135,6 +135,7 @@ struct SampleDev {
 
 struct Call {
     int mode;
+    int wf = 1;  // marking-function template for MODE_MARK
     const double *xyz1, *xyz2;
     int64_t n1, n2;
     bool autocorr;
@@ -168,7 +169,8 @@ void add_self_pairs(const Call &c, std::vector<unsigned long long> &h) {
 
 // Runs the pipeline; fills hist_host with the differential histogram
 // ((nb0+1) x (nb1+1) u64).
-int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host) {
+int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host,
+             std::vector<double> *histd_host = nullptr) {
     CK(cudaSetDevice(plan->device));
     cudaStream_t st = plan->stream;
     std::memset(&plan->stats, 0, sizeof(plan->stats));
@@ -370,21 +372,28 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
     a.nw = c.nw;
     a.wfunc = c.wfunc;
 
-    // shared histogram copies: one per warp while they stay small, else one per CTA
+    a.top0 = std::min(c.ax[0].hi[nb0 - 1], 1.0e30f);
+    a.top1 = c.naxes > 1 ? std::min(c.ax[1].hi[nb1 - 1], 1.0e30f) : 0.f;
+    a.self_bin = host_bin(nb0, c.ax[0].E.data(), 0.0);
+    const int jwb = c.mode == MODE_MARK ? (c.wf == 0 ? 8 * c.nw : 4) : 0;
+    // shared histogram copies (2-D and wide 1-D): as many as keep the CTA
+    // within ~72 KB of shared memory (3 CTAs per SM), at least one
     int copies = 1;
-    if (c.mode != MODE_3D) {
-        size_t one = (size_t)(nb0 + 1) * (size_t)(c.naxes > 1 ? nb1 + 1 : 1) * 4;
-        copies = one * GBP_WARPS <= (64u << 10) ? GBP_WARPS : 1;
+    if (c.mode != MODE_3D && c.mode != MODE_MARK) {
+        for (int cp = GBP_WARPS; cp >= 1; cp /= 2) {
+            copies = cp;
+            if (gbp_smem_layout(c.mode, T0, T1, nb0, nb1, nsten, cp, jwb).total <= (72 << 10)) break;
+        }
     }
     a.hist_copies = copies;
-    SmemLayout L = gbp_smem_layout(c.mode, T0, T1, nb0, nb1, nsten, copies);
+    SmemLayout L = gbp_smem_layout(c.mode, T0, T1, nb0, nb1, nsten, copies, jwb);
     size_t smem = (size_t)L.total;
     if (smem > (size_t)(227u << 10))
         return fail(plan, GBP_ERR_INVALID, "too many bins for one shared-memory histogram (%zu B)", smem);
-    int occ = gbp_count_occupancy(c.mode, smem);
+    int occ = gbp_count_occupancy(c.mode, c.wf, smem);
     if (occ <= 0) return fail(plan, GBP_ERR_INVALID, "count kernel does not fit (smem %zu B)", smem);
     int grid = plan->nsm * occ;
-    CK(gbp_launch_count(c.mode, a, grid, smem, st));
+    CK(gbp_launch_count(c.mode, c.wf, a, grid, smem, st));
     launches += 1;
     CK(cudaEventRecord(plan->ev[2], st));
     CK(cudaMemcpyAsync(at<char>(H, h_hist), a.hist, nhist * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
@@ -398,7 +407,8 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
     int err_word = reinterpret_cast<const int *>(hm)[2];
     if (err_word) return fail(plan, GBP_ERR_RANGE, "positions outside [0, period] or not finite");
     hist_host.assign(at<unsigned long long>(H, h_hist), at<unsigned long long>(H, h_hist) + nhist);
-    add_self_pairs(c, hist_host);
+    if (c.mode != MODE_MARK) add_self_pairs(c, hist_host);
+    if (histd_host) histd_host->assign(at<double>(H, h_histd), at<double>(H, h_histd) + nhist);
     gbp_stats &S = plan->stats;
     S.recheck_pairs = (int64_t)hm[2];
     S.candidate_pairs = (int64_t)hm[3];
@@ -658,9 +668,53 @@ int gbp_marked_npairs_3d(gbp_plan *plan, const double *xyz1, int64_t n1, const d
                          int64_t n2, const double *w1, const double *w2, int32_t nw,
                          int32_t wfunc_id, const double *rbins, int32_t nb, const double *period3,
                          int32_t pbc, int32_t mem, double *out) {
-    (void)xyz1; (void)n1; (void)xyz2; (void)n2; (void)w1; (void)w2; (void)nw; (void)wfunc_id;
-    (void)rbins; (void)nb; (void)period3; (void)pbc; (void)mem; (void)out;
-    return fail(plan, GBP_ERR_INVALID, "marked counts not built yet");
+    int rc = check_common(plan, xyz1, n1, xyz2, n2, period3, pbc, mem);
+    if (rc) return rc;
+    // marked_npairs_3d.py:281-326: number of weights per marking function
+    static const int NW[18] = {0, 1, 1, 2, 2, 2, 2, 2, 2, 2, 2, 2, 4, 4, 3, 3, 5, 5};
+    if (wfunc_id < 1 || wfunc_id > 17) return fail(plan, GBP_ERR_INVALID, "weight_func_id %d is not recognized", wfunc_id);
+    if (nw != NW[wfunc_id]) return fail(plan, GBP_ERR_INVALID, "weight_func_id %d needs %d weights per point", wfunc_id, NW[wfunc_id]);
+    if ((n1 > 0 && !w1) || (n2 > 0 && !w2)) return fail(plan, GBP_ERR_INVALID, "null weights");
+    if (!rbins || nb < 2 || nb > GBP_NB_LANE || !out)
+        return fail(plan, GBP_ERR_INVALID, "rbins must have 2..%d entries", GBP_NB_LANE);
+    double rmax = max_nan(rbins, nb);
+    double search[3] = {rmax, rmax, rmax};
+    if ((rc = check_search(plan, search, period3))) return rc;
+    // symmetric marking functions (f(a, b) == f(b, a)) may walk each unordered
+    // pair once; the others walk every ordered pair
+    const bool symmetric = wfunc_id <= 4 || wfunc_id >= 12;
+    Call c;
+    c.mode = MODE_MARK;
+    c.wf = (wfunc_id == 1) ? 1 : (wfunc_id == 2) ? 2 : 0;
+    c.xyz1 = xyz1;
+    c.xyz2 = xyz2;
+    c.n1 = n1;
+    c.n2 = n2;
+    c.autocorr = (xyz1 == xyz2 && n1 == n2 && w1 == w2 && symmetric);
+    c.mem = mem;
+    c.w1 = w1;
+    c.w2 = w2;
+    c.nw = nw;
+    c.wfunc = wfunc_id;
+    c.naxes = 1;
+    choose_grid(c.g, period3, search, pbc, n2, plan->reach, MAX_CELLS_PER_DIM);
+    build_stencil(c.g, search, 0, c.autocorr);
+    ErrModel em = err_model(c.g);
+    std::vector<double> E(nb);
+    edges_top_walk(rbins, nb, E.data());
+    c.ax[0].set(E, &em, 3);
+    c.ax[0].make_lut(no_qband);
+    for (int k = 0; k < nb; k++) out[k] = 0.0;
+    if (n1 == 0 || n2 == 0) return GBP_OK;
+    std::vector<unsigned long long> h;
+    std::vector<double> hd;
+    if ((rc = run_call(plan, c, h, &hd))) return rc;
+    double run = 0.0;
+    for (int k = 0; k < nb; k++) {
+        run += hd[k];
+        out[k] = run;
+    }
+    return GBP_OK;
 }
 
 int gbp_measure_fp32_peak(gbp_plan *plan, double *tflops) {

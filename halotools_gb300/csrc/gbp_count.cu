@@ -1,26 +1,34 @@
 // Pair-count kernels (sm_103a).  Replace the cell walks of
-// npairs_3d_engine.pyx:103-182, npairs_xy_z_engine.pyx:143-194 and
-// npairs_s_mu_engine.pyx:150-229.
+// npairs_3d_engine.pyx:103-182, npairs_xy_z_engine.pyx:143-194,
+// npairs_s_mu_engine.pyx:150-229 and marked_npairs_3d_engine.pyx:150-216.
 //
 // Work decomposition: a persistent grid pulls work items (cell, first i,
 // i count <= 256) from an atomic cursor.  Each thread holds one i-point (FP32,
 // relative to its cell) in registers; the points of the item's stencil cells
-// are staged through shared memory with the cell offset o*c already added, so
-// the inner loop is a broadcast LDS.128, three FSUB, one FMUL + two FFMA and a
-// float-bit table lookup.  When the i count is small the CTA's warps split
-// the staged j range into groups instead of idling.
+// are staged through shared memory with the cell offset o*c already added.
+// When the i count is small the CTA's warps split the staged j range into
+// groups instead of idling.
 //
-// Exactness: the FP32 squared distance is compared with FP32 thresholds that
-// bracket each FP64 edge by a rigorous error bound (built on the host).  A pair
-// whose FP32 value falls inside a bracket is re-evaluated in FP64 with the
-// reference's own operation order, ((x1 - shift) - x2) squared and summed left
-// to right, unfused (npairs_3d_engine.pyx:167-176), so integer counts equal the
+// Two stages per warp.  Stage 1 (every candidate): a broadcast LDS.128, three
+// FSUB, the squared quantities and one compare against the outermost edge;
+// in-range pairs are compacted with a ballot into a 64-entry per-warp queue
+// {v0, v1, i, j | symmetric-flag}.  Stage 2 (every 32 queued pairs, all lanes
+// busy): float-bit table lookup of the bin, the guard-band test, and the
+// histogram update.  Most candidates of a cube stencil are out of range, so
+// the binning work is paid only for the ~15-40% that count.
+//
+// Exactness: the FP32 value is compared with FP32 thresholds that bracket each
+// FP64 edge by a rigorous error bound (built on the host).  A pair whose FP32
+// value falls inside a bracket is re-evaluated in FP64 with the reference's
+// operation order, ((x1 - shift) - x2) squared and summed left to right,
+// unfused (npairs_3d_engine.pyx:167-176), so integer counts equal the
 // reference's.
 //
 // Histograms: 1-D counts go to lane-private u32 bins in shared memory (no
-// atomics, no bank conflicts: bin-major, lane-minor); 2-D counts go to one
-// shared u32 histogram per warp with shared atomics.  Both are flushed to a
-// global u64 histogram at the end (and early, before any u32 could overflow).
+// atomics, no bank conflicts: bin-major, lane-minor); 2-D counts go to shared
+// u32 copies updated with shared atomics; marked sums go to lane-private FP32
+// (sum, compensation) pairs (Kahan).  All are flushed to global u64 / FP64
+// histograms at the end (integer copies also early, before a u32 could wrap).
 #include "gbp_internal.cuh"
 
 struct AxisSm {
@@ -82,55 +90,94 @@ __device__ __forceinline__ Exact3 exact_pair(const double *p, const double *q, c
     return r;
 }
 
-// ---------------- 3-D ----------------
-// lane_stride 32: lane-private bins; 0: shared copy updated with atomics.
-__device__ __noinline__ int slow_3d(float v, int b0, int is, int js, unsigned w,
-                                    unsigned *hl, int lane_stride, const AxisSm &A,
-                                    const CountArgs &a) {
-    int k = walk_bin(v, b0, A);
-    if (k >= 0) return k;
+#define SYM_BIT 0x80000000u
+
+// ---------------- stage 2: 1-D (3-D separation) ----------------
+// Bins of a pair whose FP32 value may straddle an edge.  Returns 0 with k[0]
+// the bin when FP32 decides it after all; else re-evaluates in FP64 and
+// returns the number of orders (1, or 2 for a symmetric pair) written to k[].
+__device__ __noinline__ int slow_3d(float v, int b0, int is, int js, bool sym, int *k,
+                                    const AxisSm &A, const CountArgs &a) {
+    int kk = walk_bin(v, b0, A);
+    if (kk >= 0) {
+        k[0] = kk;
+        return 0;
+    }
     atomicAdd(a.nrecheck, 1ull);
     const double *p = a.x64_1 + 3 * (int64_t)is;
     const double *q = a.x64_2 + 3 * (int64_t)js;
-    int k1 = exact_bin(exact_pair(p, q, a).s2, b0, A);
-    if (w == 1) return k1;
-    int k2 = exact_bin(exact_pair(q, p, a).s2, b0, A);
-    if (lane_stride) {
-        hl[k1 * lane_stride] += 1u;
-        hl[k2 * lane_stride] += 1u;
-    } else {
-        if (k1 < A.nb) atomicAdd(&hl[k1], 1u);
-        if (k2 < A.nb) atomicAdd(&hl[k2], 1u);
-    }
-    return -1;
+    k[0] = exact_bin(exact_pair(p, q, a).s2, b0, A);
+    if (!sym) return 1;
+    k[1] = exact_bin(exact_pair(q, p, a).s2, b0, A);
+    return 2;
 }
 
-// LANE: lane-private bins (stride 32 words per bin); otherwise a shared copy
-// updated with atomics (wide histograms).
 template <bool LANE>
-__device__ __forceinline__ void pair_3d(const float4 &ui, const float4 &t, unsigned w,
-                                        unsigned *hl, const AxisSm &A, const CountArgs &a) {
-    float dx = ui.x - t.x, dy = ui.y - t.y, dz = ui.z - t.z;
-    float v = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-    float4 e = lut_entry(v, A);
-    int b = __float_as_int(e.x) + (v > e.y ? 1 : 0);
-    if ((v > e.z) & !(v > e.y)) {
-        b = slow_3d(v, __float_as_int(e.x), __float_as_int(ui.w), __float_as_int(t.w), w, hl,
-                    LANE ? 32 : 0, A, a);
-        if (b < 0) return;
+__device__ __forceinline__ void bin_3d(const float4 &e, unsigned *h, const AxisSm &A,
+                                       const CountArgs &a) {
+    const float v = e.x;
+    const unsigned jw = __float_as_uint(e.w);
+    const bool sym = jw & SYM_BIT;
+    const unsigned w = sym ? 2u : 1u;
+    float4 t = lut_entry(v, A);
+    int b = __float_as_int(t.x) + (v > t.y ? 1 : 0);
+    if ((v > t.z) & !(v > t.y)) {
+        int k[2];
+        int n = slow_3d(v, __float_as_int(t.x), __float_as_int(e.z), (int)(jw & ~SYM_BIT), sym, k,
+                        A, a);
+        if (n == 0) {
+            b = k[0];
+        } else {
+            for (int q = 0; q < n; q++) {
+                if (LANE) h[k[q] * 32] += 1u;
+                else if (k[q] < A.nb) atomicAdd(&h[k[q]], 1u);
+            }
+            return;
+        }
     }
-    if (LANE) hl[b * 32] += w;
-    else if (b < A.nb) atomicAdd(&hl[b], w);
+    if (LANE) h[b * 32] += w;
+    else if (b < A.nb) atomicAdd(&h[b], w);
 }
 
-// ---------------- (rp, pi) ----------------
+// ---------------- stage 2: marked (Kahan in lane-private FP32 pairs) ----------------
+__device__ __forceinline__ void kahan_add(float *hs, float *hc, int b, float x) {
+    float s = hs[b * 32], c = hc[b * 32];
+    float y = x - c;
+    float t = s + y;
+    hc[b * 32] = (t - s) - y;
+    hs[b * 32] = t;
+}
+
+__device__ __forceinline__ void bin_mark(const float4 &e, float *hs, float *hc, const AxisSm &A,
+                                         const CountArgs &a) {
+    const float v = e.x, wt = e.y;
+    const unsigned jw = __float_as_uint(e.w);
+    const bool sym = jw & SYM_BIT;
+    float4 t = lut_entry(v, A);
+    int b = __float_as_int(t.x) + (v > t.y ? 1 : 0);
+    if ((v > t.z) & !(v > t.y)) {
+        int k[2];
+        int n = slow_3d(v, __float_as_int(t.x), __float_as_int(e.z), (int)(jw & ~SYM_BIT), sym, k,
+                        A, a);
+        if (n == 0) {
+            b = k[0];
+        } else {
+            for (int q = 0; q < n; q++)
+                if (k[q] < A.nb) kahan_add(hs, hc, k[q], wt);
+            return;
+        }
+    }
+    if (b < A.nb) kahan_add(hs, hc, b, sym ? 2.0f * wt : wt);
+}
+
+// ---------------- stage 2: (rp, pi) ----------------
 __device__ __noinline__ void slow_xyz(float v0, float v1, int b0a, int b0b, int is, int js,
-                                      unsigned w, unsigned *hw, int stride, const AxisSm &A,
+                                      bool sym, unsigned *hw, int stride, const AxisSm &A,
                                       const AxisSm &Bx, const CountArgs &a) {
     int ka = walk_bin(v0, b0a, A);
     int kb = walk_bin(v1, b0b, Bx);
     if (ka >= 0 && kb >= 0) {
-        if (ka < A.nb && kb < Bx.nb) atomicAdd(&hw[ka * stride + kb], w);
+        if (ka < A.nb && kb < Bx.nb) atomicAdd(&hw[ka * stride + kb], sym ? 2u : 1u);
         return;
     }
     atomicAdd(a.nrecheck, 1ull);
@@ -140,55 +187,53 @@ __device__ __noinline__ void slow_xyz(float v0, float v1, int b0a, int b0b, int 
     int ea = ka >= 0 ? ka : exact_bin(r.dxy, b0a, A);
     int eb = kb >= 0 ? kb : exact_bin(r.dz2, b0b, Bx);
     if (ea < A.nb && eb < Bx.nb) atomicAdd(&hw[ea * stride + eb], 1u);
-    if (w == 1) return;
+    if (!sym) return;
     Exact3 s = exact_pair(q, p, a);
     int fa = ka >= 0 ? ka : exact_bin(s.dxy, b0a, A);
     int fb = kb >= 0 ? kb : exact_bin(s.dz2, b0b, Bx);
     if (fa < A.nb && fb < Bx.nb) atomicAdd(&hw[fa * stride + fb], 1u);
 }
 
-__device__ __forceinline__ void pair_xyz(const float4 &ui, const float4 &t, unsigned w,
-                                         unsigned *hw, int stride, const AxisSm &A,
-                                         const AxisSm &Bx, const CountArgs &a) {
-    float dx = ui.x - t.x, dy = ui.y - t.y, dz = ui.z - t.z;
-    float v0 = fmaf(dy, dy, dx * dx);
-    float v1 = dz * dz;
+__device__ __forceinline__ void bin_xyz(const float4 &e, unsigned *hw, int stride, const AxisSm &A,
+                                        const AxisSm &Bx, const CountArgs &a) {
+    const float v0 = e.x, v1 = e.y;
+    const unsigned jw = __float_as_uint(e.w);
+    const bool sym = jw & SYM_BIT;
     float4 e0 = lut_entry(v0, A);
     float4 e1 = lut_entry(v1, Bx);
     int ba = __float_as_int(e0.x) + (v0 > e0.y ? 1 : 0);
     int bb = __float_as_int(e1.x) + (v1 > e1.y ? 1 : 0);
     bool amb = ((v0 > e0.z) & !(v0 > e0.y)) | ((v1 > e1.z) & !(v1 > e1.y));
     if (amb) {
-        slow_xyz(v0, v1, __float_as_int(e0.x), __float_as_int(e1.x), __float_as_int(ui.w),
-                 __float_as_int(t.w), w, hw, stride, A, Bx, a);
+        slow_xyz(v0, v1, __float_as_int(e0.x), __float_as_int(e1.x), __float_as_int(e.z),
+                 (int)(jw & ~SYM_BIT), sym, hw, stride, A, Bx, a);
         return;
     }
-    if ((ba < A.nb) & (bb < Bx.nb)) atomicAdd(&hw[ba * stride + bb], w);
+    if ((ba < A.nb) & (bb < Bx.nb)) atomicAdd(&hw[ba * stride + bb], sym ? 2u : 1u);
 }
 
-// ---------------- (s, mu') ----------------
+// ---------------- stage 2: (s, mu') ----------------
 // v = s^2 on axis 0; q = dxy / s^2 on axis 1, whose FP32 error depends on s:
 // the s table's 4th field holds the q error bound for the slot's smallest s.
 __device__ __noinline__ void slow_smu(float v, float q, float qb, int b0s, int is, int js,
-                                      unsigned w, unsigned *hw, int stride, const AxisSm &A,
+                                      bool sym, unsigned *hw, int stride, const AxisSm &A,
                                       const AxisSm &Q, const CountArgs &a) {
     int ks = walk_bin(v, b0s, A);
     int kq = -1;
     if (ks >= 0 && ks < A.nb && v > 0.0f) {
-        // q decided only if it is farther than qb from every edge it could straddle
         int g = 0;
         while (g < Q.nb && q > Q.hi[g] + qb) g++;
         if (!(g < Q.nb && q > Q.lo[g] - qb)) kq = g;
     }
     if (ks >= A.nb) return;  // beyond the s gate: never counted
     if (ks >= 0 && kq >= 0) {
-        if (kq < Q.nb) atomicAdd(&hw[ks * stride + kq], w);
+        if (kq < Q.nb) atomicAdd(&hw[ks * stride + kq], sym ? 2u : 1u);
         return;
     }
     atomicAdd(a.nrecheck, 1ull);
     const double *p = a.x64_1 + 3 * (int64_t)is;
     const double *qq = a.x64_2 + 3 * (int64_t)js;
-    for (int o = 0; o < (w == 1 ? 1 : 2); o++) {
+    for (int o = 0; o < (sym ? 2 : 1); o++) {
         Exact3 r = o == 0 ? exact_pair(p, qq, a) : exact_pair(qq, p, a);
         int es = exact_bin(r.s2, 0, A);
         if (es >= A.nb) continue;
@@ -199,15 +244,14 @@ __device__ __noinline__ void slow_smu(float v, float q, float qb, int b0s, int i
     }
 }
 
-__device__ __forceinline__ void pair_smu(const float4 &ui, const float4 &t, unsigned w,
-                                         unsigned *hw, int stride, const AxisSm &A,
-                                         const AxisSm &Q, const CountArgs &a) {
-    float dx = ui.x - t.x, dy = ui.y - t.y, dz = ui.z - t.z;
-    float dxy = fmaf(dy, dy, dx * dx);
-    float v = fmaf(dz, dz, dxy);
+__device__ __forceinline__ void bin_smu(const float4 &e, unsigned *hw, int stride, const AxisSm &A,
+                                        const AxisSm &Q, const CountArgs &a) {
+    const float v = e.x, dxy = e.y;
+    const unsigned jw = __float_as_uint(e.w);
+    const bool sym = jw & SYM_BIT;
     float4 e0 = lut_entry(v, A);
     int bs = __float_as_int(e0.x) + (v > e0.y ? 1 : 0);
-    if (bs >= A.nb) return;  // beyond the s gate (the common case for far pairs)
+    if (bs >= A.nb) return;  // beyond the s gate
     float q = __fdividef(dxy, v);
     float qb = e0.w;
     float4 e1 = lut_entry(q, Q);
@@ -218,27 +262,75 @@ __device__ __forceinline__ void pair_smu(const float4 &ui, const float4 &t, unsi
     bool amb = ((v > e0.z) & !(v > e0.y)) | !(q - below > qb) | !(above - q > qb) |
                (e1.y > 3.0e38f);
     if (amb) {
-        slow_smu(v, q, qb, __float_as_int(e0.x), __float_as_int(ui.w), __float_as_int(t.w), w,
+        slow_smu(v, q, qb, __float_as_int(e0.x), __float_as_int(e.z), (int)(jw & ~SYM_BIT), sym,
                  hw, stride, A, Q, a);
         return;
     }
-    if (bq >= Q.nb) return;  // beyond the mu' gate
-    atomicAdd(&hw[bs * stride + bq], w);
+    if (bq < Q.nb) atomicAdd(&hw[bs * stride + bq], sym ? 2u : 1u);
+}
+
+// ---------------- marking functions (marking_functions.pyx:21-218) ----------------
+// WF 1 and 2 evaluate in FP32 (product, sum).  WF 0 evaluates any id 1-17 in
+// FP64 from the FP64 weights, exactly as the reference does (comparisons
+// included), and rounds the result to FP32 for accumulation.
+__device__ __forceinline__ double wfunc64(int id, const double *A, const double *B) {
+    switch (id) {
+    case 1: return A[0] * B[0];
+    case 2: return A[0] + B[0];
+    case 3: return (A[0] == B[0]) ? A[1] * B[1] : 0.0;
+    case 4: return (A[0] != B[0]) ? A[1] * B[1] : 0.0;
+    case 5: return (B[0] > A[0]) ? A[1] * B[1] : 0.0;
+    case 6: return (B[0] < A[0]) ? A[1] * B[1] : 0.0;
+    case 7: return (B[0] > (A[0] + A[1])) ? B[1] : 0.0;
+    case 8: return (B[0] < (A[0] + A[1])) ? B[1] : 0.0;
+    case 9: return (fabs(A[0] - B[0]) < A[1]) ? B[1] : 0.0;
+    case 10: return (fabs(A[0] - B[0]) > A[1]) ? B[1] : 0.0;
+    case 11: return (B[0] > A[0] * A[1]) ? B[1] : 0.0;
+    case 12: return A[0] * B[0] * (A[1] * B[1] + A[2] * B[2] + A[3] * B[3]);
+    case 13: {
+        double d = A[1] * B[1] + A[2] * B[2] + A[3] * B[3];
+        return A[0] * B[0] * d * d;
+    }
+    case 14: return A[0] * B[0] * (A[1] * B[1] + A[2] * B[2]);
+    case 15: {
+        double d = A[1] * B[1] + A[2] * B[2];
+        return A[0] * B[0] * d * d;
+    }
+    case 16:
+        if (A[4] == B[4]) {
+            double d = A[1] * B[1] + A[2] * B[2] + A[3] * B[3];
+            return A[0] * B[0] * d * d;
+        }
+        return 0.0;
+    case 17:
+        if (A[4] != B[4]) {
+            double d = A[1] * B[1] + A[2] * B[2] + A[3] * B[3];
+            return A[0] * B[0] * d * d;
+        }
+        return 0.0;
+    default: return 0.0;
+    }
 }
 
 // ---------------- kernel ----------------
-template <int MODE>
-__global__ void __launch_bounds__(GBP_BLOCK) k_count(const CountArgs a) {
+template <int MODE, int WF>
+__global__ void __launch_bounds__(GBP_BLOCK, 3) k_count(const CountArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     constexpr bool TWO = (MODE == MODE_XYZ || MODE == MODE_SMU);
+    constexpr bool MARK = (MODE == MODE_MARK);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nb0 = a.ax[0].nb, nb1 = TWO ? a.ax[1].nb : 0;
     const int T0 = a.ax[0].T, T1 = TWO ? a.ax[1].T : 0;
     const int copies = a.hist_copies;
-    const SmemLayout L = gbp_smem_layout(MODE, T0, T1, nb0, nb1, a.nsten, copies);
+    const int nw = MARK ? a.nw : 0;
+    const int jwb = MARK ? (WF == 0 ? 8 * nw : 4) : 0;
+    const SmemLayout L = gbp_smem_layout(MODE, T0, T1, nb0, nb1, a.nsten, copies, jwb);
     float4 *s_lut0 = (float4 *)(smem + L.off_lut0);
     float4 *s_lut1 = (float4 *)(smem + L.off_lut1);
     float4 *s_j = (float4 *)(smem + L.off_j);
+    float *s_jw = (float *)(smem + L.off_jw);
+    double *s_jw64 = (double *)(smem + L.off_jw);
+    float4 *s_q = (float4 *)(smem + L.off_q) + warp * GBP_QCAP;
     float4 *s_D = (float4 *)(smem + L.off_D);
     double *s_E0 = (double *)(smem + L.off_E0);
     double *s_E1 = (double *)(smem + L.off_E1);
@@ -270,7 +362,8 @@ __global__ void __launch_bounds__(GBP_BLOCK) k_count(const CountArgs a) {
         s_D[i] = a.stenD[i];
     }
     const int nbin = (nb0 + 1) * (TWO ? nb1 + 1 : 1);
-    const int hist_words = (MODE == MODE_3D) ? GBP_WARPS * (nb0 + 1) * 32 : copies * nbin;
+    const int hist_words = (MODE == MODE_3D) ? GBP_WARPS * (nb0 + 1) * 32
+                         : MARK ? GBP_WARPS * (nb0 + 1) * 32 * 2 : copies * nbin;
     for (int i = tid; i < hist_words; i += GBP_BLOCK) s_hist[i] = 0u;
     if (tid == 0) s_nitems = *a.nitems;
 
@@ -278,10 +371,15 @@ __global__ void __launch_bounds__(GBP_BLOCK) k_count(const CountArgs a) {
     AxisSm A1{s_lut1, s_hi1, s_lo1, s_E1, nb1, TWO ? a.ax[1].S : 0, TWO ? a.ax[1].B : 0,
               TWO ? a.ax[1].vlo : 0.f, TWO ? a.ax[1].vhi : 0.f};
     const int stride2 = nb1 + 1;
-    unsigned *hl = s_hist + warp * (nb0 + 1) * 32 + lane;          // 3-D: lane-private column
+    unsigned *hl = s_hist + warp * (nb0 + 1) * 32 + lane;          // 1-D: lane-private column
+    float *hs = (float *)s_hist + warp * (nb0 + 1) * 32 + lane;     // marked: sums
+    float *hc = hs + GBP_WARPS * (nb0 + 1) * 32;                    // marked: compensations
     unsigned *hw = s_hist + (warp % copies) * nbin;                // shared copy of this warp
     const int n0 = a.n[0], n1 = a.n[1], n2 = a.n[2];
+    const float top0 = a.top0, top1 = a.top1;
+    const unsigned ltmask = (1u << lane) - 1u;
     unsigned long long since_flush = 0, cand = 0;
+    int qn = 0;  // entries in this warp's queue (warp-uniform)
     __syncthreads();
 
     while (true) {
@@ -339,8 +437,19 @@ __global__ void __launch_bounds__(GBP_BLOCK) k_count(const CountArgs a) {
         const int grp = warp / wpg;
         const int within = (warp % wpg) * 32 + lane;
         const bool in_group = grp < G;
-        float4 ui = make_float4(GBP_FAR, GBP_FAR, GBP_FAR, __int_as_float(0));
-        if (in_group && within < icnt) ui = a.pos1[ifirst + within];
+        const bool active_i = in_group && within < icnt;
+        float4 ui = make_float4(GBP_FAR, GBP_FAR, GBP_FAR, __int_as_float(-1));
+        if (active_i) ui = a.pos1[ifirst + within];
+        const int iself = __float_as_int(ui.w);
+        float wi32 = 0.f;
+        double wi64[5] = {0, 0, 0, 0, 0};
+        if (MARK && active_i) {
+            if (WF == 0) {
+                for (int k = 0; k < nw; k++) wi64[k] = a.w64_1[(int64_t)(ifirst + within) * nw + k];
+            } else {
+                wi32 = a.w1[ifirst + within];
+            }
+        }
         cand += (unsigned long long)icnt * (unsigned long long)total;
 
         for (int base = 0; base < total; base += GBP_JCAP) {
@@ -352,61 +461,107 @@ __global__ void __launch_bounds__(GBP_BLOCK) k_count(const CountArgs a) {
                     int mid = (lo + hi + 1) >> 1;
                     if (s_pre[mid] <= g) lo = mid; else hi = mid - 1;
                 }
-                float4 p = a.pos2[s_cstart[lo] + (g - s_pre[lo])];
+                const int j = s_cstart[lo] + (g - s_pre[lo]);
+                float4 p = a.pos2[j];
                 float4 D = s_D[lo];
                 s_j[f] = make_float4(p.x + D.x, p.y + D.y, p.z + D.z, p.w);
+                if (MARK) {
+                    if (WF == 0) {
+                        for (int k = 0; k < nw; k++) s_jw64[f * nw + k] = a.w64_2[(int64_t)j * nw + k];
+                    } else {
+                        s_jw[f] = a.w2[j];
+                    }
+                }
             }
             __syncthreads();
             if (in_group) {
                 const int split = min(max(nselfj - base, 0), len);
-                const unsigned wrest = a.nself ? 2u : 1u;
-                int jj = grp;
-                // own-cell segment: every ordered pair once, except (i, i), whose
-                // FP64 separation is exactly 0 and is added on the host
-                const int iself = __float_as_int(ui.w);
-                if (MODE == MODE_3D) {
-#pragma unroll 4
-                    for (; jj < split; jj += G)
-                        if (__float_as_int(s_j[jj].w) != iself) pair_3d<true>(ui, s_j[jj], 1u, hl, A0, a);
-#pragma unroll 4
-                    for (; jj < len; jj += G) pair_3d<true>(ui, s_j[jj], wrest, hl, A0, a);
-                } else if (MODE == MODE_3DS) {
-#pragma unroll 4
-                    for (; jj < split; jj += G)
-                        if (__float_as_int(s_j[jj].w) != iself) pair_3d<false>(ui, s_j[jj], 1u, hw, A0, a);
-#pragma unroll 4
-                    for (; jj < len; jj += G) pair_3d<false>(ui, s_j[jj], wrest, hw, A0, a);
-                } else if (MODE == MODE_XYZ) {
+                for (int seg = 0; seg < 2; seg++) {
+                    // seg 0: own cell in auto mode (ordered pairs, i == j excluded);
+                    // seg 1: the rest (each unordered pair once in auto mode)
+                    const int jbeg = seg == 0 ? grp : split + ((grp - split) % G + G) % G;
+                    const int jend = seg == 0 ? split : len;
+                    const unsigned symbit = (seg == 1 && a.nself) ? SYM_BIT : 0u;
 #pragma unroll 2
-                    for (; jj < split; jj += G)
-                        if (__float_as_int(s_j[jj].w) != iself) pair_xyz(ui, s_j[jj], 1u, hw, stride2, A0, A1, a);
-#pragma unroll 2
-                    for (; jj < len; jj += G) pair_xyz(ui, s_j[jj], wrest, hw, stride2, A0, A1, a);
-                } else if (MODE == MODE_SMU) {
-#pragma unroll 2
-                    for (; jj < split; jj += G)
-                        if (__float_as_int(s_j[jj].w) != iself) pair_smu(ui, s_j[jj], 1u, hw, stride2, A0, A1, a);
-#pragma unroll 2
-                    for (; jj < len; jj += G) pair_smu(ui, s_j[jj], wrest, hw, stride2, A0, A1, a);
+                    for (int jj = jbeg; jj < jend; jj += G) {
+                        const float4 t = s_j[jj];
+                        const float dx = ui.x - t.x, dy = ui.y - t.y, dz = ui.z - t.z;
+                        float v0, v1 = 0.f;
+                        bool in;
+                        if (MODE == MODE_XYZ) {
+                            v0 = fmaf(dy, dy, dx * dx);
+                            v1 = dz * dz;
+                            in = (v0 <= top0) & (v1 <= top1);
+                        } else if (MODE == MODE_SMU) {
+                            v1 = fmaf(dy, dy, dx * dx);
+                            v0 = fmaf(dz, dz, v1);
+                            in = v0 <= top0;
+                        } else {
+                            v0 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+                            in = v0 <= top0;
+                        }
+                        const bool self = seg == 0 && __float_as_int(t.w) == iself;
+                        if (MARK) {
+                            if (WF == 1) v1 = wi32 * s_jw[jj];
+                            else if (WF == 2) v1 = wi32 + s_jw[jj];
+                            else if (in) v1 = (float)wfunc64(a.wfunc, wi64, s_jw64 + jj * nw);
+                            // (i, i): separation exactly 0, its weight goes straight to that bin
+                            if (self && a.self_bin < nb0) kahan_add(hs, hc, a.self_bin, v1);
+                        }
+                        in = in & !self;
+                        const unsigned m = __ballot_sync(0xffffffffu, in);
+                        if (m) {
+                            if (in) {
+                                const int pos = qn + __popc(m & ltmask);
+                                s_q[pos] = make_float4(v0, v1, ui.w,
+                                                       __uint_as_float(__float_as_uint(t.w) | symbit));
+                            }
+                            qn += __popc(m);
+                            if (qn >= 32) {
+                                // stage 2 on the top 32 entries, all lanes busy
+                                __syncwarp();
+                                const float4 e = s_q[qn - 32 + lane];
+                                if (MODE == MODE_3D) bin_3d<true>(e, hl, A0, a);
+                                else if (MODE == MODE_3DS) bin_3d<false>(e, hw, A0, a);
+                                else if (MODE == MODE_XYZ) bin_xyz(e, hw, stride2, A0, A1, a);
+                                else if (MODE == MODE_SMU) bin_smu(e, hw, stride2, A0, A1, a);
+                                else if (MARK) bin_mark(e, hs, hc, A0, a);
+                                qn -= 32;
+                                __syncwarp();
+                            }
+                        }
+                    }
                 }
             }
             __syncthreads();
         }
-        // a lane adds at most 2 per staged j it visits; flush long before u32 overflow
-        since_flush += 2ull * (unsigned long long)total *
-                       (MODE == MODE_3D ? 1ull : (unsigned long long)(GBP_BLOCK / copies));
-        if (since_flush > (1ull << 31)) {
-            for (int i = tid; i < hist_words; i += GBP_BLOCK) {
-                unsigned v = s_hist[i];
-                if (v) {
-                    int bin = (MODE == MODE_3D) ? (i / 32) % (nb0 + 1) : i % nbin;
-                    atomicAdd(&a.hist[bin], (unsigned long long)v);
-                    s_hist[i] = 0u;
+        // a lane adds at most 2 per queued pair it drains; flush long before u32 overflow
+        if (!MARK) {
+            since_flush += 2ull * (unsigned long long)total *
+                           (MODE == MODE_3D ? 1ull : (unsigned long long)(GBP_BLOCK / copies)) + 64ull;
+            if (since_flush > (1ull << 31)) {
+                for (int i = tid; i < hist_words; i += GBP_BLOCK) {
+                    unsigned v = s_hist[i];
+                    if (v) {
+                        int bin = (MODE == MODE_3D) ? (i / 32) % (nb0 + 1) : i % nbin;
+                        atomicAdd(&a.hist[bin], (unsigned long long)v);
+                        s_hist[i] = 0u;
+                    }
                 }
+                since_flush = 0;
+                __syncthreads();
             }
-            since_flush = 0;
-            __syncthreads();
         }
+    }
+    // drain what is left in this warp's queue (fewer than 32 entries)
+    __syncwarp();
+    if (lane < qn) {
+        const float4 e = s_q[lane];
+        if (MODE == MODE_3D) bin_3d<true>(e, hl, A0, a);
+        else if (MODE == MODE_3DS) bin_3d<false>(e, hw, A0, a);
+        else if (MODE == MODE_XYZ) bin_xyz(e, hw, stride2, A0, A1, a);
+        else if (MODE == MODE_SMU) bin_smu(e, hw, stride2, A0, A1, a);
+        else if (MARK) bin_mark(e, hs, hc, A0, a);
     }
     // final flush: reduce the copies and add to the global histogram
     __syncthreads();
@@ -418,6 +573,19 @@ __global__ void __launch_bounds__(GBP_BLOCK) k_count(const CountArgs a) {
             for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
             if (lane == 0 && s) atomicAdd(&a.hist[b], s);
         }
+    } else if (MARK) {
+        const float *S = (const float *)s_hist;
+        const float *C = S + GBP_WARPS * (nb0 + 1) * 32;
+        for (int b = warp; b < nb0; b += GBP_WARPS) {
+            double s = 0.0;
+            for (int w = 0; w < GBP_WARPS; w++) {
+                int idx = (w * (nb0 + 1) + b) * 32 + lane;
+                s += (double)S[idx] - (double)C[idx];
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+            if (lane == 0 && s != 0.0) atomicAdd(&a.histd[b], s);
+        }
     } else {
         for (int b = tid; b < nbin; b += GBP_BLOCK) {
             unsigned long long s = 0;
@@ -428,60 +596,52 @@ __global__ void __launch_bounds__(GBP_BLOCK) k_count(const CountArgs a) {
     if (tid == 0 && cand) atomicAdd(a.nrecheck + 1, cand);
 }
 
-template <int MODE>
-static cudaError_t set_smem_attr(size_t smem) {
-    return cudaFuncSetAttribute(k_count<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)smem);
-}
-
-cudaError_t gbp_launch_count(int mode, const CountArgs &a, int grid, size_t smem, cudaStream_t st) {
-    cudaError_t e = cudaSuccess;
-    switch (mode) {
-    case MODE_3D:
-        e = set_smem_attr<MODE_3D>(smem);
-        if (e == cudaSuccess) k_count<MODE_3D><<<grid, GBP_BLOCK, smem, st>>>(a);
-        break;
-    case MODE_XYZ:
-        e = set_smem_attr<MODE_XYZ>(smem);
-        if (e == cudaSuccess) k_count<MODE_XYZ><<<grid, GBP_BLOCK, smem, st>>>(a);
-        break;
-    case MODE_SMU:
-        e = set_smem_attr<MODE_SMU>(smem);
-        if (e == cudaSuccess) k_count<MODE_SMU><<<grid, GBP_BLOCK, smem, st>>>(a);
-        break;
-    case MODE_3DS:
-        e = set_smem_attr<MODE_3DS>(smem);
-        if (e == cudaSuccess) k_count<MODE_3DS><<<grid, GBP_BLOCK, smem, st>>>(a);
-        break;
-    default:
-        return cudaErrorInvalidValue;
-    }
+template <int MODE, int WF>
+static cudaError_t launch_t(const CountArgs &a, int grid, size_t smem, cudaStream_t st) {
+    cudaError_t e = cudaFuncSetAttribute(k_count<MODE, WF>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
+    k_count<MODE, WF><<<grid, GBP_BLOCK, smem, st>>>(a);
     return cudaGetLastError();
 }
 
-int gbp_count_occupancy(int mode, size_t smem) {
+template <int MODE, int WF>
+static int occ_t(size_t smem) {
     int nblk = 0;
-    cudaError_t e = cudaSuccess;
-    switch (mode) {
-    case MODE_3D:
-        set_smem_attr<MODE_3D>(smem);
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nblk, k_count<MODE_3D>, GBP_BLOCK, smem);
-        break;
-    case MODE_XYZ:
-        set_smem_attr<MODE_XYZ>(smem);
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nblk, k_count<MODE_XYZ>, GBP_BLOCK, smem);
-        break;
-    case MODE_SMU:
-        set_smem_attr<MODE_SMU>(smem);
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nblk, k_count<MODE_SMU>, GBP_BLOCK, smem);
-        break;
-    case MODE_3DS:
-        set_smem_attr<MODE_3DS>(smem);
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nblk, k_count<MODE_3DS>, GBP_BLOCK, smem);
-        break;
-    default:
+    if (cudaFuncSetAttribute(k_count<MODE, WF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem) != cudaSuccess)
         return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nblk, k_count<MODE, WF>, GBP_BLOCK, smem) !=
+        cudaSuccess)
+        return 0;
+    return nblk;
+}
+
+cudaError_t gbp_launch_count(int mode, int wf, const CountArgs &a, int grid, size_t smem,
+                             cudaStream_t st) {
+    switch (mode) {
+    case MODE_3D: return launch_t<MODE_3D, 1>(a, grid, smem, st);
+    case MODE_3DS: return launch_t<MODE_3DS, 1>(a, grid, smem, st);
+    case MODE_XYZ: return launch_t<MODE_XYZ, 1>(a, grid, smem, st);
+    case MODE_SMU: return launch_t<MODE_SMU, 1>(a, grid, smem, st);
+    case MODE_MARK:
+        if (wf == 1) return launch_t<MODE_MARK, 1>(a, grid, smem, st);
+        if (wf == 2) return launch_t<MODE_MARK, 2>(a, grid, smem, st);
+        return launch_t<MODE_MARK, 0>(a, grid, smem, st);
+    default: return cudaErrorInvalidValue;
     }
-    return e == cudaSuccess ? nblk : 0;
+}
+
+int gbp_count_occupancy(int mode, int wf, size_t smem) {
+    switch (mode) {
+    case MODE_3D: return occ_t<MODE_3D, 1>(smem);
+    case MODE_3DS: return occ_t<MODE_3DS, 1>(smem);
+    case MODE_XYZ: return occ_t<MODE_XYZ, 1>(smem);
+    case MODE_SMU: return occ_t<MODE_SMU, 1>(smem);
+    case MODE_MARK:
+        if (wf == 1) return occ_t<MODE_MARK, 1>(smem);
+        if (wf == 2) return occ_t<MODE_MARK, 2>(smem);
+        return occ_t<MODE_MARK, 0>(smem);
+    default: return 0;
+    }
 }

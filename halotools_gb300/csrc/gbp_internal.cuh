@@ -16,7 +16,8 @@
 #define GBP_WARPS (GBP_BLOCK / 32)
 #define GBP_TI 256          // max i-points per work item (one per thread)
 #define GBP_JCAP 1024       // staged j-points per chunk
-#define GBP_LUT_MAX 2048    // float-bit lookup slots per axis
+#define GBP_LUT_MAX 1024    // float-bit lookup slots per axis
+#define GBP_QCAP 64         // per-warp queue of in-range pairs (entries)
 #define GBP_NB_MAX 1024     // edges per axis
 #define GBP_NB_LANE 64      // 1-D histograms up to this size use lane-private bins
 #define GBP_SMAX 512        // stencil cells
@@ -62,31 +63,37 @@ struct CountArgs {
     int hist_copies;        // shared histogram copies (2-D and wide 1-D): 8 = one per warp, or 1
     unsigned long long *hist;   // global differential histogram(s)
     unsigned long long *nrecheck;
+    float top0, top1;       // above these a pair is out of range on that axis
     // marked / adjoint
     const float *w1;        // sorted weights, (N1, nw) FP32
     const float *w2;
-    const double *w64_1;    // sorted FP64 weights (marking-function conditions)
+    const double *w64_1;    // sorted FP64 weights (marking functions evaluated in FP64)
     const double *w64_2;
     int nw;
     int wfunc;
+    int self_bin;           // bin of separation 0 (marked auto mode adds f(w_i, w_i) there)
     double *histd;          // FP64 weighted histogram (marked)
 };
 
 // Shared-memory layout of the count kernel, identical on host and device.
+// jw: bytes of staged weights per j-point (marked mode), copies: shared
+// histogram copies (2-D and wide 1-D modes).
 struct SmemLayout {
-    int off_lut0, off_lut1, off_j, off_D, off_E0, off_E1, off_hi0, off_lo0, off_hi1, off_lo1,
-        off_off, off_cstart, off_pre, off_hist, total;
+    int off_lut0, off_lut1, off_j, off_jw, off_q, off_D, off_E0, off_E1, off_hi0, off_lo0,
+        off_hi1, off_lo1, off_off, off_cstart, off_pre, off_hist, total;
 };
 
 __host__ __device__ inline int gbp_align(int x, int a) { return (x + a - 1) / a * a; }
 
 __host__ __device__ inline SmemLayout gbp_smem_layout(int mode, int T0, int T1, int nb0, int nb1,
-                                                      int nsten, int copies) {
+                                                      int nsten, int copies, int jw) {
     SmemLayout L;
     int o = 0;
     L.off_lut0 = o; o += T0 * 16;
     L.off_lut1 = o; o += T1 * 16;
     L.off_j = o; o += GBP_JCAP * 16;
+    L.off_jw = o; o += gbp_align(GBP_JCAP * jw, 16);
+    L.off_q = o; o += GBP_WARPS * GBP_QCAP * 16;
     L.off_D = o; o += nsten * 16;
     L.off_E0 = o; o += gbp_align(nb0 * 8, 16);
     L.off_E1 = o; o += gbp_align(nb1 * 8, 16);
@@ -136,7 +143,9 @@ cudaError_t gbp_scan_exclusive(const int *d_in, int *d_out, int64_t n, int *d_tm
                                cudaStream_t st, int *launches);
 size_t gbp_scan_tmp_ints(int64_t n);
 
-cudaError_t gbp_launch_count(int mode, const CountArgs &a, int grid, size_t smem, cudaStream_t st);
-int gbp_count_occupancy(int mode, size_t smem);
+// mode: MODE_*; wf: marking-function template (1 product, 2 sum, 0 any id in FP64)
+cudaError_t gbp_launch_count(int mode, int wf, const CountArgs &a, int grid, size_t smem,
+                             cudaStream_t st);
+int gbp_count_occupancy(int mode, int wf, size_t smem);
 cudaError_t gbp_count_set_smem(size_t smem);
 cudaError_t gbp_run_ffma_probe(int nsm, cudaStream_t st, float *ms_out, double *flops_out);

@@ -205,11 +205,13 @@ extern "C" int gbp_npairs_3d_static(const double *xyz, int64_t n, const double *
     a.hist_copies = 1;
     a.hist = reinterpret_cast<unsigned long long *>(W + O_HIST);
     a.nrecheck = misc + 2;
-    SmemLayout L = gbp_smem_layout(MODE_3D, li.T, 0, nbins, 0, g.nsten, 1);
+    a.top0 = std::min(hi[nbins - 1], 1.0e30f);
+    a.self_bin = self_bin;
+    SmemLayout L = gbp_smem_layout(MODE_3D, li.T, 0, nbins, 0, g.nsten, 1, 0);
     size_t smem = (size_t)L.total;
-    int occ = gbp_count_occupancy(MODE_3D, smem);
+    int occ = gbp_count_occupancy(MODE_3D, 1, smem);
     if (occ <= 0) return GBP_ERR_INVALID;
-    e = gbp_launch_count(MODE_3D, a, nsm * occ, smem, st);
+    e = gbp_launch_count(MODE_3D, 1, a, nsm * occ, smem, st);
     if (e != cudaSuccess) return GBP_ERR_CUDA;
     k_static_finalize<<<1, 32, 0, st>>>(a.hist, misc, nbins, self_bin, (long long)n,
                                         reinterpret_cast<long long *>(counts));

@@ -176,3 +176,29 @@ def test_out_of_box_and_nonfinite_positions_rejected(gpu):
         gpu.npairs_3d(bad, s, [0.1, 0.2])
     # the plan stays usable after a rejected call
     assert gpu.npairs_3d(s, s, [0.1, 0.2], period=1)[-1] >= 500
+
+
+MARKED_CASES = G.names("marked")
+
+
+@pytest.mark.parametrize("name", MARKED_CASES)
+def test_marked_golden(gpu, name):
+    # FP32 compensated sums: within 1e-6 relative of the reference's FP64 sums
+    c = G.load(name)
+    got = G.call(gpu, c)
+    assert got.dtype == np.float64
+    np.testing.assert_allclose(got, c["out"], rtol=1e-6, atol=1e-9)
+
+
+def test_marked_product_clustered_matches_oracle(gpu):
+    rng = np.random.default_rng(21)
+    L = 400.0
+    s = clustered(rng, 60000, L, 3000)
+    w = rng.lognormal(0.0, 0.5, len(s))
+    rb = np.logspace(np.log10(0.5), np.log10(40), 30)
+    want = oracle.marked_npairs_3d(s, s, rb, 1, period=L, weights1=w, weights2=w, num_threads=8)
+    got = gpu.marked_npairs_3d(s, s, rb, 1, period=L, weights1=w, weights2=w)
+    np.testing.assert_allclose(got, want, rtol=1e-6)
+    # the unweighted count with unit marks is exact
+    ones = gpu.marked_npairs_3d(s, s, rb, 1, period=L)
+    assert np.array_equal(ones, gpu.npairs_3d(s, s, rb, period=L).astype(np.float64))
