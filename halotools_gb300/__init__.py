@@ -10,10 +10,11 @@ halotools' estimators bound at import time, so ``tpcf``, ``wp``,
 from .pair_counters import (HalotoolsError, marked_npairs_3d, npairs_3d, npairs_s_mu,
                             npairs_xy_z)
 from ._native import GBPairsError, GBPairsUnavailable, Plan, default_plan
+from .batched import BatchedCounter, npairs_3d_batched
 
 __all__ = ("npairs_3d", "npairs_xy_z", "npairs_s_mu", "marked_npairs_3d", "HalotoolsError",
            "GBPairsError", "GBPairsUnavailable", "Plan", "default_plan",
-           "install_into_halotools")
+           "npairs_3d_batched", "BatchedCounter", "install_into_halotools")
 
 # module attribute -> our function, for every place halotools binds a counter
 _BINDINGS = (

@@ -27,7 +27,8 @@ EXPORTED = (
     "gbp_plan_create", "gbp_plan_destroy", "gbp_plan_set_stream", "gbp_plan_set_reach",
     "gbp_plan_last_error", "gbp_plan_stats", "gbp_npairs_3d", "gbp_npairs_xy_z",
     "gbp_npairs_s_mu", "gbp_marked_npairs_3d", "gbp_measure_fp32_peak",
-    "gbp_npairs_3d_static",
+    "gbp_npairs_3d_static", "gbp_batched_npairs_3d", "gbp_plan_set_graph", "gbp_plan_set_autotune",
+    "gbp_weighted_adjoint_3d", "gbp_zheng07_weights", "gbp_zheng07_vjp",
 )
 
 
@@ -108,6 +109,12 @@ def load(build_if_missing: bool = True):
                                            i32, i32, pd]
         L.gbp_measure_fp32_peak.argtypes = [vp, pd]
         L.gbp_npairs_3d_static.argtypes = [vp, i64, pd, i32, pd, i32, vp, vp]
+        L.gbp_batched_npairs_3d.argtypes = [vp, vp, i32, pi64, i32, pd, i32, pd, i32, i32, pi64]
+        L.gbp_plan_set_graph.argtypes = [vp, ctypes.c_int]
+        L.gbp_weighted_adjoint_3d.argtypes = [vp, vp, i64, vp, pd, i32, pd, i32, i32, pd, vp]
+        L.gbp_zheng07_weights.argtypes = [vp, vp, i64, pd, i32, vp]
+        L.gbp_zheng07_vjp.argtypes = [vp, vp, i64, pd, vp, i32, pd]
+        L.gbp_plan_set_autotune.argtypes = [vp, ctypes.c_int]
         _lib = L
         return L
 
@@ -160,6 +167,12 @@ class Plan:
         self.check(self.lib.gbp_measure_fp32_peak(self.handle, ctypes.byref(v)))
         return v.value
 
+    def set_graph(self, enable: bool):
+        self.check(self.lib.gbp_plan_set_graph(self.handle, int(bool(enable))))
+
+    def set_autotune(self, enable: bool):
+        self.check(self.lib.gbp_plan_set_autotune(self.handle, int(bool(enable))))
+
     def set_reach(self, reach: int):
         self.check(self.lib.gbp_plan_set_reach(self.handle, int(reach)))
 
@@ -179,6 +192,10 @@ def default_plan(device: int = 0) -> Plan:
 
 def dptr(a: np.ndarray):
     return ctypes.c_void_p(a.ctypes.data)
+
+
+def dptr_int(addr: int):
+    return ctypes.c_void_p(int(addr))
 
 
 def pd(a: np.ndarray):

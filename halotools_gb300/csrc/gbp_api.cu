@@ -39,6 +39,10 @@ struct gbp_plan {
     void *pinned = nullptr;
     size_t pinned_bytes = 0;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    bool graph_mode = false;          // capture each call into a CUDA graph and replay it
+    bool autotune = false;            // time the feasible reaches on a new workload shape
+    std::vector<std::pair<std::string, int>> tuned;  // workload signature -> best reach
+    cudaGraphExec_t gexec = nullptr;  // reused (updated in place) across calls
     gbp_stats stats;
     std::string err;
 };
@@ -136,6 +140,11 @@ struct SampleDev {
 struct Call {
     int mode;
     int wf = 1;  // marking-function template for MODE_MARK
+    int nmocks = 1;                  // batched auto-correlations of mocks (sample 1 only)
+    std::vector<int64_t> offsets;    // nmocks+1 point offsets when nmocks > 1
+    int xyz_f32 = 0;                 // sample 1 positions are float32
+    std::vector<float> gt;           // adjoint: suffix sums of the upstream gradient (nb+1)
+    double *grad_out = nullptr;      // adjoint: dL/dw, caller's order, in `mem` memory
     const double *xyz1, *xyz2;
     int64_t n1, n2;
     bool autocorr;
@@ -158,13 +167,18 @@ void add_self_pairs(const Call &c, std::vector<unsigned long long> &h) {
     if (!c.autocorr) return;
     int a = host_bin(c.ax[0].nb, c.ax[0].E.data(), 0.0);
     if (a >= c.ax[0].nb) return;
-    if (c.naxes == 1) {
-        h[a] += (unsigned long long)c.n1;
-        return;
+    size_t idx = (size_t)a;
+    size_t nh = (size_t)(c.ax[0].nb + 1);
+    if (c.naxes > 1) {
+        int b = host_bin(c.ax[1].nb, c.ax[1].E.data(), 0.0);
+        if (b >= c.ax[1].nb) return;
+        idx = (size_t)a * (c.ax[1].nb + 1) + b;
+        nh *= (size_t)(c.ax[1].nb + 1);
     }
-    int b = host_bin(c.ax[1].nb, c.ax[1].E.data(), 0.0);
-    if (b >= c.ax[1].nb) return;
-    h[(size_t)a * (c.ax[1].nb + 1) + b] += (unsigned long long)c.n1;
+    for (int m = 0; m < c.nmocks; m++) {
+        int64_t n = c.nmocks > 1 ? c.offsets[m + 1] - c.offsets[m] : c.n1;
+        h[m * nh + idx] += (unsigned long long)n;
+    }
 }
 
 // Runs the pipeline; fills hist_host with the differential histogram
@@ -175,6 +189,8 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
     cudaStream_t st = plan->stream;
     std::memset(&plan->stats, 0, sizeof(plan->stats));
     const int64_t ncells = c.g.ncells;
+    const int nm = c.nmocks;
+    const int64_t nkeys = ncells * nm;  // cell keys: mock * ncells + cell
     const int nb0 = c.ax[0].nb, nb1 = c.naxes > 1 ? c.ax[1].nb : 0;
     const int T0 = c.ax[0].T, T1 = c.naxes > 1 ? c.ax[1].T : 0;
     const int nsten = c.g.nsten;
@@ -191,8 +207,8 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
         if (c.mem == GBP_MEM_HOST) o_xyz[s] = cv.take<double>(3 * n);
         o_cellid[s] = cv.take<int>(n);
         o_rank[s] = cv.take<int>(n);
-        o_count[s] = cv.take<int>((size_t)ncells + 1);
-        o_start[s] = cv.take<int>((size_t)ncells + 1);
+        o_count[s] = cv.take<int>((size_t)nkeys + 1);
+        o_start[s] = cv.take<int>((size_t)nkeys + 1);
         o_orig[s] = cv.take<int>(n);
         o_pos32[s] = cv.take<float4>(2 * n);
         o_pos64[s] = cv.take<double>(3 * n);
@@ -202,18 +218,22 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
             o_w64[s] = cv.take<double>(n * c.nw);
         }
     }
-    size_t scan_ints = gbp_scan_tmp_ints(ncells + 1);
+    size_t scan_ints = gbp_scan_tmp_ints(nkeys + 1);
     size_t o_scan = cv.take<int>(scan_ints);
-    size_t max_items = (size_t)ncells + (size_t)(c.n1 / GBP_TI) + 16;
+    size_t max_items = (size_t)nkeys + (size_t)(c.n1 / GBP_TI) + 16;
     size_t o_items = cv.take<int4>(max_items);
-    size_t o_itmp = cv.take<int>(2 * ((size_t)ncells + 2));
+    size_t o_itmp = cv.take<int>(2 * ((size_t)nkeys + 2));
+    size_t o_offs = cv.take<int64_t>((size_t)nm + 1);
+    const bool adj = c.mode == MODE_ADJ;
+    size_t o_gt = cv.take<float>((size_t)nb0 + 1);
+    size_t o_grad = cv.take<double>(adj && c.mem == GBP_MEM_HOST ? (size_t)c.n1 : 1);
     size_t o_lut0 = cv.take<float4>(T0), o_lut1 = cv.take<float4>(std::max(T1, 1));
     size_t o_E0 = cv.take<double>(nb0), o_E1 = cv.take<double>(std::max(nb1, 1));
     size_t o_hi0 = cv.take<float>(nb0), o_lo0 = cv.take<float>(nb0);
     size_t o_hi1 = cv.take<float>(std::max(nb1, 1)), o_lo1 = cv.take<float>(std::max(nb1, 1));
     size_t o_sten = cv.take<int>(nsten), o_stenD = cv.take<float4>(nsten);
-    size_t o_hist = cv.take<unsigned long long>(nhist);
-    size_t o_histd = cv.take<double>(nhist);
+    size_t o_hist = cv.take<unsigned long long>(nhist * nm);
+    size_t o_histd = cv.take<double>(nhist * nm);
     size_t o_misc = cv.take<unsigned long long>(8);  // counter, nitems, err, recheck, cand
     size_t total = cv.take<char>(0) + 256;
     int rc = ensure_work(plan, total);
@@ -227,9 +247,11 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
     size_t h_hi0 = hv.take<float>(nb0), h_lo0 = hv.take<float>(nb0);
     size_t h_hi1 = hv.take<float>(std::max(nb1, 1)), h_lo1 = hv.take<float>(std::max(nb1, 1));
     size_t h_sten = hv.take<int>(nsten), h_stenD = hv.take<float4>(nsten);
+    size_t h_offs = hv.take<int64_t>((size_t)nm + 1);
+    size_t h_gt = hv.take<float>((size_t)nb0 + 1);
     size_t h_end = hv.take<char>(0);
-    size_t h_hist = hv.take<unsigned long long>(nhist);
-    size_t h_histd = hv.take<double>(nhist);
+    size_t h_hist = hv.take<unsigned long long>(nhist * nm);
+    size_t h_histd = hv.take<double>(nhist * nm);
     size_t h_misc = hv.take<unsigned long long>(8);
     rc = ensure_pinned(plan, hv.take<char>(0) + 256);
     if (rc) return rc;
@@ -246,169 +268,233 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
     }
     std::memcpy(at<char>(H, h_sten), c.g.sten, sizeof(int) * nsten);
     std::memcpy(at<char>(H, h_stenD), c.g.stenD, sizeof(float4) * nsten);
+    if (nm > 1) std::memcpy(at<char>(H, h_offs), c.offsets.data(), sizeof(int64_t) * (nm + 1));
+    if (adj) std::memcpy(at<char>(H, h_gt), c.gt.data(), sizeof(float) * (nb0 + 1));
 
-    CK(cudaEventRecord(plan->ev[0], st));
-    int64_t h2d = 0, d2h = 0;
-    h2d += (int64_t)(sizeof(float4) * (T0 + T1) + sizeof(double) * (nb0 + nb1) +
-                     sizeof(float) * 2 * (nb0 + nb1) + (sizeof(int) + sizeof(float4)) * nsten);
-    CK(cudaMemcpyAsync(at<char>(W, o_lut0), at<char>(H, h_lut0), sizeof(float4) * T0, cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(at<char>(W, o_E0), at<char>(H, h_E0), sizeof(double) * nb0, cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(at<char>(W, o_hi0), at<char>(H, h_hi0), sizeof(float) * nb0, cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(at<char>(W, o_lo0), at<char>(H, h_lo0), sizeof(float) * nb0, cudaMemcpyHostToDevice, st));
-    if (c.naxes > 1) {
-        CK(cudaMemcpyAsync(at<char>(W, o_lut1), at<char>(H, h_lut1), sizeof(float4) * T1, cudaMemcpyHostToDevice, st));
-        CK(cudaMemcpyAsync(at<char>(W, o_E1), at<char>(H, h_E1), sizeof(double) * nb1, cudaMemcpyHostToDevice, st));
-        CK(cudaMemcpyAsync(at<char>(W, o_hi1), at<char>(H, h_hi1), sizeof(float) * nb1, cudaMemcpyHostToDevice, st));
-        CK(cudaMemcpyAsync(at<char>(W, o_lo1), at<char>(H, h_lo1), sizeof(float) * nb1, cudaMemcpyHostToDevice, st));
-    }
-    CK(cudaMemcpyAsync(at<char>(W, o_sten), at<char>(H, h_sten), sizeof(int) * nsten, cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(at<char>(W, o_stenD), at<char>(H, h_stenD), sizeof(float4) * nsten, cudaMemcpyHostToDevice, st));
-    (void)h_end;
-
-    // ---- positions and weights ----
-    SampleDev sd[2];
-    for (int s = 0; s < nsamp; s++) {
-        const double *src = s == 0 ? c.xyz1 : c.xyz2;
-        const double *wsrc = s == 0 ? c.w1 : c.w2;
-        size_t n = (size_t)ns[s];
-        if (c.mem == GBP_MEM_HOST) {
-            sd[s].xyz = at<double>(W, o_xyz[s]);
-            if (n) CK(cudaMemcpyAsync((void *)sd[s].xyz, src, 3 * n * sizeof(double), cudaMemcpyHostToDevice, st));
-            h2d += (int64_t)(3 * n * sizeof(double));
-        } else {
-            sd[s].xyz = src;
-        }
-        sd[s].cellid = at<int>(W, o_cellid[s]);
-        sd[s].rank = at<int>(W, o_rank[s]);
-        sd[s].count = at<int>(W, o_count[s]);
-        sd[s].start = at<int>(W, o_start[s]);
-        sd[s].orig = at<int>(W, o_orig[s]);
-        sd[s].pos32 = at<float4>(W, o_pos32[s]);
-        sd[s].pos64 = at<double>(W, o_pos64[s]);
-        if (c.nw > 0) {
-            const double *wd = wsrc;
-            if (c.mem == GBP_MEM_HOST) {
-                wd = at<double>(W, o_win[s]);
-                if (n) CK(cudaMemcpyAsync((void *)wd, wsrc, n * c.nw * sizeof(double), cudaMemcpyHostToDevice, st));
-                h2d += (int64_t)(n * c.nw * sizeof(double));
-            }
-            sd[s].w32 = at<float>(W, o_w32[s]);
-            sd[s].w64 = at<double>(W, o_w64[s]);
-            wsrc = wd;
-        }
-        if (s == 0) c.w1 = wsrc; else c.w2 = wsrc;
-    }
-    unsigned long long *misc = at<unsigned long long>(W, o_misc);
-    CK(cudaMemsetAsync(misc, 0, 8 * sizeof(unsigned long long), st));
-    int *d_counter = reinterpret_cast<int *>(misc);
-    int *d_nitems = reinterpret_cast<int *>(misc) + 1;
-    int *d_err = reinterpret_cast<int *>(misc) + 2;
-    unsigned long long *d_stat = misc + 2;  // [0] rechecks, [1] candidate pairs
-
-    MeshDev md;
-    for (int d = 0; d < 3; d++) {
-        md.n[d] = c.g.n[d];
-        md.c[d] = c.g.c[d];
-        md.L[d] = c.g.L[d];
-    }
-    md.ncells = ncells;
     int launches = 0;
-    for (int s = 0; s < nsamp; s++) {
-        const double *wsrc = s == 0 ? c.w1 : c.w2;
-        cudaError_t e = gbp_build_cells(sd[s].xyz, ns[s], md, sd[s].cellid, sd[s].rank, sd[s].count,
-                                        sd[s].start, at<int>(W, o_scan), sd[s].pos32, sd[s].pos64,
-                                        sd[s].orig, c.nw > 0 ? wsrc : nullptr, c.nw, sd[s].w32,
-                                        sd[s].w64, d_err, st, &launches);
-        CK(e);
-    }
-    CK(gbp_build_items(sd[0].start, ncells, at<int4>(W, o_items), d_nitems, at<int>(W, o_itmp),
-                       at<int>(W, o_scan), st, &launches));
-    CK(cudaMemsetAsync(at<char>(W, o_hist), 0, nhist * sizeof(unsigned long long), st));
-    CK(cudaMemsetAsync(at<char>(W, o_histd), 0, nhist * sizeof(double), st));
-    CK(cudaEventRecord(plan->ev[1], st));
-
-    const SampleDev &s2 = c.autocorr ? sd[0] : sd[1];
-    CountArgs a;
-    std::memset(&a, 0, sizeof(a));
-    a.pos1 = sd[0].pos32;
-    a.pos2 = s2.pos32;
-    a.x64_1 = sd[0].pos64;
-    a.x64_2 = s2.pos64;
-    a.start2 = s2.start;
-    a.items = at<int4>(W, o_items);
-    a.nitems = d_nitems;
-    a.counter = d_counter;
-    a.sten = at<int>(W, o_sten);
-    a.stenD = at<float4>(W, o_stenD);
-    a.nsten = nsten;
-    a.nself = c.g.nself;
-    for (int d = 0; d < 3; d++) {
-        a.n[d] = c.g.n[d];
-        a.L[d] = c.g.L[d];
-    }
-    a.pbc = c.g.pbc;
-    for (int x = 0; x < c.naxes; x++) {
-        AxisDev &ad = a.ax[x];
-        const AxisHost &ah = c.ax[x];
-        ad.lut = at<float4>(W, x == 0 ? o_lut0 : o_lut1);
-        ad.E = at<double>(W, x == 0 ? o_E0 : o_E1);
-        ad.hi = at<float>(W, x == 0 ? o_hi0 : o_hi1);
-        ad.lo = at<float>(W, x == 0 ? o_lo0 : o_lo1);
-        ad.nb = ah.nb;
-        ad.T = ah.T;
-        ad.S = ah.S;
-        ad.B = ah.B;
-        ad.vlo = ah.vlo;
-        ad.vhi = ah.vhi;
-    }
-    a.hist_stride = c.naxes > 1 ? nb1 + 1 : 1;
-    a.hist = at<unsigned long long>(W, o_hist);
-    a.histd = at<double>(W, o_histd);
-    a.nrecheck = d_stat;
-    a.w1 = sd[0].w32;
-    a.w2 = s2.w32;
-    a.w64_1 = sd[0].w64;
-    a.w64_2 = s2.w64;
-    a.nw = c.nw;
-    a.wfunc = c.wfunc;
-
-    a.top0 = std::min(c.ax[0].hi[nb0 - 1], 1.0e30f);
-    a.top1 = c.naxes > 1 ? std::min(c.ax[1].hi[nb1 - 1], 1.0e30f) : 0.f;
-    a.self_bin = host_bin(nb0, c.ax[0].E.data(), 0.0);
-    const int jwb = c.mode == MODE_MARK ? (c.wf == 0 ? 8 * c.nw : 4) : 0;
-    // shared histogram copies (2-D and wide 1-D): as many as keep the CTA
-    // within ~72 KB of shared memory (3 CTAs per SM), at least one
-    int copies = 1;
-    if (c.mode != MODE_3D && c.mode != MODE_MARK) {
-        for (int cp = GBP_WARPS; cp >= 1; cp /= 2) {
-            copies = cp;
-            if (gbp_smem_layout(c.mode, T0, T1, nb0, nb1, nsten, cp, jwb).total <= (72 << 10)) break;
+    int64_t h2d = 0, d2h = 0;
+    const bool graph = plan->graph_mode;
+    // event records inside a capture must be external to be timed on replay
+    auto rec = [&](cudaEvent_t ev) {
+        return graph ? cudaEventRecordWithFlags(ev, st, cudaEventRecordExternal)
+                     : cudaEventRecord(ev, st);
+    };
+    // every stream operation of the call, from the table uploads to the result
+    // copies: run directly, or captured into one CUDA graph and replayed
+    auto enqueue = [&]() -> int {
+        CK(rec(plan->ev[0]));
+        h2d += (int64_t)(sizeof(float4) * (T0 + T1) + sizeof(double) * (nb0 + nb1) +
+                         sizeof(float) * 2 * (nb0 + nb1) + (sizeof(int) + sizeof(float4)) * nsten);
+        CK(cudaMemcpyAsync(at<char>(W, o_lut0), at<char>(H, h_lut0), sizeof(float4) * T0, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(at<char>(W, o_E0), at<char>(H, h_E0), sizeof(double) * nb0, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(at<char>(W, o_hi0), at<char>(H, h_hi0), sizeof(float) * nb0, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(at<char>(W, o_lo0), at<char>(H, h_lo0), sizeof(float) * nb0, cudaMemcpyHostToDevice, st));
+        if (c.naxes > 1) {
+            CK(cudaMemcpyAsync(at<char>(W, o_lut1), at<char>(H, h_lut1), sizeof(float4) * T1, cudaMemcpyHostToDevice, st));
+            CK(cudaMemcpyAsync(at<char>(W, o_E1), at<char>(H, h_E1), sizeof(double) * nb1, cudaMemcpyHostToDevice, st));
+            CK(cudaMemcpyAsync(at<char>(W, o_hi1), at<char>(H, h_hi1), sizeof(float) * nb1, cudaMemcpyHostToDevice, st));
+            CK(cudaMemcpyAsync(at<char>(W, o_lo1), at<char>(H, h_lo1), sizeof(float) * nb1, cudaMemcpyHostToDevice, st));
         }
+        CK(cudaMemcpyAsync(at<char>(W, o_sten), at<char>(H, h_sten), sizeof(int) * nsten, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(at<char>(W, o_stenD), at<char>(H, h_stenD), sizeof(float4) * nsten, cudaMemcpyHostToDevice, st));
+        if (adj) {
+            CK(cudaMemcpyAsync(at<char>(W, o_gt), at<char>(H, h_gt), sizeof(float) * (nb0 + 1), cudaMemcpyHostToDevice, st));
+            h2d += (int64_t)(sizeof(float) * (nb0 + 1));
+        }
+        if (nm > 1) {
+            CK(cudaMemcpyAsync(at<char>(W, o_offs), at<char>(H, h_offs), sizeof(int64_t) * (nm + 1), cudaMemcpyHostToDevice, st));
+            h2d += (int64_t)(sizeof(int64_t) * (nm + 1));
+        }
+        (void)h_end;
+
+        // ---- positions and weights ----
+        SampleDev sd[2];
+        for (int s = 0; s < nsamp; s++) {
+            const double *src = s == 0 ? c.xyz1 : c.xyz2;
+            const double *wsrc = s == 0 ? c.w1 : c.w2;
+            size_t n = (size_t)ns[s];
+            const size_t esz = (s == 0 && c.xyz_f32) ? sizeof(float) : sizeof(double);
+            if (c.mem == GBP_MEM_HOST) {
+                sd[s].xyz = at<double>(W, o_xyz[s]);
+                if (n) CK(cudaMemcpyAsync((void *)sd[s].xyz, src, 3 * n * esz, cudaMemcpyHostToDevice, st));
+                h2d += (int64_t)(3 * n * esz);
+            } else {
+                sd[s].xyz = src;
+            }
+            sd[s].cellid = at<int>(W, o_cellid[s]);
+            sd[s].rank = at<int>(W, o_rank[s]);
+            sd[s].count = at<int>(W, o_count[s]);
+            sd[s].start = at<int>(W, o_start[s]);
+            sd[s].orig = at<int>(W, o_orig[s]);
+            sd[s].pos32 = at<float4>(W, o_pos32[s]);
+            sd[s].pos64 = at<double>(W, o_pos64[s]);
+            if (c.nw > 0) {
+                const double *wd = wsrc;
+                if (c.mem == GBP_MEM_HOST) {
+                    wd = at<double>(W, o_win[s]);
+                    if (n) CK(cudaMemcpyAsync((void *)wd, wsrc, n * c.nw * sizeof(double), cudaMemcpyHostToDevice, st));
+                    h2d += (int64_t)(n * c.nw * sizeof(double));
+                }
+                sd[s].w32 = at<float>(W, o_w32[s]);
+                sd[s].w64 = at<double>(W, o_w64[s]);
+                wsrc = wd;
+            }
+            if (s == 0) c.w1 = wsrc; else c.w2 = wsrc;
+        }
+        unsigned long long *misc = at<unsigned long long>(W, o_misc);
+        CK(cudaMemsetAsync(misc, 0, 8 * sizeof(unsigned long long), st));
+        int *d_counter = reinterpret_cast<int *>(misc);
+        int *d_nitems = reinterpret_cast<int *>(misc) + 1;
+        int *d_err = reinterpret_cast<int *>(misc) + 2;
+        unsigned long long *d_stat = misc + 2;  // [0] rechecks, [1] candidate pairs
+
+        MeshDev md;
+        for (int d = 0; d < 3; d++) {
+            md.n[d] = c.g.n[d];
+            md.c[d] = c.g.c[d];
+            md.L[d] = c.g.L[d];
+        }
+        md.ncells = ncells;
+        md.offsets = nm > 1 ? at<int64_t>(W, o_offs) : nullptr;
+        md.nmocks = nm;
+        for (int s = 0; s < nsamp; s++) {
+            const double *wsrc = s == 0 ? c.w1 : c.w2;
+            cudaError_t e = gbp_build_cells(sd[s].xyz, s == 0 ? c.xyz_f32 : 0, ns[s], md, sd[s].cellid, sd[s].rank, sd[s].count,
+                                            sd[s].start, at<int>(W, o_scan), sd[s].pos32, sd[s].pos64,
+                                            sd[s].orig, c.nw > 0 ? wsrc : nullptr, c.nw, sd[s].w32,
+                                            sd[s].w64, d_err, st, &launches);
+            CK(e);
+        }
+        CK(gbp_build_items(sd[0].start, nkeys, at<int4>(W, o_items), d_nitems, at<int>(W, o_itmp),
+                           at<int>(W, o_scan), st, &launches));
+        CK(cudaMemsetAsync(at<char>(W, o_hist), 0, nm * nhist * sizeof(unsigned long long), st));
+        CK(cudaMemsetAsync(at<char>(W, o_histd), 0, nm * nhist * sizeof(double), st));
+        CK(rec(plan->ev[1]));
+
+        const SampleDev &s2 = c.autocorr ? sd[0] : sd[1];
+        CountArgs a;
+        std::memset(&a, 0, sizeof(a));
+        a.pos1 = sd[0].pos32;
+        a.pos2 = s2.pos32;
+        a.x64_1 = sd[0].pos64;
+        a.x64_2 = s2.pos64;
+        a.start2 = s2.start;
+        a.items = at<int4>(W, o_items);
+        a.nitems = d_nitems;
+        a.counter = d_counter;
+        a.sten = at<int>(W, o_sten);
+        a.stenD = at<float4>(W, o_stenD);
+        a.nsten = nsten;
+        a.nself = c.g.nself;
+        for (int d = 0; d < 3; d++) {
+            a.n[d] = c.g.n[d];
+            a.L[d] = c.g.L[d];
+        }
+        a.pbc = c.g.pbc;
+        for (int x = 0; x < c.naxes; x++) {
+            AxisDev &ad = a.ax[x];
+            const AxisHost &ah = c.ax[x];
+            ad.lut = at<float4>(W, x == 0 ? o_lut0 : o_lut1);
+            ad.E = at<double>(W, x == 0 ? o_E0 : o_E1);
+            ad.hi = at<float>(W, x == 0 ? o_hi0 : o_hi1);
+            ad.lo = at<float>(W, x == 0 ? o_lo0 : o_lo1);
+            ad.nb = ah.nb;
+            ad.T = ah.T;
+            ad.S = ah.S;
+            ad.B = ah.B;
+            ad.vlo = ah.vlo;
+            ad.vhi = ah.vhi;
+        }
+        a.hist_stride = (int)nhist;
+        a.ncells_mock = (int)ncells;
+        a.hist = at<unsigned long long>(W, o_hist);
+        a.histd = at<double>(W, o_histd);
+        a.nrecheck = d_stat;
+        a.w1 = sd[0].w32;
+        a.w2 = s2.w32;
+        a.w64_1 = sd[0].w64;
+        a.w64_2 = s2.w64;
+        a.nw = c.nw;
+        a.wfunc = c.wfunc;
+
+        a.top0 = std::min(c.ax[0].hi[nb0 - 1], 1.0e30f);
+        a.top1 = c.naxes > 1 ? std::min(c.ax[1].hi[nb1 - 1], 1.0e30f) : 0.f;
+        a.self_bin = host_bin(nb0, c.ax[0].E.data(), 0.0);
+        const int jwb = c.mode == MODE_MARK ? (c.wf == 0 ? 8 * c.nw : 4) : (c.mode == MODE_ADJ ? 4 : 0);
+        // shared histogram copies (2-D and wide 1-D): as many as keep the CTA
+        // within ~72 KB of shared memory (3 CTAs per SM), at least one
+        int copies = 1;
+        if (c.mode != MODE_3D && c.mode != MODE_MARK && c.mode != MODE_ADJ) {
+            for (int cp = GBP_WARPS; cp >= 1; cp /= 2) {
+                copies = cp;
+                if (gbp_smem_layout(c.mode, T0, T1, nb0, nb1, nsten, cp, jwb).total <= (72 << 10)) break;
+            }
+        }
+        a.hist_copies = copies;
+        SmemLayout L = gbp_smem_layout(c.mode, T0, T1, nb0, nb1, nsten, copies, jwb);
+        size_t smem = (size_t)L.total;
+        if (smem > (size_t)(227u << 10))
+            return fail(plan, GBP_ERR_INVALID, "too many bins for one shared-memory histogram (%zu B)", smem);
+        a.gt = at<float>(W, o_gt);
+        a.orig = sd[0].orig;
+        a.grad = adj ? (c.mem == GBP_MEM_HOST ? at<double>(W, o_grad) : c.grad_out) : nullptr;
+        int occ = adj ? gbp_adjoint_occupancy(smem) : gbp_count_occupancy(c.mode, c.wf, smem);
+        if (occ <= 0) return fail(plan, GBP_ERR_INVALID, "count kernel does not fit (smem %zu B)", smem);
+        int grid = plan->nsm * occ;
+        if (adj) CK(gbp_launch_adjoint(a, grid, smem, st));
+        else CK(gbp_launch_count(c.mode, c.wf, a, grid, smem, st));
+        if (adj && c.mem == GBP_MEM_HOST && c.n1 > 0) {
+            CK(cudaMemcpyAsync(c.grad_out, a.grad, sizeof(double) * c.n1, cudaMemcpyDeviceToHost, st));
+            d2h += (int64_t)(sizeof(double) * c.n1);
+        }
+        launches += 1;
+        CK(rec(plan->ev[2]));
+        CK(cudaMemcpyAsync(at<char>(H, h_hist), a.hist, nm * nhist * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(at<char>(H, h_histd), a.histd, nm * nhist * sizeof(double), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(at<char>(H, h_misc), misc, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+        CK(rec(plan->ev[3]));
+        d2h += (int64_t)(nm * nhist * (sizeof(unsigned long long) + sizeof(double)) + 8 * sizeof(unsigned long long));
+        return GBP_OK;
+    };
+    if (graph) {
+        CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
+        int erc = enqueue();
+        cudaGraph_t gr = nullptr;
+        cudaError_t ce = cudaStreamEndCapture(st, &gr);
+        if (erc) {
+            if (gr) cudaGraphDestroy(gr);
+            return erc;
+        }
+        CK(ce);
+        if (plan->gexec) {
+            cudaGraphExecUpdateResultInfo info;
+            if (cudaGraphExecUpdate(plan->gexec, gr, &info) != cudaSuccess) {
+                cudaGetLastError();
+                cudaGraphExecDestroy(plan->gexec);
+                plan->gexec = nullptr;
+            }
+        }
+        if (!plan->gexec) {
+            cudaError_t ie = cudaGraphInstantiate(&plan->gexec, gr, 0);
+            if (ie != cudaSuccess) {
+                cudaGraphDestroy(gr);
+                CK(ie);
+            }
+        }
+        cudaGraphDestroy(gr);
+        CK(cudaGraphLaunch(plan->gexec, st));
+    } else {
+        int erc = enqueue();
+        if (erc) return erc;
     }
-    a.hist_copies = copies;
-    SmemLayout L = gbp_smem_layout(c.mode, T0, T1, nb0, nb1, nsten, copies, jwb);
-    size_t smem = (size_t)L.total;
-    if (smem > (size_t)(227u << 10))
-        return fail(plan, GBP_ERR_INVALID, "too many bins for one shared-memory histogram (%zu B)", smem);
-    int occ = gbp_count_occupancy(c.mode, c.wf, smem);
-    if (occ <= 0) return fail(plan, GBP_ERR_INVALID, "count kernel does not fit (smem %zu B)", smem);
-    int grid = plan->nsm * occ;
-    CK(gbp_launch_count(c.mode, c.wf, a, grid, smem, st));
-    launches += 1;
-    CK(cudaEventRecord(plan->ev[2], st));
-    CK(cudaMemcpyAsync(at<char>(H, h_hist), a.hist, nhist * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(at<char>(H, h_histd), a.histd, nhist * sizeof(double), cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(at<char>(H, h_misc), misc, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
-    CK(cudaEventRecord(plan->ev[3], st));
-    d2h += (int64_t)(nhist * (sizeof(unsigned long long) + sizeof(double)) + 8 * sizeof(unsigned long long));
     CK(cudaStreamSynchronize(st));
 
     const unsigned long long *hm = at<unsigned long long>(H, h_misc);
     int err_word = reinterpret_cast<const int *>(hm)[2];
     if (err_word) return fail(plan, GBP_ERR_RANGE, "positions outside [0, period] or not finite");
-    hist_host.assign(at<unsigned long long>(H, h_hist), at<unsigned long long>(H, h_hist) + nhist);
+    hist_host.assign(at<unsigned long long>(H, h_hist), at<unsigned long long>(H, h_hist) + nm * nhist);
     if (c.mode != MODE_MARK) add_self_pairs(c, hist_host);
-    if (histd_host) histd_host->assign(at<double>(H, h_histd), at<double>(H, h_histd) + nhist);
+    if (histd_host) histd_host->assign(at<double>(H, h_histd), at<double>(H, h_histd) + nm * nhist);
     gbp_stats &S = plan->stats;
     S.recheck_pairs = (int64_t)hm[2];
     S.candidate_pairs = (int64_t)hm[3];
@@ -486,6 +572,7 @@ int gbp_plan_destroy(gbp_plan *plan) {
     if (!plan) return GBP_OK;
     cudaSetDevice(plan->device);
     if (plan->stream) cudaStreamSynchronize(plan->stream);
+    if (plan->gexec) cudaGraphExecDestroy(plan->gexec);
     if (plan->work.p) cudaFree(plan->work.p);
     if (plan->pinned) cudaFreeHost(plan->pinned);
     for (int i = 0; i < 4; i++)
@@ -504,6 +591,18 @@ int gbp_plan_set_stream(gbp_plan *plan, void *s) {
 int gbp_plan_set_reach(gbp_plan *plan, int reach) {
     if (!plan || reach < 0 || reach > 4) return GBP_ERR_INVALID;
     plan->reach = reach;
+    return GBP_OK;
+}
+
+int gbp_plan_set_graph(gbp_plan *plan, int enable) {
+    if (!plan) return GBP_ERR_INVALID;
+    plan->graph_mode = enable != 0;
+    return GBP_OK;
+}
+
+int gbp_plan_set_autotune(gbp_plan *plan, int enable) {
+    if (!plan) return GBP_ERR_INVALID;
+    plan->autotune = enable != 0;
     return GBP_OK;
 }
 
@@ -551,6 +650,89 @@ int gbp_npairs_3d(gbp_plan *plan, const double *xyz1, int64_t n1, const double *
     for (int k = 0; k < nb; k++) {
         run += h[k];
         counts[k] = (int64_t)run;
+    }
+    return GBP_OK;
+}
+
+int gbp_batched_npairs_3d(gbp_plan *plan, const void *xyz, int32_t xyz_f32, const int64_t *offsets,
+                          int32_t nmocks, const double *rbins, int32_t nb, const double *period3,
+                          int32_t pbc, int32_t mem, int64_t *counts) {
+    if (!plan) return GBP_ERR_INVALID;
+    if (nmocks < 1 || !offsets) return fail(plan, GBP_ERR_INVALID, "nmocks must be >= 1 with offsets");
+    if (offsets[0] != 0) return fail(plan, GBP_ERR_INVALID, "offsets[0] must be 0");
+    for (int m = 0; m < nmocks; m++)
+        if (offsets[m + 1] < offsets[m]) return fail(plan, GBP_ERR_INVALID, "offsets must be non-decreasing");
+    const int64_t n = offsets[nmocks];
+    int rc = check_common(plan, (const double *)xyz, n, (const double *)xyz, n, period3, pbc, mem);
+    if (rc) return rc;
+    if (!rbins || nb < 2 || nb > GBP_NB_LANE || !counts)
+        return fail(plan, GBP_ERR_INVALID, "rbins must have 2..%d entries", GBP_NB_LANE);
+    double rmax = max_nan(rbins, nb);
+    double search[3] = {rmax, rmax, rmax};
+    if ((rc = check_search(plan, search, period3))) return rc;
+    Call c;
+    c.mode = MODE_3D;
+    c.xyz1 = c.xyz2 = (const double *)xyz;
+    c.n1 = c.n2 = n;
+    c.autocorr = true;
+    c.mem = mem;
+    c.naxes = 1;
+    c.nmocks = nmocks;
+    c.xyz_f32 = xyz_f32 ? 1 : 0;
+    c.offsets.assign(offsets, offsets + nmocks + 1);
+    for (int k = 0; k < nmocks * nb; k++) counts[k] = 0;
+    if (n == 0) return GBP_OK;
+    // the grid follows the mean mock density
+    const int64_t nmean = std::max<int64_t>(1, n / nmocks);
+    auto plan_geometry = [&](int reach) {
+        choose_grid(c.g, period3, search, pbc, nmean, reach, MAX_CELLS_PER_DIM);
+        // cell keys of all mocks must fit an int
+        while (c.g.ncells * nmocks >= (1ll << 31) - 1 && c.g.K > 1)
+            choose_grid(c.g, period3, search, pbc, nmean, c.g.K - 1, MAX_CELLS_PER_DIM);
+        build_stencil(c.g, search, 0, true);
+        ErrModel em = err_model(c.g);
+        std::vector<double> E(nb);
+        edges_top_walk(rbins, nb, E.data());
+        c.ax[0].set(E, &em, 3);
+        c.ax[0].make_lut(no_qband);
+    };
+    std::vector<unsigned long long> h;
+    int reach = plan->reach;
+    if (plan->autotune && reach == 0) {
+        char sig[256];
+        snprintf(sig, sizeof(sig), "b3d:%d:%lld:%d:%.17g:%.17g:%.17g:%.17g:%d", nmocks, (long long)n,
+                 nb, rmax, period3[0], period3[1], period3[2], pbc);
+        int found = 0;
+        for (auto &t : plan->tuned)
+            if (t.first == sig) found = t.second;
+        if (!found) {
+            float best = 1e30f;
+            int bestK = 1;
+            for (int K = 1; K <= 3; K++) {
+                plan_geometry(K);
+                if (c.g.K != K) continue;  // not feasible
+                if ((rc = run_call(plan, c, h))) return rc;
+                if (plan->stats.ms_count < best) {
+                    best = plan->stats.ms_count;
+                    bestK = K;
+                }
+            }
+            plan->tuned.emplace_back(sig, bestK);
+            found = bestK;
+        }
+        reach = found;
+    }
+    plan_geometry(reach);
+    if (c.g.ncells * nmocks >= (1ll << 31) - 1)
+        return fail(plan, GBP_ERR_INVALID, "too many mocks for one batched grid");
+    if ((rc = run_call(plan, c, h))) return rc;
+    const size_t nh = (size_t)nb + 1;
+    for (int m = 0; m < nmocks; m++) {
+        unsigned long long run = 0;
+        for (int k = 0; k < nb; k++) {
+            run += h[m * nh + k];
+            counts[(size_t)m * nb + k] = (int64_t)run;
+        }
     }
     return GBP_OK;
 }
@@ -714,6 +896,110 @@ int gbp_marked_npairs_3d(gbp_plan *plan, const double *xyz1, int64_t n1, const d
         run += hd[k];
         out[k] = run;
     }
+    return GBP_OK;
+}
+
+int gbp_weighted_adjoint_3d(gbp_plan *plan, const double *xyz, int64_t n, const double *w,
+                            const double *rbins, int32_t nb, const double *period3, int32_t pbc,
+                            int32_t mem, const double *gbar, double *grad_w) {
+    int rc = check_common(plan, xyz, n, xyz, n, period3, pbc, mem);
+    if (rc) return rc;
+    if ((n > 0 && (!w || !grad_w)) || !gbar) return fail(plan, GBP_ERR_INVALID, "null weights or gradients");
+    if (!rbins || nb < 2 || nb > GBP_NB_MAX)
+        return fail(plan, GBP_ERR_INVALID, "rbins must have 2..%d entries", GBP_NB_MAX);
+    double rmax = max_nan(rbins, nb);
+    double search[3] = {rmax, rmax, rmax};
+    if ((rc = check_search(plan, search, period3))) return rc;
+    if (n == 0) return GBP_OK;
+    Call c;
+    c.mode = MODE_ADJ;
+    c.xyz1 = c.xyz2 = xyz;
+    c.n1 = c.n2 = n;
+    c.autocorr = true;  // one sorted copy ...
+    c.mem = mem;
+    c.w1 = c.w2 = w;
+    c.nw = 1;
+    c.wfunc = 1;
+    c.naxes = 1;
+    c.grad_out = grad_w;
+    choose_grid(c.g, period3, search, pbc, n, plan->reach, MAX_CELLS_PER_DIM);
+    build_stencil(c.g, search, 0, false);  // ... but the full stencil: gather only
+    ErrModel em = err_model(c.g);
+    std::vector<double> E(nb);
+    edges_top_walk(rbins, nb, E.data());
+    c.ax[0].set(E, &em, 3);
+    c.ax[0].make_lut(no_qband);
+    c.gt.assign(nb + 1, 0.f);
+    double run = 0.0;
+    for (int k = nb - 1; k >= 0; k--) {
+        run += gbar[k];
+        c.gt[k] = (float)run;
+    }
+    std::vector<unsigned long long> h;
+    return run_call(plan, c, h);
+}
+
+static int zheng07_args(gbp_plan *plan, const double *theta, Zheng07 *th) {
+    if (!theta) return fail(plan, GBP_ERR_INVALID, "null theta");
+    th->logMmin = theta[0];
+    th->sigma = theta[1];
+    th->logM0 = theta[2];
+    th->logM1 = theta[3];
+    th->alpha = theta[4];
+    if (!(th->sigma > 0)) return fail(plan, GBP_ERR_INVALID, "sigma_logM must be positive");
+    return GBP_OK;
+}
+
+int gbp_zheng07_weights(gbp_plan *plan, const double *mass, int64_t n, const double *theta,
+                        int32_t mem, double *w) {
+    if (!plan) return GBP_ERR_INVALID;
+    Zheng07 th;
+    int rc = zheng07_args(plan, theta, &th);
+    if (rc) return rc;
+    if (n < 0 || (n > 0 && (!mass || !w))) return fail(plan, GBP_ERR_INVALID, "null arrays");
+    if (n == 0) return GBP_OK;
+    CK(cudaSetDevice(plan->device));
+    cudaStream_t st = plan->stream;
+    const double *dm = mass;
+    double *dw = w;
+    if (mem == GBP_MEM_HOST) {
+        if ((rc = ensure_work(plan, 2 * n * sizeof(double) + 256))) return rc;
+        dm = static_cast<double *>(plan->work.p);
+        dw = static_cast<double *>(plan->work.p) + n;
+        CK(cudaMemcpyAsync((void *)dm, mass, n * sizeof(double), cudaMemcpyHostToDevice, st));
+    }
+    CK(gbp_launch_zheng07_w(dm, n, th, dw, st));
+    if (mem == GBP_MEM_HOST) CK(cudaMemcpyAsync(w, dw, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    return GBP_OK;
+}
+
+int gbp_zheng07_vjp(gbp_plan *plan, const double *mass, int64_t n, const double *theta,
+                    const double *grad_w, int32_t mem, double *grad_theta) {
+    if (!plan) return GBP_ERR_INVALID;
+    Zheng07 th;
+    int rc = zheng07_args(plan, theta, &th);
+    if (rc) return rc;
+    if (!grad_theta || n < 0 || (n > 0 && (!mass || !grad_w)))
+        return fail(plan, GBP_ERR_INVALID, "null arrays");
+    CK(cudaSetDevice(plan->device));
+    cudaStream_t st = plan->stream;
+    size_t need = (mem == GBP_MEM_HOST ? 2 * (size_t)n : 0) * sizeof(double) + 8 * sizeof(double) + 512;
+    if ((rc = ensure_work(plan, need))) return rc;
+    double *out = static_cast<double *>(plan->work.p);
+    const double *dm = mass, *dg = grad_w;
+    if (mem == GBP_MEM_HOST) {
+        double *buf = out + 8;
+        dm = buf;
+        dg = buf + n;
+        if (n) {
+            CK(cudaMemcpyAsync((void *)dm, mass, n * sizeof(double), cudaMemcpyHostToDevice, st));
+            CK(cudaMemcpyAsync((void *)dg, grad_w, n * sizeof(double), cudaMemcpyHostToDevice, st));
+        }
+    }
+    CK(gbp_launch_zheng07_vjp(dm, n, th, dg, out, st));
+    CK(cudaMemcpyAsync(grad_theta, out, 5 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
     return GBP_OK;
 }
 

@@ -31,64 +31,7 @@
 // histograms at the end (integer copies also early, before a u32 could wrap).
 #include "gbp_internal.cuh"
 
-struct AxisSm {
-    const float4 *lut;
-    const float *hi;
-    const float *lo;
-    const double *E;
-    int nb, S, B;
-    float vlo, vhi;
-};
-
-__device__ __forceinline__ float4 lut_entry(float v, const AxisSm &a) {
-    float vc = fminf(fmaxf(v, a.vlo), a.vhi);
-    int idx = (int)(__float_as_uint(vc) >> a.S) - a.B;
-    return a.lut[idx];
-}
-
-// Walk from the table's start bin with the per-edge thresholds.  Returns the
-// bin if the FP32 value decides it, or -1 - k if it is ambiguous at edge k.
-__device__ __forceinline__ int walk_bin(float v, int b0, const AxisSm &a) {
-    int k = b0;
-    while (k < a.nb && v > a.hi[k]) k++;
-    if (k < a.nb && v > a.lo[k]) return -1 - k;
-    return k;
-}
-
-__device__ __forceinline__ int exact_bin(double v, int b0, const AxisSm &a) {
-    int k = b0;
-    while (k < a.nb && !(v <= a.E[k])) k++;
-    return k;
-}
-
-// halotools' shift: x1tmp = x1 - x2shift, dx = x1tmp - x2 with x2shift in
-// {-L, 0, +L}; for a pair inside the search range exactly one shift gives
-// |dx| <= L/3, which is the one the reference's stencil visit applies.
-__device__ __forceinline__ double ref_delta(double a, double b, double L, int pbc) {
-    double d0 = __dsub_rn(a, b);
-    if (!pbc) return d0;
-    double dp = __dsub_rn(__dsub_rn(a, L), b);
-    double dm = __dsub_rn(__dadd_rn(a, L), b);
-    double best = d0;
-    if (fabs(dp) < fabs(best)) best = dp;
-    if (fabs(dm) < fabs(best)) best = dm;
-    return best;
-}
-
-struct Exact3 {
-    double dxy, dz2, s2;
-};
-
-__device__ __forceinline__ Exact3 exact_pair(const double *p, const double *q, const CountArgs &a) {
-    double dx = ref_delta(p[0], q[0], a.L[0], a.pbc);
-    double dy = ref_delta(p[1], q[1], a.L[1], a.pbc);
-    double dz = ref_delta(p[2], q[2], a.L[2], a.pbc);
-    Exact3 r;
-    r.dxy = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
-    r.dz2 = __dmul_rn(dz, dz);
-    r.s2 = __dadd_rn(r.dxy, r.dz2);
-    return r;
-}
+#include "gbp_device.cuh"
 
 #define SYM_BIT 0x80000000u
 
@@ -380,6 +323,56 @@ __global__ void __launch_bounds__(GBP_BLOCK, 3) k_count(const CountArgs a) {
     const unsigned ltmask = (1u << lane) - 1u;
     unsigned long long since_flush = 0, cand = 0;
     int qn = 0;  // entries in this warp's queue (warp-uniform)
+    int cur_mock = -1;
+
+    // Bin what is left in every warp's queue, then add the shared histograms
+    // to mock `mk`'s global histogram and clear them.  Called by all threads.
+    auto flush_all = [&](int mk) {
+        __syncwarp();
+        if (lane < qn) {
+            const float4 e = s_q[lane];
+            if (MODE == MODE_3D) bin_3d<true>(e, hl, A0, a);
+            else if (MODE == MODE_3DS) bin_3d<false>(e, hw, A0, a);
+            else if (MODE == MODE_XYZ) bin_xyz(e, hw, stride2, A0, A1, a);
+            else if (MODE == MODE_SMU) bin_smu(e, hw, stride2, A0, A1, a);
+            else if (MARK) bin_mark(e, hs, hc, A0, a);
+        }
+        qn = 0;
+        __syncthreads();
+        unsigned long long *gh = a.hist + (size_t)mk * a.hist_stride;
+        if (MODE == MODE_3D) {
+            for (int b = warp; b < nb0 + 1; b += GBP_WARPS) {
+                unsigned long long s = 0;
+                for (int w = 0; w < GBP_WARPS; w++) s += s_hist[(w * (nb0 + 1) + b) * 32 + lane];
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+                if (lane == 0 && s) atomicAdd(&gh[b], s);
+            }
+        } else if (MARK) {
+            double *gd = a.histd + (size_t)mk * a.hist_stride;
+            const float *S = (const float *)s_hist;
+            const float *C = S + GBP_WARPS * (nb0 + 1) * 32;
+            for (int b = warp; b < nb0; b += GBP_WARPS) {
+                double s = 0.0;
+                for (int w = 0; w < GBP_WARPS; w++) {
+                    int idx = (w * (nb0 + 1) + b) * 32 + lane;
+                    s += (double)S[idx] - (double)C[idx];
+                }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+                if (lane == 0 && s != 0.0) atomicAdd(&gd[b], s);
+            }
+        } else {
+            for (int b = tid; b < nbin; b += GBP_BLOCK) {
+                unsigned long long s = 0;
+                for (int w = 0; w < copies; w++) s += s_hist[w * nbin + b];
+                if (s) atomicAdd(&gh[b], s);
+            }
+        }
+        __syncthreads();
+        for (int i = tid; i < hist_words; i += GBP_BLOCK) s_hist[i] = 0u;
+        __syncthreads();
+    };
     __syncthreads();
 
     while (true) {
@@ -388,8 +381,15 @@ __global__ void __launch_bounds__(GBP_BLOCK, 3) k_count(const CountArgs a) {
         const int it = s_item;
         if (it >= s_nitems) break;
         const int4 item = a.items[it];
-        const int cell = item.x, ifirst = item.y, icnt = item.z;
+        const int mock = item.x / a.ncells_mock;
+        const int cell = item.x - mock * a.ncells_mock, ifirst = item.y, icnt = item.z;
         const int cz = cell % n2, cy = (cell / n2) % n1, cx = cell / (n1 * n2);
+        if (mock != cur_mock) {
+            // batched mocks: a new mock's histogram starts here
+            if (cur_mock >= 0) flush_all(cur_mock);
+            cur_mock = mock;
+        }
+        const int keybase = mock * a.ncells_mock;
         for (int s = tid; s < a.nsten; s += GBP_BLOCK) {
             int pk = s_off[s];
             int x = cx + (pk & 255) - 64, y = cy + ((pk >> 8) & 255) - 64,
@@ -404,7 +404,7 @@ __global__ void __launch_bounds__(GBP_BLOCK, 3) k_count(const CountArgs a) {
             }
             int st = 0, cn = 0;
             if (ok) {
-                int c2 = (x * n1 + y) * n2 + z;
+                int c2 = keybase + (x * n1 + y) * n2 + z;
                 st = a.start2[c2];
                 cn = a.start2[c2 + 1] - st;
             }
@@ -540,59 +540,12 @@ __global__ void __launch_bounds__(GBP_BLOCK, 3) k_count(const CountArgs a) {
             since_flush += 2ull * (unsigned long long)total *
                            (MODE == MODE_3D ? 1ull : (unsigned long long)(GBP_BLOCK / copies)) + 64ull;
             if (since_flush > (1ull << 31)) {
-                for (int i = tid; i < hist_words; i += GBP_BLOCK) {
-                    unsigned v = s_hist[i];
-                    if (v) {
-                        int bin = (MODE == MODE_3D) ? (i / 32) % (nb0 + 1) : i % nbin;
-                        atomicAdd(&a.hist[bin], (unsigned long long)v);
-                        s_hist[i] = 0u;
-                    }
-                }
+                flush_all(cur_mock);
                 since_flush = 0;
-                __syncthreads();
             }
         }
     }
-    // drain what is left in this warp's queue (fewer than 32 entries)
-    __syncwarp();
-    if (lane < qn) {
-        const float4 e = s_q[lane];
-        if (MODE == MODE_3D) bin_3d<true>(e, hl, A0, a);
-        else if (MODE == MODE_3DS) bin_3d<false>(e, hw, A0, a);
-        else if (MODE == MODE_XYZ) bin_xyz(e, hw, stride2, A0, A1, a);
-        else if (MODE == MODE_SMU) bin_smu(e, hw, stride2, A0, A1, a);
-        else if (MARK) bin_mark(e, hs, hc, A0, a);
-    }
-    // final flush: reduce the copies and add to the global histogram
-    __syncthreads();
-    if (MODE == MODE_3D) {
-        for (int b = warp; b < nb0 + 1; b += GBP_WARPS) {
-            unsigned long long s = 0;
-            for (int w = 0; w < GBP_WARPS; w++) s += s_hist[(w * (nb0 + 1) + b) * 32 + lane];
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-            if (lane == 0 && s) atomicAdd(&a.hist[b], s);
-        }
-    } else if (MARK) {
-        const float *S = (const float *)s_hist;
-        const float *C = S + GBP_WARPS * (nb0 + 1) * 32;
-        for (int b = warp; b < nb0; b += GBP_WARPS) {
-            double s = 0.0;
-            for (int w = 0; w < GBP_WARPS; w++) {
-                int idx = (w * (nb0 + 1) + b) * 32 + lane;
-                s += (double)S[idx] - (double)C[idx];
-            }
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-            if (lane == 0 && s != 0.0) atomicAdd(&a.histd[b], s);
-        }
-    } else {
-        for (int b = tid; b < nbin; b += GBP_BLOCK) {
-            unsigned long long s = 0;
-            for (int w = 0; w < copies; w++) s += s_hist[w * nbin + b];
-            if (s) atomicAdd(&a.hist[b], s);
-        }
-    }
+    if (cur_mock >= 0) flush_all(cur_mock);
     if (tid == 0 && cand) atomicAdd(a.nrecheck + 1, cand);
 }
 

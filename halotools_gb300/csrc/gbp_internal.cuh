@@ -59,7 +59,8 @@ struct CountArgs {
     int pbc;
     double L[3];
     AxisDev ax[2];
-    int hist_stride;        // bins per histogram copy
+    int hist_stride;        // histogram words per mock (global histogram is [mock][bin])
+    int ncells_mock;        // cells per mock: work-item key = mock * ncells_mock + cell
     int hist_copies;        // shared histogram copies (2-D and wide 1-D): 8 = one per warp, or 1
     unsigned long long *hist;   // global differential histogram(s)
     unsigned long long *nrecheck;
@@ -73,6 +74,10 @@ struct CountArgs {
     int wfunc;
     int self_bin;           // bin of separation 0 (marked auto mode adds f(w_i, w_i) there)
     double *histd;          // FP64 weighted histogram (marked)
+    // adjoint
+    const float *gt;        // gt[b] = sum of the upstream gradient over cumulative bins >= b
+    const int *orig;        // sorted position -> caller's index
+    double *grad;           // dL/dw in the caller's order
 };
 
 // Shared-memory layout of the count kernel, identical on host and device.
@@ -111,7 +116,7 @@ __host__ __device__ inline SmemLayout gbp_smem_layout(int mode, int T0, int T1, 
     } else if (mode == MODE_MARK) {
         hist_bytes = GBP_WARPS * (nb0 + 1) * 32 * 4 * 2;      // lane-private FP32 sum + compensation
     } else if (mode == MODE_ADJ) {
-        hist_bytes = GBP_BLOCK * 8 + 16;                      // per-thread partial gradients
+        hist_bytes = GBP_BLOCK * 8 + gbp_align((nb0 + 1) * 4, 16);  // partial sums + gt table
     } else if (mode == MODE_3DS) {
         hist_bytes = copies * (nb0 + 1) * 4;                  // shared u32 copies (wide 1-D)
     } else {
@@ -127,11 +132,14 @@ struct MeshDev {
     int n[3];
     double c[3];
     double L[3];
-    int64_t ncells;
+    int64_t ncells;             // cells per mock
+    const int64_t *offsets;     // device, nmocks+1 point offsets (null: one sample)
+    int nmocks;                 // samples sorted together; cell key = mock * ncells + cell
 };
 
-// Digitise, count, scan and scatter one sample into the cell-sorted layout.
-cudaError_t gbp_build_cells(const double *d_xyz, int64_t npts, const MeshDev &m, int *d_cellid,
+// Digitise, count, scan and scatter one sample (or a batch of mocks) into the
+// cell-sorted layout.  xyz_f32: positions are float32 (upcast exactly).
+cudaError_t gbp_build_cells(const void *d_xyz, int xyz_f32, int64_t npts, const MeshDev &m, int *d_cellid,
                             int *d_rank, int *d_count, int *d_start, int *d_scan_tmp,
                             float4 *d_pos32, double *d_pos64, int *d_orig, const double *d_w,
                             int nw, float *d_w32, double *d_w64, int *d_err, cudaStream_t st,
@@ -148,4 +156,13 @@ cudaError_t gbp_launch_count(int mode, int wf, const CountArgs &a, int grid, siz
                              cudaStream_t st);
 int gbp_count_occupancy(int mode, int wf, size_t smem);
 cudaError_t gbp_count_set_smem(size_t smem);
+cudaError_t gbp_launch_adjoint(const CountArgs &a, int grid, size_t smem, cudaStream_t st);
+int gbp_adjoint_occupancy(size_t smem);
+struct Zheng07 {
+    double logMmin, sigma, logM0, logM1, alpha;
+};
+cudaError_t gbp_launch_zheng07_w(const double *mass, int64_t n, Zheng07 th, double *w,
+                                 cudaStream_t st);
+cudaError_t gbp_launch_zheng07_vjp(const double *mass, int64_t n, Zheng07 th, const double *gw,
+                                   double *out5, cudaStream_t st);
 cudaError_t gbp_run_ffma_probe(int nsm, cudaStream_t st, float *ms_out, double *flops_out);

@@ -14,17 +14,27 @@
 #define SCAN_THREADS 1024
 #define SCAN_TILE (SCAN_THREADS * 4)
 
-__global__ void k_digitize(const double *__restrict__ xyz, int64_t npts, MeshDev m,
+template <class T>
+__global__ void k_digitize(const T *__restrict__ xyz, int64_t npts, MeshDev m,
                            int *__restrict__ cellid, int *__restrict__ rank,
                            int *__restrict__ count, float4 *__restrict__ rel, int *err) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= npts) return;
+    int mock = 0;
+    if (m.offsets) {  // largest mock with offsets[mock] <= i
+        int lo = 0, hi = m.nmocks - 1;
+        while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if (m.offsets[mid] <= i) lo = mid; else hi = mid - 1;
+        }
+        mock = lo;
+    }
     int ic[3];
     float u[3];
     bool bad = false;
 #pragma unroll
     for (int d = 0; d < 3; d++) {
-        double x = xyz[3 * i + d];
+        double x = (double)xyz[3 * i + d];
         if (!(x >= 0.0 && x <= m.L[d])) bad = true;  // also catches NaN
         double t = x * (1.0 / m.c[d]);
         int k = (int)floor(t);
@@ -37,13 +47,14 @@ __global__ void k_digitize(const double *__restrict__ xyz, int64_t npts, MeshDev
         ic[0] = ic[1] = ic[2] = 0;
         u[0] = u[1] = u[2] = GBP_FAR;
     }
-    int c = (ic[0] * m.n[1] + ic[1]) * m.n[2] + ic[2];
+    int c = (int)(mock * m.ncells) + (ic[0] * m.n[1] + ic[1]) * m.n[2] + ic[2];
     cellid[i] = c;
     rank[i] = atomicAdd(&count[c], 1);
     rel[i] = make_float4(u[0], u[1], u[2], __int_as_float((int)i));
 }
 
-__global__ void k_scatter(const double *__restrict__ xyz, int64_t npts,
+template <class T>
+__global__ void k_scatter(const T *__restrict__ xyz, int64_t npts,
                           const int *__restrict__ cellid, const int *__restrict__ rank,
                           const int *__restrict__ start, const float4 *__restrict__ rel,
                           float4 *__restrict__ pos32, double *__restrict__ pos64,
@@ -55,9 +66,9 @@ __global__ void k_scatter(const double *__restrict__ xyz, int64_t npts,
     float4 r = rel[i];
     r.w = __int_as_float(dst);
     pos32[dst] = r;
-    pos64[3 * (int64_t)dst + 0] = xyz[3 * i + 0];
-    pos64[3 * (int64_t)dst + 1] = xyz[3 * i + 1];
-    pos64[3 * (int64_t)dst + 2] = xyz[3 * i + 2];
+    pos64[3 * (int64_t)dst + 0] = (double)xyz[3 * i + 0];
+    pos64[3 * (int64_t)dst + 1] = (double)xyz[3 * i + 1];
+    pos64[3 * (int64_t)dst + 2] = (double)xyz[3 * i + 2];
     orig[dst] = (int)i;
     if (w) {
         for (int k = 0; k < nw; k++) {
@@ -151,27 +162,37 @@ cudaError_t gbp_scan_exclusive(const int *d_in, int *d_out, int64_t n, int *d_tm
     return cudaGetLastError();
 }
 
-cudaError_t gbp_build_cells(const double *d_xyz, int64_t npts, const MeshDev &m, int *d_cellid,
-                            int *d_rank, int *d_count, int *d_start, int *d_scan_tmp,
+cudaError_t gbp_build_cells(const void *d_xyz, int xyz_f32, int64_t npts, const MeshDev &m,
+                            int *d_cellid, int *d_rank, int *d_count, int *d_start, int *d_scan_tmp,
                             float4 *d_pos32, double *d_pos64, int *d_orig, const double *d_w,
                             int nw, float *d_w32, double *d_w64, int *d_err, cudaStream_t st,
                             int *launches) {
-    cudaError_t e = cudaMemsetAsync(d_count, 0, sizeof(int) * (size_t)m.ncells, st);
+    const int64_t nkeys = m.ncells * (int64_t)(m.offsets ? m.nmocks : 1);
+    cudaError_t e = cudaMemsetAsync(d_count, 0, sizeof(int) * (size_t)nkeys, st);
     if (e != cudaSuccess) return e;
     // the FP32 relative records are staged in the pos32 buffer's twin (d_pos32 + npts)
     float4 *rel = d_pos32 + npts;
+    unsigned g = (unsigned)((npts + 255) / 256);
     if (npts > 0) {
-        unsigned g = (unsigned)((npts + 255) / 256);
-        k_digitize<<<g, 256, 0, st>>>(d_xyz, npts, m, d_cellid, d_rank, d_count, rel, d_err);
+        if (xyz_f32)
+            k_digitize<float><<<g, 256, 0, st>>>((const float *)d_xyz, npts, m, d_cellid, d_rank,
+                                                 d_count, rel, d_err);
+        else
+            k_digitize<double><<<g, 256, 0, st>>>((const double *)d_xyz, npts, m, d_cellid, d_rank,
+                                                  d_count, rel, d_err);
         if (launches) *launches += 1;
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
-    e = gbp_scan_exclusive(d_count, d_start, m.ncells, d_scan_tmp, st, launches);
+    e = gbp_scan_exclusive(d_count, d_start, nkeys, d_scan_tmp, st, launches);
     if (e != cudaSuccess) return e;
     if (npts > 0) {
-        unsigned g = (unsigned)((npts + 255) / 256);
-        k_scatter<<<g, 256, 0, st>>>(d_xyz, npts, d_cellid, d_rank, d_start, rel, d_pos32, d_pos64,
-                                     d_orig, d_w, nw, d_w32, d_w64);
+        if (xyz_f32)
+            k_scatter<float><<<g, 256, 0, st>>>((const float *)d_xyz, npts, d_cellid, d_rank, d_start,
+                                                rel, d_pos32, d_pos64, d_orig, d_w, nw, d_w32, d_w64);
+        else
+            k_scatter<double><<<g, 256, 0, st>>>((const double *)d_xyz, npts, d_cellid, d_rank,
+                                                 d_start, rel, d_pos32, d_pos64, d_orig, d_w, nw,
+                                                 d_w32, d_w64);
         if (launches) *launches += 1;
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }

@@ -159,10 +159,12 @@ extern "C" int gbp_npairs_3d_static(const double *xyz, int64_t n, const double *
         md.L[d] = g.L[d];
     }
     md.ncells = g.ncells;
+    md.offsets = nullptr;
+    md.nmocks = 1;
     float4 *pos32 = reinterpret_cast<float4 *>(W + O_POS32);
     double *pos64 = reinterpret_cast<double *>(W + O_POS64);
     int *start = reinterpret_cast<int *>(W + O_START);
-    e = gbp_build_cells(xyz, n, md, reinterpret_cast<int *>(W + O_CELLID),
+    e = gbp_build_cells(xyz, 0, n, md, reinterpret_cast<int *>(W + O_CELLID),
                         reinterpret_cast<int *>(W + O_RANK), reinterpret_cast<int *>(W + O_COUNT),
                         start, reinterpret_cast<int *>(W + O_SCAN), pos32, pos64,
                         reinterpret_cast<int *>(W + O_ORIG), nullptr, 0, nullptr, nullptr,
@@ -201,7 +203,8 @@ extern "C" int gbp_npairs_3d_static(const double *xyz, int64_t n, const double *
     ad.B = li.B;
     ad.vlo = li.vlo;
     ad.vhi = li.vhi;
-    a.hist_stride = 1;
+    a.hist_stride = nbins + 1;
+    a.ncells_mock = (int)g.ncells;
     a.hist_copies = 1;
     a.hist = reinterpret_cast<unsigned long long *>(W + O_HIST);
     a.nrecheck = misc + 2;

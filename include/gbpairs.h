@@ -64,6 +64,12 @@ int gbp_plan_destroy(gbp_plan *plan);
 int gbp_plan_set_stream(gbp_plan *plan, void *cuda_stream);
 /* Force the stencil reach (1..4 cells per search length); 0 = automatic. */
 int gbp_plan_set_reach(gbp_plan *plan, int reach);
+/* 1: capture each call's stream work into one CUDA graph (instantiated once,
+ * updated in place on later calls) and launch that; 0: launch directly. */
+int gbp_plan_set_graph(gbp_plan *plan, int enable);
+/* 1: on the first call of a new workload shape, time every feasible reach and
+ * keep the fastest for later calls of that shape; 0: density heuristic. */
+int gbp_plan_set_autotune(gbp_plan *plan, int enable);
 const char *gbp_plan_last_error(const gbp_plan *plan);
 int gbp_plan_stats(const gbp_plan *plan, gbp_stats *stats);
 
@@ -77,6 +83,21 @@ int gbp_plan_stats(const gbp_plan *plan, gbp_stats *stats);
 int gbp_npairs_3d(gbp_plan *plan, const double *xyz1, int64_t n1, const double *xyz2,
                   int64_t n2, const double *rbins, int32_t nbins, const double *period3,
                   int32_t pbc, int32_t mem, int64_t *counts);
+
+/*
+ * Batched auto-correlation counts of many samples ("mocks", e.g. HOD
+ * realisations on one halo catalogue) in one cell-list build and one
+ * persistent count launch over a shared grid: counts[m][k] equals
+ * gbp_npairs_3d of mock m alone.  Sample m is rows offsets[m] ..
+ * offsets[m+1]-1 of xyz ((N, 3), float64, or float32 if xyz_f32 = 1, which
+ * the reference upcasts exactly, npairs_3d_engine.pyx:58-63); offsets is a
+ * host array of nmocks+1 non-decreasing entries from 0 to N.  No reference
+ * counterpart as one call: it replaces nmocks calls of npairs_3d
+ * (npairs_3d.py:20), e.g. the loop marked_tpcf.py:327-345 runs.
+ */
+int gbp_batched_npairs_3d(gbp_plan *plan, const void *xyz, int32_t xyz_f32, const int64_t *offsets,
+                          int32_t nmocks, const double *rbins, int32_t nbins,
+                          const double *period3, int32_t pbc, int32_t mem, int64_t *counts);
 
 /*
  * Cumulative (r_p, pi) counts, row-major [n_rp][n_pi].
@@ -107,6 +128,31 @@ int gbp_marked_npairs_3d(gbp_plan *plan, const double *xyz1, int64_t n1, const d
                          int64_t n2, const double *w1, const double *w2, int32_t nw,
                          int32_t wfunc_id, const double *rbins, int32_t nbins,
                          const double *period3, int32_t pbc, int32_t mem, double *out);
+
+/*
+ * Reverse pass of occupation-weighted counts, no reference counterpart
+ * (halotools has no gradients).  For the forward
+ * gbp_marked_npairs_3d(xyz, xyz, w, w, 1 weight, wfunc 1) =
+ * C_k = sum_ij w_i w_j [d_ij <= r_k] and an upstream gradient gbar[k]
+ * (host, nbins), writes grad_w[m] = dL/dw_m = sum_j w_j (G(d_mj) + G(d_jm)),
+ * G(d) = sum_{k: d <= r_k} gbar[k], in the caller's order.  xyz (n, 3), w (n)
+ * and grad_w (n) live in `mem` memory.
+ */
+int gbp_weighted_adjoint_3d(gbp_plan *plan, const double *xyz, int64_t n, const double *w,
+                            const double *rbins, int32_t nbins, const double *period3,
+                            int32_t pbc, int32_t mem, const double *gbar, double *grad_w);
+
+/*
+ * Zheng07 occupation weights w = <Ncen> + <Nsat> per halo mass M
+ * (zheng07_components.py:149-153 and 455-470, satellites not modulated by the
+ * central occupation), theta = (logMmin, sigma_logM, logM0, logM1, alpha)
+ * (host array of 5), and the vector-Jacobian product
+ * grad_theta = sum_m grad_w[m] dw_m/dtheta (host array of 5).
+ */
+int gbp_zheng07_weights(gbp_plan *plan, const double *mass, int64_t n, const double *theta,
+                        int32_t mem, double *w);
+int gbp_zheng07_vjp(gbp_plan *plan, const double *mass, int64_t n, const double *theta,
+                    const double *grad_w, int32_t mem, double *grad_theta);
 
 /*
  * Allocation-free npairs_3d.  No counterpart in the reference: it exists for

@@ -45,6 +45,7 @@ def lib():
         L.orc_npairs_s_mu.argtypes = [pd, i64, pd, i64, pd, i, pd, i, pd, i, pd, pd, i, pi64]
         L.orc_marked_npairs_3d.argtypes = [pd, i64, pd, i64, pd, pd, i, i, pd, i, pd, i, pd, pd, i, pd]
         L.orc_bf_npairs_3d.argtypes = [pd, i64, pd, i64, pd, i, pd, i, pi64]
+        L.orc_weighted_adjoint_3d.argtypes = [pd, i64, pd, pd, i, pd, i, pd, i, pd]
         _lib = L
     return _lib
 
@@ -175,4 +176,17 @@ def brute_force_npairs_3d(sample1, sample2, rbins, period=None):
     out = np.zeros(len(rbins), dtype=np.int64)
     _check(lib().orc_bf_npairs_3d(_p(x1), len(x1), _p(x2), len(x2), _p(rbins), len(rbins),
                                   _p(lbox), pbc, _pi(out)))
+    return out
+
+
+def weighted_adjoint_3d(xyz, w, rbins, period, gbar, num_threads=8):
+    """FP64 dL/dw of sum_ij w_i w_j [d_ij <= r_k] for upstream gradient gbar (brute force)."""
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+    w = np.ascontiguousarray(w, dtype=np.float64)
+    rbins = np.ascontiguousarray(rbins, dtype=np.float64)
+    gbar = np.ascontiguousarray(gbar, dtype=np.float64)
+    box = np.ascontiguousarray(np.broadcast_to(np.atleast_1d(period).astype(np.float64), (3,)))
+    out = np.zeros(len(xyz), dtype=np.float64)
+    _check(lib().orc_weighted_adjoint_3d(_p(xyz), len(xyz), _p(w), _p(rbins), len(rbins), _p(box),
+                                         1, _p(gbar), int(num_threads), _p(out)))
     return out

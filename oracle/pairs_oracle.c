@@ -518,3 +518,65 @@ int orc_bf_npairs_3d(const double *xyz1, int64_t n1, const double *xyz2, int64_t
     free(e);
     return 0;
 }
+
+/*
+ * FP64 reference gradient of occupation-weighted counts (no reference
+ * counterpart: halotools has no gradients).  For C_k = sum_ij w_i w_j
+ * [d_ij <= r_k] and an upstream gradient gbar, grad[m] = dL/dw_m =
+ * 2 sum_j w_j G(d_mj), G(d) = sum_{k: d <= r_k} gbar_k, by brute force over
+ * all j with the reference's shift and FP64 operation order.  Threads split m.
+ */
+typedef struct {
+    const double *xyz, *w, *e, *gbar;
+    int64_t n, m0, m1;
+    int nb, pbc;
+    const double *period;
+    double *grad;
+} adj_job_t;
+
+static void *adj_thread(void *arg) {
+    adj_job_t *J = (adj_job_t *)arg;
+    for (int64_t m = J->m0; m < J->m1; m++) {
+        double acc = 0.0;
+        for (int64_t j = 0; j < J->n; j++) {
+            double dx = shifted_delta(J->xyz[3 * m], J->xyz[3 * j], J->period[0], J->pbc);
+            double dy = shifted_delta(J->xyz[3 * m + 1], J->xyz[3 * j + 1], J->period[1], J->pbc);
+            double dz = shifted_delta(J->xyz[3 * m + 2], J->xyz[3 * j + 2], J->period[2], J->pbc);
+            double dsq = dx * dx + dy * dy + dz * dz;
+            double G = 0.0;
+            int k = J->nb - 1;
+            while (dsq <= J->e[k]) { G += J->gbar[k]; k--; if (k < 0) break; }
+            acc += J->w[j] * G;
+        }
+        J->grad[m] = 2.0 * acc;
+    }
+    return NULL;
+}
+
+int orc_weighted_adjoint_3d(const double *xyz, int64_t n, const double *w, const double *rbins,
+                            int nb, const double period[3], int pbc, const double *gbar,
+                            int nthreads, double *grad) {
+    double *e = (double *)malloc(sizeof(double) * (size_t)nb);
+    if (!e) return -1;
+    for (int k = 0; k < nb; k++) e[k] = rbins[k] * rbins[k];
+    if (nthreads < 1) nthreads = 1;
+    adj_job_t *jobs = (adj_job_t *)calloc((size_t)nthreads, sizeof(adj_job_t));
+    pthread_t *th = (pthread_t *)calloc((size_t)nthreads, sizeof(pthread_t));
+    if (!jobs || !th) { free(e); free(jobs); free(th); return -1; }
+    int64_t per = (n + nthreads - 1) / nthreads;
+    char *running = (char *)calloc((size_t)nthreads, 1);
+    if (!running) { free(e); free(jobs); free(th); return -1; }
+    for (int t = 0; t < nthreads; t++) {
+        adj_job_t J = {xyz, w, e, gbar, n, t * per, (t + 1) * per < n ? (t + 1) * per : n,
+                       nb, pbc, period, grad};
+        jobs[t] = J;
+        if (jobs[t].m0 >= jobs[t].m1) continue;
+        if (pthread_create(&th[t], NULL, adj_thread, &jobs[t]) == 0) running[t] = 1;
+        else adj_thread(&jobs[t]);
+    }
+    for (int t = 0; t < nthreads; t++)
+        if (running[t]) pthread_join(th[t], NULL);
+    free(running);
+    free(jobs); free(th); free(e);
+    return 0;
+}

@@ -52,3 +52,16 @@ def test_oracle_planted_error_is_caught():
     s2[0, 0] = np.nextafter(s2[0, 0], np.inf if s2[0, 0] < c["s1"][0, 0] else -np.inf) + 1e-9
     got = oracle.npairs_3d(c["s1"], s2, c["bins"], period=c["period"])
     assert not np.array_equal(got, c["out"])
+
+
+def test_oracle_adjoint_matches_marked_identity():
+    rng = np.random.default_rng(9)
+    x = rng.uniform(0, 40, (1500, 3))
+    w = rng.uniform(0, 1, 1500)
+    rb = np.array([1.0, 3.0, 7.0])
+    g = np.array([0.3, -1.0, 2.0])
+    grad = oracle.weighted_adjoint_3d(x, w, rb, 40.0, g)
+    for m in (0, 700, 1499):
+        c = oracle.marked_npairs_3d(x[m:m + 1], x, rb, 1, period=40.0, weights1=np.ones(1),
+                                    weights2=w)
+        assert abs(grad[m] - 2 * np.dot(g, c)) < 1e-9 * max(1.0, abs(grad[m]))
