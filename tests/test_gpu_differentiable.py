@@ -32,7 +32,9 @@ def test_zheng07_weights_and_vjp(gpu):
     th = torch.tensor(THETA, dtype=torch.float64, device="cuda", requires_grad=True)
     m = torch.from_numpy(mass).cuda()
     w = D.zheng07_weights(th, m)
-    np.testing.assert_allclose(w.detach().cpu().numpy(), zheng07_np(THETA, mass), rtol=1e-12)
+    # 0.5 (1 + erf x) cancels for x << 0: compare to an absolute 1e-15 as well
+    np.testing.assert_allclose(w.detach().cpu().numpy(), zheng07_np(THETA, mass), rtol=1e-12,
+                               atol=1e-15)
     g = torch.from_numpy(np.random.default_rng(2).normal(size=len(mass))).cuda()
     (w * g).sum().backward()
     # finite differences of the FP64 numpy formula

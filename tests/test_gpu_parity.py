@@ -207,7 +207,8 @@ def test_marked_product_clustered_matches_oracle(gpu):
 # ---------------- batched mocks ----------------
 def _mocks(seed, sizes, L):
     rng = np.random.default_rng(seed)
-    return [clustered(rng, n, L, max(n // 20, 10)) for n in sizes]
+    return [clustered(rng, n, L, max(n // 20, 10)) if n >= 1000 else rng.uniform(0, L, (n, 3))
+            for n in sizes]
 
 
 @pytest.mark.parametrize("graph", [False, True])
