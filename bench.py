@@ -142,6 +142,136 @@ def run_cpu(w, x, steps, warmup, frac_side, threads):
     return pairs / dt, dt, len(sub)
 
 
+def _events():
+    import torch
+    return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+def extra_batched(dev, reps=3):
+    """Config 3: 64 Zheng07 mocks on a 1M-halo table (L = 1000, float32), npairs_3d
+    15 log bins 0.1-20: one batched launch vs one plain call per mock."""
+    import torch
+    from halotools_gb300 import BatchedCounter, mocks
+    from halotools_gb300 import _native as N
+    L = 1000.0
+    pos, mass, conc = mocks.halo_table(1_000_000, L, seed=11)
+    rng = np.random.default_rng(12)
+    lmin = rng.uniform(11.8, 12.4, 64)
+    thetas = np.stack([lmin, rng.uniform(0.2, 0.5, 64), lmin, lmin + 1.3,
+                       rng.uniform(0.9, 1.1, 64)], axis=1)
+    xyz, offs = mocks.hod_mocks_torch(pos, mass, conc, L, thetas, seed=13)
+    rb = np.logspace(-1, np.log10(20), 15)
+    bc = BatchedCounter(dev, graph=True, autotune=True)
+    stream = torch.cuda.current_stream(dev)
+    bc.plan.set_stream(stream.cuda_stream)
+    for _ in range(2):
+        out = bc.count_device(xyz, offs, rb, L)
+    pairs = int(out[:, -1].sum())
+    t = []
+    for _ in range(reps):
+        a, b = _events()
+        a.record(stream)
+        bc.count_device(xyz, offs, rb, L)
+        b.record(stream)
+        torch.cuda.synchronize()
+        t.append(a.elapsed_time(b) / 1e3)
+    tb = float(np.median(t))
+    st = bc.stats()
+    # plain path: one npairs_3d call per mock (FP64 positions on the device)
+    plan = N.Plan(dev)
+    plan.set_stream(stream.cuda_stream)
+    x64 = xyz.double()
+    box = np.array([L] * 3)
+    o1 = np.zeros(len(rb), dtype=np.int64)
+
+    def plain_all():
+        tot = 0
+        for m in range(len(offs) - 1):
+            lo, hi = int(offs[m]), int(offs[m + 1])
+            ptr = x64.data_ptr() + lo * 24
+            plan.check(plan.lib.gbp_npairs_3d(plan.handle, N.dptr_int(ptr), hi - lo, N.dptr_int(ptr),
+                                              hi - lo, N.pd(rb), len(rb), N.pd(box), 1,
+                                              N.GBP_MEM_DEVICE, N.pi64(o1)))
+            tot += int(o1[-1])
+        return tot
+    plain_all()
+    a, b = _events()
+    a.record(stream)
+    tot = plain_all()
+    b.record(stream)
+    torch.cuda.synchronize()
+    tp = a.elapsed_time(b) / 1e3
+    assert tot == pairs
+    return {"mocks": len(offs) - 1, "galaxies": int(offs[-1]),
+            "galaxies_per_mock": [int(offs[1] - offs[0]), int(np.max(np.diff(offs)))],
+            "in_range_pairs": pairs, "batched_pairs_per_s": pairs / tb, "batched_ms": tb * 1e3,
+            "plain_pairs_per_s": pairs / tp, "plain_ms": tp * 1e3, "speedup_vs_plain": tp / tb,
+            "reach": st["reach"], "graph": True, "autotune": True}
+
+
+def extra_differentiable(dev, reps=3):
+    """Config 4: 2M halos in L = 1000, Zheng07 weights at theta = (12, 0.3, 12, 13.3, 1),
+    weighted npairs_3d over 20 log bins 0.1-30, forward + hand-written backward."""
+    import torch
+    from halotools_gb300 import differentiable as D, mocks
+    L = 1000.0
+    pos, mass, _ = mocks.halo_table(2_000_000, L, seed=21)
+    rb = np.logspace(-1, np.log10(30), 20)
+    xd = torch.from_numpy(pos).cuda(dev)
+    md = torch.from_numpy(mass).cuda(dev)
+    gbar = torch.ones(len(rb), dtype=torch.float64, device=f"cuda:{dev}")
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        th = torch.tensor([12.0, 0.3, 12.0, 13.3, 1.0], dtype=torch.float64,
+                          device=f"cuda:{dev}", requires_grad=True)
+        C = D.hod_pair_counts(th, xd, md, rb, L)
+        (C * gbar).sum().backward()
+        return C, th.grad
+    step()
+    t = []
+    for _ in range(reps):
+        a, b = _events()
+        a.record(stream)
+        C, g = step()
+        b.record(stream)
+        torch.cuda.synchronize()
+        t.append(a.elapsed_time(b) / 1e3)
+    tfb = float(np.median(t))
+    import halotools_gb300 as H
+    pairs = int(H.npairs_3d(pos, pos, rb, period=L)[-1])
+    return {"halos": len(pos), "in_range_pairs": pairs, "fwd_bwd_ms": tfb * 1e3,
+            "pair_evals_per_s": 2 * pairs / tfb, "passes": 2,
+            "dC_dtheta_last_bin": [float(v) for v in g.cpu().numpy()]}
+
+
+def extra_npairs_3d_10m(dev, threads):
+    """Config 5 geometry: plain npairs_3d on 10M clustered points (L = 2000, 30 log bins
+    0.5-50) against the all-core CPU oracle on a 1/64-volume sub-cube."""
+    import torch
+    from halotools_gb300 import _native as N
+    w = WORKLOADS["3d10m"]
+    x = make_points(w)
+    xd = torch.from_numpy(x).cuda(dev)
+    plan = N.Plan(dev)
+    stream = torch.cuda.current_stream(dev)
+    plan.set_stream(stream.cuda_stream)
+    box = np.array([w["L"]] * 3)
+    out = np.zeros(len(w["bins"]), dtype=np.int64)
+    call_device(plan, "3d", xd, len(x), w, box, out)
+    a, b = _events()
+    a.record(stream)
+    call_device(plan, "3d", xd, len(x), w, box, out)
+    b.record(stream)
+    torch.cuda.synchronize()
+    tg = a.elapsed_time(b) / 1e3
+    gpu = int(out[-1]) / tg
+    cpu, dt, nsub = run_cpu(w, x, 1, 0, 0.25, threads)
+    return {"points": len(x), "gpu_pairs_per_s": gpu, "gpu_ms": tg * 1e3,
+            "cpu_pairs_per_s": cpu, "cpu_cores": threads, "cpu_sample_points": nsub,
+            "gpu_over_cpu": gpu / cpu}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -150,6 +280,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="xyz2m", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the batched / differentiable / 10M-point comparison paths")
     args = ap.parse_args()
     w = WORKLOADS[args.workload]
     rank = int(os.environ.get("RANK", "0"))
@@ -283,6 +415,16 @@ def main():
         line["cpu_baseline"] = {"value": v, "unit": "pairs/s", "cores": threads, "kind": "port",
                                 "sample": "%d points in the sub-cube [0, %.0f)^3, non-periodic, "
                                           "C oracle cell walk, %.1f s" % (nsub, frac_side * w["L"], dt)}
+    if rank == 0 and world == 1 and not args.no_extras:
+        extras = {}
+        for name, fn in (("batched_hod64", lambda: extra_batched(dev)),
+                         ("differentiable_2m", lambda: extra_differentiable(dev)),
+                         ("npairs_3d_10m", lambda: extra_npairs_3d_10m(dev, threads))):
+            try:
+                extras[name] = fn()
+            except Exception as exc:  # report, never hide
+                extras[name] = {"error": repr(exc)[:300]}
+        line["paths"] = extras
     if rank == 0:
         print(json.dumps(line))
     if world > 1:

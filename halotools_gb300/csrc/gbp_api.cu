@@ -684,11 +684,11 @@ int gbp_batched_npairs_3d(gbp_plan *plan, const void *xyz, int32_t xyz_f32, cons
     if (n == 0) return GBP_OK;
     // the grid follows the mean mock density
     const int64_t nmean = std::max<int64_t>(1, n / nmocks);
-    auto plan_geometry = [&](int reach) {
-        choose_grid(c.g, period3, search, pbc, nmean, reach, MAX_CELLS_PER_DIM);
+    auto plan_geometry = [&](int reach, double ppc) {
+        choose_grid(c.g, period3, search, pbc, nmean, reach, MAX_CELLS_PER_DIM, ppc);
         // cell keys of all mocks must fit an int
         while (c.g.ncells * nmocks >= (1ll << 31) - 1 && c.g.K > 1)
-            choose_grid(c.g, period3, search, pbc, nmean, c.g.K - 1, MAX_CELLS_PER_DIM);
+            choose_grid(c.g, period3, search, pbc, nmean, c.g.K - 1, MAX_CELLS_PER_DIM, ppc);
         build_stencil(c.g, search, 0, true);
         ErrModel em = err_model(c.g);
         std::vector<double> E(nb);
@@ -698,31 +698,36 @@ int gbp_batched_npairs_3d(gbp_plan *plan, const void *xyz, int32_t xyz_f32, cons
     };
     std::vector<unsigned long long> h;
     int reach = plan->reach;
+    double ppc = 0.0;
     if (plan->autotune && reach == 0) {
         char sig[256];
         snprintf(sig, sizeof(sig), "b3d:%d:%lld:%d:%.17g:%.17g:%.17g:%.17g:%d", nmocks, (long long)n,
                  nb, rmax, period3[0], period3[1], period3[2], pbc);
-        int found = 0;
-        for (auto &t : plan->tuned)
-            if (t.first == sig) found = t.second;
-        if (!found) {
+        int found = -1;
+        for (size_t t = 0; t < plan->tuned.size(); t++)
+            if (plan->tuned[t].first == sig) found = plan->tuned[t].second;
+        // candidates: (reach, points per cell for coarse reach-1 grids)
+        static const int RK[6] = {1, 1, 1, 1, 2, 3};
+        static const double PPC[6] = {-1.0, 16.0, 32.0, 64.0, 0.0, 0.0};
+        if (found < 0) {
             float best = 1e30f;
-            int bestK = 1;
-            for (int K = 1; K <= 3; K++) {
-                plan_geometry(K);
-                if (c.g.K != K) continue;  // not feasible
+            int bi = 0;
+            for (int q = 0; q < 6; q++) {
+                plan_geometry(RK[q], PPC[q]);
+                if (c.g.K != RK[q]) continue;  // not feasible
                 if ((rc = run_call(plan, c, h))) return rc;
-                if (plan->stats.ms_count < best) {
-                    best = plan->stats.ms_count;
-                    bestK = K;
+                if (plan->stats.ms_count + plan->stats.ms_build < best) {
+                    best = plan->stats.ms_count + plan->stats.ms_build;
+                    bi = q;
                 }
             }
-            plan->tuned.emplace_back(sig, bestK);
-            found = bestK;
+            plan->tuned.emplace_back(sig, bi);
+            found = bi;
         }
-        reach = found;
+        reach = RK[found];
+        ppc = PPC[found];
     }
-    plan_geometry(reach);
+    plan_geometry(reach, ppc);
     if (c.g.ncells * nmocks >= (1ll << 31) - 1)
         return fail(plan, GBP_ERR_INVALID, "too many mocks for one batched grid");
     if ((rc = run_call(plan, c, h))) return rc;

@@ -215,8 +215,11 @@ inline bool grid_for_reach(int K, const double L[3], const double search[3], int
 // Reach K in 1..4 (hint > 0 forces it when feasible); the automatic choice
 // keeps about 28+ points of sample 2 per cell: finer cells prune more of the
 // cube stencil, but each work item then streams fewer points per i-point.
+// Sparse samples (fewer than ~12 points per reach-1 cell) get cells larger
+// than the search length, about `ppc` points each (default 24): per-item
+// set-up then amortises over enough pairs.  ppc < 0 disables coarsening.
 inline void choose_grid(Geometry &g, const double L[3], const double search[3], int pbc,
-                        int64_t n2, int reach_hint, int64_t cap_per_dim) {
+                        int64_t n2, int reach_hint, int64_t cap_per_dim, double ppc = 0.0) {
     for (int d = 0; d < 3; d++) g.L[d] = L[d];
     g.pbc = pbc;
     double vol = L[0] * L[1] * L[2];
@@ -234,6 +237,18 @@ inline void choose_grid(Geometry &g, const double L[3], const double search[3], 
     }
     int64_t n[3];
     grid_for_reach(best, L, search, pbc, n, cap_per_dim);
+    if (best == 1 && ppc >= 0.0 && rho > 0) {
+        double cvol = (L[0] / n[0]) * (L[1] / n[1]) * (L[2] / n[2]);
+        double want = ppc > 0.0 ? ppc : 24.0;
+        if (ppc > 0.0 || rho * cvol < 12.0) {
+            double ct = std::cbrt(want / rho);
+            for (int d = 0; d < 3; d++) {
+                int64_t m = (int64_t)std::floor(L[d] / ct);
+                m = std::max<int64_t>(m, pbc ? 3 : 1);
+                n[d] = std::min(n[d], m);  // never finer than the reach-1 grid
+            }
+        }
+    }
     g.K = best;
     g.ncells = 1;
     for (int d = 0; d < 3; d++) {
