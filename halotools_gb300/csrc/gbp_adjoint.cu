@@ -22,6 +22,7 @@ __device__ __noinline__ float slow_adj(float v, int b0, int is, int js, const fl
                                        const AxisSm &A, const CountArgs &a) {
     int k = walk_bin(v, b0, A);
     if (k >= 0) return gt[k];
+    if (is < 0 || js < 0) return 0.f;  // never a real pair
     atomicAdd(a.nrecheck, 1ull);
     const double *p = a.x64_1 + 3 * (int64_t)is;
     const double *q = a.x64_2 + 3 * (int64_t)js;
@@ -30,25 +31,24 @@ __device__ __noinline__ float slow_adj(float v, int b0, int is, int js, const fl
     return 0.5f * (gt[k1] + gt[k2]);
 }
 
-__global__ void __launch_bounds__(GBP_BLOCK, 3) k_adjoint(const CountArgs a) {
+// Warp-centric like the count kernel: each warp pulls (cell chunk, stencil
+// group) items, two i-points per lane, 32 j-points per step; the partial
+// gradient of an i-point over one item is added to dL/dw (zeroed first).
+__global__ void __launch_bounds__(GBP_BLOCK, 2) k_adjoint(const CountArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
+    constexpr unsigned FULL = 0xffffffffu;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nb0 = a.ax[0].nb, T0 = a.ax[0].T;
-    const SmemLayout L = gbp_smem_layout(MODE_ADJ, T0, 0, nb0, 0, a.nsten, 1, 4);
+    const SmemLayout L = gbp_smem_layout(MODE_ADJ, T0, 0, nb0, 0, a.nsten, 0, 4);
     float4 *s_lut0 = (float4 *)(smem + L.off_lut0);
-    float4 *s_j = (float4 *)(smem + L.off_j);
-    float *s_jw = (float *)(smem + L.off_jw);
+    float4 *jb = (float4 *)(smem + L.off_j) + warp * 32;
+    float *jw = (float *)(smem + L.off_jw) + warp * 32;
     float4 *s_D = (float4 *)(smem + L.off_D);
     double *s_E0 = (double *)(smem + L.off_E0);
     float *s_hi0 = (float *)(smem + L.off_hi0);
     float *s_lo0 = (float *)(smem + L.off_lo0);
     int *s_off = (int *)(smem + L.off_off);
-    int *s_cstart = (int *)(smem + L.off_cstart);
-    int *s_pre = (int *)(smem + L.off_pre);
-    float2 *s_part = (float2 *)(smem + L.off_hist);
     float *s_gt = (float *)(smem + L.off_hist + GBP_BLOCK * 8);
-    __shared__ int s_item;
-    __shared__ int s_nitems;
 
     for (int i = tid; i < T0; i += GBP_BLOCK) s_lut0[i] = a.ax[0].lut[i];
     for (int i = tid; i < nb0; i += GBP_BLOCK) {
@@ -61,125 +61,116 @@ __global__ void __launch_bounds__(GBP_BLOCK, 3) k_adjoint(const CountArgs a) {
         s_off[i] = a.sten[i];
         s_D[i] = a.stenD[i];
     }
-    if (tid == 0) s_nitems = *a.nitems;
     AxisSm A0{s_lut0, s_hi0, s_lo0, s_E0, nb0, a.ax[0].S, a.ax[0].B, a.ax[0].vlo, a.ax[0].vhi};
+    const int nitems = *a.nitems;
     const int n0 = a.n[0], n1 = a.n[1], n2 = a.n[2];
     const float top0 = a.top0;
     unsigned long long cand = 0;
     __syncthreads();
 
     while (true) {
-        if (tid == 0) s_item = atomicAdd(a.counter, 1);
-        __syncthreads();
-        const int it = s_item;
-        if (it >= s_nitems) break;
+        int it = 0;
+        if (lane == 0) it = atomicAdd(a.counter, 1);
+        it = __shfl_sync(FULL, it, 0);
+        if (it >= nitems) break;
         const int4 item = a.items[it];
-        const int cell = item.x, ifirst = item.y, icnt = item.z;
+        const int cell = item.x, ifirst = item.y;
+        const int icnt = item.z & 127, s0 = (item.z >> 7) & 1023, s1 = (item.z >> 17) & 1023;
         const int cz = cell % n2, cy = (cell / n2) % n1, cx = cell / (n1 * n2);
-        for (int s = tid; s < a.nsten; s += GBP_BLOCK) {
-            int pk = s_off[s];
-            int x = cx + (pk & 255) - 64, y = cy + ((pk >> 8) & 255) - 64,
-                z = cz + ((pk >> 16) & 255) - 64;
-            bool ok = true;
-            if (a.pbc) {
-                x = x < 0 ? x + n0 : (x >= n0 ? x - n0 : x);
-                y = y < 0 ? y + n1 : (y >= n1 ? y - n1 : y);
-                z = z < 0 ? z + n2 : (z >= n2 ? z - n2 : z);
-            } else {
-                ok = x >= 0 && x < n0 && y >= 0 && y < n1 && z >= 0 && z < n2;
-            }
+        float4 u0 = make_float4(GBP_FAR, GBP_FAR, GBP_FAR, __int_as_float(0));
+        float4 u1 = u0;
+        if (lane < icnt) u0 = a.pos1[ifirst + lane];
+        if (lane + 32 < icnt) u1 = a.pos1[ifirst + 32 + lane];
+        float acc0 = 0.f, cmp0 = 0.f, acc1 = 0.f, cmp1 = 0.f;  // Kahan: sum ~ acc - cmp
+        for (int sb = s0; sb < s1; sb += 32) {
+            const int s = sb + lane;
             int st = 0, cn = 0;
-            if (ok) {
-                int c2 = (x * n1 + y) * n2 + z;
-                st = a.start2[c2];
-                cn = a.start2[c2 + 1] - st;
+            float4 D = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (s < s1) {
+                const int pk = s_off[s];
+                int x = cx + (pk & 255) - 64, y = cy + ((pk >> 8) & 255) - 64,
+                    z = cz + ((pk >> 16) & 255) - 64;
+                bool ok = true;
+                if (a.pbc) {
+                    x = x < 0 ? x + n0 : (x >= n0 ? x - n0 : x);
+                    y = y < 0 ? y + n1 : (y >= n1 ? y - n1 : y);
+                    z = z < 0 ? z + n2 : (z >= n2 ? z - n2 : z);
+                } else {
+                    ok = x >= 0 && x < n0 && y >= 0 && y < n1 && z >= 0 && z < n2;
+                }
+                if (ok) {
+                    const int c2 = (x * n1 + y) * n2 + z;
+                    st = a.start2[c2];
+                    cn = a.start2[c2 + 1] - st;
+                }
+                D = s_D[s];
             }
-            s_cstart[s] = st;
-            s_pre[s] = cn;
-        }
-        __syncthreads();
-        if (warp == 0) {
-            int carry = 0;
-            for (int b = 0; b < a.nsten; b += 32) {
-                int idx = b + lane;
-                int v = idx < a.nsten ? s_pre[idx] : 0;
-                int incl = v;
+            int incl = cn;
 #pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    int t = __shfl_up_sync(0xffffffffu, incl, o);
-                    if (lane >= o) incl += t;
-                }
-                if (idx < a.nsten) s_pre[idx] = carry + incl - v;
-                carry += __shfl_sync(0xffffffffu, incl, 31);
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(FULL, incl, o);
+                if (lane >= o) incl += t;
             }
-            if (lane == 0) s_pre[a.nsten] = carry;
-        }
-        __syncthreads();
-        const int total = s_pre[a.nsten];
-        const int wpg = (icnt + 31) >> 5;
-        const int G = GBP_WARPS / wpg;
-        const int grp = warp / wpg;
-        const int within = (warp % wpg) * 32 + lane;
-        const bool in_group = grp < G;
-        float4 ui = make_float4(GBP_FAR, GBP_FAR, GBP_FAR, __int_as_float(0));
-        if (in_group && within < icnt) ui = a.pos1[ifirst + within];
-        float acc = 0.f, comp = 0.f;  // Kahan: true sum ~ acc - comp
-        cand += (unsigned long long)icnt * (unsigned long long)total;
-
-        for (int base = 0; base < total; base += GBP_JCAP) {
-            const int len = min(GBP_JCAP, total - base);
-            for (int f = tid; f < len; f += GBP_BLOCK) {
-                const int g = base + f;
-                int lo = 0, hi = a.nsten - 1;
-                while (lo < hi) {
-                    int mid = (lo + hi + 1) >> 1;
-                    if (s_pre[mid] <= g) lo = mid; else hi = mid - 1;
+            const int T = __shfl_sync(FULL, incl, 31);
+            cand += (unsigned long long)icnt * (unsigned long long)T;
+            for (int f0 = 0; f0 < T; f0 += 32) {
+                const int f = f0 + lane;
+                int k = 0;
+#pragma unroll
+                for (int step = 16; step > 0; step >>= 1) {
+                    const int v = __shfl_sync(FULL, incl, k + step - 1);
+                    if (v <= f) k += step;
                 }
-                const int j = s_cstart[lo] + (g - s_pre[lo]);
-                float4 p = a.pos2[j];
-                float4 D = s_D[lo];
-                s_j[f] = make_float4(p.x + D.x, p.y + D.y, p.z + D.z, p.w);
-                s_jw[f] = a.w2[j];
-            }
-            __syncthreads();
-            if (in_group) {
-#pragma unroll 2
-                for (int jj = grp; jj < len; jj += G) {
-                    const float4 t = s_j[jj];
-                    const float dx = ui.x - t.x, dy = ui.y - t.y, dz = ui.z - t.z;
-                    const float v = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-                    if (__any_sync(0xffffffffu, v <= top0)) {
-                        float4 e = lut_entry(v, A0);
-                        int b = __float_as_int(e.x) + (v > e.y ? 1 : 0);
-                        float gv;
-                        if ((v > e.z) & !(v > e.y))
-                            gv = slow_adj(v, __float_as_int(e.x), __float_as_int(ui.w),
-                                          __float_as_int(t.w), s_gt, A0, a);
-                        else
-                            gv = s_gt[b];
-                        const float y = fmaf(s_jw[jj], gv, -comp);
-                        const float s2 = acc + y;
-                        comp = (s2 - acc) - y;
-                        acc = s2;
+                k &= 31;
+                const int stk = __shfl_sync(FULL, st, k);
+                const int exk = __shfl_sync(FULL, incl - cn, k);
+                const float Dx = __shfl_sync(FULL, D.x, k), Dy = __shfl_sync(FULL, D.y, k),
+                            Dz = __shfl_sync(FULL, D.z, k);
+                if (f < T) {
+                    const int j = stk + (f - exk);
+                    const float4 p = a.pos2[j];
+                    jb[lane] = make_float4(p.x + Dx, p.y + Dy, p.z + Dz, p.w);
+                    jw[lane] = a.w2[j];
+                }
+                __syncwarp();
+                const int nj = min(32, T - f0);
+                for (int jj = 0; jj < nj; jj++) {
+                    const float4 t = jb[jj];
+                    const float dx0 = u0.x - t.x, dy0 = u0.y - t.y, dz0 = u0.z - t.z;
+                    const float dx1 = u1.x - t.x, dy1 = u1.y - t.y, dz1 = u1.z - t.z;
+                    const float v0 = fmaf(dz0, dz0, fmaf(dy0, dy0, dx0 * dx0));
+                    const float v1 = fmaf(dz1, dz1, fmaf(dy1, dy1, dx1 * dx1));
+                    if (__any_sync(FULL, (v0 <= top0) | (v1 <= top0))) {
+                        const float wj = jw[jj];
+                        float4 e = lut_entry(v0, A0);
+                        int b = __float_as_int(e.x) + (v0 > e.y ? 1 : 0);
+                        float g0 = ((v0 > e.z) & !(v0 > e.y))
+                                       ? slow_adj(v0, __float_as_int(e.x), __float_as_int(u0.w),
+                                                  __float_as_int(t.w), s_gt, A0, a)
+                                       : s_gt[b];
+                        e = lut_entry(v1, A0);
+                        b = __float_as_int(e.x) + (v1 > e.y ? 1 : 0);
+                        float g1 = ((v1 > e.z) & !(v1 > e.y))
+                                       ? slow_adj(v1, __float_as_int(e.x), __float_as_int(u1.w),
+                                                  __float_as_int(t.w), s_gt, A0, a)
+                                       : s_gt[b];
+                        float y = fmaf(wj, g0, -cmp0), s2 = acc0 + y;
+                        cmp0 = (s2 - acc0) - y;
+                        acc0 = s2;
+                        y = fmaf(wj, g1, -cmp1);
+                        s2 = acc1 + y;
+                        cmp1 = (s2 - acc1) - y;
+                        acc1 = s2;
                     }
                 }
+                __syncwarp();
             }
-            __syncthreads();
         }
-        // reduce the j-groups of this item and write dL/dw in the caller's order
-        s_part[tid] = make_float2(acc, comp);
-        __syncthreads();
-        if (in_group && grp == 0 && within < icnt) {
-            double sum = 0.0;
-            for (int g2 = 0; g2 < G; g2++) {
-                float2 pc = s_part[(g2 * wpg + (warp % wpg)) * 32 + lane];
-                sum += (double)pc.x - (double)pc.y;
-            }
-            a.grad[a.orig[ifirst + within]] = 2.0 * sum;
-        }
-        __syncthreads();
+        if (lane < icnt) atomicAdd(&a.grad[a.orig[ifirst + lane]], 2.0 * ((double)acc0 - (double)cmp0));
+        if (lane + 32 < icnt)
+            atomicAdd(&a.grad[a.orig[ifirst + 32 + lane]], 2.0 * ((double)acc1 - (double)cmp1));
     }
-    if (tid == 0 && cand) atomicAdd(a.nrecheck + 1, cand);
+    if (lane == 0 && cand) atomicAdd(a.nrecheck + 1, cand);
 }
 
 cudaError_t gbp_launch_adjoint(const CountArgs &a, int grid, size_t smem, cudaStream_t st) {

@@ -41,6 +41,7 @@ struct gbp_plan {
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     bool graph_mode = false;          // capture each call into a CUDA graph and replay it
     bool autotune = false;            // time the feasible reaches on a new workload shape
+    size_t item_cap = 0;              // work-item capacity learned from an overflow
     std::vector<std::pair<std::string, int>> tuned;  // workload signature -> best reach
     cudaGraphExec_t gexec = nullptr;  // reused (updated in place) across calls
     gbp_stats stats;
@@ -220,7 +221,12 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
     }
     size_t scan_ints = gbp_scan_tmp_ints(nkeys + 1);
     size_t o_scan = cv.take<int>(scan_ints);
-    size_t max_items = (size_t)nkeys + (size_t)(c.n1 / GBP_TI) + 16;
+    // work items: i-chunks of GBP_TI times stencil groups of <= GBP_JCAP_ITEM
+    // j-points; the builder flags an overflow and the call is repeated larger
+    size_t max_items = std::max<size_t>(
+        plan->item_cap,
+        2 * ((size_t)nkeys + (size_t)(c.n1 / GBP_TI)) +
+            (size_t)nsten * (size_t)(c.n2 / GBP_JCAP_ITEM) + 65536);
     size_t o_items = cv.take<int4>(max_items);
     size_t o_itmp = cv.take<int>(2 * ((size_t)nkeys + 2));
     size_t o_offs = cv.take<int64_t>((size_t)nm + 1);
@@ -365,7 +371,18 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
                                             sd[s].w64, d_err, st, &launches);
             CK(e);
         }
-        CK(gbp_build_items(sd[0].start, nkeys, at<int4>(W, o_items), d_nitems, at<int>(W, o_itmp),
+        ItemPlan ip;
+        ip.start1 = sd[0].start;
+        ip.start2 = (c.autocorr ? sd[0] : sd[1]).start;
+        ip.nkeys = nkeys;
+        ip.ncm = (int)ncells;
+        for (int d = 0; d < 3; d++) ip.n[d] = c.g.n[d];
+        ip.pbc = c.g.pbc;
+        ip.sten = at<int>(W, o_sten);
+        ip.nsten = nsten;
+        ip.jcap = GBP_JCAP_ITEM;
+        CK(gbp_build_items(ip, at<int4>(W, o_items), (int)std::min<size_t>(max_items, INT32_MAX),
+                           d_nitems, reinterpret_cast<int *>(misc) + 3, at<int>(W, o_itmp),
                            at<int>(W, o_scan), st, &launches));
         CK(cudaMemsetAsync(at<char>(W, o_hist), 0, nm * nhist * sizeof(unsigned long long), st));
         CK(cudaMemsetAsync(at<char>(W, o_histd), 0, nm * nhist * sizeof(double), st));
@@ -421,14 +438,12 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
         a.top1 = c.naxes > 1 ? std::min(c.ax[1].hi[nb1 - 1], 1.0e30f) : 0.f;
         a.self_bin = host_bin(nb0, c.ax[0].E.data(), 0.0);
         const int jwb = c.mode == MODE_MARK ? (c.wf == 0 ? 8 * c.nw : 4) : (c.mode == MODE_ADJ ? 4 : 0);
-        // shared histogram copies (2-D and wide 1-D): as many as keep the CTA
-        // within ~72 KB of shared memory (3 CTAs per SM), at least one
-        int copies = 1;
+        // 2-D and wide 1-D histograms: one shared copy per warp while they fit,
+        // else the warps add straight into the global histogram
+        int copies = GBP_WARPS;
         if (c.mode != MODE_3D && c.mode != MODE_MARK && c.mode != MODE_ADJ) {
-            for (int cp = GBP_WARPS; cp >= 1; cp /= 2) {
-                copies = cp;
-                if (gbp_smem_layout(c.mode, T0, T1, nb0, nb1, nsten, cp, jwb).total <= (72 << 10)) break;
-            }
+            size_t one = (size_t)(nb0 + 1) * (size_t)(c.naxes > 1 ? nb1 + 1 : 1) * 4;
+            if (one * GBP_WARPS > (96u << 10)) copies = 0;
         }
         a.hist_copies = copies;
         SmemLayout L = gbp_smem_layout(c.mode, T0, T1, nb0, nb1, nsten, copies, jwb);
@@ -441,6 +456,7 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
         int occ = adj ? gbp_adjoint_occupancy(smem) : gbp_count_occupancy(c.mode, c.wf, smem);
         if (occ <= 0) return fail(plan, GBP_ERR_INVALID, "count kernel does not fit (smem %zu B)", smem);
         int grid = plan->nsm * occ;
+        if (adj) CK(cudaMemsetAsync(a.grad, 0, sizeof(double) * (size_t)c.n1, st));
         if (adj) CK(gbp_launch_adjoint(a, grid, smem, st));
         else CK(gbp_launch_count(c.mode, c.wf, a, grid, smem, st));
         if (adj && c.mem == GBP_MEM_HOST && c.n1 > 0) {
@@ -492,6 +508,13 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
     const unsigned long long *hm = at<unsigned long long>(H, h_misc);
     int err_word = reinterpret_cast<const int *>(hm)[2];
     if (err_word) return fail(plan, GBP_ERR_RANGE, "positions outside [0, period] or not finite");
+    if (reinterpret_cast<const int *>(hm)[3]) {
+        // more work items than the estimate: grow and repeat the call
+        if (max_items >= (size_t)INT32_MAX / 2)
+            return fail(plan, GBP_ERR_NOMEM, "too many work items");
+        plan->item_cap = 2 * max_items;
+        return run_call(plan, c, hist_host, histd_host);
+    }
     hist_host.assign(at<unsigned long long>(H, h_hist), at<unsigned long long>(H, h_hist) + nm * nhist);
     if (c.mode != MODE_MARK) add_self_pairs(c, hist_host);
     if (histd_host) histd_host->assign(at<double>(H, h_histd), at<double>(H, h_histd) + nm * nhist);

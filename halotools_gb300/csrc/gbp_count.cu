@@ -46,6 +46,10 @@ __device__ __noinline__ int slow_3d(float v, int b0, int is, int js, bool sym, i
         k[0] = kk;
         return 0;
     }
+    if (is < 0 || js < 0) {  // never a real pair (idle lane or padding)
+        k[0] = A.nb;
+        return 0;
+    }
     atomicAdd(a.nrecheck, 1ull);
     const double *p = a.x64_1 + 3 * (int64_t)is;
     const double *q = a.x64_2 + 3 * (int64_t)js;
@@ -55,8 +59,8 @@ __device__ __noinline__ int slow_3d(float v, int b0, int is, int js, bool sym, i
     return 2;
 }
 
-template <bool LANE>
-__device__ __forceinline__ void bin_3d(const float4 &e, unsigned *h, const AxisSm &A,
+template <bool LANE, class HT>
+__device__ __forceinline__ void bin_3d(const float4 &e, HT *h, const AxisSm &A,
                                        const CountArgs &a) {
     const float v = e.x;
     const unsigned jw = __float_as_uint(e.w);
@@ -73,13 +77,13 @@ __device__ __forceinline__ void bin_3d(const float4 &e, unsigned *h, const AxisS
         } else {
             for (int q = 0; q < n; q++) {
                 if (LANE) h[k[q] * 32] += 1u;
-                else if (k[q] < A.nb) atomicAdd(&h[k[q]], 1u);
+                else if (k[q] < A.nb) atomicAdd(&h[k[q]], (HT)1);
             }
             return;
         }
     }
     if (LANE) h[b * 32] += w;
-    else if (b < A.nb) atomicAdd(&h[b], w);
+    else if (b < A.nb) atomicAdd(&h[b], (HT)w);
 }
 
 // ---------------- stage 2: marked (Kahan in lane-private FP32 pairs) ----------------
@@ -114,30 +118,33 @@ __device__ __forceinline__ void bin_mark(const float4 &e, float *hs, float *hc, 
 }
 
 // ---------------- stage 2: (rp, pi) ----------------
+template <class HT>
 __device__ __noinline__ void slow_xyz(float v0, float v1, int b0a, int b0b, int is, int js,
-                                      bool sym, unsigned *hw, int stride, const AxisSm &A,
+                                      bool sym, HT *hw, int stride, const AxisSm &A,
                                       const AxisSm &Bx, const CountArgs &a) {
     int ka = walk_bin(v0, b0a, A);
     int kb = walk_bin(v1, b0b, Bx);
     if (ka >= 0 && kb >= 0) {
-        if (ka < A.nb && kb < Bx.nb) atomicAdd(&hw[ka * stride + kb], sym ? 2u : 1u);
+        if (ka < A.nb && kb < Bx.nb) atomicAdd(&hw[ka * stride + kb], (HT)(sym ? 2 : 1));
         return;
     }
+    if (is < 0 || js < 0) return;  // never a real pair (idle lane or padding)
     atomicAdd(a.nrecheck, 1ull);
     const double *p = a.x64_1 + 3 * (int64_t)is;
     const double *q = a.x64_2 + 3 * (int64_t)js;
     Exact3 r = exact_pair(p, q, a);
     int ea = ka >= 0 ? ka : exact_bin(r.dxy, b0a, A);
     int eb = kb >= 0 ? kb : exact_bin(r.dz2, b0b, Bx);
-    if (ea < A.nb && eb < Bx.nb) atomicAdd(&hw[ea * stride + eb], 1u);
+    if (ea < A.nb && eb < Bx.nb) atomicAdd(&hw[ea * stride + eb], (HT)1);
     if (!sym) return;
     Exact3 s = exact_pair(q, p, a);
     int fa = ka >= 0 ? ka : exact_bin(s.dxy, b0a, A);
     int fb = kb >= 0 ? kb : exact_bin(s.dz2, b0b, Bx);
-    if (fa < A.nb && fb < Bx.nb) atomicAdd(&hw[fa * stride + fb], 1u);
+    if (fa < A.nb && fb < Bx.nb) atomicAdd(&hw[fa * stride + fb], (HT)1);
 }
 
-__device__ __forceinline__ void bin_xyz(const float4 &e, unsigned *hw, int stride, const AxisSm &A,
+template <class HT>
+__device__ __forceinline__ void bin_xyz(const float4 &e, HT *hw, int stride, const AxisSm &A,
                                         const AxisSm &Bx, const CountArgs &a) {
     const float v0 = e.x, v1 = e.y;
     const unsigned jw = __float_as_uint(e.w);
@@ -152,14 +159,15 @@ __device__ __forceinline__ void bin_xyz(const float4 &e, unsigned *hw, int strid
                  (int)(jw & ~SYM_BIT), sym, hw, stride, A, Bx, a);
         return;
     }
-    if ((ba < A.nb) & (bb < Bx.nb)) atomicAdd(&hw[ba * stride + bb], sym ? 2u : 1u);
+    if ((ba < A.nb) & (bb < Bx.nb)) atomicAdd(&hw[ba * stride + bb], (HT)(sym ? 2 : 1));
 }
 
 // ---------------- stage 2: (s, mu') ----------------
 // v = s^2 on axis 0; q = dxy / s^2 on axis 1, whose FP32 error depends on s:
 // the s table's 4th field holds the q error bound for the slot's smallest s.
+template <class HT>
 __device__ __noinline__ void slow_smu(float v, float q, float qb, int b0s, int is, int js,
-                                      bool sym, unsigned *hw, int stride, const AxisSm &A,
+                                      bool sym, HT *hw, int stride, const AxisSm &A,
                                       const AxisSm &Q, const CountArgs &a) {
     int ks = walk_bin(v, b0s, A);
     int kq = -1;
@@ -170,9 +178,10 @@ __device__ __noinline__ void slow_smu(float v, float q, float qb, int b0s, int i
     }
     if (ks >= A.nb) return;  // beyond the s gate: never counted
     if (ks >= 0 && kq >= 0) {
-        if (kq < Q.nb) atomicAdd(&hw[ks * stride + kq], sym ? 2u : 1u);
+        if (kq < Q.nb) atomicAdd(&hw[ks * stride + kq], (HT)(sym ? 2 : 1));
         return;
     }
+    if (is < 0 || js < 0) return;  // never a real pair (idle lane or padding)
     atomicAdd(a.nrecheck, 1ull);
     const double *p = a.x64_1 + 3 * (int64_t)is;
     const double *qq = a.x64_2 + 3 * (int64_t)js;
@@ -183,11 +192,12 @@ __device__ __noinline__ void slow_smu(float v, float q, float qb, int b0s, int i
         double mu2 = (r.s2 > 0.0) ? __ddiv_rn(r.dxy, r.s2) : 0.0;
         int eq = exact_bin(mu2, 0, Q);
         if (eq >= Q.nb) continue;
-        atomicAdd(&hw[es * stride + eq], 1u);
+        atomicAdd(&hw[es * stride + eq], (HT)1);
     }
 }
 
-__device__ __forceinline__ void bin_smu(const float4 &e, unsigned *hw, int stride, const AxisSm &A,
+template <class HT>
+__device__ __forceinline__ void bin_smu(const float4 &e, HT *hw, int stride, const AxisSm &A,
                                         const AxisSm &Q, const CountArgs &a) {
     const float v = e.x, dxy = e.y;
     const unsigned jw = __float_as_uint(e.w);
@@ -209,7 +219,7 @@ __device__ __forceinline__ void bin_smu(const float4 &e, unsigned *hw, int strid
                  hw, stride, A, Q, a);
         return;
     }
-    if (bq < Q.nb) atomicAdd(&hw[bs * stride + bq], sym ? 2u : 1u);
+    if (bq < Q.nb) atomicAdd(&hw[bs * stride + bq], (HT)(sym ? 2 : 1));
 }
 
 // ---------------- marking functions (marking_functions.pyx:21-218) ----------------
@@ -256,24 +266,28 @@ __device__ __forceinline__ double wfunc64(int id, const double *A, const double 
 }
 
 // ---------------- kernel ----------------
+// Warp-centric: every warp independently pulls items, loads the i-points of
+// its item (two per lane), walks the item's stencil group 32 j-points at a
+// time through a per-warp buffer and feeds its own queue.  There is no CTA
+// barrier in the main loop; the CTA only shares the read-only tables.
 template <int MODE, int WF>
-__global__ void __launch_bounds__(GBP_BLOCK, 3) k_count(const CountArgs a) {
+__global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     constexpr bool TWO = (MODE == MODE_XYZ || MODE == MODE_SMU);
     constexpr bool MARK = (MODE == MODE_MARK);
+    constexpr unsigned FULL = 0xffffffffu;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nb0 = a.ax[0].nb, nb1 = TWO ? a.ax[1].nb : 0;
     const int T0 = a.ax[0].T, T1 = TWO ? a.ax[1].T : 0;
-    const int copies = a.hist_copies;
+    const int copies = a.hist_copies;  // 2-D / wide: GBP_WARPS (one per warp) or 0 (global)
     const int nw = MARK ? a.nw : 0;
     const int jwb = MARK ? (WF == 0 ? 8 * nw : 4) : 0;
     const SmemLayout L = gbp_smem_layout(MODE, T0, T1, nb0, nb1, a.nsten, copies, jwb);
     float4 *s_lut0 = (float4 *)(smem + L.off_lut0);
     float4 *s_lut1 = (float4 *)(smem + L.off_lut1);
-    float4 *s_j = (float4 *)(smem + L.off_j);
-    float *s_jw = (float *)(smem + L.off_jw);
-    double *s_jw64 = (double *)(smem + L.off_jw);
-    float4 *s_q = (float4 *)(smem + L.off_q) + warp * GBP_QCAP;
+    float4 *jb = (float4 *)(smem + L.off_j) + warp * 32;
+    float *jw = (float *)(smem + L.off_jw) + warp * 32;
+    double *jw64 = (double *)(smem + L.off_jw) + warp * 32 * (nw > 0 ? nw : 1);
     float4 *s_D = (float4 *)(smem + L.off_D);
     double *s_E0 = (double *)(smem + L.off_E0);
     double *s_E1 = (double *)(smem + L.off_E1);
@@ -282,11 +296,13 @@ __global__ void __launch_bounds__(GBP_BLOCK, 3) k_count(const CountArgs a) {
     float *s_hi1 = (float *)(smem + L.off_hi1);
     float *s_lo1 = (float *)(smem + L.off_lo1);
     int *s_off = (int *)(smem + L.off_off);
-    int *s_cstart = (int *)(smem + L.off_cstart);
-    int *s_pre = (int *)(smem + L.off_pre);
     unsigned *s_hist = (unsigned *)(smem + L.off_hist);
-    __shared__ int s_item;
-    __shared__ int s_nitems;
+    // this warp's 64 i-points (and their weights) for stage 2
+    float4 *s_u = (float4 *)(smem + L.off_q) + warp * 64;
+    float *s_uw = (float *)(smem + L.off_q + GBP_WARPS * 64 * 16) + warp * 64;
+    double *s_uw64 = (double *)(smem + L.off_q + GBP_WARPS * 64 * 16) + warp * 64 * (nw > 0 ? nw : 1);
+    // this warp's pair codes of one 32-point j batch: at most 64 x 32
+    unsigned short *s_code = (unsigned short *)(smem + L.off_code) + warp * 2048;
 
     for (int i = tid; i < T0; i += GBP_BLOCK) s_lut0[i] = a.ax[0].lut[i];
     for (int i = tid; i < T1; i += GBP_BLOCK) s_lut1[i] = a.ax[1].lut[i];
@@ -305,248 +321,305 @@ __global__ void __launch_bounds__(GBP_BLOCK, 3) k_count(const CountArgs a) {
         s_D[i] = a.stenD[i];
     }
     const int nbin = (nb0 + 1) * (TWO ? nb1 + 1 : 1);
-    const int hist_words = (MODE == MODE_3D) ? GBP_WARPS * (nb0 + 1) * 32
-                         : MARK ? GBP_WARPS * (nb0 + 1) * 32 * 2 : copies * nbin;
-    for (int i = tid; i < hist_words; i += GBP_BLOCK) s_hist[i] = 0u;
-    if (tid == 0) s_nitems = *a.nitems;
-
+    // this warp's histogram words: lane-private (3-D, marked) or its own copy
+    const int warp_words = (MODE == MODE_3D) ? (nb0 + 1) * 32 : MARK ? (nb0 + 1) * 32 * 2
+                                                                : (copies ? nbin : 0);
+    unsigned *wh = s_hist + warp * warp_words;
+    for (int i = lane; i < warp_words; i += 32) wh[i] = 0u;
     AxisSm A0{s_lut0, s_hi0, s_lo0, s_E0, nb0, a.ax[0].S, a.ax[0].B, a.ax[0].vlo, a.ax[0].vhi};
     AxisSm A1{s_lut1, s_hi1, s_lo1, s_E1, nb1, TWO ? a.ax[1].S : 0, TWO ? a.ax[1].B : 0,
               TWO ? a.ax[1].vlo : 0.f, TWO ? a.ax[1].vhi : 0.f};
     const int stride2 = nb1 + 1;
-    unsigned *hl = s_hist + warp * (nb0 + 1) * 32 + lane;          // 1-D: lane-private column
-    float *hs = (float *)s_hist + warp * (nb0 + 1) * 32 + lane;     // marked: sums
-    float *hc = hs + GBP_WARPS * (nb0 + 1) * 32;                    // marked: compensations
-    unsigned *hw = s_hist + (warp % copies) * nbin;                // shared copy of this warp
+    unsigned *hl = wh + lane;                       // 1-D: lane-private column
+    float *hs = (float *)wh + lane;                 // marked: sums
+    float *hc = hs + (nb0 + 1) * 32;                // marked: compensations
+    const int nitems = *a.nitems;
     const int n0 = a.n[0], n1 = a.n[1], n2 = a.n[2];
     const float top0 = a.top0, top1 = a.top1;
-    const unsigned ltmask = (1u << lane) - 1u;
-    unsigned long long since_flush = 0, cand = 0;
-    int qn = 0;  // entries in this warp's queue (warp-uniform)
-    int cur_mock = -1;
+    unsigned long long drained = 0, cand = 0;
+    int cur_mock = -1;   // mock whose histogram this warp is filling
+    __syncthreads();
 
-    // Bin what is left in every warp's queue, then add the shared histograms
-    // to mock `mk`'s global histogram and clear them.  Called by all threads.
-    auto flush_all = [&](int mk) {
+    // 2-D / wide histograms go to this warp's u32 copy, or (too many bins for
+    // shared memory) straight to the mock's u64 global histogram
+    auto bin_entry = [&](const float4 &e, int mk) {
+        unsigned long long *gh = a.hist + (size_t)mk * a.hist_stride;
+        if (MODE == MODE_3D) bin_3d<true>(e, hl, A0, a);
+        else if (MODE == MODE_3DS) {
+            if (copies) bin_3d<false>(e, wh, A0, a); else bin_3d<false>(e, gh, A0, a);
+        } else if (MODE == MODE_XYZ) {
+            if (copies) bin_xyz(e, wh, stride2, A0, A1, a); else bin_xyz(e, gh, stride2, A0, A1, a);
+        } else if (MODE == MODE_SMU) {
+            if (copies) bin_smu(e, wh, stride2, A0, A1, a); else bin_smu(e, gh, stride2, A0, A1, a);
+        } else if (MARK) bin_mark(e, hs, hc, A0, a);
+    };
+    // Bin the rest of the queue, add this warp's histogram to mock mk and clear it.
+    auto warp_flush = [&](int mk) {
         __syncwarp();
-        if (lane < qn) {
-            const float4 e = s_q[lane];
-            if (MODE == MODE_3D) bin_3d<true>(e, hl, A0, a);
-            else if (MODE == MODE_3DS) bin_3d<false>(e, hw, A0, a);
-            else if (MODE == MODE_XYZ) bin_xyz(e, hw, stride2, A0, A1, a);
-            else if (MODE == MODE_SMU) bin_smu(e, hw, stride2, A0, A1, a);
-            else if (MARK) bin_mark(e, hs, hc, A0, a);
-        }
-        qn = 0;
-        __syncthreads();
         unsigned long long *gh = a.hist + (size_t)mk * a.hist_stride;
         if (MODE == MODE_3D) {
-            for (int b = warp; b < nb0 + 1; b += GBP_WARPS) {
-                unsigned long long s = 0;
-                for (int w = 0; w < GBP_WARPS; w++) s += s_hist[(w * (nb0 + 1) + b) * 32 + lane];
+            for (int b = 0; b <= nb0; b++) {
+                unsigned long long v = hl[b * 32];
+                hl[b * 32] = 0u;
 #pragma unroll
-                for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-                if (lane == 0 && s) atomicAdd(&gh[b], s);
+                for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(FULL, v, o);
+                if (lane == 0 && v) atomicAdd(&gh[b], v);
             }
         } else if (MARK) {
             double *gd = a.histd + (size_t)mk * a.hist_stride;
-            const float *S = (const float *)s_hist;
-            const float *C = S + GBP_WARPS * (nb0 + 1) * 32;
-            for (int b = warp; b < nb0; b += GBP_WARPS) {
-                double s = 0.0;
-                for (int w = 0; w < GBP_WARPS; w++) {
-                    int idx = (w * (nb0 + 1) + b) * 32 + lane;
-                    s += (double)S[idx] - (double)C[idx];
-                }
+            for (int b = 0; b < nb0; b++) {
+                double v = (double)hs[b * 32] - (double)hc[b * 32];
+                hs[b * 32] = 0.f;
+                hc[b * 32] = 0.f;
 #pragma unroll
-                for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-                if (lane == 0 && s != 0.0) atomicAdd(&gd[b], s);
+                for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(FULL, v, o);
+                if (lane == 0 && v != 0.0) atomicAdd(&gd[b], v);
             }
-        } else {
-            for (int b = tid; b < nbin; b += GBP_BLOCK) {
-                unsigned long long s = 0;
-                for (int w = 0; w < copies; w++) s += s_hist[w * nbin + b];
-                if (s) atomicAdd(&gh[b], s);
+        } else if (copies) {
+            for (int b = lane; b < nbin; b += 32) {
+                unsigned v = wh[b];
+                wh[b] = 0u;
+                if (v) atomicAdd(&gh[b], (unsigned long long)v);
             }
         }
-        __syncthreads();
-        for (int i = tid; i < hist_words; i += GBP_BLOCK) s_hist[i] = 0u;
-        __syncthreads();
+        __syncwarp();
+        drained = 0;
     };
-    __syncthreads();
 
     while (true) {
-        if (tid == 0) s_item = atomicAdd(a.counter, 1);
-        __syncthreads();
-        const int it = s_item;
-        if (it >= s_nitems) break;
+        int it = 0;
+        if (lane == 0) it = atomicAdd(a.counter, 1);
+        it = __shfl_sync(FULL, it, 0);
+        if (it >= nitems) break;
         const int4 item = a.items[it];
         const int mock = item.x / a.ncells_mock;
-        const int cell = item.x - mock * a.ncells_mock, ifirst = item.y, icnt = item.z;
-        const int cz = cell % n2, cy = (cell / n2) % n1, cx = cell / (n1 * n2);
+        const int cell = item.x - mock * a.ncells_mock, ifirst = item.y;
+        const int icnt = item.z & 127, s0 = (item.z >> 7) & 1023, s1 = (item.z >> 17) & 1023;
         if (mock != cur_mock) {
-            // batched mocks: a new mock's histogram starts here
-            if (cur_mock >= 0) flush_all(cur_mock);
+            // batched mocks: this warp's histogram changes owner here
+            if (cur_mock >= 0) warp_flush(cur_mock);
             cur_mock = mock;
         }
+        const int cz = cell % n2, cy = (cell / n2) % n1, cx = cell / (n1 * n2);
         const int keybase = mock * a.ncells_mock;
-        for (int s = tid; s < a.nsten; s += GBP_BLOCK) {
-            int pk = s_off[s];
-            int x = cx + (pk & 255) - 64, y = cy + ((pk >> 8) & 255) - 64,
-                z = cz + ((pk >> 16) & 255) - 64;
-            bool ok = true;
-            if (a.pbc) {
-                x = x < 0 ? x + n0 : (x >= n0 ? x - n0 : x);
-                y = y < 0 ? y + n1 : (y >= n1 ? y - n1 : y);
-                z = z < 0 ? z + n2 : (z >= n2 ? z - n2 : z);
-            } else {
-                ok = x >= 0 && x < n0 && y >= 0 && y < n1 && z >= 0 && z < n2;
-            }
-            int st = 0, cn = 0;
-            if (ok) {
-                int c2 = keybase + (x * n1 + y) * n2 + z;
-                st = a.start2[c2];
-                cn = a.start2[c2 + 1] - st;
-            }
-            s_cstart[s] = st;
-            s_pre[s] = cn;
-        }
-        __syncthreads();
-        if (warp == 0) {
-            // exclusive scan of the stencil cell counts, 32 entries per step
-            int carry = 0;
-            for (int b = 0; b < a.nsten; b += 32) {
-                int idx = b + lane;
-                int v = idx < a.nsten ? s_pre[idx] : 0;
-                int incl = v;
-#pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    int t = __shfl_up_sync(0xffffffffu, incl, o);
-                    if (lane >= o) incl += t;
-                }
-                if (idx < a.nsten) s_pre[idx] = carry + incl - v;
-                carry += __shfl_sync(0xffffffffu, incl, 31);
-            }
-            if (lane == 0) s_pre[a.nsten] = carry;
-        }
-        __syncthreads();
-        const int total = s_pre[a.nsten];
-        const int nselfj = a.nself ? s_pre[1] : 0;
-        const int wpg = (icnt + 31) >> 5;
-        const int G = GBP_WARPS / wpg;
-        const int grp = warp / wpg;
-        const int within = (warp % wpg) * 32 + lane;
-        const bool in_group = grp < G;
-        const bool active_i = in_group && within < icnt;
-        float4 ui = make_float4(GBP_FAR, GBP_FAR, GBP_FAR, __int_as_float(-1));
-        if (active_i) ui = a.pos1[ifirst + within];
-        const int iself = __float_as_int(ui.w);
-        float wi32 = 0.f;
-        double wi64[5] = {0, 0, 0, 0, 0};
-        if (MARK && active_i) {
+        // two i-points per lane
+        float4 u0 = make_float4(GBP_FAR, GBP_FAR, GBP_FAR, __int_as_float(-1));
+        float4 u1 = u0;
+        if (lane < icnt) u0 = a.pos1[ifirst + lane];
+        if (lane + 32 < icnt) u1 = a.pos1[ifirst + 32 + lane];
+        const int is0 = __float_as_int(u0.w), is1 = __float_as_int(u1.w);
+        s_u[lane] = u0;
+        s_u[lane + 32] = u1;
+        float w0 = 0.f, w1 = 0.f;
+        double wa[5] = {0, 0, 0, 0, 0}, wb[5] = {0, 0, 0, 0, 0};
+        if (MARK) {
             if (WF == 0) {
-                for (int k = 0; k < nw; k++) wi64[k] = a.w64_1[(int64_t)(ifirst + within) * nw + k];
+                for (int k = 0; k < nw; k++) {
+                    if (lane < icnt) wa[k] = a.w64_1[(int64_t)(ifirst + lane) * nw + k];
+                    if (lane + 32 < icnt) wb[k] = a.w64_1[(int64_t)(ifirst + 32 + lane) * nw + k];
+                }
             } else {
-                wi32 = a.w1[ifirst + within];
+                if (lane < icnt) w0 = a.w1[ifirst + lane];
+                if (lane + 32 < icnt) w1 = a.w1[ifirst + 32 + lane];
+            }
+            if (WF == 0) {
+                for (int k = 0; k < nw; k++) {
+                    s_uw64[lane * nw + k] = wa[k];
+                    s_uw64[(lane + 32) * nw + k] = wb[k];
+                }
+            } else {
+                s_uw[lane] = w0;
+                s_uw[lane + 32] = w1;
             }
         }
-        cand += (unsigned long long)icnt * (unsigned long long)total;
-
-        for (int base = 0; base < total; base += GBP_JCAP) {
-            const int len = min(GBP_JCAP, total - base);
-            for (int f = tid; f < len; f += GBP_BLOCK) {
-                const int g = base + f;
-                int lo = 0, hi = a.nsten - 1;
-                while (lo < hi) {
-                    int mid = (lo + hi + 1) >> 1;
-                    if (s_pre[mid] <= g) lo = mid; else hi = mid - 1;
+        __syncwarp();
+        for (int sb = s0; sb < s1; sb += 32) {
+            // one stencil entry per lane: its j range and FP32 cell offset
+            const int s = sb + lane;
+            int st = 0, cn = 0;
+            float4 D = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (s < s1) {
+                const int pk = s_off[s];
+                int x = cx + (pk & 255) - 64, y = cy + ((pk >> 8) & 255) - 64,
+                    z = cz + ((pk >> 16) & 255) - 64;
+                bool ok = true;
+                if (a.pbc) {
+                    x = x < 0 ? x + n0 : (x >= n0 ? x - n0 : x);
+                    y = y < 0 ? y + n1 : (y >= n1 ? y - n1 : y);
+                    z = z < 0 ? z + n2 : (z >= n2 ? z - n2 : z);
+                } else {
+                    ok = x >= 0 && x < n0 && y >= 0 && y < n1 && z >= 0 && z < n2;
                 }
-                const int j = s_cstart[lo] + (g - s_pre[lo]);
-                float4 p = a.pos2[j];
-                float4 D = s_D[lo];
-                s_j[f] = make_float4(p.x + D.x, p.y + D.y, p.z + D.z, p.w);
-                if (MARK) {
-                    if (WF == 0) {
-                        for (int k = 0; k < nw; k++) s_jw64[f * nw + k] = a.w64_2[(int64_t)j * nw + k];
+                if (ok) {
+                    const int c2 = keybase + (x * n1 + y) * n2 + z;
+                    st = a.start2[c2];
+                    cn = a.start2[c2 + 1] - st;
+                }
+                D = s_D[s];
+            }
+            int incl = cn;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(FULL, incl, o);
+                if (lane >= o) incl += t;
+            }
+            const int T = __shfl_sync(FULL, incl, 31);
+            // own-cell j-slots (auto mode, stencil entry 0): ordered pairs, i == j excluded
+            const int selfT = (sb == 0 && a.nself) ? __shfl_sync(FULL, cn, 0) : 0;
+            cand += (unsigned long long)icnt * (unsigned long long)T;
+            for (int f0 = 0; f0 < T; f0 += 32) {
+                // lane l stages j-slot f0 + l: the stencil entry k holding it is the
+                // smallest k with incl[k] > f (5-step search over the lanes)
+                const int f = f0 + lane;
+                int k = 0;
+#pragma unroll
+                for (int step = 16; step > 0; step >>= 1) {
+                    const int v = __shfl_sync(FULL, incl, k + step - 1);
+                    if (v <= f) k += step;
+                }
+                k &= 31;
+                const int stk = __shfl_sync(FULL, st, k);
+                const int exk = __shfl_sync(FULL, incl - cn, k);
+                const float Dx = __shfl_sync(FULL, D.x, k), Dy = __shfl_sync(FULL, D.y, k),
+                            Dz = __shfl_sync(FULL, D.z, k);
+                if (f < T) {
+                    const int j = stk + (f - exk);
+                    const float4 p = a.pos2[j];
+                    jb[lane] = make_float4(p.x + Dx, p.y + Dy, p.z + Dz, p.w);
+                    if (MARK) {
+                        if (WF == 0) {
+                            for (int q = 0; q < nw; q++) jw64[lane * nw + q] = a.w64_2[(int64_t)j * nw + q];
+                        } else {
+                            jw[lane] = a.w2[j];
+                        }
+                    }
+                } else {
+                    // padding slot: at -FAR, so it is 2*FAR from an idle i-lane (+FAR)
+                    // and farther still from every real point; its bits are also masked
+                    jb[lane] = make_float4(-GBP_FAR, -GBP_FAR, -GBP_FAR, __int_as_float(-2));
+                }
+                __syncwarp();
+                const int nj = min(32, T - f0);
+                const int ns = min(max(selfT - f0, 0), nj);
+                // stage 1: one bit per in-range (i, j) for each of the lane's two i-points
+                unsigned m0 = 0u, m1 = 0u;
+#pragma unroll 8
+                for (int jj = 0; jj < 32; jj++) {
+                    const float4 t = jb[jj];
+                    const float dx0 = u0.x - t.x, dy0 = u0.y - t.y, dz0 = u0.z - t.z;
+                    const float dx1 = u1.x - t.x, dy1 = u1.y - t.y, dz1 = u1.z - t.z;
+                    bool in0, in1;
+                    if (MODE == MODE_XYZ) {
+                        in0 = (fmaf(dy0, dy0, dx0 * dx0) <= top0) & (dz0 * dz0 <= top1);
+                        in1 = (fmaf(dy1, dy1, dx1 * dx1) <= top0) & (dz1 * dz1 <= top1);
                     } else {
-                        s_jw[f] = a.w2[j];
+                        in0 = fmaf(dz0, dz0, fmaf(dy0, dy0, dx0 * dx0)) <= top0;
+                        in1 = fmaf(dz1, dz1, fmaf(dy1, dy1, dx1 * dx1)) <= top0;
+                    }
+                    m0 |= (unsigned)in0 << jj;
+                    m1 |= (unsigned)in1 << jj;
+                }
+                const unsigned valid = nj >= 32 ? 0xffffffffu : ((1u << nj) - 1u);
+                m0 &= valid;
+                m1 &= valid;
+                if (ns > 0) {
+                    // own cell: (i, i) has separation exactly 0 and is handled apart
+                    for (int jj = 0; jj < ns; jj++) {
+                        const int jt = __float_as_int(jb[jj].w);
+                        if (jt == is0) {
+                            m0 &= ~(1u << jj);
+                            if (MARK && a.self_bin < nb0) {
+                                const float ws = WF == 1 ? w0 * jw[jj] : WF == 2 ? w0 + jw[jj]
+                                                 : (float)wfunc64(a.wfunc, wa, jw64 + jj * nw);
+                                kahan_add(hs, hc, a.self_bin, ws);
+                            }
+                        }
+                        if (jt == is1) {
+                            m1 &= ~(1u << jj);
+                            if (MARK && a.self_bin < nb0) {
+                                const float ws = WF == 1 ? w1 * jw[jj] : WF == 2 ? w1 + jw[jj]
+                                                 : (float)wfunc64(a.wfunc, wb, jw64 + jj * nw);
+                                kahan_add(hs, hc, a.self_bin, ws);
+                            }
+                        }
                     }
                 }
-            }
-            __syncthreads();
-            if (in_group) {
-                const int split = min(max(nselfj - base, 0), len);
-                for (int seg = 0; seg < 2; seg++) {
-                    // seg 0: own cell in auto mode (ordered pairs, i == j excluded);
-                    // seg 1: the rest (each unordered pair once in auto mode)
-                    const int jbeg = seg == 0 ? grp : split + ((grp - split) % G + G) % G;
-                    const int jend = seg == 0 ? split : len;
-                    const unsigned symbit = (seg == 1 && a.nself) ? SYM_BIT : 0u;
-#pragma unroll 2
-                    for (int jj = jbeg; jj < jend; jj += G) {
-                        const float4 t = s_j[jj];
-                        const float dx = ui.x - t.x, dy = ui.y - t.y, dz = ui.z - t.z;
+                // stage 2, warp-cooperative: the warp's in-range pairs are numbered
+                // lane by lane (prefix sum of the bit counts) and each lane bins one
+                // pair per round; the owner lane is found by a 5-step search over
+                // the prefix and the pair's bit by __fns (n-th set bit)
+                const unsigned own_bits = ns >= 32 ? 0xffffffffu : ((1u << ns) - 1u);
+                const unsigned sym_bits = a.nself ? ~own_bits : 0u;
+                const int c0 = __popc(m0);
+                const int cl = c0 + __popc(m1);
+                int pre = cl;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int t = __shfl_up_sync(FULL, pre, o);
+                    if (lane >= o) pre += t;
+                }
+                const int C = __shfl_sync(FULL, pre, 31);
+                pre -= cl;  // exclusive
+                // each lane writes a 16-bit code (owner lane, i-slot, j-slot) per
+                // in-range pair at its prefix offset; the warp then bins 32 codes
+                // per round with every lane busy
+                {
+                    int k = pre;
+                    unsigned m = m0;
+                    while (m) {
+                        const int jj = __ffs(m) - 1;
+                        m &= m - 1u;
+                        s_code[k++] = (unsigned short)(lane | (jj << 6));
+                    }
+                    m = m1;
+                    while (m) {
+                        const int jj = __ffs(m) - 1;
+                        m &= m - 1u;
+                        s_code[k++] = (unsigned short)(lane | 32 | (jj << 6));
+                    }
+                }
+                __syncwarp();
+                for (int r0 = 0; r0 < C; r0 += 32) {
+                    const int slot = r0 + lane;
+                    if (slot < C) {
+                        const int code = s_code[slot];
+                        const int iu = code & 63, jj = code >> 6;
+                        const float4 u = s_u[iu];
+                        const float4 t = jb[jj];
+                        const float dx = u.x - t.x, dy = u.y - t.y, dz = u.z - t.z;
                         float v0, v1 = 0.f;
-                        bool in;
                         if (MODE == MODE_XYZ) {
                             v0 = fmaf(dy, dy, dx * dx);
                             v1 = dz * dz;
-                            in = (v0 <= top0) & (v1 <= top1);
                         } else if (MODE == MODE_SMU) {
                             v1 = fmaf(dy, dy, dx * dx);
                             v0 = fmaf(dz, dz, v1);
-                            in = v0 <= top0;
                         } else {
                             v0 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-                            in = v0 <= top0;
                         }
-                        const bool self = seg == 0 && __float_as_int(t.w) == iself;
                         if (MARK) {
-                            if (WF == 1) v1 = wi32 * s_jw[jj];
-                            else if (WF == 2) v1 = wi32 + s_jw[jj];
-                            else if (in) v1 = (float)wfunc64(a.wfunc, wi64, s_jw64 + jj * nw);
-                            // (i, i): separation exactly 0, its weight goes straight to that bin
-                            if (self && a.self_bin < nb0) kahan_add(hs, hc, a.self_bin, v1);
-                        }
-                        in = in & !self;
-                        const unsigned m = __ballot_sync(0xffffffffu, in);
-                        if (m) {
-                            if (in) {
-                                const int pos = qn + __popc(m & ltmask);
-                                s_q[pos] = make_float4(v0, v1, ui.w,
-                                                       __uint_as_float(__float_as_uint(t.w) | symbit));
-                            }
-                            qn += __popc(m);
-                            if (qn >= 32) {
-                                // stage 2 on the top 32 entries, all lanes busy
-                                __syncwarp();
-                                const float4 e = s_q[qn - 32 + lane];
-                                if (MODE == MODE_3D) bin_3d<true>(e, hl, A0, a);
-                                else if (MODE == MODE_3DS) bin_3d<false>(e, hw, A0, a);
-                                else if (MODE == MODE_XYZ) bin_xyz(e, hw, stride2, A0, A1, a);
-                                else if (MODE == MODE_SMU) bin_smu(e, hw, stride2, A0, A1, a);
-                                else if (MARK) bin_mark(e, hs, hc, A0, a);
-                                qn -= 32;
-                                __syncwarp();
+                            if (WF == 0) {
+                                v1 = (float)wfunc64(a.wfunc, s_uw64 + iu * nw, jw64 + jj * nw);
+                            } else {
+                                const float wi = s_uw[iu];
+                                v1 = WF == 1 ? wi * jw[jj] : wi + jw[jj];
                             }
                         }
+                        const unsigned jwbits =
+                            __float_as_uint(t.w) | (((sym_bits >> jj) & 1u) ? SYM_BIT : 0u);
+                        bin_entry(make_float4(v0, v1, u.w, __uint_as_float(jwbits)), cur_mock);
                     }
                 }
-            }
-            __syncthreads();
-        }
-        // a lane adds at most 2 per queued pair it drains; flush long before u32 overflow
-        if (!MARK) {
-            since_flush += 2ull * (unsigned long long)total *
-                           (MODE == MODE_3D ? 1ull : (unsigned long long)(GBP_BLOCK / copies)) + 64ull;
-            if (since_flush > (1ull << 31)) {
-                flush_all(cur_mock);
-                since_flush = 0;
+                drained += 64;
+                __syncwarp();
             }
         }
+        // a lane adds at most 2 per pair of its own and a warp copy at most 64
+        // per lane: flush long before a u32 could wrap
+        if (!MARK && drained > (1ull << 24)) warp_flush(cur_mock);
     }
-    if (cur_mock >= 0) flush_all(cur_mock);
-    if (tid == 0 && cand) atomicAdd(a.nrecheck + 1, cand);
+    if (cur_mock >= 0) warp_flush(cur_mock);
+    if (lane == 0 && cand) atomicAdd(a.nrecheck + 1, cand);
 }
 
 template <int MODE, int WF>

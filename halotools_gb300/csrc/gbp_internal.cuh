@@ -14,10 +14,11 @@
 
 #define GBP_BLOCK 256
 #define GBP_WARPS (GBP_BLOCK / 32)
-#define GBP_TI 256          // max i-points per work item (one per thread)
-#define GBP_JCAP 1024       // staged j-points per chunk
+#define GBP_TI 64           // max i-points per work item (two per lane of one warp)
+#define GBP_JCAP_ITEM 2048  // j-points per work item (stencil group cap)
+#define GBP_JCAP (GBP_WARPS * 32)  // staged j-points: 32 per warp
 #define GBP_LUT_MAX 1024    // float-bit lookup slots per axis
-#define GBP_QCAP 64         // per-warp queue of in-range pairs (entries)
+#define GBP_QCAP 0          // per-warp queue of in-range pairs (entries; unused)
 #define GBP_NB_MAX 1024     // edges per axis
 #define GBP_NB_LANE 64      // 1-D histograms up to this size use lane-private bins
 #define GBP_SMAX 512        // stencil cells
@@ -84,7 +85,7 @@ struct CountArgs {
 // jw: bytes of staged weights per j-point (marked mode), copies: shared
 // histogram copies (2-D and wide 1-D modes).
 struct SmemLayout {
-    int off_lut0, off_lut1, off_j, off_jw, off_q, off_D, off_E0, off_E1, off_hi0, off_lo0,
+    int off_lut0, off_lut1, off_j, off_jw, off_q, off_code, off_D, off_E0, off_E1, off_hi0, off_lo0,
         off_hi1, off_lo1, off_off, off_cstart, off_pre, off_hist, total;
 };
 
@@ -98,7 +99,8 @@ __host__ __device__ inline SmemLayout gbp_smem_layout(int mode, int T0, int T1, 
     L.off_lut1 = o; o += T1 * 16;
     L.off_j = o; o += GBP_JCAP * 16;
     L.off_jw = o; o += gbp_align(GBP_JCAP * jw, 16);
-    L.off_q = o; o += GBP_WARPS * GBP_QCAP * 16;
+    L.off_q = o; o += GBP_WARPS * 64 * 16 + gbp_align(GBP_WARPS * 64 * (jw > 4 ? jw : 4), 16);
+    L.off_code = o; o += (mode == MODE_ADJ) ? 0 : GBP_WARPS * 2048 * 2;
     L.off_D = o; o += nsten * 16;
     L.off_E0 = o; o += gbp_align(nb0 * 8, 16);
     L.off_E1 = o; o += gbp_align(nb1 * 8, 16);
@@ -144,9 +146,22 @@ cudaError_t gbp_build_cells(const void *d_xyz, int xyz_f32, int64_t npts, const 
                             float4 *d_pos32, double *d_pos64, int *d_orig, const double *d_w,
                             int nw, float *d_w32, double *d_w64, int *d_err, cudaStream_t st,
                             int *launches);
-// Work items (cell, first, count) for every non-empty cell of a sorted sample.
-cudaError_t gbp_build_items(const int *d_start, int64_t ncells, int4 *d_items, int *d_nitems,
-                            int *d_tmp, int *d_scan_tmp, cudaStream_t st, int *launches);
+// Work items (cell key, first i, packed {count, stencil range}) for every
+// non-empty cell of the sorted sample 1; writes at most `cap` items and sets
+// *d_overflow if more were needed.
+struct ItemPlan {
+    const int *start1, *start2;
+    int64_t nkeys;
+    int ncm;
+    int n[3];
+    int pbc;
+    const int *sten;  // device
+    int nsten;
+    int jcap;
+};
+cudaError_t gbp_build_items(const ItemPlan &ip, int4 *d_items, int cap, int *d_nitems,
+                            int *d_overflow, int *d_tmp, int *d_scan_tmp, cudaStream_t st,
+                            int *launches);
 cudaError_t gbp_scan_exclusive(const int *d_in, int *d_out, int64_t n, int *d_tmp,
                                cudaStream_t st, int *launches);
 size_t gbp_scan_tmp_ints(int64_t n);

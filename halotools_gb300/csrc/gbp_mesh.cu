@@ -45,7 +45,8 @@ __global__ void k_digitize(const T *__restrict__ xyz, int64_t npts, MeshDev m,
     if (bad) {
         atomicOr(err, 1);
         ic[0] = ic[1] = ic[2] = 0;
-        u[0] = u[1] = u[2] = GBP_FAR;
+        // far from everything, including idle lanes (+FAR) and padding (-FAR)
+        u[0] = u[1] = u[2] = -0.5f * GBP_FAR;
     }
     int c = (int)(mock * m.ncells) + (ic[0] * m.n[1] + ic[1]) * m.n[2] + ic[2];
     cellid[i] = c;
@@ -199,40 +200,100 @@ cudaError_t gbp_build_cells(const void *d_xyz, int xyz_f32, int64_t npts, const 
     return cudaSuccess;
 }
 
-__global__ void k_item_chunks(const int *__restrict__ start, int64_t ncells, int *__restrict__ nch) {
-    int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= ncells) return;
-    int cnt = start[c + 1] - start[c];
-    nch[c] = (cnt + GBP_TI - 1) / GBP_TI;
-}
+// Work items: (cell key, first i-point, packed {i count <= GBP_TI, first and
+// one-past-last stencil entry}).  A cell's i-points are cut into chunks of
+// GBP_TI; its stencil entries are cut into consecutive groups of at most
+// `jcap` j-points (a group closes before the entry that would overflow it),
+// so every item costs at most GBP_TI * jcap pair evaluations plus one cell.
+struct ItemPlanDev {
+    const int *start1, *start2;
+    int64_t nkeys;
+    int ncm;  // cells per mock
+    int n[3];
+    int pbc;
+    const int *sten;
+    int nsten;
+    int jcap;
+};
 
-__global__ void k_item_write(const int *__restrict__ start, int64_t ncells,
-                             const int *__restrict__ off, int4 *__restrict__ items,
-                             int *__restrict__ nitems) {
-    int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c == 0) *nitems = off[ncells];
-    if (c >= ncells) return;
-    int s = start[c], cnt = start[c + 1] - s;
-    int o = off[c];
-    for (int q = 0; q * GBP_TI < cnt; q++) {
-        int first = s + q * GBP_TI;
-        int num = min(GBP_TI, cnt - q * GBP_TI);
-        items[o + q] = make_int4((int)c, first, num, 0);
+__device__ __forceinline__ int stencil_count(const ItemPlanDev &P, int keybase, int cx, int cy,
+                                             int cz, int s) {
+    int pk = P.sten[s];
+    int x = cx + (pk & 255) - 64, y = cy + ((pk >> 8) & 255) - 64, z = cz + ((pk >> 16) & 255) - 64;
+    if (P.pbc) {
+        x = x < 0 ? x + P.n[0] : (x >= P.n[0] ? x - P.n[0] : x);
+        y = y < 0 ? y + P.n[1] : (y >= P.n[1] ? y - P.n[1] : y);
+        z = z < 0 ? z + P.n[2] : (z >= P.n[2] ? z - P.n[2] : z);
+    } else if (x < 0 || x >= P.n[0] || y < 0 || y >= P.n[1] || z < 0 || z >= P.n[2]) {
+        return 0;
     }
+    int c2 = keybase + (x * P.n[1] + y) * P.n[2] + z;
+    return P.start2[c2 + 1] - P.start2[c2];
 }
 
-cudaError_t gbp_build_items(const int *d_start, int64_t ncells, int4 *d_items, int *d_nitems,
-                            int *d_tmp, int *d_scan_tmp, cudaStream_t st, int *launches) {
-    unsigned g = (unsigned)((ncells + 255) / 256);
-    int *nch = d_tmp;
-    int *off = d_tmp + ncells + 1;
-    k_item_chunks<<<g, 256, 0, st>>>(d_start, ncells, nch);
+// emit == false: count the items of every key; true: write them at off[key]
+template <bool EMIT>
+__global__ void k_items(ItemPlanDev P, int *__restrict__ nitem, const int *__restrict__ off,
+                        int4 *__restrict__ items, int cap, int *__restrict__ nitems_total,
+                        int *__restrict__ overflow) {
+    int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (EMIT && k == 0) *nitems_total = min(off[P.nkeys], cap);
+    if (EMIT && k == 0 && off[P.nkeys] > cap) *overflow = 1;
+    if (k >= P.nkeys) return;
+    const int first = P.start1[k], cnt = P.start1[k + 1] - first;
+    const int q = (cnt + GBP_TI - 1) / GBP_TI;
+    const int mock = (int)(k / P.ncm), cell = (int)(k - (int64_t)mock * P.ncm);
+    const int cz = cell % P.n[2], cy = (cell / P.n[2]) % P.n[1], cx = cell / (P.n[1] * P.n[2]);
+    const int keybase = mock * P.ncm;
+    int o = EMIT ? off[k] : 0;
+    int groups = 0, acc = 0, s0 = 0;
+    if (cnt > 0) {
+        for (int s = 0; s <= P.nsten; s++) {
+            const int cn = s < P.nsten ? stencil_count(P, keybase, cx, cy, cz, s) : 0;
+            const bool close = s == P.nsten ? acc > 0 : (acc > 0 && acc + cn > P.jcap);
+            if (close) {
+                if (EMIT) {
+                    for (int c = 0; c < q; c++) {
+                        const int num = min(GBP_TI, cnt - c * GBP_TI);
+                        if (o < cap)
+                            items[o] = make_int4((int)k, first + c * GBP_TI,
+                                                 num | (s0 << 7) | (s << 17), 0);
+                        o++;
+                    }
+                }
+                groups++;
+                acc = 0;
+                s0 = s;
+            }
+            acc += cn;
+        }
+    }
+    if (!EMIT) nitem[k] = q * groups;
+}
+
+cudaError_t gbp_build_items(const ItemPlan &ip, int4 *d_items, int cap, int *d_nitems,
+                            int *d_overflow, int *d_tmp, int *d_scan_tmp, cudaStream_t st,
+                            int *launches) {
+    ItemPlanDev P;
+    P.start1 = ip.start1;
+    P.start2 = ip.start2;
+    P.nkeys = ip.nkeys;
+    P.ncm = ip.ncm;
+    for (int d = 0; d < 3; d++) P.n[d] = ip.n[d];
+    P.pbc = ip.pbc;
+    P.sten = ip.sten;
+    P.nsten = ip.nsten;
+    P.jcap = ip.jcap;
+    unsigned g = (unsigned)((ip.nkeys + 255) / 256);
+    int *nitem = d_tmp;
+    int *off = d_tmp + ip.nkeys + 1;
+    k_items<false><<<g, 256, 0, st>>>(P, nitem, nullptr, nullptr, cap, nullptr, nullptr);
     if (launches) *launches += 1;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    e = gbp_scan_exclusive(nch, off, ncells, d_scan_tmp, st, launches);
+    e = gbp_scan_exclusive(nitem, off, ip.nkeys, d_scan_tmp, st, launches);
     if (e != cudaSuccess) return e;
-    k_item_write<<<g, 256, 0, st>>>(d_start, ncells, off, d_items, d_nitems);
+    k_items<true><<<g, 256, 0, st>>>(P, nitem, off, d_items, cap, d_nitems, d_overflow);
     if (launches) *launches += 1;
     return cudaGetLastError();
 }

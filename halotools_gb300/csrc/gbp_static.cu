@@ -10,7 +10,7 @@
 // in the file-scope device array below.  It calls no cudaMalloc, cudaFree,
 // cudaMallocHost or other allocating routine, device or host.
 //
-// The array is GBP_STATIC_SCRATCH_BYTES (about 13 MB); every GPU that loads
+// The array is GBP_STATIC_SCRATCH_BYTES (16 MiB); every GPU that loads
 // this library holds it until the process exits.  Limits: at most
 // GBP_STATIC_MAX_POINTS points (auto-correlation of one sample), at most 64
 // bin edges; larger inputs are rejected with GBP_ERR_INVALID.
@@ -47,7 +47,8 @@ constexpr size_t O_COUNT = O_POS64 + al(3 * SP * 8);
 constexpr size_t O_START = O_COUNT + al((SC + 1) * 4);
 constexpr size_t O_SCAN = O_START + al((SC + 1) * 4);
 constexpr size_t O_ITEMS = O_SCAN + al(4096 * 4);
-constexpr size_t O_ITMP = O_ITEMS + al((SC + SP / GBP_TI + 16) * 16);
+constexpr int64_t SITEMS = 2 * SC + SP / GBP_TI + 65536;  // work-item capacity
+constexpr size_t O_ITMP = O_ITEMS + al(SITEMS * 16);
 constexpr size_t O_LUT = O_ITMP + al(2 * (SC + 2) * 4);
 constexpr size_t O_E = O_LUT + al(GBP_LUT_MAX * 16);
 constexpr size_t O_HI = O_E + al(SNB * 8);
@@ -86,11 +87,12 @@ cudaError_t scratch_for_device(int dev, unsigned char **out) {
 
 // Cumulative counts from the differential histogram, plus the n self-pairs
 // (separation exactly 0) in bin `self_bin`; every count is -1 if the
-// digitiser flagged a position outside the box.
+// digitiser flagged a position outside the box or the work items overflowed
+// the scratch (an input far denser than the point limit suggests).
 __global__ void k_static_finalize(const unsigned long long *hist, const unsigned long long *misc,
                                   int nb, int self_bin, long long nself, long long *counts) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    int err = reinterpret_cast<const int *>(misc)[2];
+    int err = reinterpret_cast<const int *>(misc)[2] | reinterpret_cast<const int *>(misc)[3];
     long long run = 0;
     for (int k = 0; k < nb; k++) {
         run += (long long)hist[k] + (k == self_bin ? nself : 0);
@@ -170,9 +172,20 @@ extern "C" int gbp_npairs_3d_static(const double *xyz, int64_t n, const double *
                         reinterpret_cast<int *>(W + O_ORIG), nullptr, 0, nullptr, nullptr,
                         misc_i + 2, st, nullptr);
     if (e != cudaSuccess) return GBP_ERR_CUDA;
-    e = gbp_build_items(start, g.ncells, reinterpret_cast<int4 *>(W + O_ITEMS), misc_i + 1,
-                        reinterpret_cast<int *>(W + O_ITMP), reinterpret_cast<int *>(W + O_SCAN),
-                        st, nullptr);
+    ItemPlan ip;
+    ip.start1 = ip.start2 = start;
+    ip.nkeys = g.ncells;
+    ip.ncm = (int)g.ncells;
+    for (int d = 0; d < 3; d++) ip.n[d] = g.n[d];
+    ip.pbc = g.pbc;
+    ip.sten = reinterpret_cast<const int *>(W + O_STEN);
+    ip.nsten = g.nsten;
+    ip.jcap = GBP_JCAP_ITEM;
+    // item capacity: every item holds >= 1 i-point and a group of >= 1 stencil
+    // entry or >= GBP_JCAP_ITEM j-points, so chunks x groups stays within this
+    e = gbp_build_items(ip, reinterpret_cast<int4 *>(W + O_ITEMS), (int)SITEMS, misc_i + 1,
+                        misc_i + 3, reinterpret_cast<int *>(W + O_ITMP),
+                        reinterpret_cast<int *>(W + O_SCAN), st, nullptr);
     if (e != cudaSuccess) return GBP_ERR_CUDA;
 
     CountArgs a;
@@ -204,13 +217,14 @@ extern "C" int gbp_npairs_3d_static(const double *xyz, int64_t n, const double *
     ad.vlo = li.vlo;
     ad.vhi = li.vhi;
     a.hist_stride = nbins + 1;
+    a.hist_copies = GBP_WARPS;
     a.ncells_mock = (int)g.ncells;
     a.hist_copies = 1;
     a.hist = reinterpret_cast<unsigned long long *>(W + O_HIST);
     a.nrecheck = misc + 2;
     a.top0 = std::min(hi[nbins - 1], 1.0e30f);
     a.self_bin = self_bin;
-    SmemLayout L = gbp_smem_layout(MODE_3D, li.T, 0, nbins, 0, g.nsten, 1, 0);
+    SmemLayout L = gbp_smem_layout(MODE_3D, li.T, 0, nbins, 0, g.nsten, GBP_WARPS, 0);
     size_t smem = (size_t)L.total;
     int occ = gbp_count_occupancy(MODE_3D, 1, smem);
     if (occ <= 0) return GBP_ERR_INVALID;

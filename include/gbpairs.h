@@ -177,7 +177,7 @@ int gbp_zheng07_vjp(gbp_plan *plan, const double *mass, int64_t n, const double 
  */
 #define GBP_STATIC_MAX_POINTS 131072
 #define GBP_STATIC_MAX_CELLS 131072
-#define GBP_STATIC_SCRATCH_BYTES (13u << 20)
+#define GBP_STATIC_SCRATCH_BYTES (16u << 20)
 int gbp_npairs_3d_static(const double *xyz, int64_t n, const double *rbins, int32_t nbins,
                          const double *period3, int32_t pbc, int64_t *counts, void *stream);
 
