@@ -66,7 +66,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "100"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -275,7 +275,7 @@ def extra_npairs_3d_10m(dev, threads):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="xyz2m", choices=sorted(WORKLOADS))
@@ -396,7 +396,7 @@ def main():
                 "candidate_pairs": st["candidate_pairs"], "recheck_pairs": st["recheck_pairs"],
                 "grid_cells": st["cells"], "reach": st["reach"],
                 "stencil_cells": st["stencil_cells"]}
-    tf = os.path.join(ROOT, "profiles", "traffic.json")
+    tf = os.path.join(ROOT, "profiles", "k_count_dram_traffic.json")
     if os.path.exists(tf):
         try:
             roofline["traffic"] = json.load(open(tf)).get(args.workload)

@@ -35,6 +35,19 @@
 
 #define SYM_BIT 0x80000000u
 
+// One in-range pair for stage 2: its FP32 value(s), the i-slot and j-slot it
+// came from (indices are looked up only when the pair needs the FP64 recheck)
+// and whether it stands for both orders.
+struct PairV {
+    float v0, v1;
+    int iu, jj;
+    bool sym;
+};
+struct Ix {
+    const int *ui;  // sorted index of each i-slot
+    const int *jw;  // sorted index of each j-slot
+};
+
 // ---------------- stage 2: 1-D (3-D separation) ----------------
 // Bins of a pair whose FP32 value may straddle an edge.  Returns 0 with k[0]
 // the bin when FP32 decides it after all; else re-evaluates in FP64 and
@@ -60,18 +73,16 @@ __device__ __noinline__ int slow_3d(float v, int b0, int is, int js, bool sym, i
 }
 
 template <bool LANE, class HT>
-__device__ __forceinline__ void bin_3d(const float4 &e, HT *h, const AxisSm &A,
+__device__ __forceinline__ void bin_3d(const PairV &p, HT *h, const AxisSm &A, const Ix &ix,
                                        const CountArgs &a) {
-    const float v = e.x;
-    const unsigned jw = __float_as_uint(e.w);
-    const bool sym = jw & SYM_BIT;
+    const float v = p.v0;
+    const bool sym = p.sym;
     const unsigned w = sym ? 2u : 1u;
-    float4 t = lut_entry(v, A);
+    float4 t = lut_entry_c<false>(v, A);
     int b = __float_as_int(t.x) + (v > t.y ? 1 : 0);
     if ((v > t.z) & !(v > t.y)) {
         int k[2];
-        int n = slow_3d(v, __float_as_int(t.x), __float_as_int(e.z), (int)(jw & ~SYM_BIT), sym, k,
-                        A, a);
+        int n = slow_3d(v, __float_as_int(t.x), ix.ui[p.iu], ix.jw[p.jj], sym, k, A, a);
         if (n == 0) {
             b = k[0];
         } else {
@@ -95,17 +106,15 @@ __device__ __forceinline__ void kahan_add(float *hs, float *hc, int b, float x) 
     hs[b * 32] = t;
 }
 
-__device__ __forceinline__ void bin_mark(const float4 &e, float *hs, float *hc, const AxisSm &A,
-                                         const CountArgs &a) {
-    const float v = e.x, wt = e.y;
-    const unsigned jw = __float_as_uint(e.w);
-    const bool sym = jw & SYM_BIT;
-    float4 t = lut_entry(v, A);
+__device__ __forceinline__ void bin_mark(const PairV &p, float *hs, float *hc, const AxisSm &A,
+                                         const Ix &ix, const CountArgs &a) {
+    const float v = p.v0, wt = p.v1;
+    const bool sym = p.sym;
+    float4 t = lut_entry_c<false>(v, A);
     int b = __float_as_int(t.x) + (v > t.y ? 1 : 0);
     if ((v > t.z) & !(v > t.y)) {
         int k[2];
-        int n = slow_3d(v, __float_as_int(t.x), __float_as_int(e.z), (int)(jw & ~SYM_BIT), sym, k,
-                        A, a);
+        int n = slow_3d(v, __float_as_int(t.x), ix.ui[p.iu], ix.jw[p.jj], sym, k, A, a);
         if (n == 0) {
             b = k[0];
         } else {
@@ -144,19 +153,18 @@ __device__ __noinline__ void slow_xyz(float v0, float v1, int b0a, int b0b, int 
 }
 
 template <class HT>
-__device__ __forceinline__ void bin_xyz(const float4 &e, HT *hw, int stride, const AxisSm &A,
-                                        const AxisSm &Bx, const CountArgs &a) {
-    const float v0 = e.x, v1 = e.y;
-    const unsigned jw = __float_as_uint(e.w);
-    const bool sym = jw & SYM_BIT;
-    float4 e0 = lut_entry(v0, A);
-    float4 e1 = lut_entry(v1, Bx);
+__device__ __forceinline__ void bin_xyz(const PairV &p, HT *hw, int stride, const AxisSm &A,
+                                        const AxisSm &Bx, const Ix &ix, const CountArgs &a) {
+    const float v0 = p.v0, v1 = p.v1;
+    const bool sym = p.sym;
+    float4 e0 = lut_entry_c<false>(v0, A);
+    float4 e1 = lut_entry_c<false>(v1, Bx);
     int ba = __float_as_int(e0.x) + (v0 > e0.y ? 1 : 0);
     int bb = __float_as_int(e1.x) + (v1 > e1.y ? 1 : 0);
     bool amb = ((v0 > e0.z) & !(v0 > e0.y)) | ((v1 > e1.z) & !(v1 > e1.y));
     if (amb) {
-        slow_xyz(v0, v1, __float_as_int(e0.x), __float_as_int(e1.x), __float_as_int(e.z),
-                 (int)(jw & ~SYM_BIT), sym, hw, stride, A, Bx, a);
+        slow_xyz(v0, v1, __float_as_int(e0.x), __float_as_int(e1.x), ix.ui[p.iu], ix.jw[p.jj], sym,
+                 hw, stride, A, Bx, a);
         return;
     }
     if ((ba < A.nb) & (bb < Bx.nb)) atomicAdd(&hw[ba * stride + bb], (HT)(sym ? 2 : 1));
@@ -197,17 +205,16 @@ __device__ __noinline__ void slow_smu(float v, float q, float qb, int b0s, int i
 }
 
 template <class HT>
-__device__ __forceinline__ void bin_smu(const float4 &e, HT *hw, int stride, const AxisSm &A,
-                                        const AxisSm &Q, const CountArgs &a) {
-    const float v = e.x, dxy = e.y;
-    const unsigned jw = __float_as_uint(e.w);
-    const bool sym = jw & SYM_BIT;
-    float4 e0 = lut_entry(v, A);
+__device__ __forceinline__ void bin_smu(const PairV &p, HT *hw, int stride, const AxisSm &A,
+                                        const AxisSm &Q, const Ix &ix, const CountArgs &a) {
+    const float v = p.v0, dxy = p.v1;
+    const bool sym = p.sym;
+    float4 e0 = lut_entry_c<true>(v, A);
     int bs = __float_as_int(e0.x) + (v > e0.y ? 1 : 0);
     if (bs >= A.nb) return;  // beyond the s gate
     float q = __fdividef(dxy, v);
     float qb = e0.w;
-    float4 e1 = lut_entry(q, Q);
+    float4 e1 = lut_entry_c<false>(q, Q);
     int bq = __float_as_int(e1.x) + (q > e1.y ? 1 : 0);
     // nearest edges around q must be farther than qb
     float below = bq > 0 ? Q.hi[bq - 1] : -3.0e38f;
@@ -215,8 +222,8 @@ __device__ __forceinline__ void bin_smu(const float4 &e, HT *hw, int stride, con
     bool amb = ((v > e0.z) & !(v > e0.y)) | !(q - below > qb) | !(above - q > qb) |
                (e1.y > 3.0e38f);
     if (amb) {
-        slow_smu(v, q, qb, __float_as_int(e0.x), __float_as_int(e.z), (int)(jw & ~SYM_BIT), sym,
-                 hw, stride, A, Q, a);
+        slow_smu(v, q, qb, __float_as_int(e0.x), ix.ui[p.iu], ix.jw[p.jj], sym, hw, stride, A, Q,
+                 a);
         return;
     }
     if (bq < Q.nb) atomicAdd(&hw[bs * stride + bq], (HT)(sym ? 2 : 1));
@@ -265,6 +272,42 @@ __device__ __forceinline__ double wfunc64(int id, const double *A, const double 
     }
 }
 
+// Stage-1 range test folded into one FP32 value per pair: R0 - dx^2 - dy^2 - dz^2
+// (3-D, s_mu) or (R0 - dx^2 - dy^2) | (R1 - dz^2) bits (xy_z).  Its sign bit is
+// set exactly when the pair lies beyond the thresholds.
+template <int MODE>
+__device__ __forceinline__ unsigned out_bits(const float4 &u, const float4 &t, float R0, float R1) {
+    const float dx = u.x - t.x, dy = u.y - t.y, dz = u.z - t.z;
+    if (MODE == MODE_XYZ) {
+        const float a = fmaf(-dy, dy, fmaf(-dx, dx, R0));
+        const float b = fmaf(-dz, dz, R1);
+        return __float_as_uint(a) | __float_as_uint(b);
+    }
+    return __float_as_uint(fmaf(-dz, dz, fmaf(-dy, dy, fmaf(-dx, dx, R0))));
+}
+
+// Packed FP32 pairs (low word = element 0).  sub/mul/fma.rn.f32x2 round each
+// element exactly as the scalar FSUB/FMUL/FFMA do.
+__device__ __forceinline__ unsigned long long pk2(float lo, float hi) {
+    return ((unsigned long long)__float_as_uint(hi) << 32) | __float_as_uint(lo);
+}
+__device__ __forceinline__ unsigned long long f2_sub(unsigned long long a, unsigned long long b) {
+    unsigned long long d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ unsigned long long f2_mul(unsigned long long a, unsigned long long b) {
+    unsigned long long d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ unsigned long long f2_fma(unsigned long long a, unsigned long long b,
+                                                     unsigned long long c) {
+    unsigned long long d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+
 // ---------------- kernel ----------------
 // Warp-centric: every warp independently pulls items, loads the i-points of
 // its item (two per lane), walks the item's stencil group 32 j-points at a
@@ -283,9 +326,18 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
     const int nw = MARK ? a.nw : 0;
     const int jwb = MARK ? (WF == 0 ? 8 * nw : 4) : 0;
     const SmemLayout L = gbp_smem_layout(MODE, T0, T1, nb0, nb1, a.nsten, copies, jwb);
-    float4 *s_lut0 = (float4 *)(smem + L.off_lut0);
-    float4 *s_lut1 = (float4 *)(smem + L.off_lut1);
-    float4 *jb = (float4 *)(smem + L.off_j) + warp * 32;
+    unsigned *s_l0 = (unsigned *)(smem + L.off_lut0);
+    unsigned *s_l1 = (unsigned *)(smem + L.off_lut1);
+    float *s_qb = MODE == MODE_SMU ? (float *)(smem + L.off_qb) : nullptr;
+    float2 *s_hl0 = (float2 *)(smem + L.off_hl0);
+    float2 *s_hl1 = (float2 *)(smem + L.off_hl1);
+    // this warp's 32 staged j-points: x, y, z (cell offset added) and sorted index
+    float *jx = (float *)(smem + L.off_j) + warp * 128;
+    float *jy = jx + 32, *jz = jx + 64;
+    int *jix = (int *)(jx + 96);
+    // the same j-points with each coordinate twice, for the packed stage 1
+    ulonglong2 *jxy = (ulonglong2 *)(smem + L.off_j2) + warp * 32;
+    unsigned long long *jzz = (unsigned long long *)(smem + L.off_j2 + GBP_JCAP * 16) + warp * 32;
     float *jw = (float *)(smem + L.off_jw) + warp * 32;
     double *jw64 = (double *)(smem + L.off_jw) + warp * 32 * (nw > 0 ? nw : 1);
     float4 *s_D = (float4 *)(smem + L.off_D);
@@ -297,15 +349,20 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
     float *s_lo1 = (float *)(smem + L.off_lo1);
     int *s_off = (int *)(smem + L.off_off);
     unsigned *s_hist = (unsigned *)(smem + L.off_hist);
-    // this warp's 64 i-points (and their weights) for stage 2
-    float4 *s_u = (float4 *)(smem + L.off_q) + warp * 64;
-    float *s_uw = (float *)(smem + L.off_q + GBP_WARPS * 64 * 16) + warp * 64;
-    double *s_uw64 = (double *)(smem + L.off_q + GBP_WARPS * 64 * 16) + warp * 64 * (nw > 0 ? nw : 1);
+    // this warp's 64 i-points (and their weights) for stage 2, at slots gbp_uslot(iu)
+    float *ux = (float *)(smem + L.off_q) + warp * 4 * GBP_USLOTS;
+    float *uy = ux + GBP_USLOTS, *uz = ux + 2 * GBP_USLOTS;
+    int *uix = (int *)(ux + 3 * GBP_USLOTS);
+    float *s_uw = (float *)(smem + L.off_q + GBP_WARPS * GBP_USLOTS * 16) + warp * GBP_USLOTS;
+    double *s_uw64 = (double *)(smem + L.off_q + GBP_WARPS * GBP_USLOTS * 16) +
+                     warp * GBP_USLOTS * (nw > 0 ? nw : 1);
+    const Ix ix{uix, jix};
     // this warp's pair codes of one 32-point j batch: at most 64 x 32
     unsigned short *s_code = (unsigned short *)(smem + L.off_code) + warp * 2048;
 
-    for (int i = tid; i < T0; i += GBP_BLOCK) s_lut0[i] = a.ax[0].lut[i];
-    for (int i = tid; i < T1; i += GBP_BLOCK) s_lut1[i] = a.ax[1].lut[i];
+    lut_compact(a.ax[0].lut, T0, a.ax[0].hi, a.ax[0].lo, nb0, s_l0, s_hl0, s_qb, tid, GBP_BLOCK);
+    if (TWO) lut_compact(a.ax[1].lut, T1, a.ax[1].hi, a.ax[1].lo, nb1, s_l1, s_hl1, nullptr, tid,
+                         GBP_BLOCK);
     for (int i = tid; i < nb0; i += GBP_BLOCK) {
         s_E0[i] = a.ax[0].E[i];
         s_hi0[i] = a.ax[0].hi[i];
@@ -326,32 +383,39 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                                                                 : (copies ? nbin : 0);
     unsigned *wh = s_hist + warp * warp_words;
     for (int i = lane; i < warp_words; i += 32) wh[i] = 0u;
-    AxisSm A0{s_lut0, s_hi0, s_lo0, s_E0, nb0, a.ax[0].S, a.ax[0].B, a.ax[0].vlo, a.ax[0].vhi};
-    AxisSm A1{s_lut1, s_hi1, s_lo1, s_E1, nb1, TWO ? a.ax[1].S : 0, TWO ? a.ax[1].B : 0,
-              TWO ? a.ax[1].vlo : 0.f, TWO ? a.ax[1].vhi : 0.f};
+    AxisSm A0{nullptr, s_hi0, s_lo0, s_E0, nb0, a.ax[0].S, a.ax[0].B, a.ax[0].vlo, a.ax[0].vhi,
+              s_l0, s_hl0, s_qb};
+    AxisSm A1{nullptr, s_hi1, s_lo1, s_E1, nb1, TWO ? a.ax[1].S : 0, TWO ? a.ax[1].B : 0,
+              TWO ? a.ax[1].vlo : 0.f, TWO ? a.ax[1].vhi : 0.f, s_l1, s_hl1, nullptr};
     const int stride2 = nb1 + 1;
     unsigned *hl = wh + lane;                       // 1-D: lane-private column
     float *hs = (float *)wh + lane;                 // marked: sums
     float *hc = hs + (nb0 + 1) * 32;                // marked: compensations
     const int nitems = *a.nitems;
     const int n0 = a.n[0], n1 = a.n[1], n2 = a.n[2];
-    const float top0 = a.top0, top1 = a.top1;
+    // stage-1 thresholds: top * (1 + 2^-18) + 1e-30 covers the rounding of the
+    // folded R - v against the stage-2 value v (three roundings of 2^-24 each)
+    const float R0 = fmaf(a.top0, 0x1p-18f, a.top0) + 1.0e-30f;
+    const float R1 = fmaf(a.top1, 0x1p-18f, a.top1) + 1.0e-30f;
+    const unsigned long long RR0 = pk2(R0, R0), RR1 = pk2(R1, R1);
     unsigned long long drained = 0, cand = 0;
     int cur_mock = -1;   // mock whose histogram this warp is filling
     __syncthreads();
 
     // 2-D / wide histograms go to this warp's u32 copy, or (too many bins for
     // shared memory) straight to the mock's u64 global histogram
-    auto bin_entry = [&](const float4 &e, int mk) {
+    auto bin_entry = [&](const PairV &e, int mk) {
         unsigned long long *gh = a.hist + (size_t)mk * a.hist_stride;
-        if (MODE == MODE_3D) bin_3d<true>(e, hl, A0, a);
+        if (MODE == MODE_3D) bin_3d<true>(e, hl, A0, ix, a);
         else if (MODE == MODE_3DS) {
-            if (copies) bin_3d<false>(e, wh, A0, a); else bin_3d<false>(e, gh, A0, a);
+            if (copies) bin_3d<false>(e, wh, A0, ix, a); else bin_3d<false>(e, gh, A0, ix, a);
         } else if (MODE == MODE_XYZ) {
-            if (copies) bin_xyz(e, wh, stride2, A0, A1, a); else bin_xyz(e, gh, stride2, A0, A1, a);
+            if (copies) bin_xyz(e, wh, stride2, A0, A1, ix, a);
+            else bin_xyz(e, gh, stride2, A0, A1, ix, a);
         } else if (MODE == MODE_SMU) {
-            if (copies) bin_smu(e, wh, stride2, A0, A1, a); else bin_smu(e, gh, stride2, A0, A1, a);
-        } else if (MARK) bin_mark(e, hs, hc, A0, a);
+            if (copies) bin_smu(e, wh, stride2, A0, A1, ix, a);
+            else bin_smu(e, gh, stride2, A0, A1, ix, a);
+        } else if (MARK) bin_mark(e, hs, hc, A0, ix, a);
     };
     // Bin the rest of the queue, add this warp's histogram to mock mk and clear it.
     auto warp_flush = [&](int mk) {
@@ -408,8 +472,9 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
         if (lane < icnt) u0 = a.pos1[ifirst + lane];
         if (lane + 32 < icnt) u1 = a.pos1[ifirst + 32 + lane];
         const int is0 = __float_as_int(u0.w), is1 = __float_as_int(u1.w);
-        s_u[lane] = u0;
-        s_u[lane + 32] = u1;
+        const unsigned long long UX = pk2(u0.x, u1.x), UY = pk2(u0.y, u1.y), UZ = pk2(u0.z, u1.z);
+        ux[lane] = u0.x; uy[lane] = u0.y; uz[lane] = u0.z; uix[lane] = is0;
+        ux[lane + 48] = u1.x; uy[lane + 48] = u1.y; uz[lane + 48] = u1.z; uix[lane + 48] = is1;
         float w0 = 0.f, w1 = 0.f;
         double wa[5] = {0, 0, 0, 0, 0}, wb[5] = {0, 0, 0, 0, 0};
         if (MARK) {
@@ -425,11 +490,11 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
             if (WF == 0) {
                 for (int k = 0; k < nw; k++) {
                     s_uw64[lane * nw + k] = wa[k];
-                    s_uw64[(lane + 32) * nw + k] = wb[k];
+                    s_uw64[(lane + 48) * nw + k] = wb[k];
                 }
             } else {
                 s_uw[lane] = w0;
-                s_uw[lane + 32] = w1;
+                s_uw[lane + 48] = w1;
             }
         }
         __syncwarp();
@@ -485,7 +550,10 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                 if (f < T) {
                     const int j = stk + (f - exk);
                     const float4 p = a.pos2[j];
-                    jb[lane] = make_float4(p.x + Dx, p.y + Dy, p.z + Dz, p.w);
+                    const float tx = p.x + Dx, ty = p.y + Dy, tz = p.z + Dz;
+                    jx[lane] = tx; jy[lane] = ty; jz[lane] = tz; jix[lane] = __float_as_int(p.w);
+                    jxy[lane] = make_ulonglong2(pk2(tx, tx), pk2(ty, ty));
+                    jzz[lane] = pk2(tz, tz);
                     if (MARK) {
                         if (WF == 0) {
                             for (int q = 0; q < nw; q++) jw64[lane * nw + q] = a.w64_2[(int64_t)j * nw + q];
@@ -496,36 +564,55 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                 } else {
                     // padding slot: at -FAR, so it is 2*FAR from an idle i-lane (+FAR)
                     // and farther still from every real point; its bits are also masked
-                    jb[lane] = make_float4(-GBP_FAR, -GBP_FAR, -GBP_FAR, __int_as_float(-2));
+                    jx[lane] = -GBP_FAR; jy[lane] = -GBP_FAR; jz[lane] = -GBP_FAR; jix[lane] = -2;
+                    jxy[lane] = make_ulonglong2(pk2(-GBP_FAR, -GBP_FAR), pk2(-GBP_FAR, -GBP_FAR));
+                    jzz[lane] = pk2(-GBP_FAR, -GBP_FAR);
                 }
                 __syncwarp();
                 const int nj = min(32, T - f0);
                 const int ns = min(max(selfT - f0, 0), nj);
-                // stage 1: one bit per in-range (i, j) for each of the lane's two i-points
-                unsigned m0 = 0u, m1 = 0u;
+                // stage 1: the sign bit of R - v is 1 exactly when the pair is out
+                // of range; a funnel shift appends it to the lane's out-mask, so
+                // slot jj lands in bit 31 - jj.  Items of at most 32 points take
+                // the one-point loop.
+                unsigned o0 = 0u, o1 = 0u;
+                if (icnt > 32) {
+                    // both i-points in packed f32x2 arithmetic: v exactly as stage 2
+                    // forms it, then R - v
 #pragma unroll 8
-                for (int jj = 0; jj < 32; jj++) {
-                    const float4 t = jb[jj];
-                    const float dx0 = u0.x - t.x, dy0 = u0.y - t.y, dz0 = u0.z - t.z;
-                    const float dx1 = u1.x - t.x, dy1 = u1.y - t.y, dz1 = u1.z - t.z;
-                    bool in0, in1;
-                    if (MODE == MODE_XYZ) {
-                        in0 = (fmaf(dy0, dy0, dx0 * dx0) <= top0) & (dz0 * dz0 <= top1);
-                        in1 = (fmaf(dy1, dy1, dx1 * dx1) <= top0) & (dz1 * dz1 <= top1);
-                    } else {
-                        in0 = fmaf(dz0, dz0, fmaf(dy0, dy0, dx0 * dx0)) <= top0;
-                        in1 = fmaf(dz1, dz1, fmaf(dy1, dy1, dx1 * dx1)) <= top0;
+                    for (int jj = 0; jj < 32; jj++) {
+                        const ulonglong2 txy = jxy[jj];
+                        const unsigned long long tzz = jzz[jj];
+                        const unsigned long long dX = f2_sub(UX, txy.x), dY = f2_sub(UY, txy.y),
+                                                 dZ = f2_sub(UZ, tzz);
+                        unsigned long long d;
+                        if (MODE == MODE_XYZ) {
+                            d = f2_sub(RR0, f2_fma(dY, dY, f2_mul(dX, dX))) |
+                                f2_sub(RR1, f2_mul(dZ, dZ));
+                        } else {
+                            d = f2_sub(RR0, f2_fma(dZ, dZ, f2_fma(dY, dY, f2_mul(dX, dX))));
+                        }
+                        o0 = __funnelshift_l((unsigned)d, o0, 1);
+                        o1 = __funnelshift_l((unsigned)(d >> 32), o1, 1);
                     }
-                    m0 |= (unsigned)in0 << jj;
-                    m1 |= (unsigned)in1 << jj;
+                } else {
+#pragma unroll 8
+                    for (int jj = 0; jj < 32; jj++) {
+                        const ulonglong2 txy = jxy[jj];
+                        const float4 t = make_float4(__uint_as_float((unsigned)txy.x),
+                                                     __uint_as_float((unsigned)txy.y),
+                                                     __uint_as_float((unsigned)jzz[jj]), 0.f);
+                        o0 = __funnelshift_l(out_bits<MODE>(u0, t, R0, R1), o0, 1);
+                    }
+                    o1 = 0xffffffffu;
                 }
                 const unsigned valid = nj >= 32 ? 0xffffffffu : ((1u << nj) - 1u);
-                m0 &= valid;
-                m1 &= valid;
+                unsigned m0 = __brev(~o0) & valid;
+                unsigned m1 = __brev(~o1) & valid;
                 if (ns > 0) {
                     // own cell: (i, i) has separation exactly 0 and is handled apart
                     for (int jj = 0; jj < ns; jj++) {
-                        const int jt = __float_as_int(jb[jj].w);
+                        const int jt = jix[jj];
                         if (jt == is0) {
                             m0 &= ~(1u << jj);
                             if (MARK && a.self_bin < nb0) {
@@ -560,55 +647,55 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                 }
                 const int C = __shfl_sync(FULL, pre, 31);
                 pre -= cl;  // exclusive
-                // each lane writes a 16-bit code (owner lane, i-slot, j-slot) per
-                // in-range pair at its prefix offset; the warp then bins 32 codes
-                // per round with every lane busy
+                // each lane writes a 16-bit code (i-slot, j-slot) per in-range pair
+                // at its prefix offset; the warp then bins 64 codes per round, two
+                // per lane, every lane busy
                 {
                     int k = pre;
                     unsigned m = m0;
                     while (m) {
                         const int jj = __ffs(m) - 1;
                         m &= m - 1u;
-                        s_code[k++] = (unsigned short)(lane | (jj << 6));
+                        s_code[k++] = (unsigned short)(lane | (jj << 7));
                     }
                     m = m1;
                     while (m) {
                         const int jj = __ffs(m) - 1;
                         m &= m - 1u;
-                        s_code[k++] = (unsigned short)(lane | 32 | (jj << 6));
+                        s_code[k++] = (unsigned short)((lane + 48) | (jj << 7));
                     }
                 }
                 __syncwarp();
-                for (int r0 = 0; r0 < C; r0 += 32) {
-                    const int slot = r0 + lane;
-                    if (slot < C) {
-                        const int code = s_code[slot];
-                        const int iu = code & 63, jj = code >> 6;
-                        const float4 u = s_u[iu];
-                        const float4 t = jb[jj];
-                        const float dx = u.x - t.x, dy = u.y - t.y, dz = u.z - t.z;
-                        float v0, v1 = 0.f;
-                        if (MODE == MODE_XYZ) {
-                            v0 = fmaf(dy, dy, dx * dx);
-                            v1 = dz * dz;
-                        } else if (MODE == MODE_SMU) {
-                            v1 = fmaf(dy, dy, dx * dx);
-                            v0 = fmaf(dz, dz, v1);
-                        } else {
-                            v0 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-                        }
-                        if (MARK) {
-                            if (WF == 0) {
-                                v1 = (float)wfunc64(a.wfunc, s_uw64 + iu * nw, jw64 + jj * nw);
-                            } else {
-                                const float wi = s_uw[iu];
-                                v1 = WF == 1 ? wi * jw[jj] : wi + jw[jj];
-                            }
-                        }
-                        const unsigned jwbits =
-                            __float_as_uint(t.w) | (((sym_bits >> jj) & 1u) ? SYM_BIT : 0u);
-                        bin_entry(make_float4(v0, v1, u.w, __uint_as_float(jwbits)), cur_mock);
+                auto entry = [&](int code) {
+                    const int iu = code & 127, jj = code >> 7;
+                    const float dx = ux[iu] - jx[jj], dy = uy[iu] - jy[jj], dz = uz[iu] - jz[jj];
+                    float v0, v1 = 0.f;
+                    if (MODE == MODE_XYZ) {
+                        v0 = fmaf(dy, dy, dx * dx);
+                        v1 = dz * dz;
+                    } else if (MODE == MODE_SMU) {
+                        v1 = fmaf(dy, dy, dx * dx);
+                        v0 = fmaf(dz, dz, v1);
+                    } else {
+                        v0 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
                     }
+                    if (MARK) {
+                        if (WF == 0) {
+                            v1 = (float)wfunc64(a.wfunc, s_uw64 + iu * nw, jw64 + jj * nw);
+                        } else {
+                            const float wi = s_uw[iu];
+                            v1 = WF == 1 ? wi * jw[jj] : wi + jw[jj];
+                        }
+                    }
+                    return PairV{v0, v1, iu, jj, ((sym_bits >> jj) & 1u) != 0u};
+                };
+                for (int r0 = 0; r0 < C; r0 += 64) {
+                    const int sa = r0 + lane, sb = sa + 32;
+                    const bool ha = sa < C, hb = sb < C;
+                    const PairV ea = entry(ha ? s_code[sa] : 0);
+                    const PairV eb = entry(hb ? s_code[sb] : 0);
+                    if (ha) bin_entry(ea, cur_mock);
+                    if (hb) bin_entry(eb, cur_mock);
                 }
                 drained += 64;
                 __syncwarp();

@@ -5,18 +5,53 @@
 #include "gbp_internal.cuh"
 
 struct AxisSm {
-    const float4 *lut;
+    const float4 *lut;      // adjoint: {b0, thr, lo, qband} per slot
     const float *hi;
     const float *lo;
     const double *E;
     int nb, S, B;
     float vlo, vhi;
+    const unsigned *l32;    // count kernels: b0 | (threshold-pair index << 16) per slot
+    const float2 *hl;       // threshold pairs (thr, lo): nb edges, the top, the always-walk pair
+    const float *qb;        // s_mu: q error bound per slot
 };
 
-__device__ __forceinline__ float4 lut_entry(float v, const AxisSm &a) {
+__device__ __forceinline__ int lut_slot(float v, const AxisSm &a) {
     float vc = fminf(fmaxf(v, a.vlo), a.vhi);
-    int idx = (int)(__float_as_uint(vc) >> a.S) - a.B;
-    return a.lut[idx];
+    return (int)(__float_as_uint(vc) >> a.S) - a.B;
+}
+
+__device__ __forceinline__ float4 lut_entry(float v, const AxisSm &a) {
+    return a.lut[lut_slot(v, a)];
+}
+
+// The same entry from the compact tables: a 4-byte slot word and a shared
+// threshold pair (few distinct addresses, so few bank conflicts).
+template <bool QB>
+__device__ __forceinline__ float4 lut_entry_c(float v, const AxisSm &a) {
+    const int s = lut_slot(v, a);
+    const unsigned w = a.l32[s];
+    const float2 t = a.hl[w >> 16];
+    return make_float4(__int_as_float((int)(w & 0xffffu)), t.x, t.y, QB ? a.qb[s] : 0.f);
+}
+
+// Build the compact tables in shared memory from the float4 table.
+__device__ __forceinline__ void lut_compact(const float4 *lut, int T, const float *hi,
+                                            const float *lo, int nb, unsigned *l32, float2 *hl,
+                                            float *qb, int tid, int nthr) {
+    for (int s = tid; s < T; s += nthr) {
+        const float4 e = lut[s];
+        const int b0 = __float_as_int(e.x);
+        // simple slot: (hi[b0], lo[b0]); top: (inf, inf) at nb; always-walk: (inf, -inf) at nb + 1
+        const int h = (b0 < nb && e.z == -INFINITY) ? nb + 1 : b0;
+        l32[s] = (unsigned)b0 | ((unsigned)h << 16);
+        if (qb) qb[s] = e.w;
+    }
+    for (int k = tid; k < nb; k += nthr) hl[k] = make_float2(hi[k], lo[k]);
+    if (tid == 0) {
+        hl[nb] = make_float2(INFINITY, INFINITY);
+        hl[nb + 1] = make_float2(INFINITY, -INFINITY);
+    }
 }
 
 // Walk from the table's start bin with the per-edge thresholds.  Returns the

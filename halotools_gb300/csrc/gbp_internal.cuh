@@ -85,9 +85,14 @@ struct CountArgs {
 // jw: bytes of staged weights per j-point (marked mode), copies: shared
 // histogram copies (2-D and wide 1-D modes).
 struct SmemLayout {
-    int off_lut0, off_lut1, off_j, off_jw, off_q, off_code, off_D, off_E0, off_E1, off_hi0, off_lo0,
-        off_hi1, off_lo1, off_off, off_cstart, off_pre, off_hist, total;
+    int off_lut0, off_lut1, off_qb, off_hl0, off_hl1, off_j, off_j2, off_jw, off_q, off_code, off_D,
+        off_E0, off_E1, off_hi0, off_lo0, off_hi1, off_lo1, off_off, off_hist, total;
 };
+
+// Stage-2 i-slots per warp: the lane's first point at slot lane, its second at
+// lane + 48, so that the two never share a shared-memory bank.
+#define GBP_USLOTS 80
+__host__ __device__ inline int gbp_uslot(int iu) { return iu + ((iu >> 5) << 4); }
 
 __host__ __device__ inline int gbp_align(int x, int a) { return (x + a - 1) / a * a; }
 
@@ -95,11 +100,20 @@ __host__ __device__ inline SmemLayout gbp_smem_layout(int mode, int T0, int T1, 
                                                       int nsten, int copies, int jw) {
     SmemLayout L;
     int o = 0;
-    L.off_lut0 = o; o += T0 * 16;
-    L.off_lut1 = o; o += T1 * 16;
-    L.off_j = o; o += GBP_JCAP * 16;
+    // adjoint: float4 tables {b0, thr, lo, qband}; count kernels: u32 table
+    // {b0 | threshold-pair index << 16} and the threshold pairs (hi, lo)
+    const bool adj = mode == MODE_ADJ;
+    L.off_lut0 = o; o += adj ? T0 * 16 : gbp_align(T0 * 4, 16);
+    L.off_lut1 = o; o += adj ? T1 * 16 : gbp_align(T1 * 4, 16);
+    L.off_qb = o; o += (mode == MODE_SMU) ? gbp_align(T0 * 4, 16) : 0;
+    L.off_hl0 = o; o += adj ? 0 : gbp_align((nb0 + 2) * 8, 16);
+    L.off_hl1 = o; o += adj ? 0 : gbp_align((nb1 + 2) * 8, 16);
+    L.off_j = o; o += GBP_JCAP * 16;   // adjoint: float4 per j; count: x, y, z, index arrays
+    L.off_j2 = o; o += (mode == MODE_ADJ) ? 0 : GBP_JCAP * 24;   // (x,x,y,y), (z,z) per j
     L.off_jw = o; o += gbp_align(GBP_JCAP * jw, 16);
-    L.off_q = o; o += GBP_WARPS * 64 * 16 + gbp_align(GBP_WARPS * 64 * (jw > 4 ? jw : 4), 16);
+    L.off_q = o;
+    o += adj ? 0 : GBP_WARPS * GBP_USLOTS * 16 +
+                       gbp_align(GBP_WARPS * GBP_USLOTS * (jw > 4 ? jw : 4), 16);
     L.off_code = o; o += (mode == MODE_ADJ) ? 0 : GBP_WARPS * 2048 * 2;
     L.off_D = o; o += nsten * 16;
     L.off_E0 = o; o += gbp_align(nb0 * 8, 16);
@@ -109,8 +123,6 @@ __host__ __device__ inline SmemLayout gbp_smem_layout(int mode, int T0, int T1, 
     L.off_hi1 = o; o += gbp_align(nb1 * 4, 16);
     L.off_lo1 = o; o += gbp_align(nb1 * 4, 16);
     L.off_off = o; o += gbp_align(nsten * 4, 16);
-    L.off_cstart = o; o += gbp_align(nsten * 4, 16);
-    L.off_pre = o; o += gbp_align((nsten + 1) * 4, 16);
     L.off_hist = o;
     int hist_bytes;
     if (mode == MODE_3D) {
