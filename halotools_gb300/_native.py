@@ -28,6 +28,7 @@ EXPORTED = (
     "gbp_plan_last_error", "gbp_plan_stats", "gbp_npairs_3d", "gbp_npairs_xy_z",
     "gbp_npairs_s_mu", "gbp_marked_npairs_3d", "gbp_measure_fp32_peak",
     "gbp_npairs_3d_static", "gbp_batched_npairs_3d", "gbp_plan_set_graph", "gbp_plan_set_autotune",
+    "gbp_plan_set_block",
     "gbp_weighted_adjoint_3d", "gbp_zheng07_weights", "gbp_zheng07_vjp",
 )
 
@@ -55,6 +56,8 @@ class Stats(ctypes.Structure):
         ("kernel_launches", ctypes.c_int32),
         ("h2d_bytes", ctypes.c_int64),
         ("d2h_bytes", ctypes.c_int64),
+        ("block", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
     ]
 
     def as_dict(self):
@@ -115,6 +118,7 @@ def load(build_if_missing: bool = True):
         L.gbp_zheng07_weights.argtypes = [vp, vp, i64, pd, i32, vp]
         L.gbp_zheng07_vjp.argtypes = [vp, vp, i64, pd, vp, i32, pd]
         L.gbp_plan_set_autotune.argtypes = [vp, ctypes.c_int]
+        L.gbp_plan_set_block.argtypes = [vp, ctypes.c_int]
         _lib = L
         return L
 
@@ -175,6 +179,10 @@ class Plan:
 
     def set_reach(self, reach: int):
         self.check(self.lib.gbp_plan_set_reach(self.handle, int(reach)))
+
+    def set_block(self, block: int):
+        """Fine cells per block edge of the two-level grid (1..4); 0 = automatic."""
+        self.check(self.lib.gbp_plan_set_block(self.handle, int(block)))
 
 
 _plans = {}

@@ -24,8 +24,9 @@ __device__ __noinline__ float slow_adj(float v, int b0, int is, int js, const fl
     if (k >= 0) return gt[k];
     if (is < 0 || js < 0) return 0.f;  // never a real pair
     atomicAdd(a.nrecheck, 1ull);
-    const double *p = a.x64_1 + 3 * (int64_t)is;
-    const double *q = a.x64_2 + 3 * (int64_t)js;
+    double p[3], q[3];
+    ref_pos(a, 0, is, p);
+    ref_pos(a, 1, js, q);
     int k1 = exact_bin(exact_pair(p, q, a).s2, b0, A);
     int k2 = exact_bin(exact_pair(q, p, a).s2, b0, A);
     return 0.5f * (gt[k1] + gt[k2]);
@@ -87,23 +88,12 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_adjoint(const CountArgs a) {
             int st = 0, cn = 0;
             float4 D = make_float4(0.f, 0.f, 0.f, 0.f);
             if (s < s1) {
-                const int pk = s_off[s];
-                int x = cx + (pk & 255) - 64, y = cy + ((pk >> 8) & 255) - 64,
-                    z = cz + ((pk >> 16) & 255) - 64;
-                bool ok = true;
-                if (a.pbc) {
-                    x = x < 0 ? x + n0 : (x >= n0 ? x - n0 : x);
-                    y = y < 0 ? y + n1 : (y >= n1 ? y - n1 : y);
-                    z = z < 0 ? z + n2 : (z >= n2 ? z - n2 : z);
-                } else {
-                    ok = x >= 0 && x < n0 && y >= 0 && y < n1 && z >= 0 && z < n2;
-                }
-                if (ok) {
-                    const int c2 = (x * n1 + y) * n2 + z;
-                    st = a.start2[c2];
-                    cn = a.start2[c2 + 1] - st;
-                }
                 D = s_D[s];
+                const int key = gbp_run_key(s_off[s], cx, cy, cz, a.n, a.pbc, 0, a.bf3);
+                if (key >= 0) {
+                    st = a.start2[key];
+                    cn = a.start2[key + __float_as_int(D.w)] - st;
+                }
             }
             int incl = cn;
 #pragma unroll

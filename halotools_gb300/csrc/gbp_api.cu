@@ -34,6 +34,7 @@ struct gbp_plan {
     cudaStream_t own = nullptr;
     cudaStream_t stream = nullptr;
     int reach = 0;
+    int block = 0;         // forced block factor of the two-level grid, 0 = automatic
     int nsm = 0;
     DevBuf work;           // device workspace, grow-only
     void *pinned = nullptr;
@@ -133,7 +134,6 @@ struct SampleDev {
     const double *xyz = nullptr;
     int *cellid, *rank, *count, *start, *orig;
     float4 *pos32;
-    double *pos64;
     float *w32 = nullptr;
     double *w64 = nullptr;
 };
@@ -202,7 +202,7 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
     // ---- carve the workspace ----
     Carve cv;
     size_t o_xyz[2] = {0, 0}, o_cellid[2], o_rank[2], o_count[2], o_start[2], o_orig[2],
-           o_pos32[2], o_pos64[2], o_w32[2] = {0, 0}, o_w64[2] = {0, 0}, o_win[2] = {0, 0};
+           o_pos32[2], o_w32[2] = {0, 0}, o_w64[2] = {0, 0}, o_win[2] = {0, 0};
     for (int s = 0; s < nsamp; s++) {
         size_t n = (size_t)std::max<int64_t>(ns[s], 1);
         if (c.mem == GBP_MEM_HOST) o_xyz[s] = cv.take<double>(3 * n);
@@ -212,7 +212,6 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
         o_start[s] = cv.take<int>((size_t)nkeys + 1);
         o_orig[s] = cv.take<int>(n);
         o_pos32[s] = cv.take<float4>(2 * n);
-        o_pos64[s] = cv.take<double>(3 * n);
         if (c.nw > 0) {
             if (c.mem == GBP_MEM_HOST) o_win[s] = cv.take<double>(n * c.nw);
             o_w32[s] = cv.take<float>(n * c.nw);
@@ -333,7 +332,6 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
             sd[s].start = at<int>(W, o_start[s]);
             sd[s].orig = at<int>(W, o_orig[s]);
             sd[s].pos32 = at<float4>(W, o_pos32[s]);
-            sd[s].pos64 = at<double>(W, o_pos64[s]);
             if (c.nw > 0) {
                 const double *wd = wsrc;
                 if (c.mem == GBP_MEM_HOST) {
@@ -355,8 +353,10 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
         unsigned long long *d_stat = misc + 2;  // [0] rechecks, [1] candidate pairs
 
         MeshDev md;
+        md.bf = c.g.bf;
         for (int d = 0; d < 3; d++) {
             md.n[d] = c.g.n[d];
+            md.nb[d] = c.g.nb[d];
             md.c[d] = c.g.c[d];
             md.L[d] = c.g.L[d];
         }
@@ -366,7 +366,7 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
         for (int s = 0; s < nsamp; s++) {
             const double *wsrc = s == 0 ? c.w1 : c.w2;
             cudaError_t e = gbp_build_cells(sd[s].xyz, s == 0 ? c.xyz_f32 : 0, ns[s], md, sd[s].cellid, sd[s].rank, sd[s].count,
-                                            sd[s].start, at<int>(W, o_scan), sd[s].pos32, sd[s].pos64,
+                                            sd[s].start, at<int>(W, o_scan), sd[s].pos32,
                                             sd[s].orig, c.nw > 0 ? wsrc : nullptr, c.nw, sd[s].w32,
                                             sd[s].w64, d_err, st, &launches);
             CK(e);
@@ -374,11 +374,13 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
         ItemPlan ip;
         ip.start1 = sd[0].start;
         ip.start2 = (c.autocorr ? sd[0] : sd[1]).start;
-        ip.nkeys = nkeys;
-        ip.ncm = (int)ncells;
-        for (int d = 0; d < 3; d++) ip.n[d] = c.g.n[d];
+        ip.nkeys = c.g.nblocks * nm;
+        ip.ncm = (int)c.g.nblocks;
+        ip.bf3 = c.g.bf * c.g.bf * c.g.bf;
+        for (int d = 0; d < 3; d++) ip.n[d] = c.g.nb[d];
         ip.pbc = c.g.pbc;
         ip.sten = at<int>(W, o_sten);
+        ip.stenD = at<float4>(W, o_stenD);
         ip.nsten = nsten;
         ip.jcap = GBP_JCAP_ITEM;
         CK(gbp_build_items(ip, at<int4>(W, o_items), (int)std::min<size_t>(max_items, INT32_MAX),
@@ -393,8 +395,12 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
         std::memset(&a, 0, sizeof(a));
         a.pos1 = sd[0].pos32;
         a.pos2 = s2.pos32;
-        a.x64_1 = sd[0].pos64;
-        a.x64_2 = s2.pos64;
+        a.xyz1 = sd[0].xyz;
+        a.xyz2 = s2.xyz;
+        a.xyz1_f32 = c.xyz_f32;
+        a.xyz2_f32 = c.autocorr ? c.xyz_f32 : 0;
+        a.orig1 = sd[0].orig;
+        a.orig2 = s2.orig;
         a.start2 = s2.start;
         a.items = at<int4>(W, o_items);
         a.nitems = d_nitems;
@@ -404,9 +410,10 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
         a.nsten = nsten;
         a.nself = c.g.nself;
         for (int d = 0; d < 3; d++) {
-            a.n[d] = c.g.n[d];
+            a.n[d] = c.g.nb[d];
             a.L[d] = c.g.L[d];
         }
+        a.bf3 = c.g.bf * c.g.bf * c.g.bf;
         a.pbc = c.g.pbc;
         for (int x = 0; x < c.naxes; x++) {
             AxisDev &ad = a.ax[x];
@@ -423,7 +430,7 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
             ad.vhi = ah.vhi;
         }
         a.hist_stride = (int)nhist;
-        a.ncells_mock = (int)ncells;
+        a.ncells_mock = (int)c.g.nblocks;
         a.hist = at<unsigned long long>(W, o_hist);
         a.histd = at<double>(W, o_histd);
         a.nrecheck = d_stat;
@@ -523,6 +530,7 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
     S.candidate_pairs = (int64_t)hm[3];
     for (int d = 0; d < 3; d++) S.cells[d] = c.g.n[d];
     S.reach = c.g.K;
+    S.block = c.g.bf;
     S.stencil_cells = nsten;
     int nit = reinterpret_cast<const int *>(hm)[1];
     S.work_items = nit;
@@ -617,6 +625,12 @@ int gbp_plan_set_reach(gbp_plan *plan, int reach) {
     return GBP_OK;
 }
 
+int gbp_plan_set_block(gbp_plan *plan, int block) {
+    if (!plan || block < 0 || block > 4) return GBP_ERR_INVALID;
+    plan->block = block;
+    return GBP_OK;
+}
+
 int gbp_plan_set_graph(gbp_plan *plan, int enable) {
     if (!plan) return GBP_ERR_INVALID;
     plan->graph_mode = enable != 0;
@@ -656,7 +670,7 @@ int gbp_npairs_3d(gbp_plan *plan, const double *xyz1, int64_t n1, const double *
     c.autocorr = (xyz1 == xyz2 && n1 == n2);
     c.mem = mem;
     c.naxes = 1;
-    choose_grid(c.g, period3, search, pbc, n2, plan->reach, MAX_CELLS_PER_DIM);
+    choose_grid(c.g, period3, search, pbc, n2, plan->reach, MAX_CELLS_PER_DIM, 0.0, plan->block);
     build_stencil(c.g, search, 0, c.autocorr);
     ErrModel em = err_model(c.g);
     std::vector<double> E(nb);
@@ -707,11 +721,11 @@ int gbp_batched_npairs_3d(gbp_plan *plan, const void *xyz, int32_t xyz_f32, cons
     if (n == 0) return GBP_OK;
     // the grid follows the mean mock density
     const int64_t nmean = std::max<int64_t>(1, n / nmocks);
-    auto plan_geometry = [&](int reach, double ppc) {
-        choose_grid(c.g, period3, search, pbc, nmean, reach, MAX_CELLS_PER_DIM, ppc);
+    auto plan_geometry = [&](int reach, double ppc, int bf) {
+        choose_grid(c.g, period3, search, pbc, nmean, reach, MAX_CELLS_PER_DIM, ppc, bf);
         // cell keys of all mocks must fit an int
         while (c.g.ncells * nmocks >= (1ll << 31) - 1 && c.g.K > 1)
-            choose_grid(c.g, period3, search, pbc, nmean, c.g.K - 1, MAX_CELLS_PER_DIM, ppc);
+            choose_grid(c.g, period3, search, pbc, nmean, c.g.K - 1, MAX_CELLS_PER_DIM, ppc, bf);
         build_stencil(c.g, search, 0, true);
         ErrModel em = err_model(c.g);
         std::vector<double> E(nb);
@@ -722,22 +736,25 @@ int gbp_batched_npairs_3d(gbp_plan *plan, const void *xyz, int32_t xyz_f32, cons
     std::vector<unsigned long long> h;
     int reach = plan->reach;
     double ppc = 0.0;
-    if (plan->autotune && reach == 0) {
+    int bf = plan->block;
+    if (plan->autotune && reach == 0 && bf == 0) {
         char sig[256];
         snprintf(sig, sizeof(sig), "b3d:%d:%lld:%d:%.17g:%.17g:%.17g:%.17g:%d", nmocks, (long long)n,
                  nb, rmax, period3[0], period3[1], period3[2], pbc);
         int found = -1;
         for (size_t t = 0; t < plan->tuned.size(); t++)
             if (plan->tuned[t].first == sig) found = plan->tuned[t].second;
-        // candidates: (reach, points per cell for coarse reach-1 grids)
-        static const int RK[6] = {1, 1, 1, 1, 2, 3};
-        static const double PPC[6] = {-1.0, 16.0, 32.0, 64.0, 0.0, 0.0};
+        // candidates: (reach, points per cell of coarse reach-1 cells, block factor)
+        constexpr int NCAND = 9;
+        static const int RK[NCAND] = {1, 1, 1, 1, 1, 1, 2, 2, 3};
+        static const double PPC[NCAND] = {0.0, 0.0, 0.0, -1.0, 32.0, 64.0, 0.0, 0.0, 0.0};
+        static const int BF[NCAND] = {2, 3, 4, 1, 1, 1, 1, 2, 1};
         if (found < 0) {
             float best = 1e30f;
-            int bi = 0;
-            for (int q = 0; q < 6; q++) {
-                plan_geometry(RK[q], PPC[q]);
-                if (c.g.K != RK[q]) continue;  // not feasible
+            int bi = 3;
+            for (int q = 0; q < NCAND; q++) {
+                plan_geometry(RK[q], PPC[q], BF[q]);
+                if (c.g.K != RK[q] || c.g.bf != BF[q]) continue;  // not feasible
                 if ((rc = run_call(plan, c, h))) return rc;
                 if (plan->stats.ms_count + plan->stats.ms_build < best) {
                     best = plan->stats.ms_count + plan->stats.ms_build;
@@ -749,8 +766,9 @@ int gbp_batched_npairs_3d(gbp_plan *plan, const void *xyz, int32_t xyz_f32, cons
         }
         reach = RK[found];
         ppc = PPC[found];
+        bf = BF[found];
     }
-    plan_geometry(reach, ppc);
+    plan_geometry(reach, ppc, bf);
     if (c.g.ncells * nmocks >= (1ll << 31) - 1)
         return fail(plan, GBP_ERR_INVALID, "too many mocks for one batched grid");
     if ((rc = run_call(plan, c, h))) return rc;
@@ -784,7 +802,7 @@ int gbp_npairs_xy_z(gbp_plan *plan, const double *xyz1, int64_t n1, const double
     c.autocorr = (xyz1 == xyz2 && n1 == n2);
     c.mem = mem;
     c.naxes = 2;
-    choose_grid(c.g, period3, search, pbc, n2, plan->reach, MAX_CELLS_PER_DIM);
+    choose_grid(c.g, period3, search, pbc, n2, plan->reach, MAX_CELLS_PER_DIM, 0.0, plan->block);
     build_stencil(c.g, search, 1, c.autocorr);
     ErrModel em = err_model(c.g);
     std::vector<double> E0(n_rp), E1(n_pi);
@@ -832,7 +850,7 @@ int gbp_npairs_s_mu(gbp_plan *plan, const double *xyz1, int64_t n1, const double
     c.autocorr = (xyz1 == xyz2 && n1 == n2);
     c.mem = mem;
     c.naxes = 2;
-    choose_grid(c.g, period3, search, pbc, n2, plan->reach, MAX_CELLS_PER_DIM);
+    choose_grid(c.g, period3, search, pbc, n2, plan->reach, MAX_CELLS_PER_DIM, 0.0, plan->block);
     build_stencil(c.g, search, 0, c.autocorr);
     ErrModel em = err_model(c.g);
     std::vector<double> Es(n_s), Em(n_mu), Eps(n_s), Epm(n_mu);
@@ -907,7 +925,7 @@ int gbp_marked_npairs_3d(gbp_plan *plan, const double *xyz1, int64_t n1, const d
     c.nw = nw;
     c.wfunc = wfunc_id;
     c.naxes = 1;
-    choose_grid(c.g, period3, search, pbc, n2, plan->reach, MAX_CELLS_PER_DIM);
+    choose_grid(c.g, period3, search, pbc, n2, plan->reach, MAX_CELLS_PER_DIM, 0.0, plan->block);
     build_stencil(c.g, search, 0, c.autocorr);
     ErrModel em = err_model(c.g);
     std::vector<double> E(nb);
@@ -950,7 +968,7 @@ int gbp_weighted_adjoint_3d(gbp_plan *plan, const double *xyz, int64_t n, const 
     c.wfunc = 1;
     c.naxes = 1;
     c.grad_out = grad_w;
-    choose_grid(c.g, period3, search, pbc, n, plan->reach, MAX_CELLS_PER_DIM);
+    choose_grid(c.g, period3, search, pbc, n, plan->reach, MAX_CELLS_PER_DIM, 0.0, plan->block);
     build_stencil(c.g, search, 0, false);  // ... but the full stencil: gather only
     ErrModel em = err_model(c.g);
     std::vector<double> E(nb);

@@ -64,8 +64,9 @@ __device__ __noinline__ int slow_3d(float v, int b0, int is, int js, bool sym, i
         return 0;
     }
     atomicAdd(a.nrecheck, 1ull);
-    const double *p = a.x64_1 + 3 * (int64_t)is;
-    const double *q = a.x64_2 + 3 * (int64_t)js;
+    double p[3], q[3];
+    ref_pos(a, 0, is, p);
+    ref_pos(a, 1, js, q);
     k[0] = exact_bin(exact_pair(p, q, a).s2, b0, A);
     if (!sym) return 1;
     k[1] = exact_bin(exact_pair(q, p, a).s2, b0, A);
@@ -139,8 +140,9 @@ __device__ __noinline__ void slow_xyz(float v0, float v1, int b0a, int b0b, int 
     }
     if (is < 0 || js < 0) return;  // never a real pair (idle lane or padding)
     atomicAdd(a.nrecheck, 1ull);
-    const double *p = a.x64_1 + 3 * (int64_t)is;
-    const double *q = a.x64_2 + 3 * (int64_t)js;
+    double p[3], q[3];
+    ref_pos(a, 0, is, p);
+    ref_pos(a, 1, js, q);
     Exact3 r = exact_pair(p, q, a);
     int ea = ka >= 0 ? ka : exact_bin(r.dxy, b0a, A);
     int eb = kb >= 0 ? kb : exact_bin(r.dz2, b0b, Bx);
@@ -191,8 +193,9 @@ __device__ __noinline__ void slow_smu(float v, float q, float qb, int b0s, int i
     }
     if (is < 0 || js < 0) return;  // never a real pair (idle lane or padding)
     atomicAdd(a.nrecheck, 1ull);
-    const double *p = a.x64_1 + 3 * (int64_t)is;
-    const double *qq = a.x64_2 + 3 * (int64_t)js;
+    double p[3], qq[3];
+    ref_pos(a, 0, is, p);
+    ref_pos(a, 1, js, qq);
     for (int o = 0; o < (sym ? 2 : 1); o++) {
         Exact3 r = o == 0 ? exact_pair(p, qq, a) : exact_pair(qq, p, a);
         int es = exact_bin(r.s2, 0, A);
@@ -504,23 +507,12 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
             int st = 0, cn = 0;
             float4 D = make_float4(0.f, 0.f, 0.f, 0.f);
             if (s < s1) {
-                const int pk = s_off[s];
-                int x = cx + (pk & 255) - 64, y = cy + ((pk >> 8) & 255) - 64,
-                    z = cz + ((pk >> 16) & 255) - 64;
-                bool ok = true;
-                if (a.pbc) {
-                    x = x < 0 ? x + n0 : (x >= n0 ? x - n0 : x);
-                    y = y < 0 ? y + n1 : (y >= n1 ? y - n1 : y);
-                    z = z < 0 ? z + n2 : (z >= n2 ? z - n2 : z);
-                } else {
-                    ok = x >= 0 && x < n0 && y >= 0 && y < n1 && z >= 0 && z < n2;
-                }
-                if (ok) {
-                    const int c2 = keybase + (x * n1 + y) * n2 + z;
-                    st = a.start2[c2];
-                    cn = a.start2[c2 + 1] - st;
-                }
                 D = s_D[s];
+                const int key = gbp_run_key(s_off[s], cx, cy, cz, a.n, a.pbc, keybase, a.bf3);
+                if (key >= 0) {
+                    st = a.start2[key];
+                    cn = a.start2[key + __float_as_int(D.w)] - st;
+                }
             }
             int incl = cn;
 #pragma unroll

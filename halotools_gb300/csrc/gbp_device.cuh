@@ -83,6 +83,24 @@ __device__ __forceinline__ double ref_delta(double a, double b, double L, int pb
     return best;
 }
 
+// FP64 position of sorted point `sorted` of sample `side` (0: sample 1), read
+// from the caller's array, float32 rows upcast exactly.
+__device__ __forceinline__ void ref_pos(const CountArgs &a, int side, int sorted, double p[3]) {
+    const int64_t r = 3 * (int64_t)(side ? a.orig2[sorted] : a.orig1[sorted]);
+    const void *x = side ? a.xyz2 : a.xyz1;
+    if (side ? a.xyz2_f32 : a.xyz1_f32) {
+        const float *f = (const float *)x + r;
+        p[0] = (double)f[0];
+        p[1] = (double)f[1];
+        p[2] = (double)f[2];
+    } else {
+        const double *d = (const double *)x + r;
+        p[0] = d[0];
+        p[1] = d[1];
+        p[2] = d[2];
+    }
+}
+
 struct Exact3 {
     double dxy, dz2, s2;
 };

@@ -14,7 +14,7 @@
 
 #include "gbp_internal.cuh"
 
-#define GBP_STEN_CAP 729  // (2*4+1)^3 cells for reach <= 4
+#define GBP_STEN_CAP 729  // (2*4+1)^3 cells for reach <= 4; runs of blocked grids fit too
 
 namespace gbp {
 
@@ -80,8 +80,9 @@ inline float bitsf(uint32_t u) {
     return f;
 }
 
-// Error model.  Coordinates are FP32 offsets from a cell corner, |u| <= c, the
-// stencil offset o*c is rounded to FP32 and added, and dx is formed in FP32:
+// Error model.  Coordinates are FP32 offsets from a block corner, |u| <= c
+// (c = block size here), the stencil offset o*c (|o| <= K blocks) is rounded
+// to FP32 and added, and dx is formed in FP32:
 // |dx32 - dx| <= delta = 2^-24 (c + c + K c + (K+1) c + |dx|) plus the FP64
 // rounding of the corner and of the reference's own dx (~2^-50 L).
 struct ErrModel {
@@ -183,12 +184,21 @@ inline int host_bin(int nb, const double *E, double v) {
 }
 
 // ---------------- grid & stencil ----------------
+// Two-level grid: fine cells of size c (K c >= search) grouped into blocks of
+// bf^3 fine cells.  Points are sorted block-major (key = block * bf^3 + fine
+// cell within the block), so a block's points are contiguous and form the
+// i-side of a work item; the j-side is the list of fine cells within the search
+// of the block's box.  bf = 1 is the plain cell list.
 struct Geometry {
-    int n[3];
+    int n[3];       // fine cells per dimension (n = nb * bf)
+    int nb[3];      // blocks per dimension
+    int bf = 1;     // fine cells per block edge
     double c[3], L[3];
-    int K;
+    int K;          // fine reach
+    int DB = 1;     // block reach of the stencil
     int pbc;
-    int64_t ncells;
+    int64_t ncells;   // fine cells
+    int64_t nblocks;
     int nsten;
     int nself;
     int sten[GBP_STEN_CAP];
@@ -215,11 +225,15 @@ inline bool grid_for_reach(int K, const double L[3], const double search[3], int
 // Reach K in 1..4 (hint > 0 forces it when feasible); the automatic choice
 // keeps about 28+ points of sample 2 per cell: finer cells prune more of the
 // cube stencil, but each work item then streams fewer points per i-point.
-// Sparse samples (fewer than ~12 points per reach-1 cell) get cells larger
-// than the search length, about `ppc` points each (default 24): per-item
-// set-up then amortises over enough pairs.  ppc < 0 disables coarsening.
+// Sparse samples (fewer than ~12 points per reach-1 cell): by default reach-1
+// fine cells grouped into blocks of about 32 points (bf = round(cbrt(32 /
+// occupancy)), at most 4), so that an item's i-points come from a block while
+// its j-cells hug the block's search region; with ppc > 0, single cells larger
+// than the search holding about ppc points instead.  ppc < 0 disables both.
+// bf_hint > 0 forces the block factor (when the grid allows it).
 inline void choose_grid(Geometry &g, const double L[3], const double search[3], int pbc,
-                        int64_t n2, int reach_hint, int64_t cap_per_dim, double ppc = 0.0) {
+                        int64_t n2, int reach_hint, int64_t cap_per_dim, double ppc = 0.0,
+                        int bf_hint = 0) {
     for (int d = 0; d < 3; d++) g.L[d] = L[d];
     g.pbc = pbc;
     double vol = L[0] * L[1] * L[2];
@@ -237,69 +251,115 @@ inline void choose_grid(Geometry &g, const double L[3], const double search[3], 
     }
     int64_t n[3];
     grid_for_reach(best, L, search, pbc, n, cap_per_dim);
+    int bf = 1;
     if (best == 1 && ppc >= 0.0 && rho > 0) {
         double cvol = (L[0] / n[0]) * (L[1] / n[1]) * (L[2] / n[2]);
-        double want = ppc > 0.0 ? ppc : 24.0;
-        if (ppc > 0.0 || rho * cvol < 12.0) {
-            double ct = std::cbrt(want / rho);
+        if (ppc > 0.0) {
+            double ct = std::cbrt(ppc / rho);
             for (int d = 0; d < 3; d++) {
                 int64_t m = (int64_t)std::floor(L[d] / ct);
                 m = std::max<int64_t>(m, pbc ? 3 : 1);
                 n[d] = std::min(n[d], m);  // never finer than the reach-1 grid
             }
+        } else if (bf_hint > 0) {
+            bf = bf_hint;
+        } else if (bf_hint == 0 && rho * cvol < 12.0) {
+            bf = (int)std::lround(std::cbrt(32.0 / std::max(rho * cvol, 1e-6)));
         }
+    } else if (bf_hint > 0) {
+        bf = bf_hint;
+    }
+    bf = std::max(1, std::min(bf, 4));
+    // blocks must tile the grid and, with periodic wrap, every block offset of
+    // the stencil must reach a distinct block
+    for (; bf > 1; bf--) {
+        const int DB = (best + bf - 1) / bf;
+        // at most bf^2 runs per neighbour block
+        bool ok = (2 * DB + 1) * (2 * DB + 1) * (2 * DB + 1) * bf * bf <= GBP_STEN_CAP;
+        for (int d = 0; d < 3; d++) {
+            const int64_t nbk = n[d] / bf;
+            if (nbk < 1 || (pbc && nbk < 2 * DB + 1)) ok = false;
+        }
+        if (ok) break;
     }
     g.K = best;
+    g.bf = bf;
+    g.DB = (best + bf - 1) / bf;
     g.ncells = 1;
+    g.nblocks = 1;
     for (int d = 0; d < 3; d++) {
-        g.n[d] = (int)n[d];
-        g.c[d] = L[d] / (double)n[d];
-        g.ncells *= n[d];
+        g.nb[d] = (int)(n[d] / bf);
+        g.n[d] = g.nb[d] * bf;
+        g.c[d] = L[d] / (double)g.n[d];
+        g.ncells *= g.n[d];
+        g.nblocks *= g.nb[d];
     }
 }
 
 // kind 0: sphere of radius search[0]; kind 1: cylinder (rp = search[0], pi = search[2]).
-// Offsets whose cell boxes are farther apart than the search are dropped.  In
-// auto mode the own cell comes first and only the lexicographically positive
-// half of the other offsets is kept (each unordered cell pair once).
+// An entry is a run of consecutive fine-cell keys of one neighbour block:
+// sten = block offset (8 bits each, biased by 64) | first fine cell << 24, and
+// stenD = (block offset * block size, run length).  Fine cells whose box is
+// farther than the search from the item block's box are dropped.  The own
+// block comes first as one run of bf^3 cells; in auto mode only the
+// lexicographically positive half of the other block offsets follows (each
+// unordered block pair once).
 inline void build_stencil(Geometry &g, const double search[3], int kind, bool autocorr) {
-    int K = g.K;
+    const int bf = g.bf, bf3 = bf * bf * bf;
+    const int DB = (g.K + bf - 1) / bf;
+    g.DB = DB;
     g.nsten = 0;
-    auto push = [&](int ox, int oy, int oz) {
-        g.sten[g.nsten] = (ox + 64) | ((oy + 64) << 8) | ((oz + 64) << 16);
-        g.stenD[g.nsten] = make_float4((float)(ox * g.c[0]), (float)(oy * g.c[1]),
-                                       (float)(oz * g.c[2]), 0.f);
+    auto push = [&](int ox, int oy, int oz, int l0, int span) {
+        g.sten[g.nsten] = (ox + 64) | ((oy + 64) << 8) | ((oz + 64) << 16) | (l0 << 24);
+        float sp;
+        std::memcpy(&sp, &span, 4);
+        g.stenD[g.nsten] = make_float4((float)(ox * bf * g.c[0]), (float)(oy * bf * g.c[1]),
+                                       (float)(oz * bf * g.c[2]), sp);
         g.nsten++;
     };
-    auto keep = [&](int ox, int oy, int oz) {
-        double gx = std::max(std::abs(ox) - 1, 0) * g.c[0];
-        double gy = std::max(std::abs(oy) - 1, 0) * g.c[1];
-        double gz = std::max(std::abs(oz) - 1, 0) * g.c[2];
+    // gap along d between fine cell f (block-relative) and the block [0, bf)
+    auto gap = [&](int f, int d) { return g.c[d] * std::max(0, std::max(f - bf, -f - 1)); };
+    auto keep = [&](int fx, int fy, int fz) {
+        double gx = gap(fx, 0), gy = gap(fy, 1), gz = gap(fz, 2);
         const double slack = 1.0 + 1e-9;
         if (kind == 0) return gx * gx + gy * gy + gz * gz <= search[0] * search[0] * slack;
         return gx * gx + gy * gy <= search[0] * search[0] * slack && gz <= search[2] * slack;
     };
-    int Kx = std::min(K, g.pbc ? K : g.n[0] - 1);
-    int Ky = std::min(K, g.pbc ? K : g.n[1] - 1);
-    int Kz = std::min(K, g.pbc ? K : g.n[2] - 1);
-    push(0, 0, 0);
-    for (int ox = -Kx; ox <= Kx; ox++)
-        for (int oy = -Ky; oy <= Ky; oy++)
-            for (int oz = -Kz; oz <= Kz; oz++) {
+    int Dx = std::min(DB, g.pbc ? DB : g.nb[0] - 1);
+    int Dy = std::min(DB, g.pbc ? DB : g.nb[1] - 1);
+    int Dz = std::min(DB, g.pbc ? DB : g.nb[2] - 1);
+    push(0, 0, 0, 0, bf3);
+    for (int ox = -Dx; ox <= Dx; ox++)
+        for (int oy = -Dy; oy <= Dy; oy++)
+            for (int oz = -Dz; oz <= Dz; oz++) {
                 if (ox == 0 && oy == 0 && oz == 0) continue;
                 if (autocorr) {
                     bool pos = ox > 0 || (ox == 0 && (oy > 0 || (oy == 0 && oz > 0)));
                     if (!pos) continue;
                 }
-                if (keep(ox, oy, oz)) push(ox, oy, oz);
+                int run = -1;
+                for (int l = 0; l <= bf3; l++) {
+                    bool k = false;
+                    if (l < bf3) {
+                        const int lx = l / (bf * bf), ly = (l / bf) % bf, lz = l % bf;
+                        k = keep(ox * bf + lx, oy * bf + ly, oz * bf + lz);
+                    }
+                    if (k && run < 0) run = l;
+                    if (!k && run >= 0) {
+                        push(ox, oy, oz, run, l - run);
+                        run = -1;
+                    }
+                }
             }
     g.nself = autocorr ? 1 : 0;
 }
 
+// Coordinates are FP32 offsets from the point's block corner, |u| <= bf c, and
+// stencil offsets are block offsets of at most DB blocks.
 inline ErrModel err_model(const Geometry &g) {
     ErrModel em;
-    em.cmax = std::max(g.c[0], std::max(g.c[1], g.c[2]));
-    em.K = g.K;
+    em.cmax = g.bf * std::max(g.c[0], std::max(g.c[1], g.c[2]));
+    em.K = g.DB;
     em.Lmax = std::max(g.L[0], std::max(g.L[1], g.L[2]));
     return em;
 }

@@ -1,13 +1,13 @@
 // Internal definitions shared by the gbpairs CUDA translation units.
 //
 // Data layout in HBM (one sample; the auto-correlation path sorts once):
-//   pos32[N]  float4  cell-relative FP32 coordinates (x - ix*cx, ...) in
-//                     cell-sorted order, .w = sorted index (int bits)
-//   pos64[3N] double  the FP64 positions in the same order (edge recheck)
-//   orig[N]   int     sorted position -> caller's index
-//   start[ncells+1]   CSR offsets of each cell's points
-// A count kernel walks work items (cell, first point, point count) and, per
-// item, streams the stencil cells' points through shared memory.
+//   pos32[N]  float4  block-relative FP32 coordinates (x - bx*bf*cx, ...) in
+//                     block-major cell-sorted order, .w = sorted index (int bits)
+//   orig[N]   int     sorted position -> caller's row (the FP64 recheck reads
+//                     the caller's positions through it)
+//   start[ncells+1]   CSR offsets of each fine cell's points (block-major keys)
+// A count kernel walks work items (block, first point, point count, stencil
+// group) and, per item, streams the stencil runs' points through shared memory.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -46,22 +46,26 @@ struct AxisDev {
 struct CountArgs {
     const float4 *pos1;
     const float4 *pos2;
-    const double *x64_1;
-    const double *x64_2;
+    const void *xyz1;       // caller's positions on the device, (N, 3); the FP64 recheck
+    const void *xyz2;       // reads them through orig1 / orig2
+    int xyz1_f32, xyz2_f32; // positions are float32 (upcast exactly)
+    const int *orig1;       // sorted position -> row of xyz1
+    const int *orig2;       // sorted position -> row of xyz2
     const int *start2;
     const int4 *items;
     const int *nitems;      // device scalar (written by the item builder)
     int *counter;           // work-item cursor, zero before launch
-    const int *sten;        // packed (ox+64) | (oy+64)<<8 | (oz+64)<<16
-    const float4 *stenD;    // FP32 cell offsets o*c per stencil cell
+    const int *sten;        // runs: block offset (ox+64) | (oy+64)<<8 | (oz+64)<<16 | first cell<<24
+    const float4 *stenD;    // FP32 block offsets o*bf*c and (bits of) the run length
     int nsten;
-    int nself;              // 1 if stencil[0] is the own cell counted once (auto mode), else 0
-    int n[3];
+    int nself;              // 1 if stencil[0] is the own block counted once (auto mode), else 0
+    int n[3];               // blocks per dimension
+    int bf3;                // fine cells per block
     int pbc;
     double L[3];
     AxisDev ax[2];
     int hist_stride;        // histogram words per mock (global histogram is [mock][bin])
-    int ncells_mock;        // cells per mock: work-item key = mock * ncells_mock + cell
+    int ncells_mock;        // blocks per mock: work-item key = mock * ncells_mock + block
     int hist_copies;        // shared histogram copies (2-D and wide 1-D): 8 = one per warp, or 1
     unsigned long long *hist;   // global differential histogram(s)
     unsigned long long *nrecheck;
@@ -141,9 +145,27 @@ __host__ __device__ inline SmemLayout gbp_smem_layout(int mode, int T0, int T1, 
     return L;
 }
 
+// Fine-cell key of stencil run `pk` seen from block (cx, cy, cz) of the mock
+// whose first block key is `keybase`; -1 when the neighbour block lies outside
+// a non-periodic box.
+__device__ __forceinline__ int gbp_run_key(int pk, int cx, int cy, int cz, const int n[3], int pbc,
+                                           int keybase, int bf3) {
+    int x = cx + (pk & 255) - 64, y = cy + ((pk >> 8) & 255) - 64, z = cz + ((pk >> 16) & 255) - 64;
+    if (pbc) {
+        x = x < 0 ? x + n[0] : (x >= n[0] ? x - n[0] : x);
+        y = y < 0 ? y + n[1] : (y >= n[1] ? y - n[1] : y);
+        z = z < 0 ? z + n[2] : (z >= n[2] ? z - n[2] : z);
+    } else if (x < 0 || x >= n[0] || y < 0 || y >= n[1] || z < 0 || z >= n[2]) {
+        return -1;
+    }
+    return (keybase + (x * n[1] + y) * n[2] + z) * bf3 + ((pk >> 24) & 127);
+}
+
 // ---- launchers (defined in the .cu files) ----
 struct MeshDev {
-    int n[3];
+    int n[3];                   // fine cells per dimension
+    int bf;                     // fine cells per block edge (keys are block-major)
+    int nb[3];                  // blocks per dimension
     double c[3];
     double L[3];
     int64_t ncells;             // cells per mock
@@ -155,19 +177,21 @@ struct MeshDev {
 // cell-sorted layout.  xyz_f32: positions are float32 (upcast exactly).
 cudaError_t gbp_build_cells(const void *d_xyz, int xyz_f32, int64_t npts, const MeshDev &m, int *d_cellid,
                             int *d_rank, int *d_count, int *d_start, int *d_scan_tmp,
-                            float4 *d_pos32, double *d_pos64, int *d_orig, const double *d_w,
+                            float4 *d_pos32, int *d_orig, const double *d_w,
                             int nw, float *d_w32, double *d_w64, int *d_err, cudaStream_t st,
                             int *launches);
 // Work items (cell key, first i, packed {count, stencil range}) for every
 // non-empty cell of the sorted sample 1; writes at most `cap` items and sets
 // *d_overflow if more were needed.
 struct ItemPlan {
-    const int *start1, *start2;
-    int64_t nkeys;
-    int ncm;
-    int n[3];
+    const int *start1, *start2;   // over fine-cell keys
+    int64_t nkeys;                // block keys (all mocks)
+    int ncm;                      // blocks per mock
+    int bf3;                      // fine cells per block
+    int n[3];                     // blocks per dimension
     int pbc;
-    const int *sten;  // device
+    const int *sten;      // device
+    const float4 *stenD;  // device (run lengths in .w)
     int nsten;
     int jcap;
 };

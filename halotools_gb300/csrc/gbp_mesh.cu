@@ -1,14 +1,17 @@
 // Cell-list build on the GPU: a counting sort that replaces the reference's
 // argsort/searchsorted mesh (halotools rectangular_mesh.py:118-222).
 //
-// k_digitize   one thread per point: cell index, rank within the cell (atomic
-//              counter), FP32 cell-relative coordinates.  Positions outside
-//              [0, L] or non-finite raise the error word.
+// k_digitize   one thread per point: cell key, rank within the cell (one atomic
+//              per distinct cell of a warp), FP32 block-relative coordinates.
+//              Positions outside [0, L] or non-finite raise the error word.
 // scan         exclusive prefix sum of the cell counts (three-kernel tile scan)
-// k_scatter    one thread per point: writes the sorted FP32/FP64 records.
-// items        one work item per (cell, chunk of <= GBP_TI points).
+// k_scatter    one thread per point: writes the sorted FP32 record and the
+//              sorted -> caller's row map (the FP64 recheck reads the caller's
+//              positions through it).
+// items        one work item per (block, chunk of <= GBP_TI points).
 //
-// Roofline: HBM-bound, about 24 B read + 48 B written per point per pass.
+// Roofline: HBM-bound, about 12-24 B (positions) + 24 B read and 44 B written
+// per point over the two passes.
 #include "gbp_internal.cuh"
 
 #define SCAN_THREADS 1024
@@ -18,58 +21,71 @@ template <class T>
 __global__ void k_digitize(const T *__restrict__ xyz, int64_t npts, MeshDev m,
                            int *__restrict__ cellid, int *__restrict__ rank,
                            int *__restrict__ count, float4 *__restrict__ rel, int *err) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= npts) return;
-    int mock = 0;
-    if (m.offsets) {  // largest mock with offsets[mock] <= i
-        int lo = 0, hi = m.nmocks - 1;
-        while (lo < hi) {
-            int mid = (lo + hi + 1) >> 1;
-            if (m.offsets[mid] <= i) lo = mid; else hi = mid - 1;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    // every lane of the warp stays to the end (the cell match is warp-wide)
+    const bool live = i < npts;
+    int c = -1;
+    float u[3] = {0.f, 0.f, 0.f};
+    if (live) {
+        int mock = 0;
+        if (m.offsets) {  // largest mock with offsets[mock] <= i
+            int lo = 0, hi = m.nmocks - 1;
+            while (lo < hi) {
+                int mid = (lo + hi + 1) >> 1;
+                if (m.offsets[mid] <= i) lo = mid; else hi = mid - 1;
+            }
+            mock = lo;
         }
-        mock = lo;
-    }
-    int ic[3];
-    float u[3];
-    bool bad = false;
+        int ib[3], il[3];
+        bool bad = false;
 #pragma unroll
-    for (int d = 0; d < 3; d++) {
-        double x = (double)xyz[3 * i + d];
-        if (!(x >= 0.0 && x <= m.L[d])) bad = true;  // also catches NaN
-        double t = x * (1.0 / m.c[d]);
-        int k = (int)floor(t);
-        k = k < 0 ? 0 : (k >= m.n[d] ? m.n[d] - 1 : k);
-        ic[d] = k;
-        u[d] = __double2float_rn(__dsub_rn(x, __dmul_rn((double)k, m.c[d])));
+        for (int d = 0; d < 3; d++) {
+            double x = (double)xyz[3 * i + d];
+            if (!(x >= 0.0 && x <= m.L[d])) bad = true;  // also catches NaN
+            double t = x * (1.0 / m.c[d]);
+            int k = (int)floor(t);
+            k = k < 0 ? 0 : (k >= m.n[d] ? m.n[d] - 1 : k);
+            ib[d] = k / m.bf;
+            il[d] = k - ib[d] * m.bf;
+            // offset from the block corner
+            u[d] = __double2float_rn(__dsub_rn(x, __dmul_rn((double)(ib[d] * m.bf), m.c[d])));
+        }
+        if (bad) {
+            atomicOr(err, 1);
+            ib[0] = ib[1] = ib[2] = il[0] = il[1] = il[2] = 0;
+            // far from everything, including idle lanes (+FAR) and padding (-FAR)
+            u[0] = u[1] = u[2] = -0.5f * GBP_FAR;
+        }
+        // block-major key: a block's fine cells (and so its points) are contiguous
+        const int bf = m.bf;
+        c = (int)(mock * m.ncells) + ((ib[0] * m.nb[1] + ib[1]) * m.nb[2] + ib[2]) * (bf * bf * bf) +
+            (il[0] * bf + il[1]) * bf + il[2];
     }
-    if (bad) {
-        atomicOr(err, 1);
-        ic[0] = ic[1] = ic[2] = 0;
-        // far from everything, including idle lanes (+FAR) and padding (-FAR)
-        u[0] = u[1] = u[2] = -0.5f * GBP_FAR;
+    // points of one cell in one warp share a single atomic (input order often
+    // follows the clustering, e.g. satellites listed with their host)
+    const unsigned peers = __match_any_sync(0xffffffffu, c);
+    const int lane = threadIdx.x & 31, leader = __ffs(peers) - 1;
+    int base = 0;
+    if (live && lane == leader) base = atomicAdd(&count[c], __popc(peers));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (live) {
+        cellid[i] = c;
+        rank[i] = base + __popc(peers & ((1u << lane) - 1u));
+        rel[i] = make_float4(u[0], u[1], u[2], __int_as_float((int)i));
     }
-    int c = (int)(mock * m.ncells) + (ic[0] * m.n[1] + ic[1]) * m.n[2] + ic[2];
-    cellid[i] = c;
-    rank[i] = atomicAdd(&count[c], 1);
-    rel[i] = make_float4(u[0], u[1], u[2], __int_as_float((int)i));
 }
 
-template <class T>
-__global__ void k_scatter(const T *__restrict__ xyz, int64_t npts,
-                          const int *__restrict__ cellid, const int *__restrict__ rank,
+__global__ void k_scatter(int64_t npts, const int *__restrict__ cellid, const int *__restrict__ rank,
                           const int *__restrict__ start, const float4 *__restrict__ rel,
-                          float4 *__restrict__ pos32, double *__restrict__ pos64,
-                          int *__restrict__ orig, const double *__restrict__ w, int nw,
-                          float *__restrict__ w32, double *__restrict__ w64) {
+                          float4 *__restrict__ pos32, int *__restrict__ orig,
+                          const double *__restrict__ w, int nw, float *__restrict__ w32,
+                          double *__restrict__ w64) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= npts) return;
     int dst = start[cellid[i]] + rank[i];
     float4 r = rel[i];
     r.w = __int_as_float(dst);
     pos32[dst] = r;
-    pos64[3 * (int64_t)dst + 0] = (double)xyz[3 * i + 0];
-    pos64[3 * (int64_t)dst + 1] = (double)xyz[3 * i + 1];
-    pos64[3 * (int64_t)dst + 2] = (double)xyz[3 * i + 2];
     orig[dst] = (int)i;
     if (w) {
         for (int k = 0; k < nw; k++) {
@@ -165,7 +181,7 @@ cudaError_t gbp_scan_exclusive(const int *d_in, int *d_out, int64_t n, int *d_tm
 
 cudaError_t gbp_build_cells(const void *d_xyz, int xyz_f32, int64_t npts, const MeshDev &m,
                             int *d_cellid, int *d_rank, int *d_count, int *d_start, int *d_scan_tmp,
-                            float4 *d_pos32, double *d_pos64, int *d_orig, const double *d_w,
+                            float4 *d_pos32, int *d_orig, const double *d_w,
                             int nw, float *d_w32, double *d_w64, int *d_err, cudaStream_t st,
                             int *launches) {
     const int64_t nkeys = m.ncells * (int64_t)(m.offsets ? m.nmocks : 1);
@@ -187,48 +203,37 @@ cudaError_t gbp_build_cells(const void *d_xyz, int xyz_f32, int64_t npts, const 
     e = gbp_scan_exclusive(d_count, d_start, nkeys, d_scan_tmp, st, launches);
     if (e != cudaSuccess) return e;
     if (npts > 0) {
-        if (xyz_f32)
-            k_scatter<float><<<g, 256, 0, st>>>((const float *)d_xyz, npts, d_cellid, d_rank, d_start,
-                                                rel, d_pos32, d_pos64, d_orig, d_w, nw, d_w32, d_w64);
-        else
-            k_scatter<double><<<g, 256, 0, st>>>((const double *)d_xyz, npts, d_cellid, d_rank,
-                                                 d_start, rel, d_pos32, d_pos64, d_orig, d_w, nw,
-                                                 d_w32, d_w64);
+        k_scatter<<<g, 256, 0, st>>>(npts, d_cellid, d_rank, d_start, rel, d_pos32, d_orig, d_w, nw,
+                                     d_w32, d_w64);
         if (launches) *launches += 1;
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
     return cudaSuccess;
 }
 
-// Work items: (cell key, first i-point, packed {i count <= GBP_TI, first and
-// one-past-last stencil entry}).  A cell's i-points are cut into chunks of
-// GBP_TI; its stencil entries are cut into consecutive groups of at most
-// `jcap` j-points (a group closes before the entry that would overflow it),
-// so every item costs at most GBP_TI * jcap pair evaluations plus one cell.
+// Work items: (block key, first i-point, packed {i count <= GBP_TI, first and
+// one-past-last stencil entry}).  A block's i-points are cut into chunks of
+// GBP_TI; its stencil runs are cut into consecutive groups of at most `jcap`
+// j-points (a group closes before the run that would overflow it), so every
+// item costs at most GBP_TI * jcap pair evaluations plus one run.
 struct ItemPlanDev {
     const int *start1, *start2;
-    int64_t nkeys;
-    int ncm;  // cells per mock
-    int n[3];
+    int64_t nkeys;  // block keys
+    int ncm;        // blocks per mock
+    int bf3;        // fine cells per block
+    int n[3];       // blocks per dimension
     int pbc;
     const int *sten;
+    const float4 *stenD;
     int nsten;
     int jcap;
 };
 
 __device__ __forceinline__ int stencil_count(const ItemPlanDev &P, int keybase, int cx, int cy,
                                              int cz, int s) {
-    int pk = P.sten[s];
-    int x = cx + (pk & 255) - 64, y = cy + ((pk >> 8) & 255) - 64, z = cz + ((pk >> 16) & 255) - 64;
-    if (P.pbc) {
-        x = x < 0 ? x + P.n[0] : (x >= P.n[0] ? x - P.n[0] : x);
-        y = y < 0 ? y + P.n[1] : (y >= P.n[1] ? y - P.n[1] : y);
-        z = z < 0 ? z + P.n[2] : (z >= P.n[2] ? z - P.n[2] : z);
-    } else if (x < 0 || x >= P.n[0] || y < 0 || y >= P.n[1] || z < 0 || z >= P.n[2]) {
-        return 0;
-    }
-    int c2 = keybase + (x * P.n[1] + y) * P.n[2] + z;
-    return P.start2[c2 + 1] - P.start2[c2];
+    const int key = gbp_run_key(P.sten[s], cx, cy, cz, P.n, P.pbc, keybase, P.bf3);
+    if (key < 0) return 0;
+    return P.start2[key + __float_as_int(P.stenD[s].w)] - P.start2[key];
 }
 
 // emit == false: count the items of every key; true: write them at off[key]
@@ -240,7 +245,7 @@ __global__ void k_items(ItemPlanDev P, int *__restrict__ nitem, const int *__res
     if (EMIT && k == 0) *nitems_total = min(off[P.nkeys], cap);
     if (EMIT && k == 0 && off[P.nkeys] > cap) *overflow = 1;
     if (k >= P.nkeys) return;
-    const int first = P.start1[k], cnt = P.start1[k + 1] - first;
+    const int first = P.start1[k * P.bf3], cnt = P.start1[(k + 1) * P.bf3] - first;
     const int q = (cnt + GBP_TI - 1) / GBP_TI;
     const int mock = (int)(k / P.ncm), cell = (int)(k - (int64_t)mock * P.ncm);
     const int cz = cell % P.n[2], cy = (cell / P.n[2]) % P.n[1], cx = cell / (P.n[1] * P.n[2]);
@@ -279,9 +284,11 @@ cudaError_t gbp_build_items(const ItemPlan &ip, int4 *d_items, int cap, int *d_n
     P.start2 = ip.start2;
     P.nkeys = ip.nkeys;
     P.ncm = ip.ncm;
+    P.bf3 = ip.bf3;
     for (int d = 0; d < 3; d++) P.n[d] = ip.n[d];
     P.pbc = ip.pbc;
     P.sten = ip.sten;
+    P.stenD = ip.stenD;
     P.nsten = ip.nsten;
     P.jcap = ip.jcap;
     unsigned g = (unsigned)((ip.nkeys + 255) / 256);

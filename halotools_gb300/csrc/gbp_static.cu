@@ -42,8 +42,7 @@ constexpr size_t O_CELLID = 0;
 constexpr size_t O_RANK = O_CELLID + al(SP * 4);
 constexpr size_t O_ORIG = O_RANK + al(SP * 4);
 constexpr size_t O_POS32 = O_ORIG + al(SP * 4);
-constexpr size_t O_POS64 = O_POS32 + al(2 * SP * 16);
-constexpr size_t O_COUNT = O_POS64 + al(3 * SP * 8);
+constexpr size_t O_COUNT = O_POS32 + al(2 * SP * 16);
 constexpr size_t O_START = O_COUNT + al((SC + 1) * 4);
 constexpr size_t O_SCAN = O_START + al((SC + 1) * 4);
 constexpr size_t O_ITEMS = O_SCAN + al(4096 * 4);
@@ -155,8 +154,10 @@ extern "C" int gbp_npairs_3d_static(const double *xyz, int64_t n, const double *
     int *misc_i = reinterpret_cast<int *>(W + O_MISC);
     unsigned long long *misc = reinterpret_cast<unsigned long long *>(W + O_MISC);
     MeshDev md;
+    md.bf = g.bf;
     for (int d = 0; d < 3; d++) {
         md.n[d] = g.n[d];
+        md.nb[d] = g.nb[d];
         md.c[d] = g.c[d];
         md.L[d] = g.L[d];
     }
@@ -164,21 +165,22 @@ extern "C" int gbp_npairs_3d_static(const double *xyz, int64_t n, const double *
     md.offsets = nullptr;
     md.nmocks = 1;
     float4 *pos32 = reinterpret_cast<float4 *>(W + O_POS32);
-    double *pos64 = reinterpret_cast<double *>(W + O_POS64);
     int *start = reinterpret_cast<int *>(W + O_START);
     e = gbp_build_cells(xyz, 0, n, md, reinterpret_cast<int *>(W + O_CELLID),
                         reinterpret_cast<int *>(W + O_RANK), reinterpret_cast<int *>(W + O_COUNT),
-                        start, reinterpret_cast<int *>(W + O_SCAN), pos32, pos64,
+                        start, reinterpret_cast<int *>(W + O_SCAN), pos32,
                         reinterpret_cast<int *>(W + O_ORIG), nullptr, 0, nullptr, nullptr,
                         misc_i + 2, st, nullptr);
     if (e != cudaSuccess) return GBP_ERR_CUDA;
     ItemPlan ip;
     ip.start1 = ip.start2 = start;
-    ip.nkeys = g.ncells;
-    ip.ncm = (int)g.ncells;
-    for (int d = 0; d < 3; d++) ip.n[d] = g.n[d];
+    ip.nkeys = g.nblocks;
+    ip.ncm = (int)g.nblocks;
+    ip.bf3 = g.bf * g.bf * g.bf;
+    for (int d = 0; d < 3; d++) ip.n[d] = g.nb[d];
     ip.pbc = g.pbc;
     ip.sten = reinterpret_cast<const int *>(W + O_STEN);
+    ip.stenD = reinterpret_cast<const float4 *>(W + O_STEND);
     ip.nsten = g.nsten;
     ip.jcap = GBP_JCAP_ITEM;
     // item capacity: every item holds >= 1 i-point and a group of >= 1 stencil
@@ -191,7 +193,8 @@ extern "C" int gbp_npairs_3d_static(const double *xyz, int64_t n, const double *
     CountArgs a;
     std::memset(&a, 0, sizeof(a));
     a.pos1 = a.pos2 = pos32;
-    a.x64_1 = a.x64_2 = pos64;
+    a.xyz1 = a.xyz2 = xyz;
+    a.orig1 = a.orig2 = reinterpret_cast<const int *>(W + O_ORIG);
     a.start2 = start;
     a.items = reinterpret_cast<const int4 *>(W + O_ITEMS);
     a.nitems = misc_i + 1;
@@ -201,9 +204,10 @@ extern "C" int gbp_npairs_3d_static(const double *xyz, int64_t n, const double *
     a.nsten = g.nsten;
     a.nself = g.nself;
     for (int d = 0; d < 3; d++) {
-        a.n[d] = g.n[d];
+        a.n[d] = g.nb[d];
         a.L[d] = g.L[d];
     }
+    a.bf3 = g.bf * g.bf * g.bf;
     a.pbc = g.pbc;
     AxisDev &ad = a.ax[0];
     ad.lut = reinterpret_cast<const float4 *>(W + O_LUT);
@@ -218,7 +222,7 @@ extern "C" int gbp_npairs_3d_static(const double *xyz, int64_t n, const double *
     ad.vhi = li.vhi;
     a.hist_stride = nbins + 1;
     a.hist_copies = GBP_WARPS;
-    a.ncells_mock = (int)g.ncells;
+    a.ncells_mock = (int)g.nblocks;
     a.hist_copies = 1;
     a.hist = reinterpret_cast<unsigned long long *>(W + O_HIST);
     a.nrecheck = misc + 2;

@@ -54,6 +54,8 @@ typedef struct {
     int32_t kernel_launches;  /* all kernel launches of the call */
     int64_t h2d_bytes;        /* host-to-device bytes copied by the call */
     int64_t d2h_bytes;        /* device-to-host bytes copied by the call */
+    int32_t block;            /* fine cells per block edge of the two-level grid (1: plain cells) */
+    int32_t reserved;
 } gbp_stats;
 
 /* Plan: a CUDA stream, cached device workspace and statistics. Not
@@ -64,6 +66,9 @@ int gbp_plan_destroy(gbp_plan *plan);
 int gbp_plan_set_stream(gbp_plan *plan, void *cuda_stream);
 /* Force the stencil reach (1..4 cells per search length); 0 = automatic. */
 int gbp_plan_set_reach(gbp_plan *plan, int reach);
+/* Force the block factor of the two-level grid (1..4 fine cells per block
+ * edge; 1 = plain cell list); 0 = automatic (blocks for sparse samples). */
+int gbp_plan_set_block(gbp_plan *plan, int block);
 /* 1: capture each call's stream work into one CUDA graph (instantiated once,
  * updated in place on later calls) and launch that; 0: launch directly. */
 int gbp_plan_set_graph(gbp_plan *plan, int enable);
