@@ -358,6 +358,8 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
             md.n[d] = c.g.n[d];
             md.nb[d] = c.g.nb[d];
             md.c[d] = c.g.c[d];
+            md.inv_c[d] = 1.0 / c.g.c[d]; md.inv_cf[d] = (float)(1.0 / c.g.c[d]);
+            md.Lf[d] = f_down(c.g.L[d]);
             md.L[d] = c.g.L[d];
         }
         md.ncells = ncells;

@@ -81,16 +81,17 @@ inline float bitsf(uint32_t u) {
 }
 
 // Error model.  Coordinates are FP32 offsets from a block corner, |u| <= c
-// (c = block size here), the stencil offset o*c (|o| <= K blocks) is rounded
+// (c = block size here), each rounded at most twice (float32 input forms
+// (x - hi) - lo in FP32), the stencil offset o*c (|o| <= K blocks) is rounded
 // to FP32 and added, and dx is formed in FP32:
-// |dx32 - dx| <= delta = 2^-24 (c + c + K c + (K+1) c + |dx|) plus the FP64
-// rounding of the corner and of the reference's own dx (~2^-50 L).
+// |dx32 - dx| <= delta = 2^-24 (2c + 2c + K c + (K+1) c + |dx|) plus the
+// corner's representation and the reference's own dx rounding (~2^-46 L).
 struct ErrModel {
     double cmax = 0, K = 1, Lmax = 0;
     double delta(double Ebound) const {
         double dxmax = std::sqrt(std::max(Ebound, 0.0));
-        return std::ldexp(1.0, -24) * (2 * cmax + K * cmax + (K + 1) * cmax + dxmax) * 1.02 +
-               std::ldexp(1.0, -50) * Lmax;
+        return std::ldexp(1.0, -24) * (4 * cmax + K * cmax + (K + 1) * cmax + dxmax) * 1.02 +
+               std::ldexp(1.0, -46) * Lmax;
     }
     // bound on |v32 - v64| for v a sum of m squares near E
     double band(double E, int m) const {
@@ -317,8 +318,13 @@ inline void build_stencil(Geometry &g, const double search[3], int kind, bool au
                                        (float)(oz * bf * g.c[2]), sp);
         g.nsten++;
     };
-    // gap along d between fine cell f (block-relative) and the block [0, bf)
-    auto gap = [&](int f, int d) { return g.c[d] * std::max(0, std::max(f - bf, -f - 1)); };
+    // gap along d between fine cell f (block-relative) and the block [0, bf),
+    // less the few-ulp distance a point may lie outside its cell (the digitiser
+    // picks the cell with a rounded reciprocal, in FP32 for float32 input)
+    const double slop = std::ldexp(std::max(g.L[0], std::max(g.L[1], g.L[2])), -19);
+    auto gap = [&](int f, int d) {
+        return std::max(0.0, g.c[d] * std::max(0, std::max(f - bf, -f - 1)) - slop);
+    };
     auto keep = [&](int fx, int fy, int fz) {
         double gx = gap(fx, 0), gy = gap(fy, 1), gz = gap(fz, 2);
         const double slack = 1.0 + 1e-9;

@@ -167,6 +167,9 @@ struct MeshDev {
     int bf;                     // fine cells per block edge (keys are block-major)
     int nb[3];                  // blocks per dimension
     double c[3];
+    double inv_c[3];            // 1 / c, rounded (only picks the cell)
+    float inv_cf[3];            // the same in FP32 (float32 input)
+    float Lf[3];                // largest float <= L (range check of float32 input)
     double L[3];
     int64_t ncells;             // cells per mock
     const int64_t *offsets;     // device, nmocks+1 point offsets (null: one sample)

@@ -14,64 +14,98 @@
 // per point over the two passes.
 #include "gbp_internal.cuh"
 
+#include <algorithm>
+
 #define SCAN_THREADS 1024
 #define SCAN_TILE (SCAN_THREADS * 4)
 
+// Block corners kb * bf * c per dimension: FP64 for FP64 input; for float32
+// input an unevaluated float pair (hi, lo) with hi + lo = the corner to 2^-48,
+// so that the cell-relative offset is formed in FP32 alone.
+#define GBP_CORNERS 256
+
 template <class T>
-__global__ void k_digitize(const T *__restrict__ xyz, int64_t npts, MeshDev m,
-                           int *__restrict__ cellid, int *__restrict__ rank,
-                           int *__restrict__ count, float4 *__restrict__ rel, int *err) {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    // every lane of the warp stays to the end (the cell match is warp-wide)
-    const bool live = i < npts;
-    int c = -1;
-    float u[3] = {0.f, 0.f, 0.f};
-    if (live) {
-        int mock = 0;
-        if (m.offsets) {  // largest mock with offsets[mock] <= i
-            int lo = 0, hi = m.nmocks - 1;
-            while (lo < hi) {
-                int mid = (lo + hi + 1) >> 1;
-                if (m.offsets[mid] <= i) lo = mid; else hi = mid - 1;
-            }
-            mock = lo;
+__global__ void __launch_bounds__(256) k_digitize(const T *__restrict__ xyz, int64_t npts, MeshDev m,
+                                                  int *__restrict__ cellid, int *__restrict__ rank,
+                                                  int *__restrict__ count, float4 *__restrict__ rel,
+                                                  int *err) {
+    constexpr bool F32 = sizeof(T) == 4;
+    __shared__ double s_cd[F32 ? 1 : 3 * GBP_CORNERS];
+    __shared__ float2 s_cf[F32 ? 3 * GBP_CORNERS : 1];
+    for (int t = threadIdx.x; t < 3 * GBP_CORNERS; t += blockDim.x) {
+        const int d = t / GBP_CORNERS, kb = t - d * GBP_CORNERS;
+        const double C = (double)(kb * m.bf) * m.c[d];
+        if (F32) {
+            const float hi = __double2float_rn(C);
+            s_cf[t] = make_float2(hi, __double2float_rn(C - (double)hi));
+        } else {
+            s_cd[t] = C;
         }
-        int ib[3], il[3];
-        bool bad = false;
-#pragma unroll
-        for (int d = 0; d < 3; d++) {
-            double x = (double)xyz[3 * i + d];
-            if (!(x >= 0.0 && x <= m.L[d])) bad = true;  // also catches NaN
-            double t = x * (1.0 / m.c[d]);
-            int k = (int)floor(t);
-            k = k < 0 ? 0 : (k >= m.n[d] ? m.n[d] - 1 : k);
-            ib[d] = k / m.bf;
-            il[d] = k - ib[d] * m.bf;
-            // offset from the block corner
-            u[d] = __double2float_rn(__dsub_rn(x, __dmul_rn((double)(ib[d] * m.bf), m.c[d])));
-        }
-        if (bad) {
-            atomicOr(err, 1);
-            ib[0] = ib[1] = ib[2] = il[0] = il[1] = il[2] = 0;
-            // far from everything, including idle lanes (+FAR) and padding (-FAR)
-            u[0] = u[1] = u[2] = -0.5f * GBP_FAR;
-        }
-        // block-major key: a block's fine cells (and so its points) are contiguous
-        const int bf = m.bf;
-        c = (int)(mock * m.ncells) + ((ib[0] * m.nb[1] + ib[1]) * m.nb[2] + ib[2]) * (bf * bf * bf) +
-            (il[0] * bf + il[1]) * bf + il[2];
     }
-    // points of one cell in one warp share a single atomic (input order often
-    // follows the clustering, e.g. satellites listed with their host)
-    const unsigned peers = __match_any_sync(0xffffffffu, c);
-    const int lane = threadIdx.x & 31, leader = __ffs(peers) - 1;
-    int base = 0;
-    if (live && lane == leader) base = atomicAdd(&count[c], __popc(peers));
-    base = __shfl_sync(0xffffffffu, base, leader);
-    if (live) {
-        cellid[i] = c;
-        rank[i] = base + __popc(peers & ((1u << lane) - 1u));
-        rel[i] = make_float4(u[0], u[1], u[2], __int_as_float((int)i));
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i - lane < npts; i += stride) {
+        // every lane of the warp stays to the end (the cell match is warp-wide)
+        const bool live = i < npts;
+        int c = -1;
+        float u[3] = {0.f, 0.f, 0.f};
+        if (live) {
+            int mock = 0;
+            if (m.offsets) {  // largest mock with offsets[mock] <= i
+                int lo = 0, hi = m.nmocks - 1;
+                while (lo < hi) {
+                    int mid = (lo + hi + 1) >> 1;
+                    if (m.offsets[mid] <= i) lo = mid; else hi = mid - 1;
+                }
+                mock = lo;
+            }
+            int ib[3], il[3];
+            bool bad = false;
+#pragma unroll
+            for (int d = 0; d < 3; d++) {
+                const T x = xyz[3 * i + d];
+                // also catches NaN; a float compares exactly against the largest float <= L
+                if (F32 ? !(x >= T(0) && (float)x <= m.Lf[d]) : !(x >= T(0) && (double)x <= m.L[d]))
+                    bad = true;
+                // the cell only needs to be right to a few ulps: the stencil's pruning
+                // and the error bound allow a point that far outside its cell
+                int k = F32 ? (int)floorf((float)x * m.inv_cf[d]) : (int)floor((double)x * m.inv_c[d]);
+                k = k < 0 ? 0 : (k >= m.n[d] ? m.n[d] - 1 : k);
+                ib[d] = k / m.bf;
+                il[d] = k - ib[d] * m.bf;
+                // offset from the block corner
+                if (F32) {
+                    const float2 C = s_cf[d * GBP_CORNERS + ib[d]];
+                    u[d] = ((float)x - C.x) - C.y;
+                } else {
+                    u[d] = __double2float_rn(__dsub_rn((double)x, s_cd[d * GBP_CORNERS + ib[d]]));
+                }
+            }
+            if (bad) {
+                atomicOr(err, 1);
+                ib[0] = ib[1] = ib[2] = il[0] = il[1] = il[2] = 0;
+                // far from everything, including idle lanes (+FAR) and padding (-FAR)
+                u[0] = u[1] = u[2] = -0.5f * GBP_FAR;
+            }
+            // block-major key: a block's fine cells (and so its points) are contiguous
+            const int bf = m.bf;
+            c = (int)(mock * m.ncells) +
+                ((ib[0] * m.nb[1] + ib[1]) * m.nb[2] + ib[2]) * (bf * bf * bf) +
+                (il[0] * bf + il[1]) * bf + il[2];
+        }
+        // points of one cell in one warp share a single atomic (input order often
+        // follows the clustering, e.g. satellites listed with their host)
+        const unsigned peers = __match_any_sync(0xffffffffu, c);
+        const int leader = __ffs(peers) - 1;
+        int base = 0;
+        if (live && lane == leader) base = atomicAdd(&count[c], __popc(peers));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (live) {
+            cellid[i] = c;
+            rank[i] = base + __popc(peers & ((1u << lane) - 1u));
+            rel[i] = make_float4(u[0], u[1], u[2], __int_as_float((int)i));
+        }
     }
 }
 
@@ -190,12 +224,14 @@ cudaError_t gbp_build_cells(const void *d_xyz, int xyz_f32, int64_t npts, const 
     // the FP32 relative records are staged in the pos32 buffer's twin (d_pos32 + npts)
     float4 *rel = d_pos32 + npts;
     unsigned g = (unsigned)((npts + 255) / 256);
+    // digitise: a grid-stride loop over a few waves of CTAs (each builds the corner table once)
+    const unsigned gd = (unsigned)std::min<int64_t>((npts + 255) / 256, 152 * 8);
     if (npts > 0) {
         if (xyz_f32)
-            k_digitize<float><<<g, 256, 0, st>>>((const float *)d_xyz, npts, m, d_cellid, d_rank,
+            k_digitize<float><<<gd, 256, 0, st>>>((const float *)d_xyz, npts, m, d_cellid, d_rank,
                                                  d_count, rel, d_err);
         else
-            k_digitize<double><<<g, 256, 0, st>>>((const double *)d_xyz, npts, m, d_cellid, d_rank,
+            k_digitize<double><<<gd, 256, 0, st>>>((const double *)d_xyz, npts, m, d_cellid, d_rank,
                                                   d_count, rel, d_err);
         if (launches) *launches += 1;
         if ((e = cudaGetLastError()) != cudaSuccess) return e;

@@ -159,6 +159,8 @@ extern "C" int gbp_npairs_3d_static(const double *xyz, int64_t n, const double *
         md.n[d] = g.n[d];
         md.nb[d] = g.nb[d];
         md.c[d] = g.c[d];
+        md.inv_c[d] = 1.0 / g.c[d]; md.inv_cf[d] = (float)(1.0 / g.c[d]);
+        md.Lf[d] = f_down(g.L[d]);
         md.L[d] = g.L[d];
     }
     md.ncells = g.ncells;
