@@ -245,13 +245,118 @@ def extra_differentiable(dev, reps=3):
             "dC_dtheta_last_bin": [float(v) for v in g.cpu().numpy()]}
 
 
+_POINTS_10M = []
+
+
+def points_10m():
+    """The 10M-point clustered sample of config 5 (generated once per process)."""
+    if not _POINTS_10M:
+        _POINTS_10M.append(make_points(WORKLOADS["3d10m"]))
+    return _POINTS_10M[0]
+
+
+def _time_gpu(stream, fn, reps=3):
+    fn()
+    t = []
+    for _ in range(reps):
+        a, b = _events()
+        a.record(stream)
+        fn()
+        b.record(stream)
+        import torch
+        torch.cuda.synchronize()
+        t.append(a.elapsed_time(b) / 1e3)
+    return float(np.median(t))
+
+
+def extra_marked_10m(dev, threads):
+    """Config 5: marked_npairs_3d with the product weight function (id 1), 30 log bins
+    0.5-50, on 10M clustered points (L = 2000).  Marks: a lognormal(0, 0.5) and a
+    uniform[0, 1) component, one call per component.  CPU: the oracle on the
+    1/64-volume sub-cube [0, 500)^3, non-periodic."""
+    import torch
+    from halotools_gb300 import _native as N
+    from oracle import oracle
+    w = WORKLOADS["3d10m"]
+    x = points_10m()
+    n = len(x)
+    rng = np.random.default_rng(51)
+    marks = [rng.lognormal(0.0, 0.5, n), rng.uniform(0.0, 1.0, n)]
+    xd = torch.from_numpy(x).cuda(dev)
+    md = [torch.from_numpy(m).cuda(dev) for m in marks]
+    plan = N.Plan(dev)
+    stream = torch.cuda.current_stream(dev)
+    plan.set_stream(stream.cuda_stream)
+    box = np.array([w["L"]] * 3)
+    rb = w["bins"]
+    outs = [np.zeros(len(rb)), np.zeros(len(rb))]
+
+    def run():
+        for m, o in zip(md, outs):
+            plan.check(plan.lib.gbp_marked_npairs_3d(
+                plan.handle, xd.data_ptr(), n, xd.data_ptr(), n, m.data_ptr(), m.data_ptr(), 1, 1,
+                N.pd(rb), len(rb), N.pd(box), 1, N.GBP_MEM_DEVICE, N.pd(o)))
+    tg = _time_gpu(stream, run)
+    ones = np.zeros(len(rb), dtype=np.int64)
+    call_device(plan, "3d", xd, n, w, box, ones)
+    pairs = 2 * int(ones[-1])  # two marked passes over the same pairs
+    sub_mask = np.all(x < 0.25 * w["L"], axis=1)
+    sub = np.ascontiguousarray(x[sub_mask])
+    msub = np.ascontiguousarray(marks[0][sub_mask])
+    t0 = time.perf_counter()
+    oracle.marked_npairs_3d(sub, sub, rb, 1, weights1=msub, weights2=msub, num_threads=threads)
+    dt = time.perf_counter() - t0
+    cpu_pairs = int(oracle.npairs_3d(sub, sub, rb, num_threads=threads)[-1])
+    return {"points": n, "channels": 2, "weight_func_id": 1, "gpu_ms": tg * 1e3,
+            "gpu_pairs_per_s": pairs / tg, "weighted_sums_last_bin": [float(o[-1]) for o in outs],
+            "cpu_pairs_per_s": cpu_pairs / dt, "cpu_cores": threads, "cpu_sample_points": len(sub),
+            "gpu_over_cpu": (pairs / tg) / (cpu_pairs / dt)}
+
+
+def extra_s_mu_10m(dev, threads):
+    """Config 5: npairs_s_mu, 30 log s bins 0.5-50 x 20 linear mu bins (21 edges 0-1),
+    line of sight z, on 10M clustered points (L = 2000).  CPU: the oracle on the
+    1/64-volume sub-cube [0, 500)^3, non-periodic."""
+    import torch
+    from halotools_gb300 import _native as N
+    from oracle import oracle
+    w = WORKLOADS["3d10m"]
+    x = points_10m()
+    n = len(x)
+    sb = w["bins"]
+    mu = np.linspace(0.0, 1.0, 21)
+    mup = np.sort(np.sin(np.arccos(mu)))
+    xd = torch.from_numpy(x).cuda(dev)
+    plan = N.Plan(dev)
+    stream = torch.cuda.current_stream(dev)
+    plan.set_stream(stream.cuda_stream)
+    box = np.array([w["L"]] * 3)
+    out = np.zeros((len(sb), len(mu)), dtype=np.int64)
+
+    def run():
+        plan.check(plan.lib.gbp_npairs_s_mu(plan.handle, xd.data_ptr(), n, xd.data_ptr(), n,
+                                            N.pd(sb), len(sb), N.pd(mup), len(mup), N.pd(box), 1,
+                                            N.GBP_MEM_DEVICE, N.pi64(out)))
+    tg = _time_gpu(stream, run)
+    pairs = int(out[-1, -1])
+    sub = cpu_sample(x, w, 0.25)
+    t0 = time.perf_counter()
+    c = oracle.npairs_s_mu(sub, sub, sb, mu, num_threads=threads)
+    dt = time.perf_counter() - t0
+    cpu = int(c[-1, -1]) / dt
+    return {"points": n, "gpu_ms": tg * 1e3, "gpu_pairs_per_s": pairs / tg,
+            "cpu_pairs_per_s": cpu, "cpu_cores": threads, "cpu_sample_points": len(sub),
+            "gpu_over_cpu": (pairs / tg) / cpu, "stats": {k: plan.stats()[k] for k in
+                                                       ("ms_build", "ms_count", "block", "reach")}}
+
+
 def extra_npairs_3d_10m(dev, threads):
     """Config 5 geometry: plain npairs_3d on 10M clustered points (L = 2000, 30 log bins
     0.5-50) against the all-core CPU oracle on a 1/64-volume sub-cube."""
     import torch
     from halotools_gb300 import _native as N
     w = WORKLOADS["3d10m"]
-    x = make_points(w)
+    x = points_10m()
     xd = torch.from_numpy(x).cuda(dev)
     plan = N.Plan(dev)
     stream = torch.cuda.current_stream(dev)
@@ -272,6 +377,15 @@ def extra_npairs_3d_10m(dev, threads):
             "gpu_over_cpu": gpu / cpu}
 
 
+EXTRAS = {
+    "batched_hod64": lambda dev, threads: extra_batched(dev),
+    "differentiable_2m": lambda dev, threads: extra_differentiable(dev),
+    "npairs_3d_10m": extra_npairs_3d_10m,
+    "marked_10m": extra_marked_10m,
+    "s_mu_10m": extra_s_mu_10m,
+}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -282,7 +396,15 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the batched / differentiable / 10M-point comparison paths")
+    ap.add_argument("--only-path", choices=sorted(EXTRAS),
+                    help="run one comparison path alone and print its JSON (profiling)")
     args = ap.parse_args()
+    if args.only_path:
+        import torch
+        torch.cuda.set_device(0)
+        print(json.dumps({"path": args.only_path,
+                          **EXTRAS[args.only_path](0, os.cpu_count() or 1)}))
+        return 0
     w = WORKLOADS[args.workload]
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -417,11 +539,9 @@ def main():
                                           "C oracle cell walk, %.1f s" % (nsub, frac_side * w["L"], dt)}
     if rank == 0 and world == 1 and not args.no_extras:
         extras = {}
-        for name, fn in (("batched_hod64", lambda: extra_batched(dev)),
-                         ("differentiable_2m", lambda: extra_differentiable(dev)),
-                         ("npairs_3d_10m", lambda: extra_npairs_3d_10m(dev, threads))):
+        for name, fn in EXTRAS.items():
             try:
-                extras[name] = fn()
+                extras[name] = fn(dev, threads)
             except Exception as exc:  # report, never hide
                 extras[name] = {"error": repr(exc)[:300]}
         line["paths"] = extras
