@@ -270,9 +270,11 @@ def _time_gpu(stream, fn, reps=3):
 
 
 def extra_marked_10m(dev, threads):
-    """Config 5: marked_npairs_3d with the product weight function (id 1), 30 log bins
+    """Config 5: marked counts with the product weight function (id 1), 30 log bins
     0.5-50, on 10M clustered points (L = 2000).  Marks: a lognormal(0, 0.5) and a
-    uniform[0, 1) component, one call per component.  CPU: the oracle on the
+    uniform[0, 1) component, both channels in one launch; then 8 random-mark draws
+    (permutations of the lognormal component, as marked_tpcf's randomisation) in one
+    launch against 8 single-channel calls.  CPU: the oracle, one channel, on the
     1/64-volume sub-cube [0, 500)^3, non-periodic."""
     import torch
     from halotools_gb300 import _native as N
@@ -281,36 +283,53 @@ def extra_marked_10m(dev, threads):
     x = points_10m()
     n = len(x)
     rng = np.random.default_rng(51)
-    marks = [rng.lognormal(0.0, 0.5, n), rng.uniform(0.0, 1.0, n)]
+    comp = np.stack([rng.lognormal(0.0, 0.5, n), rng.uniform(0.0, 1.0, n)], axis=1)
+    draws = np.stack([rng.permutation(comp[:, 0]) for _ in range(8)], axis=1)
     xd = torch.from_numpy(x).cuda(dev)
-    md = [torch.from_numpy(m).cuda(dev) for m in marks]
+    cd = torch.from_numpy(np.ascontiguousarray(comp)).cuda(dev)
+    dd = torch.from_numpy(np.ascontiguousarray(draws)).cuda(dev)
+    cols = [dd[:, c].contiguous() for c in range(8)]
     plan = N.Plan(dev)
     stream = torch.cuda.current_stream(dev)
     plan.set_stream(stream.cuda_stream)
     box = np.array([w["L"]] * 3)
     rb = w["bins"]
-    outs = [np.zeros(len(rb)), np.zeros(len(rb))]
+    o2 = np.zeros((2, len(rb)))
+    o8 = np.zeros((8, len(rb)))
+    o1 = np.zeros(len(rb))
 
-    def run():
-        for m, o in zip(md, outs):
+    def channels(wt, out):
+        plan.check(plan.lib.gbp_marked_npairs_3d_channels(
+            plan.handle, xd.data_ptr(), n, xd.data_ptr(), n, wt.data_ptr(), wt.data_ptr(),
+            wt.shape[1], N.pd(rb), len(rb), N.pd(box), 1, N.GBP_MEM_DEVICE, N.pd(out)))
+
+    def separate():
+        for col in cols:
             plan.check(plan.lib.gbp_marked_npairs_3d(
-                plan.handle, xd.data_ptr(), n, xd.data_ptr(), n, m.data_ptr(), m.data_ptr(), 1, 1,
-                N.pd(rb), len(rb), N.pd(box), 1, N.GBP_MEM_DEVICE, N.pd(o)))
-    tg = _time_gpu(stream, run)
+                plan.handle, xd.data_ptr(), n, xd.data_ptr(), n, col.data_ptr(), col.data_ptr(), 1,
+                1, N.pd(rb), len(rb), N.pd(box), 1, N.GBP_MEM_DEVICE, N.pd(o1)))
+    t2 = _time_gpu(stream, lambda: channels(cd, o2))
+    t8 = _time_gpu(stream, lambda: channels(dd, o8))
+    t8s = _time_gpu(stream, separate, reps=1)
+    np.testing.assert_allclose(o8[-1], o1, rtol=1e-6)  # last draw: one launch == separate call
     ones = np.zeros(len(rb), dtype=np.int64)
     call_device(plan, "3d", xd, n, w, box, ones)
-    pairs = 2 * int(ones[-1])  # two marked passes over the same pairs
+    pairs = int(ones[-1])
     sub_mask = np.all(x < 0.25 * w["L"], axis=1)
     sub = np.ascontiguousarray(x[sub_mask])
-    msub = np.ascontiguousarray(marks[0][sub_mask])
+    msub = np.ascontiguousarray(comp[sub_mask, 0])
     t0 = time.perf_counter()
     oracle.marked_npairs_3d(sub, sub, rb, 1, weights1=msub, weights2=msub, num_threads=threads)
     dt = time.perf_counter() - t0
     cpu_pairs = int(oracle.npairs_3d(sub, sub, rb, num_threads=threads)[-1])
-    return {"points": n, "channels": 2, "weight_func_id": 1, "gpu_ms": tg * 1e3,
-            "gpu_pairs_per_s": pairs / tg, "weighted_sums_last_bin": [float(o[-1]) for o in outs],
+    return {"points": n, "in_range_pairs": pairs, "weight_func_id": 1,
+            "two_components_one_launch_ms": t2 * 1e3,
+            "two_components_pair_evals_per_s": 2 * pairs / t2,
+            "eight_draws_one_launch_ms": t8 * 1e3, "eight_draws_separate_ms": t8s * 1e3,
+            "eight_draws_speedup": t8s / t8, "eight_draws_pair_evals_per_s": 8 * pairs / t8,
+            "weighted_sums_last_bin": [float(v) for v in o2[:, -1]],
             "cpu_pairs_per_s": cpu_pairs / dt, "cpu_cores": threads, "cpu_sample_points": len(sub),
-            "gpu_over_cpu": (pairs / tg) / (cpu_pairs / dt)}
+            "gpu_over_cpu": (2 * pairs / t2) / (cpu_pairs / dt)}
 
 
 def extra_s_mu_10m(dev, threads):

@@ -7,13 +7,13 @@ run on hand-written sm_103a CUDA kernels through the C ABI declared in
 halotools' estimators bound at import time, so ``tpcf``, ``wp``,
 ``rp_pi_tpcf``, ``s_mu_tpcf`` and ``marked_tpcf`` pick them up as drop-ins.
 """
-from .pair_counters import (HalotoolsError, marked_npairs_3d, npairs_3d, npairs_s_mu,
-                            npairs_xy_z)
+from .pair_counters import (HalotoolsError, marked_npairs_3d, marked_npairs_3d_channels,
+                            npairs_3d, npairs_s_mu, npairs_xy_z)
 from ._native import GBPairsError, GBPairsUnavailable, Plan, default_plan
 from .batched import BatchedCounter, npairs_3d_batched
 
-__all__ = ("npairs_3d", "npairs_xy_z", "npairs_s_mu", "marked_npairs_3d", "HalotoolsError",
-           "GBPairsError", "GBPairsUnavailable", "Plan", "default_plan",
+__all__ = ("npairs_3d", "npairs_xy_z", "npairs_s_mu", "marked_npairs_3d",
+           "marked_npairs_3d_channels", "HalotoolsError", "GBPairsError", "GBPairsUnavailable", "Plan", "default_plan",
            "npairs_3d_batched", "BatchedCounter", "install_into_halotools")
 
 # module attribute -> our function, for every place halotools binds a counter

@@ -195,7 +195,9 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
     const int nb0 = c.ax[0].nb, nb1 = c.naxes > 1 ? c.ax[1].nb : 0;
     const int T0 = c.ax[0].T, T1 = c.naxes > 1 ? c.ax[1].T : 0;
     const int nsten = c.g.nsten;
-    const size_t nhist = (size_t)(nb0 + 1) * (size_t)(c.naxes > 1 ? nb1 + 1 : 1);
+    // MARKC: one (nb0 + 1) histogram per mark channel
+    const size_t nhist = (size_t)(nb0 + 1) * (size_t)(c.naxes > 1 ? nb1 + 1 : 1) *
+                         (size_t)(c.mode == MODE_MARKC ? c.nw : 1);
     const int nsamp = c.autocorr ? 1 : 2;
     const int64_t ns[2] = {c.n1, c.n2};
 
@@ -446,11 +448,14 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
         a.top0 = std::min(c.ax[0].hi[nb0 - 1], 1.0e30f);
         a.top1 = c.naxes > 1 ? std::min(c.ax[1].hi[nb1 - 1], 1.0e30f) : 0.f;
         a.self_bin = host_bin(nb0, c.ax[0].E.data(), 0.0);
-        const int jwb = c.mode == MODE_MARK ? (c.wf == 0 ? 8 * c.nw : 4) : (c.mode == MODE_ADJ ? 4 : 0);
+        const int jwb = c.mode == MODE_MARK    ? (c.wf == 0 ? 8 * c.nw : 4)
+                        : c.mode == MODE_MARKC ? 4 * c.nw
+                        : c.mode == MODE_ADJ   ? 4
+                                               : 0;
         // 2-D and wide 1-D histograms: one shared copy per warp while they fit,
         // else the warps add straight into the global histogram
         int copies = GBP_WARPS;
-        if (c.mode != MODE_3D && c.mode != MODE_MARK && c.mode != MODE_ADJ) {
+        if (c.mode != MODE_3D && c.mode != MODE_MARK && c.mode != MODE_MARKC && c.mode != MODE_ADJ) {
             size_t one = (size_t)(nb0 + 1) * (size_t)(c.naxes > 1 ? nb1 + 1 : 1) * 4;
             if (one * GBP_WARPS > (96u << 10)) copies = 0;
         }
@@ -525,7 +530,7 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
         return run_call(plan, c, hist_host, histd_host);
     }
     hist_host.assign(at<unsigned long long>(H, h_hist), at<unsigned long long>(H, h_hist) + nm * nhist);
-    if (c.mode != MODE_MARK) add_self_pairs(c, hist_host);
+    if (c.mode != MODE_MARK && c.mode != MODE_MARKC) add_self_pairs(c, hist_host);
     if (histd_host) histd_host->assign(at<double>(H, h_histd), at<double>(H, h_histd) + nm * nhist);
     gbp_stats &S = plan->stats;
     S.recheck_pairs = (int64_t)hm[2];
@@ -943,6 +948,56 @@ int gbp_marked_npairs_3d(gbp_plan *plan, const double *xyz1, int64_t n1, const d
     for (int k = 0; k < nb; k++) {
         run += hd[k];
         out[k] = run;
+    }
+    return GBP_OK;
+}
+
+int gbp_marked_npairs_3d_channels(gbp_plan *plan, const double *xyz1, int64_t n1,
+                                  const double *xyz2, int64_t n2, const double *w1,
+                                  const double *w2, int32_t nch, const double *rbins, int32_t nb,
+                                  const double *period3, int32_t pbc, int32_t mem, double *out) {
+    int rc = check_common(plan, xyz1, n1, xyz2, n2, period3, pbc, mem);
+    if (rc) return rc;
+    if (nch < 1 || nch > 32) return fail(plan, GBP_ERR_INVALID, "nch must be 1..32, got %d", nch);
+    if ((n1 > 0 && !w1) || (n2 > 0 && !w2)) return fail(plan, GBP_ERR_INVALID, "null weights");
+    if (!rbins || nb < 2 || nb > GBP_NB_LANE || !out)
+        return fail(plan, GBP_ERR_INVALID, "rbins must have 2..%d entries", GBP_NB_LANE);
+    double rmax = max_nan(rbins, nb);
+    double search[3] = {rmax, rmax, rmax};
+    if ((rc = check_search(plan, search, period3))) return rc;
+    Call c;
+    c.mode = MODE_MARKC;
+    c.wf = 1;
+    c.xyz1 = xyz1;
+    c.xyz2 = xyz2;
+    c.n1 = n1;
+    c.n2 = n2;
+    // the product is symmetric: an auto-correlation walks each unordered pair once
+    c.autocorr = (xyz1 == xyz2 && n1 == n2 && w1 == w2);
+    c.mem = mem;
+    c.w1 = w1;
+    c.w2 = w2;
+    c.nw = nch;
+    c.wfunc = 1;
+    c.naxes = 1;
+    choose_grid(c.g, period3, search, pbc, n2, plan->reach, MAX_CELLS_PER_DIM, 0.0, plan->block);
+    build_stencil(c.g, search, 0, c.autocorr);
+    ErrModel em = err_model(c.g);
+    std::vector<double> E(nb);
+    edges_top_walk(rbins, nb, E.data());
+    c.ax[0].set(E, &em, 3);
+    c.ax[0].make_lut(no_qband);
+    for (int k = 0; k < nch * nb; k++) out[k] = 0.0;
+    if (n1 == 0 || n2 == 0) return GBP_OK;
+    std::vector<unsigned long long> h;
+    std::vector<double> hd;
+    if ((rc = run_call(plan, c, h, &hd))) return rc;
+    for (int ch = 0; ch < nch; ch++) {
+        double run = 0.0;
+        for (int k = 0; k < nb; k++) {
+            run += hd[(size_t)ch * (nb + 1) + k];
+            out[(size_t)ch * nb + k] = run;
+        }
     }
     return GBP_OK;
 }

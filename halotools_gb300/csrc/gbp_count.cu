@@ -321,13 +321,14 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     constexpr bool TWO = (MODE == MODE_XYZ || MODE == MODE_SMU);
     constexpr bool MARK = (MODE == MODE_MARK);
+    constexpr bool MARKC = (MODE == MODE_MARKC);  // nw = channels of product marks
     constexpr unsigned FULL = 0xffffffffu;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nb0 = a.ax[0].nb, nb1 = TWO ? a.ax[1].nb : 0;
     const int T0 = a.ax[0].T, T1 = TWO ? a.ax[1].T : 0;
     const int copies = a.hist_copies;  // 2-D / wide: GBP_WARPS (one per warp) or 0 (global)
-    const int nw = MARK ? a.nw : 0;
-    const int jwb = MARK ? (WF == 0 ? 8 * nw : 4) : 0;
+    const int nw = (MARK || MARKC) ? a.nw : 0;
+    const int jwb = MARK ? (WF == 0 ? 8 * nw : 4) : MARKC ? 4 * nw : 0;
     const SmemLayout L = gbp_smem_layout(MODE, T0, T1, nb0, nb1, a.nsten, copies, jwb);
     unsigned *s_l0 = (unsigned *)(smem + L.off_lut0);
     unsigned *s_l1 = (unsigned *)(smem + L.off_lut1);
@@ -341,7 +342,7 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
     // the same j-points with each coordinate twice, for the packed stage 1
     ulonglong2 *jxy = (ulonglong2 *)(smem + L.off_j2) + warp * 32;
     unsigned long long *jzz = (unsigned long long *)(smem + L.off_j2 + GBP_JCAP * 16) + warp * 32;
-    float *jw = (float *)(smem + L.off_jw) + warp * 32;
+    float *jw = (float *)(smem + L.off_jw) + warp * 32 * (MARKC ? nw : 1);
     double *jw64 = (double *)(smem + L.off_jw) + warp * 32 * (nw > 0 ? nw : 1);
     float4 *s_D = (float4 *)(smem + L.off_D);
     double *s_E0 = (double *)(smem + L.off_E0);
@@ -356,7 +357,10 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
     float *ux = (float *)(smem + L.off_q) + warp * 4 * GBP_USLOTS;
     float *uy = ux + GBP_USLOTS, *uz = ux + 2 * GBP_USLOTS;
     int *uix = (int *)(ux + 3 * GBP_USLOTS);
-    float *s_uw = (float *)(smem + L.off_q + GBP_WARPS * GBP_USLOTS * 16) + warp * GBP_USLOTS;
+    float *s_uw = (float *)(smem + L.off_q + GBP_WARPS * GBP_USLOTS * 16) +
+                  warp * GBP_USLOTS * (MARKC ? nw : 1);
+    // MARKC: this warp's binned pairs of one round {bin | multiplicity << 16, second bin, i, j}
+    int4 *s_rec = (int4 *)(smem + L.off_rec) + warp * 32;
     double *s_uw64 = (double *)(smem + L.off_q + GBP_WARPS * GBP_USLOTS * 16) +
                      warp * GBP_USLOTS * (nw > 0 ? nw : 1);
     const Ix ix{uix, jix};
@@ -382,8 +386,8 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
     }
     const int nbin = (nb0 + 1) * (TWO ? nb1 + 1 : 1);
     // this warp's histogram words: lane-private (3-D, marked) or its own copy
-    const int warp_words = (MODE == MODE_3D) ? (nb0 + 1) * 32 : MARK ? (nb0 + 1) * 32 * 2
-                                                                : (copies ? nbin : 0);
+    const int warp_words = (MODE == MODE_3D) ? (nb0 + 1) * 32
+                           : (MARK || MARKC) ? (nb0 + 1) * 32 * 2 : (copies ? nbin : 0);
     unsigned *wh = s_hist + warp * warp_words;
     for (int i = lane; i < warp_words; i += 32) wh[i] = 0u;
     AxisSm A0{nullptr, s_hi0, s_lo0, s_E0, nb0, a.ax[0].S, a.ax[0].B, a.ax[0].vlo, a.ax[0].vhi,
@@ -431,6 +435,18 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(FULL, v, o);
                 if (lane == 0 && v) atomicAdd(&gh[b], v);
+            }
+        } else if (MARKC) {
+            // lane = (pair group g, channel c): channel c sums lanes c, c + nw, ...
+            double *gd = a.histd + (size_t)mk * a.hist_stride;
+            const int G = 32 / nw, c = lane % nw;
+            for (int b = 0; b < nb0; b++) {
+                const double v = (double)hs[b * 32] - (double)hc[b * 32];
+                hs[b * 32] = 0.f;
+                hc[b * 32] = 0.f;
+                double tot = 0.0;
+                for (int g = 0; g < G; g++) tot += __shfl_sync(FULL, v, g * nw + c);
+                if (lane < nw && tot != 0.0) atomicAdd(&gd[lane * (nb0 + 1) + b], tot);
             }
         } else if (MARK) {
             double *gd = a.histd + (size_t)mk * a.hist_stride;
@@ -500,6 +516,13 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                 s_uw[lane + 48] = w1;
             }
         }
+        if (MARKC) {
+            for (int k = 0; k < nw; k++) {
+                s_uw[lane * nw + k] = lane < icnt ? a.w1[(int64_t)(ifirst + lane) * nw + k] : 0.f;
+                s_uw[(lane + 48) * nw + k] =
+                    lane + 32 < icnt ? a.w1[(int64_t)(ifirst + 32 + lane) * nw + k] : 0.f;
+            }
+        }
         __syncwarp();
         for (int sb = s0; sb < s1; sb += 32) {
             // one stencil entry per lane: its j range and FP32 cell offset
@@ -553,6 +576,8 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                             jw[lane] = a.w2[j];
                         }
                     }
+                    if (MARKC)
+                        for (int q = 0; q < nw; q++) jw[lane * nw + q] = a.w2[(int64_t)j * nw + q];
                 } else {
                     // padding slot: at -FAR, so it is 2*FAR from an idle i-lane (+FAR)
                     // and farther still from every real point; its bits are also masked
@@ -601,8 +626,9 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                 const unsigned valid = nj >= 32 ? 0xffffffffu : ((1u << nj) - 1u);
                 unsigned m0 = __brev(~o0) & valid;
                 unsigned m1 = __brev(~o1) & valid;
-                if (ns > 0) {
+                if (ns > 0 && !MARKC) {
                     // own cell: (i, i) has separation exactly 0 and is handled apart
+                    // (MARKC bins it like any pair: v = 0 exactly)
                     for (int jj = 0; jj < ns; jj++) {
                         const int jt = jix[jj];
                         if (jt == is0) {
@@ -623,10 +649,8 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                         }
                     }
                 }
-                // stage 2, warp-cooperative: the warp's in-range pairs are numbered
-                // lane by lane (prefix sum of the bit counts) and each lane bins one
-                // pair per round; the owner lane is found by a 5-step search over
-                // the prefix and the pair's bit by __fns (n-th set bit)
+                // stage 2: the warp's in-range pairs are numbered lane by lane
+                // (prefix sum of the bit counts), written as codes, then binned
                 const unsigned own_bits = ns >= 32 ? 0xffffffffu : ((1u << ns) - 1u);
                 const unsigned sym_bits = a.nself ? ~own_bits : 0u;
                 const int c0 = __popc(m0);
@@ -681,13 +705,54 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                     }
                     return PairV{v0, v1, iu, jj, ((sym_bits >> jj) & 1u) != 0u};
                 };
-                for (int r0 = 0; r0 < C; r0 += 64) {
-                    const int sa = r0 + lane, sb = sa + 32;
-                    const bool ha = sa < C, hb = sb < C;
-                    const PairV ea = entry(ha ? s_code[sa] : 0);
-                    const PairV eb = entry(hb ? s_code[sb] : 0);
-                    if (ha) bin_entry(ea, cur_mock);
-                    if (hb) bin_entry(eb, cur_mock);
+                if (MARKC) {
+                    // each lane bins one pair per round; then lane (g, c) adds channel
+                    // c's product for pairs g, g + G, ... of the round to its own
+                    // Kahan column, so no two lanes touch one column
+                    const int G = 32 / nw, g = lane / nw, ch = lane - g * nw;
+                    for (int r0 = 0; r0 < C; r0 += 32) {
+                        const int sa = r0 + lane;
+                        int b0 = nb0, b1 = nb0, mult = 1, iu = 0, jj = 0;
+                        if (sa < C) {
+                            const PairV e = entry(s_code[sa]);
+                            iu = e.iu;
+                            jj = e.jj;
+                            mult = e.sym ? 2 : 1;
+                            const float4 t = lut_entry_c<false>(e.v0, A0);
+                            b0 = __float_as_int(t.x) + (e.v0 > t.y ? 1 : 0);
+                            if ((e.v0 > t.z) & !(e.v0 > t.y)) {
+                                int k[2];
+                                const int n = slow_3d(e.v0, __float_as_int(t.x), ix.ui[iu], ix.jw[jj],
+                                                      e.sym, k, A0, a);
+                                b0 = k[0];
+                                if (n == 2) {
+                                    b1 = k[1];
+                                    mult = 1;
+                                }
+                            }
+                        }
+                        s_rec[lane] = make_int4(b0 | (mult << 16), b1, iu, jj);
+                        __syncwarp();
+                        const int np = min(32, C - r0);
+                        for (int p = g; p < np; p += G) {
+                            if (g >= G) break;
+                            const int4 r = s_rec[p];
+                            const float val = s_uw[r.z * nw + ch] * jw[r.w * nw + ch];
+                            const int rb0 = r.x & 0xffff;
+                            if (rb0 < nb0) kahan_add(hs, hc, rb0, (r.x >> 16) == 2 ? 2.0f * val : val);
+                            if (r.y < nb0) kahan_add(hs, hc, r.y, val);
+                        }
+                        __syncwarp();
+                    }
+                } else {
+                    for (int r0 = 0; r0 < C; r0 += 64) {
+                        const int sa = r0 + lane, sb = sa + 32;
+                        const bool ha = sa < C, hb = sb < C;
+                        const PairV ea = entry(ha ? s_code[sa] : 0);
+                        const PairV eb = entry(hb ? s_code[sb] : 0);
+                        if (ha) bin_entry(ea, cur_mock);
+                        if (hb) bin_entry(eb, cur_mock);
+                    }
                 }
                 drained += 64;
                 __syncwarp();
@@ -695,7 +760,7 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
         }
         // a lane adds at most 2 per pair of its own and a warp copy at most 64
         // per lane: flush long before a u32 could wrap
-        if (!MARK && drained > (1ull << 24)) warp_flush(cur_mock);
+        if (!MARK && !MARKC && drained > (1ull << 24)) warp_flush(cur_mock);
     }
     if (cur_mock >= 0) warp_flush(cur_mock);
     if (lane == 0 && cand) atomicAdd(a.nrecheck + 1, cand);
@@ -729,6 +794,8 @@ cudaError_t gbp_launch_count(int mode, int wf, const CountArgs &a, int grid, siz
     case MODE_3DS: return launch_t<MODE_3DS, 1>(a, grid, smem, st);
     case MODE_XYZ: return launch_t<MODE_XYZ, 1>(a, grid, smem, st);
     case MODE_SMU: return launch_t<MODE_SMU, 1>(a, grid, smem, st);
+    case MODE_MARKC:
+        return launch_t<MODE_MARKC, 1>(a, grid, smem, st);
     case MODE_MARK:
         if (wf == 1) return launch_t<MODE_MARK, 1>(a, grid, smem, st);
         if (wf == 2) return launch_t<MODE_MARK, 2>(a, grid, smem, st);
@@ -743,6 +810,8 @@ int gbp_count_occupancy(int mode, int wf, size_t smem) {
     case MODE_3DS: return occ_t<MODE_3DS, 1>(smem);
     case MODE_XYZ: return occ_t<MODE_XYZ, 1>(smem);
     case MODE_SMU: return occ_t<MODE_SMU, 1>(smem);
+    case MODE_MARKC:
+        return occ_t<MODE_MARKC, 1>(smem);
     case MODE_MARK:
         if (wf == 1) return occ_t<MODE_MARK, 1>(smem);
         if (wf == 2) return occ_t<MODE_MARK, 2>(smem);

@@ -24,7 +24,8 @@
 #define GBP_SMAX 512        // stencil cells
 #define GBP_FAR 1.0e18f     // coordinate of an idle lane: far outside every edge
 
-enum { MODE_3D = 0, MODE_XYZ = 1, MODE_SMU = 2, MODE_MARK = 3, MODE_ADJ = 4, MODE_3DS = 5 };
+enum { MODE_3D = 0, MODE_XYZ = 1, MODE_SMU = 2, MODE_MARK = 3, MODE_ADJ = 4, MODE_3DS = 5,
+       MODE_MARKC = 6 };  // MARKC: product marks (id 1) over several channels in one pass
 
 // One binning axis: squared quantity v compared with edges E'[0..nb-1]
 // (non-decreasing); bin(v) = smallest k with v <= E'[k], nb if none.
@@ -89,7 +90,7 @@ struct CountArgs {
 // jw: bytes of staged weights per j-point (marked mode), copies: shared
 // histogram copies (2-D and wide 1-D modes).
 struct SmemLayout {
-    int off_lut0, off_lut1, off_qb, off_hl0, off_hl1, off_j, off_j2, off_jw, off_q, off_code, off_D,
+    int off_lut0, off_lut1, off_qb, off_hl0, off_hl1, off_j, off_j2, off_jw, off_q, off_code, off_rec, off_D,
         off_E0, off_E1, off_hi0, off_lo0, off_hi1, off_lo1, off_off, off_hist, total;
 };
 
@@ -119,6 +120,7 @@ __host__ __device__ inline SmemLayout gbp_smem_layout(int mode, int T0, int T1, 
     o += adj ? 0 : GBP_WARPS * GBP_USLOTS * 16 +
                        gbp_align(GBP_WARPS * GBP_USLOTS * (jw > 4 ? jw : 4), 16);
     L.off_code = o; o += (mode == MODE_ADJ) ? 0 : GBP_WARPS * 2048 * 2;
+    L.off_rec = o; o += (mode == MODE_MARKC) ? GBP_WARPS * 32 * 16 : 0;  // binned pairs of a round
     L.off_D = o; o += nsten * 16;
     L.off_E0 = o; o += gbp_align(nb0 * 8, 16);
     L.off_E1 = o; o += gbp_align(nb1 * 8, 16);
@@ -131,7 +133,7 @@ __host__ __device__ inline SmemLayout gbp_smem_layout(int mode, int T0, int T1, 
     int hist_bytes;
     if (mode == MODE_3D) {
         hist_bytes = GBP_WARPS * (nb0 + 1) * 32 * 4;          // lane-private u32
-    } else if (mode == MODE_MARK) {
+    } else if (mode == MODE_MARK || mode == MODE_MARKC) {
         hist_bytes = GBP_WARPS * (nb0 + 1) * 32 * 4 * 2;      // lane-private FP32 sum + compensation
     } else if (mode == MODE_ADJ) {
         hist_bytes = GBP_BLOCK * 8 + gbp_align((nb0 + 1) * 4, 16);  // partial sums + gt table

@@ -308,3 +308,54 @@ def marked_npairs_3d(sample1, sample2, rbins, weight_func_id, period=None, weigh
                                              _native.pd(rbins), len(rbins), _native.pd(box), pbc,
                                              GBP_MEM_HOST, _native.pd(out)))
     return out
+
+
+def marked_npairs_3d_channels(sample1, sample2, rbins, period=None, weights1=None,
+                              weights2=None, num_threads=1, approx_cell1_size=None,
+                              approx_cell2_size=None):
+    """Product-mark counts over several mark channels in one pass.
+
+    ``weights1`` / ``weights2``: (N, nch) arrays, nch <= 32 (a 1-D array is one
+    channel). Returns (nch, len(rbins)) float64 whose row c equals
+    ``marked_npairs_3d(sample1, sample2, rbins, 1, period, weights1[:, c],
+    weights2[:, c])`` (marked_npairs_3d.py:25 with the product weight function,
+    marking_functions.pyx:36-43): e.g. the random-mark draws of marked_tpcf
+    (marked_tpcf.py:327-345) evaluated together. Each pair is binned once.
+    """
+    _check_num_threads(num_threads)
+    rbins = _bins(rbins, "Input ``rbins`` must be a monotonically increasing 1D array with at "
+                         "least two entries")
+    rmax = np.max(rbins)
+    _approx_cells(approx_cell1_size, [rmax] * 3, "approx_cell1_size")
+    _approx_cells(approx_cell2_size, [rmax] * 3, "approx_cell2_size")
+    x1, x2, box, pbc = _positions(sample1, sample2, period, [rmax] * 3, [rmax * 3.0] * 3)
+    _nonneg(rbins, "rbins")
+
+    def marks(w, n, name):
+        if w is None:
+            return np.ones((n, 1))
+        w = np.asarray(w, dtype=np.float64)
+        if w.ndim == 1:
+            w = w[:, None]
+        if w.ndim != 2 or w.shape[0] != n:
+            raise HalotoolsError("``%s`` must have shape (N, nch) with N the number of "
+                                 "points" % name)
+        return np.ascontiguousarray(w)
+    w1 = marks(weights1, len(x1), "weights1")
+    w2 = marks(weights2, len(x2), "weights2") if weights2 is not None or x2 is not x1 else w1
+    if w1.shape[1] != w2.shape[1]:
+        raise HalotoolsError("``weights1`` and ``weights2`` must have the same number of channels")
+    nch = w1.shape[1]
+    if not 1 <= nch <= 32:
+        raise ValueError("1 to 32 mark channels are supported, got %d" % nch)
+    if x2 is x1 and not (w2 is w1 or np.array_equal(w1, w2)):
+        x2 = x1.copy()  # same points, different marks: count as a cross-correlation
+    if x2 is x1:
+        w2 = w1
+    plan = _native.default_plan()
+    out = np.zeros((nch, len(rbins)), dtype=np.float64)
+    plan.check(plan.lib.gbp_marked_npairs_3d_channels(
+        plan.handle, _native.dptr(x1), len(x1), _native.dptr(x2), len(x2), _native.dptr(w1),
+        _native.dptr(w2), nch, _native.pd(rbins), len(rbins), _native.pd(box), pbc,
+        GBP_MEM_HOST, _native.pd(out)))
+    return out

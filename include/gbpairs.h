@@ -135,6 +135,21 @@ int gbp_marked_npairs_3d(gbp_plan *plan, const double *xyz1, int64_t n1, const d
                          const double *period3, int32_t pbc, int32_t mem, double *out);
 
 /*
+ * Product-mark counts over nch channels in one pass (no single reference
+ * counterpart): out[c][k] equals marked_npairs_3d(xyz1, xyz2, rbins, 1,
+ * weights1=w1[:, c], weights2=w2[:, c]) (marked_npairs_3d.py:25,
+ * marking_functions.pyx:36-43), e.g. the random-mark draws of marked_tpcf
+ * (marked_tpcf.py:327-345) or the components of a vector mark. w1, w2: (n, nch)
+ * row-major FP64; every pair is binned once and each channel's product is
+ * accumulated in FP32 Kahan pairs. nch <= 32; out is (nch, nbins).
+ */
+int gbp_marked_npairs_3d_channels(gbp_plan *plan, const double *xyz1, int64_t n1,
+                                  const double *xyz2, int64_t n2, const double *w1,
+                                  const double *w2, int32_t nch, const double *rbins,
+                                  int32_t nbins, const double *period3, int32_t pbc, int32_t mem,
+                                  double *out);
+
+/*
  * Reverse pass of occupation-weighted counts, no reference counterpart
  * (halotools has no gradients).  For the forward
  * gbp_marked_npairs_3d(xyz, xyz, w, w, 1 weight, wfunc 1) =

@@ -143,3 +143,39 @@ def test_batched_with_blocks_equals_per_mock(gpu, block):
         want = oracle.npairs_3d(s, s, rb, period=L, num_threads=8) if len(s) else \
             np.zeros(len(rb), np.int64)
         assert np.array_equal(got[m], want), m
+
+
+# ---------------- product marks over several channels in one pass ----------------
+@pytest.mark.parametrize("nch", [1, 2, 3, 8])
+def test_marked_channels_match_oracle(gpu, nch):
+    rng = np.random.default_rng(60 + nch)
+    L = 400.0
+    s = clustered(rng, 30000, L, 1500)
+    w = np.stack([rng.lognormal(0.0, 0.5, len(s)) if c % 2 == 0 else rng.uniform(0, 1, len(s))
+                  for c in range(nch)], axis=1)
+    rb = np.logspace(np.log10(0.5), np.log10(25), 20)
+    got = gpu.marked_npairs_3d_channels(s, s, rb, period=L, weights1=w, weights2=w)
+    assert got.shape == (nch, len(rb))
+    for c in range(nch):
+        want = oracle.marked_npairs_3d(s, s, rb, 1, period=L, weights1=w[:, c],
+                                       weights2=w[:, c], num_threads=8)
+        np.testing.assert_allclose(got[c], want, rtol=1e-6)
+
+
+def test_marked_channels_cross_nonperiodic_and_ones(gpu):
+    rng = np.random.default_rng(70)
+    s1 = rng.uniform(0, 150, (20000, 3))
+    s2 = rng.uniform(10, 140, (15000, 3))
+    w1 = rng.uniform(0.5, 2.0, (len(s1), 4))
+    w2 = rng.uniform(0.5, 2.0, (len(s2), 4))
+    rb = np.logspace(-1, np.log10(12), 12)
+    got = gpu.marked_npairs_3d_channels(s1, s2, rb, weights1=w1, weights2=w2)
+    for c in range(4):
+        want = oracle.marked_npairs_3d(s1, s2, rb, 1, weights1=w1[:, c], weights2=w2[:, c],
+                                       num_threads=8)
+        np.testing.assert_allclose(got[c], want, rtol=1e-6)
+    # unit marks give the integer counts
+    ones = gpu.marked_npairs_3d_channels(s1, s2, rb, weights1=np.ones((len(s1), 2)),
+                                         weights2=np.ones((len(s2), 2)))
+    cnt = gpu.npairs_3d(s1, s2, rb).astype(np.float64)
+    assert np.array_equal(ones[0], cnt) and np.array_equal(ones[1], cnt)
