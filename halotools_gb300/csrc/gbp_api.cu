@@ -867,6 +867,9 @@ int gbp_npairs_s_mu(gbp_plan *plan, const double *xyz1, int64_t n1, const double
     edges_smu(Em.data(), n_mu, Epm.data());
     c.ax[0].set(Eps, &em, 3);
     c.ax[1].set(Epm, nullptr, 0);
+    // dxy / s^2 never exceeds 1 in FP64 (dxy <= fl(dz^2 + dxy)), so a top mu'^2
+    // edge >= 1 is never crossed: no pair needs a recheck against it
+    if (Epm[n_mu - 1] >= 1.0) c.ax[1].hi[n_mu - 1] = c.ax[1].lo[n_mu - 1] = INFINITY;
     // q = dxy/s^2 error bound for pairs with s^2 >= a (FP32 value), factor 2 margin
     double dtop = em.delta(smax * smax);
     double Lm = em.Lmax;

@@ -222,8 +222,9 @@ __device__ __forceinline__ void bin_smu(const PairV &p, HT *hw, int stride, cons
     // nearest edges around q must be farther than qb
     float below = bq > 0 ? Q.hi[bq - 1] : -3.0e38f;
     float above = bq < Q.nb ? Q.lo[bq] : 3.0e38f;
+    // (e1.z = -inf marks a slot where several mu' edges may be crossed)
     bool amb = ((v > e0.z) & !(v > e0.y)) | !(q - below > qb) | !(above - q > qb) |
-               (e1.y > 3.0e38f);
+               (e1.z < -3.0e38f);
     if (amb) {
         slow_smu(v, q, qb, __float_as_int(e0.x), ix.ui[p.iu], ix.jw[p.jj], sym, hw, stride, A, Q,
                  a);
