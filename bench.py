@@ -142,6 +142,20 @@ def run_cpu(w, x, steps, warmup, frac_side, threads):
     return pairs / dt, dt, len(sub)
 
 
+def replica_throughput(units_per_rank, seconds, device=None):
+    """Whole-job throughput of N independent replicas (no data-path collective):
+    every rank processed ``units_per_rank`` units and the job took the slowest
+    rank's time.  Returns (units per second over all ranks, max seconds)."""
+    import torch
+    import torch.distributed as dist
+    world = dist.get_world_size() if dist.is_available() and dist.is_initialized() else 1
+    if world > 1:
+        t = torch.tensor([float(seconds)], dtype=torch.float64, device=device or "cpu")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        seconds = float(t.item())
+    return units_per_rank * world / seconds, seconds
+
+
 def _events():
     import torch
     return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -499,11 +513,7 @@ def main():
         torch.distributed.barrier()
     step_ms = [a.elapsed_time(b) for a, b in ev]
     total_s = sum(step_ms) / 1e3
-    if world > 1:
-        t = torch.tensor([total_s], device=f"cuda:{dev}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_s = float(t.item())
-    value = pairs_step * args.steps * world / total_s
+    value, total_s = replica_throughput(pairs_step * args.steps, total_s, device=f"cuda:{dev}")
     st = plan.stats()
 
     # e2e: public drop-in API from pinned host memory, result back on the host
