@@ -43,6 +43,9 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_adjoint(const CountArgs a) {
     const SmemLayout L = gbp_smem_layout(MODE_ADJ, T0, 0, nb0, 0, a.nsten, 0, 4);
     float4 *s_lut0 = (float4 *)(smem + L.off_lut0);
     float4 *jb = (float4 *)(smem + L.off_j) + warp * 32;
+    // the same j-points with each coordinate twice, for the packed range test
+    ulonglong2 *jxy = (ulonglong2 *)(smem + L.off_j2) + warp * 32;
+    unsigned long long *jzz = (unsigned long long *)(smem + L.off_j2 + GBP_JCAP * 16) + warp * 32;
     float *jw = (float *)(smem + L.off_jw) + warp * 32;
     float4 *s_D = (float4 *)(smem + L.off_D);
     double *s_E0 = (double *)(smem + L.off_E0);
@@ -65,7 +68,10 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_adjoint(const CountArgs a) {
     AxisSm A0{s_lut0, s_hi0, s_lo0, s_E0, nb0, a.ax[0].S, a.ax[0].B, a.ax[0].vlo, a.ax[0].vhi};
     const int nitems = *a.nitems;
     const int n0 = a.n[0], n1 = a.n[1], n2 = a.n[2];
-    const float top0 = a.top0;
+    // range-test threshold with the slack of the count kernels (never drops a pair
+    // that the binning would count)
+    const float R0 = fmaf(a.top0, 0x1p-18f, a.top0) + 1.0e-30f;
+    const unsigned long long RR0 = pk2(R0, R0);
     unsigned long long cand = 0;
     __syncthreads();
 
@@ -82,6 +88,7 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_adjoint(const CountArgs a) {
         float4 u1 = u0;
         if (lane < icnt) u0 = a.pos1[ifirst + lane];
         if (lane + 32 < icnt) u1 = a.pos1[ifirst + 32 + lane];
+        const unsigned long long UX = pk2(u0.x, u1.x), UY = pk2(u0.y, u1.y), UZ = pk2(u0.z, u1.z);
         float acc0 = 0.f, cmp0 = 0.f, acc1 = 0.f, cmp1 = 0.f;  // Kahan: sum ~ acc - cmp
         for (int sb = s0; sb < s1; sb += 32) {
             const int s = sb + lane;
@@ -119,38 +126,54 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_adjoint(const CountArgs a) {
                 if (f < T) {
                     const int j = stk + (f - exk);
                     const float4 p = a.pos2[j];
-                    jb[lane] = make_float4(p.x + Dx, p.y + Dy, p.z + Dz, p.w);
+                    const float tx = p.x + Dx, ty = p.y + Dy, tz = p.z + Dz;
+                    jb[lane] = make_float4(tx, ty, tz, p.w);
+                    jxy[lane] = make_ulonglong2(pk2(tx, tx), pk2(ty, ty));
+                    jzz[lane] = pk2(tz, tz);
                     jw[lane] = a.w2[j];
                 }
                 __syncwarp();
                 const int nj = min(32, T - f0);
-                for (int jj = 0; jj < nj; jj++) {
+                // range test of both i-points against all 32 slots (packed f32x2,
+                // v exactly as below); slot jj lands in bit 31 - jj of the out-mask
+                unsigned o0 = 0u, o1 = 0u;
+#pragma unroll 8
+                for (int jj = 0; jj < 32; jj++) {
+                    const ulonglong2 txy = jxy[jj];
+                    const unsigned long long dX = f2_sub(UX, txy.x), dY = f2_sub(UY, txy.y),
+                                             dZ = f2_sub(UZ, jzz[jj]);
+                    const unsigned long long d =
+                        f2_sub(RR0, f2_fma(dZ, dZ, f2_fma(dY, dY, f2_mul(dX, dX))));
+                    o0 = __funnelshift_l((unsigned)d, o0, 1);
+                    o1 = __funnelshift_l((unsigned)(d >> 32), o1, 1);
+                }
+                const unsigned valid = nj >= 32 ? 0xffffffffu : ((1u << nj) - 1u);
+                unsigned m0 = __brev(~o0) & valid, m1 = __brev(~o1) & valid;
+                // each lane bins only its own in-range pairs: g = G(d_ij), and
+                // accumulates w_j g for the i-point the pair belongs to
+                while (m0 | m1) {
+                    const bool first = m0 != 0u;
+                    const int jj = 31 - __clz(first ? m0 : m1);
+                    if (first) m0 ^= 1u << jj;
+                    else m1 ^= 1u << jj;
+                    const float4 u = first ? u0 : u1;
                     const float4 t = jb[jj];
-                    const float dx0 = u0.x - t.x, dy0 = u0.y - t.y, dz0 = u0.z - t.z;
-                    const float dx1 = u1.x - t.x, dy1 = u1.y - t.y, dz1 = u1.z - t.z;
-                    const float v0 = fmaf(dz0, dz0, fmaf(dy0, dy0, dx0 * dx0));
-                    const float v1 = fmaf(dz1, dz1, fmaf(dy1, dy1, dx1 * dx1));
-                    if (__any_sync(FULL, (v0 <= top0) | (v1 <= top0))) {
-                        const float wj = jw[jj];
-                        float4 e = lut_entry(v0, A0);
-                        int b = __float_as_int(e.x) + (v0 > e.y ? 1 : 0);
-                        float g0 = ((v0 > e.z) & !(v0 > e.y))
-                                       ? slow_adj(v0, __float_as_int(e.x), __float_as_int(u0.w),
-                                                  __float_as_int(t.w), s_gt, A0, a)
-                                       : s_gt[b];
-                        e = lut_entry(v1, A0);
-                        b = __float_as_int(e.x) + (v1 > e.y ? 1 : 0);
-                        float g1 = ((v1 > e.z) & !(v1 > e.y))
-                                       ? slow_adj(v1, __float_as_int(e.x), __float_as_int(u1.w),
-                                                  __float_as_int(t.w), s_gt, A0, a)
-                                       : s_gt[b];
-                        float y = fmaf(wj, g0, -cmp0), s2 = acc0 + y;
-                        cmp0 = (s2 - acc0) - y;
+                    const float dx = u.x - t.x, dy = u.y - t.y, dz = u.z - t.z;
+                    const float v = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+                    const float4 e = lut_entry(v, A0);
+                    const int b = __float_as_int(e.x) + (v > e.y ? 1 : 0);
+                    const float g = ((v > e.z) & !(v > e.y))
+                                        ? slow_adj(v, __float_as_int(e.x), __float_as_int(u.w),
+                                                   __float_as_int(t.w), s_gt, A0, a)
+                                        : s_gt[b];
+                    const float acc = first ? acc0 : acc1, cmp = first ? cmp0 : cmp1;
+                    const float y = fmaf(jw[jj], g, -cmp), s2 = acc + y, c2 = (s2 - acc) - y;
+                    if (first) {
                         acc0 = s2;
-                        y = fmaf(wj, g1, -cmp1);
-                        s2 = acc1 + y;
-                        cmp1 = (s2 - acc1) - y;
+                        cmp0 = c2;
+                    } else {
                         acc1 = s2;
+                        cmp1 = c2;
                     }
                 }
                 __syncwarp();

@@ -114,7 +114,7 @@ __host__ __device__ inline SmemLayout gbp_smem_layout(int mode, int T0, int T1, 
     L.off_hl0 = o; o += adj ? 0 : gbp_align((nb0 + 2) * 8, 16);
     L.off_hl1 = o; o += adj ? 0 : gbp_align((nb1 + 2) * 8, 16);
     L.off_j = o; o += GBP_JCAP * 16;   // adjoint: float4 per j; count: x, y, z, index arrays
-    L.off_j2 = o; o += (mode == MODE_ADJ) ? 0 : GBP_JCAP * 24;   // (x,x,y,y), (z,z) per j
+    L.off_j2 = o; o += GBP_JCAP * 24;   // (x,x,y,y), (z,z) per j
     L.off_jw = o; o += gbp_align(GBP_JCAP * jw, 16);
     L.off_q = o;
     o += adj ? 0 : GBP_WARPS * GBP_USLOTS * 16 +
