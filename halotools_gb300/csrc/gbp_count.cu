@@ -343,8 +343,10 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
     double *s_uw64 = (double *)(smem + L.off_q + GBP_WARPS * GBP_USLOTS * 16) +
                      warp * GBP_USLOTS * (nw > 0 ? nw : 1);
     const Ix ix{uix, jix};
-    // this warp's pair codes of one 32-point j batch: at most 64 x 32
-    unsigned short *s_code = (unsigned short *)(smem + L.off_code) + warp * 2048;
+    // this warp's pair codes of one 32-point j batch: at most 64 x 32 (marked
+    // modes: one i-point at a time, 32 x 32)
+    unsigned short *s_code =
+        (unsigned short *)(smem + L.off_code) + warp * ((MARK || MARKC) ? 1024 : 2048);
 
     lut_compact(a.ax[0].lut, T0, a.ax[0].hi, a.ax[0].lo, nb0, s_l0, s_hl0, s_qb, tid, GBP_BLOCK);
     if (TWO) lut_compact(a.ax[1].lut, T1, a.ax[1].hi, a.ax[1].lo, nb1, s_l1, s_hl1, nullptr, tid,
@@ -632,106 +634,116 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                 // (prefix sum of the bit counts), written as codes, then binned
                 const unsigned own_bits = ns >= 32 ? 0xffffffffu : ((1u << ns) - 1u);
                 const unsigned sym_bits = a.nself ? ~own_bits : 0u;
-                const int c0 = __popc(m0);
-                const int cl = c0 + __popc(m1);
-                int pre = cl;
+                // (marked modes bin the two i-points' codes in two phases: half the
+                // code buffer, which keeps two CTAs per SM beside the Kahan columns)
+                auto stage2 = [&](const unsigned mA, const unsigned mB) {
+                    const int cl = __popc(mA) + __popc(mB);
+                    int pre = cl;
 #pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    const int t = __shfl_up_sync(FULL, pre, o);
-                    if (lane >= o) pre += t;
-                }
-                const int C = __shfl_sync(FULL, pre, 31);
-                pre -= cl;  // exclusive
-                // each lane writes a 16-bit code (i-slot, j-slot) per in-range pair
-                // at its prefix offset; the warp then bins 64 codes per round, two
-                // per lane, every lane busy
-                {
-                    int k = pre;
-                    unsigned m = m0;
-                    while (m) {
-                        const int jj = __ffs(m) - 1;
-                        m &= m - 1u;
-                        s_code[k++] = (unsigned short)(lane | (jj << 7));
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const int t = __shfl_up_sync(FULL, pre, o);
+                        if (lane >= o) pre += t;
                     }
-                    m = m1;
-                    while (m) {
-                        const int jj = __ffs(m) - 1;
-                        m &= m - 1u;
-                        s_code[k++] = (unsigned short)((lane + 48) | (jj << 7));
-                    }
-                }
-                __syncwarp();
-                auto entry = [&](int code) {
-                    const int iu = code & 127, jj = code >> 7;
-                    const float dx = ux[iu] - jx[jj], dy = uy[iu] - jy[jj], dz = uz[iu] - jz[jj];
-                    float v0, v1 = 0.f;
-                    if (MODE == MODE_XYZ) {
-                        v0 = fmaf(dy, dy, dx * dx);
-                        v1 = dz * dz;
-                    } else if (MODE == MODE_SMU) {
-                        v1 = fmaf(dy, dy, dx * dx);
-                        v0 = fmaf(dz, dz, v1);
-                    } else {
-                        v0 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-                    }
-                    if (MARK) {
-                        if (WF == 0) {
-                            v1 = (float)wfunc64(a.wfunc, s_uw64 + iu * nw, jw64 + jj * nw);
-                        } else {
-                            const float wi = s_uw[iu];
-                            v1 = WF == 1 ? wi * jw[jj] : wi + jw[jj];
+                    const int C = __shfl_sync(FULL, pre, 31);
+                    pre -= cl;  // exclusive
+                    // each lane writes a 16-bit code (i-slot, j-slot) per in-range pair
+                    // at its prefix offset; the warp then bins 64 codes per round, two
+                    // per lane, every lane busy
+                    {
+                        int k = pre;
+                        unsigned m = mA;
+                        while (m) {
+                            const int jj = __ffs(m) - 1;
+                            m &= m - 1u;
+                            s_code[k++] = (unsigned short)(lane | (jj << 7));
+                        }
+                        m = mB;
+                        while (m) {
+                            const int jj = __ffs(m) - 1;
+                            m &= m - 1u;
+                            s_code[k++] = (unsigned short)((lane + 48) | (jj << 7));
                         }
                     }
-                    return PairV{v0, v1, iu, jj, ((sym_bits >> jj) & 1u) != 0u};
-                };
-                if (MARKC) {
-                    // each lane bins one pair per round; then lane (g, c) adds channel
-                    // c's product for pairs g, g + G, ... of the round to its own
-                    // Kahan column, so no two lanes touch one column
-                    const int G = 32 / nw, g = lane / nw, ch = lane - g * nw;
-                    for (int r0 = 0; r0 < C; r0 += 32) {
-                        const int sa = r0 + lane;
-                        int b0 = nb0, b1 = nb0, mult = 1, iu = 0, jj = 0;
-                        if (sa < C) {
-                            const PairV e = entry(s_code[sa]);
-                            iu = e.iu;
-                            jj = e.jj;
-                            mult = e.sym ? 2 : 1;
-                            const float4 t = lut_entry_c<false>(e.v0, A0);
-                            b0 = __float_as_int(t.x) + (e.v0 > t.y ? 1 : 0);
-                            if ((e.v0 > t.z) & !(e.v0 > t.y)) {
-                                int k[2];
-                                const int n = slow_3d(e.v0, __float_as_int(t.x), ix.ui[iu], ix.jw[jj],
-                                                      e.sym, k, A0, a);
-                                b0 = k[0];
-                                if (n == 2) {
-                                    b1 = k[1];
-                                    mult = 1;
-                                }
+                    __syncwarp();
+                    auto entry = [&](int code) {
+                        const int iu = code & 127, jj = code >> 7;
+                        const float dx = ux[iu] - jx[jj], dy = uy[iu] - jy[jj], dz = uz[iu] - jz[jj];
+                        float v0, v1 = 0.f;
+                        if (MODE == MODE_XYZ) {
+                            v0 = fmaf(dy, dy, dx * dx);
+                            v1 = dz * dz;
+                        } else if (MODE == MODE_SMU) {
+                            v1 = fmaf(dy, dy, dx * dx);
+                            v0 = fmaf(dz, dz, v1);
+                        } else {
+                            v0 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+                        }
+                        if (MARK) {
+                            if (WF == 0) {
+                                v1 = (float)wfunc64(a.wfunc, s_uw64 + iu * nw, jw64 + jj * nw);
+                            } else {
+                                const float wi = s_uw[iu];
+                                v1 = WF == 1 ? wi * jw[jj] : wi + jw[jj];
                             }
                         }
-                        s_rec[lane] = make_int4(b0 | (mult << 16), b1, iu, jj);
-                        __syncwarp();
-                        const int np = min(32, C - r0);
-                        for (int p = g; p < np; p += G) {
-                            if (g >= G) break;
-                            const int4 r = s_rec[p];
-                            const float val = s_uw[r.z * nw + ch] * jw[r.w * nw + ch];
-                            const int rb0 = r.x & 0xffff;
-                            if (rb0 < nb0) kahan_add(hs, hc, rb0, (r.x >> 16) == 2 ? 2.0f * val : val);
-                            if (r.y < nb0) kahan_add(hs, hc, r.y, val);
+                        return PairV{v0, v1, iu, jj, ((sym_bits >> jj) & 1u) != 0u};
+                    };
+                    if (MARKC) {
+                        // each lane bins one pair per round; then lane (g, c) adds channel
+                        // c's product for pairs g, g + G, ... of the round to its own
+                        // Kahan column, so no two lanes touch one column
+                        const int G = 32 / nw, g = lane / nw, ch = lane - g * nw;
+                        for (int r0 = 0; r0 < C; r0 += 32) {
+                            const int sa = r0 + lane;
+                            int b0 = nb0, b1 = nb0, mult = 1, iu = 0, jj = 0;
+                            if (sa < C) {
+                                const PairV e = entry(s_code[sa]);
+                                iu = e.iu;
+                                jj = e.jj;
+                                mult = e.sym ? 2 : 1;
+                                const float4 t = lut_entry_c<false>(e.v0, A0);
+                                b0 = __float_as_int(t.x) + (e.v0 > t.y ? 1 : 0);
+                                if ((e.v0 > t.z) & !(e.v0 > t.y)) {
+                                    int k[2];
+                                    const int n = slow_3d(e.v0, __float_as_int(t.x), ix.ui[iu], ix.jw[jj],
+                                                          e.sym, k, A0, a);
+                                    b0 = k[0];
+                                    if (n == 2) {
+                                        b1 = k[1];
+                                        mult = 1;
+                                    }
+                                }
+                            }
+                            s_rec[lane] = make_int4(b0 | (mult << 16), b1, iu, jj);
+                            __syncwarp();
+                            const int np = min(32, C - r0);
+                            for (int p = g; p < np; p += G) {
+                                if (g >= G) break;
+                                const int4 r = s_rec[p];
+                                const float val = s_uw[r.z * nw + ch] * jw[r.w * nw + ch];
+                                const int rb0 = r.x & 0xffff;
+                                if (rb0 < nb0) kahan_add(hs, hc, rb0, (r.x >> 16) == 2 ? 2.0f * val : val);
+                                if (r.y < nb0) kahan_add(hs, hc, r.y, val);
+                            }
+                            __syncwarp();
                         }
-                        __syncwarp();
+                    } else {
+                        for (int r0 = 0; r0 < C; r0 += 64) {
+                            const int sa = r0 + lane, sb = sa + 32;
+                            const bool ha = sa < C, hb = sb < C;
+                            const PairV ea = entry(ha ? s_code[sa] : 0);
+                            const PairV eb = entry(hb ? s_code[sb] : 0);
+                            if (ha) bin_entry(ea, cur_mock);
+                            if (hb) bin_entry(eb, cur_mock);
+                        }
                     }
+                    __syncwarp();
+                };
+                if (MARK || MARKC) {
+                    stage2(m0, 0u);
+                    stage2(0u, m1);
                 } else {
-                    for (int r0 = 0; r0 < C; r0 += 64) {
-                        const int sa = r0 + lane, sb = sa + 32;
-                        const bool ha = sa < C, hb = sb < C;
-                        const PairV ea = entry(ha ? s_code[sa] : 0);
-                        const PairV eb = entry(hb ? s_code[sb] : 0);
-                        if (ha) bin_entry(ea, cur_mock);
-                        if (hb) bin_entry(eb, cur_mock);
-                    }
+                    stage2(m0, m1);
                 }
                 drained += 64;
                 __syncwarp();

@@ -119,7 +119,9 @@ __host__ __device__ inline SmemLayout gbp_smem_layout(int mode, int T0, int T1, 
     L.off_q = o;
     o += adj ? 0 : GBP_WARPS * GBP_USLOTS * 16 +
                        gbp_align(GBP_WARPS * GBP_USLOTS * (jw > 4 ? jw : 4), 16);
-    L.off_code = o; o += (mode == MODE_ADJ) ? 0 : GBP_WARPS * 2048 * 2;
+    // codes of one 32-point j batch: 64 x 32 (marked modes: one i-point at a time, 32 x 32)
+    L.off_code = o;
+    o += (mode == MODE_ADJ) ? 0 : GBP_WARPS * ((mode == MODE_MARK || mode == MODE_MARKC) ? 1024 : 2048) * 2;
     L.off_rec = o; o += (mode == MODE_MARKC) ? GBP_WARPS * 32 * 16 : 0;  // binned pairs of a round
     L.off_D = o; o += nsten * 16;
     L.off_E0 = o; o += gbp_align(nb0 * 8, 16);
