@@ -11,10 +11,11 @@ from .pair_counters import (HalotoolsError, marked_npairs_3d, marked_npairs_3d_c
                             npairs_3d, npairs_s_mu, npairs_xy_z)
 from ._native import GBPairsError, GBPairsUnavailable, Plan, default_plan
 from .batched import BatchedCounter, npairs_3d_batched
+from . import estimators
 
 __all__ = ("npairs_3d", "npairs_xy_z", "npairs_s_mu", "marked_npairs_3d",
            "marked_npairs_3d_channels", "HalotoolsError", "GBPairsError", "GBPairsUnavailable", "Plan", "default_plan",
-           "npairs_3d_batched", "BatchedCounter", "install_into_halotools")
+           "npairs_3d_batched", "BatchedCounter", "install_into_halotools", "estimators")
 
 # module attribute -> our function, for every place halotools binds a counter
 _BINDINGS = (

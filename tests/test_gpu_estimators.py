@@ -1,0 +1,24 @@
+"""tpcf / rp_pi_tpcf / wp with every pair count on the GPU, against halotools'
+own estimators over its own counters (golden vectors, make_estimator_golden.py)."""
+import os
+
+import numpy as np
+import pytest
+
+from tests.golden import make_estimator_golden as E
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("name", sorted(E.CASES))
+def test_estimator_matches_reference(gpu, name):
+    d = np.load(os.path.join(E.OUT, "est_" + name + ".npz"))
+    if str(d["sha"]) != E.input_sha():
+        pytest.skip("seeded generator differs on this platform")
+    want = [d["out%d" % k] for k in range(int(d["n"]))]
+    from halotools_gb300 import estimators
+    mods = {"pc": gpu, "tpcf": estimators, "rp_pi_tpcf": estimators, "wp": estimators}
+    got = E.run_case(mods, name)
+    assert len(got) == len(want)
+    for g, w in zip(got, want):
+        np.testing.assert_allclose(np.asarray(g), w, rtol=1e-12, atol=1e-12, equal_nan=True)
