@@ -1,4 +1,5 @@
-"""Two-point estimators on the GB300 pair counters: ``tpcf``, ``rp_pi_tpcf``, ``wp``.
+"""Two-point estimators on the GB300 pair counters: ``tpcf``, ``rp_pi_tpcf``,
+``wp``, ``s_mu_tpcf`` and ``marked_tpcf``.
 
 halotools' estimator layer (two_point_clustering/tpcf.py, rp_pi_tpcf.py, wp.py,
 tpcf_estimators.py) is plain Python around ``npairs_3d`` / ``npairs_xy_z``; the
@@ -12,7 +13,13 @@ package. Signatures, defaults and return shapes follow halotools:
   NR_precomputed=None, seed=None)`` (tpcf.py:212-228);
 * ``rp_pi_tpcf(sample1, rp_bins, pi_bins, sample2=None, randoms=None, ...)``
   (rp_pi_tpcf.py);
-* ``wp(sample1, rp_bins, pi_max, sample2=None, randoms=None, ...)`` (wp.py:20-23).
+* ``wp(sample1, rp_bins, pi_max, sample2=None, randoms=None, ...)`` (wp.py:20-23);
+* ``s_mu_tpcf(sample1, s_bins, mu_bins, sample2=None, randoms=None, ...)``
+  (s_mu_tpcf.py), analytic randoms from spherical sectors (s_mu_tpcf.py:323-334);
+* ``marked_tpcf(sample1, rbins, sample2=None, marks1=None, marks2=None, ...)``
+  (marked_tpcf.py). Its random-mark normalisation draws ``iterations`` mark
+  permutations; with the product weight (id 1) they are counted as channels of
+  one launch (``marked_npairs_3d_channels``), otherwise one call each.
 
 With a periodic box and no randoms, random counts are analytic: ``N_R N dV / V``
 with spherical shells for ``tpcf`` (tpcf.py:120-144) and cylindrical annuli of
@@ -28,9 +35,10 @@ import warnings
 
 import numpy as np
 
-from .pair_counters import HalotoolsError, npairs_3d, npairs_xy_z
+from .pair_counters import (HalotoolsError, marked_npairs_3d, marked_npairs_3d_channels,
+                            npairs_3d, npairs_s_mu, npairs_xy_z)
 
-__all__ = ("tpcf", "rp_pi_tpcf", "wp", "ESTIMATORS")
+__all__ = ("tpcf", "rp_pi_tpcf", "wp", "s_mu_tpcf", "marked_tpcf", "ESTIMATORS")
 
 ESTIMATORS = ("Natural", "Davis-Peebles", "Hewett", "Hamilton", "Landy-Szalay")
 # which of DD, DR, RR each estimator needs (tpcf_estimators.py:126-160)
@@ -276,3 +284,209 @@ def wp(sample1, rp_bins, pi_max, sample2=None, randoms=None, period=None, do_aut
     if isinstance(res, tuple):
         return tuple(2.0 * r[:, 0] * pi_max for r in res)
     return 2.0 * res[:, 0] * pi_max
+
+
+# ---------------- (s, mu) ----------------
+def s_mu_tpcf(sample1, s_bins, mu_bins, sample2=None, randoms=None, period=None, do_auto=True,
+              do_cross=True, estimator="Natural", num_threads=1, approx_cell1_size=None,
+              approx_cell2_size=None, approx_cellran_size=None, seed=None):
+    """xi(s, mu) (halotools s_mu_tpcf.py), every pair count on the GPU. Returns
+    arrays of shape (len(s_bins) - 1, len(mu_bins) - 1) in increasing mu."""
+    sample1 = _shape(sample1)
+    sample2, s1_is_s2, do_cross = _sample2(sample1, sample2, do_cross)
+    s_bins = np.atleast_1d(s_bins).astype(float)
+    mu_bins = np.atleast_1d(mu_bins).astype(float)
+    if np.min(mu_bins) < 0.0 or np.max(mu_bins) > 1.0:
+        raise ValueError("`mu_bins` must be in the range [0,1].")
+    period, pbc = _period(period)
+    _check_common(estimator, do_auto, do_cross, randoms, pbc)
+    do_dd, do_dr, do_rr = _NEEDS[estimator]
+    N1, N2 = len(sample1), len(sample2)
+    NR = len(randoms) if randoms is not None else N1
+    kw = dict(period=period, num_threads=num_threads)
+
+    def diff2(a, b, c1, c2):
+        c = npairs_s_mu(a, b, s_bins, mu_bins, approx_cell1_size=c1, approx_cell2_size=c2, **kw)
+        return np.diff(np.diff(c, axis=0), axis=1)
+
+    D11 = diff2(sample1, sample1, approx_cell1_size, approx_cell1_size) if do_auto else None
+    if s1_is_s2:
+        D12 = D22 = D11
+    else:
+        D12 = diff2(sample1, sample2, approx_cell1_size, approx_cell2_size) if do_cross else None
+        D22 = diff2(sample2, sample2, approx_cell2_size, approx_cell2_size) if do_auto else None
+
+    if randoms is not None:
+        randoms = _shape(randoms, "randoms")
+        RR = diff2(randoms, randoms, approx_cellran_size, approx_cellran_size) if do_rr else None
+        D1R = diff2(sample1, randoms, approx_cell1_size, approx_cellran_size) if do_dr else None
+        D2R = None if s1_is_s2 else (
+            diff2(sample2, randoms, approx_cell2_size, approx_cellran_size) if do_dr else None)
+    else:
+        # wedges of spherical sectors, doubled for the reflection (s_mu_tpcf.py:323-334, 418-440)
+        mu_rev = np.sort(mu_bins)[::-1]
+        v = (2.0 * np.pi / 3.0) * np.outer(s_bins ** 3.0, 1.0 - np.cos(np.arccos(mu_rev))) * 2.0
+        dv = np.diff(np.diff(v, axis=1), axis=0)
+        vol = period.prod()
+        D1R = (N1 - 1.0) * (dv * (N1 / vol))
+        D2R = (N2 - 1.0) * (dv * (N2 / vol))
+        RR = dv * (NR ** 2 / vol)
+
+    # counts run in increasing sin(theta_LOS), i.e. decreasing mu: reverse the last axis
+    def auto(k):
+        x = _xi(D11, D1R, RR, N1, N1, NR, NR, estimator) if k == 1 else \
+            _xi(D22, D2R, RR, N2, N2, NR, NR, estimator)
+        return x[:, ::-1]
+
+    def cross():
+        return _xi_cross(D12, D1R, D2R, RR, N1, N2, NR, NR, estimator)[:, ::-1]
+
+    return _combine(auto, cross, s1_is_s2, do_auto, do_cross)
+
+
+# ---------------- marked ----------------
+class _LegacySeed:
+    """Seed numpy's legacy global generator inside a ``with`` block and restore
+    it afterwards (the permutation draws of marked_tpcf.py:150-165)."""
+
+    def __init__(self, seed):
+        self.seed = seed
+
+    def __enter__(self):
+        self.state = np.random.get_state()
+        np.random.seed(self.seed)
+
+    def __exit__(self, *exc):
+        np.random.set_state(self.state)
+
+
+def _marks(m, n, name):
+    m = np.ones(n) if m is None else np.atleast_1d(m).astype(float)
+    if m.ndim == 1:
+        m = m.reshape((len(m), 1))
+    elif m.ndim != 2:
+        raise HalotoolsError("\n You must either pass in a 1-D or 2-D array \n"
+                             "for the input `%s`." % name)
+    if len(m) != n:
+        raise HalotoolsError("\n `%s` must have same length as `%s`." %
+                             (name, "sample1" if name == "marks1" else "sample2"))
+    return m
+
+
+def marked_tpcf(sample1, rbins, sample2=None, marks1=None, marks2=None, period=None,
+                do_auto=True, do_cross=True, num_threads=1, weight_func_id=1,
+                normalize_by="random_marks", iterations=1, randomize_marks=None, seed=None):
+    """Marked correlation function M(r) = W(r) / R(r) (halotools marked_tpcf.py),
+    every weighted count on the GPU.
+
+    ``normalize_by="random_marks"`` divides by the weighted counts with the marks
+    permuted among the points, ``iterations`` times (the median is kept);
+    ``"number_counts"`` by the plain pair counts. As in halotools, each iteration
+    re-seeds the permutation draws with ``seed`` and permutes the already
+    permuted marks, and both sides of a random auto count use the permuted
+    marks (marked_tpcf.py:150-221).
+    """
+    sample1 = _shape(sample1)
+    sample2, s1_is_s2, do_cross = _sample2(sample1, sample2, do_cross)
+    try:
+        int(weight_func_id) == weight_func_id
+    except Exception:
+        raise ValueError("\n `wfunc` parameter must be an integer ID of the desired function.")
+    if normalize_by not in ("random_marks", "number_counts"):
+        raise ValueError("\n `normalize_by` parameter not recognized.")
+    marks1 = _marks(marks1, len(sample1), "marks1")
+    marks2 = _marks(marks2, len(sample2), "marks2")
+    randomize = np.atleast_1d(randomize_marks) if randomize_marks is not None else \
+        np.array([True] * marks1.shape[1])
+    if randomize.ndim != 1:
+        raise HalotoolsError("\n `randomize_marks` must be one dimensional.")
+    if len(randomize) != marks1.shape[1]:
+        raise HalotoolsError("\n `randomize_marks` must have same length \n"
+                             " as the number of weights per point.")
+    rbins = np.atleast_1d(rbins).astype(float)
+    period, _ = _period(period)
+    if do_auto != bool(do_auto) or do_cross != bool(do_cross):
+        raise ValueError("`do_auto` and `do_cross` keywords must be boolean-valued.")
+    wid = int(weight_func_id)
+    kw = dict(period=period, num_threads=num_threads)
+
+    def w(a, b, m1, m2):
+        return np.diff(marked_npairs_3d(a, b, rbins, wid, weights1=m1, weights2=m2, **kw))
+
+    W11 = w(sample1, sample1, marks1, marks1) if do_auto else None
+    if s1_is_s2:
+        W12 = W22 = W11
+    else:
+        W12 = w(sample1, sample2, marks1, marks2) if do_cross else None
+        W22 = w(sample2, sample2, marks2, marks2) if do_auto else None
+
+    if normalize_by == "number_counts":
+        def c(a, b):
+            return np.diff(npairs_3d(a, b, rbins, **kw))
+        R11 = c(sample1, sample1) if do_auto else None
+        if s1_is_s2:
+            R12 = R22 = R11
+        else:
+            R12 = c(sample1, sample2) if do_cross else None
+            R22 = c(sample2, sample2) if do_auto else None
+    else:
+        # the marks of every iteration, drawn and composed as halotools does
+        p1s, p2s = [], []
+        m1, m2 = marks1.copy(), marks2.copy()
+        for _ in range(int(iterations)):
+            with _LegacySeed(seed):
+                perm1 = np.random.permutation(np.arange(0, len(sample1)))
+                perm2 = np.random.permutation(np.arange(0, len(sample2)))
+            for k in range(m1.shape[1]):
+                if randomize[k]:
+                    m1[:, k] = m1[perm1, k]
+            for k in range(m2.shape[1]):
+                if randomize[k]:
+                    m2[:, k] = m2[perm2, k]
+            p1s.append(m1.copy())
+            p2s.append(m2.copy())
+        R11, R12, R22 = _random_marked(sample1, sample2, rbins, wid, p1s, p2s, s1_is_s2,
+                                       do_auto, do_cross, kw)
+        if int(iterations) > 1:
+            R11 = None if R11 is None else np.median(R11, axis=0)
+            R12 = None if R12 is None else np.median(R12, axis=0)
+            R22 = None if R22 is None else np.median(R22, axis=0)
+        else:
+            R11 = None if R11 is None else R11[0]
+            R12 = None if R12 is None else R12[0]
+            R22 = None if R22 is None else R22[0]
+
+    with np.errstate(divide="ignore", invalid="ignore"):
+        def auto(k):
+            return W11 / R11 if k == 1 else W22 / R22
+
+        def cross():
+            return W12 / R12
+
+        return _combine(auto, cross, s1_is_s2, do_auto, do_cross)
+
+
+def _random_marked(sample1, sample2, rbins, wid, p1s, p2s, s1_is_s2, do_auto, do_cross, kw):
+    """Weighted counts with permuted marks, one row per iteration: product marks
+    (id 1, one weight per point) as channels of one launch (32 per launch),
+    other marking functions one call per iteration."""
+    its = len(p1s)
+
+    def rows(a, b, ma, mb):
+        if wid == 1 and ma[0].shape[1] == 1:
+            out = []
+            for c0 in range(0, its, 32):
+                wa = np.ascontiguousarray(np.concatenate(ma[c0:c0 + 32], axis=1))
+                wb = wa if mb is ma else np.ascontiguousarray(np.concatenate(mb[c0:c0 + 32], axis=1))
+                out.append(np.diff(marked_npairs_3d_channels(a, b, rbins, weights1=wa, weights2=wb,
+                                                             **kw), axis=1))
+            return np.concatenate(out, axis=0)
+        return np.stack([np.diff(marked_npairs_3d(a, b, rbins, wid, weights1=x, weights2=y, **kw))
+                         for x, y in zip(ma, mb)])
+
+    R11 = rows(sample1, sample1, p1s, p1s) if do_auto else None
+    if s1_is_s2:
+        return R11, R11, R11
+    R12 = rows(sample1, sample2, p1s, p2s) if do_cross else None
+    R22 = rows(sample2, sample2, p2s, p2s) if do_auto else None
+    return R11, R12, R22

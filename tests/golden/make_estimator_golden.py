@@ -1,6 +1,6 @@
 """Golden vectors for the estimator layer, made by running halotools' own
-``tpcf``, ``rp_pi_tpcf`` and ``wp`` (two_point_clustering/tpcf.py, rp_pi_tpcf.py,
-wp.py) over its own pair counters (the Cython engines built by
+``tpcf``, ``rp_pi_tpcf``, ``wp``, ``s_mu_tpcf`` and ``marked_tpcf``
+(two_point_clustering/*.py) over its own pair counters (the Cython engines built by
 ``oracle/build_ref.py``, imported through ``oracle/ref_loader.py``).
 
 Inputs are regenerated from their seeds by ``estimator_inputs`` (shared with the
@@ -30,6 +30,8 @@ L = 100.0
 RBINS = np.logspace(-0.5, 1.0, 9)
 RP_BINS = np.logspace(-0.5, 1.0, 8)
 PI_BINS = np.linspace(0.0, 12.0, 7)
+S_BINS = np.logspace(-0.3, 1.0, 7)
+MU_BINS = np.linspace(0.0, 1.0, 6)
 
 # name: (function, sample2?, randoms?, periodic?, estimator, do_auto, do_cross, extra)
 CASES = {
@@ -47,6 +49,19 @@ CASES = {
     "wp_auto_natural_pbc": ("wp", False, False, True, "Natural", True, True, {}),
     "wp_cross_natural_pbc": ("wp", True, False, True, "Natural", True, True, {}),
     "wp_auto_ls_randoms_nopbc": ("wp", False, True, False, "Landy-Szalay", True, True, {}),
+    "s_mu_auto_natural_pbc": ("s_mu_tpcf", False, False, True, "Natural", True, True, {}),
+    "s_mu_cross_ls_randoms_nopbc": ("s_mu_tpcf", True, True, False, "Landy-Szalay", True, True, {}),
+    "marked_auto_random_marks": ("marked_tpcf", False, False, True, None, True, True,
+                                 {"normalize_by": "random_marks", "iterations": 1, "seed": 3}),
+    "marked_auto_random_marks_5it": ("marked_tpcf", False, False, True, None, True, True,
+                                     {"normalize_by": "random_marks", "iterations": 5, "seed": 3}),
+    "marked_cross_random_marks_3it": ("marked_tpcf", True, False, True, None, True, True,
+                                      {"normalize_by": "random_marks", "iterations": 3, "seed": 5}),
+    "marked_cross_number_counts": ("marked_tpcf", True, False, True, None, True, True,
+                                   {"normalize_by": "number_counts"}),
+    "marked_auto_sum_2it": ("marked_tpcf", False, False, True, None, True, True,
+                            {"normalize_by": "random_marks", "iterations": 2, "seed": 9,
+                             "weight_func_id": 2}),
 }
 
 
@@ -58,7 +73,9 @@ def estimator_inputs(seed=7):
     s1 = np.mod(np.concatenate([cen, sat]), L)
     s2 = rng.uniform(0, L, (2000, 3))
     ran = rng.uniform(0, L, (5000, 3))
-    return s1, s2, ran
+    m1 = rng.lognormal(0.0, 0.5, len(s1))
+    m2 = rng.uniform(0.0, 1.0, len(s2))
+    return s1, s2, ran, m1, m2
 
 
 def input_sha():
@@ -70,9 +87,17 @@ def input_sha():
 
 def run_case(mods, name):
     fn, use2, useran, pbc, est, da, dc, extra = CASES[name]
-    s1, s2, ran = estimator_inputs()
+    s1, s2, ran, m1, m2 = estimator_inputs()
+    if fn == "marked_tpcf":
+        out = mods["marked_tpcf"].marked_tpcf(
+            s1, RBINS, sample2=s2 if use2 else None, marks1=m1, marks2=m2 if use2 else None,
+            period=L, do_auto=da, do_cross=dc, **extra)
+        return out if isinstance(out, tuple) else (out,)
     kw = dict(sample2=s2 if use2 else None, randoms=ran if useran else None,
               period=L if pbc else None, do_auto=da, do_cross=dc, estimator=est)
+    if fn == "s_mu_tpcf":
+        out = mods["s_mu_tpcf"].s_mu_tpcf(s1, S_BINS, MU_BINS, **kw)
+        return out if isinstance(out, tuple) else (out,)
     if fn == "tpcf":
         if extra.get("rr"):
             # RR precomputed for 5000 randoms, as tpcf.py's docstring suggests
@@ -99,7 +124,9 @@ def load_reference(src):
     base = "halotools.mock_observables.two_point_clustering."
     return {"pc": pc, "tpcf": importlib.import_module(base + "tpcf"),
             "rp_pi_tpcf": importlib.import_module(base + "rp_pi_tpcf"),
-            "wp": importlib.import_module(base + "wp")}
+            "wp": importlib.import_module(base + "wp"),
+            "s_mu_tpcf": importlib.import_module(base + "s_mu_tpcf"),
+            "marked_tpcf": importlib.import_module(base + "marked_tpcf")}
 
 
 def main():
