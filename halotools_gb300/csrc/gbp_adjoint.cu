@@ -7,10 +7,15 @@
 // which is 2 sum_j w_j G(d_mj) except where the two orders of a pair fall in
 // different bins (guard-band pairs, re-evaluated in FP64 both ways here).
 //
-// k_adjoint: gather-only; each thread owns one point m of a work item and
-// walks the full stencil (no symmetric half: no scatter, no atomics per
-// point), accumulating w_j G(bin) in registers with a compensated (Kahan)
-// FP32 sum; the j-groups of an item are reduced in shared memory at the end.
+// k_gather<false> (adjoint): gather-only over the full stencil (no symmetric
+// half: no scatter), two i-points per lane; a packed range test marks the
+// in-range j-slots, then each lane bins its own pairs and accumulates w_j G(bin)
+// in registers with a compensated (Kahan) FP32 sum, added to dL/dw per item.
+//
+// k_gather<true> (npairs_per_object_3d, npairs_per_object_3d_engine.pyx): the
+// same walk with lane-private per-point bin counters in shared memory, added to
+// the (N1, nbins + 1) table per item; counts[i][k] = #j with d_ij^2 <= rbins[k]^2
+// in the reference's (x_i - shift) - x_j order.
 //
 // k_zheng07_w / k_zheng07_vjp: Zheng07 mean occupations
 // (zheng07_components.py:149-153, 455-470) as per-halo weights and the
@@ -32,15 +37,30 @@ __device__ __noinline__ float slow_adj(float v, int b0, int is, int js, const fl
     return 0.5f * (gt[k1] + gt[k2]);
 }
 
-// Warp-centric like the count kernel: each warp pulls (cell chunk, stencil
-// group) items, two i-points per lane, 32 j-points per step; the partial
-// gradient of an i-point over one item is added to dL/dw (zeroed first).
-__global__ void __launch_bounds__(GBP_BLOCK, 2) k_adjoint(const CountArgs a) {
+// Bin of one ordered pair (i, j) in the reference's order when the FP32 value
+// cannot decide it (per-object counts).
+__device__ __noinline__ int slow_one(float v, int b0, int is, int js, const AxisSm &A,
+                                     const CountArgs &a) {
+    int k = walk_bin(v, b0, A);
+    if (k >= 0) return k;
+    if (is < 0 || js < 0) return A.nb;  // never a real pair
+    atomicAdd(a.nrecheck, 1ull);
+    double p[3], q[3];
+    ref_pos(a, 0, is, p);
+    ref_pos(a, 1, js, q);
+    return exact_bin(exact_pair(p, q, a).s2, b0, A);
+}
+
+// Warp-centric like the count kernel: each warp pulls (block chunk, stencil
+// group) items, two i-points per lane, 32 j-points per step.
+template <bool POBJ>
+__global__ void __launch_bounds__(GBP_BLOCK, 2) k_gather(const CountArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     constexpr unsigned FULL = 0xffffffffu;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nb0 = a.ax[0].nb, T0 = a.ax[0].T;
-    const SmemLayout L = gbp_smem_layout(MODE_ADJ, T0, 0, nb0, 0, a.nsten, 0, 4);
+    const SmemLayout L = gbp_smem_layout(POBJ ? MODE_POBJ : MODE_ADJ, T0, 0, nb0, 0, a.nsten, 0, 4);
+    if (gbp_smem_too_small(L.total, a.err)) return;
     float4 *s_lut0 = (float4 *)(smem + L.off_lut0);
     float4 *jb = (float4 *)(smem + L.off_j) + warp * 32;
     // the same j-points with each coordinate twice, for the packed range test
@@ -53,6 +73,11 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_adjoint(const CountArgs a) {
     float *s_lo0 = (float *)(smem + L.off_lo0);
     int *s_off = (int *)(smem + L.off_off);
     float *s_gt = (float *)(smem + L.off_hist + GBP_BLOCK * 8);
+    // per-object: this warp's lane-private counters [i-point 0/1][bin][lane]
+    const int nbc = nb0 + 1;
+    unsigned *cnt = (unsigned *)(smem + L.off_hist) + warp * 2 * nbc * 32 + lane;
+    if (POBJ)
+        for (int i = 0; i < 2 * nbc; i++) cnt[i * 32] = 0u;
 
     for (int i = tid; i < T0; i += GBP_BLOCK) s_lut0[i] = a.ax[0].lut[i];
     for (int i = tid; i < nb0; i += GBP_BLOCK) {
@@ -60,7 +85,8 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_adjoint(const CountArgs a) {
         s_hi0[i] = a.ax[0].hi[i];
         s_lo0[i] = a.ax[0].lo[i];
     }
-    for (int i = tid; i <= nb0; i += GBP_BLOCK) s_gt[i] = a.gt[i];
+    if (!POBJ)
+        for (int i = tid; i <= nb0; i += GBP_BLOCK) s_gt[i] = a.gt[i];
     for (int i = tid; i < a.nsten; i += GBP_BLOCK) {
         s_off[i] = a.sten[i];
         s_D[i] = a.stenD[i];
@@ -130,7 +156,7 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_adjoint(const CountArgs a) {
                     jb[lane] = make_float4(tx, ty, tz, p.w);
                     jxy[lane] = make_ulonglong2(pk2(tx, tx), pk2(ty, ty));
                     jzz[lane] = pk2(tz, tz);
-                    jw[lane] = a.w2[j];
+                    if (!POBJ) jw[lane] = a.w2[j];
                 }
                 __syncwarp();
                 const int nj = min(32, T - f0);
@@ -161,7 +187,14 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_adjoint(const CountArgs a) {
                     const float dx = u.x - t.x, dy = u.y - t.y, dz = u.z - t.z;
                     const float v = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
                     const float4 e = lut_entry(v, A0);
-                    const int b = __float_as_int(e.x) + (v > e.y ? 1 : 0);
+                    int b = __float_as_int(e.x) + (v > e.y ? 1 : 0);
+                    if (POBJ) {
+                        if ((v > e.z) & !(v > e.y))
+                            b = slow_one(v, __float_as_int(e.x), __float_as_int(u.w),
+                                         __float_as_int(t.w), A0, a);
+                        cnt[((first ? 0 : nbc) + b) * 32] += 1u;
+                        continue;
+                    }
                     const float g = ((v > e.z) & !(v > e.y))
                                         ? slow_adj(v, __float_as_int(e.x), __float_as_int(u.w),
                                                    __float_as_int(t.w), s_gt, A0, a)
@@ -179,30 +212,58 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_adjoint(const CountArgs a) {
                 __syncwarp();
             }
         }
-        if (lane < icnt) atomicAdd(&a.grad[a.orig[ifirst + lane]], 2.0 * ((double)acc0 - (double)cmp0));
-        if (lane + 32 < icnt)
-            atomicAdd(&a.grad[a.orig[ifirst + 32 + lane]], 2.0 * ((double)acc1 - (double)cmp1));
+        if (POBJ) {
+            // this item's counts of the lane's two points, added to their rows
+            for (int h = 0; h < 2; h++) {
+                const int i = lane + 32 * h;
+                const bool real = i < icnt;
+                unsigned *row = real ? a.pobj + (size_t)a.orig[ifirst + i] * nbc : nullptr;
+                for (int k = 0; k < nbc; k++) {
+                    const unsigned c = cnt[(h * nbc + k) * 32];
+                    if (c) {
+                        if (real) atomicAdd(&row[k], c);
+                        cnt[(h * nbc + k) * 32] = 0u;
+                    }
+                }
+            }
+        } else {
+            if (lane < icnt)
+                atomicAdd(&a.grad[a.orig[ifirst + lane]], 2.0 * ((double)acc0 - (double)cmp0));
+            if (lane + 32 < icnt)
+                atomicAdd(&a.grad[a.orig[ifirst + 32 + lane]], 2.0 * ((double)acc1 - (double)cmp1));
+        }
     }
     if (lane == 0 && cand) atomicAdd(a.nrecheck + 1, cand);
 }
 
-cudaError_t gbp_launch_adjoint(const CountArgs &a, int grid, size_t smem, cudaStream_t st) {
-    cudaError_t e = cudaFuncSetAttribute(k_adjoint, cudaFuncAttributeMaxDynamicSharedMemorySize,
+template <bool POBJ>
+static cudaError_t gather_launch(const CountArgs &a, int grid, size_t smem, cudaStream_t st) {
+    cudaError_t e = cudaFuncSetAttribute(k_gather<POBJ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return e;
-    k_adjoint<<<grid, GBP_BLOCK, smem, st>>>(a);
+    k_gather<POBJ><<<grid, GBP_BLOCK, smem, st>>>(a);
     return cudaGetLastError();
 }
 
-int gbp_adjoint_occupancy(size_t smem) {
+template <bool POBJ>
+static int gather_occupancy(size_t smem) {
     int nblk = 0;
-    if (cudaFuncSetAttribute(k_adjoint, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-        cudaSuccess)
+    if (cudaFuncSetAttribute(k_gather<POBJ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem) != cudaSuccess)
         return 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nblk, k_adjoint, GBP_BLOCK, smem) !=
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nblk, k_gather<POBJ>, GBP_BLOCK, smem) !=
         cudaSuccess)
         return 0;
     return nblk;
+}
+
+cudaError_t gbp_launch_adjoint(const CountArgs &a, int grid, size_t smem, cudaStream_t st,
+                               bool per_object) {
+    return per_object ? gather_launch<true>(a, grid, smem, st) : gather_launch<false>(a, grid, smem, st);
+}
+
+int gbp_adjoint_occupancy(size_t smem, bool per_object) {
+    return per_object ? gather_occupancy<true>(smem) : gather_occupancy<false>(smem);
 }
 
 // ---------------- Zheng07 weights ----------------

@@ -145,6 +145,9 @@ struct Call {
     std::vector<int64_t> offsets;    // nmocks+1 point offsets when nmocks > 1
     int xyz_f32 = 0;                 // sample 1 positions are float32
     std::vector<float> gt;           // adjoint: suffix sums of the upstream gradient (nb+1)
+    int ntag = 0;                    // jackknife: tags 0..ntag-1 (N_samples + 1)
+    std::vector<unsigned long long> htag;  // jackknife: (ntag, nb+1) pair ends by tag
+    std::vector<unsigned> pobj;      // per-object: (n1, nb+1) differential counts, caller's order
     double *grad_out = nullptr;      // adjoint: dL/dw, caller's order, in `mem` memory
     const double *xyz1, *xyz2;
     int64_t n1, n2;
@@ -232,8 +235,11 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
     size_t o_itmp = cv.take<int>(2 * ((size_t)nkeys + 2));
     size_t o_offs = cv.take<int64_t>((size_t)nm + 1);
     const bool adj = c.mode == MODE_ADJ;
+    const bool pobj = c.mode == MODE_POBJ;
+    const size_t npobj = pobj ? (size_t)c.n1 * (size_t)(nb0 + 1) : 0;
     size_t o_gt = cv.take<float>((size_t)nb0 + 1);
     size_t o_grad = cv.take<double>(adj && c.mem == GBP_MEM_HOST ? (size_t)c.n1 : 1);
+    size_t o_pobj = cv.take<unsigned>(npobj > 0 ? npobj : 1);
     size_t o_lut0 = cv.take<float4>(T0), o_lut1 = cv.take<float4>(std::max(T1, 1));
     size_t o_E0 = cv.take<double>(nb0), o_E1 = cv.take<double>(std::max(nb1, 1));
     size_t o_hi0 = cv.take<float>(nb0), o_lo0 = cv.take<float>(nb0);
@@ -241,6 +247,8 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
     size_t o_sten = cv.take<int>(nsten), o_stenD = cv.take<float4>(nsten);
     size_t o_hist = cv.take<unsigned long long>(nhist * nm);
     size_t o_histd = cv.take<double>(nhist * nm);
+    const size_t ntab = (size_t)c.ntag * (size_t)(nb0 + 1);
+    size_t o_htag = cv.take<unsigned long long>(ntab > 0 ? ntab : 1);
     size_t o_misc = cv.take<unsigned long long>(8);  // counter, nitems, err, recheck, cand
     size_t total = cv.take<char>(0) + 256;
     int rc = ensure_work(plan, total);
@@ -259,6 +267,7 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
     size_t h_end = hv.take<char>(0);
     size_t h_hist = hv.take<unsigned long long>(nhist * nm);
     size_t h_histd = hv.take<double>(nhist * nm);
+    size_t h_htag = hv.take<unsigned long long>(ntab > 0 ? ntab : 1);
     size_t h_misc = hv.take<unsigned long long>(8);
     rc = ensure_pinned(plan, hv.take<char>(0) + 256);
     if (rc) return rc;
@@ -392,6 +401,7 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
                            at<int>(W, o_scan), st, &launches));
         CK(cudaMemsetAsync(at<char>(W, o_hist), 0, nm * nhist * sizeof(unsigned long long), st));
         CK(cudaMemsetAsync(at<char>(W, o_histd), 0, nm * nhist * sizeof(double), st));
+        if (ntab) CK(cudaMemsetAsync(at<char>(W, o_htag), 0, ntab * sizeof(unsigned long long), st));
         CK(rec(plan->ev[1]));
 
         const SampleDev &s2 = c.autocorr ? sd[0] : sd[1];
@@ -437,6 +447,8 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
         a.ncells_mock = (int)c.g.nblocks;
         a.hist = at<unsigned long long>(W, o_hist);
         a.histd = at<double>(W, o_histd);
+        a.htag = at<unsigned long long>(W, o_htag);
+        a.ntag = c.ntag;
         a.nrecheck = d_stat;
         a.w1 = sd[0].w32;
         a.w2 = s2.w32;
@@ -451,36 +463,54 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
         const int jwb = c.mode == MODE_MARK    ? (c.wf == 0 ? 8 * c.nw : 4)
                         : c.mode == MODE_MARKC ? 4 * c.nw
                         : c.mode == MODE_ADJ   ? 4
+                        : c.mode == MODE_POBJ  ? 4   // the gather kernel's fixed stride
+                        : c.mode == MODE_JACK  ? 4
                                                : 0;
         // 2-D and wide 1-D histograms: one shared copy per warp while they fit,
         // else the warps add straight into the global histogram
         int copies = GBP_WARPS;
-        if (c.mode != MODE_3D && c.mode != MODE_MARK && c.mode != MODE_MARKC && c.mode != MODE_ADJ) {
+        if (c.mode != MODE_3D && c.mode != MODE_MARK && c.mode != MODE_MARKC && c.mode != MODE_ADJ &&
+            c.mode != MODE_JACK && c.mode != MODE_POBJ) {
             size_t one = (size_t)(nb0 + 1) * (size_t)(c.naxes > 1 ? nb1 + 1 : 1) * 4;
             if (one * GBP_WARPS > (96u << 10)) copies = 0;
         }
         a.hist_copies = copies;
-        SmemLayout L = gbp_smem_layout(c.mode, T0, T1, nb0, nb1, nsten, copies, jwb);
+        SmemLayout L = gbp_smem_layout(c.mode, T0, T1, nb0, nb1, nsten, copies, jwb, c.ntag);
         size_t smem = (size_t)L.total;
         if (smem > (size_t)(227u << 10))
             return fail(plan, GBP_ERR_INVALID, "too many bins for one shared-memory histogram (%zu B)", smem);
         a.gt = at<float>(W, o_gt);
         a.orig = sd[0].orig;
         a.grad = adj ? (c.mem == GBP_MEM_HOST ? at<double>(W, o_grad) : c.grad_out) : nullptr;
-        int occ = adj ? gbp_adjoint_occupancy(smem) : gbp_count_occupancy(c.mode, c.wf, smem);
+        a.pobj = at<unsigned>(W, o_pobj);
+        a.err = d_err;
+        int occ = (adj || pobj) ? gbp_adjoint_occupancy(smem, pobj)
+                                : gbp_count_occupancy(c.mode, c.wf, smem);
         if (occ <= 0) return fail(plan, GBP_ERR_INVALID, "count kernel does not fit (smem %zu B)", smem);
         int grid = plan->nsm * occ;
         if (adj) CK(cudaMemsetAsync(a.grad, 0, sizeof(double) * (size_t)c.n1, st));
-        if (adj) CK(gbp_launch_adjoint(a, grid, smem, st));
+        if (pobj) CK(cudaMemsetAsync(a.pobj, 0, sizeof(unsigned) * npobj, st));
+        if (adj || pobj) CK(gbp_launch_adjoint(a, grid, smem, st, pobj));
         else CK(gbp_launch_count(c.mode, c.wf, a, grid, smem, st));
         if (adj && c.mem == GBP_MEM_HOST && c.n1 > 0) {
             CK(cudaMemcpyAsync(c.grad_out, a.grad, sizeof(double) * c.n1, cudaMemcpyDeviceToHost, st));
             d2h += (int64_t)(sizeof(double) * c.n1);
         }
+        if (pobj && npobj) {
+            // (the caller sized c.pobj; a pageable copy, the call syncs at the end anyway)
+            CK(cudaMemcpyAsync(c.pobj.data(), a.pobj, sizeof(unsigned) * npobj,
+                               cudaMemcpyDeviceToHost, st));
+            d2h += (int64_t)(sizeof(unsigned) * npobj);
+        }
         launches += 1;
         CK(rec(plan->ev[2]));
         CK(cudaMemcpyAsync(at<char>(H, h_hist), a.hist, nm * nhist * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
         CK(cudaMemcpyAsync(at<char>(H, h_histd), a.histd, nm * nhist * sizeof(double), cudaMemcpyDeviceToHost, st));
+        if (ntab) {
+            CK(cudaMemcpyAsync(at<char>(H, h_htag), a.htag, ntab * sizeof(unsigned long long),
+                               cudaMemcpyDeviceToHost, st));
+            d2h += (int64_t)(ntab * sizeof(unsigned long long));
+        }
         CK(cudaMemcpyAsync(at<char>(H, h_misc), misc, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
         CK(rec(plan->ev[3]));
         d2h += (int64_t)(nm * nhist * (sizeof(unsigned long long) + sizeof(double)) + 8 * sizeof(unsigned long long));
@@ -521,6 +551,8 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
 
     const unsigned long long *hm = at<unsigned long long>(H, h_misc);
     int err_word = reinterpret_cast<const int *>(hm)[2];
+    if (err_word & GBP_ERR_SMEM_LAYOUT)
+        return fail(plan, GBP_ERR_CUDA, "internal: kernel shared-memory layout exceeds its launch");
     if (err_word) return fail(plan, GBP_ERR_RANGE, "positions outside [0, period] or not finite");
     if (reinterpret_cast<const int *>(hm)[3]) {
         // more work items than the estimate: grow and repeat the call
@@ -532,6 +564,7 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
     hist_host.assign(at<unsigned long long>(H, h_hist), at<unsigned long long>(H, h_hist) + nm * nhist);
     if (c.mode != MODE_MARK && c.mode != MODE_MARKC) add_self_pairs(c, hist_host);
     if (histd_host) histd_host->assign(at<double>(H, h_histd), at<double>(H, h_histd) + nm * nhist);
+    if (ntab) c.htag.assign(at<unsigned long long>(H, h_htag), at<unsigned long long>(H, h_htag) + ntab);
     gbp_stats &S = plan->stats;
     S.recheck_pairs = (int64_t)hm[2];
     S.candidate_pairs = (int64_t)hm[3];
@@ -1000,6 +1033,128 @@ int gbp_marked_npairs_3d_channels(gbp_plan *plan, const double *xyz1, int64_t n1
         for (int k = 0; k < nb; k++) {
             run += hd[(size_t)ch * (nb + 1) + k];
             out[(size_t)ch * nb + k] = run;
+        }
+    }
+    return GBP_OK;
+}
+
+int gbp_npairs_jackknife_3d(gbp_plan *plan, const double *xyz1, int64_t n1, const double *xyz2,
+                            int64_t n2, const int32_t *jtags1, const int32_t *jtags2,
+                            int32_t n_samples, const double *rbins, int32_t nb,
+                            const double *period3, int32_t pbc, int32_t mem, double *out) {
+    int rc = check_common(plan, xyz1, n1, xyz2, n2, period3, pbc, mem);
+    if (rc) return rc;
+    if (mem != GBP_MEM_HOST)
+        return fail(plan, GBP_ERR_INVALID, "jackknife counts take host positions and tags");
+    if (n_samples < 1 || (n1 > 0 && !jtags1) || (n2 > 0 && !jtags2))
+        return fail(plan, GBP_ERR_INVALID, "N_samples must be >= 1 with one tag per point");
+    if (!rbins || nb < 2 || nb > GBP_NB_LANE || !out)
+        return fail(plan, GBP_ERR_INVALID, "rbins must have 2..%d entries", GBP_NB_LANE);
+    if ((int64_t)(n_samples + 1) * (nb + 1) * 8 > (48 << 10))
+        return fail(plan, GBP_ERR_INVALID, "too many jackknife samples x bins for one table");
+    double rmax = max_nan(rbins, nb);
+    double search[3] = {rmax, rmax, rmax};
+    if ((rc = check_search(plan, search, period3))) return rc;
+    // tags go through the weight path as exact FP64 / FP32 integers
+    const bool autocorr = (xyz1 == xyz2 && n1 == n2 && jtags1 == jtags2);
+    std::vector<double> t1((size_t)n1), t2;
+    for (int64_t i = 0; i < n1; i++) {
+        if (jtags1[i] < 1 || jtags1[i] > n_samples)
+            return fail(plan, GBP_ERR_INVALID, "jtags1 must be in [1, N_samples]");
+        t1[(size_t)i] = (double)jtags1[i];
+    }
+    if (!autocorr) {
+        t2.resize((size_t)n2);
+        for (int64_t i = 0; i < n2; i++) {
+            if (jtags2[i] < 1 || jtags2[i] > n_samples)
+                return fail(plan, GBP_ERR_INVALID, "jtags2 must be in [1, N_samples]");
+            t2[(size_t)i] = (double)jtags2[i];
+        }
+    }
+    Call c;
+    c.mode = MODE_JACK;
+    c.xyz1 = xyz1;
+    c.xyz2 = xyz2;
+    c.n1 = n1;
+    c.n2 = n2;
+    c.autocorr = autocorr;
+    c.mem = mem;
+    c.w1 = t1.data();
+    c.w2 = autocorr ? t1.data() : t2.data();
+    c.nw = 1;
+    c.wf = 1;
+    c.ntag = n_samples + 1;
+    c.naxes = 1;
+    choose_grid(c.g, period3, search, pbc, n2, plan->reach, MAX_CELLS_PER_DIM, 0.0, plan->block);
+    build_stencil(c.g, search, 0, c.autocorr);
+    ErrModel em = err_model(c.g);
+    std::vector<double> E(nb);
+    edges_top_walk(rbins, nb, E.data());
+    c.ax[0].set(E, &em, 3);
+    c.ax[0].make_lut(no_qband);
+    const int rows = n_samples + 1;
+    for (int k = 0; k < rows * nb; k++) out[k] = 0.0;
+    if (n1 == 0 || n2 == 0) return GBP_OK;
+    std::vector<unsigned long long> h;
+    if ((rc = run_call(plan, c, h))) return rc;
+    std::vector<unsigned long long> &tab = c.htag;
+    if (autocorr) {
+        // (i, i): distance 0, both ends carry tag_i (the kernels skip it)
+        const int sb = host_bin(nb, c.ax[0].E.data(), 0.0);
+        if (sb < nb)
+            for (int64_t i = 0; i < n1; i++) tab[(size_t)jtags1[i] * (nb + 1) + sb] += 2;
+    }
+    double cT = 0.0;
+    std::vector<double> cQ((size_t)rows, 0.0);
+    for (int k = 0; k < nb; k++) {
+        cT += (double)h[k];
+        out[k] = cT;
+        for (int s = 1; s < rows; s++) {
+            cQ[(size_t)s] += (double)tab[(size_t)s * (nb + 1) + k];
+            out[(size_t)s * nb + k] = cT - 0.5 * cQ[(size_t)s];
+        }
+    }
+    return GBP_OK;
+}
+
+int gbp_npairs_per_object_3d(gbp_plan *plan, const double *xyz1, int64_t n1, const double *xyz2,
+                             int64_t n2, const double *rbins, int32_t nb, const double *period3,
+                             int32_t pbc, int32_t mem, int64_t *counts) {
+    int rc = check_common(plan, xyz1, n1, xyz2, n2, period3, pbc, mem);
+    if (rc) return rc;
+    if (!rbins || nb < 2 || nb > GBP_NB_LANE || (n1 > 0 && !counts))
+        return fail(plan, GBP_ERR_INVALID, "rbins must have 2..%d entries", GBP_NB_LANE);
+    double rmax = max_nan(rbins, nb);
+    double search[3] = {rmax, rmax, rmax};
+    if ((rc = check_search(plan, search, period3))) return rc;
+    for (int64_t k = 0; k < n1 * nb; k++) counts[k] = 0;
+    if (n1 == 0 || n2 == 0) return GBP_OK;
+    Call c;
+    c.mode = MODE_POBJ;
+    c.xyz1 = xyz1;
+    c.xyz2 = xyz2;
+    c.n1 = n1;
+    c.n2 = n2;
+    c.autocorr = (xyz1 == xyz2 && n1 == n2);  // one sorted copy; the walk is a gather
+    c.mem = mem;
+    c.naxes = 1;
+    choose_grid(c.g, period3, search, pbc, n2, plan->reach, MAX_CELLS_PER_DIM, 0.0, plan->block);
+    build_stencil(c.g, search, 0, false);  // full stencil: each row gathers its own pairs
+    ErrModel em = err_model(c.g);
+    std::vector<double> E(nb);
+    edges_top_walk(rbins, nb, E.data());
+    c.ax[0].set(E, &em, 3);
+    c.ax[0].make_lut(no_qband);
+    c.pobj.assign((size_t)n1 * (size_t)(nb + 1), 0u);
+    std::vector<unsigned long long> h;
+    if ((rc = run_call(plan, c, h))) return rc;
+    // cumulative per row (npairs_per_object_3d_engine.pyx: walk from the top edge)
+    for (int64_t i = 0; i < n1; i++) {
+        const unsigned *r = c.pobj.data() + (size_t)i * (nb + 1);
+        int64_t run = 0;
+        for (int k = 0; k < nb; k++) {
+            run += r[k];
+            counts[(size_t)i * nb + k] = run;
         }
     }
     return GBP_OK;

@@ -98,6 +98,37 @@ __device__ __forceinline__ void bin_3d(const PairV &p, HT *h, const AxisSm &A, c
     else if (b < A.nb) atomicAdd(&h[b], (HT)w);
 }
 
+// ---------------- stage 2: jackknife (counts + pair ends by tag) ----------------
+// Each ordered pair in bin k adds 1 to the counts and 1 to (tag_i, k) and to
+// (tag_j, k) of the CTA's table; with N_k(s) = sum of those ends, the count
+// without subsample s is C_k - N_k(s) / 2 (npairs_jackknife_3d_engine.pyx:238-289).
+__device__ __forceinline__ void bin_jack(const PairV &p, int ti, int tj, unsigned *h,
+                                         unsigned long long *tab, const AxisSm &A, const Ix &ix,
+                                         const CountArgs &a) {
+    const float v = p.v0;
+    const int ts = A.nb + 1;
+    float4 t = lut_entry_c<false>(v, A);
+    int b = __float_as_int(t.x) + (v > t.y ? 1 : 0);
+    if ((v > t.z) & !(v > t.y)) {
+        int k[2];
+        const int n = slow_3d(v, __float_as_int(t.x), ix.ui[p.iu], ix.jw[p.jj], p.sym, k, A, a);
+        if (n == 0) {
+            b = k[0];
+        } else {
+            for (int q = 0; q < n; q++) {
+                h[k[q] * 32] += 1u;
+                atomicAdd(&tab[ti * ts + k[q]], 1ull);
+                atomicAdd(&tab[tj * ts + k[q]], 1ull);
+            }
+            return;
+        }
+    }
+    const unsigned w = p.sym ? 2u : 1u;
+    h[b * 32] += w;
+    atomicAdd(&tab[ti * ts + b], (unsigned long long)w);
+    atomicAdd(&tab[tj * ts + b], (unsigned long long)w);
+}
+
 // ---------------- stage 2: marked (Kahan in lane-private FP32 pairs) ----------------
 __device__ __forceinline__ void kahan_add(float *hs, float *hc, int b, float x) {
     float s = hs[b * 32], c = hc[b * 32];
@@ -306,9 +337,11 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
     const int nb0 = a.ax[0].nb, nb1 = TWO ? a.ax[1].nb : 0;
     const int T0 = a.ax[0].T, T1 = TWO ? a.ax[1].T : 0;
     const int copies = a.hist_copies;  // 2-D / wide: GBP_WARPS (one per warp) or 0 (global)
-    const int nw = (MARK || MARKC) ? a.nw : 0;
-    const int jwb = MARK ? (WF == 0 ? 8 * nw : 4) : MARKC ? 4 * nw : 0;
-    const SmemLayout L = gbp_smem_layout(MODE, T0, T1, nb0, nb1, a.nsten, copies, jwb);
+    constexpr bool JACK = (MODE == MODE_JACK);    // w1 / w2 hold the subsample tags
+    const int nw = (MARK || MARKC || JACK) ? a.nw : 0;
+    const int jwb = MARK ? (WF == 0 ? 8 * nw : 4) : MARKC ? 4 * nw : JACK ? 4 : 0;
+    const SmemLayout L = gbp_smem_layout(MODE, T0, T1, nb0, nb1, a.nsten, copies, jwb, a.ntag);
+    if (gbp_smem_too_small(L.total, a.err)) return;
     unsigned *s_l0 = (unsigned *)(smem + L.off_lut0);
     unsigned *s_l1 = (unsigned *)(smem + L.off_lut1);
     float *s_qb = MODE == MODE_SMU ? (float *)(smem + L.off_qb) : nullptr;
@@ -367,10 +400,15 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
     }
     const int nbin = (nb0 + 1) * (TWO ? nb1 + 1 : 1);
     // this warp's histogram words: lane-private (3-D, marked) or its own copy
-    const int warp_words = (MODE == MODE_3D) ? (nb0 + 1) * 32
+    const int warp_words = (MODE == MODE_3D || JACK) ? (nb0 + 1) * 32
                            : (MARK || MARKC) ? (nb0 + 1) * 32 * 2 : (copies ? nbin : 0);
     unsigned *wh = s_hist + warp * warp_words;
     for (int i = lane; i < warp_words; i += 32) wh[i] = 0u;
+    // jackknife: the CTA's (tag, bin) table of pair ends, after the warps' counts
+    unsigned long long *s_tab =
+        (unsigned long long *)(smem + L.off_hist + gbp_align(GBP_WARPS * (nb0 + 1) * 32 * 4, 16));
+    if (JACK)
+        for (int i = tid; i < a.ntag * (nb0 + 1); i += GBP_BLOCK) s_tab[i] = 0ull;
     AxisSm A0{nullptr, s_hi0, s_lo0, s_E0, nb0, a.ax[0].S, a.ax[0].B, a.ax[0].vlo, a.ax[0].vhi,
               s_l0, s_hl0, s_qb};
     AxisSm A1{nullptr, s_hi1, s_lo1, s_E1, nb1, TWO ? a.ax[1].S : 0, TWO ? a.ax[1].B : 0,
@@ -395,6 +433,7 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
     auto bin_entry = [&](const PairV &e, int mk) {
         unsigned long long *gh = a.hist + (size_t)mk * a.hist_stride;
         if (MODE == MODE_3D) bin_3d<true>(e, hl, A0, ix, a);
+        else if (JACK) bin_jack(e, (int)s_uw[e.iu], (int)jw[e.jj], hl, s_tab, A0, ix, a);
         else if (MODE == MODE_3DS) {
             if (copies) bin_3d<false>(e, wh, A0, ix, a); else bin_3d<false>(e, gh, A0, ix, a);
         } else if (MODE == MODE_XYZ) {
@@ -409,7 +448,7 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
     auto warp_flush = [&](int mk) {
         __syncwarp();
         unsigned long long *gh = a.hist + (size_t)mk * a.hist_stride;
-        if (MODE == MODE_3D) {
+        if (MODE == MODE_3D || JACK) {
             for (int b = 0; b <= nb0; b++) {
                 unsigned long long v = hl[b * 32];
                 hl[b * 32] = 0u;
@@ -477,6 +516,10 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
         ux[lane + 48] = u1.x; uy[lane + 48] = u1.y; uz[lane + 48] = u1.z; uix[lane + 48] = is1;
         float w0 = 0.f, w1 = 0.f;
         double wa[5] = {0, 0, 0, 0, 0}, wb[5] = {0, 0, 0, 0, 0};
+        if (JACK) {
+            s_uw[lane] = lane < icnt ? a.w1[ifirst + lane] : 0.f;
+            s_uw[lane + 48] = lane + 32 < icnt ? a.w1[ifirst + 32 + lane] : 0.f;
+        }
         if (MARK) {
             if (WF == 0) {
                 for (int k = 0; k < nw; k++) {
@@ -559,6 +602,7 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                     }
                     if (MARKC)
                         for (int q = 0; q < nw; q++) jw[lane * nw + q] = a.w2[(int64_t)j * nw + q];
+                    if (JACK) jw[lane] = a.w2[j];
                 } else {
                     // padding slot: at -FAR, so it is 2*FAR from an idle i-lane (+FAR)
                     // and farther still from every real point; its bits are also masked
@@ -755,6 +799,12 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
     }
     if (cur_mock >= 0) warp_flush(cur_mock);
     if (lane == 0 && cand) atomicAdd(a.nrecheck + 1, cand);
+    if (JACK) {
+        // every warp has left the item loop: add the CTA's table to the global one
+        __syncthreads();
+        for (int i = tid; i < a.ntag * (nb0 + 1); i += GBP_BLOCK)
+            if (s_tab[i]) atomicAdd(&a.htag[i], s_tab[i]);
+    }
 }
 
 template <int MODE, int WF>
@@ -787,6 +837,8 @@ cudaError_t gbp_launch_count(int mode, int wf, const CountArgs &a, int grid, siz
     case MODE_SMU: return launch_t<MODE_SMU, 1>(a, grid, smem, st);
     case MODE_MARKC:
         return launch_t<MODE_MARKC, 1>(a, grid, smem, st);
+    case MODE_JACK:
+        return launch_t<MODE_JACK, 1>(a, grid, smem, st);
     case MODE_MARK:
         if (wf == 1) return launch_t<MODE_MARK, 1>(a, grid, smem, st);
         if (wf == 2) return launch_t<MODE_MARK, 2>(a, grid, smem, st);
@@ -803,6 +855,8 @@ int gbp_count_occupancy(int mode, int wf, size_t smem) {
     case MODE_SMU: return occ_t<MODE_SMU, 1>(smem);
     case MODE_MARKC:
         return occ_t<MODE_MARKC, 1>(smem);
+    case MODE_JACK:
+        return occ_t<MODE_JACK, 1>(smem);
     case MODE_MARK:
         if (wf == 1) return occ_t<MODE_MARK, 1>(smem);
         if (wf == 2) return occ_t<MODE_MARK, 2>(smem);

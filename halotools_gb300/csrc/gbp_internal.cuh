@@ -25,7 +25,9 @@
 #define GBP_FAR 1.0e18f     // coordinate of an idle lane: far outside every edge
 
 enum { MODE_3D = 0, MODE_XYZ = 1, MODE_SMU = 2, MODE_MARK = 3, MODE_ADJ = 4, MODE_3DS = 5,
-       MODE_MARKC = 6 };  // MARKC: product marks (id 1) over several channels in one pass
+       MODE_MARKC = 6,    // product marks (id 1) over several channels in one pass
+       MODE_JACK = 7,     // jackknife: counts plus a (tag, bin) table of pair ends
+       MODE_POBJ = 8 };   // per-object counts (gather walk of the adjoint)
 
 // One binning axis: squared quantity v compared with edges E'[0..nb-1]
 // (non-decreasing); bin(v) = smallest k with v <= E'[k], nb if none.
@@ -69,6 +71,10 @@ struct CountArgs {
     int ncells_mock;        // blocks per mock: work-item key = mock * ncells_mock + block
     int hist_copies;        // shared histogram copies (2-D and wide 1-D): 8 = one per warp, or 1
     unsigned long long *hist;   // global differential histogram(s)
+    unsigned long long *htag;   // jackknife: (ntag, nb0 + 1) counts of pair ends by tag
+    unsigned *pobj;             // per-object: (N1, nb0 + 1) counts, caller's order
+    int *err;                   // error word: bit 1 = shared-memory layout larger than the launch
+    int ntag;                   // jackknife: number of tags (N_samples + 1)
     unsigned long long *nrecheck;
     float top0, top1;       // above these a pair is out of range on that axis
     // marked / adjoint
@@ -102,12 +108,13 @@ __host__ __device__ inline int gbp_uslot(int iu) { return iu + ((iu >> 5) << 4);
 __host__ __device__ inline int gbp_align(int x, int a) { return (x + a - 1) / a * a; }
 
 __host__ __device__ inline SmemLayout gbp_smem_layout(int mode, int T0, int T1, int nb0, int nb1,
-                                                      int nsten, int copies, int jw) {
+                                                      int nsten, int copies, int jw,
+                                                      int ntag = 0) {
     SmemLayout L;
     int o = 0;
     // adjoint: float4 tables {b0, thr, lo, qband}; count kernels: u32 table
     // {b0 | threshold-pair index << 16} and the threshold pairs (hi, lo)
-    const bool adj = mode == MODE_ADJ;
+    const bool adj = mode == MODE_ADJ || mode == MODE_POBJ;  // the gather kernel
     L.off_lut0 = o; o += adj ? T0 * 16 : gbp_align(T0 * 4, 16);
     L.off_lut1 = o; o += adj ? T1 * 16 : gbp_align(T1 * 4, 16);
     L.off_qb = o; o += (mode == MODE_SMU) ? gbp_align(T0 * 4, 16) : 0;
@@ -121,7 +128,7 @@ __host__ __device__ inline SmemLayout gbp_smem_layout(int mode, int T0, int T1, 
                        gbp_align(GBP_WARPS * GBP_USLOTS * (jw > 4 ? jw : 4), 16);
     // codes of one 32-point j batch: 64 x 32 (marked modes: one i-point at a time, 32 x 32)
     L.off_code = o;
-    o += (mode == MODE_ADJ) ? 0 : GBP_WARPS * ((mode == MODE_MARK || mode == MODE_MARKC) ? 1024 : 2048) * 2;
+    o += adj ? 0 : GBP_WARPS * ((mode == MODE_MARK || mode == MODE_MARKC) ? 1024 : 2048) * 2;
     L.off_rec = o; o += (mode == MODE_MARKC) ? GBP_WARPS * 32 * 16 : 0;  // binned pairs of a round
     L.off_D = o; o += nsten * 16;
     L.off_E0 = o; o += gbp_align(nb0 * 8, 16);
@@ -135,10 +142,15 @@ __host__ __device__ inline SmemLayout gbp_smem_layout(int mode, int T0, int T1, 
     int hist_bytes;
     if (mode == MODE_3D) {
         hist_bytes = GBP_WARPS * (nb0 + 1) * 32 * 4;          // lane-private u32
+    } else if (mode == MODE_JACK) {
+        // lane-private u32 counts, then the CTA's u64 (tag, bin) table
+        hist_bytes = gbp_align(GBP_WARPS * (nb0 + 1) * 32 * 4, 16) + ntag * (nb0 + 1) * 8;
     } else if (mode == MODE_MARK || mode == MODE_MARKC) {
         hist_bytes = GBP_WARPS * (nb0 + 1) * 32 * 4 * 2;      // lane-private FP32 sum + compensation
     } else if (mode == MODE_ADJ) {
         hist_bytes = GBP_BLOCK * 8 + gbp_align((nb0 + 1) * 4, 16);  // partial sums + gt table
+    } else if (mode == MODE_POBJ) {
+        hist_bytes = GBP_WARPS * 2 * (nb0 + 1) * 32 * 4;      // lane-private counters, 2 points
     } else if (mode == MODE_3DS) {
         hist_bytes = copies * (nb0 + 1) * 4;                  // shared u32 copies (wide 1-D)
     } else {
@@ -147,6 +159,19 @@ __host__ __device__ inline SmemLayout gbp_smem_layout(int mode, int T0, int T1, 
     o += gbp_align(hist_bytes, 16);
     L.total = o;
     return L;
+}
+
+#define GBP_ERR_SMEM_LAYOUT 2
+
+// True (and the error bit set) when the kernel's own shared-memory layout does
+// not fit the dynamic shared memory it was launched with; the kernel then
+// returns before touching shared memory.
+__device__ __forceinline__ bool gbp_smem_too_small(int total, int *err) {
+    unsigned dyn;
+    asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dyn));
+    if ((unsigned)total <= dyn) return false;
+    if (threadIdx.x == 0 && err) atomicOr(err, GBP_ERR_SMEM_LAYOUT);
+    return true;
 }
 
 // Fine-cell key of stencil run `pk` seen from block (cx, cy, cz) of the mock
@@ -214,8 +239,10 @@ cudaError_t gbp_launch_count(int mode, int wf, const CountArgs &a, int grid, siz
                              cudaStream_t st);
 int gbp_count_occupancy(int mode, int wf, size_t smem);
 cudaError_t gbp_count_set_smem(size_t smem);
-cudaError_t gbp_launch_adjoint(const CountArgs &a, int grid, size_t smem, cudaStream_t st);
-int gbp_adjoint_occupancy(size_t smem);
+// the gather kernel: adjoint (dL/dw), or per-object counts when per_object
+cudaError_t gbp_launch_adjoint(const CountArgs &a, int grid, size_t smem, cudaStream_t st,
+                               bool per_object = false);
+int gbp_adjoint_occupancy(size_t smem, bool per_object = false);
 struct Zheng07 {
     double logMmin, sigma, logM0, logM1, alpha;
 };

@@ -196,6 +196,7 @@ extern "C" int gbp_npairs_3d_static(const double *xyz, int64_t n, const double *
     std::memset(&a, 0, sizeof(a));
     a.pos1 = a.pos2 = pos32;
     a.xyz1 = a.xyz2 = xyz;
+    a.err = misc_i + 2;
     a.orig1 = a.orig2 = reinterpret_cast<const int *>(W + O_ORIG);
     a.start2 = start;
     a.items = reinterpret_cast<const int4 *>(W + O_ITEMS);

@@ -21,13 +21,16 @@ bin edges must be non-negative with a positive maximum.
 from __future__ import annotations
 
 import multiprocessing
+import warnings
 
 import numpy as np
 
 from . import _native
 from ._native import GBP_MEM_HOST
 
-__all__ = ("npairs_3d", "npairs_xy_z", "npairs_s_mu", "marked_npairs_3d", "HalotoolsError")
+__all__ = ("npairs_3d", "npairs_xy_z", "npairs_s_mu", "marked_npairs_3d", "npairs_projected",
+           "npairs_jackknife_3d", "npairs_per_object_3d", "marked_npairs_3d_channels",
+           "HalotoolsError")
 
 
 class HalotoolsError(Exception):
@@ -196,6 +199,38 @@ def npairs_xy_z(sample1, sample2, rp_bins, pi_bins, period=None, num_threads=1,
     return out
 
 
+def npairs_projected(sample1, sample2, rp_bins, pi_max, period=None, num_threads=1,
+                     approx_cell1_size=None, approx_cell2_size=None):
+    """Cumulative projected pair counts, length ``len(rp_bins)``: pairs with
+    ``r_p <= rp_bins[k]`` and ``|pi| <= pi_max``.
+
+    Same inputs and output as halotools ``npairs_projected``
+    (npairs_projected.py:20-21). It is the ``pi_max`` column of the (r_p, pi)
+    count with pi edges ``[0, pi_max]``: the projected engine tests the same
+    squared quantities, ``dx*dx + dy*dy <= rp^2`` and ``dz*dz <= pi_max^2``
+    (npairs_projected_engine.pyx), with the same cumulative walk over rp.
+    """
+    _check_num_threads(num_threads)
+    rp_bins = _bins(rp_bins, "Input ``rp_bins`` must be a monotonically increasing 1D array "
+                             "with at least two entries")
+    rpm = np.max(rp_bins)
+    _approx_cells(approx_cell1_size, [rpm, rpm, rpm], "approx_cell1_size")
+    _approx_cells(approx_cell2_size, [rpm, rpm, rpm], "approx_cell2_size")
+    msg = "Input ``pi_max`` must be a positive scalar less than period[2]/3"
+    if period is None:
+        pi_max_f = float(pi_max)
+        x1, _, box = _enclose_in_box(_columns(sample1), _columns(sample2),
+                                     [rpm * 3.0, rpm * 3.0, pi_max_f * 3.0])
+    else:
+        box = _period(period)
+    if not (pi_max > 0.0 and pi_max < box[2] / 3.0):
+        raise ValueError(msg)
+    _nonneg(rp_bins, "rp_bins")
+    counts = npairs_xy_z(sample1, sample2, rp_bins, np.array([0.0, float(pi_max)]), period=period,
+                         num_threads=num_threads)
+    return np.ascontiguousarray(counts[:, -1])
+
+
 def npairs_s_mu(sample1, sample2, s_bins, mu_bins, period=None, num_threads=1,
                 approx_cell1_size=None, approx_cell2_size=None):
     """Cumulative (s, mu) pair counts, shape ``(len(s_bins), len(mu_bins))``.
@@ -358,4 +393,86 @@ def marked_npairs_3d_channels(sample1, sample2, rbins, period=None, weights1=Non
         plan.handle, _native.dptr(x1), len(x1), _native.dptr(x2), len(x2), _native.dptr(w1),
         _native.dptr(w2), nch, _native.pd(rbins), len(rbins), _native.pd(box), pbc,
         GBP_MEM_HOST, _native.pd(out)))
+    return out
+
+
+def npairs_jackknife_3d(sample1, sample2, rbins, jtags1, jtags2, N_samples, period=None,
+                        weights1=None, weights2=None, num_threads=1, approx_cell1_size=None,
+                        approx_cell2_size=None):
+    """Jackknife pair counts, shape ``(N_samples + 1, len(rbins))``, float64.
+
+    Same inputs and output as halotools ``npairs_jackknife_3d``
+    (npairs_jackknife_3d.py:29-31): row 0 is the cumulative count of all pairs,
+    row s the count with subsample s removed, where a pair with one end in s
+    counts one half (npairs_jackknife_3d_engine.pyx:238-289). Exact for unit
+    weights (the ``tpcf_jackknife`` case); other weights are not supported on
+    the GPU and raise ``NotImplementedError``.
+    """
+    _check_num_threads(num_threads)
+    rbins = _bins(rbins, "Input ``rbins`` must be a monotonically increasing 1D array with at "
+                         "least two entries")
+    rmax = np.max(rbins)
+    _approx_cells(approx_cell1_size, [rmax] * 3, "approx_cell1_size")
+    _approx_cells(approx_cell2_size, [rmax] * 3, "approx_cell2_size")
+    s1 = _columns(sample1)
+    s2 = s1 if sample2 is sample1 else _columns(sample2)
+    for w, s, name in ((weights1, s1, "weights1"), (weights2, s2, "weights2")):
+        if w is not None:
+            w = np.asarray(w).astype("float64")
+            if np.shape(w)[0] != np.shape(s)[0]:
+                raise HalotoolsError("%s should have same len as %s" % (name, name.replace(
+                    "weights", "sample")))
+            if np.any(w != 1.0):
+                raise NotImplementedError("weighted jackknife counts are not supported on the "
+                                          "GPU; pass unit weights")
+    t1 = np.asarray(jtags1).astype("int")
+    t2 = np.asarray(jtags2).astype("int")
+    if np.shape(t1)[0] != np.shape(s1)[0]:
+        raise HalotoolsError("jtags1 should have same len as sample1")
+    if np.shape(t2)[0] != np.shape(s2)[0]:
+        raise HalotoolsError("jtags2 should have same len as sample2")
+    if len(t1) and np.min(t1) < 1:
+        raise HalotoolsError("jtags1 must be >= 1")
+    if len(t2) and np.min(t2) < 1:
+        raise HalotoolsError("jtags2 must be >= 1")
+    if len(t1) and np.max(t1) > N_samples:
+        raise HalotoolsError("jtags1 must be <= N_samples")
+    if len(t2) and np.max(t2) > N_samples:
+        raise HalotoolsError("jtags2 must be <= N_samples")
+    if not np.array_equal(np.unique(t1), np.arange(1, N_samples + 1)):
+        warnings.warn("Warning: sample1 does not contain points in every jackknife sample.")
+    _nonneg(rbins, "rbins")
+    x1, x2, box, pbc = _positions(s1, s2, period, [rmax] * 3, [rmax * 3.0] * 3)
+    j1 = np.ascontiguousarray(t1, dtype=np.int32)
+    j2 = j1 if (x2 is x1 and np.array_equal(t1, t2)) else np.ascontiguousarray(t2, dtype=np.int32)
+    if x2 is x1 and j2 is not j1:
+        x2 = x1.copy()  # same points, different tags: count as a cross-correlation
+    plan = _native.default_plan()
+    out = np.zeros((int(N_samples) + 1, len(rbins)), dtype=np.float64)
+    plan.check(plan.lib.gbp_npairs_jackknife_3d(
+        plan.handle, _native.dptr(x1), len(x1), _native.dptr(x2), len(x2), _native.dptr(j1),
+        _native.dptr(j2), int(N_samples), _native.pd(rbins), len(rbins), _native.pd(box), pbc,
+        GBP_MEM_HOST, _native.pd(out)))
+    return out
+
+
+def npairs_per_object_3d(sample1, sample2, rbins, period=None, num_threads=1,
+                         approx_cell1_size=None, approx_cell2_size=None):
+    """Counts of ``sample2`` points around each point of ``sample1``, shape
+    ``(Npts1, len(rbins))`` int64, as halotools ``npairs_per_object_3d``
+    (npairs_per_object_3d.py:20-21): entry [i, k] counts j with separation
+    <= rbins[k] (self pairs included when the samples coincide)."""
+    _check_num_threads(num_threads)
+    rbins = _bins(rbins, "Input ``rbins`` must be a monotonically increasing 1D array with at "
+                         "least two entries")
+    rmax = np.max(rbins)
+    _approx_cells(approx_cell1_size, [rmax] * 3, "approx_cell1_size")
+    _approx_cells(approx_cell2_size, [rmax] * 3, "approx_cell2_size")
+    x1, x2, box, pbc = _positions(sample1, sample2, period, [rmax] * 3, [rmax * 3.0] * 3)
+    _nonneg(rbins, "rbins")
+    plan = _native.default_plan()
+    out = np.zeros((len(x1), len(rbins)), dtype=np.int64)
+    plan.check(plan.lib.gbp_npairs_per_object_3d(
+        plan.handle, _native.dptr(x1), len(x1), _native.dptr(x2), len(x2), _native.pd(rbins),
+        len(rbins), _native.pd(box), pbc, GBP_MEM_HOST, _native.pi64(out)))
     return out

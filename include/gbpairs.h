@@ -150,6 +150,28 @@ int gbp_marked_npairs_3d_channels(gbp_plan *plan, const double *xyz1, int64_t n1
                                   double *out);
 
 /*
+ * Jackknife pair counts, as npairs_jackknife_3d (npairs_jackknife_3d.py:29-31,
+ * engine npairs_jackknife_3d_engine.pyx) without weights: out[0][k] is the
+ * cumulative count, out[s][k] (s = 1..n_samples) the count with subsample s
+ * removed, a pair with one end in s counting one half. jtags in [1, n_samples];
+ * positions and tags in host memory; out is (n_samples + 1, nbins) FP64.
+ */
+int gbp_npairs_jackknife_3d(gbp_plan *plan, const double *xyz1, int64_t n1, const double *xyz2,
+                            int64_t n2, const int32_t *jtags1, const int32_t *jtags2,
+                            int32_t n_samples, const double *rbins, int32_t nbins,
+                            const double *period3, int32_t pbc, int32_t mem, double *out);
+
+/*
+ * Per-object counts, as npairs_per_object_3d (npairs_per_object_3d.py:20-21,
+ * engine npairs_per_object_3d_engine.pyx): counts[i][k] = number of points j of
+ * sample 2 with (FP64, reference order) d_ij^2 <= rbins[k]^2, self pairs
+ * included; counts is (n1, nbins) int64 in sample 1's order, host memory.
+ */
+int gbp_npairs_per_object_3d(gbp_plan *plan, const double *xyz1, int64_t n1, const double *xyz2,
+                             int64_t n2, const double *rbins, int32_t nbins,
+                             const double *period3, int32_t pbc, int32_t mem, int64_t *counts);
+
+/*
  * Reverse pass of occupation-weighted counts, no reference counterpart
  * (halotools has no gradients).  For the forward
  * gbp_marked_npairs_3d(xyz, xyz, w, w, 1 weight, wfunc 1) =

@@ -76,7 +76,14 @@ def load(src_root: str = DEFAULT_SRC):
     mcp = _pkg("halotools.mock_observables.pair_counters.marked_cpairs",
                [os.path.join(ht, pc, "marked_cpairs"), os.path.join(bt, pc, "marked_cpairs")])
     base = "halotools.mock_observables.pair_counters"
-    for name in ("npairs_3d_engine", "npairs_xy_z_engine", "npairs_s_mu_engine"):
+    # the per-object engine imports halotools.utils.unsorting_indices, which
+    # halotools/utils/__init__.py would bind from array_utils.py
+    utils_mod = sys.modules["halotools.utils"]
+    utils_mod.unsorting_indices = importlib.import_module(
+        "halotools.utils.array_utils").unsorting_indices
+    for name in ("npairs_3d_engine", "npairs_xy_z_engine", "npairs_s_mu_engine",
+                 "npairs_projected_engine", "npairs_jackknife_3d_engine",
+                 "npairs_per_object_3d_engine"):
         m = importlib.import_module(base + ".cpairs." + name)
         setattr(cp, name, getattr(m, name))
     m = importlib.import_module(base + ".marked_cpairs.marked_npairs_3d_engine")
@@ -91,6 +98,11 @@ def _namespace():
     ns.npairs_xy_z = importlib.import_module(base + ".npairs_xy_z").npairs_xy_z
     ns.npairs_s_mu = importlib.import_module(base + ".npairs_s_mu").npairs_s_mu
     ns.marked_npairs_3d = importlib.import_module(base + ".marked_npairs_3d").marked_npairs_3d
+    ns.npairs_projected = importlib.import_module(base + ".npairs_projected").npairs_projected
+    ns.npairs_jackknife_3d = importlib.import_module(
+        base + ".npairs_jackknife_3d").npairs_jackknife_3d
+    ns.npairs_per_object_3d = importlib.import_module(
+        base + ".npairs_per_object_3d").npairs_per_object_3d
     ns.pairs = importlib.import_module(base + ".pairs")
     ns.HalotoolsError = importlib.import_module("halotools.custom_exceptions").HalotoolsError
     return ns
