@@ -16,6 +16,9 @@ package. Signatures, defaults and return shapes follow halotools:
 * ``wp(sample1, rp_bins, pi_max, sample2=None, randoms=None, ...)`` (wp.py:20-23);
 * ``s_mu_tpcf(sample1, s_bins, mu_bins, sample2=None, randoms=None, ...)``
   (s_mu_tpcf.py), analytic randoms from spherical sectors (s_mu_tpcf.py:323-334);
+* ``tpcf_jackknife(sample1, randoms, rbins, Nsub=[5, 5, 5], ...)``
+  (tpcf_jackknife.py:33-45): xi and its jackknife covariance over cuboid
+  subvolumes, from the GPU jackknife counter (DD, DR, RR);
 * ``marked_tpcf(sample1, rbins, sample2=None, marks1=None, marks2=None, ...)``
   (marked_tpcf.py). Its random-mark normalisation draws ``iterations`` mark
   permutations; with the product weight (id 1) they are counted as channels of
@@ -36,9 +39,10 @@ import warnings
 import numpy as np
 
 from .pair_counters import (HalotoolsError, marked_npairs_3d, marked_npairs_3d_channels,
-                            npairs_3d, npairs_s_mu, npairs_xy_z)
+                            npairs_3d, npairs_jackknife_3d, npairs_s_mu, npairs_xy_z)
 
-__all__ = ("tpcf", "rp_pi_tpcf", "wp", "s_mu_tpcf", "marked_tpcf", "ESTIMATORS")
+__all__ = ("tpcf", "rp_pi_tpcf", "wp", "s_mu_tpcf", "marked_tpcf", "tpcf_jackknife",
+           "ESTIMATORS")
 
 ESTIMATORS = ("Natural", "Davis-Peebles", "Hewett", "Hamilton", "Landy-Szalay")
 # which of DD, DR, RR each estimator needs (tpcf_estimators.py:126-160)
@@ -100,21 +104,27 @@ def _zero_check(DR, RR, estimator):
         raise ValueError(_ZERO_MSG.format("DR", estimator))
 
 
+def _mult(x, y):
+    """A per-sample factor times each row (jackknife subsamples), or plain product."""
+    return (x * y.T).T if np.ndim(x) > 0 else x * y
+
+
 def _xi(DD, DR, RR, ND1, ND2, NR1, NR2, estimator):
-    """Auto-type estimator from differential counts (tpcf_estimators.py:14-58)."""
+    """Auto-type estimator from differential counts (tpcf_estimators.py:14-58);
+    the N's may be per-subsample arrays (rows of DD, DR, RR)."""
     _zero_check(DR, RR, estimator)
     with np.errstate(divide="ignore", invalid="ignore"):
         if estimator == "Natural":
-            return (1.0 / (ND1 * ND2 / (NR1 * NR2))) * (DD / RR) - 1.0
+            return _mult(1.0 / (ND1 * ND2 / (NR1 * NR2)), DD / RR) - 1.0
         if estimator == "Davis-Peebles":
-            return (1.0 / (ND1 * ND2 / (ND1 * NR2))) * (DD / DR) - 1.0
+            return _mult(1.0 / (ND1 * ND2 / (ND1 * NR2)), DD / DR) - 1.0
         if estimator == "Hewett":
             f1, f2 = ND1 * ND2 / (NR1 * NR2), ND1 * NR2 / (NR1 * NR2)
-            return (1.0 / f1) * (DD / RR) - (1.0 / f2) * (DR / RR)
+            return _mult(1.0 / f1, DD / RR) - _mult(1.0 / f2, DR / RR)
         if estimator == "Hamilton":
             return (DD * RR) / (DR * DR) - 1.0
         f1, f2 = ND1 * ND2 / (NR1 * NR2), ND1 * NR2 / (NR1 * NR2)
-        return (1.0 / f1) * (DD / RR) - (1.0 / f2) * (2.0 * DR / RR) + 1.0
+        return _mult(1.0 / f1, DD / RR) - _mult(1.0 / f2, 2.0 * DR / RR) + 1.0
 
 
 def _xi_cross(DD, D1R, D2R, RR, ND1, ND2, NR1, NR2, estimator):
@@ -123,12 +133,13 @@ def _xi_cross(DD, D1R, D2R, RR, ND1, ND2, NR1, NR2, estimator):
     _zero_check(D2R, RR, estimator)
     with np.errstate(divide="ignore", invalid="ignore"):
         if estimator == "Natural":
-            return (1.0 / (ND1 * ND2 / (NR1 * NR2))) * (DD / RR) - 1.0
+            return _mult(1.0 / (ND1 * ND2 / (NR1 * NR2)), DD / RR) - 1.0
         if estimator == "Hamilton":
             return (DD * RR) / (D1R * D2R) - 1.0
         if estimator == "Landy-Szalay":
             f1, f2 = ND1 * ND2 / (NR1 * NR2), ND1 * NR2 / (NR1 * NR2)
-            return (1.0 / f1) * (DD / RR) - (1.0 / f2) * (D1R / RR) - (1.0 / f2) * (D2R / RR) + 1.0
+            return (_mult(1.0 / f1, DD / RR) - _mult(1.0 / f2, D1R / RR) -
+                    _mult(1.0 / f2, D2R / RR) + 1.0)
     raise ValueError("{0} estimator is not supported for cross-correlations".format(estimator))
 
 
@@ -490,3 +501,111 @@ def _random_marked(sample1, sample2, rbins, wid, p1s, p2s, s1_is_s2, do_auto, do
     R12 = rows(sample1, sample2, p1s, p2s) if do_cross else None
     R22 = rows(sample2, sample2, p2s, p2s) if do_auto else None
     return R11, R12, R22
+
+
+# ---------------- jackknife ----------------
+def _cuboid_labels(sample, Nsub, Lbox):
+    """Labels 1..prod(Nsub) of the cuboid subvolumes holding the points, points
+    on the upper face in the last subvolume (catalog_analysis_helpers.py:330-384)."""
+    Nsub = np.atleast_1d(Nsub).astype("i4")
+    if len(Nsub) == 1:
+        Nsub = np.array([Nsub[0]] * 3)
+    elif len(Nsub) != 3:
+        raise TypeError("Input ``Nsub`` must be a scalar or length-3 sequence")
+    Lbox = np.atleast_1d(Lbox).astype("f8")
+    if len(Lbox) == 1:
+        Lbox = np.array([Lbox[0]] * 3)
+    dL = Lbox / Nsub
+    n_sub = int(np.prod(Nsub))
+    ids = np.arange(1, n_sub + 1).reshape(Nsub[0], Nsub[1], Nsub[2])
+    idx = np.floor(sample / dL).astype(int)
+    for d in range(3):
+        idx[:, d] = np.where(idx[:, d] == Nsub[d], Nsub[d] - 1, idx[:, d])
+    return ids[idx[:, 0], idx[:, 1], idx[:, 2]].astype(int), n_sub
+
+
+def _enclose3(a, b, c):
+    """Shift three samples by their smallest coordinate; cube of the largest extent
+    (tpcf_jackknife.py:403-440)."""
+    lo = np.min([np.min(x[:, d]) for x in (a, b, c) for d in range(3)])
+    hi = np.max([np.max(x[:, d]) for x in (a, b, c) for d in range(3)]) - lo
+    return a - lo, b - lo, c - lo, np.array([hi, hi, hi])
+
+
+def tpcf_jackknife(sample1, randoms, rbins, Nsub=[5, 5, 5], sample2=None, period=None,
+                   do_auto=True, do_cross=True, estimator="Natural", num_threads=1, seed=None):
+    """xi(r) and its jackknife covariance (halotools tpcf_jackknife.py:33): the
+    box is cut into ``Nsub`` cuboids, each pair counted once per subsample with
+    the GPU jackknife counter, and the covariance is (N - 1) times the biased
+    covariance of the leave-one-out estimates. ``randoms`` may be a 1-element
+    array giving the number of uniform randoms to draw (periodic boxes)."""
+    sample1 = _shape(sample1)
+    sample2, s1_is_s2, do_cross = _sample2(sample1, sample2, do_cross)
+    period, pbc = _period(period)
+    if np.shape(randoms) == (1,):
+        n_ran = randoms[0]
+        if not pbc:
+            raise HalotoolsError("\n When no `period` parameter is passed, \n"
+                                 "the user must provide true randoms, and \n"
+                                 "not just the number of randoms desired.")
+        with _LegacySeed(seed):
+            randoms = np.random.random((n_ran, 3)) * period
+    randoms = _shape(randoms, "randoms")
+    rbins = np.atleast_1d(rbins).astype(float)
+    _check_common(estimator, do_auto, do_cross, randoms, pbc)
+    if pbc:
+        lbox = period
+    else:
+        sample1, sample2, randoms, lbox = _enclose3(sample1, sample2, randoms)
+        if s1_is_s2:
+            sample2 = sample1
+    do_dd, do_dr, do_rr = _NEEDS[estimator]
+    N1, N2, NR = len(sample1), len(sample2), len(randoms)
+    j1, nsv = _cuboid_labels(sample1, Nsub, lbox)
+    j2, _ = _cuboid_labels(sample2, Nsub, lbox)
+    jr, _ = _cuboid_labels(randoms, Nsub, lbox)
+
+    def per_sub(j):  # points in each subvolume (tpcf_jackknife.py:443-457)
+        return np.bincount(j, minlength=nsv + 1)[1:]
+    N1s, N2s, NRs = N1 - per_sub(j1), N2 - per_sub(j2), NR - per_sub(jr)
+    kw = dict(period=period, num_threads=num_threads)
+
+    def jk(a, b, ta, tb):
+        return np.diff(npairs_jackknife_3d(a, b, rbins, ta, tb, nsv, **kw), axis=1)
+
+    D11 = jk(sample1, sample1, j1, j1) if do_auto else None
+    if s1_is_s2:
+        D12 = D22 = D11
+    else:
+        D12 = jk(sample1, sample2, j1, j2) if do_cross else None
+        D22 = jk(sample2, sample2, j2, j2) if do_auto else None
+    D1R = jk(sample1, randoms, j1, jr) if do_dr else None
+    RR = jk(randoms, randoms, jr, jr) if do_rr else None
+    D2R = D1R if s1_is_s2 else (jk(sample2, randoms, j2, jr) if do_dr else None)
+
+    def full(x):
+        return None if x is None else x[0, :]
+
+    def sub(x):
+        return None if x is None else x[1:, :]
+
+    out_full, out_cov = {}, {}
+    if do_auto:
+        out_full[11] = _xi(full(D11), full(D1R), full(RR), N1, N1, NR, NR, estimator)
+        out_full[22] = _xi(full(D22), full(D2R), full(RR), N2, N2, NR, NR, estimator)
+        x11 = _xi(sub(D11), sub(D1R), sub(RR), N1s, N1s, NRs, NRs, estimator)
+        x22 = _xi(sub(D22), sub(D2R), sub(RR), N2s, N2s, NRs, NRs, estimator)
+        out_cov[11] = np.array(np.cov(x11.T, bias=True)) * (nsv - 1.0)
+        out_cov[22] = np.array(np.cov(x22.T, bias=True)) * (nsv - 1.0)
+    if do_cross:
+        out_full[12] = _xi_cross(full(D12), full(D1R), full(D2R), full(RR), N1, N2, NR, NR,
+                                 estimator)
+        x12 = _xi_cross(sub(D12), sub(D1R), sub(D2R), sub(RR), N1s, N2s, NRs, NRs, estimator)
+        out_cov[12] = np.array(np.cov(x12.T, bias=True)) * (nsv - 1.0)
+    if s1_is_s2:
+        return out_full[11], out_cov[11]
+    if do_auto and do_cross:
+        return (out_full[11], out_full[12], out_full[22], out_cov[11], out_cov[12], out_cov[22])
+    if do_auto:
+        return out_full[11], out_full[22], out_cov[11], out_cov[22]
+    return out_full[12], out_cov[12]

@@ -17,6 +17,7 @@ import hashlib
 import importlib
 import os
 import sys
+import types
 import warnings
 
 import numpy as np
@@ -62,6 +63,12 @@ CASES = {
     "marked_auto_sum_2it": ("marked_tpcf", False, False, True, None, True, True,
                             {"normalize_by": "random_marks", "iterations": 2, "seed": 9,
                              "weight_func_id": 2}),
+    "jackknife_auto_natural_pbc": ("tpcf_jackknife", False, True, True, "Natural", True, True,
+                                   {"Nsub": [3, 3, 3]}),
+    "jackknife_cross_ls_pbc": ("tpcf_jackknife", True, True, True, "Landy-Szalay", True, True,
+                               {"Nsub": [2, 3, 2]}),
+    "jackknife_auto_ls_nopbc": ("tpcf_jackknife", False, True, False, "Landy-Szalay", True, True,
+                                {"Nsub": 3}),
 }
 
 
@@ -95,6 +102,11 @@ def run_case(mods, name):
         return out if isinstance(out, tuple) else (out,)
     kw = dict(sample2=s2 if use2 else None, randoms=ran if useran else None,
               period=L if pbc else None, do_auto=da, do_cross=dc, estimator=est)
+    if fn == "tpcf_jackknife":
+        out = mods["tpcf_jackknife"].tpcf_jackknife(
+            s1, ran, RBINS, sample2=s2 if use2 else None, period=L if pbc else None,
+            do_auto=da, do_cross=dc, estimator=est, **extra)
+        return out if isinstance(out, tuple) else (out,)
     if fn == "s_mu_tpcf":
         out = mods["s_mu_tpcf"].s_mu_tpcf(s1, S_BINS, MU_BINS, **kw)
         return out if isinstance(out, tuple) else (out,)
@@ -117,8 +129,19 @@ def load_reference(src):
     ht = os.path.join(src, "halotools")
     pc = sys.modules["halotools.mock_observables.pair_counters"]
     # the package's __init__ would bind the front-end functions (pair_counters/__init__.py:3-18)
-    for n in ("npairs_3d", "npairs_xy_z", "npairs_s_mu", "marked_npairs_3d"):
+    for n in ("npairs_3d", "npairs_xy_z", "npairs_s_mu", "marked_npairs_3d", "npairs_projected",
+              "npairs_jackknife_3d", "npairs_per_object_3d"):
         setattr(pc, n, getattr(ns, n))
+    # catalog_analysis_helpers (jackknife subvolume labels) imports two names from
+    # modules that need astropy.table; the functions used here touch neither
+    em = types.ModuleType("halotools.empirical_models")
+    em.enforce_periodicity_of_box = None
+    sm = types.ModuleType("halotools.sim_manager")
+    sm.__path__ = []
+    sd = types.ModuleType("halotools.sim_manager.sim_defaults")
+    sd.default_cosmology, sd.default_redshift = None, 0.0
+    sys.modules.update({"halotools.empirical_models": em, "halotools.sim_manager": sm,
+                        "halotools.sim_manager.sim_defaults": sd})
     ref_loader._pkg("halotools.mock_observables.two_point_clustering",
                     [os.path.join(ht, "mock_observables", "two_point_clustering")])
     base = "halotools.mock_observables.two_point_clustering."
@@ -126,7 +149,8 @@ def load_reference(src):
             "rp_pi_tpcf": importlib.import_module(base + "rp_pi_tpcf"),
             "wp": importlib.import_module(base + "wp"),
             "s_mu_tpcf": importlib.import_module(base + "s_mu_tpcf"),
-            "marked_tpcf": importlib.import_module(base + "marked_tpcf")}
+            "marked_tpcf": importlib.import_module(base + "marked_tpcf"),
+            "tpcf_jackknife": importlib.import_module(base + "tpcf_jackknife")}
 
 
 def main():

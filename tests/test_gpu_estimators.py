@@ -1,4 +1,5 @@
-"""tpcf / rp_pi_tpcf / wp / s_mu_tpcf / marked_tpcf with every pair count on the GPU, against halotools'
+"""tpcf / rp_pi_tpcf / wp / s_mu_tpcf / marked_tpcf / tpcf_jackknife with every pair
+count on the GPU, against halotools'
 own estimators over its own counters (golden vectors, make_estimator_golden.py)."""
 import os
 
@@ -18,7 +19,7 @@ def test_estimator_matches_reference(gpu, name):
     want = [d["out%d" % k] for k in range(int(d["n"]))]
     from halotools_gb300 import estimators
     mods = {"pc": gpu, "tpcf": estimators, "rp_pi_tpcf": estimators, "wp": estimators,
-            "s_mu_tpcf": estimators, "marked_tpcf": estimators}
+            "s_mu_tpcf": estimators, "marked_tpcf": estimators, "tpcf_jackknife": estimators}
     got = E.run_case(mods, name)
     assert len(got) == len(want)
     # integer counts are exact, so unweighted estimators agree to rounding; marked
