@@ -270,11 +270,10 @@ int gbp_adjoint_occupancy(size_t smem, bool per_object) {
 __device__ __forceinline__ void zheng07_terms(double M, const Zheng07 &t, double *ncen,
                                               double *nsat, double *x, double *r) {
     const double logM = log10(M);
-    *x = (logM - t.logMmin) / t.sigma;
+    *x = (logM - t.logMmin) * t.inv_sigma;
     *ncen = 0.5 * (1.0 + erf(*x));
-    const double M0 = exp10(t.logM0), M1 = exp10(t.logM1);
-    *r = (M - M0) / M1;
-    *nsat = M > M0 ? pow(*r, t.alpha) : 0.0;
+    *r = (M - t.M0) * t.inv_M1;
+    *nsat = M > t.M0 ? pow(*r, t.alpha) : 0.0;
 }
 
 __global__ void k_zheng07_w(const double *__restrict__ mass, int64_t n, Zheng07 th,
@@ -297,12 +296,11 @@ __global__ void k_zheng07_vjp(const double *__restrict__ mass, int64_t n, Zheng0
         zheng07_terms(M, th, &nc, &ns, &x, &r);
         // d/dx of (1 + erf x)/2 is exp(-x^2)/sqrt(pi)
         const double dphi = exp(-x * x) * 0.56418958354775628695;
-        d[0] = g * (-dphi / th.sigma);       // logMmin
-        d[1] = g * (-dphi * x / th.sigma);   // sigma_logM
+        d[0] = g * (-dphi * th.inv_sigma);       // logMmin
+        d[1] = g * (-dphi * x * th.inv_sigma);   // sigma_logM
         const double ln10 = 2.30258509299404568402;
         if (ns > 0.0) {
-            const double M0 = exp10(th.logM0), M1 = exp10(th.logM1);
-            d[2] = g * (th.alpha * ns / r) * (-M0 * ln10 / M1);  // logM0
+            d[2] = g * (th.alpha * ns / r) * (-th.M0 * ln10 * th.inv_M1);  // logM0
             d[3] = g * (-th.alpha * ln10 * ns);                  // logM1
             d[4] = g * (ns * log(r));                            // alpha
         }

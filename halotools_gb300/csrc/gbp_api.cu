@@ -1184,7 +1184,7 @@ int gbp_weighted_adjoint_3d(gbp_plan *plan, const double *xyz, int64_t n, const 
     c.naxes = 1;
     c.grad_out = grad_w;
     choose_grid(c.g, period3, search, pbc, n, plan->reach, MAX_CELLS_PER_DIM, 0.0, plan->block);
-    build_stencil(c.g, search, 0, false);  // ... but the full stencil: gather only
+    build_stencil(c.g, search, 0, false);  // the full stencil: a gather, no scatter to j
     ErrModel em = err_model(c.g);
     std::vector<double> E(nb);
     edges_top_walk(rbins, nb, E.data());
@@ -1208,6 +1208,10 @@ static int zheng07_args(gbp_plan *plan, const double *theta, Zheng07 *th) {
     th->logM1 = theta[3];
     th->alpha = theta[4];
     if (!(th->sigma > 0)) return fail(plan, GBP_ERR_INVALID, "sigma_logM must be positive");
+    th->M0 = std::pow(10.0, th->logM0);
+    th->M1 = std::pow(10.0, th->logM1);
+    th->inv_sigma = 1.0 / th->sigma;
+    th->inv_M1 = 1.0 / th->M1;
     return GBP_OK;
 }
 

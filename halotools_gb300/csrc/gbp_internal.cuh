@@ -245,6 +245,8 @@ cudaError_t gbp_launch_adjoint(const CountArgs &a, int grid, size_t smem, cudaSt
 int gbp_adjoint_occupancy(size_t smem, bool per_object = false);
 struct Zheng07 {
     double logMmin, sigma, logM0, logM1, alpha;
+    // derived on the host once per call (FP64 transcendentals are slow on the GPU)
+    double M0, M1, inv_sigma, inv_M1;
 };
 cudaError_t gbp_launch_zheng07_w(const double *mass, int64_t n, Zheng07 th, double *w,
                                  cudaStream_t st);
