@@ -379,8 +379,9 @@ def extra_s_mu_10m(dev, threads):
     cpu = int(c[-1, -1]) / dt
     return {"points": n, "gpu_ms": tg * 1e3, "gpu_pairs_per_s": pairs / tg,
             "cpu_pairs_per_s": cpu, "cpu_cores": threads, "cpu_sample_points": len(sub),
-            "gpu_over_cpu": (pairs / tg) / cpu, "stats": {k: plan.stats()[k] for k in
-                                                       ("ms_build", "ms_count", "block", "reach")}}
+            "gpu_over_cpu": (pairs / tg) / cpu, "recheck_fraction": plan.stats()["recheck_pairs"] / pairs,
+            "stats": {k: plan.stats()[k] for k in ("ms_build", "ms_count", "block", "reach",
+                                                   "recheck_pairs")}}
 
 
 def extra_npairs_3d_10m(dev, threads):
@@ -560,7 +561,8 @@ def main():
             "data": "synthetic (seeded; shapes of the named configuration)", "config": cfg,
             "roofline": roofline, "e2e": e2e, "clocks": clk.summary(),
             "gpu_launches": int(st["kernel_launches"]) * args.steps,
-            "ms_build": st["ms_build"], "ms_count": cnt_ms, "pairs_per_step": pairs_step}
+            "ms_build": st["ms_build"], "ms_count": cnt_ms, "pairs_per_step": pairs_step,
+            "recheck_pairs_per_step": int(st["recheck_pairs"])}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         v, dt, nsub = run_cpu(w, x, 1, 0, frac_side, threads)
         line["cpu_baseline"] = {"value": v, "unit": "pairs/s", "cores": threads, "kind": "port",

@@ -158,7 +158,28 @@ __device__ __forceinline__ void bin_mark(const PairV &p, float *hs, float *hc, c
     if (b < A.nb) kahan_add(hs, hc, b, sym ? 2.0f * wt : wt);
 }
 
+// ---------------- deferred FP64 rechecks (s, mu') ----------------
+// A pair whose bins FP32 cannot settle joins the warp's ring as {i, j, walk
+// starts, flags}; the warp re-evaluates 32 at once, every lane busy, which
+// costs one FP64 warp instruction where a lone lane's recheck costs the same.
+// A pair that finds the ring full is re-evaluated at once by its own lane.
+#define RQ_SYM 1
+#define RQ_KNOWN_A 2
+struct RQ {
+    int4 *ring;      // GBP_RQCAP entries of this warp
+    unsigned *tail;  // slots taken so far
+    unsigned head;   // warp-uniform: slots re-evaluated so far
+};
+
+__device__ __forceinline__ bool rq_push(const RQ &q, int4 e) {
+    const unsigned t = atomicAdd(q.tail, 1u);
+    if (t - q.head >= GBP_RQCAP) return false;
+    q.ring[t % GBP_RQCAP] = e;
+    return true;
+}
+
 // ---------------- stage 2: (rp, pi) ----------------
+// (rechecks are rare here, about 1e-4 of the pairs: each lane re-evaluates its own)
 template <class HT>
 __device__ __noinline__ void slow_xyz(float v0, float v1, int b0a, int b0b, int is, int js,
                                       bool sym, HT *hw, int stride, const AxisSm &A,
@@ -169,20 +190,19 @@ __device__ __noinline__ void slow_xyz(float v0, float v1, int b0a, int b0b, int 
         if (ka < A.nb && kb < Bx.nb) atomicAdd(&hw[ka * stride + kb], (HT)(sym ? 2 : 1));
         return;
     }
+    // a settled bin beyond the last edge leaves the pair out in both orders
+    if (ka >= A.nb || kb >= Bx.nb) return;
     if (is < 0 || js < 0) return;  // never a real pair (idle lane or padding)
     atomicAdd(a.nrecheck, 1ull);
     double p[3], q[3];
     ref_pos(a, 0, is, p);
     ref_pos(a, 1, js, q);
-    Exact3 r = exact_pair(p, q, a);
-    int ea = ka >= 0 ? ka : exact_bin(r.dxy, b0a, A);
-    int eb = kb >= 0 ? kb : exact_bin(r.dz2, b0b, Bx);
-    if (ea < A.nb && eb < Bx.nb) atomicAdd(&hw[ea * stride + eb], (HT)1);
-    if (!sym) return;
-    Exact3 s = exact_pair(q, p, a);
-    int fa = ka >= 0 ? ka : exact_bin(s.dxy, b0a, A);
-    int fb = kb >= 0 ? kb : exact_bin(s.dz2, b0b, Bx);
-    if (fa < A.nb && fb < Bx.nb) atomicAdd(&hw[fa * stride + fb], (HT)1);
+    for (int o = 0; o < (sym ? 2 : 1); o++) {
+        const Exact3 r = o == 0 ? exact_pair(p, q, a) : exact_pair(q, p, a);
+        const int ea = ka >= 0 ? ka : exact_bin(r.dxy, b0a, A);
+        const int eb = kb >= 0 ? kb : exact_bin(r.dz2, b0b, Bx);
+        if (ea < A.nb && eb < Bx.nb) atomicAdd(&hw[ea * stride + eb], (HT)1);
+    }
 }
 
 template <class HT>
@@ -207,15 +227,20 @@ __device__ __forceinline__ void bin_xyz(const PairV &p, HT *hw, int stride, cons
 // v = s^2 on axis 0; q = dxy / s^2 on axis 1, whose FP32 error depends on s:
 // the s table's 4th field holds the q error bound for the slot's smallest s.
 template <class HT>
+__device__ __forceinline__ void exact_smu(const int4 &e, HT *hw, int stride, const AxisSm &A,
+                                          const AxisSm &Q, const CountArgs &a);
+
+template <class HT>
 __device__ __noinline__ void slow_smu(float v, float q, float qb, int b0s, int is, int js,
                                       bool sym, HT *hw, int stride, const AxisSm &A,
-                                      const AxisSm &Q, const CountArgs &a) {
+                                      const AxisSm &Q, const RQ &rq, const CountArgs &a) {
     int ks = walk_bin(v, b0s, A);
-    int kq = -1;
+    int kq = -1, gq = 0;
     if (ks >= 0 && ks < A.nb && v > 0.0f) {
         int g = 0;
         while (g < Q.nb && q > Q.hi[g] + qb) g++;
         if (!(g < Q.nb && q > Q.lo[g] - qb)) kq = g;
+        gq = g > 0 ? g - 1 : 0;  // mu'^2 of both orders lies above edge g - 2
     }
     if (ks >= A.nb) return;  // beyond the s gate: never counted
     if (ks >= 0 && kq >= 0) {
@@ -223,16 +248,28 @@ __device__ __noinline__ void slow_smu(float v, float q, float qb, int b0s, int i
         return;
     }
     if (is < 0 || js < 0) return;  // never a real pair (idle lane or padding)
+    const int ss = ks >= 0 ? ks : -1 - ks;
+    const int4 e = make_int4(is, js, ss | (gq << 16), (sym ? RQ_SYM : 0) | (ks >= 0 ? RQ_KNOWN_A : 0));
+    if (rq_push(rq, e)) return;
     atomicAdd(a.nrecheck, 1ull);
+    exact_smu(e, hw, stride, A, Q, a);
+}
+
+// FP64 (s, mu') bins of a queued pair: sqr_mu = dxy / s^2 as an FP64 quotient,
+// 0 at s = 0 (npairs_s_mu_engine.pyx:200-226)
+template <class HT>
+__device__ __forceinline__ void exact_smu(const int4 &e, HT *hw, int stride, const AxisSm &A,
+                                          const AxisSm &Q, const CountArgs &a) {
     double p[3], qq[3];
-    ref_pos(a, 0, is, p);
-    ref_pos(a, 1, js, qq);
-    for (int o = 0; o < (sym ? 2 : 1); o++) {
-        Exact3 r = o == 0 ? exact_pair(p, qq, a) : exact_pair(qq, p, a);
-        int es = exact_bin(r.s2, 0, A);
+    ref_pos(a, 0, e.x, p);
+    ref_pos(a, 1, e.y, qq);
+    const int ss = e.z & 0xffff, sq = e.z >> 16;
+    for (int o = 0; o < ((e.w & RQ_SYM) ? 2 : 1); o++) {
+        const Exact3 r = o == 0 ? exact_pair(p, qq, a) : exact_pair(qq, p, a);
+        const int es = (e.w & RQ_KNOWN_A) ? ss : exact_bin(r.s2, ss, A);
         if (es >= A.nb) continue;
-        double mu2 = (r.s2 > 0.0) ? __ddiv_rn(r.dxy, r.s2) : 0.0;
-        int eq = exact_bin(mu2, 0, Q);
+        const double mu2 = (r.s2 > 0.0) ? __ddiv_rn(r.dxy, r.s2) : 0.0;
+        const int eq = exact_bin(mu2, sq, Q);
         if (eq >= Q.nb) continue;
         atomicAdd(&hw[es * stride + eq], (HT)1);
     }
@@ -240,7 +277,8 @@ __device__ __noinline__ void slow_smu(float v, float q, float qb, int b0s, int i
 
 template <class HT>
 __device__ __forceinline__ void bin_smu(const PairV &p, HT *hw, int stride, const AxisSm &A,
-                                        const AxisSm &Q, const Ix &ix, const CountArgs &a) {
+                                        const AxisSm &Q, const Ix &ix, const RQ &rq,
+                                        const CountArgs &a) {
     const float v = p.v0, dxy = p.v1;
     const bool sym = p.sym;
     float4 e0 = lut_entry_c<true>(v, A);
@@ -258,7 +296,7 @@ __device__ __forceinline__ void bin_smu(const PairV &p, HT *hw, int stride, cons
                (e1.z < -3.0e38f);
     if (amb) {
         slow_smu(v, q, qb, __float_as_int(e0.x), ix.ui[p.iu], ix.jw[p.jj], sym, hw, stride, A, Q,
-                 a);
+                 rq, a);
         return;
     }
     if (bq < Q.nb) atomicAdd(&hw[bs * stride + bq], (HT)(sym ? 2 : 1));
@@ -373,6 +411,10 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                   warp * GBP_USLOTS * (MARKC ? nw : 1);
     // MARKC: this warp's binned pairs of one round {bin | multiplicity << 16, second bin, i, j}
     int4 *s_rec = (int4 *)(smem + L.off_rec) + warp * 32;
+    // (s, mu'): this warp's ring of deferred FP64 rechecks and its tail
+    constexpr bool RQM = MODE == MODE_SMU;
+    RQ rq{(int4 *)(smem + L.off_rq) + warp * GBP_RQCAP,
+          (unsigned *)(smem + L.off_rq + GBP_WARPS * GBP_RQCAP * 16) + warp, 0u};
     double *s_uw64 = (double *)(smem + L.off_q + GBP_WARPS * GBP_USLOTS * 16) +
                      warp * GBP_USLOTS * (nw > 0 ? nw : 1);
     const Ix ix{uix, jix};
@@ -404,6 +446,7 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                            : (MARK || MARKC) ? (nb0 + 1) * 32 * 2 : (copies ? nbin : 0);
     unsigned *wh = s_hist + warp * warp_words;
     for (int i = lane; i < warp_words; i += 32) wh[i] = 0u;
+    if (RQM && lane == 0) *rq.tail = 0u;
     // jackknife: the CTA's (tag, bin) table of pair ends, after the warps' counts
     unsigned long long *s_tab =
         (unsigned long long *)(smem + L.off_hist + gbp_align(GBP_WARPS * (nb0 + 1) * 32 * 4, 16));
@@ -440,12 +483,41 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
             if (copies) bin_xyz(e, wh, stride2, A0, A1, ix, a);
             else bin_xyz(e, gh, stride2, A0, A1, ix, a);
         } else if (MODE == MODE_SMU) {
-            if (copies) bin_smu(e, wh, stride2, A0, A1, ix, a);
-            else bin_smu(e, gh, stride2, A0, A1, ix, a);
+            if (copies) bin_smu(e, wh, stride2, A0, A1, ix, rq, a);
+            else bin_smu(e, gh, stride2, A0, A1, ix, rq, a);
         } else if (MARK) bin_mark(e, hs, hc, A0, ix, a);
     };
     // Bin the rest of the queue, add this warp's histogram to mock mk and clear it.
+    // Re-evaluate queued rechecks in FP64, 32 at a time, until fewer than
+    // `keep` wait (keep = 1: all of them); they go to mock mk's histogram.
+    // Slots past a full ring were re-evaluated by their lanes: the tail
+    // drops back to the last stored slot.
+    auto rq_drain = [&](int mk, unsigned keep) {
+        __syncwarp();
+        const unsigned t = *(volatile unsigned *)rq.tail;
+        const unsigned end = rq.head + min(t - rq.head, (unsigned)GBP_RQCAP);
+        unsigned long long *gh = a.hist + (size_t)mk * a.hist_stride;
+        while (end - rq.head >= keep && end != rq.head) {
+            const unsigned n = min(end - rq.head, 32u);
+            if ((unsigned)lane < n) {
+                const int4 e = rq.ring[(rq.head + lane) % GBP_RQCAP];
+                if (copies) exact_smu(e, wh, stride2, A0, A1, a);
+                else exact_smu(e, gh, stride2, A0, A1, a);
+            }
+            if (lane == 0) atomicAdd(a.nrecheck, (unsigned long long)n);
+            rq.head += n;
+        }
+        __syncwarp();
+        if (lane == 0 && end != t) *rq.tail = end;
+        __syncwarp();
+    };
     auto warp_flush = [&](int mk) {
+        if (RQM) {
+            // the ring empties here, so its counters restart from 0
+            rq_drain(mk, 1u);
+            if (lane == 0) *rq.tail = 0u;
+            rq.head = 0;
+        }
         __syncwarp();
         unsigned long long *gh = a.hist + (size_t)mk * a.hist_stride;
         if (MODE == MODE_3D || JACK) {
@@ -780,6 +852,7 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                             if (ha) bin_entry(ea, cur_mock);
                             if (hb) bin_entry(eb, cur_mock);
                         }
+                        if (RQM) rq_drain(cur_mock, 32u);
                     }
                     __syncwarp();
                 };

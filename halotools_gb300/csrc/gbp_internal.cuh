@@ -96,9 +96,14 @@ struct CountArgs {
 // jw: bytes of staged weights per j-point (marked mode), copies: shared
 // histogram copies (2-D and wide 1-D modes).
 struct SmemLayout {
-    int off_lut0, off_lut1, off_qb, off_hl0, off_hl1, off_j, off_j2, off_jw, off_q, off_code, off_rec, off_D,
-        off_E0, off_E1, off_hi0, off_lo0, off_hi1, off_lo1, off_off, off_hist, total;
+    int off_lut0, off_lut1, off_qb, off_hl0, off_hl1, off_j, off_j2, off_jw, off_q, off_code, off_rec, off_rq,
+        off_D, off_E0, off_E1, off_hi0, off_lo0, off_hi1, off_lo1, off_off, off_hist, total;
 };
+
+// Deferred FP64 rechecks of the (s, mu') mode: each warp keeps a ring of
+// GBP_RQCAP pairs {i, j, walk starts, flags} and its tail counter, and
+// re-evaluates them 32 at a time with every lane busy.
+#define GBP_RQCAP 96
 
 // Stage-2 i-slots per warp: the lane's first point at slot lane, its second at
 // lane + 48, so that the two never share a shared-memory bank.
@@ -130,6 +135,7 @@ __host__ __device__ inline SmemLayout gbp_smem_layout(int mode, int T0, int T1, 
     L.off_code = o;
     o += adj ? 0 : GBP_WARPS * ((mode == MODE_MARK || mode == MODE_MARKC) ? 1024 : 2048) * 2;
     L.off_rec = o; o += (mode == MODE_MARKC) ? GBP_WARPS * 32 * 16 : 0;  // binned pairs of a round
+    L.off_rq = o; o += (mode == MODE_SMU) ? GBP_WARPS * (GBP_RQCAP * 16 + 16) : 0;
     L.off_D = o; o += nsten * 16;
     L.off_E0 = o; o += gbp_align(nb0 * 8, 16);
     L.off_E1 = o; o += gbp_align(nb1 * 8, 16);
