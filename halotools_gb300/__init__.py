@@ -8,19 +8,21 @@ halotools' estimators bound at import time, so ``tpcf``, ``wp``,
 ``rp_pi_tpcf``, ``s_mu_tpcf`` and ``marked_tpcf`` pick them up as drop-ins.
 """
 from .pair_counters import (HalotoolsError, marked_npairs_3d, marked_npairs_3d_channels,
-                            npairs_3d, npairs_jackknife_3d, npairs_per_object_3d,
-                            npairs_projected, npairs_s_mu, npairs_xy_z)
+                            marked_npairs_xy_z, npairs_3d, npairs_jackknife_3d,
+                            npairs_per_object_3d, npairs_projected, npairs_s_mu, npairs_xy_z,
+                            weighted_npairs_s_mu)
 from ._native import GBPairsError, GBPairsUnavailable, Plan, default_plan
 from .batched import BatchedCounter, npairs_3d_batched
 from . import estimators
 
 __all__ = ("npairs_3d", "npairs_xy_z", "npairs_s_mu", "marked_npairs_3d",
            "marked_npairs_3d_channels", "npairs_projected", "npairs_jackknife_3d",
-           "npairs_per_object_3d", "HalotoolsError", "GBPairsError", "GBPairsUnavailable", "Plan", "default_plan",
+           "npairs_per_object_3d", "marked_npairs_xy_z", "weighted_npairs_s_mu",
+           "HalotoolsError", "GBPairsError", "GBPairsUnavailable", "Plan", "default_plan",
            "npairs_3d_batched", "BatchedCounter", "install_into_halotools", "estimators")
 
 # module attribute -> our function, for every place halotools binds a counter
-_BINDINGS = (
+_BINDINGS = tuple([
     ("halotools.mock_observables.pair_counters", "npairs_3d", npairs_3d),
     ("halotools.mock_observables.pair_counters", "npairs_xy_z", npairs_xy_z),
     ("halotools.mock_observables.pair_counters", "npairs_s_mu", npairs_s_mu),
@@ -31,6 +33,14 @@ _BINDINGS = (
     ("halotools.mock_observables.pair_counters", "npairs_per_object_3d", npairs_per_object_3d),
     ("halotools.mock_observables.two_point_clustering.tpcf_jackknife", "npairs_jackknife_3d",
      npairs_jackknife_3d),
+    ("halotools.mock_observables.pair_counters", "marked_npairs_xy_z", marked_npairs_xy_z),
+    ("halotools.mock_observables.pair_counters", "weighted_npairs_s_mu", weighted_npairs_s_mu),
+] + [
+    # the intrinsic-alignment estimators bind marked_npairs_xy_z at import time
+    ("halotools.mock_observables.ia_correlations." + m, "marked_npairs_xy_z", marked_npairs_xy_z)
+    for m in ("ee_projected", "ed_projected", "ii_plus_projected", "ii_minus_projected",
+              "gi_plus_projected", "gi_minus_projected")
+] + [
     ("halotools.mock_observables", "npairs_3d", npairs_3d),
     ("halotools.mock_observables", "npairs_xy_z", npairs_xy_z),
     ("halotools.mock_observables", "npairs_s_mu", npairs_s_mu),
@@ -40,7 +50,7 @@ _BINDINGS = (
     ("halotools.mock_observables.two_point_clustering.s_mu_tpcf", "npairs_s_mu", npairs_s_mu),
     ("halotools.mock_observables.two_point_clustering.marked_tpcf", "marked_npairs_3d",
      marked_npairs_3d),
-)
+])
 
 
 def install_into_halotools():

@@ -460,7 +460,13 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
         a.top0 = std::min(c.ax[0].hi[nb0 - 1], 1.0e30f);
         a.top1 = c.naxes > 1 ? std::min(c.ax[1].hi[nb1 - 1], 1.0e30f) : 0.f;
         a.self_bin = host_bin(nb0, c.ax[0].E.data(), 0.0);
-        const int jwb = c.mode == MODE_MARK    ? (c.wf == 0 ? 8 * c.nw : 4)
+        const bool w2 = c.mode == MODE_XYZW || c.mode == MODE_SMUW;
+        if (w2) {
+            // the flat (axis 0, axis 1) bin of separation 0, or -1 when outside
+            const int sb1 = host_bin(nb1, c.ax[1].E.data(), 0.0);
+            a.self_bin = (a.self_bin < nb0 && sb1 < nb1) ? a.self_bin * (nb1 + 1) + sb1 : -1;
+        }
+        const int jwb = (c.mode == MODE_MARK || w2) ? (c.wf == 0 ? 8 * c.nw : 4)
                         : c.mode == MODE_MARKC ? 4 * c.nw
                         : c.mode == MODE_ADJ   ? 4
                         : c.mode == MODE_POBJ  ? 4   // the gather kernel's fixed stride
@@ -474,6 +480,7 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
             size_t one = (size_t)(nb0 + 1) * (size_t)(c.naxes > 1 ? nb1 + 1 : 1) * 4;
             if (one * GBP_WARPS > (96u << 10)) copies = 0;
         }
+        if (c.mode == MODE_XYZW) copies = 0;  // sums only: no integer counts
         a.hist_copies = copies;
         SmemLayout L = gbp_smem_layout(c.mode, T0, T1, nb0, nb1, nsten, copies, jwb, c.ntag);
         size_t smem = (size_t)L.total;
@@ -562,7 +569,8 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
         return run_call(plan, c, hist_host, histd_host);
     }
     hist_host.assign(at<unsigned long long>(H, h_hist), at<unsigned long long>(H, h_hist) + nm * nhist);
-    if (c.mode != MODE_MARK && c.mode != MODE_MARKC) add_self_pairs(c, hist_host);
+    if (c.mode != MODE_MARK && c.mode != MODE_MARKC && c.mode != MODE_XYZW)
+        add_self_pairs(c, hist_host);
     if (histd_host) histd_host->assign(at<double>(H, h_histd), at<double>(H, h_histd) + nm * nhist);
     if (ntab) c.htag.assign(at<unsigned long long>(H, h_htag), at<unsigned long long>(H, h_htag) + ntab);
     gbp_stats &S = plan->stats;
@@ -823,23 +831,23 @@ int gbp_batched_npairs_3d(gbp_plan *plan, const void *xyz, int32_t xyz_f32, cons
     return GBP_OK;
 }
 
-int gbp_npairs_xy_z(gbp_plan *plan, const double *xyz1, int64_t n1, const double *xyz2, int64_t n2,
-                    const double *rp_bins, int32_t n_rp, const double *pi_bins, int32_t n_pi,
-                    const double *period3, int32_t pbc, int32_t mem, int64_t *counts) {
+// (rp, pi) geometry shared by npairs_xy_z and marked_npairs_xy_z: grid, stencil,
+// edges walked from the top (npairs_xy_z_engine.pyx:183-194) and their guard bands
+static int setup_xyz(gbp_plan *plan, Call &c, const double *xyz1, int64_t n1, const double *xyz2,
+                     int64_t n2, const double *rp_bins, int32_t n_rp, const double *pi_bins,
+                     int32_t n_pi, const double *period3, int32_t pbc, int32_t mem, bool autocorr) {
     int rc = check_common(plan, xyz1, n1, xyz2, n2, period3, pbc, mem);
     if (rc) return rc;
-    if (!rp_bins || !pi_bins || n_rp < 2 || n_pi < 2 || n_rp > GBP_NB_MAX || n_pi > GBP_NB_MAX || !counts)
+    if (!rp_bins || !pi_bins || n_rp < 2 || n_pi < 2 || n_rp > GBP_NB_MAX || n_pi > GBP_NB_MAX)
         return fail(plan, GBP_ERR_INVALID, "bin arrays must have 2..%d entries", GBP_NB_MAX);
     double rpm = max_nan(rp_bins, n_rp), pim = max_nan(pi_bins, n_pi);
     double search[3] = {rpm, rpm, pim};
     if ((rc = check_search(plan, search, period3))) return rc;
-    Call c;
-    c.mode = MODE_XYZ;
     c.xyz1 = xyz1;
     c.xyz2 = xyz2;
     c.n1 = n1;
     c.n2 = n2;
-    c.autocorr = (xyz1 == xyz2 && n1 == n2);
+    c.autocorr = autocorr;
     c.mem = mem;
     c.naxes = 2;
     choose_grid(c.g, period3, search, pbc, n2, plan->reach, MAX_CELLS_PER_DIM, 0.0, plan->block);
@@ -852,42 +860,98 @@ int gbp_npairs_xy_z(gbp_plan *plan, const double *xyz1, int64_t n1, const double
     c.ax[1].set(E1, &em, 1);
     c.ax[0].make_lut(no_qband);
     c.ax[1].make_lut(no_qband);
+    return GBP_OK;
+}
+
+// out[k][g] = sum of the differential bins a <= k, b <= g: running sums along g,
+// then along k (no subtraction, so integer-valued sums stay exact)
+extern "C++" {
+template <class T, class H>
+static void cumulate_2d(const H *h, int na, int nb, T *out) {
+    const int st = nb + 1;
+    for (int k = 0; k < na; k++) {
+        T run = 0;
+        for (int g = 0; g < nb; g++) {
+            run += (T)h[(size_t)k * st + g];
+            out[k * nb + g] = run + (k > 0 ? out[(k - 1) * nb + g] : (T)0);
+        }
+    }
+}
+}
+
+int gbp_npairs_xy_z(gbp_plan *plan, const double *xyz1, int64_t n1, const double *xyz2, int64_t n2,
+                    const double *rp_bins, int32_t n_rp, const double *pi_bins, int32_t n_pi,
+                    const double *period3, int32_t pbc, int32_t mem, int64_t *counts) {
+    if (!counts) return fail(plan, GBP_ERR_INVALID, "null output");
+    Call c;
+    c.mode = MODE_XYZ;
+    int rc = setup_xyz(plan, c, xyz1, n1, xyz2, n2, rp_bins, n_rp, pi_bins, n_pi, period3, pbc,
+                       mem, xyz1 == xyz2 && n1 == n2);
+    if (rc) return rc;
     if (n1 == 0 || n2 == 0) {
         for (int k = 0; k < n_rp * n_pi; k++) counts[k] = 0;
         return GBP_OK;
     }
     std::vector<unsigned long long> h;
     if ((rc = run_call(plan, c, h))) return rc;
-    // counts[k][g] = sum over differential bins a <= k, b <= g
-    const int st = n_pi + 1;
-    for (int k = 0; k < n_rp; k++)
-        for (int g2 = 0; g2 < n_pi; g2++) {
-            int64_t v = (int64_t)h[(size_t)k * st + g2];
-            if (k > 0) v += counts[(k - 1) * n_pi + g2];
-            if (g2 > 0) v += counts[k * n_pi + g2 - 1];
-            if (k > 0 && g2 > 0) v -= counts[(k - 1) * n_pi + g2 - 1];
-            counts[k * n_pi + g2] = v;
-        }
+    cumulate_2d(h.data(), n_rp, n_pi, counts);
     return GBP_OK;
 }
 
-int gbp_npairs_s_mu(gbp_plan *plan, const double *xyz1, int64_t n1, const double *xyz2, int64_t n2,
-                    const double *s_bins, int32_t n_s, const double *mu_prime, int32_t n_mu,
-                    const double *period3, int32_t pbc, int32_t mem, int64_t *counts) {
+// marking-function ids: number of weights per point (marked_npairs_3d.py:281-326)
+static const int WFUNC_NW[18] = {0, 1, 1, 2, 2, 2, 2, 2, 2, 2, 2, 2, 4, 4, 3, 3, 5, 5};
+// f(a, b) == f(b, a): an auto-correlation may walk each unordered pair once
+static bool wfunc_symmetric(int id) { return id <= 4 || id >= 12; }
+
+int gbp_marked_npairs_xy_z(gbp_plan *plan, const double *xyz1, int64_t n1, const double *xyz2,
+                           int64_t n2, const double *w1, const double *w2, int32_t nw,
+                           int32_t wfunc_id, const double *rp_bins, int32_t n_rp,
+                           const double *pi_bins, int32_t n_pi, const double *period3, int32_t pbc,
+                           int32_t mem, double *out) {
+    if (!out) return fail(plan, GBP_ERR_INVALID, "null output");
+    if (wfunc_id < 1 || wfunc_id > 17)
+        return fail(plan, GBP_ERR_INVALID, "weight_func_id %d is not recognized", wfunc_id);
+    if (nw != WFUNC_NW[wfunc_id])
+        return fail(plan, GBP_ERR_INVALID, "weight_func_id %d needs %d weights per point", wfunc_id,
+                    WFUNC_NW[wfunc_id]);
+    if ((n1 > 0 && !w1) || (n2 > 0 && !w2)) return fail(plan, GBP_ERR_INVALID, "null weights");
+    Call c;
+    c.mode = MODE_XYZW;
+    c.wf = (wfunc_id == 1) ? 1 : (wfunc_id == 2) ? 2 : 0;
+    c.w1 = w1;
+    c.w2 = w2;
+    c.nw = nw;
+    c.wfunc = wfunc_id;
+    int rc = setup_xyz(plan, c, xyz1, n1, xyz2, n2, rp_bins, n_rp, pi_bins, n_pi, period3, pbc,
+                       mem, xyz1 == xyz2 && n1 == n2 && w1 == w2 && wfunc_symmetric(wfunc_id));
+    if (rc) return rc;
+    for (int k = 0; k < n_rp * n_pi; k++) out[k] = 0.0;
+    if (n1 == 0 || n2 == 0) return GBP_OK;
+    std::vector<unsigned long long> h;
+    std::vector<double> hd;
+    if ((rc = run_call(plan, c, h, &hd))) return rc;
+    cumulate_2d(hd.data(), n_rp, n_pi, out);
+    return GBP_OK;
+}
+
+// (s, mu') geometry shared by npairs_s_mu and weighted_npairs_s_mu: differential
+// bins found by the strict walks of npairs_s_mu_engine.pyx:200-226, the FP32
+// guard bands, and the per-slot error bound of q = dxy / s^2
+static int setup_smu(gbp_plan *plan, Call &c, const double *xyz1, int64_t n1, const double *xyz2,
+                     int64_t n2, const double *s_bins, int32_t n_s, const double *mu_prime,
+                     int32_t n_mu, const double *period3, int32_t pbc, int32_t mem) {
     int rc = check_common(plan, xyz1, n1, xyz2, n2, period3, pbc, mem);
     if (rc) return rc;
-    if (!s_bins || !mu_prime || n_s < 2 || n_mu < 2 || n_s > GBP_NB_MAX || n_mu > GBP_NB_MAX || !counts)
+    if (!s_bins || !mu_prime || n_s < 2 || n_mu < 2 || n_s > GBP_NB_MAX || n_mu > GBP_NB_MAX)
         return fail(plan, GBP_ERR_INVALID, "bin arrays must have 2..%d entries", GBP_NB_MAX);
     double smax = max_nan(s_bins, n_s);
     double search[3] = {smax, smax, smax};
     if ((rc = check_search(plan, search, period3))) return rc;
-    Call c;
-    c.mode = MODE_SMU;
     c.xyz1 = xyz1;
     c.xyz2 = xyz2;
     c.n1 = n1;
     c.n2 = n2;
-    c.autocorr = (xyz1 == xyz2 && n1 == n2);
+    c.autocorr = (xyz1 == xyz2 && n1 == n2 && c.w1 == c.w2);
     c.mem = mem;
     c.naxes = 2;
     choose_grid(c.g, period3, search, pbc, n2, plan->reach, MAX_CELLS_PER_DIM, 0.0, plan->block);
@@ -916,6 +980,17 @@ int gbp_npairs_s_mu(gbp_plan *plan, const double *xyz1, int64_t n1, const double
         return f_up(2.0 * qb);
     });
     c.ax[1].make_lut(no_qband);
+    return GBP_OK;
+}
+
+int gbp_npairs_s_mu(gbp_plan *plan, const double *xyz1, int64_t n1, const double *xyz2, int64_t n2,
+                    const double *s_bins, int32_t n_s, const double *mu_prime, int32_t n_mu,
+                    const double *period3, int32_t pbc, int32_t mem, int64_t *counts) {
+    if (!counts) return fail(plan, GBP_ERR_INVALID, "null output");
+    Call c;
+    c.mode = MODE_SMU;
+    int rc = setup_smu(plan, c, xyz1, n1, xyz2, n2, s_bins, n_s, mu_prime, n_mu, period3, pbc, mem);
+    if (rc) return rc;
     if (n1 == 0 || n2 == 0) {
         for (int k = 0; k < n_s * n_mu; k++) counts[k] = 0;
         return GBP_OK;
@@ -923,15 +998,37 @@ int gbp_npairs_s_mu(gbp_plan *plan, const double *xyz1, int64_t n1, const double
     std::vector<unsigned long long> h;
     if ((rc = run_call(plan, c, h))) return rc;
     // npairs_s_mu_engine.pyx:232-234
-    const int st = n_mu + 1;
-    for (int k = 0; k < n_s; k++)
-        for (int g2 = 0; g2 < n_mu; g2++) {
-            int64_t v = (int64_t)h[(size_t)k * st + g2];
-            if (k > 0) v += counts[(k - 1) * n_mu + g2];
-            if (g2 > 0) v += counts[k * n_mu + g2 - 1];
-            if (k > 0 && g2 > 0) v -= counts[(k - 1) * n_mu + g2 - 1];
-            counts[k * n_mu + g2] = v;
-        }
+    cumulate_2d(h.data(), n_s, n_mu, counts);
+    return GBP_OK;
+}
+
+int gbp_weighted_npairs_s_mu(gbp_plan *plan, const double *xyz1, int64_t n1, const double *xyz2,
+                             int64_t n2, const double *w1, const double *w2, const double *s_bins,
+                             int32_t n_s, const double *mu_prime, int32_t n_mu,
+                             const double *period3, int32_t pbc, int32_t mem, int64_t *counts,
+                             double *wcounts) {
+    if (!counts || !wcounts) return fail(plan, GBP_ERR_INVALID, "null output");
+    if ((n1 > 0 && !w1) || (n2 > 0 && !w2)) return fail(plan, GBP_ERR_INVALID, "null weights");
+    Call c;
+    c.mode = MODE_SMUW;
+    c.wf = 1;  // w1 * w2 (weighted_npairs_s_mu_engine.pyx:249)
+    c.w1 = w1;
+    c.w2 = w2;
+    c.nw = 1;
+    c.wfunc = 1;
+    int rc = setup_smu(plan, c, xyz1, n1, xyz2, n2, s_bins, n_s, mu_prime, n_mu, period3, pbc, mem);
+    if (rc) return rc;
+    for (int k = 0; k < n_s * n_mu; k++) {
+        counts[k] = 0;
+        wcounts[k] = 0.0;
+    }
+    if (n1 == 0 || n2 == 0) return GBP_OK;
+    std::vector<unsigned long long> h;
+    std::vector<double> hd;
+    if ((rc = run_call(plan, c, h, &hd))) return rc;
+    // weighted_npairs_s_mu_engine.pyx:251-255: rectangle sums of the differential bins
+    cumulate_2d(h.data(), n_s, n_mu, counts);
+    cumulate_2d(hd.data(), n_s, n_mu, wcounts);
     return GBP_OK;
 }
 
@@ -941,10 +1038,8 @@ int gbp_marked_npairs_3d(gbp_plan *plan, const double *xyz1, int64_t n1, const d
                          int32_t pbc, int32_t mem, double *out) {
     int rc = check_common(plan, xyz1, n1, xyz2, n2, period3, pbc, mem);
     if (rc) return rc;
-    // marked_npairs_3d.py:281-326: number of weights per marking function
-    static const int NW[18] = {0, 1, 1, 2, 2, 2, 2, 2, 2, 2, 2, 2, 4, 4, 3, 3, 5, 5};
     if (wfunc_id < 1 || wfunc_id > 17) return fail(plan, GBP_ERR_INVALID, "weight_func_id %d is not recognized", wfunc_id);
-    if (nw != NW[wfunc_id]) return fail(plan, GBP_ERR_INVALID, "weight_func_id %d needs %d weights per point", wfunc_id, NW[wfunc_id]);
+    if (nw != WFUNC_NW[wfunc_id]) return fail(plan, GBP_ERR_INVALID, "weight_func_id %d needs %d weights per point", wfunc_id, WFUNC_NW[wfunc_id]);
     if ((n1 > 0 && !w1) || (n2 > 0 && !w2)) return fail(plan, GBP_ERR_INVALID, "null weights");
     if (!rbins || nb < 2 || nb > GBP_NB_LANE || !out)
         return fail(plan, GBP_ERR_INVALID, "rbins must have 2..%d entries", GBP_NB_LANE);
@@ -953,7 +1048,7 @@ int gbp_marked_npairs_3d(gbp_plan *plan, const double *xyz1, int64_t n1, const d
     if ((rc = check_search(plan, search, period3))) return rc;
     // symmetric marking functions (f(a, b) == f(b, a)) may walk each unordered
     // pair once; the others walk every ordered pair
-    const bool symmetric = wfunc_id <= 4 || wfunc_id >= 12;
+    const bool symmetric = wfunc_symmetric(wfunc_id);
     Call c;
     c.mode = MODE_MARK;
     c.wf = (wfunc_id == 1) ? 1 : (wfunc_id == 2) ? 2 : 0;

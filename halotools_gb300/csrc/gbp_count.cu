@@ -42,6 +42,7 @@ struct PairV {
     float v0, v1;
     int iu, jj;
     bool sym;
+    float w;  // weighted 2-D modes: the pair's weight
 };
 struct Ix {
     const int *ui;  // sorted index of each i-slot
@@ -158,11 +159,27 @@ __device__ __forceinline__ void bin_mark(const PairV &p, float *hs, float *hc, c
     if (b < A.nb) kahan_add(hs, hc, b, sym ? 2.0f * wt : wt);
 }
 
+// ---------------- weighted 2-D sums (marked xy_z, weighted s_mu) ----------------
+// hi takes each weight by atomic add; the add's exact rounding error (TwoSum on
+// the value the atomic returned, the sum it stored being that value plus x
+// rounded to nearest) goes to lo, so hi + lo carries the sum to about 2^-48.
+struct WSink {
+    float *hi, *lo;
+};
+
+__device__ __forceinline__ void w2_add(const WSink &s, int b, float x) {
+    const float old = atomicAdd(&s.hi[b], x);
+    const float t = old + x;
+    const float bp = t - old;
+    const float err = (old - (t - bp)) + (x - bp);
+    if (err != 0.0f) atomicAdd(&s.lo[b], err);
+}
+
 // ---------------- deferred FP64 rechecks (s, mu') ----------------
 // A pair whose bins FP32 cannot settle joins the warp's ring as {i, j, walk
-// starts, flags}; the warp re-evaluates 32 at once, every lane busy, which
-// costs one FP64 warp instruction where a lone lane's recheck costs the same.
-// A pair that finds the ring full is re-evaluated at once by its own lane.
+// starts and flags, weight}; the warp re-evaluates 32 at once, every lane busy,
+// which costs one FP64 warp instruction where a lone lane's recheck costs the
+// same.  A pair that finds the ring full is re-evaluated at once by its lane.
 #define RQ_SYM 1
 #define RQ_KNOWN_A 2
 struct RQ {
@@ -179,15 +196,19 @@ __device__ __forceinline__ bool rq_push(const RQ &q, int4 e) {
 }
 
 // ---------------- stage 2: (rp, pi) ----------------
-// (rechecks are rare here, about 1e-4 of the pairs: each lane re-evaluates its own)
-template <class HT>
+// (rechecks are rare here, about 1e-4 of the pairs: each lane re-evaluates its
+// own).  CNT: integer counts into hw; WT: the pair's weight into ws.
+template <class HT, bool CNT, bool WT>
 __device__ __noinline__ void slow_xyz(float v0, float v1, int b0a, int b0b, int is, int js,
-                                      bool sym, HT *hw, int stride, const AxisSm &A,
-                                      const AxisSm &Bx, const CountArgs &a) {
+                                      bool sym, float wt, HT *hw, const WSink ws, int stride,
+                                      const AxisSm &A, const AxisSm &Bx, const CountArgs &a) {
     int ka = walk_bin(v0, b0a, A);
     int kb = walk_bin(v1, b0b, Bx);
     if (ka >= 0 && kb >= 0) {
-        if (ka < A.nb && kb < Bx.nb) atomicAdd(&hw[ka * stride + kb], (HT)(sym ? 2 : 1));
+        if (ka < A.nb && kb < Bx.nb) {
+            if (CNT) atomicAdd(&hw[ka * stride + kb], (HT)(sym ? 2 : 1));
+            if (WT) w2_add(ws, ka * stride + kb, sym ? 2.0f * wt : wt);
+        }
         return;
     }
     // a settled bin beyond the last edge leaves the pair out in both orders
@@ -201,13 +222,17 @@ __device__ __noinline__ void slow_xyz(float v0, float v1, int b0a, int b0b, int 
         const Exact3 r = o == 0 ? exact_pair(p, q, a) : exact_pair(q, p, a);
         const int ea = ka >= 0 ? ka : exact_bin(r.dxy, b0a, A);
         const int eb = kb >= 0 ? kb : exact_bin(r.dz2, b0b, Bx);
-        if (ea < A.nb && eb < Bx.nb) atomicAdd(&hw[ea * stride + eb], (HT)1);
+        if (ea < A.nb && eb < Bx.nb) {
+            if (CNT) atomicAdd(&hw[ea * stride + eb], (HT)1);
+            if (WT) w2_add(ws, ea * stride + eb, wt);
+        }
     }
 }
 
-template <class HT>
-__device__ __forceinline__ void bin_xyz(const PairV &p, HT *hw, int stride, const AxisSm &A,
-                                        const AxisSm &Bx, const Ix &ix, const CountArgs &a) {
+template <class HT, bool CNT, bool WT>
+__device__ __forceinline__ void bin_xyz(const PairV &p, HT *hw, const WSink &ws, int stride,
+                                        const AxisSm &A, const AxisSm &Bx, const Ix &ix,
+                                        const CountArgs &a) {
     const float v0 = p.v0, v1 = p.v1;
     const bool sym = p.sym;
     float4 e0 = lut_entry_c<false>(v0, A);
@@ -216,24 +241,29 @@ __device__ __forceinline__ void bin_xyz(const PairV &p, HT *hw, int stride, cons
     int bb = __float_as_int(e1.x) + (v1 > e1.y ? 1 : 0);
     bool amb = ((v0 > e0.z) & !(v0 > e0.y)) | ((v1 > e1.z) & !(v1 > e1.y));
     if (amb) {
-        slow_xyz(v0, v1, __float_as_int(e0.x), __float_as_int(e1.x), ix.ui[p.iu], ix.jw[p.jj], sym,
-                 hw, stride, A, Bx, a);
+        slow_xyz<HT, CNT, WT>(v0, v1, __float_as_int(e0.x), __float_as_int(e1.x), ix.ui[p.iu],
+                              ix.jw[p.jj], sym, p.w, hw, ws, stride, A, Bx, a);
         return;
     }
-    if ((ba < A.nb) & (bb < Bx.nb)) atomicAdd(&hw[ba * stride + bb], (HT)(sym ? 2 : 1));
+    if ((ba < A.nb) & (bb < Bx.nb)) {
+        if (CNT) atomicAdd(&hw[ba * stride + bb], (HT)(sym ? 2 : 1));
+        if (WT) w2_add(ws, ba * stride + bb, sym ? 2.0f * p.w : p.w);
+    }
 }
 
 // ---------------- stage 2: (s, mu') ----------------
 // v = s^2 on axis 0; q = dxy / s^2 on axis 1, whose FP32 error depends on s:
 // the s table's 4th field holds the q error bound for the slot's smallest s.
-template <class HT>
-__device__ __forceinline__ void exact_smu(const int4 &e, HT *hw, int stride, const AxisSm &A,
-                                          const AxisSm &Q, const CountArgs &a);
+// A queued pair: {i, j, s walk start | mu' walk start << 11 | flags << 22, weight}.
+template <class HT, bool CNT, bool WT>
+__device__ __forceinline__ void exact_smu(const int4 &e, HT *hw, const WSink &ws, int stride,
+                                          const AxisSm &A, const AxisSm &Q, const CountArgs &a);
 
-template <class HT>
+template <class HT, bool CNT, bool WT>
 __device__ __noinline__ void slow_smu(float v, float q, float qb, int b0s, int is, int js,
-                                      bool sym, HT *hw, int stride, const AxisSm &A,
-                                      const AxisSm &Q, const RQ &rq, const CountArgs &a) {
+                                      bool sym, float wt, HT *hw, const WSink ws, int stride,
+                                      const AxisSm &A, const AxisSm &Q, const RQ &rq,
+                                      const CountArgs &a) {
     int ks = walk_bin(v, b0s, A);
     int kq = -1, gq = 0;
     if (ks >= 0 && ks < A.nb && v > 0.0f) {
@@ -244,41 +274,48 @@ __device__ __noinline__ void slow_smu(float v, float q, float qb, int b0s, int i
     }
     if (ks >= A.nb) return;  // beyond the s gate: never counted
     if (ks >= 0 && kq >= 0) {
-        if (kq < Q.nb) atomicAdd(&hw[ks * stride + kq], (HT)(sym ? 2 : 1));
+        if (kq < Q.nb) {
+            if (CNT) atomicAdd(&hw[ks * stride + kq], (HT)(sym ? 2 : 1));
+            if (WT) w2_add(ws, ks * stride + kq, sym ? 2.0f * wt : wt);
+        }
         return;
     }
     if (is < 0 || js < 0) return;  // never a real pair (idle lane or padding)
     const int ss = ks >= 0 ? ks : -1 - ks;
-    const int4 e = make_int4(is, js, ss | (gq << 16), (sym ? RQ_SYM : 0) | (ks >= 0 ? RQ_KNOWN_A : 0));
+    const int4 e = make_int4(is, js,
+                             ss | (gq << 11) | (((sym ? RQ_SYM : 0) | (ks >= 0 ? RQ_KNOWN_A : 0)) << 22),
+                             __float_as_int(wt));
     if (rq_push(rq, e)) return;
     atomicAdd(a.nrecheck, 1ull);
-    exact_smu(e, hw, stride, A, Q, a);
+    exact_smu<HT, CNT, WT>(e, hw, ws, stride, A, Q, a);
 }
 
 // FP64 (s, mu') bins of a queued pair: sqr_mu = dxy / s^2 as an FP64 quotient,
 // 0 at s = 0 (npairs_s_mu_engine.pyx:200-226)
-template <class HT>
-__device__ __forceinline__ void exact_smu(const int4 &e, HT *hw, int stride, const AxisSm &A,
-                                          const AxisSm &Q, const CountArgs &a) {
+template <class HT, bool CNT, bool WT>
+__device__ __forceinline__ void exact_smu(const int4 &e, HT *hw, const WSink &ws, int stride,
+                                          const AxisSm &A, const AxisSm &Q, const CountArgs &a) {
     double p[3], qq[3];
     ref_pos(a, 0, e.x, p);
     ref_pos(a, 1, e.y, qq);
-    const int ss = e.z & 0xffff, sq = e.z >> 16;
-    for (int o = 0; o < ((e.w & RQ_SYM) ? 2 : 1); o++) {
+    const int ss = e.z & 0x7ff, sq = (e.z >> 11) & 0x7ff, fl = e.z >> 22;
+    const float wt = __int_as_float(e.w);
+    for (int o = 0; o < ((fl & RQ_SYM) ? 2 : 1); o++) {
         const Exact3 r = o == 0 ? exact_pair(p, qq, a) : exact_pair(qq, p, a);
-        const int es = (e.w & RQ_KNOWN_A) ? ss : exact_bin(r.s2, ss, A);
+        const int es = (fl & RQ_KNOWN_A) ? ss : exact_bin(r.s2, ss, A);
         if (es >= A.nb) continue;
         const double mu2 = (r.s2 > 0.0) ? __ddiv_rn(r.dxy, r.s2) : 0.0;
         const int eq = exact_bin(mu2, sq, Q);
         if (eq >= Q.nb) continue;
-        atomicAdd(&hw[es * stride + eq], (HT)1);
+        if (CNT) atomicAdd(&hw[es * stride + eq], (HT)1);
+        if (WT) w2_add(ws, es * stride + eq, wt);
     }
 }
 
-template <class HT>
-__device__ __forceinline__ void bin_smu(const PairV &p, HT *hw, int stride, const AxisSm &A,
-                                        const AxisSm &Q, const Ix &ix, const RQ &rq,
-                                        const CountArgs &a) {
+template <class HT, bool CNT, bool WT>
+__device__ __forceinline__ void bin_smu(const PairV &p, HT *hw, const WSink &ws, int stride,
+                                        const AxisSm &A, const AxisSm &Q, const Ix &ix,
+                                        const RQ &rq, const CountArgs &a) {
     const float v = p.v0, dxy = p.v1;
     const bool sym = p.sym;
     float4 e0 = lut_entry_c<true>(v, A);
@@ -295,11 +332,14 @@ __device__ __forceinline__ void bin_smu(const PairV &p, HT *hw, int stride, cons
     bool amb = ((v > e0.z) & !(v > e0.y)) | !(q - below > qb) | !(above - q > qb) |
                (e1.z < -3.0e38f);
     if (amb) {
-        slow_smu(v, q, qb, __float_as_int(e0.x), ix.ui[p.iu], ix.jw[p.jj], sym, hw, stride, A, Q,
-                 rq, a);
+        slow_smu<HT, CNT, WT>(v, q, qb, __float_as_int(e0.x), ix.ui[p.iu], ix.jw[p.jj], sym, p.w,
+                              hw, ws, stride, A, Q, rq, a);
         return;
     }
-    if (bq < Q.nb) atomicAdd(&hw[bs * stride + bq], (HT)(sym ? 2 : 1));
+    if (bq < Q.nb) {
+        if (CNT) atomicAdd(&hw[bs * stride + bq], (HT)(sym ? 2 : 1));
+        if (WT) w2_add(ws, bs * stride + bq, sym ? 2.0f * p.w : p.w);
+    }
 }
 
 // ---------------- marking functions (marking_functions.pyx:21-218) ----------------
@@ -351,7 +391,7 @@ __device__ __forceinline__ double wfunc64(int id, const double *A, const double 
 template <int MODE>
 __device__ __forceinline__ unsigned out_bits(const float4 &u, const float4 &t, float R0, float R1) {
     const float dx = u.x - t.x, dy = u.y - t.y, dz = u.z - t.z;
-    if (MODE == MODE_XYZ) {
+    if (MODE == MODE_XYZ || MODE == MODE_XYZW) {
         const float a = fmaf(-dy, dy, fmaf(-dx, dx, R0));
         const float b = fmaf(-dz, dz, R1);
         return __float_as_uint(a) | __float_as_uint(b);
@@ -367,8 +407,15 @@ __device__ __forceinline__ unsigned out_bits(const float4 &u, const float4 &t, f
 template <int MODE, int WF>
 __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
-    constexpr bool TWO = (MODE == MODE_XYZ || MODE == MODE_SMU);
+    constexpr bool XYZF = (MODE == MODE_XYZ || MODE == MODE_XYZW);  // (rp, pi) geometry
+    constexpr bool SMUF = (MODE == MODE_SMU || MODE == MODE_SMUW);  // (s, mu') geometry
+    constexpr bool TWO = XYZF || SMUF;
+    // weighted 2-D: a marking function's value per pair into the CTA's (hi, lo)
+    // sums; weighted s_mu also counts
+    constexpr bool W2 = (MODE == MODE_XYZW || MODE == MODE_SMUW);
+    constexpr bool CNT2 = (MODE != MODE_XYZW);
     constexpr bool MARK = (MODE == MODE_MARK);
+    constexpr bool MW = MARK || W2;  // per-pair marking function of staged weights
     constexpr bool MARKC = (MODE == MODE_MARKC);  // nw = channels of product marks
     constexpr unsigned FULL = 0xffffffffu;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -376,13 +423,13 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
     const int T0 = a.ax[0].T, T1 = TWO ? a.ax[1].T : 0;
     const int copies = a.hist_copies;  // 2-D / wide: GBP_WARPS (one per warp) or 0 (global)
     constexpr bool JACK = (MODE == MODE_JACK);    // w1 / w2 hold the subsample tags
-    const int nw = (MARK || MARKC || JACK) ? a.nw : 0;
-    const int jwb = MARK ? (WF == 0 ? 8 * nw : 4) : MARKC ? 4 * nw : JACK ? 4 : 0;
+    const int nw = (MW || MARKC || JACK) ? a.nw : 0;
+    const int jwb = MW ? (WF == 0 ? 8 * nw : 4) : MARKC ? 4 * nw : JACK ? 4 : 0;
     const SmemLayout L = gbp_smem_layout(MODE, T0, T1, nb0, nb1, a.nsten, copies, jwb, a.ntag);
     if (gbp_smem_too_small(L.total, a.err)) return;
     unsigned *s_l0 = (unsigned *)(smem + L.off_lut0);
     unsigned *s_l1 = (unsigned *)(smem + L.off_lut1);
-    float *s_qb = MODE == MODE_SMU ? (float *)(smem + L.off_qb) : nullptr;
+    float *s_qb = SMUF ? (float *)(smem + L.off_qb) : nullptr;
     float2 *s_hl0 = (float2 *)(smem + L.off_hl0);
     float2 *s_hl1 = (float2 *)(smem + L.off_hl1);
     // this warp's 32 staged j-points: x, y, z (cell offset added) and sorted index
@@ -412,7 +459,7 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
     // MARKC: this warp's binned pairs of one round {bin | multiplicity << 16, second bin, i, j}
     int4 *s_rec = (int4 *)(smem + L.off_rec) + warp * 32;
     // (s, mu'): this warp's ring of deferred FP64 rechecks and its tail
-    constexpr bool RQM = MODE == MODE_SMU;
+    constexpr bool RQM = SMUF;
     RQ rq{(int4 *)(smem + L.off_rq) + warp * GBP_RQCAP,
           (unsigned *)(smem + L.off_rq + GBP_WARPS * GBP_RQCAP * 16) + warp, 0u};
     double *s_uw64 = (double *)(smem + L.off_q + GBP_WARPS * GBP_USLOTS * 16) +
@@ -452,6 +499,18 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
         (unsigned long long *)(smem + L.off_hist + gbp_align(GBP_WARPS * (nb0 + 1) * 32 * 4, 16));
     if (JACK)
         for (int i = tid; i < a.ntag * (nb0 + 1); i += GBP_BLOCK) s_tab[i] = 0ull;
+    // weighted 2-D: the CTA's (hi, lo) FP32 sums and FP64 totals, after the copies
+    float *s_whi = (float *)(smem + L.off_hist + gbp_align(copies * nbin * 4, 16));
+    float *s_wlo = s_whi + gbp_align(nbin * 4, 16) / 4;
+    double *s_wacc = (double *)(s_wlo + gbp_align(nbin * 4, 16) / 4);
+    const WSink wsink{s_whi, s_wlo};
+    if (W2)
+        for (int i = tid; i < nbin; i += GBP_BLOCK) {
+            s_whi[i] = 0.f;
+            s_wlo[i] = 0.f;
+            s_wacc[i] = 0.0;
+        }
+    unsigned w2_binned = 0;  // pairs this warp binned since it last moved (hi, lo) to FP64
     AxisSm A0{nullptr, s_hi0, s_lo0, s_E0, nb0, a.ax[0].S, a.ax[0].B, a.ax[0].vlo, a.ax[0].vhi,
               s_l0, s_hl0, s_qb};
     AxisSm A1{nullptr, s_hi1, s_lo1, s_E1, nb1, TWO ? a.ax[1].S : 0, TWO ? a.ax[1].B : 0,
@@ -479,12 +538,12 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
         else if (JACK) bin_jack(e, (int)s_uw[e.iu], (int)jw[e.jj], hl, s_tab, A0, ix, a);
         else if (MODE == MODE_3DS) {
             if (copies) bin_3d<false>(e, wh, A0, ix, a); else bin_3d<false>(e, gh, A0, ix, a);
-        } else if (MODE == MODE_XYZ) {
-            if (copies) bin_xyz(e, wh, stride2, A0, A1, ix, a);
-            else bin_xyz(e, gh, stride2, A0, A1, ix, a);
-        } else if (MODE == MODE_SMU) {
-            if (copies) bin_smu(e, wh, stride2, A0, A1, ix, rq, a);
-            else bin_smu(e, gh, stride2, A0, A1, ix, rq, a);
+        } else if (XYZF) {
+            if (copies) bin_xyz<unsigned, CNT2, W2>(e, wh, wsink, stride2, A0, A1, ix, a);
+            else bin_xyz<unsigned long long, CNT2, W2>(e, gh, wsink, stride2, A0, A1, ix, a);
+        } else if (SMUF) {
+            if (copies) bin_smu<unsigned, CNT2, W2>(e, wh, wsink, stride2, A0, A1, ix, rq, a);
+            else bin_smu<unsigned long long, CNT2, W2>(e, gh, wsink, stride2, A0, A1, ix, rq, a);
         } else if (MARK) bin_mark(e, hs, hc, A0, ix, a);
     };
     // Bin the rest of the queue, add this warp's histogram to mock mk and clear it.
@@ -501,8 +560,8 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
             const unsigned n = min(end - rq.head, 32u);
             if ((unsigned)lane < n) {
                 const int4 e = rq.ring[(rq.head + lane) % GBP_RQCAP];
-                if (copies) exact_smu(e, wh, stride2, A0, A1, a);
-                else exact_smu(e, gh, stride2, A0, A1, a);
+                if (copies) exact_smu<unsigned, CNT2, W2>(e, wh, wsink, stride2, A0, A1, a);
+                else exact_smu<unsigned long long, CNT2, W2>(e, gh, wsink, stride2, A0, A1, a);
             }
             if (lane == 0) atomicAdd(a.nrecheck, (unsigned long long)n);
             rq.head += n;
@@ -510,6 +569,16 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
         __syncwarp();
         if (lane == 0 && end != t) *rq.tail = end;
         __syncwarp();
+    };
+    // weighted 2-D: move the CTA's (hi, lo) FP32 sums into its FP64 totals (any
+    // warp may, at any time: exchanging each word keeps every add counted once)
+    auto w2_move = [&]() {
+        for (int b = lane; b < nbin; b += 32) {
+            const float h = atomicExch(&s_whi[b], 0.f);
+            const float l = atomicExch(&s_wlo[b], 0.f);
+            if (h != 0.f || l != 0.f) atomicAdd(&s_wacc[b], (double)h + (double)l);
+        }
+        w2_binned = 0;
     };
     auto warp_flush = [&](int mk) {
         if (RQM) {
@@ -592,7 +661,7 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
             s_uw[lane] = lane < icnt ? a.w1[ifirst + lane] : 0.f;
             s_uw[lane + 48] = lane + 32 < icnt ? a.w1[ifirst + 32 + lane] : 0.f;
         }
-        if (MARK) {
+        if (MW) {
             if (WF == 0) {
                 for (int k = 0; k < nw; k++) {
                     if (lane < icnt) wa[k] = a.w64_1[(int64_t)(ifirst + lane) * nw + k];
@@ -665,7 +734,7 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                     jx[lane] = tx; jy[lane] = ty; jz[lane] = tz; jix[lane] = __float_as_int(p.w);
                     jxy[lane] = make_ulonglong2(pk2(tx, tx), pk2(ty, ty));
                     jzz[lane] = pk2(tz, tz);
-                    if (MARK) {
+                    if (MW) {
                         if (WF == 0) {
                             for (int q = 0; q < nw; q++) jw64[lane * nw + q] = a.w64_2[(int64_t)j * nw + q];
                         } else {
@@ -700,7 +769,7 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                         const unsigned long long dX = f2_sub(UX, txy.x), dY = f2_sub(UY, txy.y),
                                                  dZ = f2_sub(UZ, tzz);
                         unsigned long long d;
-                        if (MODE == MODE_XYZ) {
+                        if (XYZF) {
                             d = f2_sub(RR0, f2_fma(dY, dY, f2_mul(dX, dX))) |
                                 f2_sub(RR1, f2_mul(dZ, dZ));
                         } else {
@@ -735,6 +804,11 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                                                  : (float)wfunc64(a.wfunc, wa, jw64 + jj * nw);
                                 kahan_add(hs, hc, a.self_bin, ws);
                             }
+                            if (W2 && a.self_bin >= 0) {
+                                const float ws = WF == 1 ? w0 * jw[jj] : WF == 2 ? w0 + jw[jj]
+                                                 : (float)wfunc64(a.wfunc, wa, jw64 + jj * nw);
+                                w2_add(wsink, a.self_bin, ws);
+                            }
                         }
                         if (jt == is1) {
                             m1 &= ~(1u << jj);
@@ -742,6 +816,11 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                                 const float ws = WF == 1 ? w1 * jw[jj] : WF == 2 ? w1 + jw[jj]
                                                  : (float)wfunc64(a.wfunc, wb, jw64 + jj * nw);
                                 kahan_add(hs, hc, a.self_bin, ws);
+                            }
+                            if (W2 && a.self_bin >= 0) {
+                                const float ws = WF == 1 ? w1 * jw[jj] : WF == 2 ? w1 + jw[jj]
+                                                 : (float)wfunc64(a.wfunc, wb, jw64 + jj * nw);
+                                w2_add(wsink, a.self_bin, ws);
                             }
                         }
                     }
@@ -784,25 +863,26 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                     auto entry = [&](int code) {
                         const int iu = code & 127, jj = code >> 7;
                         const float dx = ux[iu] - jx[jj], dy = uy[iu] - jy[jj], dz = uz[iu] - jz[jj];
-                        float v0, v1 = 0.f;
-                        if (MODE == MODE_XYZ) {
+                        float v0, v1 = 0.f, wt = 0.f;
+                        if (XYZF) {
                             v0 = fmaf(dy, dy, dx * dx);
                             v1 = dz * dz;
-                        } else if (MODE == MODE_SMU) {
+                        } else if (SMUF) {
                             v1 = fmaf(dy, dy, dx * dx);
                             v0 = fmaf(dz, dz, v1);
                         } else {
                             v0 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
                         }
-                        if (MARK) {
+                        if (MW) {
                             if (WF == 0) {
-                                v1 = (float)wfunc64(a.wfunc, s_uw64 + iu * nw, jw64 + jj * nw);
+                                wt = (float)wfunc64(a.wfunc, s_uw64 + iu * nw, jw64 + jj * nw);
                             } else {
                                 const float wi = s_uw[iu];
-                                v1 = WF == 1 ? wi * jw[jj] : wi + jw[jj];
+                                wt = WF == 1 ? wi * jw[jj] : wi + jw[jj];
                             }
+                            if (MARK) v1 = wt;
                         }
-                        return PairV{v0, v1, iu, jj, ((sym_bits >> jj) & 1u) != 0u};
+                        return PairV{v0, v1, iu, jj, ((sym_bits >> jj) & 1u) != 0u, wt};
                     };
                     if (MARKC) {
                         // each lane bins one pair per round; then lane (g, c) adds channel
@@ -853,6 +933,10 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                             if (hb) bin_entry(eb, cur_mock);
                         }
                         if (RQM) rq_drain(cur_mock, 32u);
+                        if (W2) {
+                            w2_binned += (unsigned)C;
+                            if (w2_binned >= GBP_W2_FLUSH) w2_move();
+                        }
                     }
                     __syncwarp();
                 };
@@ -872,6 +956,14 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
     }
     if (cur_mock >= 0) warp_flush(cur_mock);
     if (lane == 0 && cand) atomicAdd(a.nrecheck + 1, cand);
+    if (W2) {
+        // every warp has left the item loop (one mock per call): the CTA's totals
+        __syncthreads();
+        for (int b = tid; b < nbin; b += GBP_BLOCK) {
+            const double v = s_wacc[b] + (double)s_whi[b] + (double)s_wlo[b];
+            if (v != 0.0) atomicAdd(&a.histd[b], v);
+        }
+    }
     if (JACK) {
         // every warp has left the item loop: add the CTA's table to the global one
         __syncthreads();
@@ -912,6 +1004,12 @@ cudaError_t gbp_launch_count(int mode, int wf, const CountArgs &a, int grid, siz
         return launch_t<MODE_MARKC, 1>(a, grid, smem, st);
     case MODE_JACK:
         return launch_t<MODE_JACK, 1>(a, grid, smem, st);
+    case MODE_SMUW:
+        return launch_t<MODE_SMUW, 1>(a, grid, smem, st);
+    case MODE_XYZW:
+        if (wf == 1) return launch_t<MODE_XYZW, 1>(a, grid, smem, st);
+        if (wf == 2) return launch_t<MODE_XYZW, 2>(a, grid, smem, st);
+        return launch_t<MODE_XYZW, 0>(a, grid, smem, st);
     case MODE_MARK:
         if (wf == 1) return launch_t<MODE_MARK, 1>(a, grid, smem, st);
         if (wf == 2) return launch_t<MODE_MARK, 2>(a, grid, smem, st);
@@ -930,6 +1028,12 @@ int gbp_count_occupancy(int mode, int wf, size_t smem) {
         return occ_t<MODE_MARKC, 1>(smem);
     case MODE_JACK:
         return occ_t<MODE_JACK, 1>(smem);
+    case MODE_SMUW:
+        return occ_t<MODE_SMUW, 1>(smem);
+    case MODE_XYZW:
+        if (wf == 1) return occ_t<MODE_XYZW, 1>(smem);
+        if (wf == 2) return occ_t<MODE_XYZW, 2>(smem);
+        return occ_t<MODE_XYZW, 0>(smem);
     case MODE_MARK:
         if (wf == 1) return occ_t<MODE_MARK, 1>(smem);
         if (wf == 2) return occ_t<MODE_MARK, 2>(smem);

@@ -27,7 +27,19 @@
 enum { MODE_3D = 0, MODE_XYZ = 1, MODE_SMU = 2, MODE_MARK = 3, MODE_ADJ = 4, MODE_3DS = 5,
        MODE_MARKC = 6,    // product marks (id 1) over several channels in one pass
        MODE_JACK = 7,     // jackknife: counts plus a (tag, bin) table of pair ends
-       MODE_POBJ = 8 };   // per-object counts (gather walk of the adjoint)
+       MODE_POBJ = 8,     // per-object counts (gather walk of the adjoint)
+       MODE_XYZW = 9,     // (rp, pi) sums of a marking function (marked_npairs_xy_z)
+       MODE_SMUW = 10 };  // (s, mu') counts and w1 * w2 sums (weighted_npairs_s_mu)
+
+// The weighted 2-D modes add each pair's weight to a per-CTA FP32 pair
+// (hi, lo): hi by atomic add, lo by the exact rounding error of that add
+// (TwoSum on the value the atomic returned).  Warps move (hi, lo) into a per-CTA
+// FP64 sum every GBP_W2_FLUSH binned pairs, and the CTA adds that to the global
+// FP64 histogram once at the end.
+#define GBP_W2_FLUSH 2048
+__host__ __device__ inline int gbp_w2_bytes(int nbin) {
+    return 2 * ((nbin * 4 + 15) / 16 * 16) + nbin * 8;
+}
 
 // One binning axis: squared quantity v compared with edges E'[0..nb-1]
 // (non-decreasing); bin(v) = smallest k with v <= E'[k], nb if none.
@@ -122,7 +134,8 @@ __host__ __device__ inline SmemLayout gbp_smem_layout(int mode, int T0, int T1, 
     const bool adj = mode == MODE_ADJ || mode == MODE_POBJ;  // the gather kernel
     L.off_lut0 = o; o += adj ? T0 * 16 : gbp_align(T0 * 4, 16);
     L.off_lut1 = o; o += adj ? T1 * 16 : gbp_align(T1 * 4, 16);
-    L.off_qb = o; o += (mode == MODE_SMU) ? gbp_align(T0 * 4, 16) : 0;
+    const bool smu = mode == MODE_SMU || mode == MODE_SMUW;
+    L.off_qb = o; o += smu ? gbp_align(T0 * 4, 16) : 0;
     L.off_hl0 = o; o += adj ? 0 : gbp_align((nb0 + 2) * 8, 16);
     L.off_hl1 = o; o += adj ? 0 : gbp_align((nb1 + 2) * 8, 16);
     L.off_j = o; o += GBP_JCAP * 16;   // adjoint: float4 per j; count: x, y, z, index arrays
@@ -135,7 +148,7 @@ __host__ __device__ inline SmemLayout gbp_smem_layout(int mode, int T0, int T1, 
     L.off_code = o;
     o += adj ? 0 : GBP_WARPS * ((mode == MODE_MARK || mode == MODE_MARKC) ? 1024 : 2048) * 2;
     L.off_rec = o; o += (mode == MODE_MARKC) ? GBP_WARPS * 32 * 16 : 0;  // binned pairs of a round
-    L.off_rq = o; o += (mode == MODE_SMU) ? GBP_WARPS * (GBP_RQCAP * 16 + 16) : 0;
+    L.off_rq = o; o += smu ? GBP_WARPS * (GBP_RQCAP * 16 + 16) : 0;
     L.off_D = o; o += nsten * 16;
     L.off_E0 = o; o += gbp_align(nb0 * 8, 16);
     L.off_E1 = o; o += gbp_align(nb1 * 8, 16);
@@ -161,6 +174,8 @@ __host__ __device__ inline SmemLayout gbp_smem_layout(int mode, int T0, int T1, 
         hist_bytes = copies * (nb0 + 1) * 4;                  // shared u32 copies (wide 1-D)
     } else {
         hist_bytes = copies * (nb0 + 1) * (nb1 + 1) * 4;      // shared u32 copies (2-D)
+        if (mode == MODE_XYZW || mode == MODE_SMUW)           // then the CTA's weighted sums
+            hist_bytes = gbp_align(hist_bytes, 16) + gbp_w2_bytes((nb0 + 1) * (nb1 + 1));
     }
     o += gbp_align(hist_bytes, 16);
     L.total = o;

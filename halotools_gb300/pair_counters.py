@@ -7,6 +7,8 @@ reference front-ends:
 * ``npairs_xy_z``      npairs_xy_z.py:20-237
 * ``npairs_s_mu``      npairs_s_mu.py:20-209
 * ``marked_npairs_3d`` marked_npairs_3d.py:25-326
+* ``marked_npairs_xy_z`` marked_npairs_xy_z.py:23-333
+* ``weighted_npairs_s_mu`` weighted_npairs_s_mu.py:22-230
 
 ``num_threads`` is validated as the reference does and then ignored (the GPU
 is the parallel engine).  ``approx_cell1_size`` / ``approx_cell2_size`` are
@@ -267,17 +269,23 @@ _NUM_WEIGHTS = {1: 1, 2: 1, 3: 2, 4: 2, 5: 2, 6: 2, 7: 2, 8: 2, 9: 2, 10: 2, 11:
                 12: 4, 13: 4, 14: 3, 15: 3, 16: 5, 17: 5}
 
 
-def _func_signature_int_from_wfunc(weight_func_id):
+def _func_signature_int_from_wfunc(weight_func_id, known=None):
+    known = _NUM_WEIGHTS if known is None else known
     if type(weight_func_id) != int:
         raise ValueError("\n weight_func_id parameter must be an integer ID of a weighting function.")
-    if weight_func_id not in _NUM_WEIGHTS:
+    if weight_func_id not in known:
         raise HalotoolsError("The value ``weight_func_id`` = %i is not recognized" % weight_func_id)
-    return _NUM_WEIGHTS[weight_func_id]
+    return known[weight_func_id]
 
 
-def _process_weights(sample1, sample2, weights1, weights2, weight_func_id):
-    """marked_npairs_3d.py:186-276: shape checks and float64 (N, n_w) arrays."""
-    nw = _func_signature_int_from_wfunc(weight_func_id)
+# marked_npairs_xy_z.py:292-333 knows ids 1-15 only
+_NUM_WEIGHTS_XY_Z = {k: v for k, v in _NUM_WEIGHTS.items() if k <= 15}
+
+
+def _process_weights(sample1, sample2, weights1, weights2, weight_func_id, known=None):
+    """marked_npairs_3d.py:186-276 (and the same checks in marked_npairs_xy_z.py:
+    192-289): shape checks and float64 (N, n_w) arrays."""
+    nw = _func_signature_int_from_wfunc(weight_func_id, known)
     out = []
     for which, sample, w in ((1, sample1, weights1), (2, sample2, weights2)):
         npts = np.shape(sample)[0]
@@ -343,6 +351,96 @@ def marked_npairs_3d(sample1, sample2, rbins, weight_func_id, period=None, weigh
                                              _native.pd(rbins), len(rbins), _native.pd(box), pbc,
                                              GBP_MEM_HOST, _native.pd(out)))
     return out
+
+
+def marked_npairs_xy_z(sample1, sample2, rp_bins, pi_bins, period=None, weights1=None,
+                       weights2=None, weight_func_id=0, num_threads=1, approx_cell1_size=None,
+                       approx_cell2_size=None):
+    """Cumulative (r_p, pi) sums of a marking function, float64, shape
+    ``(len(rp_bins), len(pi_bins))``.
+
+    Same inputs and output as halotools ``marked_npairs_xy_z``
+    (marked_npairs_xy_z.py:23); ``weight_func_id`` 1-15 as there.  Each pair's
+    weight is added in FP32 with an exact-error companion (moved to FP64 every
+    few thousand pairs): within 1e-6 relative of the FP64 reference, exact for
+    integer-valued weights.
+    """
+    _check_num_threads(num_threads)
+    rp_bins = _bins(rp_bins, "Input ``rp_bins`` must be a monotonically increasing 1D array "
+                             "with at least two entries")
+    pi_bins = _bins(pi_bins, "Input ``pi_bins`` must be a monotonically increasing 1D array "
+                             "with at least two entries")
+    rpm, pim = np.max(rp_bins), np.max(pi_bins)
+    _approx_cells(approx_cell1_size, [rpm, rpm, pim], "approx_cell1_size")
+    _approx_cells(approx_cell2_size, [rpm, rpm, pim], "approx_cell2_size")
+    x1, x2, box, pbc = _positions(sample1, sample2, period, [rpm, rpm, pim],
+                                  [rpm * 3.0, rpm * 3.0, pim * 3.0])
+    w1, w2, nw = _process_weights(sample1, sample2, weights1, weights2, weight_func_id,
+                                  _NUM_WEIGHTS_XY_Z)
+    _nonneg(rp_bins, "rp_bins")
+    _nonneg(pi_bins, "pi_bins")
+    if x2 is x1 and not (weights2 is weights1 or np.array_equal(w1, w2)):
+        x2 = x1.copy()  # same points, different marks: count as a cross-correlation
+    if x2 is x1:
+        w2 = w1
+    plan = _native.default_plan()
+    out = np.zeros((len(rp_bins), len(pi_bins)), dtype=np.float64)
+    plan.check(plan.lib.gbp_marked_npairs_xy_z(plan.handle, _native.dptr(x1), len(x1),
+                                               _native.dptr(x2), len(x2), _native.dptr(w1),
+                                               _native.dptr(w2), nw, int(weight_func_id),
+                                               _native.pd(rp_bins), len(rp_bins),
+                                               _native.pd(pi_bins), len(pi_bins),
+                                               _native.pd(box), pbc, GBP_MEM_HOST,
+                                               _native.pd(out)))
+    return out
+
+
+def weighted_npairs_s_mu(sample1, sample2, weights1, weights2, s_bins, mu_bins, period=None,
+                         num_threads=1, approx_cell1_size=None, approx_cell2_size=None):
+    """Cumulative (s, mu) pair counts and w1 * w2 sums: ``(counts, weighted_counts)``,
+    int64 and float64, each of shape ``(len(s_bins), len(mu_bins))``.
+
+    Same inputs and outputs as halotools ``weighted_npairs_s_mu``
+    (weighted_npairs_s_mu.py:22); the second axis runs over
+    ``sort(sin(arccos(mu_bins)))`` (weighted_npairs_s_mu.py:192-193).  Counts are
+    exact; sums within 1e-6 relative of the FP64 reference.
+    """
+    _check_num_threads(num_threads)
+    s_bins = _bins(s_bins, "Input ``rbins`` must be a monotonically increasing 1D array with at "
+                           "least two entries")
+    smax = np.max(s_bins)
+    _approx_cells(approx_cell1_size, [smax] * 3, "approx_cell1_size")
+    _approx_cells(approx_cell2_size, [smax] * 3, "approx_cell2_size")
+    x1, x2, box, pbc = _positions(sample1, sample2, period, [smax] * 3, [smax * 3.0] * 3)
+    # weighted_npairs_s_mu.py:171-176
+    w1 = np.atleast_1d(weights1)
+    w2 = np.atleast_1d(weights2)
+    assert w1.shape == (len(x1),), "``weights1`` should have shape ({0}, )".format(len(x1))
+    assert w2.shape == (len(x2),), "``weights2`` should have shape ({0}, )".format(len(x2))
+    mu_bins = np.atleast_1d(mu_bins)
+    if not (mu_bins.ndim == 1 and len(mu_bins) > 1 and
+            (len(mu_bins) <= 2 or _is_strictly_increasing(mu_bins))):
+        raise ValueError("\n Input `mu_bins` must be a monotonically increasing \n"
+                         "1D array with at least two entries")
+    _nonneg(s_bins, "s_bins")
+    w1 = np.ascontiguousarray(w1, dtype=np.float64)
+    w2 = np.ascontiguousarray(w2, dtype=np.float64)
+    if x2 is x1 and not (weights2 is weights1 or np.array_equal(w1, w2)):
+        x2 = x1.copy()  # same points, different weights: count as a cross-correlation
+    if x2 is x1:
+        w2 = w1
+    mu_prime = np.ascontiguousarray(np.sort(np.sin(np.arccos(mu_bins))), dtype=np.float64)
+    plan = _native.default_plan()
+    counts = np.zeros((len(s_bins), len(mu_prime)), dtype=np.int64)
+    wcounts = np.zeros((len(s_bins), len(mu_prime)), dtype=np.float64)
+    plan.check(plan.lib.gbp_weighted_npairs_s_mu(plan.handle, _native.dptr(x1), len(x1),
+                                                 _native.dptr(x2), len(x2), _native.dptr(w1),
+                                                 _native.dptr(w2), _native.pd(s_bins),
+                                                 len(s_bins), _native.pd(mu_prime),
+                                                 len(mu_prime), _native.pd(box), pbc,
+                                                 GBP_MEM_HOST, _native.pi64(counts),
+                                                 _native.pd(wcounts)))
+    return counts, wcounts
 
 
 def marked_npairs_3d_channels(sample1, sample2, rbins, period=None, weights1=None,

@@ -135,6 +135,34 @@ int gbp_marked_npairs_3d(gbp_plan *plan, const double *xyz1, int64_t n1, const d
                          const double *period3, int32_t pbc, int32_t mem, double *out);
 
 /*
+ * Cumulative (r_p, pi) sums of marking function `wfunc_id` (1..17), row-major
+ * [n_rp][n_pi]: out[k][g] adds wfunc(w1_i, w2_j) over ordered pairs with
+ * dxy^2 <= rp_bins[k]^2 and dz^2 <= pi_bins[g]^2.  Weights (N, nw) row-major
+ * FP64; nw as for gbp_marked_npairs_3d.  Replaces marked_npairs_xy_z_engine
+ * (marked_cpairs/marked_npairs_xy_z_engine.pyx:23-229, pair loop :209-224) and
+ * marked_npairs_xy_z (marked_npairs_xy_z.py:160-189).  Sums are FP32 with an
+ * exact-error companion, moved to FP64 every few thousand pairs.
+ */
+int gbp_marked_npairs_xy_z(gbp_plan *plan, const double *xyz1, int64_t n1, const double *xyz2,
+                           int64_t n2, const double *w1, const double *w2, int32_t nw,
+                           int32_t wfunc_id, const double *rp_bins, int32_t n_rp,
+                           const double *pi_bins, int32_t n_pi, const double *period3,
+                           int32_t pbc, int32_t mem, double *out);
+
+/*
+ * Cumulative (s, mu') counts and w1 * w2 sums, both row-major [n_s][n_mu], with
+ * mu_prime = sort(sin(arccos(mu_bins))) (weighted_npairs_s_mu.py:192-193) and
+ * one FP64 weight per point.  Replaces weighted_npairs_s_mu_engine
+ * (cpairs/weighted_npairs_s_mu_engine.pyx:15-256) and weighted_npairs_s_mu
+ * (weighted_npairs_s_mu.py:175-230).
+ */
+int gbp_weighted_npairs_s_mu(gbp_plan *plan, const double *xyz1, int64_t n1, const double *xyz2,
+                             int64_t n2, const double *w1, const double *w2,
+                             const double *s_bins, int32_t n_s, const double *mu_prime,
+                             int32_t n_mu, const double *period3, int32_t pbc, int32_t mem,
+                             int64_t *counts, double *wcounts);
+
+/*
  * Product-mark counts over nch channels in one pass (no single reference
  * counterpart): out[c][k] equals marked_npairs_3d(xyz1, xyz2, rbins, 1,
  * weights1=w1[:, c], weights2=w2[:, c]) (marked_npairs_3d.py:25,

@@ -36,9 +36,12 @@ ENGINES = [
     (os.path.join(PC, "cpairs"), "npairs_projected_engine"),
     (os.path.join(PC, "cpairs"), "npairs_jackknife_3d_engine"),
     (os.path.join(PC, "cpairs"), "npairs_per_object_3d_engine"),
+    (os.path.join(PC, "cpairs"), "weighted_npairs_s_mu_engine"),
+    (os.path.join(PC, "cpairs"), "npairs_jackknife_xy_z_engine"),
     (os.path.join(PC, "marked_cpairs"), "marking_functions"),
     (os.path.join(PC, "marked_cpairs"), "custom_marking_func"),
     (os.path.join(PC, "marked_cpairs"), "marked_npairs_3d_engine"),
+    (os.path.join(PC, "marked_cpairs"), "marked_npairs_xy_z_engine"),
 ]
 
 

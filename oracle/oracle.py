@@ -44,6 +44,10 @@ def lib():
         L.orc_npairs_xy_z.argtypes = [pd, i64, pd, i64, pd, i, pd, i, pd, i, pd, pd, i, pi64]
         L.orc_npairs_s_mu.argtypes = [pd, i64, pd, i64, pd, i, pd, i, pd, i, pd, pd, i, pi64]
         L.orc_marked_npairs_3d.argtypes = [pd, i64, pd, i64, pd, pd, i, i, pd, i, pd, i, pd, pd, i, pd]
+        L.orc_marked_npairs_xy_z.argtypes = [pd, i64, pd, i64, pd, pd, i, i, pd, i, pd, i, pd,
+                                             i, pd, pd, i, pd]
+        L.orc_weighted_npairs_s_mu.argtypes = [pd, i64, pd, i64, pd, pd, pd, i, pd, i, pd, i,
+                                               pd, pd, i, pi64, pd]
         L.orc_bf_npairs_3d.argtypes = [pd, i64, pd, i64, pd, i, pd, i, pi64]
         L.orc_weighted_adjoint_3d.argtypes = [pd, i64, pd, pd, i, pd, i, pd, i, pd]
         _lib = L
@@ -166,6 +170,51 @@ def marked_npairs_3d(sample1, sample2, rbins, weight_func_id, period=None, weigh
                                       int(weight_func_id), _p(rbins), len(rbins), _p(lbox), pbc,
                                       _p(a1), _p(a2), int(num_threads), _p(out)))
     return out
+
+
+def marked_npairs_xy_z(sample1, sample2, rp_bins, pi_bins, weight_func_id, period=None,
+                       weights1=None, weights2=None, num_threads=1, approx_cell1_size=None,
+                       approx_cell2_size=None):
+    """marked_npairs_xy_z.py:160-189 driving marked_npairs_xy_z_engine.pyx:209-224."""
+    rp = np.ascontiguousarray(np.atleast_1d(rp_bins), dtype=np.float64)
+    pi = np.ascontiguousarray(np.atleast_1d(pi_bins), dtype=np.float64)
+    rpm, pim = np.max(rp), np.max(pi)
+    nw = NUM_WEIGHTS[weight_func_id]
+    n1, n2 = len(sample1), len(sample2)
+    w1 = np.ones((n1, nw)) if weights1 is None else np.asarray(weights1, dtype=np.float64).reshape(n1, nw)
+    w2 = np.ones((n2, nw)) if weights2 is None else np.asarray(weights2, dtype=np.float64).reshape(n2, nw)
+    w1 = np.ascontiguousarray(w1)
+    w2 = np.ascontiguousarray(w2)
+    x1, x2, lbox, pbc = _geometry(sample1, sample2, [rpm, rpm, pim], period)
+    a1 = _approx(approx_cell1_size, [rpm, rpm, pim])
+    a2 = _approx(approx_cell2_size, [rpm, rpm, pim])
+    out = np.zeros((len(rp), len(pi)), dtype=np.float64)
+    _check(lib().orc_marked_npairs_xy_z(_p(x1), n1, _p(x2), n2, _p(w1), _p(w2), nw,
+                                        int(weight_func_id), _p(rp), len(rp), _p(pi), len(pi),
+                                        _p(lbox), pbc, _p(a1), _p(a2), int(num_threads), _p(out)))
+    return out
+
+
+def weighted_npairs_s_mu(sample1, sample2, weights1, weights2, s_bins, mu_bins, period=None,
+                         num_threads=1, approx_cell1_size=None, approx_cell2_size=None):
+    """weighted_npairs_s_mu.py:175-230 driving weighted_npairs_s_mu_engine.pyx:186-255:
+    returns (counts, weighted counts), both cumulative in s and mu'."""
+    s = np.ascontiguousarray(np.atleast_1d(s_bins), dtype=np.float64)
+    smax = np.max(s)
+    mu_prime = np.ascontiguousarray(np.sort(np.sin(np.arccos(np.atleast_1d(mu_bins)))),
+                                    dtype=np.float64)
+    n1, n2 = len(sample1), len(sample2)
+    w1 = np.ascontiguousarray(np.asarray(weights1, dtype=np.float64).reshape(n1))
+    w2 = np.ascontiguousarray(np.asarray(weights2, dtype=np.float64).reshape(n2))
+    x1, x2, lbox, pbc = _geometry(sample1, sample2, [smax] * 3, period)
+    a1 = _approx(approx_cell1_size, [smax] * 3)
+    a2 = _approx(approx_cell2_size, [smax] * 3)
+    out = np.zeros((len(s), len(mu_prime)), dtype=np.int64)
+    wout = np.zeros((len(s), len(mu_prime)), dtype=np.float64)
+    _check(lib().orc_weighted_npairs_s_mu(_p(x1), n1, _p(x2), n2, _p(w1), _p(w2), _p(s), len(s),
+                                          _p(mu_prime), len(mu_prime), _p(lbox), pbc, _p(a1),
+                                          _p(a2), int(num_threads), _pi(out), _p(wout)))
+    return out, wout
 
 
 def brute_force_npairs_3d(sample1, sample2, rbins, period=None):

@@ -128,7 +128,7 @@ static void mesh_free(mesh_t *m) {
     free(m->order);
 }
 
-enum { K_3D = 0, K_XYZ = 1, K_SMU = 2, K_MARKED = 3 };
+enum { K_3D = 0, K_XYZ = 1, K_SMU = 2, K_MARKED = 3, K_XYZ_MARKED = 4, K_SMU_WEIGHTED = 5 };
 
 typedef struct {
     int kind;
@@ -200,7 +200,8 @@ static void walk_range(const walk_t *w, int64_t c0, int64_t c1, int64_t *ic, dou
     const int n1y = m1->n[1], n1z = m1->n[2];
     const int n2x = m2->n[0], n2y = m2->n[1], n2z = m2->n[2];
     int64_t *diff = NULL;
-    if (w->kind == K_SMU) diff = ic; /* differential counts, summed by the caller */
+    /* differential counts (and weighted sums), summed by the caller */
+    if (w->kind == K_SMU || w->kind == K_SMU_WEIGHTED) diff = ic;
     for (int64_t icell1 = c0; icell1 < c1; icell1++) {
         int64_t if1 = m1->start[icell1], il1 = m1->start[icell1 + 1];
         int64_t Ni = il1 - if1;
@@ -260,7 +261,23 @@ static void walk_range(const walk_t *w, int64_t c0, int64_t c1, int64_t *ic, dou
                                     k--;
                                     if (k < 0) break;
                                 }
-                            } else { /* K_SMU */
+                            } else if (w->kind == K_XYZ_MARKED) {
+                                /* marked_npairs_xy_z_engine.pyx:209-224 (weight at :217, added at :222) */
+                                double dxy = dx * dx + dy * dy;
+                                double dzz = dz * dz;
+                                double wt = wfunc_eval(w->wfunc, w->w1 + i * w->nw, w->w2 + j * w->nw);
+                                int k = w->n1e - 1;
+                                while (dxy <= w->e1[k]) {
+                                    int g = w->n2e - 1;
+                                    while (dzz <= w->e2[g]) {
+                                        dc[(int64_t)k * w->n2e + g] += wt;
+                                        g--;
+                                        if (g < 0) break;
+                                    }
+                                    k--;
+                                    if (k < 0) break;
+                                }
+                            } else { /* K_SMU, K_SMU_WEIGHTED */
                                 double dxy = dx * dx + dy * dy;
                                 double dzz = dz * dz;
                                 double s2 = dzz + dxy;
@@ -278,6 +295,9 @@ static void walk_range(const walk_t *w, int64_t c0, int64_t c1, int64_t *ic, dou
                                     g--;
                                 }
                                 diff[(int64_t)(k + 1) * w->n2e + (g + 1)] += 1;
+                                /* weighted_npairs_s_mu_engine.pyx:249: w1 * w2 per pair */
+                                if (w->kind == K_SMU_WEIGHTED)
+                                    dc[(int64_t)(k + 1) * w->n2e + (g + 1)] += w->w1[i] * w->w2[j];
                             }
                         }
                     }
@@ -337,7 +357,7 @@ static int run_walk(int kind, const double *xyz1, int64_t n1, const double *xyz2
         w.x2[k] = xyz2[3 * i]; w.y2[k] = xyz2[3 * i + 1]; w.z2[k] = xyz2[3 * i + 2];
     }
     double *wb = NULL;
-    if (kind == K_MARKED) {
+    if (kind == K_MARKED || kind == K_XYZ_MARKED || kind == K_SMU_WEIGHTED) {
         wb = (double *)malloc(sizeof(double) * (size_t)nw * (s1 + s2));
         if (!wb) { free(buf); mesh_free(&w.m1); mesh_free(&w.m2); return -1; }
         w.w1 = wb; w.w2 = wb + (size_t)nw * s1;
@@ -352,6 +372,7 @@ static int run_walk(int kind, const double *xyz1, int64_t n1, const double *xyz2
     w.smax2 = smax2; w.mumax2 = mumax2;
 
     int64_t nout = (kind == K_3D || kind == K_MARKED) ? n1e : (int64_t)n1e * n2e;
+    double *dsum = NULL;
     if (nthreads < 1) nthreads = 1;
     if (nthreads > w.m1.ncells) nthreads = (int)w.m1.ncells;
     job_t *jobs = (job_t *)calloc((size_t)nthreads, sizeof(job_t));
@@ -394,7 +415,21 @@ static int run_walk(int kind, const double *xyz1, int64_t n1, const double *xyz2
         if (icounts) icounts[k] = si;
         if (dcounts) dcounts[k] = sd;
     }
-    if (kind == K_SMU && icounts) {
+    if (kind == K_SMU_WEIGHTED && dcounts) {
+        /* weighted_npairs_s_mu_engine.pyx:251-255: each cell sums its rectangle of the
+           differential weighted counts */
+        dsum = (double *)calloc((size_t)nout, sizeof(double));
+        if (!dsum) { rc = -1; goto done; }
+        for (int k = 0; k < n1e; k++)
+            for (int g = 0; g < n2e; g++) {
+                double v = 0.0;
+                for (int a = 0; a <= k; a++)
+                    for (int b = 0; b <= g; b++) v += dcounts[(int64_t)a * n2e + b];
+                dsum[(int64_t)k * n2e + g] = v;
+            }
+        memcpy(dcounts, dsum, sizeof(double) * (size_t)nout);
+    }
+    if ((kind == K_SMU || kind == K_SMU_WEIGHTED) && icounts) {
         /* npairs_s_mu_engine.pyx:232-234: 2-D cumulative sum of the differential counts */
         for (int k = 0; k < n1e; k++)
             for (int g = 0; g < n2e; g++) {
@@ -406,7 +441,7 @@ static int run_walk(int kind, const double *xyz1, int64_t n1, const double *xyz2
             }
     }
 done:
-    free(jobs); free(th); free(ipart); free(dpart);
+    free(jobs); free(th); free(ipart); free(dpart); free(dsum);
     free(wb); free(buf);
     mesh_free(&w.m1); mesh_free(&w.m2);
     return rc;
@@ -481,6 +516,49 @@ int orc_marked_npairs_3d(const double *xyz1, int64_t n1, const double *xyz2, int
     int rc = run_walk(K_MARKED, xyz1, n1, xyz2, n2, w1, w2, nw, wfunc, e, nb, NULL, 0, 0, 0,
                       period, pbc, search, approx1, approx2, nthreads, NULL, out);
     free(e);
+    return rc;
+}
+
+/* marked_npairs_xy_z_engine: out[k][g] = sum of wfunc over ordered pairs with
+   dxy <= rp[k]^2 and dz^2 <= pi[g]^2 (both walked from the top) */
+int orc_marked_npairs_xy_z(const double *xyz1, int64_t n1, const double *xyz2, int64_t n2,
+                           const double *w1, const double *w2, int nw, int wfunc,
+                           const double *rp_bins, int nrp, const double *pi_bins, int npi,
+                           const double period[3], int pbc, const double approx1[3],
+                           const double approx2[3], int nthreads, double *out) {
+    double *e1 = (double *)malloc(sizeof(double) * (size_t)(nrp + npi));
+    if (!e1) return -1;
+    double *e2 = e1 + nrp;
+    double rpmax = rp_bins[0], pimax = pi_bins[0];
+    for (int k = 0; k < nrp; k++) { e1[k] = rp_bins[k] * rp_bins[k]; if (rp_bins[k] > rpmax) rpmax = rp_bins[k]; }
+    for (int k = 0; k < npi; k++) { e2[k] = pi_bins[k] * pi_bins[k]; if (pi_bins[k] > pimax) pimax = pi_bins[k]; }
+    double search[3] = {rpmax, rpmax, pimax};
+    int rc = run_walk(K_XYZ_MARKED, xyz1, n1, xyz2, n2, w1, w2, nw, wfunc, e1, nrp, e2, npi, 0, 0,
+                      period, pbc, search, approx1, approx2, nthreads, NULL, out);
+    free(e1);
+    return rc;
+}
+
+/* weighted_npairs_s_mu_engine: cumulative (s, mu') counts and w1 * w2 sums; mu_prime
+   = sort(sin(arccos(mu_bins))) from the caller (weighted_npairs_s_mu.py:192-193) */
+int orc_weighted_npairs_s_mu(const double *xyz1, int64_t n1, const double *xyz2, int64_t n2,
+                             const double *w1, const double *w2, const double *s_bins, int ns,
+                             const double *mu_prime, int nmu, const double period[3], int pbc,
+                             const double approx1[3], const double approx2[3], int nthreads,
+                             int64_t *counts, double *wcounts) {
+    double *e1 = (double *)malloc(sizeof(double) * (size_t)(ns + nmu));
+    if (!e1) return -1;
+    double *e2 = e1 + ns;
+    double smax = s_bins[0];
+    for (int k = 0; k < ns; k++) { e1[k] = s_bins[k] * s_bins[k]; if (s_bins[k] > smax) smax = s_bins[k]; }
+    for (int k = 0; k < nmu; k++) e2[k] = mu_prime[k] * mu_prime[k];
+    double smax2 = e1[0], mumax2 = e2[0];
+    for (int k = 0; k < ns; k++) { if (isnan(e1[k]) || isnan(smax2)) smax2 = NAN; else if (e1[k] > smax2) smax2 = e1[k]; }
+    for (int k = 0; k < nmu; k++) { if (isnan(e2[k]) || isnan(mumax2)) mumax2 = NAN; else if (e2[k] > mumax2) mumax2 = e2[k]; }
+    double search[3] = {smax, smax, smax};
+    int rc = run_walk(K_SMU_WEIGHTED, xyz1, n1, xyz2, n2, w1, w2, 1, 0, e1, ns, e2, nmu, smax2,
+                      mumax2, period, pbc, search, approx1, approx2, nthreads, counts, wcounts);
+    free(e1);
     return rc;
 }
 

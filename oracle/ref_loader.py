@@ -83,11 +83,14 @@ def load(src_root: str = DEFAULT_SRC):
         "halotools.utils.array_utils").unsorting_indices
     for name in ("npairs_3d_engine", "npairs_xy_z_engine", "npairs_s_mu_engine",
                  "npairs_projected_engine", "npairs_jackknife_3d_engine",
-                 "npairs_per_object_3d_engine"):
+                 "npairs_per_object_3d_engine", "weighted_npairs_s_mu_engine",
+                 "npairs_jackknife_xy_z_engine"):
         m = importlib.import_module(base + ".cpairs." + name)
         setattr(cp, name, getattr(m, name))
     m = importlib.import_module(base + ".marked_cpairs.marked_npairs_3d_engine")
     mcp.marked_npairs_3d_engine = m.marked_npairs_3d_engine
+    m = importlib.import_module(base + ".marked_cpairs.marked_npairs_xy_z_engine")
+    mcp.marked_npairs_xy_z_engine = m.marked_npairs_xy_z_engine
     return _namespace()
 
 
@@ -103,6 +106,12 @@ def _namespace():
         base + ".npairs_jackknife_3d").npairs_jackknife_3d
     ns.npairs_per_object_3d = importlib.import_module(
         base + ".npairs_per_object_3d").npairs_per_object_3d
+    ns.weighted_npairs_s_mu = importlib.import_module(
+        base + ".weighted_npairs_s_mu").weighted_npairs_s_mu
+    ns.marked_npairs_xy_z = importlib.import_module(
+        base + ".marked_npairs_xy_z").marked_npairs_xy_z
+    ns.npairs_jackknife_xy_z = importlib.import_module(
+        base + ".npairs_jackknife_xy_z").npairs_jackknife_xy_z
     ns.pairs = importlib.import_module(base + ".pairs")
     ns.HalotoolsError = importlib.import_module("halotools.custom_exceptions").HalotoolsError
     return ns

@@ -1,6 +1,7 @@
 """Golden vectors for the sibling counters (npairs_projected, npairs_jackknife_3d,
-npairs_per_object_3d), made by running halotools' own front-ends and Cython
-engines (built by ``oracle/build_ref.py``, imported by ``oracle/ref_loader.py``).
+npairs_per_object_3d, marked_npairs_xy_z, weighted_npairs_s_mu), made by running
+halotools' own front-ends and Cython engines (built by ``oracle/build_ref.py``,
+imported by ``oracle/ref_loader.py``).
 
 Inputs are regenerated from their seeds by ``sibling_inputs`` (shared with the
 tests); each ``.npz`` stores the output and a SHA-256 of the inputs.
@@ -40,34 +41,83 @@ def sibling_inputs(seed=11):
     return s1, s2, t1, t2
 
 
+def sibling_weights(seed=12):
+    """One float mark per point (lognormal for sample1, uniform for sample2) and a
+    two-column mark (uniform in [0, 3) and [0, 1)) for the two-weight functions."""
+    s1, s2, _, _ = sibling_inputs()
+    rng = np.random.default_rng(seed)
+    w1 = rng.lognormal(0.0, 0.5, len(s1))
+    w2 = rng.uniform(0.0, 1.0, len(s2))
+    W1 = np.stack([rng.uniform(0, 3, len(s1)), rng.uniform(0, 1, len(s1))], axis=1)
+    W2 = np.stack([rng.uniform(0, 3, len(s2)), rng.uniform(0, 1, len(s2))], axis=1)
+    return w1, w2, W1, W2
+
+
 def input_sha():
     h = hashlib.sha256()
-    for a in sibling_inputs():
+    for a in sibling_inputs() + sibling_weights():
         h.update(np.ascontiguousarray(a).tobytes())
     return h.hexdigest()
 
 
+RP = np.logspace(-0.7, 1.1, 10)
+PI = np.linspace(0.0, 12.0, 7)
+SB = np.logspace(-0.5, 1.1, 9)
+MU = np.linspace(0.0, 1.0, 11)
+
+
+def _wt():
+    return sibling_weights()
+
+
+# name -> (front-end, call); calls take the module (halotools' or this package's)
 CASES = {
-    "projected_auto_pbc": lambda m, s1, s2, t1, t2: m.npairs_projected(s1, s1, RBINS, 8.0,
-                                                                        period=L),
-    "projected_cross_nopbc": lambda m, s1, s2, t1, t2: m.npairs_projected(s1, s2, RBINS, 6.5),
-    "jackknife_auto_pbc": lambda m, s1, s2, t1, t2: m.npairs_jackknife_3d(
-        s1, s1, RBINS, t1, t1, 5, period=L),
-    "jackknife_cross_pbc": lambda m, s1, s2, t1, t2: m.npairs_jackknife_3d(
-        s1, s2, RBINS, t1, t2, 5, period=L),
-    "jackknife_auto_nopbc": lambda m, s1, s2, t1, t2: m.npairs_jackknife_3d(
-        s1, s1, RBINS, t1, t1, 5),
-    "per_object_cross_pbc": lambda m, s1, s2, t1, t2: m.npairs_per_object_3d(
-        s1[:700], s2, RBINS, period=L),
-    "per_object_auto_pbc": lambda m, s1, s2, t1, t2: m.npairs_per_object_3d(
-        s1, s1, RBINS, period=L),
-    "per_object_cross_nopbc": lambda m, s1, s2, t1, t2: m.npairs_per_object_3d(
-        s2[:500], s1, RBINS),
+    "projected_auto_pbc": ("npairs_projected", lambda m, s1, s2, t1, t2: m.npairs_projected(
+        s1, s1, RBINS, 8.0, period=L)),
+    "projected_cross_nopbc": ("npairs_projected", lambda m, s1, s2, t1, t2: m.npairs_projected(
+        s1, s2, RBINS, 6.5)),
+    "jackknife_auto_pbc": ("npairs_jackknife_3d", lambda m, s1, s2, t1, t2: m.npairs_jackknife_3d(
+        s1, s1, RBINS, t1, t1, 5, period=L)),
+    "jackknife_cross_pbc": ("npairs_jackknife_3d", lambda m, s1, s2, t1, t2: m.npairs_jackknife_3d(
+        s1, s2, RBINS, t1, t2, 5, period=L)),
+    "jackknife_auto_nopbc": ("npairs_jackknife_3d", lambda m, s1, s2, t1, t2: m.npairs_jackknife_3d(
+        s1, s1, RBINS, t1, t1, 5)),
+    "per_object_cross_pbc": ("npairs_per_object_3d", lambda m, s1, s2, t1, t2: m.npairs_per_object_3d(
+        s1[:700], s2, RBINS, period=L)),
+    "per_object_auto_pbc": ("npairs_per_object_3d", lambda m, s1, s2, t1, t2: m.npairs_per_object_3d(
+        s1, s1, RBINS, period=L)),
+    "per_object_cross_nopbc": ("npairs_per_object_3d", lambda m, s1, s2, t1, t2: m.npairs_per_object_3d(
+        s2[:500], s1, RBINS)),
+    "marked_xy_z_id1_auto_pbc": ("marked_npairs_xy_z", lambda m, s1, s2, t1, t2: m.marked_npairs_xy_z(
+        s1, s1, RP, PI, weights1=_wt()[0], weights2=_wt()[0], weight_func_id=1, period=L)),
+    "marked_xy_z_id5_cross_nopbc": ("marked_npairs_xy_z", lambda m, s1, s2, t1, t2: m.marked_npairs_xy_z(
+        s1, s2, RP, PI, weights1=_wt()[2], weights2=_wt()[3], weight_func_id=5)),
+    "marked_xy_z_id9_auto_pbc": ("marked_npairs_xy_z", lambda m, s1, s2, t1, t2: m.marked_npairs_xy_z(
+        s1, s1, RP, PI, weights1=_wt()[2], weights2=_wt()[2], weight_func_id=9, period=L)),
+    "marked_xy_z_id2_cross_pbc": ("marked_npairs_xy_z", lambda m, s1, s2, t1, t2: m.marked_npairs_xy_z(
+        s1, s2, RP, PI, weights1=_wt()[0], weights2=_wt()[1], weight_func_id=2, period=L)),
+    "marked_xy_z_threes_auto_pbc": ("marked_npairs_xy_z", lambda m, s1, s2, t1, t2: m.marked_npairs_xy_z(
+        s1, s1, RP, PI, weights1=np.full(len(s1), 3.0), weights2=np.full(len(s1), 3.0),
+        weight_func_id=1, period=L)),
+    "weighted_s_mu_auto_pbc": ("weighted_npairs_s_mu", lambda m, s1, s2, t1, t2: m.weighted_npairs_s_mu(
+        s1, s1, _wt()[0], _wt()[0], SB, MU, period=L)),
+    "weighted_s_mu_cross_nopbc": ("weighted_npairs_s_mu", lambda m, s1, s2, t1, t2: m.weighted_npairs_s_mu(
+        s1, s2, _wt()[0], _wt()[1], SB, MU)),
+    "weighted_s_mu_ones_cross_pbc": ("weighted_npairs_s_mu", lambda m, s1, s2, t1, t2: m.weighted_npairs_s_mu(
+        s2, s1, np.ones(len(s2)), np.ones(len(s1)), SB, MU, period=L)),
 }
+
+# float results: within this relative tolerance of halotools' FP64 sums
+# (integer-valued marks are exact); the counts are exact
+RTOL_WEIGHTED = 1e-6
 
 
 def run_case(mod, name):
-    return np.asarray(CASES[name](mod, *sibling_inputs()))
+    """The case's output: one array, or (counts, weighted counts) for weighted_npairs_s_mu."""
+    r = CASES[name][1](mod, *sibling_inputs())
+    if isinstance(r, tuple):
+        return tuple(np.asarray(a) for a in r)
+    return np.asarray(r)
 
 
 def main():
@@ -80,8 +130,13 @@ def main():
     os.makedirs(OUT, exist_ok=True)
     for name in CASES:
         out = run_case(ns, name)
-        np.savez_compressed(os.path.join(OUT, name + ".npz"), sha=sha, out=out)
-        print(name, out.shape, out.dtype)
+        if isinstance(out, tuple):
+            np.savez_compressed(os.path.join(OUT, name + ".npz"), sha=sha, out=out[0],
+                                out_w=out[1])
+            print(name, out[0].shape, out[0].dtype, out[1].dtype)
+        else:
+            np.savez_compressed(os.path.join(OUT, name + ".npz"), sha=sha, out=out)
+            print(name, out.shape, out.dtype)
 
 
 if __name__ == "__main__":

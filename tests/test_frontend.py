@@ -76,5 +76,38 @@ def test_marked_bad_ids():
         h.marked_npairs_3d(S, S, [0.1, 0.2], 1.0, period=1)
 
 
+def test_marked_xy_z_ids_and_shapes():
+    # marked_npairs_xy_z.py:292-333 knows ids 1-15; the default id 0 is an error
+    for wid in (0, 16, 17):
+        with pytest.raises(h.HalotoolsError) as err:
+            h.marked_npairs_xy_z(S, S, [0.1, 0.2], [0.1, 0.2], period=1, weight_func_id=wid)
+        assert "is not recognized" in str(err.value)
+    with pytest.raises(ValueError):
+        h.marked_npairs_xy_z(S, S, [0.1, 0.2], [0.1, 0.2], period=1, weight_func_id=1.0)
+    with pytest.raises(h.HalotoolsError):
+        h.marked_npairs_xy_z(S, S, [0.1, 0.2], [0.1, 0.2], period=1, weight_func_id=5,
+                             weights1=np.ones((50, 3)), weights2=np.ones((50, 2)))
+    with pytest.raises(ValueError) as err:
+        h.marked_npairs_xy_z(S, S, [0.3, 0.2, 0.1], [0.1, 0.2], period=1, weight_func_id=1)
+    assert "rp_bins" in str(err.value)
+
+
+def test_weighted_s_mu_messages():
+    # weighted_npairs_s_mu.py:171-187
+    with pytest.raises(AssertionError) as err:
+        h.weighted_npairs_s_mu(S, S, np.ones(49), np.ones(50), [0.1, 0.2], [0, 1], period=1)
+    assert "``weights1`` should have shape (50, )" in str(err.value)
+    with pytest.raises(AssertionError) as err:
+        h.weighted_npairs_s_mu(S, S, np.ones(50), np.ones((50, 1)), [0.1, 0.2], [0, 1], period=1)
+    assert "``weights2`` should have shape (50, )" in str(err.value)
+    with pytest.raises(ValueError) as err:
+        h.weighted_npairs_s_mu(S, S, np.ones(50), np.ones(50), [0.1, 0.2], [0, 0.5, 0.4],
+                               period=1)
+    assert "Input `mu_bins` must be a monotonically increasing" in str(err.value)
+    with pytest.raises(ValueError) as err:
+        h.weighted_npairs_s_mu(S, S, np.ones(50), np.ones(50), [0.3, 0.2, 0.1], [0, 1], period=1)
+    assert "Input ``rbins`` must be a monotonically increasing" in str(err.value)
+
+
 def test_install_into_halotools_without_halotools_is_a_noop():
     assert isinstance(h.install_into_halotools(), list)

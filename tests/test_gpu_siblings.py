@@ -1,5 +1,6 @@
-"""Sibling counters (npairs_projected, npairs_jackknife_3d, npairs_per_object_3d)
-against halotools' own engines (golden vectors, make_sibling_golden.py)."""
+"""Sibling counters (npairs_projected, npairs_jackknife_3d, npairs_per_object_3d,
+marked_npairs_xy_z, weighted_npairs_s_mu) against halotools' own engines (golden
+vectors, make_sibling_golden.py)."""
 import os
 
 import numpy as np
@@ -10,15 +11,30 @@ from tests.golden import make_sibling_golden as G
 pytestmark = pytest.mark.gpu
 
 
+def _exact(name):
+    # integer counts, half-integer jackknife counts and integer-valued marks
+    return not (name.startswith("marked_xy_z") or name.startswith("weighted_s_mu")) or \
+        "threes" in name or "ones" in name
+
+
 @pytest.mark.parametrize("name", sorted(G.CASES))
 def test_sibling_matches_reference(gpu, name):
     d = np.load(os.path.join(G.OUT, name + ".npz"))
     if str(d["sha"]) != G.input_sha():
         pytest.skip("seeded generator differs on this platform")
-    fn = {"projected": "npairs_projected", "jackknife": "npairs_jackknife_3d",
-          "per_object": "npairs_per_object_3d"}[name.rsplit("_", 2)[0]]
+    fn = G.CASES[name][0]
     if not hasattr(gpu, fn):
         pytest.skip(fn + " not built")
     got = G.run_case(gpu, name)
-    assert got.dtype == d["out"].dtype and got.shape == d["out"].shape
-    assert np.array_equal(got, d["out"])  # integer counts and half-integers are exact
+    if isinstance(got, tuple):
+        counts, wsum = got
+        assert counts.dtype == d["out"].dtype and counts.shape == d["out"].shape
+        assert np.array_equal(counts, d["out"])
+        got, want = wsum, d["out_w"]
+    else:
+        want = d["out"]
+    assert got.dtype == want.dtype and got.shape == want.shape
+    if _exact(name):
+        assert np.array_equal(got, want)
+    else:
+        np.testing.assert_allclose(got, want, rtol=G.RTOL_WEIGHTED, atol=0)

@@ -65,3 +65,38 @@ def test_oracle_adjoint_matches_marked_identity():
         c = oracle.marked_npairs_3d(x[m:m + 1], x, rb, 1, period=40.0, weights1=np.ones(1),
                                     weights2=w)
         assert abs(grad[m] - 2 * np.dot(g, c)) < 1e-9 * max(1.0, abs(grad[m]))
+
+
+# ---- the oracle's weighted 2-D walks against halotools' own engines ----
+from tests.golden import make_sibling_golden as S  # noqa: E402
+
+_W2_CASES = sorted(n for n in S.CASES
+                   if S.CASES[n][0] in ("marked_npairs_xy_z", "weighted_npairs_s_mu"))
+
+
+@pytest.mark.parametrize("name", _W2_CASES)
+def test_oracle_weighted_2d_matches_reference_golden(name):
+    import os
+    d = np.load(os.path.join(S.OUT, name + ".npz"))
+    if str(d["sha"]) != S.input_sha():
+        pytest.skip("seeded generator differs on this platform")
+    got = S.run_case(oracle, name)
+    if isinstance(got, tuple):
+        assert np.array_equal(got[0], d["out"])
+        got, want = got[1], d["out_w"]
+    else:
+        want = d["out"]
+    # the reference engines are built with -Ofast: sums agree to a few ulps
+    np.testing.assert_allclose(got, want, rtol=1e-12, atol=0)
+
+
+def test_oracle_weighted_2d_unit_marks_give_counts():
+    rng = np.random.default_rng(3)
+    x = rng.uniform(0, 60, (1500, 3))
+    rp, pi = np.logspace(-1, 1, 6), np.linspace(0, 12, 5)
+    cnt = oracle.npairs_xy_z(x, x, rp, pi, period=60)
+    assert np.array_equal(oracle.marked_npairs_xy_z(x, x, rp, pi, 1, period=60), cnt.astype(float))
+    sb, mu = np.logspace(-1, 1, 6), np.linspace(0, 1, 7)
+    c, w = oracle.weighted_npairs_s_mu(x, x, np.ones(1500), np.ones(1500), sb, mu, period=60)
+    assert np.array_equal(c, oracle.npairs_s_mu(x, x, sb, mu, period=60))
+    assert np.array_equal(w, c.astype(float))
