@@ -9,6 +9,7 @@ halotools' estimators bound at import time, so ``tpcf``, ``wp``,
 """
 from .pair_counters import (HalotoolsError, marked_npairs_3d, marked_npairs_3d_channels,
                             marked_npairs_xy_z, npairs_3d, npairs_jackknife_3d,
+                            npairs_jackknife_xy_z,
                             npairs_per_object_3d, npairs_projected, npairs_s_mu, npairs_xy_z,
                             weighted_npairs_s_mu)
 from ._native import GBPairsError, GBPairsUnavailable, Plan, default_plan
@@ -18,6 +19,7 @@ from . import estimators
 __all__ = ("npairs_3d", "npairs_xy_z", "npairs_s_mu", "marked_npairs_3d",
            "marked_npairs_3d_channels", "npairs_projected", "npairs_jackknife_3d",
            "npairs_per_object_3d", "marked_npairs_xy_z", "weighted_npairs_s_mu",
+           "npairs_jackknife_xy_z",
            "HalotoolsError", "GBPairsError", "GBPairsUnavailable", "Plan", "default_plan",
            "npairs_3d_batched", "BatchedCounter", "install_into_halotools", "estimators")
 
@@ -35,6 +37,7 @@ _BINDINGS = tuple([
      npairs_jackknife_3d),
     ("halotools.mock_observables.pair_counters", "marked_npairs_xy_z", marked_npairs_xy_z),
     ("halotools.mock_observables.pair_counters", "weighted_npairs_s_mu", weighted_npairs_s_mu),
+    ("halotools.mock_observables.pair_counters", "npairs_jackknife_xy_z", npairs_jackknife_xy_z),
 ] + [
     # the intrinsic-alignment estimators bind marked_npairs_xy_z at import time
     ("halotools.mock_observables.ia_correlations." + m, "marked_npairs_xy_z", marked_npairs_xy_z)

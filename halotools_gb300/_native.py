@@ -30,6 +30,7 @@ EXPORTED = (
     "gbp_npairs_3d_static", "gbp_batched_npairs_3d", "gbp_plan_set_graph", "gbp_plan_set_autotune",
     "gbp_plan_set_block", "gbp_marked_npairs_3d_channels", "gbp_npairs_jackknife_3d",
     "gbp_npairs_per_object_3d", "gbp_marked_npairs_xy_z", "gbp_weighted_npairs_s_mu",
+    "gbp_npairs_jackknife_xy_z",
     "gbp_weighted_adjoint_3d", "gbp_zheng07_weights", "gbp_zheng07_vjp",
 )
 
@@ -116,6 +117,8 @@ def load(build_if_missing: bool = True):
         L.gbp_npairs_jackknife_3d.argtypes = [vp, vp, i64, vp, i64, vp, vp, i32, pd, i32, pd, i32,
                                               i32, pd]
         L.gbp_npairs_per_object_3d.argtypes = [vp, vp, i64, vp, i64, pd, i32, pd, i32, i32, pi64]
+        L.gbp_npairs_jackknife_xy_z.argtypes = [vp, vp, i64, vp, i64, vp, vp, i32, pd, i32, pd,
+                                                i32, pd, i32, i32, pd]
         L.gbp_marked_npairs_xy_z.argtypes = [vp, vp, i64, vp, i64, vp, vp, i32, i32, pd, i32, pd,
                                              i32, pd, i32, i32, pd]
         L.gbp_weighted_npairs_s_mu.argtypes = [vp, vp, i64, vp, i64, vp, vp, pd, i32, pd, i32, pd,

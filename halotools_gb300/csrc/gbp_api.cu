@@ -247,7 +247,8 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
     size_t o_sten = cv.take<int>(nsten), o_stenD = cv.take<float4>(nsten);
     size_t o_hist = cv.take<unsigned long long>(nhist * nm);
     size_t o_histd = cv.take<double>(nhist * nm);
-    const size_t ntab = (size_t)c.ntag * (size_t)(nb0 + 1);
+    // jackknife: (tag, bin) pair ends over the 1-D or 2-D differential bins
+    const size_t ntab = (size_t)c.ntag * (size_t)(nb0 + 1) * (size_t)(c.naxes > 1 ? nb1 + 1 : 1);
     size_t o_htag = cv.take<unsigned long long>(ntab > 0 ? ntab : 1);
     size_t o_misc = cv.take<unsigned long long>(8);  // counter, nitems, err, recheck, cand
     size_t total = cv.take<char>(0) + 256;
@@ -470,7 +471,7 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
                         : c.mode == MODE_MARKC ? 4 * c.nw
                         : c.mode == MODE_ADJ   ? 4
                         : c.mode == MODE_POBJ  ? 4   // the gather kernel's fixed stride
-                        : c.mode == MODE_JACK  ? 4
+                        : (c.mode == MODE_JACK || c.mode == MODE_JACKXYZ) ? 4
                                                : 0;
         // 2-D and wide 1-D histograms: one shared copy per warp while they fit,
         // else the warps add straight into the global histogram
@@ -1208,6 +1209,71 @@ int gbp_npairs_jackknife_3d(gbp_plan *plan, const double *xyz1, int64_t n1, cons
             cQ[(size_t)s] += (double)tab[(size_t)s * (nb + 1) + k];
             out[(size_t)s * nb + k] = cT - 0.5 * cQ[(size_t)s];
         }
+    }
+    return GBP_OK;
+}
+
+int gbp_npairs_jackknife_xy_z(gbp_plan *plan, const double *xyz1, int64_t n1, const double *xyz2,
+                              int64_t n2, const int32_t *jtags1, const int32_t *jtags2,
+                              int32_t n_samples, const double *rp_bins, int32_t n_rp,
+                              const double *pi_bins, int32_t n_pi, const double *period3,
+                              int32_t pbc, int32_t mem, double *out) {
+    if (!out) return fail(plan, GBP_ERR_INVALID, "null output");
+    if (mem != GBP_MEM_HOST)
+        return fail(plan, GBP_ERR_INVALID, "jackknife counts take host positions and tags");
+    // tags travel packed as tag_i | tag_j << 16
+    if (n_samples < 1 || n_samples > 32767 || (n1 > 0 && !jtags1) || (n2 > 0 && !jtags2))
+        return fail(plan, GBP_ERR_INVALID, "N_samples must be 1..32767 with one tag per point");
+    const bool autocorr = (xyz1 == xyz2 && n1 == n2 && jtags1 == jtags2);
+    // tags go through the weight path as exact FP64 / FP32 integers
+    std::vector<double> t1((size_t)n1), t2;
+    for (int64_t i = 0; i < n1; i++) {
+        if (jtags1[i] < 1 || jtags1[i] > n_samples)
+            return fail(plan, GBP_ERR_INVALID, "jtags1 must be in [1, N_samples]");
+        t1[(size_t)i] = (double)jtags1[i];
+    }
+    if (!autocorr) {
+        t2.resize((size_t)n2);
+        for (int64_t i = 0; i < n2; i++) {
+            if (jtags2[i] < 1 || jtags2[i] > n_samples)
+                return fail(plan, GBP_ERR_INVALID, "jtags2 must be in [1, N_samples]");
+            t2[(size_t)i] = (double)jtags2[i];
+        }
+    }
+    Call c;
+    c.mode = MODE_JACKXYZ;
+    c.w1 = t1.data();
+    c.w2 = autocorr ? t1.data() : t2.data();
+    c.nw = 1;
+    c.wf = 1;
+    c.ntag = n_samples + 1;
+    int rc = setup_xyz(plan, c, xyz1, n1, xyz2, n2, rp_bins, n_rp, pi_bins, n_pi, period3, pbc,
+                       mem, autocorr);
+    if (rc) return rc;
+    const int rows = n_samples + 1;
+    const size_t plane = (size_t)n_rp * n_pi;
+    for (size_t k = 0; k < rows * plane; k++) out[k] = 0.0;
+    if (n1 == 0 || n2 == 0) return GBP_OK;
+    std::vector<unsigned long long> h;
+    if ((rc = run_call(plan, c, h))) return rc;
+    std::vector<unsigned long long> &tab = c.htag;
+    const size_t nbin = (size_t)(n_rp + 1) * (n_pi + 1);
+    if (autocorr) {
+        // (i, i): separation 0, both ends carry tag_i (the kernels skip it)
+        const int a0 = host_bin(n_rp, c.ax[0].E.data(), 0.0);
+        const int b0 = host_bin(n_pi, c.ax[1].E.data(), 0.0);
+        if (a0 < n_rp && b0 < n_pi)
+            for (int64_t i = 0; i < n1; i++)
+                tab[(size_t)jtags1[i] * nbin + (size_t)a0 * (n_pi + 1) + b0] += 2;
+    }
+    // npairs_jackknife_xy_z_engine: row 0 all pairs, row s the pairs without
+    // subsample s, one end in s counting one half: C - (ends in s) / 2
+    std::vector<double> C(plane), Q(plane);
+    cumulate_2d(h.data(), n_rp, n_pi, C.data());
+    for (size_t k = 0; k < plane; k++) out[k] = C[k];
+    for (int sidx = 1; sidx < rows; sidx++) {
+        cumulate_2d(tab.data() + (size_t)sidx * nbin, n_rp, n_pi, Q.data());
+        for (size_t k = 0; k < plane; k++) out[(size_t)sidx * plane + k] = C[k] - 0.5 * Q[k];
     }
     return GBP_OK;
 }

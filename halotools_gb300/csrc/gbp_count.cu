@@ -165,6 +165,8 @@ __device__ __forceinline__ void bin_mark(const PairV &p, float *hs, float *hc, c
 // rounded to nearest) goes to lo, so hi + lo carries the sum to about 2^-48.
 struct WSink {
     float *hi, *lo;
+    unsigned long long *tab;  // jackknife (rp, pi): the global (tag, bin) table of pair ends
+    int tstride;              // its row length (bins per tag)
 };
 
 __device__ __forceinline__ void w2_add(const WSink &s, int b, float x) {
@@ -173,6 +175,21 @@ __device__ __forceinline__ void w2_add(const WSink &s, int b, float x) {
     const float bp = t - old;
     const float err = (old - (t - bp)) + (x - bp);
     if (err != 0.0f) atomicAdd(&s.lo[b], err);
+}
+
+// What a binned pair adds besides its count: X_W its weight w (times the
+// multiplicity m), X_TAG one pair end per tag (w holds tag_i | tag_j << 16)
+#define X_NONE 0
+#define X_W 1
+#define X_TAG 2
+template <int X>
+__device__ __forceinline__ void sink_add(const WSink &s, int b, int m, float w) {
+    if (X == X_W) w2_add(s, b, m == 2 ? 2.0f * w : w);
+    if (X == X_TAG) {
+        const int t = __float_as_int(w);
+        atomicAdd(&s.tab[(t & 0xffff) * s.tstride + b], (unsigned long long)m);
+        atomicAdd(&s.tab[(t >> 16) * s.tstride + b], (unsigned long long)m);
+    }
 }
 
 // ---------------- deferred FP64 rechecks (s, mu') ----------------
@@ -197,8 +214,8 @@ __device__ __forceinline__ bool rq_push(const RQ &q, int4 e) {
 
 // ---------------- stage 2: (rp, pi) ----------------
 // (rechecks are rare here, about 1e-4 of the pairs: each lane re-evaluates its
-// own).  CNT: integer counts into hw; WT: the pair's weight into ws.
-template <class HT, bool CNT, bool WT>
+// own).  CNT: integer counts into hw; X: what else the pair adds (sink_add).
+template <class HT, bool CNT, int X>
 __device__ __noinline__ void slow_xyz(float v0, float v1, int b0a, int b0b, int is, int js,
                                       bool sym, float wt, HT *hw, const WSink ws, int stride,
                                       const AxisSm &A, const AxisSm &Bx, const CountArgs &a) {
@@ -207,7 +224,7 @@ __device__ __noinline__ void slow_xyz(float v0, float v1, int b0a, int b0b, int 
     if (ka >= 0 && kb >= 0) {
         if (ka < A.nb && kb < Bx.nb) {
             if (CNT) atomicAdd(&hw[ka * stride + kb], (HT)(sym ? 2 : 1));
-            if (WT) w2_add(ws, ka * stride + kb, sym ? 2.0f * wt : wt);
+            sink_add<X>(ws, ka * stride + kb, sym ? 2 : 1, wt);
         }
         return;
     }
@@ -224,12 +241,12 @@ __device__ __noinline__ void slow_xyz(float v0, float v1, int b0a, int b0b, int 
         const int eb = kb >= 0 ? kb : exact_bin(r.dz2, b0b, Bx);
         if (ea < A.nb && eb < Bx.nb) {
             if (CNT) atomicAdd(&hw[ea * stride + eb], (HT)1);
-            if (WT) w2_add(ws, ea * stride + eb, wt);
+            sink_add<X>(ws, ea * stride + eb, 1, wt);
         }
     }
 }
 
-template <class HT, bool CNT, bool WT>
+template <class HT, bool CNT, int X>
 __device__ __forceinline__ void bin_xyz(const PairV &p, HT *hw, const WSink &ws, int stride,
                                         const AxisSm &A, const AxisSm &Bx, const Ix &ix,
                                         const CountArgs &a) {
@@ -241,13 +258,13 @@ __device__ __forceinline__ void bin_xyz(const PairV &p, HT *hw, const WSink &ws,
     int bb = __float_as_int(e1.x) + (v1 > e1.y ? 1 : 0);
     bool amb = ((v0 > e0.z) & !(v0 > e0.y)) | ((v1 > e1.z) & !(v1 > e1.y));
     if (amb) {
-        slow_xyz<HT, CNT, WT>(v0, v1, __float_as_int(e0.x), __float_as_int(e1.x), ix.ui[p.iu],
+        slow_xyz<HT, CNT, X>(v0, v1, __float_as_int(e0.x), __float_as_int(e1.x), ix.ui[p.iu],
                               ix.jw[p.jj], sym, p.w, hw, ws, stride, A, Bx, a);
         return;
     }
     if ((ba < A.nb) & (bb < Bx.nb)) {
         if (CNT) atomicAdd(&hw[ba * stride + bb], (HT)(sym ? 2 : 1));
-        if (WT) w2_add(ws, ba * stride + bb, sym ? 2.0f * p.w : p.w);
+        sink_add<X>(ws, ba * stride + bb, sym ? 2 : 1, p.w);
     }
 }
 
@@ -255,11 +272,11 @@ __device__ __forceinline__ void bin_xyz(const PairV &p, HT *hw, const WSink &ws,
 // v = s^2 on axis 0; q = dxy / s^2 on axis 1, whose FP32 error depends on s:
 // the s table's 4th field holds the q error bound for the slot's smallest s.
 // A queued pair: {i, j, s walk start | mu' walk start << 11 | flags << 22, weight}.
-template <class HT, bool CNT, bool WT>
+template <class HT, bool CNT, int X>
 __device__ __forceinline__ void exact_smu(const int4 &e, HT *hw, const WSink &ws, int stride,
                                           const AxisSm &A, const AxisSm &Q, const CountArgs &a);
 
-template <class HT, bool CNT, bool WT>
+template <class HT, bool CNT, int X>
 __device__ __noinline__ void slow_smu(float v, float q, float qb, int b0s, int is, int js,
                                       bool sym, float wt, HT *hw, const WSink ws, int stride,
                                       const AxisSm &A, const AxisSm &Q, const RQ &rq,
@@ -276,7 +293,7 @@ __device__ __noinline__ void slow_smu(float v, float q, float qb, int b0s, int i
     if (ks >= 0 && kq >= 0) {
         if (kq < Q.nb) {
             if (CNT) atomicAdd(&hw[ks * stride + kq], (HT)(sym ? 2 : 1));
-            if (WT) w2_add(ws, ks * stride + kq, sym ? 2.0f * wt : wt);
+            sink_add<X>(ws, ks * stride + kq, sym ? 2 : 1, wt);
         }
         return;
     }
@@ -287,12 +304,12 @@ __device__ __noinline__ void slow_smu(float v, float q, float qb, int b0s, int i
                              __float_as_int(wt));
     if (rq_push(rq, e)) return;
     atomicAdd(a.nrecheck, 1ull);
-    exact_smu<HT, CNT, WT>(e, hw, ws, stride, A, Q, a);
+    exact_smu<HT, CNT, X>(e, hw, ws, stride, A, Q, a);
 }
 
 // FP64 (s, mu') bins of a queued pair: sqr_mu = dxy / s^2 as an FP64 quotient,
 // 0 at s = 0 (npairs_s_mu_engine.pyx:200-226)
-template <class HT, bool CNT, bool WT>
+template <class HT, bool CNT, int X>
 __device__ __forceinline__ void exact_smu(const int4 &e, HT *hw, const WSink &ws, int stride,
                                           const AxisSm &A, const AxisSm &Q, const CountArgs &a) {
     double p[3], qq[3];
@@ -308,11 +325,11 @@ __device__ __forceinline__ void exact_smu(const int4 &e, HT *hw, const WSink &ws
         const int eq = exact_bin(mu2, sq, Q);
         if (eq >= Q.nb) continue;
         if (CNT) atomicAdd(&hw[es * stride + eq], (HT)1);
-        if (WT) w2_add(ws, es * stride + eq, wt);
+        sink_add<X>(ws, es * stride + eq, 1, wt);
     }
 }
 
-template <class HT, bool CNT, bool WT>
+template <class HT, bool CNT, int X>
 __device__ __forceinline__ void bin_smu(const PairV &p, HT *hw, const WSink &ws, int stride,
                                         const AxisSm &A, const AxisSm &Q, const Ix &ix,
                                         const RQ &rq, const CountArgs &a) {
@@ -332,13 +349,13 @@ __device__ __forceinline__ void bin_smu(const PairV &p, HT *hw, const WSink &ws,
     bool amb = ((v > e0.z) & !(v > e0.y)) | !(q - below > qb) | !(above - q > qb) |
                (e1.z < -3.0e38f);
     if (amb) {
-        slow_smu<HT, CNT, WT>(v, q, qb, __float_as_int(e0.x), ix.ui[p.iu], ix.jw[p.jj], sym, p.w,
+        slow_smu<HT, CNT, X>(v, q, qb, __float_as_int(e0.x), ix.ui[p.iu], ix.jw[p.jj], sym, p.w,
                               hw, ws, stride, A, Q, rq, a);
         return;
     }
     if (bq < Q.nb) {
         if (CNT) atomicAdd(&hw[bs * stride + bq], (HT)(sym ? 2 : 1));
-        if (WT) w2_add(ws, bs * stride + bq, sym ? 2.0f * p.w : p.w);
+        sink_add<X>(ws, bs * stride + bq, sym ? 2 : 1, p.w);
     }
 }
 
@@ -391,7 +408,7 @@ __device__ __forceinline__ double wfunc64(int id, const double *A, const double 
 template <int MODE>
 __device__ __forceinline__ unsigned out_bits(const float4 &u, const float4 &t, float R0, float R1) {
     const float dx = u.x - t.x, dy = u.y - t.y, dz = u.z - t.z;
-    if (MODE == MODE_XYZ || MODE == MODE_XYZW) {
+    if (gbp_mode_xyz(MODE)) {
         const float a = fmaf(-dy, dy, fmaf(-dx, dx, R0));
         const float b = fmaf(-dz, dz, R1);
         return __float_as_uint(a) | __float_as_uint(b);
@@ -407,8 +424,9 @@ __device__ __forceinline__ unsigned out_bits(const float4 &u, const float4 &t, f
 template <int MODE, int WF>
 __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
-    constexpr bool XYZF = (MODE == MODE_XYZ || MODE == MODE_XYZW);  // (rp, pi) geometry
-    constexpr bool SMUF = (MODE == MODE_SMU || MODE == MODE_SMUW);  // (s, mu') geometry
+    constexpr bool JACK2 = (MODE == MODE_JACKXYZ);  // jackknife (rp, pi): w1 / w2 hold tags
+    constexpr bool XYZF = gbp_mode_xyz(MODE);  // (rp, pi) geometry
+    constexpr bool SMUF = gbp_mode_smu(MODE);  // (s, mu') geometry
     constexpr bool TWO = XYZF || SMUF;
     // weighted 2-D: a marking function's value per pair into the CTA's (hi, lo)
     // sums; weighted s_mu also counts
@@ -416,6 +434,7 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
     constexpr bool CNT2 = (MODE != MODE_XYZW);
     constexpr bool MARK = (MODE == MODE_MARK);
     constexpr bool MW = MARK || W2;  // per-pair marking function of staged weights
+    constexpr int XS = W2 ? X_W : JACK2 ? X_TAG : X_NONE;  // what 2-D bins add besides counts
     constexpr bool MARKC = (MODE == MODE_MARKC);  // nw = channels of product marks
     constexpr unsigned FULL = 0xffffffffu;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -423,8 +442,8 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
     const int T0 = a.ax[0].T, T1 = TWO ? a.ax[1].T : 0;
     const int copies = a.hist_copies;  // 2-D / wide: GBP_WARPS (one per warp) or 0 (global)
     constexpr bool JACK = (MODE == MODE_JACK);    // w1 / w2 hold the subsample tags
-    const int nw = (MW || MARKC || JACK) ? a.nw : 0;
-    const int jwb = MW ? (WF == 0 ? 8 * nw : 4) : MARKC ? 4 * nw : JACK ? 4 : 0;
+    const int nw = (MW || MARKC || JACK || JACK2) ? a.nw : 0;
+    const int jwb = MW ? (WF == 0 ? 8 * nw : 4) : MARKC ? 4 * nw : (JACK || JACK2) ? 4 : 0;
     const SmemLayout L = gbp_smem_layout(MODE, T0, T1, nb0, nb1, a.nsten, copies, jwb, a.ntag);
     if (gbp_smem_too_small(L.total, a.err)) return;
     unsigned *s_l0 = (unsigned *)(smem + L.off_lut0);
@@ -503,7 +522,7 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
     float *s_whi = (float *)(smem + L.off_hist + gbp_align(copies * nbin * 4, 16));
     float *s_wlo = s_whi + gbp_align(nbin * 4, 16) / 4;
     double *s_wacc = (double *)(s_wlo + gbp_align(nbin * 4, 16) / 4);
-    const WSink wsink{s_whi, s_wlo};
+    const WSink wsink{s_whi, s_wlo, a.htag, nbin};
     if (W2)
         for (int i = tid; i < nbin; i += GBP_BLOCK) {
             s_whi[i] = 0.f;
@@ -539,11 +558,11 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
         else if (MODE == MODE_3DS) {
             if (copies) bin_3d<false>(e, wh, A0, ix, a); else bin_3d<false>(e, gh, A0, ix, a);
         } else if (XYZF) {
-            if (copies) bin_xyz<unsigned, CNT2, W2>(e, wh, wsink, stride2, A0, A1, ix, a);
-            else bin_xyz<unsigned long long, CNT2, W2>(e, gh, wsink, stride2, A0, A1, ix, a);
+            if (copies) bin_xyz<unsigned, CNT2, XS>(e, wh, wsink, stride2, A0, A1, ix, a);
+            else bin_xyz<unsigned long long, CNT2, XS>(e, gh, wsink, stride2, A0, A1, ix, a);
         } else if (SMUF) {
-            if (copies) bin_smu<unsigned, CNT2, W2>(e, wh, wsink, stride2, A0, A1, ix, rq, a);
-            else bin_smu<unsigned long long, CNT2, W2>(e, gh, wsink, stride2, A0, A1, ix, rq, a);
+            if (copies) bin_smu<unsigned, CNT2, XS>(e, wh, wsink, stride2, A0, A1, ix, rq, a);
+            else bin_smu<unsigned long long, CNT2, XS>(e, gh, wsink, stride2, A0, A1, ix, rq, a);
         } else if (MARK) bin_mark(e, hs, hc, A0, ix, a);
     };
     // Bin the rest of the queue, add this warp's histogram to mock mk and clear it.
@@ -560,8 +579,8 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
             const unsigned n = min(end - rq.head, 32u);
             if ((unsigned)lane < n) {
                 const int4 e = rq.ring[(rq.head + lane) % GBP_RQCAP];
-                if (copies) exact_smu<unsigned, CNT2, W2>(e, wh, wsink, stride2, A0, A1, a);
-                else exact_smu<unsigned long long, CNT2, W2>(e, gh, wsink, stride2, A0, A1, a);
+                if (copies) exact_smu<unsigned, CNT2, XS>(e, wh, wsink, stride2, A0, A1, a);
+                else exact_smu<unsigned long long, CNT2, XS>(e, gh, wsink, stride2, A0, A1, a);
             }
             if (lane == 0) atomicAdd(a.nrecheck, (unsigned long long)n);
             rq.head += n;
@@ -657,7 +676,7 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
         ux[lane + 48] = u1.x; uy[lane + 48] = u1.y; uz[lane + 48] = u1.z; uix[lane + 48] = is1;
         float w0 = 0.f, w1 = 0.f;
         double wa[5] = {0, 0, 0, 0, 0}, wb[5] = {0, 0, 0, 0, 0};
-        if (JACK) {
+        if (JACK || JACK2) {
             s_uw[lane] = lane < icnt ? a.w1[ifirst + lane] : 0.f;
             s_uw[lane + 48] = lane + 32 < icnt ? a.w1[ifirst + 32 + lane] : 0.f;
         }
@@ -743,7 +762,7 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                     }
                     if (MARKC)
                         for (int q = 0; q < nw; q++) jw[lane * nw + q] = a.w2[(int64_t)j * nw + q];
-                    if (JACK) jw[lane] = a.w2[j];
+                    if (JACK || JACK2) jw[lane] = a.w2[j];
                 } else {
                     // padding slot: at -FAR, so it is 2*FAR from an idle i-lane (+FAR)
                     // and farther still from every real point; its bits are also masked
@@ -882,6 +901,8 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                             }
                             if (MARK) v1 = wt;
                         }
+                        // jackknife (rp, pi): both ends' tags (exact small integers)
+                        if (JACK2) wt = __int_as_float((int)s_uw[iu] | ((int)jw[jj] << 16));
                         return PairV{v0, v1, iu, jj, ((sym_bits >> jj) & 1u) != 0u, wt};
                     };
                     if (MARKC) {
@@ -1006,6 +1027,8 @@ cudaError_t gbp_launch_count(int mode, int wf, const CountArgs &a, int grid, siz
         return launch_t<MODE_JACK, 1>(a, grid, smem, st);
     case MODE_SMUW:
         return launch_t<MODE_SMUW, 1>(a, grid, smem, st);
+    case MODE_JACKXYZ:
+        return launch_t<MODE_JACKXYZ, 1>(a, grid, smem, st);
     case MODE_XYZW:
         if (wf == 1) return launch_t<MODE_XYZW, 1>(a, grid, smem, st);
         if (wf == 2) return launch_t<MODE_XYZW, 2>(a, grid, smem, st);
@@ -1030,6 +1053,8 @@ int gbp_count_occupancy(int mode, int wf, size_t smem) {
         return occ_t<MODE_JACK, 1>(smem);
     case MODE_SMUW:
         return occ_t<MODE_SMUW, 1>(smem);
+    case MODE_JACKXYZ:
+        return occ_t<MODE_JACKXYZ, 1>(smem);
     case MODE_XYZW:
         if (wf == 1) return occ_t<MODE_XYZW, 1>(smem);
         if (wf == 2) return occ_t<MODE_XYZW, 2>(smem);

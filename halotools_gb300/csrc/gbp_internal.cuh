@@ -29,7 +29,15 @@ enum { MODE_3D = 0, MODE_XYZ = 1, MODE_SMU = 2, MODE_MARK = 3, MODE_ADJ = 4, MOD
        MODE_JACK = 7,     // jackknife: counts plus a (tag, bin) table of pair ends
        MODE_POBJ = 8,     // per-object counts (gather walk of the adjoint)
        MODE_XYZW = 9,     // (rp, pi) sums of a marking function (marked_npairs_xy_z)
-       MODE_SMUW = 10 };  // (s, mu') counts and w1 * w2 sums (weighted_npairs_s_mu)
+       MODE_SMUW = 10,    // (s, mu') counts and w1 * w2 sums (weighted_npairs_s_mu)
+       MODE_JACKXYZ = 11 };  // (rp, pi) counts plus a global (tag, bin) table of pair ends
+
+// Pair geometry of a count mode: (rp, pi) cylinders or (s, mu') cones; every
+// other mode measures 3-D separations
+__host__ __device__ constexpr bool gbp_mode_xyz(int m) {
+    return m == MODE_XYZ || m == MODE_XYZW || m == MODE_JACKXYZ;
+}
+__host__ __device__ constexpr bool gbp_mode_smu(int m) { return m == MODE_SMU || m == MODE_SMUW; }
 
 // The weighted 2-D modes add each pair's weight to a per-CTA FP32 pair
 // (hi, lo): hi by atomic add, lo by the exact rounding error of that add
@@ -134,7 +142,7 @@ __host__ __device__ inline SmemLayout gbp_smem_layout(int mode, int T0, int T1, 
     const bool adj = mode == MODE_ADJ || mode == MODE_POBJ;  // the gather kernel
     L.off_lut0 = o; o += adj ? T0 * 16 : gbp_align(T0 * 4, 16);
     L.off_lut1 = o; o += adj ? T1 * 16 : gbp_align(T1 * 4, 16);
-    const bool smu = mode == MODE_SMU || mode == MODE_SMUW;
+    const bool smu = gbp_mode_smu(mode);
     L.off_qb = o; o += smu ? gbp_align(T0 * 4, 16) : 0;
     L.off_hl0 = o; o += adj ? 0 : gbp_align((nb0 + 2) * 8, 16);
     L.off_hl1 = o; o += adj ? 0 : gbp_align((nb1 + 2) * 8, 16);

@@ -9,6 +9,7 @@ reference front-ends:
 * ``marked_npairs_3d`` marked_npairs_3d.py:25-326
 * ``marked_npairs_xy_z`` marked_npairs_xy_z.py:23-333
 * ``weighted_npairs_s_mu`` weighted_npairs_s_mu.py:22-230
+* ``npairs_jackknife_xy_z`` npairs_jackknife_xy_z.py:23-170
 
 ``num_threads`` is validated as the reference does and then ignored (the GPU
 is the parallel engine).  ``approx_cell1_size`` / ``approx_cell2_size`` are
@@ -494,24 +495,9 @@ def marked_npairs_3d_channels(sample1, sample2, rbins, period=None, weights1=Non
     return out
 
 
-def npairs_jackknife_3d(sample1, sample2, rbins, jtags1, jtags2, N_samples, period=None,
-                        weights1=None, weights2=None, num_threads=1, approx_cell1_size=None,
-                        approx_cell2_size=None):
-    """Jackknife pair counts, shape ``(N_samples + 1, len(rbins))``, float64.
-
-    Same inputs and output as halotools ``npairs_jackknife_3d``
-    (npairs_jackknife_3d.py:29-31): row 0 is the cumulative count of all pairs,
-    row s the count with subsample s removed, where a pair with one end in s
-    counts one half (npairs_jackknife_3d_engine.pyx:238-289). Exact for unit
-    weights (the ``tpcf_jackknife`` case); other weights are not supported on
-    the GPU and raise ``NotImplementedError``.
-    """
-    _check_num_threads(num_threads)
-    rbins = _bins(rbins, "Input ``rbins`` must be a monotonically increasing 1D array with at "
-                         "least two entries")
-    rmax = np.max(rbins)
-    _approx_cells(approx_cell1_size, [rmax] * 3, "approx_cell1_size")
-    _approx_cells(approx_cell2_size, [rmax] * 3, "approx_cell2_size")
+def _jackknife_inputs(sample1, sample2, jtags1, jtags2, N_samples, weights1, weights2):
+    """npairs_jackknife_3d.py / npairs_jackknife_xy_z.py weight and tag checks
+    (_npairs_jackknife_xy_z_process_weights_jtags); non-unit weights are refused."""
     s1 = _columns(sample1)
     s2 = s1 if sample2 is sample1 else _columns(sample2)
     for w, s, name in ((weights1, s1, "weights1"), (weights2, s2, "weights2")):
@@ -539,18 +525,84 @@ def npairs_jackknife_3d(sample1, sample2, rbins, jtags1, jtags2, N_samples, peri
         raise HalotoolsError("jtags2 must be <= N_samples")
     if not np.array_equal(np.unique(t1), np.arange(1, N_samples + 1)):
         warnings.warn("Warning: sample1 does not contain points in every jackknife sample.")
-    _nonneg(rbins, "rbins")
-    x1, x2, box, pbc = _positions(s1, s2, period, [rmax] * 3, [rmax * 3.0] * 3)
+    return s1, s2, t1, t2
+
+
+def _jackknife_tags(x1, x2, t1, t2):
+    """int32 tag arrays; the same points with different tags count as a cross-correlation."""
     j1 = np.ascontiguousarray(t1, dtype=np.int32)
     j2 = j1 if (x2 is x1 and np.array_equal(t1, t2)) else np.ascontiguousarray(t2, dtype=np.int32)
     if x2 is x1 and j2 is not j1:
-        x2 = x1.copy()  # same points, different tags: count as a cross-correlation
+        x2 = x1.copy()
+    return x1, x2, j1, j2
+
+
+def npairs_jackknife_3d(sample1, sample2, rbins, jtags1, jtags2, N_samples, period=None,
+                        weights1=None, weights2=None, num_threads=1, approx_cell1_size=None,
+                        approx_cell2_size=None):
+    """Jackknife pair counts, shape ``(N_samples + 1, len(rbins))``, float64.
+
+    Same inputs and output as halotools ``npairs_jackknife_3d``
+    (npairs_jackknife_3d.py:29-31): row 0 is the cumulative count of all pairs,
+    row s the count with subsample s removed, where a pair with one end in s
+    counts one half (npairs_jackknife_3d_engine.pyx:238-289). Exact for unit
+    weights (the ``tpcf_jackknife`` case); other weights are not supported on
+    the GPU and raise ``NotImplementedError``.
+    """
+    _check_num_threads(num_threads)
+    rbins = _bins(rbins, "Input ``rbins`` must be a monotonically increasing 1D array with at "
+                         "least two entries")
+    rmax = np.max(rbins)
+    _approx_cells(approx_cell1_size, [rmax] * 3, "approx_cell1_size")
+    _approx_cells(approx_cell2_size, [rmax] * 3, "approx_cell2_size")
+    s1, s2, t1, t2 = _jackknife_inputs(sample1, sample2, jtags1, jtags2, N_samples, weights1,
+                                       weights2)
+    _nonneg(rbins, "rbins")
+    x1, x2, box, pbc = _positions(s1, s2, period, [rmax] * 3, [rmax * 3.0] * 3)
+    x1, x2, j1, j2 = _jackknife_tags(x1, x2, t1, t2)
     plan = _native.default_plan()
     out = np.zeros((int(N_samples) + 1, len(rbins)), dtype=np.float64)
     plan.check(plan.lib.gbp_npairs_jackknife_3d(
         plan.handle, _native.dptr(x1), len(x1), _native.dptr(x2), len(x2), _native.dptr(j1),
         _native.dptr(j2), int(N_samples), _native.pd(rbins), len(rbins), _native.pd(box), pbc,
         GBP_MEM_HOST, _native.pd(out)))
+    return out
+
+
+def npairs_jackknife_xy_z(sample1, sample2, rp_bins, pi_bins, jtags1, jtags2, N_samples,
+                          period=None, weights1=None, weights2=None, num_threads=1,
+                          approx_cell1_size=None, approx_cell2_size=None):
+    """Jackknife (r_p, pi) pair counts, shape ``(N_samples + 1, len(rp_bins),
+    len(pi_bins))``, float64.
+
+    Same inputs and output as halotools ``npairs_jackknife_xy_z``
+    (npairs_jackknife_xy_z.py:23-26): row 0 counts all pairs, row s the pairs
+    without subsample s, a pair with one end in s counting one half
+    (npairs_jackknife_xy_z_engine.pyx:250-281).  Exact for unit weights; other
+    weights raise ``NotImplementedError``.
+    """
+    _check_num_threads(num_threads)
+    rp_bins = _bins(rp_bins, "Input ``rp_bins`` must be a monotonically increasing 1D array "
+                             "with at least two entries")
+    pi_bins = _bins(pi_bins, "Input ``pi_bins`` must be a monotonically increasing 1D array "
+                             "with at least two entries")
+    rpm, pim = np.max(rp_bins), np.max(pi_bins)
+    _approx_cells(approx_cell1_size, [rpm, rpm, pim], "approx_cell1_size")
+    _approx_cells(approx_cell2_size, [rpm, rpm, pim], "approx_cell2_size")
+    s1, s2, t1, t2 = _jackknife_inputs(sample1, sample2, jtags1, jtags2, N_samples, weights1,
+                                       weights2)
+    _nonneg(rp_bins, "rp_bins")
+    _nonneg(pi_bins, "pi_bins")
+    x1, x2, box, pbc = _positions(s1, s2, period, [rpm, rpm, pim],
+                                  [rpm * 3.0, rpm * 3.0, pim * 3.0])
+    x1, x2, j1, j2 = _jackknife_tags(x1, x2, t1, t2)
+    plan = _native.default_plan()
+    out = np.zeros((int(N_samples) + 1, len(rp_bins), len(pi_bins)), dtype=np.float64)
+    plan.check(plan.lib.gbp_npairs_jackknife_xy_z(
+        plan.handle, _native.dptr(x1), len(x1), _native.dptr(x2), len(x2), _native.dptr(j1),
+        _native.dptr(j2), int(N_samples), _native.pd(rp_bins), len(rp_bins),
+        _native.pd(pi_bins), len(pi_bins), _native.pd(box), pbc, GBP_MEM_HOST,
+        _native.pd(out)))
     return out
 
 

@@ -135,6 +135,20 @@ int gbp_marked_npairs_3d(gbp_plan *plan, const double *xyz1, int64_t n1, const d
                          const double *period3, int32_t pbc, int32_t mem, double *out);
 
 /*
+ * Jackknife (r_p, pi) pair counts, as npairs_jackknife_xy_z
+ * (npairs_jackknife_xy_z.py:23-26, engine npairs_jackknife_xy_z_engine.pyx:231-281)
+ * without weights: out[0][k][g] is the cumulative count, out[s][k][g]
+ * (s = 1..n_samples) the count with subsample s removed, a pair with one end in
+ * s counting one half.  jtags in [1, n_samples], n_samples <= 32767; positions
+ * and tags in host memory; out is (n_samples + 1, n_rp, n_pi) FP64.
+ */
+int gbp_npairs_jackknife_xy_z(gbp_plan *plan, const double *xyz1, int64_t n1, const double *xyz2,
+                              int64_t n2, const int32_t *jtags1, const int32_t *jtags2,
+                              int32_t n_samples, const double *rp_bins, int32_t n_rp,
+                              const double *pi_bins, int32_t n_pi, const double *period3,
+                              int32_t pbc, int32_t mem, double *out);
+
+/*
  * Cumulative (r_p, pi) sums of marking function `wfunc_id` (1..17), row-major
  * [n_rp][n_pi]: out[k][g] adds wfunc(w1_i, w2_j) over ordered pairs with
  * dxy^2 <= rp_bins[k]^2 and dz^2 <= pi_bins[g]^2.  Weights (N, nw) row-major

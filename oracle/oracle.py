@@ -48,6 +48,8 @@ def lib():
                                              i, pd, pd, i, pd]
         L.orc_weighted_npairs_s_mu.argtypes = [pd, i64, pd, i64, pd, pd, pd, i, pd, i, pd, i,
                                                pd, pd, i, pi64, pd]
+        L.orc_npairs_jackknife_xy_z.argtypes = [pd, i64, pd, i64, pd, pd, pi64, pi64, i, pd, i,
+                                                pd, i, pd, i, pd, pd, i, pd]
         L.orc_bf_npairs_3d.argtypes = [pd, i64, pd, i64, pd, i, pd, i, pi64]
         L.orc_weighted_adjoint_3d.argtypes = [pd, i64, pd, pd, i, pd, i, pd, i, pd]
         _lib = L
@@ -215,6 +217,31 @@ def weighted_npairs_s_mu(sample1, sample2, weights1, weights2, s_bins, mu_bins, 
                                           _p(mu_prime), len(mu_prime), _p(lbox), pbc, _p(a1),
                                           _p(a2), int(num_threads), _pi(out), _p(wout)))
     return out, wout
+
+
+def npairs_jackknife_xy_z(sample1, sample2, rp_bins, pi_bins, jtags1, jtags2, N_samples,
+                          period=None, weights1=None, weights2=None, num_threads=1,
+                          approx_cell1_size=None, approx_cell2_size=None):
+    """npairs_jackknife_xy_z.py:23-170 driving npairs_jackknife_xy_z_engine.pyx:231-281:
+    (N_samples + 1, len(rp_bins), len(pi_bins)) float64."""
+    rp = np.ascontiguousarray(np.atleast_1d(rp_bins), dtype=np.float64)
+    pi = np.ascontiguousarray(np.atleast_1d(pi_bins), dtype=np.float64)
+    rpm, pim = np.max(rp), np.max(pi)
+    n1, n2 = len(sample1), len(sample2)
+    w1 = np.ones(n1) if weights1 is None else np.asarray(weights1, dtype=np.float64)
+    w2 = np.ones(n2) if weights2 is None else np.asarray(weights2, dtype=np.float64)
+    w1, w2 = np.ascontiguousarray(w1), np.ascontiguousarray(w2)
+    t1 = np.ascontiguousarray(jtags1, dtype=np.int64)
+    t2 = np.ascontiguousarray(jtags2, dtype=np.int64)
+    x1, x2, lbox, pbc = _geometry(sample1, sample2, [rpm, rpm, pim], period)
+    a1 = _approx(approx_cell1_size, [rpm, rpm, pim])
+    a2 = _approx(approx_cell2_size, [rpm, rpm, pim])
+    out = np.zeros((int(N_samples) + 1, len(rp), len(pi)), dtype=np.float64)
+    _check(lib().orc_npairs_jackknife_xy_z(_p(x1), n1, _p(x2), n2, _p(w1), _p(w2), _pi(t1),
+                                           _pi(t2), int(N_samples), _p(rp), len(rp), _p(pi),
+                                           len(pi), _p(lbox), pbc, _p(a1), _p(a2),
+                                           int(num_threads), _p(out)))
+    return out
 
 
 def brute_force_npairs_3d(sample1, sample2, rbins, period=None):

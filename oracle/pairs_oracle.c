@@ -128,7 +128,8 @@ static void mesh_free(mesh_t *m) {
     free(m->order);
 }
 
-enum { K_3D = 0, K_XYZ = 1, K_SMU = 2, K_MARKED = 3, K_XYZ_MARKED = 4, K_SMU_WEIGHTED = 5 };
+enum { K_3D = 0, K_XYZ = 1, K_SMU = 2, K_MARKED = 3, K_XYZ_MARKED = 4, K_SMU_WEIGHTED = 5,
+       K_XYZ_JACK = 6 };
 
 typedef struct {
     int kind;
@@ -140,6 +141,8 @@ typedef struct {
     double *x1, *y1, *z1, *x2, *y2, *z2;
     double *w1, *w2;
     int nw, wfunc;
+    int64_t *t1, *t2; /* jackknife tags, sorted like the positions */
+    int nsamp;
     /* squared bin edges */
     const double *e1;
     int n1e;
@@ -154,6 +157,14 @@ typedef struct {
     int64_t *icounts;
     double *dcounts;
 } job_t;
+
+/* npairs_jackknife_xy_z_engine.pyx:250-281: weight of a pair in row j */
+static double jweight(int64_t j, int64_t j1, int64_t j2, double w1, double w2) {
+    if (j == 0) return w1 * w2;
+    if (j1 == j2 && j1 == j) return 0.0;
+    if (j1 != j && j2 != j) return w1 * w2;
+    return 0.5 * (w1 * w2);
+}
 
 /* marking_functions.pyx:21-218 (ids 1-17); id 0 is the custom hook, zero. */
 static double wfunc_eval(int id, const double *a, const double *b) {
@@ -277,6 +288,25 @@ static void walk_range(const walk_t *w, int64_t c0, int64_t c1, int64_t *ic, dou
                                     k--;
                                     if (k < 0) break;
                                 }
+                            } else if (w->kind == K_XYZ_JACK) {
+                                /* npairs_jackknife_xy_z_engine.pyx:231-245 */
+                                double dxy = dx * dx + dy * dy;
+                                double dzz = dz * dz;
+                                const int64_t plane = (int64_t)w->n1e * w->n2e;
+                                for (int sidx = 0; sidx <= w->nsamp; sidx++) {
+                                    int k = w->n1e - 1;
+                                    while (dxy <= w->e1[k]) {
+                                        int g = w->n2e - 1;
+                                        while (dzz <= w->e2[g]) {
+                                            dc[sidx * plane + (int64_t)k * w->n2e + g] +=
+                                                jweight(sidx, w->t1[i], w->t2[j], w->w1[i], w->w2[j]);
+                                            g--;
+                                            if (g < 0) break;
+                                        }
+                                        k--;
+                                        if (k < 0) break;
+                                    }
+                                }
                             } else { /* K_SMU, K_SMU_WEIGHTED */
                                 double dxy = dx * dx + dy * dy;
                                 double dzz = dz * dz;
@@ -321,6 +351,7 @@ static void *walk_thread(void *arg) {
  */
 static int run_walk(int kind, const double *xyz1, int64_t n1, const double *xyz2, int64_t n2,
                     const double *w1, const double *w2, int nw, int wfunc,
+                    const int64_t *tags1, const int64_t *tags2, int nsamp,
                     const double *e1, int n1e, const double *e2, int n2e,
                     double smax2, double mumax2,
                     const double period[3], int pbc, const double search[3],
@@ -357,7 +388,16 @@ static int run_walk(int kind, const double *xyz1, int64_t n1, const double *xyz2
         w.x2[k] = xyz2[3 * i]; w.y2[k] = xyz2[3 * i + 1]; w.z2[k] = xyz2[3 * i + 2];
     }
     double *wb = NULL;
-    if (kind == K_MARKED || kind == K_XYZ_MARKED || kind == K_SMU_WEIGHTED) {
+    int64_t *tb = NULL;
+    if (kind == K_XYZ_JACK) {
+        tb = (int64_t *)malloc(sizeof(int64_t) * (s1 + s2));
+        if (!tb) { free(buf); mesh_free(&w.m1); mesh_free(&w.m2); return -1; }
+        w.t1 = tb; w.t2 = tb + s1;
+        for (int64_t k = 0; k < n1; k++) w.t1[k] = tags1[w.m1.order[k]];
+        for (int64_t k = 0; k < n2; k++) w.t2[k] = tags2[w.m2.order[k]];
+        w.nsamp = nsamp;
+    }
+    if (kind == K_MARKED || kind == K_XYZ_MARKED || kind == K_SMU_WEIGHTED || kind == K_XYZ_JACK) {
         wb = (double *)malloc(sizeof(double) * (size_t)nw * (s1 + s2));
         if (!wb) { free(buf); mesh_free(&w.m1); mesh_free(&w.m2); return -1; }
         w.w1 = wb; w.w2 = wb + (size_t)nw * s1;
@@ -372,6 +412,7 @@ static int run_walk(int kind, const double *xyz1, int64_t n1, const double *xyz2
     w.smax2 = smax2; w.mumax2 = mumax2;
 
     int64_t nout = (kind == K_3D || kind == K_MARKED) ? n1e : (int64_t)n1e * n2e;
+    if (kind == K_XYZ_JACK) nout *= (int64_t)(nsamp + 1);
     double *dsum = NULL;
     if (nthreads < 1) nthreads = 1;
     if (nthreads > w.m1.ncells) nthreads = (int)w.m1.ncells;
@@ -442,7 +483,7 @@ static int run_walk(int kind, const double *xyz1, int64_t n1, const double *xyz2
     }
 done:
     free(jobs); free(th); free(ipart); free(dpart); free(dsum);
-    free(wb); free(buf);
+    free(wb); free(tb); free(buf);
     mesh_free(&w.m1); mesh_free(&w.m2);
     return rc;
 }
@@ -458,7 +499,7 @@ int orc_npairs_3d(const double *xyz1, int64_t n1, const double *xyz2, int64_t n2
     double rmax = rbins[0];
     for (int k = 0; k < nb; k++) { e[k] = rbins[k] * rbins[k]; if (rbins[k] > rmax) rmax = rbins[k]; }
     double search[3] = {rmax, rmax, rmax};
-    int rc = run_walk(K_3D, xyz1, n1, xyz2, n2, NULL, NULL, 0, 0, e, nb, NULL, 0, 0, 0,
+    int rc = run_walk(K_3D, xyz1, n1, xyz2, n2, NULL, NULL, 0, 0, NULL, NULL, 0, e, nb, NULL, 0, 0, 0,
                       period, pbc, search, approx1, approx2, nthreads, out, NULL);
     free(e);
     return rc;
@@ -475,7 +516,7 @@ int orc_npairs_xy_z(const double *xyz1, int64_t n1, const double *xyz2, int64_t 
     for (int k = 0; k < nrp; k++) { e1[k] = rp_bins[k] * rp_bins[k]; if (rp_bins[k] > rpmax) rpmax = rp_bins[k]; }
     for (int k = 0; k < npi; k++) { e2[k] = pi_bins[k] * pi_bins[k]; if (pi_bins[k] > pimax) pimax = pi_bins[k]; }
     double search[3] = {rpmax, rpmax, pimax};
-    int rc = run_walk(K_XYZ, xyz1, n1, xyz2, n2, NULL, NULL, 0, 0, e1, nrp, e2, npi, 0, 0,
+    int rc = run_walk(K_XYZ, xyz1, n1, xyz2, n2, NULL, NULL, 0, 0, NULL, NULL, 0, e1, nrp, e2, npi, 0, 0,
                       period, pbc, search, approx1, approx2, nthreads, out, NULL);
     free(e1);
     return rc;
@@ -497,7 +538,7 @@ int orc_npairs_s_mu(const double *xyz1, int64_t n1, const double *xyz2, int64_t 
     for (int k = 0; k < ns; k++) { if (isnan(e1[k]) || isnan(smax2)) smax2 = NAN; else if (e1[k] > smax2) smax2 = e1[k]; }
     for (int k = 0; k < nmu; k++) { if (isnan(e2[k]) || isnan(mumax2)) mumax2 = NAN; else if (e2[k] > mumax2) mumax2 = e2[k]; }
     double search[3] = {smax, smax, smax};
-    int rc = run_walk(K_SMU, xyz1, n1, xyz2, n2, NULL, NULL, 0, 0, e1, ns, e2, nmu, smax2, mumax2,
+    int rc = run_walk(K_SMU, xyz1, n1, xyz2, n2, NULL, NULL, 0, 0, NULL, NULL, 0, e1, ns, e2, nmu, smax2, mumax2,
                       period, pbc, search, approx1, approx2, nthreads, out, NULL);
     free(e1);
     return rc;
@@ -513,7 +554,7 @@ int orc_marked_npairs_3d(const double *xyz1, int64_t n1, const double *xyz2, int
     double rmax = rbins[0];
     for (int k = 0; k < nb; k++) { e[k] = rbins[k] * rbins[k]; if (rbins[k] > rmax) rmax = rbins[k]; }
     double search[3] = {rmax, rmax, rmax};
-    int rc = run_walk(K_MARKED, xyz1, n1, xyz2, n2, w1, w2, nw, wfunc, e, nb, NULL, 0, 0, 0,
+    int rc = run_walk(K_MARKED, xyz1, n1, xyz2, n2, w1, w2, nw, wfunc, NULL, NULL, 0, e, nb, NULL, 0, 0, 0,
                       period, pbc, search, approx1, approx2, nthreads, NULL, out);
     free(e);
     return rc;
@@ -533,7 +574,7 @@ int orc_marked_npairs_xy_z(const double *xyz1, int64_t n1, const double *xyz2, i
     for (int k = 0; k < nrp; k++) { e1[k] = rp_bins[k] * rp_bins[k]; if (rp_bins[k] > rpmax) rpmax = rp_bins[k]; }
     for (int k = 0; k < npi; k++) { e2[k] = pi_bins[k] * pi_bins[k]; if (pi_bins[k] > pimax) pimax = pi_bins[k]; }
     double search[3] = {rpmax, rpmax, pimax};
-    int rc = run_walk(K_XYZ_MARKED, xyz1, n1, xyz2, n2, w1, w2, nw, wfunc, e1, nrp, e2, npi, 0, 0,
+    int rc = run_walk(K_XYZ_MARKED, xyz1, n1, xyz2, n2, w1, w2, nw, wfunc, NULL, NULL, 0, e1, nrp, e2, npi, 0, 0,
                       period, pbc, search, approx1, approx2, nthreads, NULL, out);
     free(e1);
     return rc;
@@ -556,8 +597,29 @@ int orc_weighted_npairs_s_mu(const double *xyz1, int64_t n1, const double *xyz2,
     for (int k = 0; k < ns; k++) { if (isnan(e1[k]) || isnan(smax2)) smax2 = NAN; else if (e1[k] > smax2) smax2 = e1[k]; }
     for (int k = 0; k < nmu; k++) { if (isnan(e2[k]) || isnan(mumax2)) mumax2 = NAN; else if (e2[k] > mumax2) mumax2 = e2[k]; }
     double search[3] = {smax, smax, smax};
-    int rc = run_walk(K_SMU_WEIGHTED, xyz1, n1, xyz2, n2, w1, w2, 1, 0, e1, ns, e2, nmu, smax2,
+    int rc = run_walk(K_SMU_WEIGHTED, xyz1, n1, xyz2, n2, w1, w2, 1, 0, NULL, NULL, 0, e1, ns, e2, nmu, smax2,
                       mumax2, period, pbc, search, approx1, approx2, nthreads, counts, wcounts);
+    free(e1);
+    return rc;
+}
+
+/* npairs_jackknife_xy_z_engine: out[s][k][g] = sum of jweight(s, ...) over ordered
+   pairs with dxy <= rp[k]^2 and dz^2 <= pi[g]^2; w1, w2 one weight per point */
+int orc_npairs_jackknife_xy_z(const double *xyz1, int64_t n1, const double *xyz2, int64_t n2,
+                              const double *w1, const double *w2, const int64_t *tags1,
+                              const int64_t *tags2, int nsamp, const double *rp_bins, int nrp,
+                              const double *pi_bins, int npi, const double period[3], int pbc,
+                              const double approx1[3], const double approx2[3], int nthreads,
+                              double *out) {
+    double *e1 = (double *)malloc(sizeof(double) * (size_t)(nrp + npi));
+    if (!e1) return -1;
+    double *e2 = e1 + nrp;
+    double rpmax = rp_bins[0], pimax = pi_bins[0];
+    for (int k = 0; k < nrp; k++) { e1[k] = rp_bins[k] * rp_bins[k]; if (rp_bins[k] > rpmax) rpmax = rp_bins[k]; }
+    for (int k = 0; k < npi; k++) { e2[k] = pi_bins[k] * pi_bins[k]; if (pi_bins[k] > pimax) pimax = pi_bins[k]; }
+    double search[3] = {rpmax, rpmax, pimax};
+    int rc = run_walk(K_XYZ_JACK, xyz1, n1, xyz2, n2, w1, w2, 1, 0, tags1, tags2, nsamp, e1, nrp,
+                      e2, npi, 0, 0, period, pbc, search, approx1, approx2, nthreads, NULL, out);
     free(e1);
     return rc;
 }

@@ -1,5 +1,6 @@
 """Golden vectors for the sibling counters (npairs_projected, npairs_jackknife_3d,
-npairs_per_object_3d, marked_npairs_xy_z, weighted_npairs_s_mu), made by running
+npairs_per_object_3d, marked_npairs_xy_z, weighted_npairs_s_mu,
+npairs_jackknife_xy_z), made by running
 halotools' own front-ends and Cython engines (built by ``oracle/build_ref.py``,
 imported by ``oracle/ref_loader.py``).
 
@@ -99,6 +100,12 @@ CASES = {
     "marked_xy_z_threes_auto_pbc": ("marked_npairs_xy_z", lambda m, s1, s2, t1, t2: m.marked_npairs_xy_z(
         s1, s1, RP, PI, weights1=np.full(len(s1), 3.0), weights2=np.full(len(s1), 3.0),
         weight_func_id=1, period=L)),
+    "jackknife_xy_z_auto_pbc": ("npairs_jackknife_xy_z", lambda m, s1, s2, t1, t2:
+                                m.npairs_jackknife_xy_z(s1, s1, RP, PI, t1, t1, 5, period=L)),
+    "jackknife_xy_z_cross_pbc": ("npairs_jackknife_xy_z", lambda m, s1, s2, t1, t2:
+                                 m.npairs_jackknife_xy_z(s1, s2, RP, PI, t1, t2, 5, period=L)),
+    "jackknife_xy_z_auto_nopbc": ("npairs_jackknife_xy_z", lambda m, s1, s2, t1, t2:
+                                  m.npairs_jackknife_xy_z(s1, s1, RP, PI, t1, t1, 5)),
     "weighted_s_mu_auto_pbc": ("weighted_npairs_s_mu", lambda m, s1, s2, t1, t2: m.weighted_npairs_s_mu(
         s1, s1, _wt()[0], _wt()[0], SB, MU, period=L)),
     "weighted_s_mu_cross_nopbc": ("weighted_npairs_s_mu", lambda m, s1, s2, t1, t2: m.weighted_npairs_s_mu(

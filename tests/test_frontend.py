@@ -111,3 +111,20 @@ def test_weighted_s_mu_messages():
 
 def test_install_into_halotools_without_halotools_is_a_noop():
     assert isinstance(h.install_into_halotools(), list)
+
+
+def test_jackknife_xy_z_messages():
+    t = np.ones(50, dtype=int)
+    with pytest.raises(h.HalotoolsError) as err:
+        h.npairs_jackknife_xy_z(S, S, [0.1, 0.2], [0.1, 0.2], t[:49], t, 1, period=1)
+    assert "jtags1 should have same len as sample1" in str(err.value)
+    with pytest.raises(h.HalotoolsError) as err:
+        h.npairs_jackknife_xy_z(S, S, [0.1, 0.2], [0.1, 0.2], t, t * 3, 2, period=1)
+    assert "jtags2 must be <= N_samples" in str(err.value)
+    with pytest.raises(h.HalotoolsError) as err:
+        h.npairs_jackknife_xy_z(S, S, [0.1, 0.2], [0.1, 0.2], t, t, 1, period=1,
+                                weights1=np.ones(49))
+    assert "weights1 should have same len as sample1" in str(err.value)
+    with pytest.raises(NotImplementedError):
+        h.npairs_jackknife_xy_z(S, S, [0.1, 0.2], [0.1, 0.2], t, t, 1, period=1,
+                                weights1=np.full(50, 2.0))

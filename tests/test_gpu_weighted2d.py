@@ -1,6 +1,7 @@
-"""marked_npairs_xy_z and weighted_npairs_s_mu on the GPU against the C oracle
-(a restatement of marked_npairs_xy_z_engine.pyx and weighted_npairs_s_mu_engine.pyx,
-itself pinned to halotools' engines in test_oracle.py).
+"""marked_npairs_xy_z, weighted_npairs_s_mu and npairs_jackknife_xy_z on the GPU
+against the C oracle (a restatement of marked_npairs_xy_z_engine.pyx,
+weighted_npairs_s_mu_engine.pyx and npairs_jackknife_xy_z_engine.pyx, itself
+pinned to halotools' engines in test_oracle.py).
 
 Sums are FP32 with an exact-error companion moved to FP64 every few thousand
 pairs: 1e-6 relative of the FP64 reference for non-negative marks (signed marks:
@@ -172,3 +173,41 @@ def test_weighted_2d_empty_and_errors(gpu):
                                weights1=np.ones((500, 5)), weights2=np.ones((500, 5)))
     with pytest.raises(AssertionError):
         gpu.weighted_npairs_s_mu(s, s, np.ones(499), np.ones(500), rp, np.linspace(0, 1, 3))
+
+
+# ---------------- npairs_jackknife_xy_z ----------------
+def _cuboid_tags(s, L, n=3):
+    c = np.minimum((s / (L / n)).astype(int), n - 1)
+    return 1 + c[:, 0] * n * n + c[:, 1] * n + c[:, 2]
+
+
+@pytest.mark.parametrize("pbc", [True, False])
+def test_jackknife_xy_z_matches_oracle(gpu, pbc):
+    rng = np.random.default_rng(50)
+    L = 300.0
+    s = clustered(rng, 30000, L, 1500)
+    t = _cuboid_tags(s, L)
+    rp = np.logspace(-1, np.log10(20), 12)
+    pi = np.linspace(0, 25, 11)
+    per = L if pbc else None
+    want = oracle.npairs_jackknife_xy_z(s, s, rp, pi, t, t, 27, period=per, num_threads=8)
+    got = gpu.npairs_jackknife_xy_z(s, s, rp, pi, t, t, 27, period=per)
+    assert got.shape == (28, 12, 11)
+    assert np.array_equal(got, want)
+    assert np.array_equal(got[0], gpu.npairs_xy_z(s, s, rp, pi, period=per).astype(np.float64))
+
+
+def test_jackknife_xy_z_cross_and_blocks(gpu):
+    rng = np.random.default_rng(51)
+    L = 250.0
+    s1 = clustered(rng, 20000, L, 1000)
+    s2 = rng.uniform(0, L, (15000, 3))
+    t1, t2 = _cuboid_tags(s1, L), _cuboid_tags(s2, L)
+    rp = np.logspace(-1, np.log10(15), 10)
+    pi = np.linspace(0, 20, 21)
+    want = oracle.npairs_jackknife_xy_z(s1, s2, rp, pi, t1, t2, 27, period=L, num_threads=8)
+    assert np.array_equal(gpu.npairs_jackknife_xy_z(s1, s2, rp, pi, t1, t2, 27, period=L), want)
+    with forced(gpu, 2) as plan:
+        got = gpu.npairs_jackknife_xy_z(s1, s2, rp, pi, t1, t2, 27, period=L)
+        assert plan.stats()["block"] == 2
+    assert np.array_equal(got, want)

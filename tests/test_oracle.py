@@ -67,11 +67,12 @@ def test_oracle_adjoint_matches_marked_identity():
         assert abs(grad[m] - 2 * np.dot(g, c)) < 1e-9 * max(1.0, abs(grad[m]))
 
 
-# ---- the oracle's weighted 2-D walks against halotools' own engines ----
+# ---- the oracle's weighted and jackknife 2-D walks against halotools' own engines ----
 from tests.golden import make_sibling_golden as S  # noqa: E402
 
 _W2_CASES = sorted(n for n in S.CASES
-                   if S.CASES[n][0] in ("marked_npairs_xy_z", "weighted_npairs_s_mu"))
+                   if S.CASES[n][0] in ("marked_npairs_xy_z", "weighted_npairs_s_mu",
+                                        "npairs_jackknife_xy_z"))
 
 
 @pytest.mark.parametrize("name", _W2_CASES)
