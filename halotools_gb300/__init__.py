@@ -13,13 +13,17 @@ from .pair_counters import (HalotoolsError, marked_npairs_3d, marked_npairs_3d_c
                             npairs_per_object_3d, npairs_projected, npairs_s_mu, npairs_xy_z,
                             weighted_npairs_s_mu)
 from ._native import GBPairsError, GBPairsUnavailable, Plan, default_plan
+from .neighbours import (conditional_cylindrical_isolation, conditional_spherical_isolation,
+                         counts_in_cylinders, cylindrical_isolation, spherical_isolation)
 from .batched import BatchedCounter, npairs_3d_batched
 from . import estimators
 
 __all__ = ("npairs_3d", "npairs_xy_z", "npairs_s_mu", "marked_npairs_3d",
            "marked_npairs_3d_channels", "npairs_projected", "npairs_jackknife_3d",
            "npairs_per_object_3d", "marked_npairs_xy_z", "weighted_npairs_s_mu",
-           "npairs_jackknife_xy_z",
+           "npairs_jackknife_xy_z", "counts_in_cylinders", "spherical_isolation",
+           "cylindrical_isolation", "conditional_spherical_isolation",
+           "conditional_cylindrical_isolation",
            "HalotoolsError", "GBPairsError", "GBPairsUnavailable", "Plan", "default_plan",
            "npairs_3d_batched", "BatchedCounter", "install_into_halotools", "estimators")
 
@@ -38,6 +42,21 @@ _BINDINGS = tuple([
     ("halotools.mock_observables.pair_counters", "marked_npairs_xy_z", marked_npairs_xy_z),
     ("halotools.mock_observables.pair_counters", "weighted_npairs_s_mu", weighted_npairs_s_mu),
     ("halotools.mock_observables.pair_counters", "npairs_jackknife_xy_z", npairs_jackknife_xy_z),
+    ("halotools.mock_observables", "counts_in_cylinders", counts_in_cylinders),
+    ("halotools.mock_observables.counts_in_cells", "counts_in_cylinders", counts_in_cylinders),
+    ("halotools.mock_observables", "spherical_isolation", spherical_isolation),
+    ("halotools.mock_observables", "cylindrical_isolation", cylindrical_isolation),
+    ("halotools.mock_observables", "conditional_spherical_isolation",
+     conditional_spherical_isolation),
+    ("halotools.mock_observables", "conditional_cylindrical_isolation",
+     conditional_cylindrical_isolation),
+    ("halotools.mock_observables.isolation_functions", "spherical_isolation", spherical_isolation),
+    ("halotools.mock_observables.isolation_functions", "cylindrical_isolation",
+     cylindrical_isolation),
+    ("halotools.mock_observables.isolation_functions", "conditional_spherical_isolation",
+     conditional_spherical_isolation),
+    ("halotools.mock_observables.isolation_functions", "conditional_cylindrical_isolation",
+     conditional_cylindrical_isolation),
 ] + [
     # the intrinsic-alignment estimators bind marked_npairs_xy_z at import time
     ("halotools.mock_observables.ia_correlations." + m, "marked_npairs_xy_z", marked_npairs_xy_z)

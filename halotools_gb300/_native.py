@@ -30,7 +30,8 @@ EXPORTED = (
     "gbp_npairs_3d_static", "gbp_batched_npairs_3d", "gbp_plan_set_graph", "gbp_plan_set_autotune",
     "gbp_plan_set_block", "gbp_marked_npairs_3d_channels", "gbp_npairs_jackknife_3d",
     "gbp_npairs_per_object_3d", "gbp_marked_npairs_xy_z", "gbp_weighted_npairs_s_mu",
-    "gbp_npairs_jackknife_xy_z",
+    "gbp_npairs_jackknife_xy_z", "gbp_counts_in_cylinders", "gbp_cylinder_pairs",
+    "gbp_isolation",
     "gbp_weighted_adjoint_3d", "gbp_zheng07_weights", "gbp_zheng07_vjp",
 )
 
@@ -66,6 +67,21 @@ class Stats(ctypes.Structure):
         d = {f: getattr(self, f) for f, _ in self._fields_}
         d["cells"] = list(self.cells)
         return d
+
+
+class NeighCond(ctypes.Structure):
+    """gbp_neigh_cond: the condition a neighbour pair must meet (include/gbpairs.h)."""
+    _fields_ = [
+        ("kind", ctypes.c_int32),
+        ("func", ctypes.c_int32),
+        ("marks1", ctypes.c_void_p),
+        ("marks2", ctypes.c_void_p),
+        ("nmarks", ctypes.c_int32),
+        ("lower_inclusive", ctypes.c_int32),
+        ("upper_inclusive", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+        ("lim", ctypes.c_double * 2),
+    ]
 
 
 _lib = None
@@ -117,6 +133,12 @@ def load(build_if_missing: bool = True):
         L.gbp_npairs_jackknife_3d.argtypes = [vp, vp, i64, vp, i64, vp, vp, i32, pd, i32, pd, i32,
                                               i32, pd]
         L.gbp_npairs_per_object_3d.argtypes = [vp, vp, i64, vp, i64, pd, i32, pd, i32, i32, pi64]
+        pcond = P(NeighCond)
+        L.gbp_counts_in_cylinders.argtypes = [vp, vp, i64, vp, i64, pd, pd, pd, i32, pcond, pi64]
+        L.gbp_cylinder_pairs.argtypes = [vp, vp, i64, vp, i64, pd, pd, pd, i32, pcond, pi64,
+                                         P(ctypes.c_uint32)]
+        L.gbp_isolation.argtypes = [vp, vp, i64, vp, i64, pd, pd, pd, i32, pcond,
+                                    P(ctypes.c_uint8)]
         L.gbp_npairs_jackknife_xy_z.argtypes = [vp, vp, i64, vp, i64, vp, vp, i32, pd, i32, pd,
                                                 i32, pd, i32, i32, pd]
         L.gbp_marked_npairs_xy_z.argtypes = [vp, vp, i64, vp, i64, vp, vp, i32, i32, pd, i32, pd,
@@ -225,3 +247,15 @@ def pd(a: np.ndarray):
 
 def pi64(a: np.ndarray):
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
+
+
+def pu32(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))
+
+
+def pu8(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))
+
+
+def ref(obj):
+    return ctypes.byref(obj)

@@ -149,6 +149,13 @@ struct Call {
     std::vector<unsigned long long> htag;  // jackknife: (ntag, nb+1) pair ends by tag
     std::vector<unsigned> pobj;      // per-object: (n1, nb+1) differential counts, caller's order
     double *grad_out = nullptr;      // adjoint: dL/dw, caller's order, in `mem` memory
+    // per-object neighbours: geometry, separation > 0, condition, output kind
+    int ngeo = 0, nexcl0 = 0, ncond = 0, nout = 0;
+    double ncpar[2] = {0, 0};
+    int nceq[2] = {0, 0};
+    std::vector<long long> poff;     // pair list: first slot per caller-order sample-1 point
+    int64_t npairs = 0;              // pair list: total slots
+    uint32_t *pairs_out = nullptr;   // pair list: (i1, i2) per slot, host memory
     const double *xyz1, *xyz2;
     int64_t n1, n2;
     bool autocorr;
@@ -236,7 +243,13 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
     size_t o_offs = cv.take<int64_t>((size_t)nm + 1);
     const bool adj = c.mode == MODE_ADJ;
     const bool pobj = c.mode == MODE_POBJ;
-    const size_t npobj = pobj ? (size_t)c.n1 * (size_t)(nb0 + 1) : 0;
+    const bool neigh = c.mode == MODE_NEIGH;
+    const size_t npobj = pobj ? (size_t)c.n1 * (size_t)(nb0 + 1) : neigh ? (size_t)c.n1 : 0;
+    const bool plist = neigh && c.nout == 2;
+    size_t o_nthr = cv.take<float4>(neigh ? (size_t)std::max<int64_t>(c.n1, 1) : 1);
+    size_t o_poff = cv.take<long long>(plist ? (size_t)c.n1 + 1 : 1);
+    size_t o_pcur = cv.take<unsigned>(plist ? (size_t)std::max<int64_t>(c.n1, 1) : 1);
+    size_t o_pairs = cv.take<unsigned>(plist ? 2 * (size_t)std::max<int64_t>(c.npairs, 1) : 1);
     size_t o_gt = cv.take<float>((size_t)nb0 + 1);
     size_t o_grad = cv.take<double>(adj && c.mem == GBP_MEM_HOST ? (size_t)c.n1 : 1);
     size_t o_pobj = cv.take<unsigned>(npobj > 0 ? npobj : 1);
@@ -472,6 +485,7 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
                         : c.mode == MODE_ADJ   ? 4
                         : c.mode == MODE_POBJ  ? 4   // the gather kernel's fixed stride
                         : (c.mode == MODE_JACK || c.mode == MODE_JACKXYZ) ? 4
+                        : neigh                ? 4   // the j-slots' sorted indices
                                                : 0;
         // 2-D and wide 1-D histograms: one shared copy per warp while they fit,
         // else the warps add straight into the global histogram
@@ -492,25 +506,56 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
         a.grad = adj ? (c.mem == GBP_MEM_HOST ? at<double>(W, o_grad) : c.grad_out) : nullptr;
         a.pobj = at<unsigned>(W, o_pobj);
         a.err = d_err;
+        if (neigh) {
+            ErrModel em = err_model(c.g);
+            a.nthr = at<float4>(W, o_nthr);
+            a.nerr[0] = em.cmax;
+            a.nerr[1] = em.K;
+            a.nerr[2] = em.Lmax;
+            a.ngeo = c.ngeo;
+            a.nexcl0 = c.nexcl0;
+            a.ncond = c.ncond;
+            a.ncpar[0] = c.ncpar[0];
+            a.ncpar[1] = c.ncpar[1];
+            a.nceq[0] = c.nceq[0];
+            a.nceq[1] = c.nceq[1];
+            a.same = c.autocorr ? 1 : 0;
+            if (plist) {
+                a.poff = at<long long>(W, o_poff);
+                a.pcur = at<unsigned>(W, o_pcur);
+                a.pairs = at<unsigned>(W, o_pairs);
+                CK(cudaMemcpyAsync((void *)a.poff, c.poff.data(), sizeof(long long) * (c.n1 + 1),
+                                   cudaMemcpyHostToDevice, st));
+                CK(cudaMemsetAsync(a.pcur, 0, sizeof(unsigned) * c.n1, st));
+                h2d += (int64_t)(sizeof(long long) * (c.n1 + 1));
+            }
+        }
         int occ = (adj || pobj) ? gbp_adjoint_occupancy(smem, pobj)
+                  : neigh       ? gbp_neigh_occupancy(smem)
                                 : gbp_count_occupancy(c.mode, c.wf, smem);
         if (occ <= 0) return fail(plan, GBP_ERR_INVALID, "count kernel does not fit (smem %zu B)", smem);
         int grid = plan->nsm * occ;
         if (adj) CK(cudaMemsetAsync(a.grad, 0, sizeof(double) * (size_t)c.n1, st));
-        if (pobj) CK(cudaMemsetAsync(a.pobj, 0, sizeof(unsigned) * npobj, st));
+        if (pobj || neigh) CK(cudaMemsetAsync(a.pobj, 0, sizeof(unsigned) * npobj, st));
         if (adj || pobj) CK(gbp_launch_adjoint(a, grid, smem, st, pobj));
+        else if (neigh) CK(gbp_launch_neigh(a, (int)c.n1, c.nout, grid, smem, st));
         else CK(gbp_launch_count(c.mode, c.wf, a, grid, smem, st));
         if (adj && c.mem == GBP_MEM_HOST && c.n1 > 0) {
             CK(cudaMemcpyAsync(c.grad_out, a.grad, sizeof(double) * c.n1, cudaMemcpyDeviceToHost, st));
             d2h += (int64_t)(sizeof(double) * c.n1);
         }
-        if (pobj && npobj) {
+        if (plist && c.npairs > 0) {
+            CK(cudaMemcpyAsync(c.pairs_out, a.pairs, 2 * sizeof(unsigned) * (size_t)c.npairs,
+                               cudaMemcpyDeviceToHost, st));
+            d2h += (int64_t)(2 * sizeof(unsigned) * (size_t)c.npairs);
+        }
+        if ((pobj || (neigh && !plist)) && npobj) {
             // (the caller sized c.pobj; a pageable copy, the call syncs at the end anyway)
             CK(cudaMemcpyAsync(c.pobj.data(), a.pobj, sizeof(unsigned) * npobj,
                                cudaMemcpyDeviceToHost, st));
             d2h += (int64_t)(sizeof(unsigned) * npobj);
         }
-        launches += 1;
+        launches += neigh ? 2 : 1;  // (neighbours: the thresholds pre-pass too)
         CK(rec(plan->ev[2]));
         CK(cudaMemcpyAsync(at<char>(H, h_hist), a.hist, nm * nhist * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
         CK(cudaMemcpyAsync(at<char>(H, h_histd), a.histd, nm * nhist * sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -561,6 +606,8 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
     int err_word = reinterpret_cast<const int *>(hm)[2];
     if (err_word & GBP_ERR_SMEM_LAYOUT)
         return fail(plan, GBP_ERR_CUDA, "internal: kernel shared-memory layout exceeds its launch");
+    if (err_word & GBP_ERR_PAIR_SLOTS)
+        return fail(plan, GBP_ERR_INVALID, "the pair list has more pairs than the given counts");
     if (err_word) return fail(plan, GBP_ERR_RANGE, "positions outside [0, period] or not finite");
     if (reinterpret_cast<const int *>(hm)[3]) {
         // more work items than the estimate: grow and repeat the call
@@ -570,7 +617,7 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
         return run_call(plan, c, hist_host, histd_host);
     }
     hist_host.assign(at<unsigned long long>(H, h_hist), at<unsigned long long>(H, h_hist) + nm * nhist);
-    if (c.mode != MODE_MARK && c.mode != MODE_MARKC && c.mode != MODE_XYZW)
+    if (c.mode != MODE_MARK && c.mode != MODE_MARKC && c.mode != MODE_XYZW && c.mode != MODE_NEIGH)
         add_self_pairs(c, hist_host);
     if (histd_host) histd_host->assign(at<double>(H, h_histd), at<double>(H, h_histd) + nm * nhist);
     if (ntab) c.htag.assign(at<unsigned long long>(H, h_htag), at<unsigned long long>(H, h_htag) + ntab);
@@ -1275,6 +1322,156 @@ int gbp_npairs_jackknife_xy_z(gbp_plan *plan, const double *xyz1, int64_t n1, co
         cumulate_2d(tab.data() + (size_t)sidx * nbin, n_rp, n_pi, Q.data());
         for (size_t k = 0; k < plane; k++) out[(size_t)sidx * plane + k] = C[k] - 0.5 * Q[k];
     }
+    return GBP_OK;
+}
+
+// ---------------- per-object neighbours ----------------
+// Shared set-up of counts_in_cylinders, its pair list and the isolation
+// functions: sample-1 FP64 rows {r or rp, pi, marks...}, sample-2 rows
+// {0, 0, marks...}, the grid for the largest radius, the full stencil.
+static int neigh_setup(gbp_plan *plan, Call &c, std::vector<double> &wa, std::vector<double> &wb,
+                       const double *xyz1, int64_t n1, const double *xyz2, int64_t n2,
+                       const double *r, const double *pi, const double *period3, int32_t pbc,
+                       const gbp_neigh_cond *cond) {
+    int rc = check_common(plan, xyz1, n1, xyz2, n2, period3, pbc, GBP_MEM_HOST);
+    if (rc) return rc;
+    if (n1 > 0 && !r) return fail(plan, GBP_ERR_INVALID, "null radii");
+    const int kind = cond ? cond->kind : 0;
+    const int nm = cond ? cond->nmarks : 0;
+    if (kind < 0 || kind > 2 || nm < 0 || nm > 2 || (kind == 1 && nm != 1) ||
+        (kind == 2 && (cond->func < 0 || cond->func > 6 || nm < 1)))
+        return fail(plan, GBP_ERR_INVALID, "unknown neighbour condition");
+    if (kind && ((n1 > 0 && !cond->marks1) || (n2 > 0 && !cond->marks2)))
+        return fail(plan, GBP_ERR_INVALID, "null marks");
+    double rmax = 0.0, pmax = 0.0;
+    for (int64_t i = 0; i < n1; i++) {
+        const double ri = r[i], pj = pi ? pi[i] : 0.0;
+        if (!(ri >= 0.0 && ri < INFINITY) || !(pj >= 0.0 && pj < INFINITY))
+            return fail(plan, GBP_ERR_INVALID, "radii must be finite and non-negative");
+        rmax = std::max(rmax, ri);
+        pmax = std::max(pmax, pj);
+    }
+    if (!pi) pmax = rmax;
+    // a tiny positive search keeps the grid sane when every radius is 0
+    double search[3] = {std::max(rmax, 1e-300), std::max(rmax, 1e-300), std::max(pmax, 1e-300)};
+    if ((rc = check_search(plan, search, period3))) return rc;
+    const int nw = 2 + nm;
+    const bool same = xyz1 == xyz2 && n1 == n2 && (!kind || cond->marks1 == cond->marks2);
+    wa.assign((size_t)std::max<int64_t>(n1, 1) * nw, 0.0);
+    for (int64_t i = 0; i < n1; i++) {
+        wa[(size_t)i * nw] = r[i];
+        wa[(size_t)i * nw + 1] = pi ? pi[i] : 0.0;
+        for (int k = 0; k < nm; k++) wa[(size_t)i * nw + 2 + k] = cond->marks1[(size_t)i * nm + k];
+    }
+    if (!same) {
+        wb.assign((size_t)std::max<int64_t>(n2, 1) * nw, 0.0);
+        for (int64_t j = 0; j < n2; j++)
+            for (int k = 0; k < nm; k++) wb[(size_t)j * nw + 2 + k] = cond->marks2[(size_t)j * nm + k];
+    }
+    c.mode = MODE_NEIGH;
+    c.xyz1 = xyz1;
+    c.xyz2 = same ? xyz1 : xyz2;
+    c.n1 = n1;
+    c.n2 = n2;
+    c.autocorr = same;  // one sorted copy; the walk is a gather
+    c.mem = GBP_MEM_HOST;
+    c.w1 = wa.data();
+    c.w2 = same ? wa.data() : wb.data();
+    c.nw = nw;
+    c.wf = 0;
+    c.ngeo = pi ? 1 : 0;
+    if (kind == 1) {
+        c.ncond = 1;
+        c.ncpar[0] = cond->lim[0];
+        c.ncpar[1] = cond->lim[1];
+        c.nceq[0] = cond->lower_inclusive ? 1 : 0;
+        c.nceq[1] = cond->upper_inclusive ? 1 : 0;
+    } else if (kind == 2) {
+        c.ncond = 10 + cond->func;
+    }
+    choose_grid(c.g, period3, search, pbc, n2, plan->reach, MAX_CELLS_PER_DIM, 0.0, plan->block);
+    build_stencil(c.g, search, pi ? 1 : 0, false);  // full stencil: each row gathers its own
+    // the pre-filter of the walk: one edge per axis at the largest radius squared
+    ErrModel em = err_model(c.g);
+    if (pi) {
+        std::vector<double> E0(1, search[0] * search[0]), E1(1, search[2] * search[2]);
+        c.naxes = 2;
+        c.ax[0].set(E0, &em, 2);
+        c.ax[1].set(E1, &em, 1);
+        c.ax[0].make_lut(no_qband);
+        c.ax[1].make_lut(no_qband);
+    } else {
+        std::vector<double> E0(1, search[0] * search[0]);
+        c.naxes = 1;
+        c.ax[0].set(E0, &em, 3);
+        c.ax[0].make_lut(no_qband);
+    }
+    return GBP_OK;
+}
+
+int gbp_counts_in_cylinders(gbp_plan *plan, const double *xyz1, int64_t n1, const double *xyz2,
+                            int64_t n2, const double *rp, const double *pi, const double *period3,
+                            int32_t pbc, const gbp_neigh_cond *cond, int64_t *counts) {
+    if (!pi || (n1 > 0 && !counts)) return fail(plan, GBP_ERR_INVALID, "null argument");
+    Call c;
+    std::vector<double> wa, wb;
+    int rc = neigh_setup(plan, c, wa, wb, xyz1, n1, xyz2, n2, rp, pi, period3, pbc, cond);
+    if (rc) return rc;
+    for (int64_t i = 0; i < n1; i++) counts[i] = 0;
+    if (n1 == 0 || n2 == 0) return GBP_OK;
+    c.nout = 0;
+    c.pobj.assign((size_t)n1, 0u);
+    std::vector<unsigned long long> h;
+    if ((rc = run_call(plan, c, h))) return rc;
+    for (int64_t i = 0; i < n1; i++) counts[i] = (int64_t)c.pobj[(size_t)i];
+    return GBP_OK;
+}
+
+int gbp_cylinder_pairs(gbp_plan *plan, const double *xyz1, int64_t n1, const double *xyz2,
+                       int64_t n2, const double *rp, const double *pi, const double *period3,
+                       int32_t pbc, const gbp_neigh_cond *cond, const int64_t *counts,
+                       uint32_t *pairs) {
+    if (!pi || (n1 > 0 && !counts)) return fail(plan, GBP_ERR_INVALID, "null argument");
+    if (n1 > (int64_t)UINT32_MAX || n2 > (int64_t)UINT32_MAX)
+        return fail(plan, GBP_ERR_INVALID, "pair indexes are uint32: at most 2^32 - 1 points");
+    Call c;
+    std::vector<double> wa, wb;
+    int rc = neigh_setup(plan, c, wa, wb, xyz1, n1, xyz2, n2, rp, pi, period3, pbc, cond);
+    if (rc) return rc;
+    c.poff.assign((size_t)n1 + 1, 0);
+    int64_t tot = 0;
+    for (int64_t i = 0; i < n1; i++) {
+        if (counts[i] < 0) return fail(plan, GBP_ERR_INVALID, "negative count");
+        c.poff[(size_t)i] = tot;
+        tot += counts[i];
+    }
+    c.poff[(size_t)n1] = tot;
+    if (tot == 0 || n2 == 0) return GBP_OK;
+    if (!pairs) return fail(plan, GBP_ERR_INVALID, "null pair buffer");
+    c.nout = 2;
+    c.npairs = tot;
+    c.pairs_out = pairs;
+    std::vector<unsigned long long> h;
+    return run_call(plan, c, h);
+}
+
+int gbp_isolation(gbp_plan *plan, const double *xyz1, int64_t n1, const double *xyz2, int64_t n2,
+                  const double *r, const double *pi, const double *period3, int32_t pbc,
+                  const gbp_neigh_cond *cond, uint8_t *is_isolated) {
+    if (n1 > 0 && !is_isolated) return fail(plan, GBP_ERR_INVALID, "null output");
+    if (cond && cond->kind == 1) return fail(plan, GBP_ERR_INVALID, "isolation takes marking functions");
+    Call c;
+    std::vector<double> wa, wb;
+    int rc = neigh_setup(plan, c, wa, wb, xyz1, n1, xyz2, n2, r, pi, period3, pbc, cond);
+    if (rc) return rc;
+    for (int64_t i = 0; i < n1; i++) is_isolated[i] = 1;
+    if (n1 == 0 || n2 == 0) return GBP_OK;
+    c.nout = 1;
+    c.nexcl0 = 1;  // a neighbour sits at separation > 0
+    c.pobj.assign((size_t)n1, 0u);
+    std::vector<unsigned long long> h;
+    if ((rc = run_call(plan, c, h))) return rc;
+    for (int64_t i = 0; i < n1; i++) is_isolated[i] = c.pobj[(size_t)i] ? 0 : 1;
     return GBP_OK;
 }
 

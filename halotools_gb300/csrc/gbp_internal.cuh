@@ -30,7 +30,8 @@ enum { MODE_3D = 0, MODE_XYZ = 1, MODE_SMU = 2, MODE_MARK = 3, MODE_ADJ = 4, MOD
        MODE_POBJ = 8,     // per-object counts (gather walk of the adjoint)
        MODE_XYZW = 9,     // (rp, pi) sums of a marking function (marked_npairs_xy_z)
        MODE_SMUW = 10,    // (s, mu') counts and w1 * w2 sums (weighted_npairs_s_mu)
-       MODE_JACKXYZ = 11 };  // (rp, pi) counts plus a global (tag, bin) table of pair ends
+       MODE_JACKXYZ = 11,    // (rp, pi) counts plus a global (tag, bin) table of pair ends
+       MODE_NEIGH = 12 };    // per-object neighbours in per-point spheres / cylinders
 
 // Pair geometry of a count mode: (rp, pi) cylinders or (s, mu') cones; every
 // other mode measures 3-D separations
@@ -110,6 +111,19 @@ struct CountArgs {
     const float *gt;        // gt[b] = sum of the upstream gradient over cumulative bins >= b
     const int *orig;        // sorted position -> caller's index
     double *grad;           // dL/dw in the caller's order
+    // per-object neighbours (MODE_NEIGH): sample 1 rows of w64_1 hold
+    // {r or rp, pi, marks...}, sample 2 rows {0, 0, marks...}
+    float4 *nthr;           // per sorted sample-1 point: FP32 guard thresholds
+    double nerr[3];         // error model: cell size bound, reach, box size bound
+    int ngeo;               // 0: sphere s^2 < r^2; 1: cylinder dxy^2 < rp^2 and dz^2 < pi^2
+    int nexcl0;             // isolation: a neighbour needs separation > 0
+    int ncond;              // 0 none; 1 mass fraction; 10 + id: isolation marking function id
+    double ncpar[2];        // mass fraction limits (fmin, fmax)
+    int nceq[2];            // mass fraction: lower / upper bound inclusive
+    int same;               // sample 2 is sample 1 (same indices)
+    const long long *poff;  // pair list: first slot of each caller-order sample-1 point (n1 + 1)
+    unsigned *pcur;         // pair list: slots taken per point
+    unsigned *pairs;        // pair list: (i1, i2) caller indices
 };
 
 // Shared-memory layout of the count kernel, identical on host and device.
@@ -139,7 +153,7 @@ __host__ __device__ inline SmemLayout gbp_smem_layout(int mode, int T0, int T1, 
     int o = 0;
     // adjoint: float4 tables {b0, thr, lo, qband}; count kernels: u32 table
     // {b0 | threshold-pair index << 16} and the threshold pairs (hi, lo)
-    const bool adj = mode == MODE_ADJ || mode == MODE_POBJ;  // the gather kernel
+    const bool adj = mode == MODE_ADJ || mode == MODE_POBJ || mode == MODE_NEIGH;  // gather kernels
     L.off_lut0 = o; o += adj ? T0 * 16 : gbp_align(T0 * 4, 16);
     L.off_lut1 = o; o += adj ? T1 * 16 : gbp_align(T1 * 4, 16);
     const bool smu = gbp_mode_smu(mode);
@@ -176,6 +190,8 @@ __host__ __device__ inline SmemLayout gbp_smem_layout(int mode, int T0, int T1, 
         hist_bytes = GBP_WARPS * (nb0 + 1) * 32 * 4 * 2;      // lane-private FP32 sum + compensation
     } else if (mode == MODE_ADJ) {
         hist_bytes = GBP_BLOCK * 8 + gbp_align((nb0 + 1) * 4, 16);  // partial sums + gt table
+    } else if (mode == MODE_NEIGH) {
+        hist_bytes = 0;                                       // counters live in registers
     } else if (mode == MODE_POBJ) {
         hist_bytes = GBP_WARPS * 2 * (nb0 + 1) * 32 * 4;      // lane-private counters, 2 points
     } else if (mode == MODE_3DS) {
@@ -191,6 +207,7 @@ __host__ __device__ inline SmemLayout gbp_smem_layout(int mode, int T0, int T1, 
 }
 
 #define GBP_ERR_SMEM_LAYOUT 2
+#define GBP_ERR_PAIR_SLOTS 4  // a pair-list pass found more pairs than the counts gave
 
 // True (and the error bit set) when the kernel's own shared-memory layout does
 // not fit the dynamic shared memory it was launched with; the kernel then
@@ -272,6 +289,11 @@ cudaError_t gbp_count_set_smem(size_t smem);
 cudaError_t gbp_launch_adjoint(const CountArgs &a, int grid, size_t smem, cudaStream_t st,
                                bool per_object = false);
 int gbp_adjoint_occupancy(size_t smem, bool per_object = false);
+// per-object neighbours: thresholds pre-pass then k_neigh<geometry, out>
+// (out 0 counts, 1 has-neighbour flags, 2 pair list)
+cudaError_t gbp_launch_neigh(const CountArgs &a, int n1, int out, int grid, size_t smem,
+                             cudaStream_t st);
+int gbp_neigh_occupancy(size_t smem);
 struct Zheng07 {
     double logMmin, sigma, logM0, logM1, alpha;
     // derived on the host once per call (FP64 transcendentals are slow on the GPU)

@@ -135,6 +135,64 @@ int gbp_marked_npairs_3d(gbp_plan *plan, const double *xyz1, int64_t n1, const d
                          const double *period3, int32_t pbc, int32_t mem, double *out);
 
 /*
+ * Condition a neighbour pair (i, j) must meet besides its separation.
+ * kind 0: none.  kind 1: the mass fraction of counts_in_cylinders
+ * (counts_in_cells/engines/conditions/conditions.pyx, MassFrac.func):
+ * f = marks2[j] / marks1[i] (1 when both are 0, inf when only marks1[i] is)
+ * within (lim[0], lim[1]), each bound inclusive when its flag is set; nmarks 1.
+ * kind 2: marking function `func` 0..6 of the conditional isolation functions
+ * (isolation_functions/engines/isolation_criteria_marking_functions.pyx) on
+ * (n, nmarks) row-major FP64 marks, nmarks 1 or 2.  Marks in caller order.
+ */
+typedef struct {
+    int32_t kind;
+    int32_t func;
+    const double *marks1;
+    const double *marks2;
+    int32_t nmarks;
+    int32_t lower_inclusive;
+    int32_t upper_inclusive;
+    int32_t reserved;
+    double lim[2];
+} gbp_neigh_cond;
+
+/*
+ * counts[i] = number of sample-2 points j with dx^2 + dy^2 < rp[i]^2 and
+ * dz^2 < pi[i]^2 (strict, FP64 in the reference's order, radii squared in
+ * FP64) that meet `cond` (NULL: none).  Replaces counts_in_cylinders_engine
+ * (counts_in_cells/engines/counts_in_cylinders_engine.pyx:255-281) and the
+ * mesh and Pool fan-out of counts_in_cylinders (counts_in_cylinders.py:27-195);
+ * the front-end subtracts the self match for its auto-correlation.  Host
+ * memory; rp, pi per sample-1 point.
+ */
+int gbp_counts_in_cylinders(gbp_plan *plan, const double *xyz1, int64_t n1, const double *xyz2,
+                            int64_t n2, const double *rp, const double *pi,
+                            const double *period3, int32_t pbc, const gbp_neigh_cond *cond,
+                            int64_t *counts);
+
+/*
+ * The pairs behind gbp_counts_in_cylinders' counts (its return_indexes):
+ * given those counts, writes (i1, i2) caller indices, 2 x sum(counts) uint32,
+ * the pairs of point i in slots [sum(counts[:i]), sum(counts[:i+1])) in no
+ * particular order.
+ */
+int gbp_cylinder_pairs(gbp_plan *plan, const double *xyz1, int64_t n1, const double *xyz2,
+                       int64_t n2, const double *rp, const double *pi, const double *period3,
+                       int32_t pbc, const gbp_neigh_cond *cond, const int64_t *counts,
+                       uint32_t *pairs);
+
+/*
+ * is_isolated[i] = 1 when no sample-2 point lies at separation > 0 inside
+ * point i's sphere (pi == NULL: s^2 < r[i]^2) or cylinder (dx^2 + dy^2 <
+ * r[i]^2 and dz^2 < pi[i]^2) while meeting `cond` (NULL, or kind 2).
+ * Replaces spherical_isolation_engine, cylindrical_isolation_engine and their
+ * marked forms (isolation_functions/engines/*_isolation_engine.pyx).
+ */
+int gbp_isolation(gbp_plan *plan, const double *xyz1, int64_t n1, const double *xyz2, int64_t n2,
+                  const double *r, const double *pi, const double *period3, int32_t pbc,
+                  const gbp_neigh_cond *cond, uint8_t *is_isolated);
+
+/*
  * Jackknife (r_p, pi) pair counts, as npairs_jackknife_xy_z
  * (npairs_jackknife_xy_z.py:23-26, engine npairs_jackknife_xy_z_engine.pyx:231-281)
  * without weights: out[0][k][g] is the cumulative count, out[s][k][g]

@@ -28,6 +28,8 @@ OUT = os.path.join(HERE, "_ref")
 DEFAULT_SRC = "/root/reference"
 
 PC = os.path.join("halotools", "mock_observables", "pair_counters")
+CIC = os.path.join("halotools", "mock_observables", "counts_in_cells")
+ISO = os.path.join("halotools", "mock_observables", "isolation_functions")
 # engines on the pair-counting path, plus the cimported marking-function modules
 ENGINES = [
     (os.path.join(PC, "cpairs"), "npairs_3d_engine"),
@@ -42,6 +44,14 @@ ENGINES = [
     (os.path.join(PC, "marked_cpairs"), "custom_marking_func"),
     (os.path.join(PC, "marked_cpairs"), "marked_npairs_3d_engine"),
     (os.path.join(PC, "marked_cpairs"), "marked_npairs_xy_z_engine"),
+    # per-object neighbours: counts in cylinders and the isolation functions
+    (os.path.join(CIC, "engines", "conditions"), "conditions"),
+    (os.path.join(CIC, "engines"), "counts_in_cylinders_engine"),
+    (os.path.join(ISO, "engines"), "isolation_criteria_marking_functions"),
+    (os.path.join(ISO, "engines"), "spherical_isolation_engine"),
+    (os.path.join(ISO, "engines"), "cylindrical_isolation_engine"),
+    (os.path.join(ISO, "engines"), "marked_spherical_isolation_engine"),
+    (os.path.join(ISO, "engines"), "marked_cylindrical_isolation_engine"),
 ]
 
 

@@ -50,6 +50,8 @@ def lib():
                                                pd, pd, i, pi64, pd]
         L.orc_npairs_jackknife_xy_z.argtypes = [pd, i64, pd, i64, pd, pd, pi64, pi64, i, pd, i,
                                                 pd, i, pd, i, pd, pd, i, pd]
+        L.orc_neighbours.argtypes = [pd, i64, pd, i64, pd, pd, pd, pd, i, i, i, d, d, i, i, i,
+                                     pd, i, pd, pd, i, pi64]
         L.orc_bf_npairs_3d.argtypes = [pd, i64, pd, i64, pd, i, pd, i, pi64]
         L.orc_weighted_adjoint_3d.argtypes = [pd, i64, pd, pd, i, pd, i, pd, i, pd]
         _lib = L
@@ -242,6 +244,90 @@ def npairs_jackknife_xy_z(sample1, sample2, rp_bins, pi_bins, jtags1, jtags2, N_
                                            len(pi), _p(lbox), pbc, _p(a1), _p(a2),
                                            int(num_threads), _p(out)))
     return out
+
+
+def _neighbours(sample1, sample2, r, pi, period, marks1=None, marks2=None, ckind=0, cfunc=0,
+                lim=(0.0, 0.0), eq=(False, False), excl0=0, num_threads=1):
+    n1, n2 = len(sample1), len(sample2)
+    r = np.ascontiguousarray(r, dtype=np.float64)
+    pic = None if pi is None else np.ascontiguousarray(pi, dtype=np.float64)
+    rm = float(np.max(r)) if n1 else 0.0
+    pm = (float(np.max(pic)) if n1 else 0.0) if pic is not None else rm
+    x1, x2, lbox, pbc = _geometry(sample1, sample2, [rm, rm, pm], period)
+    a1 = _approx(None, [rm, rm, pm])
+    nm = 0
+    m1 = m2 = np.zeros(1)
+    if marks1 is not None:
+        m1 = np.ascontiguousarray(marks1, dtype=np.float64).reshape(n1, -1)
+        m2 = np.ascontiguousarray(marks2, dtype=np.float64).reshape(n2, -1)
+        nm = m1.shape[1]
+    out = np.zeros(max(n1, 1), dtype=np.int64)
+    _check(lib().orc_neighbours(_p(x1), n1, _p(x2), n2, _p(r),
+                                _p(pic) if pic is not None else None, _p(m1), _p(m2), nm,
+                                int(ckind), int(cfunc), float(lim[0]), float(lim[1]),
+                                int(bool(eq[0])), int(bool(eq[1])), int(excl0), _p(lbox), pbc,
+                                _p(a1), _p(a1), int(num_threads), _pi(out)))
+    return out[:n1]
+
+
+def counts_in_cylinders(sample1, sample2, proj_search_radius, cylinder_half_length,
+                        period=None, num_threads=1, condition=None, condition_args=()):
+    """counts_in_cylinders.py:27-195 driving counts_in_cylinders_engine.pyx:255-281."""
+    autocorr = sample2 is None
+    s2 = sample1 if autocorr else sample2
+    n1 = len(sample1)
+    rp = np.zeros(n1) + np.atleast_1d(proj_search_radius).astype("f8") if \
+        np.size(proj_search_radius) == 1 else np.asarray(proj_search_radius, dtype=np.float64)
+    pi = np.zeros(n1) + np.atleast_1d(cylinder_half_length).astype("f8") if \
+        np.size(cylinder_half_length) == 1 else np.asarray(cylinder_half_length, dtype=np.float64)
+    kw = {}
+    if condition == "mass_frac":
+        eq = list(condition_args[3:]) + [False, False]
+        kw = dict(marks1=condition_args[0], marks2=condition_args[1], ckind=1,
+                  lim=condition_args[2], eq=eq[:2])
+    c = _neighbours(sample1, s2, rp, pi, period, num_threads=num_threads, **kw)
+    return c - 1 if autocorr else c
+
+
+def isolation(sample1, sample2, r, pi=None, period=None, marks1=None, marks2=None, cond_func=None,
+              num_threads=1):
+    """spherical / cylindrical isolation (pi None: spheres), conditional with a
+    marking function id when cond_func is given (isolation_functions/engines)."""
+    kw = {}
+    if cond_func is not None:
+        kw = dict(marks1=marks1, marks2=marks2, ckind=2, cfunc=cond_func)
+    c = _neighbours(sample1, sample2, r, pi, period, excl0=1, num_threads=num_threads, **kw)
+    return c == 0
+
+
+def spherical_isolation(sample1, sample2, r_max, period=None, num_threads=1):
+    """spherical_isolation.py:27-113 driving spherical_isolation_engine.pyx:190-199."""
+    r = np.zeros(len(sample1)) + np.asarray(r_max, dtype=np.float64)
+    return isolation(sample1, sample2, r, None, period, num_threads=num_threads)
+
+
+def cylindrical_isolation(sample1, sample2, rp_max, pi_max, period=None, num_threads=1):
+    """cylindrical_isolation.py:28-137 driving cylindrical_isolation_engine.pyx:198-208."""
+    n = len(sample1)
+    return isolation(sample1, sample2, np.zeros(n) + np.asarray(rp_max, dtype=np.float64),
+                     np.zeros(n) + np.asarray(pi_max, dtype=np.float64), period,
+                     num_threads=num_threads)
+
+
+def conditional_spherical_isolation(sample1, sample2, r_max, marks1=None, marks2=None,
+                                    cond_func=0, period=None, num_threads=1):
+    """conditional_spherical_isolation.py:25-150 (marked_spherical_isolation_engine.pyx)."""
+    r = np.zeros(len(sample1)) + np.asarray(r_max, dtype=np.float64)
+    return isolation(sample1, sample2, r, None, period, marks1, marks2, cond_func, num_threads)
+
+
+def conditional_cylindrical_isolation(sample1, sample2, rp_max, pi_max, marks1=None, marks2=None,
+                                      cond_func=0, period=None, num_threads=1):
+    """conditional_cylindrical_isolation.py:25-160 (marked_cylindrical_isolation_engine.pyx)."""
+    n = len(sample1)
+    return isolation(sample1, sample2, np.zeros(n) + np.asarray(rp_max, dtype=np.float64),
+                     np.zeros(n) + np.asarray(pi_max, dtype=np.float64), period, marks1, marks2,
+                     cond_func, num_threads)
 
 
 def brute_force_npairs_3d(sample1, sample2, rbins, period=None):

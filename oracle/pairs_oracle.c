@@ -129,7 +129,7 @@ static void mesh_free(mesh_t *m) {
 }
 
 enum { K_3D = 0, K_XYZ = 1, K_SMU = 2, K_MARKED = 3, K_XYZ_MARKED = 4, K_SMU_WEIGHTED = 5,
-       K_XYZ_JACK = 6 };
+       K_XYZ_JACK = 6, K_NEIGH = 7 };
 
 typedef struct {
     int kind;
@@ -143,6 +143,9 @@ typedef struct {
     int nw, wfunc;
     int64_t *t1, *t2; /* jackknife tags, sorted like the positions */
     int nsamp;
+    /* per-object neighbours: rows of w1 are {r or rp, pi, marks}, of w2 {0, 0, marks} */
+    int geo, excl0, ckind, cfunc, ceq0, ceq1;
+    double clim0, clim1;
     /* squared bin edges */
     const double *e1;
     int n1e;
@@ -164,6 +167,30 @@ static double jweight(int64_t j, int64_t j1, int64_t j2, double w1, double w2) {
     if (j1 == j2 && j1 == j) return 0.0;
     if (j1 != j && j2 != j) return w1 * w2;
     return 0.5 * (w1 * w2);
+}
+
+/* conditions.pyx MassFrac.func (counts_in_cylinders' "mass_frac") */
+static int mass_frac_ok(const walk_t *w, double m1, double m2) {
+    double f;
+    if (m1 == 0.0) f = (m2 == 0.0) ? 1.0 : INFINITY;
+    else f = m2 / m1;
+    int t1 = w->ceq0 ? (w->clim0 <= f) : (w->clim0 < f);
+    int t2 = w->ceq1 ? (f <= w->clim1) : (f < w->clim1);
+    return t1 && t2;
+}
+
+/* isolation_criteria_marking_functions.pyx:30-136 */
+static int iso_cond(int id, const double *a, const double *b) {
+    switch (id) {
+    case 0: return 1;
+    case 1: return a[0] > b[0];
+    case 2: return a[0] < b[0];
+    case 3: return a[0] == b[0];
+    case 4: return a[0] != b[0];
+    case 5: return a[0] > (b[0] + a[1]);
+    case 6: return a[0] < (b[0] + a[1]);
+    default: return 0;
+    }
 }
 
 /* marking_functions.pyx:21-218 (ids 1-17); id 0 is the custom hook, zero. */
@@ -307,6 +334,27 @@ static void walk_range(const walk_t *w, int64_t c0, int64_t c1, int64_t *ic, dou
                                         if (k < 0) break;
                                     }
                                 }
+                            } else if (w->kind == K_NEIGH) {
+                                /* counts_in_cylinders_engine.pyx:262-281,
+                                   spherical_isolation_engine.pyx:190-199,
+                                   cylindrical_isolation_engine.pyx:198-208 and the marked
+                                   isolation engines: strict tests, radii squared in FP64 */
+                                const double *a = w->w1 + i * w->nw, *b = w->w2 + j * w->nw;
+                                const double r2 = a[0] * a[0];
+                                int in;
+                                if (w->geo == 0) {
+                                    double dsq = dx * dx + dy * dy + dz * dz;
+                                    in = dsq < r2;
+                                    if (in && w->excl0) in = dsq > 0.0;
+                                } else {
+                                    double dxy = dx * dx + dy * dy;
+                                    double dzz = dz * dz;
+                                    in = (dxy < r2) && (dzz < a[1] * a[1]);
+                                    if (in && w->excl0) in = (dzz + dxy) > 0.0;
+                                }
+                                if (in && w->ckind == 1) in = mass_frac_ok(w, a[2], b[2]);
+                                if (in && w->ckind == 2) in = iso_cond(w->cfunc, a + 2, b + 2);
+                                if (in) ic[i] += 1;
                             } else { /* K_SMU, K_SMU_WEIGHTED */
                                 double dxy = dx * dx + dy * dy;
                                 double dzz = dz * dz;
@@ -356,9 +404,14 @@ static int run_walk(int kind, const double *xyz1, int64_t n1, const double *xyz2
                     double smax2, double mumax2,
                     const double period[3], int pbc, const double search[3],
                     const double approx1[3], const double approx2[3], int nthreads,
-                    int64_t *icounts, double *dcounts) {
+                    int64_t *icounts, double *dcounts, const walk_t *nopt) {
     walk_t w;
     memset(&w, 0, sizeof(w));
+    if (nopt) {
+        /* per-object neighbours: geometry, separation > 0, condition */
+        w.geo = nopt->geo; w.excl0 = nopt->excl0; w.ckind = nopt->ckind; w.cfunc = nopt->cfunc;
+        w.ceq0 = nopt->ceq0; w.ceq1 = nopt->ceq1; w.clim0 = nopt->clim0; w.clim1 = nopt->clim1;
+    }
     w.kind = kind;
     w.pbc = pbc;
     for (int d = 0; d < 3; d++) {
@@ -397,7 +450,8 @@ static int run_walk(int kind, const double *xyz1, int64_t n1, const double *xyz2
         for (int64_t k = 0; k < n2; k++) w.t2[k] = tags2[w.m2.order[k]];
         w.nsamp = nsamp;
     }
-    if (kind == K_MARKED || kind == K_XYZ_MARKED || kind == K_SMU_WEIGHTED || kind == K_XYZ_JACK) {
+    if (kind == K_MARKED || kind == K_XYZ_MARKED || kind == K_SMU_WEIGHTED || kind == K_XYZ_JACK ||
+        kind == K_NEIGH) {
         wb = (double *)malloc(sizeof(double) * (size_t)nw * (s1 + s2));
         if (!wb) { free(buf); mesh_free(&w.m1); mesh_free(&w.m2); return -1; }
         w.w1 = wb; w.w2 = wb + (size_t)nw * s1;
@@ -413,6 +467,7 @@ static int run_walk(int kind, const double *xyz1, int64_t n1, const double *xyz2
 
     int64_t nout = (kind == K_3D || kind == K_MARKED) ? n1e : (int64_t)n1e * n2e;
     if (kind == K_XYZ_JACK) nout *= (int64_t)(nsamp + 1);
+    if (kind == K_NEIGH) nout = n1 > 0 ? n1 : 1;  /* one count per sorted sample-1 point */
     double *dsum = NULL;
     if (nthreads < 1) nthreads = 1;
     if (nthreads > w.m1.ncells) nthreads = (int)w.m1.ncells;
@@ -455,6 +510,14 @@ static int run_walk(int kind, const double *xyz1, int64_t n1, const double *xyz2
         }
         if (icounts) icounts[k] = si;
         if (dcounts) dcounts[k] = sd;
+    }
+    if (kind == K_NEIGH && icounts) {
+        /* per sorted point -> caller's order */
+        int64_t *tmp = (int64_t *)malloc(sizeof(int64_t) * (size_t)nout);
+        if (!tmp) { rc = -1; goto done; }
+        memcpy(tmp, icounts, sizeof(int64_t) * (size_t)nout);
+        for (int64_t k = 0; k < n1; k++) icounts[w.m1.order[k]] = tmp[k];
+        free(tmp);
     }
     if (kind == K_SMU_WEIGHTED && dcounts) {
         /* weighted_npairs_s_mu_engine.pyx:251-255: each cell sums its rectangle of the
@@ -500,7 +563,7 @@ int orc_npairs_3d(const double *xyz1, int64_t n1, const double *xyz2, int64_t n2
     for (int k = 0; k < nb; k++) { e[k] = rbins[k] * rbins[k]; if (rbins[k] > rmax) rmax = rbins[k]; }
     double search[3] = {rmax, rmax, rmax};
     int rc = run_walk(K_3D, xyz1, n1, xyz2, n2, NULL, NULL, 0, 0, NULL, NULL, 0, e, nb, NULL, 0, 0, 0,
-                      period, pbc, search, approx1, approx2, nthreads, out, NULL);
+                      period, pbc, search, approx1, approx2, nthreads, out, NULL, NULL);
     free(e);
     return rc;
 }
@@ -517,7 +580,7 @@ int orc_npairs_xy_z(const double *xyz1, int64_t n1, const double *xyz2, int64_t 
     for (int k = 0; k < npi; k++) { e2[k] = pi_bins[k] * pi_bins[k]; if (pi_bins[k] > pimax) pimax = pi_bins[k]; }
     double search[3] = {rpmax, rpmax, pimax};
     int rc = run_walk(K_XYZ, xyz1, n1, xyz2, n2, NULL, NULL, 0, 0, NULL, NULL, 0, e1, nrp, e2, npi, 0, 0,
-                      period, pbc, search, approx1, approx2, nthreads, out, NULL);
+                      period, pbc, search, approx1, approx2, nthreads, out, NULL, NULL);
     free(e1);
     return rc;
 }
@@ -539,7 +602,7 @@ int orc_npairs_s_mu(const double *xyz1, int64_t n1, const double *xyz2, int64_t 
     for (int k = 0; k < nmu; k++) { if (isnan(e2[k]) || isnan(mumax2)) mumax2 = NAN; else if (e2[k] > mumax2) mumax2 = e2[k]; }
     double search[3] = {smax, smax, smax};
     int rc = run_walk(K_SMU, xyz1, n1, xyz2, n2, NULL, NULL, 0, 0, NULL, NULL, 0, e1, ns, e2, nmu, smax2, mumax2,
-                      period, pbc, search, approx1, approx2, nthreads, out, NULL);
+                      period, pbc, search, approx1, approx2, nthreads, out, NULL, NULL);
     free(e1);
     return rc;
 }
@@ -555,7 +618,7 @@ int orc_marked_npairs_3d(const double *xyz1, int64_t n1, const double *xyz2, int
     for (int k = 0; k < nb; k++) { e[k] = rbins[k] * rbins[k]; if (rbins[k] > rmax) rmax = rbins[k]; }
     double search[3] = {rmax, rmax, rmax};
     int rc = run_walk(K_MARKED, xyz1, n1, xyz2, n2, w1, w2, nw, wfunc, NULL, NULL, 0, e, nb, NULL, 0, 0, 0,
-                      period, pbc, search, approx1, approx2, nthreads, NULL, out);
+                      period, pbc, search, approx1, approx2, nthreads, NULL, out, NULL);
     free(e);
     return rc;
 }
@@ -575,7 +638,7 @@ int orc_marked_npairs_xy_z(const double *xyz1, int64_t n1, const double *xyz2, i
     for (int k = 0; k < npi; k++) { e2[k] = pi_bins[k] * pi_bins[k]; if (pi_bins[k] > pimax) pimax = pi_bins[k]; }
     double search[3] = {rpmax, rpmax, pimax};
     int rc = run_walk(K_XYZ_MARKED, xyz1, n1, xyz2, n2, w1, w2, nw, wfunc, NULL, NULL, 0, e1, nrp, e2, npi, 0, 0,
-                      period, pbc, search, approx1, approx2, nthreads, NULL, out);
+                      period, pbc, search, approx1, approx2, nthreads, NULL, out, NULL);
     free(e1);
     return rc;
 }
@@ -598,7 +661,7 @@ int orc_weighted_npairs_s_mu(const double *xyz1, int64_t n1, const double *xyz2,
     for (int k = 0; k < nmu; k++) { if (isnan(e2[k]) || isnan(mumax2)) mumax2 = NAN; else if (e2[k] > mumax2) mumax2 = e2[k]; }
     double search[3] = {smax, smax, smax};
     int rc = run_walk(K_SMU_WEIGHTED, xyz1, n1, xyz2, n2, w1, w2, 1, 0, NULL, NULL, 0, e1, ns, e2, nmu, smax2,
-                      mumax2, period, pbc, search, approx1, approx2, nthreads, counts, wcounts);
+                      mumax2, period, pbc, search, approx1, approx2, nthreads, counts, wcounts, NULL);
     free(e1);
     return rc;
 }
@@ -619,8 +682,46 @@ int orc_npairs_jackknife_xy_z(const double *xyz1, int64_t n1, const double *xyz2
     for (int k = 0; k < npi; k++) { e2[k] = pi_bins[k] * pi_bins[k]; if (pi_bins[k] > pimax) pimax = pi_bins[k]; }
     double search[3] = {rpmax, rpmax, pimax};
     int rc = run_walk(K_XYZ_JACK, xyz1, n1, xyz2, n2, w1, w2, 1, 0, tags1, tags2, nsamp, e1, nrp,
-                      e2, npi, 0, 0, period, pbc, search, approx1, approx2, nthreads, NULL, out);
+                      e2, npi, 0, 0, period, pbc, search, approx1, approx2, nthreads, NULL, out, NULL);
     free(e1);
+    return rc;
+}
+
+/* Per-object neighbours (counts_in_cylinders, the isolation functions): counts[i]
+   = #sample-2 points in point i's sphere (pi == NULL) or cylinder meeting the
+   condition (ckind 0 none, 1 mass fraction on marks column 0, 2 isolation marking
+   function cfunc), separation > 0 when excl0.  marks (n, nmarks) row-major. */
+int orc_neighbours(const double *xyz1, int64_t n1, const double *xyz2, int64_t n2,
+                   const double *r, const double *pi, const double *marks1,
+                   const double *marks2, int nmarks, int ckind, int cfunc, double lim0,
+                   double lim1, int ceq0, int ceq1, int excl0, const double period[3], int pbc,
+                   const double approx1[3], const double approx2[3], int nthreads,
+                   int64_t *counts) {
+    const int nw = 2 + nmarks;
+    size_t s1 = (size_t)(n1 > 0 ? n1 : 1), s2 = (size_t)(n2 > 0 ? n2 : 1);
+    double *wa = (double *)calloc(s1 * nw + s2 * nw, sizeof(double));
+    if (!wa) return -1;
+    double *wb = wa + s1 * nw;
+    double rmax = 0.0, pmax = 0.0;
+    for (int64_t i = 0; i < n1; i++) {
+        wa[i * nw] = r[i];
+        wa[i * nw + 1] = pi ? pi[i] : 0.0;
+        for (int k = 0; k < nmarks; k++) wa[i * nw + 2 + k] = marks1[i * nmarks + k];
+        if (r[i] > rmax) rmax = r[i];
+        if (pi && pi[i] > pmax) pmax = pi[i];
+    }
+    for (int64_t j = 0; j < n2; j++)
+        for (int k = 0; k < nmarks; k++) wb[j * nw + 2 + k] = marks2[j * nmarks + k];
+    if (!pi) pmax = rmax;
+    double search[3] = {rmax, rmax, pmax};
+    walk_t opt;
+    memset(&opt, 0, sizeof(opt));
+    opt.geo = pi ? 1 : 0; opt.excl0 = excl0; opt.ckind = ckind; opt.cfunc = cfunc;
+    opt.ceq0 = ceq0; opt.ceq1 = ceq1; opt.clim0 = lim0; opt.clim1 = lim1;
+    double e = 0.0;
+    int rc = run_walk(K_NEIGH, xyz1, n1, xyz2, n2, wa, wb, nw, 0, NULL, NULL, 0, &e, 1, NULL, 0,
+                      0, 0, period, pbc, search, approx1, approx2, nthreads, counts, NULL, &opt);
+    free(wa);
     return rc;
 }
 

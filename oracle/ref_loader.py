@@ -91,6 +91,27 @@ def load(src_root: str = DEFAULT_SRC):
     mcp.marked_npairs_3d_engine = m.marked_npairs_3d_engine
     m = importlib.import_module(base + ".marked_cpairs.marked_npairs_xy_z_engine")
     mcp.marked_npairs_xy_z_engine = m.marked_npairs_xy_z_engine
+    # counts in cylinders and the isolation functions (engines bound on their packages)
+    mo = os.path.join(ht, "mock_observables")
+    mb = os.path.join(bt, "mock_observables")
+    _pkg("halotools.mock_observables.counts_in_cells", [os.path.join(mo, "counts_in_cells")])
+    ce = _pkg("halotools.mock_observables.counts_in_cells.engines",
+              [os.path.join(mo, "counts_in_cells", "engines"),
+               os.path.join(mb, "counts_in_cells", "engines")])
+    _pkg("halotools.mock_observables.counts_in_cells.engines.conditions",
+         [os.path.join(mo, "counts_in_cells", "engines", "conditions"),
+          os.path.join(mb, "counts_in_cells", "engines", "conditions")])
+    m = importlib.import_module("halotools.mock_observables.counts_in_cells.engines."
+                                "counts_in_cylinders_engine")
+    ce.counts_in_cylinders_engine = m.counts_in_cylinders_engine
+    _pkg("halotools.mock_observables.isolation_functions", [os.path.join(mo, "isolation_functions")])
+    ie = _pkg("halotools.mock_observables.isolation_functions.engines",
+              [os.path.join(mo, "isolation_functions", "engines"),
+               os.path.join(mb, "isolation_functions", "engines")])
+    for name in ("spherical_isolation_engine", "cylindrical_isolation_engine",
+                 "marked_spherical_isolation_engine", "marked_cylindrical_isolation_engine"):
+        m = importlib.import_module("halotools.mock_observables.isolation_functions.engines." + name)
+        setattr(ie, name, getattr(m, name))
     return _namespace()
 
 
@@ -112,6 +133,16 @@ def _namespace():
         base + ".marked_npairs_xy_z").marked_npairs_xy_z
     ns.npairs_jackknife_xy_z = importlib.import_module(
         base + ".npairs_jackknife_xy_z").npairs_jackknife_xy_z
+    ns.counts_in_cylinders = importlib.import_module(
+        "halotools.mock_observables.counts_in_cells.counts_in_cylinders").counts_in_cylinders
+    iso = "halotools.mock_observables.isolation_functions."
+    ns.spherical_isolation = importlib.import_module(iso + "spherical_isolation").spherical_isolation
+    ns.cylindrical_isolation = importlib.import_module(
+        iso + "cylindrical_isolation").cylindrical_isolation
+    ns.conditional_spherical_isolation = importlib.import_module(
+        iso + "conditional_spherical_isolation").conditional_spherical_isolation
+    ns.conditional_cylindrical_isolation = importlib.import_module(
+        iso + "conditional_cylindrical_isolation").conditional_cylindrical_isolation
     ns.pairs = importlib.import_module(base + ".pairs")
     ns.HalotoolsError = importlib.import_module("halotools.custom_exceptions").HalotoolsError
     return ns

@@ -1,6 +1,6 @@
 """Golden vectors for the sibling counters (npairs_projected, npairs_jackknife_3d,
 npairs_per_object_3d, marked_npairs_xy_z, weighted_npairs_s_mu,
-npairs_jackknife_xy_z), made by running
+npairs_jackknife_xy_z, counts_in_cylinders and the isolation functions), made by running
 halotools' own front-ends and Cython engines (built by ``oracle/build_ref.py``,
 imported by ``oracle/ref_loader.py``).
 
@@ -54,9 +54,25 @@ def sibling_weights(seed=12):
     return w1, w2, W1, W2
 
 
+def neigh_inputs(seed=13):
+    """Per-point radii (sphere r, cylinder rp and pi), masses and two-column marks."""
+    s1, s2, _, _ = sibling_inputs()
+    rng = np.random.default_rng(seed)
+    r = rng.uniform(0.5, 5.0, len(s1))
+    rp = rng.uniform(0.5, 4.0, len(s1))
+    pi = rng.uniform(1.0, 8.0, len(s1))
+    # (arithmetic only: a libm power may round differently on another platform,
+    # which would change the inputs' hash)
+    m1 = rng.uniform(1.0, 1.0e4, len(s1))
+    m2 = rng.uniform(1.0, 1.0e4, len(s2))
+    k1 = rng.uniform(0, 3, (len(s1), 2))
+    k2 = rng.uniform(0, 3, (len(s2), 2))
+    return r, rp, pi, m1, m2, k1, k2
+
+
 def input_sha():
     h = hashlib.sha256()
-    for a in sibling_inputs() + sibling_weights():
+    for a in sibling_inputs() + sibling_weights() + neigh_inputs():
         h.update(np.ascontiguousarray(a).tobytes())
     return h.hexdigest()
 
@@ -69,6 +85,17 @@ MU = np.linspace(0.0, 1.0, 11)
 
 def _wt():
     return sibling_weights()
+
+
+def _nb():
+    return neigh_inputs()
+
+
+def _sorted_pairs(r):
+    """(counts, pair list): the pairs as an (n, 2) uint32 array sorted by (i1, i2)."""
+    counts, idx = r
+    idx = np.sort(np.asarray(idx), order=["i1", "i2"])
+    return np.asarray(counts), np.stack([idx["i1"], idx["i2"]], axis=1).astype(np.uint32)
 
 
 # name -> (front-end, call); calls take the module (halotools' or this package's)
@@ -106,6 +133,42 @@ CASES = {
                                  m.npairs_jackknife_xy_z(s1, s2, RP, PI, t1, t2, 5, period=L)),
     "jackknife_xy_z_auto_nopbc": ("npairs_jackknife_xy_z", lambda m, s1, s2, t1, t2:
                                   m.npairs_jackknife_xy_z(s1, s1, RP, PI, t1, t1, 5)),
+    "cic_auto_pbc": ("counts_in_cylinders", lambda m, s1, s2, t1, t2: m.counts_in_cylinders(
+        s1, None, _nb()[1], _nb()[2], period=L)),
+    "cic_cross_pbc": ("counts_in_cylinders", lambda m, s1, s2, t1, t2: m.counts_in_cylinders(
+        s1, s2, _nb()[1], _nb()[2], period=L)),
+    "cic_cross_scalar_nopbc": ("counts_in_cylinders", lambda m, s1, s2, t1, t2:
+                               m.counts_in_cylinders(s1, s2, 2.5, 6.0)),
+    "cic_mass_frac_pbc": ("counts_in_cylinders", lambda m, s1, s2, t1, t2: m.counts_in_cylinders(
+        s1, s2, _nb()[1], _nb()[2], period=L, condition="mass_frac",
+        condition_args=(_nb()[3], _nb()[4], (0.1, 2.0), True, False))),
+    "cic_indexes_auto_pbc": ("counts_in_cylinders", lambda m, s1, s2, t1, t2: _sorted_pairs(
+        m.counts_in_cylinders(s1, None, _nb()[1], _nb()[2], period=L, return_indexes=True))),
+    "cic_indexes_cross_nopbc": ("counts_in_cylinders", lambda m, s1, s2, t1, t2: _sorted_pairs(
+        m.counts_in_cylinders(s2, s1, 1.5, 4.0, return_indexes=True))),
+    "iso_sph_cross_pbc": ("spherical_isolation", lambda m, s1, s2, t1, t2: m.spherical_isolation(
+        s1, s2, _nb()[0], period=L)),
+    "iso_sph_auto_pbc": ("spherical_isolation", lambda m, s1, s2, t1, t2: m.spherical_isolation(
+        s1, s1, _nb()[0], period=L)),
+    "iso_sph_cross_nopbc": ("spherical_isolation", lambda m, s1, s2, t1, t2: m.spherical_isolation(
+        s1, s2, _nb()[0])),
+    "iso_cyl_cross_pbc": ("cylindrical_isolation", lambda m, s1, s2, t1, t2:
+                          m.cylindrical_isolation(s1, s2, _nb()[1], _nb()[2], period=L)),
+    "iso_cyl_auto_pbc": ("cylindrical_isolation", lambda m, s1, s2, t1, t2:
+                         m.cylindrical_isolation(s1, s1, _nb()[1], _nb()[2], period=L)),
+    "iso_csph_f1_pbc": ("conditional_spherical_isolation", lambda m, s1, s2, t1, t2:
+                        m.conditional_spherical_isolation(s1, s2, _nb()[0], _nb()[5][:, 0],
+                                                          _nb()[6][:, 0], 1, period=L)),
+    "iso_csph_f6_auto_pbc": ("conditional_spherical_isolation", lambda m, s1, s2, t1, t2:
+                             m.conditional_spherical_isolation(s1, s1, _nb()[0], _nb()[5],
+                                                               _nb()[5], 6, period=L)),
+    "iso_ccyl_f2_pbc": ("conditional_cylindrical_isolation", lambda m, s1, s2, t1, t2:
+                        m.conditional_cylindrical_isolation(s1, s2, _nb()[1], _nb()[2],
+                                                            _nb()[5][:, 0], _nb()[6][:, 0], 2,
+                                                            period=L)),
+    "iso_ccyl_f5_nopbc": ("conditional_cylindrical_isolation", lambda m, s1, s2, t1, t2:
+                          m.conditional_cylindrical_isolation(s1, s2, _nb()[1], _nb()[2],
+                                                              _nb()[5], _nb()[6], 5)),
     "weighted_s_mu_auto_pbc": ("weighted_npairs_s_mu", lambda m, s1, s2, t1, t2: m.weighted_npairs_s_mu(
         s1, s1, _wt()[0], _wt()[0], SB, MU, period=L)),
     "weighted_s_mu_cross_nopbc": ("weighted_npairs_s_mu", lambda m, s1, s2, t1, t2: m.weighted_npairs_s_mu(

@@ -128,3 +128,30 @@ def test_jackknife_xy_z_messages():
     with pytest.raises(NotImplementedError):
         h.npairs_jackknife_xy_z(S, S, [0.1, 0.2], [0.1, 0.2], t, t, 1, period=1,
                                 weights1=np.full(50, 2.0))
+
+
+def test_neighbour_messages():
+    with pytest.raises(ValueError) as err:
+        h.counts_in_cylinders(S, S, np.ones(3), 0.1, period=1)
+    assert "``proj_search_radius`` must be a scalar or length-Npts1 array" in str(err.value)
+    with pytest.raises(ValueError) as err:
+        h.counts_in_cylinders(S, S, 0.1, np.ones(3), period=1)
+    assert "``cylinder_half_length`` must be a scalar or length-Npts1 array" in str(err.value)
+    with pytest.raises(ValueError) as err:
+        h.counts_in_cylinders(S, S, 0.1, 0.1, period=1, condition="bogus")
+    assert "'condition' must be None or a permitted descriptive string" in str(err.value)
+    with pytest.raises(ValueError) as err:
+        h.spherical_isolation(S, S, 0.0, period=1)
+    assert "bounded positive numbers" in str(err.value)
+    with pytest.raises(ValueError) as err:
+        h.cylindrical_isolation(S, S, np.ones(3), 0.1, period=1)
+    assert "must be the same length as ``sample1``" in str(err.value)
+    with pytest.raises(h.HalotoolsError):
+        h.conditional_spherical_isolation(S, S, 0.1, cond_func=7, period=1)
+    with pytest.raises(ValueError) as err:
+        h.conditional_cylindrical_isolation(S, S, 0.1, 0.1, marks1=np.ones((50, 1)),
+                                            marks2=np.ones((50, 1)), cond_func=5, period=1)
+    assert "there should be 2 marks per point" in str(err.value)
+    with pytest.raises(ValueError) as err:
+        h.spherical_isolation(S, S, 0.5, period=1)
+    assert "cannot be larger than Lbox/3" in str(err.value)
