@@ -411,12 +411,101 @@ def extra_npairs_3d_10m(dev, threads):
             "gpu_over_cpu": gpu / cpu}
 
 
+def extra_siblings_10m(dev, threads):
+    """The sibling engines on the config-5 sample (10M clustered points, L = 2000):
+    marked_npairs_xy_z (id 1, lognormal marks; rp 30 log bins 0.5-50 x pi 26 linear
+    edges 0-50) and weighted_npairs_s_mu (30 x 21 edges) through the C ABI on device
+    memory; counts_in_cylinders (rp 2, pi 10) and spherical_isolation (r 1) through
+    their host-memory front-ends (the count kernel's own time reported beside the
+    call).  CPU: the oracle on the 1/64-volume sub-cube [0, 500)^3, non-periodic."""
+    import torch
+    import halotools_gb300 as H
+    from halotools_gb300 import _native as N
+    from oracle import oracle
+    w = WORKLOADS["3d10m"]
+    x = points_10m()
+    n = len(x)
+    rng = np.random.default_rng(5)
+    mk = rng.lognormal(0.0, 0.5, n)
+    rp = w["bins"]
+    pi = np.linspace(0.0, 50.0, 26)
+    mu = np.linspace(0.0, 1.0, 21)
+    mup = np.sort(np.sin(np.arccos(mu)))
+    xd = torch.from_numpy(x).cuda(dev)
+    wd = torch.from_numpy(np.ascontiguousarray(mk)).cuda(dev)
+    plan = N.Plan(dev)
+    stream = torch.cuda.current_stream(dev)
+    plan.set_stream(stream.cuda_stream)
+    box = np.array([w["L"]] * 3)
+    res = {"points": n}
+    out = np.zeros((len(rp), len(pi)))
+
+    def mxyz():
+        plan.check(plan.lib.gbp_marked_npairs_xy_z(
+            plan.handle, xd.data_ptr(), n, xd.data_ptr(), n, wd.data_ptr(), wd.data_ptr(), 1, 1,
+            N.pd(rp), len(rp), N.pd(pi), len(pi), N.pd(box), 1, N.GBP_MEM_DEVICE, N.pd(out)))
+    t = _time_gpu(stream, mxyz)
+    cnt = np.zeros((len(rp), len(pi)), dtype=np.int64)
+    plan.check(plan.lib.gbp_npairs_xy_z(plan.handle, xd.data_ptr(), n, xd.data_ptr(), n, N.pd(rp),
+                                        len(rp), N.pd(pi), len(pi), N.pd(box), 1,
+                                        N.GBP_MEM_DEVICE, N.pi64(cnt)))
+    pairs = int(cnt[-1, -1])
+    res["marked_xy_z"] = {"ms": t * 1e3, "in_range_pairs": pairs, "pairs_per_s": pairs / t}
+    c2 = np.zeros((len(rp), len(mup)), dtype=np.int64)
+    w2 = np.zeros((len(rp), len(mup)))
+
+    def wsmu():
+        plan.check(plan.lib.gbp_weighted_npairs_s_mu(
+            plan.handle, xd.data_ptr(), n, xd.data_ptr(), n, wd.data_ptr(), wd.data_ptr(),
+            N.pd(rp), len(rp), N.pd(mup), len(mup), N.pd(box), 1, N.GBP_MEM_DEVICE, N.pi64(c2),
+            N.pd(w2)))
+    t = _time_gpu(stream, wsmu)
+    res["weighted_s_mu"] = {"ms": t * 1e3, "in_range_pairs": int(c2[-1, -1]),
+                            "pairs_per_s": int(c2[-1, -1]) / t,
+                            "recheck_pairs": plan.stats()["recheck_pairs"]}
+    # host-memory front-ends: wall time of the call, and the kernel's event time
+    dp = H.default_plan(dev)
+    for name, fn in (("counts_in_cylinders", lambda: H.counts_in_cylinders(x, x, 2.0, 10.0,
+                                                                            period=w["L"])),
+                     ("spherical_isolation", lambda: H.spherical_isolation(x, x, 1.0,
+                                                                            period=w["L"]))):
+        fn()
+        t0 = time.perf_counter()
+        r = fn()
+        dt = time.perf_counter() - t0
+        st = dp.stats()
+        res[name] = {"call_ms": dt * 1e3, "ms_count": st["ms_count"], "ms_build": st["ms_build"],
+                     "points_per_s": n / dt,
+                     "result_sum": int(np.sum(r))}
+    sub = cpu_sample(x, w, 0.25)
+    msub = mk[np.all(x < 0.25 * w["L"], axis=1)]
+    t0 = time.perf_counter()
+    c = oracle.marked_npairs_xy_z(sub, sub, rp, pi, 1, weights1=msub, weights2=msub,
+                                  num_threads=threads)
+    dt = time.perf_counter() - t0
+    cc = oracle.npairs_xy_z(sub, sub, rp, pi, num_threads=threads)
+    res["marked_xy_z"]["cpu_pairs_per_s"] = int(cc[-1, -1]) / dt
+    t0 = time.perf_counter()
+    c, wc = oracle.weighted_npairs_s_mu(sub, sub, msub, msub, rp, mu, num_threads=threads)
+    dt = time.perf_counter() - t0
+    res["weighted_s_mu"]["cpu_pairs_per_s"] = int(c[-1, -1]) / dt
+    t0 = time.perf_counter()
+    oracle.counts_in_cylinders(sub, sub, 2.0, 10.0, num_threads=threads)
+    res["counts_in_cylinders"]["cpu_points_per_s"] = len(sub) / (time.perf_counter() - t0)
+    t0 = time.perf_counter()
+    oracle.isolation(sub, sub, np.ones(len(sub)), None, num_threads=threads)
+    res["spherical_isolation"]["cpu_points_per_s"] = len(sub) / (time.perf_counter() - t0)
+    res.update({"cpu_cores": threads, "cpu_sample_points": len(sub)})
+    return res
+
+
 EXTRAS = {
     "batched_hod64": lambda dev, threads: extra_batched(dev),
     "differentiable_2m": lambda dev, threads: extra_differentiable(dev),
     "npairs_3d_10m": extra_npairs_3d_10m,
     "marked_10m": extra_marked_10m,
     "s_mu_10m": extra_s_mu_10m,
+    "siblings_10m": extra_siblings_10m,
 }
 
 

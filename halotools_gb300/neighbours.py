@@ -53,7 +53,7 @@ def _get_r_max(n1, r_max):
     # isolation_functions_helpers.py:11-35
     r = np.atleast_1d(r_max).astype(float)
     if len(r) == 1:
-        r = np.array([r[0]] * n1)
+        r = np.full(n1, r[0])
     elif len(r) != n1:
         raise ValueError("Input ``r_max`` must be the same length as ``sample1``.")
     if not (np.all(r < np.inf) and np.all(r > 0)):
