@@ -746,10 +746,13 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                 const int exk = __shfl_sync(FULL, incl - cn, k);
                 const float Dx = __shfl_sync(FULL, D.x, k), Dy = __shfl_sync(FULL, D.y, k),
                             Dz = __shfl_sync(FULL, D.z, k);
+                // this lane's j-slot in registers too (the transposed stage 1)
+                float jtx = -GBP_FAR, jty = -GBP_FAR, jtz = -GBP_FAR;
                 if (f < T) {
                     const int j = stk + (f - exk);
                     const float4 p = a.pos2[j];
                     const float tx = p.x + Dx, ty = p.y + Dy, tz = p.z + Dz;
+                    jtx = tx; jty = ty; jtz = tz;
                     jx[lane] = tx; jy[lane] = ty; jz[lane] = tz; jix[lane] = __float_as_int(p.w);
                     jxy[lane] = make_ulonglong2(pk2(tx, tx), pk2(ty, ty));
                     jzz[lane] = pk2(tz, tz);
@@ -776,9 +779,23 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                 // stage 1: the sign bit of R - v is 1 exactly when the pair is out
                 // of range; a funnel shift appends it to the lane's out-mask, so
                 // slot jj lands in bit 31 - jj.  Items of at most 32 points take
-                // the one-point loop.
+                // the one-point loop, items of at most GBP_TRANSPOSE points the
+                // transposed one.
                 unsigned o0 = 0u, o1 = 0u;
-                if (icnt > 32) {
+                if (icnt <= GBP_TRANSPOSE) {
+                    // few i-points: each lane tests its own j-slot against every
+                    // i-point of the item, and a ballot hands i-point i (lane i) its
+                    // in-range bits, slot jj at bit jj
+                    const float4 tj = make_float4(jtx, jty, jtz, 0.f);
+                    unsigned mine = 0u;
+                    for (int i = 0; i < icnt; i++) {
+                        const float4 ui = make_float4(ux[i], uy[i], uz[i], 0.f);
+                        const unsigned in = __ballot_sync(FULL, (int)out_bits<MODE>(ui, tj, R0, R1) >= 0);
+                        if (lane == i) mine = in;
+                    }
+                    o0 = __brev(~mine);
+                    o1 = 0xffffffffu;
+                } else if (icnt > 32) {
                     // both i-points in packed f32x2 arithmetic: v exactly as stage 2
                     // forms it, then R - v
 #pragma unroll 8
@@ -950,8 +967,58 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                             const bool ha = sa < C, hb = sb < C;
                             const PairV ea = entry(ha ? s_code[sa] : 0);
                             const PairV eb = entry(hb ? s_code[sb] : 0);
-                            if (ha) bin_entry(ea, cur_mock);
-                            if (hb) bin_entry(eb, cur_mock);
+                            if (MODE == MODE_3D) {
+                                // both pairs' table lookups first (independent chains
+                                // the scheduler can overlap), then the updates
+                                const float4 ta = lut_entry_c<false>(ea.v0, A0);
+                                const float4 tb = lut_entry_c<false>(eb.v0, A0);
+                                const bool sla = (ea.v0 > ta.z) & !(ea.v0 > ta.y);
+                                const bool slb = (eb.v0 > tb.z) & !(eb.v0 > tb.y);
+                                const int ba = __float_as_int(ta.x) + (ea.v0 > ta.y ? 1 : 0);
+                                const int bb = __float_as_int(tb.x) + (eb.v0 > tb.y ? 1 : 0);
+                                if (ha) {
+                                    if (sla) bin_3d<true>(ea, hl, A0, ix, a);
+                                    else hl[ba * 32] += ea.sym ? 2u : 1u;
+                                }
+                                if (hb) {
+                                    if (slb) bin_3d<true>(eb, hl, A0, ix, a);
+                                    else hl[bb * 32] += eb.sym ? 2u : 1u;
+                                }
+                            } else if (MODE == MODE_XYZ) {
+                                const float4 a0 = lut_entry_c<false>(ea.v0, A0);
+                                const float4 a1 = lut_entry_c<false>(ea.v1, A1);
+                                const float4 b0 = lut_entry_c<false>(eb.v0, A0);
+                                const float4 b1 = lut_entry_c<false>(eb.v1, A1);
+                                const bool sla = ((ea.v0 > a0.z) & !(ea.v0 > a0.y)) |
+                                                 ((ea.v1 > a1.z) & !(ea.v1 > a1.y));
+                                const bool slb = ((eb.v0 > b0.z) & !(eb.v0 > b0.y)) |
+                                                 ((eb.v1 > b1.z) & !(eb.v1 > b1.y));
+                                const int ka = __float_as_int(a0.x) + (ea.v0 > a0.y ? 1 : 0);
+                                const int ga = __float_as_int(a1.x) + (ea.v1 > a1.y ? 1 : 0);
+                                const int kb = __float_as_int(b0.x) + (eb.v0 > b0.y ? 1 : 0);
+                                const int gb = __float_as_int(b1.x) + (eb.v1 > b1.y ? 1 : 0);
+                                if (ha) {
+                                    if (sla) bin_entry(ea, cur_mock);
+                                    else if ((ka < nb0) & (ga < nb1)) {
+                                        if (copies) atomicAdd(&wh[ka * stride2 + ga], ea.sym ? 2u : 1u);
+                                        else atomicAdd(&a.hist[(size_t)cur_mock * a.hist_stride +
+                                                               ka * stride2 + ga],
+                                                       ea.sym ? 2ull : 1ull);
+                                    }
+                                }
+                                if (hb) {
+                                    if (slb) bin_entry(eb, cur_mock);
+                                    else if ((kb < nb0) & (gb < nb1)) {
+                                        if (copies) atomicAdd(&wh[kb * stride2 + gb], eb.sym ? 2u : 1u);
+                                        else atomicAdd(&a.hist[(size_t)cur_mock * a.hist_stride +
+                                                               kb * stride2 + gb],
+                                                       eb.sym ? 2ull : 1ull);
+                                    }
+                                }
+                            } else {
+                                if (ha) bin_entry(ea, cur_mock);
+                                if (hb) bin_entry(eb, cur_mock);
+                            }
                         }
                         if (RQM) rq_drain(cur_mock, 32u);
                         if (W2) {

@@ -142,6 +142,12 @@ struct SmemLayout {
 // Stage-2 i-slots per warp: the lane's first point at slot lane, its second at
 // lane + 48, so that the two never share a shared-memory bank.
 #define GBP_USLOTS 80
+// Items of at most this many i-points run stage 1 transposed (lanes over the
+// j-slots, a loop over the i-points): cheaper than 32 j-steps per lane when the
+// item is small
+#ifndef GBP_TRANSPOSE
+#define GBP_TRANSPOSE 20
+#endif
 __host__ __device__ inline int gbp_uslot(int iu) { return iu + ((iu >> 5) << 4); }
 
 __host__ __device__ inline int gbp_align(int x, int a) { return (x + a - 1) / a * a; }
