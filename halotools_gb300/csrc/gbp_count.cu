@@ -1015,6 +1015,52 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                                                        eb.sym ? 2ull : 1ull);
                                     }
                                 }
+                            } else if (MARK) {
+                                const float4 ta = lut_entry_c<false>(ea.v0, A0);
+                                const float4 tb = lut_entry_c<false>(eb.v0, A0);
+                                const bool sla = (ea.v0 > ta.z) & !(ea.v0 > ta.y);
+                                const bool slb = (eb.v0 > tb.z) & !(eb.v0 > tb.y);
+                                const int ba = __float_as_int(ta.x) + (ea.v0 > ta.y ? 1 : 0);
+                                const int bb = __float_as_int(tb.x) + (eb.v0 > tb.y ? 1 : 0);
+                                if (ha) {
+                                    if (sla) bin_entry(ea, cur_mock);
+                                    else if (ba < nb0) kahan_add(hs, hc, ba, ea.sym ? 2.0f * ea.v1 : ea.v1);
+                                }
+                                if (hb) {
+                                    if (slb) bin_entry(eb, cur_mock);
+                                    else if (bb < nb0) kahan_add(hs, hc, bb, eb.sym ? 2.0f * eb.v1 : eb.v1);
+                                }
+                            } else if (MODE == MODE_SMU && copies) {
+                                // s slots and q = dxy / s^2 of both pairs, then their mu'
+                                // slots and the neighbouring edges, then the updates
+                                const float4 sa4 = lut_entry_c<true>(ea.v0, A0);
+                                const float4 sb4 = lut_entry_c<true>(eb.v0, A0);
+                                const float qa = __fdividef(ea.v1, ea.v0), qb = __fdividef(eb.v1, eb.v0);
+                                const float4 qa4 = lut_entry_c<false>(qa, A1);
+                                const float4 qb4 = lut_entry_c<false>(qb, A1);
+                                const int bsa = __float_as_int(sa4.x) + (ea.v0 > sa4.y ? 1 : 0);
+                                const int bsb = __float_as_int(sb4.x) + (eb.v0 > sb4.y ? 1 : 0);
+                                const int bqa = __float_as_int(qa4.x) + (qa > qa4.y ? 1 : 0);
+                                const int bqb = __float_as_int(qb4.x) + (qb > qb4.y ? 1 : 0);
+                                const float lwa = bqa > 0 ? A1.hi[bqa - 1] : -3.0e38f;
+                                const float upa = bqa < nb1 ? A1.lo[bqa] : 3.0e38f;
+                                const float lwb = bqb > 0 ? A1.hi[bqb - 1] : -3.0e38f;
+                                const float upb = bqb < nb1 ? A1.lo[bqb] : 3.0e38f;
+                                const bool amba = ((ea.v0 > sa4.z) & !(ea.v0 > sa4.y)) |
+                                                  !(qa - lwa > sa4.w) | !(upa - qa > sa4.w) |
+                                                  (qa4.z < -3.0e38f);
+                                const bool ambb = ((eb.v0 > sb4.z) & !(eb.v0 > sb4.y)) |
+                                                  !(qb - lwb > sb4.w) | !(upb - qb > sb4.w) |
+                                                  (qb4.z < -3.0e38f);
+                                // (as bin_smu: past the s gate first, then the guard bands)
+                                if (ha && bsa < nb0) {
+                                    if (amba) bin_entry(ea, cur_mock);
+                                    else if (bqa < nb1) atomicAdd(&wh[bsa * stride2 + bqa], ea.sym ? 2u : 1u);
+                                }
+                                if (hb && bsb < nb0) {
+                                    if (ambb) bin_entry(eb, cur_mock);
+                                    else if (bqb < nb1) atomicAdd(&wh[bsb * stride2 + bqb], eb.sym ? 2u : 1u);
+                                }
                             } else {
                                 if (ha) bin_entry(ea, cur_mock);
                                 if (hb) bin_entry(eb, cur_mock);
