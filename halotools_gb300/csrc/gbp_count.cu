@@ -984,7 +984,7 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                                     if (slb) bin_3d<true>(eb, hl, A0, ix, a);
                                     else hl[bb * 32] += eb.sym ? 2u : 1u;
                                 }
-                            } else if (MODE == MODE_XYZ) {
+                            } else if (XYZF) {
                                 const float4 a0 = lut_entry_c<false>(ea.v0, A0);
                                 const float4 a1 = lut_entry_c<false>(ea.v1, A1);
                                 const float4 b0 = lut_entry_c<false>(eb.v0, A0);
@@ -1000,19 +1000,25 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                                 if (ha) {
                                     if (sla) bin_entry(ea, cur_mock);
                                     else if ((ka < nb0) & (ga < nb1)) {
-                                        if (copies) atomicAdd(&wh[ka * stride2 + ga], ea.sym ? 2u : 1u);
-                                        else atomicAdd(&a.hist[(size_t)cur_mock * a.hist_stride +
-                                                               ka * stride2 + ga],
-                                                       ea.sym ? 2ull : 1ull);
+                                        if (CNT2) {
+                                            if (copies) atomicAdd(&wh[ka * stride2 + ga], ea.sym ? 2u : 1u);
+                                            else atomicAdd(&a.hist[(size_t)cur_mock * a.hist_stride +
+                                                                   ka * stride2 + ga],
+                                                           ea.sym ? 2ull : 1ull);
+                                        }
+                                        sink_add<XS>(wsink, ka * stride2 + ga, ea.sym ? 2 : 1, ea.w);
                                     }
                                 }
                                 if (hb) {
                                     if (slb) bin_entry(eb, cur_mock);
                                     else if ((kb < nb0) & (gb < nb1)) {
-                                        if (copies) atomicAdd(&wh[kb * stride2 + gb], eb.sym ? 2u : 1u);
-                                        else atomicAdd(&a.hist[(size_t)cur_mock * a.hist_stride +
-                                                               kb * stride2 + gb],
-                                                       eb.sym ? 2ull : 1ull);
+                                        if (CNT2) {
+                                            if (copies) atomicAdd(&wh[kb * stride2 + gb], eb.sym ? 2u : 1u);
+                                            else atomicAdd(&a.hist[(size_t)cur_mock * a.hist_stride +
+                                                                   kb * stride2 + gb],
+                                                           eb.sym ? 2ull : 1ull);
+                                        }
+                                        sink_add<XS>(wsink, kb * stride2 + gb, eb.sym ? 2 : 1, eb.w);
                                     }
                                 }
                             } else if (MARK) {
@@ -1030,7 +1036,7 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                                     if (slb) bin_entry(eb, cur_mock);
                                     else if (bb < nb0) kahan_add(hs, hc, bb, eb.sym ? 2.0f * eb.v1 : eb.v1);
                                 }
-                            } else if (MODE == MODE_SMU && copies) {
+                            } else if (SMUF && copies) {
                                 // s slots and q = dxy / s^2 of both pairs, then their mu'
                                 // slots and the neighbouring edges, then the updates
                                 const float4 sa4 = lut_entry_c<true>(ea.v0, A0);
@@ -1055,11 +1061,17 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                                 // (as bin_smu: past the s gate first, then the guard bands)
                                 if (ha && bsa < nb0) {
                                     if (amba) bin_entry(ea, cur_mock);
-                                    else if (bqa < nb1) atomicAdd(&wh[bsa * stride2 + bqa], ea.sym ? 2u : 1u);
+                                    else if (bqa < nb1) {
+                                        atomicAdd(&wh[bsa * stride2 + bqa], ea.sym ? 2u : 1u);
+                                        sink_add<XS>(wsink, bsa * stride2 + bqa, ea.sym ? 2 : 1, ea.w);
+                                    }
                                 }
                                 if (hb && bsb < nb0) {
                                     if (ambb) bin_entry(eb, cur_mock);
-                                    else if (bqb < nb1) atomicAdd(&wh[bsb * stride2 + bqb], eb.sym ? 2u : 1u);
+                                    else if (bqb < nb1) {
+                                        atomicAdd(&wh[bsb * stride2 + bqb], eb.sym ? 2u : 1u);
+                                        sink_add<XS>(wsink, bsb * stride2 + bqb, eb.sym ? 2 : 1, eb.w);
+                                    }
                                 }
                             } else {
                                 if (ha) bin_entry(ea, cur_mock);
