@@ -1573,6 +1573,78 @@ static int zheng07_args(gbp_plan *plan, const double *theta, Zheng07 *th) {
     return GBP_OK;
 }
 
+int gbp_hod_mocks(gbp_plan *plan, const double *halo_xyz, const double *mass, const double *conc,
+                  const double *rvir, int64_t n_halo, const double *thetas, int32_t n_theta,
+                  double lbox, uint64_t seed, int32_t mem, float *gal_xyz, int64_t cap,
+                  int64_t *offsets) {
+    if (!plan) return GBP_ERR_INVALID;
+    if (mem != GBP_MEM_HOST && mem != GBP_MEM_DEVICE) return fail(plan, GBP_ERR_INVALID, "bad memory kind");
+    if (n_halo < 0 || n_theta < 1 || !thetas || !offsets ||
+        (n_halo > 0 && (!halo_xyz || !mass || !conc || !rvir)))
+        return fail(plan, GBP_ERR_INVALID, "null arrays or no parameter vector");
+    if (n_halo > (int64_t)UINT32_MAX) return fail(plan, GBP_ERR_INVALID, "at most 2^32 - 1 halos");
+    if (!(lbox > 0.0 && lbox < INFINITY)) return fail(plan, GBP_ERR_INVALID, "box size must be positive and finite");
+    for (int m = 0; m < n_theta; m++) {
+        const double *t = thetas + 5 * (size_t)m;
+        if (!(t[1] > 0.0) || !std::isfinite(t[0]) || !std::isfinite(t[2]) || !std::isfinite(t[3]) ||
+            !std::isfinite(t[4]))
+            return fail(plan, GBP_ERR_INVALID, "theta %d: sigma_logM must be > 0 and all finite", m);
+    }
+    for (int m = 0; m <= n_theta; m++) offsets[m] = 0;
+    if (n_halo == 0) return GBP_OK;
+    CK(cudaSetDevice(plan->device));
+    cudaStream_t st = plan->stream;
+    const int64_t items = n_halo * (int64_t)n_theta;
+    if (items >= (int64_t)INT32_MAX) return fail(plan, GBP_ERR_INVALID, "too many (theta, halo) pairs");
+    const size_t tb = gbp_hod_theta_bytes();
+    Carve cv;
+    size_t o_in = mem == GBP_MEM_HOST ? cv.take<double>(6 * (size_t)n_halo) : 0;
+    size_t o_logm = cv.take<double>((size_t)n_halo);
+    size_t o_th = cv.take<char>(tb * n_theta);
+    size_t o_cnt = cv.take<int>((size_t)items + 1);
+    size_t o_off = cv.take<int>((size_t)items + 1);
+    size_t o_scan = cv.take<int>(gbp_scan_tmp_ints(items + 1));
+    size_t o_gal = mem == GBP_MEM_HOST && gal_xyz ? cv.take<float>(3 * (size_t)std::max<int64_t>(cap, 1)) : 0;
+    int rc = ensure_work(plan, cv.take<char>(0) + 256);
+    if (rc) return rc;
+    void *W = plan->work.p;
+    const double *dxyz = halo_xyz, *dm = mass, *dc = conc, *dr = rvir;
+    if (mem == GBP_MEM_HOST) {
+        double *in = at<double>(W, o_in);
+        CK(cudaMemcpyAsync(in, halo_xyz, 3 * n_halo * sizeof(double), cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(in + 3 * n_halo, mass, n_halo * sizeof(double), cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(in + 4 * n_halo, conc, n_halo * sizeof(double), cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(in + 5 * n_halo, rvir, n_halo * sizeof(double), cudaMemcpyHostToDevice, st));
+        dxyz = in;
+        dm = in + 3 * n_halo;
+        dc = in + 4 * n_halo;
+        dr = in + 5 * n_halo;
+    }
+    std::vector<char> th(tb * n_theta);
+    gbp_hod_thetas(thetas, n_theta, th.data());
+    CK(cudaMemcpyAsync(at<char>(W, o_th), th.data(), th.size(), cudaMemcpyHostToDevice, st));
+    int *cnt = at<int>(W, o_cnt), *off = at<int>(W, o_off);
+    CK(cudaMemsetAsync(cnt + items, 0, sizeof(int), st));
+    CK(gbp_hod_count(dm, at<double>(W, o_logm), n_halo, at<char>(W, o_th), n_theta, seed, cnt, st));
+    CK(gbp_scan_exclusive(cnt, off, items, at<int>(W, o_scan), st, nullptr));
+    // per-mock offsets: the scan at the first halo of each parameter vector
+    std::vector<int> hoff((size_t)n_theta + 1);
+    for (int m = 0; m <= n_theta; m++)
+        CK(cudaMemcpyAsync(&hoff[(size_t)m], off + (int64_t)m * n_halo, sizeof(int),
+                           cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    for (int m = 0; m <= n_theta; m++) offsets[m] = hoff[(size_t)m];
+    const int64_t total = offsets[n_theta];
+    if (!gal_xyz || cap < total || total == 0) return GBP_OK;  // offsets only
+    float *dg = mem == GBP_MEM_HOST ? at<float>(W, o_gal) : gal_xyz;
+    CK(gbp_hod_write(dxyz, dm, at<double>(W, o_logm), dc, dr, n_halo, at<char>(W, o_th), n_theta,
+                     seed, off, lbox, dg, st));
+    if (mem == GBP_MEM_HOST)
+        CK(cudaMemcpyAsync(gal_xyz, dg, 3 * total * sizeof(float), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    return GBP_OK;
+}
+
 int gbp_zheng07_weights(gbp_plan *plan, const double *mass, int64_t n, const double *theta,
                         int32_t mem, double *w) {
     if (!plan) return GBP_ERR_INVALID;

@@ -309,4 +309,14 @@ cudaError_t gbp_launch_zheng07_w(const double *mass, int64_t n, Zheng07 th, doub
                                  cudaStream_t st);
 cudaError_t gbp_launch_zheng07_vjp(const double *mass, int64_t n, Zheng07 th, const double *gw,
                                    double *out5, cudaStream_t st);
+// Zheng07 mocks on the GPU (gbp_hod.cu): thetas as (n, 5) rows converted by
+// gbp_hod_thetas into gbp_hod_theta_bytes() each
+cudaError_t gbp_hod_count(const double *mass, double *logm, int64_t nh, const void *thetas,
+                          int nth, unsigned long long seed, int *count, cudaStream_t st);
+cudaError_t gbp_hod_write(const double *xyz, const double *mass, const double *logm,
+                          const double *conc, const double *rvir, int64_t nh, const void *thetas,
+                          int nth, unsigned long long seed, const int *off, double L, float *gal,
+                          cudaStream_t st);
+size_t gbp_hod_theta_bytes();
+void gbp_hod_thetas(const double *theta, int nth, void *out);
 cudaError_t gbp_run_ffma_probe(int nsm, cudaStream_t st, float *ms_out, double *flops_out);

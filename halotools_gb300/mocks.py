@@ -159,3 +159,37 @@ def hod_mocks_torch(pos, mass, conc, lbox, thetas, seed=0, dtype=None):
         parts.append(gal.to(dtype))
         offsets.append(offsets[-1] + len(gal))
     return torch.cat(parts).contiguous(), np.asarray(offsets, dtype=np.int64)
+
+
+def hod_mocks_gpu(pos, mass, conc, lbox, thetas, seed=0, rvir=None, plan=None):
+    """Many Zheng07 realisations drawn by the GPU kernels (``gbp_hod_mocks``).
+
+    pos (N, 3), mass, conc (and optionally rvir, default (M / 1e14)^(1/3) as the
+    other generators here) as numpy arrays or CUDA tensors; thetas (M, 5) of
+    (logMmin, sigma_logM, logM0, logM1, alpha).  Returns (xyz, offsets): a float32
+    CUDA tensor (total, 3) with mock m in rows [offsets[m], offsets[m+1]), and the
+    numpy int64 offsets.  The draws are fixed by (seed, halo, mock, draw index).
+    """
+    import torch
+    from . import _native
+    dev = torch.device("cuda")
+
+    def col(a):
+        return torch.as_tensor(a, dtype=torch.float64, device=dev).contiguous()
+
+    P, M, C = col(pos), col(mass), col(conc)
+    R = col(rvir) if rvir is not None else (M / 1e14) ** (1.0 / 3.0)
+    th = np.ascontiguousarray(np.atleast_2d(np.asarray(thetas, dtype=np.float64)))
+    n = int(M.numel())
+    plan = plan or _native.default_plan()
+    plan.set_stream(torch.cuda.current_stream().cuda_stream)
+    offs = np.zeros(len(th) + 1, dtype=np.int64)
+    args = (plan.handle, _native.dptr_int(P.data_ptr()), _native.dptr_int(M.data_ptr()),
+            _native.dptr_int(C.data_ptr()), _native.dptr_int(R.data_ptr()), n, _native.pd(th),
+            len(th), float(lbox), int(seed) & 0xFFFFFFFFFFFFFFFF, _native.GBP_MEM_DEVICE)
+    plan.check(plan.lib.gbp_hod_mocks(*args, None, 0, _native.pi64(offs)))
+    out = torch.empty((max(int(offs[-1]), 1), 3), dtype=torch.float32, device=dev)
+    if offs[-1] > 0:
+        plan.check(plan.lib.gbp_hod_mocks(*args, _native.dptr_int(out.data_ptr()), int(offs[-1]),
+                                          _native.pi64(offs)))
+    return out[:int(offs[-1])], offs

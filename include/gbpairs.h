@@ -135,6 +135,26 @@ int gbp_marked_npairs_3d(gbp_plan *plan, const double *xyz1, int64_t n1, const d
                          const double *period3, int32_t pbc, int32_t mem, double *out);
 
 /*
+ * Zheng07 HOD mocks on the GPU, one per parameter vector thetas[m] =
+ * (logMmin, sigma_logM, logM0, logM1, alpha), (n_theta, 5) row-major: a
+ * Bernoulli central with <Ncen> = (1 + erf((log10 M - logMmin) / sigma_logM)) / 2
+ * at the halo centre and a Poisson number of satellites with <Nsat> =
+ * ((M - 10^logM0) / 10^logM1)^alpha at NFW radii (concentration conc, radius
+ * rvir) in isotropic directions, wrapped into [0, lbox) (zheng07_components.py:
+ * 149-153, 455-470; population as hod_mock_factory.py:196-401 does it).  Draws
+ * are Philox4x32-10 counters of (halo, m, draw) under `seed`, so a mock is fixed
+ * by its inputs.  offsets[0..n_theta]: mock m is rows [offsets[m], offsets[m+1])
+ * of gal_xyz, (offsets[n_theta], 3) float32.  With gal_xyz NULL or cap (rows)
+ * below the total, only offsets are written: call again with a buffer of
+ * offsets[n_theta] rows.  mem: all arrays on the host or all on the device
+ * (offsets always on the host).
+ */
+int gbp_hod_mocks(gbp_plan *plan, const double *halo_xyz, const double *mass, const double *conc,
+                  const double *rvir, int64_t n_halo, const double *thetas, int32_t n_theta,
+                  double lbox, uint64_t seed, int32_t mem, float *gal_xyz, int64_t cap,
+                  int64_t *offsets);
+
+/*
  * Condition a neighbour pair (i, j) must meet besides its separation.
  * kind 0: none.  kind 1: the mass fraction of counts_in_cylinders
  * (counts_in_cells/engines/conditions/conditions.pyx, MassFrac.func):
