@@ -474,13 +474,16 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
         a.top0 = std::min(c.ax[0].hi[nb0 - 1], 1.0e30f);
         a.top1 = c.naxes > 1 ? std::min(c.ax[1].hi[nb1 - 1], 1.0e30f) : 0.f;
         a.self_bin = host_bin(nb0, c.ax[0].E.data(), 0.0);
-        const bool w2 = c.mode == MODE_XYZW || c.mode == MODE_SMUW;
+        const bool jw = c.mode == MODE_JACKW || c.mode == MODE_JACKXYZW;
+        const bool w2 = c.mode == MODE_XYZW || c.mode == MODE_SMUW || jw;
         if (w2) {
             // the flat (axis 0, axis 1) bin of separation 0, or -1 when outside
-            const int sb1 = host_bin(nb1, c.ax[1].E.data(), 0.0);
-            a.self_bin = (a.self_bin < nb0 && sb1 < nb1) ? a.self_bin * (nb1 + 1) + sb1 : -1;
+            const int sb1 = c.naxes > 1 ? host_bin(nb1, c.ax[1].E.data(), 0.0) : 0;
+            const int ok = a.self_bin < nb0 && (c.naxes == 1 || sb1 < nb1);
+            a.self_bin = ok ? a.self_bin * (c.naxes > 1 ? nb1 + 1 : 1) + sb1 : -1;
         }
-        const int jwb = (c.mode == MODE_MARK || w2) ? (c.wf == 0 ? 8 * c.nw : 4)
+        const int jwb = jw ? 4 * c.nw   // {w, tag} columns
+                        : (c.mode == MODE_MARK || w2) ? (c.wf == 0 ? 8 * c.nw : 4)
                         : c.mode == MODE_MARKC ? 4 * c.nw
                         : c.mode == MODE_ADJ   ? 4
                         : c.mode == MODE_POBJ  ? 4   // the gather kernel's fixed stride
@@ -495,7 +498,8 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
             size_t one = (size_t)(nb0 + 1) * (size_t)(c.naxes > 1 ? nb1 + 1 : 1) * 4;
             if (one * GBP_WARPS > (96u << 10)) copies = 0;
         }
-        if (c.mode == MODE_XYZW) copies = 0;  // sums only: no integer counts
+        if (c.mode == MODE_XYZW || c.mode == MODE_JACKW || c.mode == MODE_JACKXYZW)
+            copies = 0;  // sums only: no integer counts
         a.hist_copies = copies;
         SmemLayout L = gbp_smem_layout(c.mode, T0, T1, nb0, nb1, nsten, copies, jwb, c.ntag);
         size_t smem = (size_t)L.total;
@@ -617,7 +621,8 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
         return run_call(plan, c, hist_host, histd_host);
     }
     hist_host.assign(at<unsigned long long>(H, h_hist), at<unsigned long long>(H, h_hist) + nm * nhist);
-    if (c.mode != MODE_MARK && c.mode != MODE_MARKC && c.mode != MODE_XYZW && c.mode != MODE_NEIGH)
+    if (c.mode != MODE_MARK && c.mode != MODE_MARKC && c.mode != MODE_XYZW && c.mode != MODE_NEIGH &&
+        c.mode != MODE_JACKW && c.mode != MODE_JACKXYZW)
         add_self_pairs(c, hist_host);
     if (histd_host) histd_host->assign(at<double>(H, h_histd), at<double>(H, h_histd) + nm * nhist);
     if (ntab) c.htag.assign(at<unsigned long long>(H, h_htag), at<unsigned long long>(H, h_htag) + ntab);
@@ -1320,6 +1325,134 @@ int gbp_npairs_jackknife_xy_z(gbp_plan *plan, const double *xyz1, int64_t n1, co
     for (size_t k = 0; k < plane; k++) out[k] = C[k];
     for (int sidx = 1; sidx < rows; sidx++) {
         cumulate_2d(tab.data() + (size_t)sidx * nbin, n_rp, n_pi, Q.data());
+        for (size_t k = 0; k < plane; k++) out[(size_t)sidx * plane + k] = C[k] - 0.5 * Q[k];
+    }
+    return GBP_OK;
+}
+
+// Weighted jackknife counts (npairs_jackknife_3d.py / npairs_jackknife_xy_z.py
+// with weights; jweight of the engines): rows {w, tag} per point, C_w and the
+// FP64 (tag, bin) table of w_i w_j per pair end, row s = C_w - Q_w(s) / 2.
+static int jackknife_weighted(gbp_plan *plan, Call &c, const double *xyz1, int64_t n1,
+                              const double *xyz2, int64_t n2, const double *w1, const double *w2,
+                              const int32_t *jtags1, const int32_t *jtags2, int32_t n_samples,
+                              std::vector<double> &r1, std::vector<double> &r2) {
+    if (n_samples < 1 || n_samples > 32767 || (n1 > 0 && (!jtags1 || !w1)) ||
+        (n2 > 0 && (!jtags2 || !w2)))
+        return fail(plan, GBP_ERR_INVALID, "N_samples must be 1..32767 with one tag and weight per point");
+    const bool autocorr = (xyz1 == xyz2 && n1 == n2 && jtags1 == jtags2 && w1 == w2);
+    r1.assign(2 * (size_t)std::max<int64_t>(n1, 1), 0.0);
+    for (int64_t i = 0; i < n1; i++) {
+        if (jtags1[i] < 1 || jtags1[i] > n_samples)
+            return fail(plan, GBP_ERR_INVALID, "jtags1 must be in [1, N_samples]");
+        r1[2 * (size_t)i] = w1[i];
+        r1[2 * (size_t)i + 1] = (double)jtags1[i];
+    }
+    if (!autocorr) {
+        r2.assign(2 * (size_t)std::max<int64_t>(n2, 1), 0.0);
+        for (int64_t i = 0; i < n2; i++) {
+            if (jtags2[i] < 1 || jtags2[i] > n_samples)
+                return fail(plan, GBP_ERR_INVALID, "jtags2 must be in [1, N_samples]");
+            r2[2 * (size_t)i] = w2[i];
+            r2[2 * (size_t)i + 1] = (double)jtags2[i];
+        }
+    }
+    c.w1 = r1.data();
+    c.w2 = autocorr ? r1.data() : r2.data();
+    c.nw = 2;
+    c.wf = 1;
+    c.ntag = n_samples + 1;
+    c.autocorr = autocorr;
+    return GBP_OK;
+}
+
+int gbp_npairs_jackknife_3d_weighted(gbp_plan *plan, const double *xyz1, int64_t n1,
+                                     const double *xyz2, int64_t n2, const double *w1,
+                                     const double *w2, const int32_t *jtags1,
+                                     const int32_t *jtags2, int32_t n_samples,
+                                     const double *rbins, int32_t nb, const double *period3,
+                                     int32_t pbc, int32_t mem, double *out) {
+    int rc = check_common(plan, xyz1, n1, xyz2, n2, period3, pbc, mem);
+    if (rc) return rc;
+    if (mem != GBP_MEM_HOST)
+        return fail(plan, GBP_ERR_INVALID, "jackknife counts take host positions and tags");
+    if (!rbins || nb < 2 || nb > GBP_NB_LANE || !out)
+        return fail(plan, GBP_ERR_INVALID, "rbins must have 2..%d entries", GBP_NB_LANE);
+    double rmax = max_nan(rbins, nb);
+    double search[3] = {rmax, rmax, rmax};
+    if ((rc = check_search(plan, search, period3))) return rc;
+    Call c;
+    c.mode = MODE_JACKW;
+    std::vector<double> r1, r2;
+    if ((rc = jackknife_weighted(plan, c, xyz1, n1, xyz2, n2, w1, w2, jtags1, jtags2, n_samples,
+                                 r1, r2)))
+        return rc;
+    c.xyz1 = xyz1;
+    c.xyz2 = xyz2;
+    c.n1 = n1;
+    c.n2 = n2;
+    c.mem = mem;
+    c.naxes = 1;
+    choose_grid(c.g, period3, search, pbc, n2, plan->reach, MAX_CELLS_PER_DIM, 0.0, plan->block);
+    build_stencil(c.g, search, 0, c.autocorr);
+    ErrModel em = err_model(c.g);
+    std::vector<double> E(nb);
+    edges_top_walk(rbins, nb, E.data());
+    c.ax[0].set(E, &em, 3);
+    c.ax[0].make_lut(no_qband);
+    const int rows = n_samples + 1;
+    for (int k = 0; k < rows * nb; k++) out[k] = 0.0;
+    if (n1 == 0 || n2 == 0) return GBP_OK;
+    std::vector<unsigned long long> h;
+    std::vector<double> hd;
+    if ((rc = run_call(plan, c, h, &hd))) return rc;
+    const double *tab = reinterpret_cast<const double *>(c.htag.data());
+    double cT = 0.0;
+    std::vector<double> cQ((size_t)rows, 0.0);
+    for (int k = 0; k < nb; k++) {
+        cT += hd[k];
+        out[k] = cT;
+        for (int sidx = 1; sidx < rows; sidx++) {
+            cQ[(size_t)sidx] += tab[(size_t)sidx * (nb + 1) + k];
+            out[(size_t)sidx * nb + k] = cT - 0.5 * cQ[(size_t)sidx];
+        }
+    }
+    return GBP_OK;
+}
+
+int gbp_npairs_jackknife_xy_z_weighted(gbp_plan *plan, const double *xyz1, int64_t n1,
+                                       const double *xyz2, int64_t n2, const double *w1,
+                                       const double *w2, const int32_t *jtags1,
+                                       const int32_t *jtags2, int32_t n_samples,
+                                       const double *rp_bins, int32_t n_rp, const double *pi_bins,
+                                       int32_t n_pi, const double *period3, int32_t pbc,
+                                       int32_t mem, double *out) {
+    if (!out) return fail(plan, GBP_ERR_INVALID, "null output");
+    if (mem != GBP_MEM_HOST)
+        return fail(plan, GBP_ERR_INVALID, "jackknife counts take host positions and tags");
+    Call c;
+    c.mode = MODE_JACKXYZW;
+    std::vector<double> r1, r2;
+    int rc = jackknife_weighted(plan, c, xyz1, n1, xyz2, n2, w1, w2, jtags1, jtags2, n_samples,
+                                r1, r2);
+    if (rc) return rc;
+    if ((rc = setup_xyz(plan, c, xyz1, n1, xyz2, n2, rp_bins, n_rp, pi_bins, n_pi, period3, pbc,
+                        mem, c.autocorr)))
+        return rc;
+    const int rows = n_samples + 1;
+    const size_t plane = (size_t)n_rp * n_pi;
+    for (size_t k = 0; k < rows * plane; k++) out[k] = 0.0;
+    if (n1 == 0 || n2 == 0) return GBP_OK;
+    std::vector<unsigned long long> h;
+    std::vector<double> hd;
+    if ((rc = run_call(plan, c, h, &hd))) return rc;
+    const double *tab = reinterpret_cast<const double *>(c.htag.data());
+    const size_t nbin = (size_t)(n_rp + 1) * (n_pi + 1);
+    std::vector<double> C(plane), Q(plane);
+    cumulate_2d(hd.data(), n_rp, n_pi, C.data());
+    for (size_t k = 0; k < plane; k++) out[k] = C[k];
+    for (int sidx = 1; sidx < rows; sidx++) {
+        cumulate_2d(tab + (size_t)sidx * nbin, n_rp, n_pi, Q.data());
         for (size_t k = 0; k < plane; k++) out[(size_t)sidx * plane + k] = C[k] - 0.5 * Q[k];
     }
     return GBP_OK;

@@ -42,7 +42,8 @@ struct PairV {
     float v0, v1;
     int iu, jj;
     bool sym;
-    float w;  // weighted 2-D modes: the pair's weight
+    float w;  // weighted modes: the pair's weight
+    int tg;   // weighted jackknife: tag_i | tag_j << 16
 };
 struct Ix {
     const int *ui;  // sorted index of each i-slot
@@ -178,18 +179,50 @@ __device__ __forceinline__ void w2_add(const WSink &s, int b, float x) {
 }
 
 // What a binned pair adds besides its count: X_W its weight w (times the
-// multiplicity m), X_TAG one pair end per tag (w holds tag_i | tag_j << 16)
+// multiplicity m), X_TAG one pair end per tag (w holds tag_i | tag_j << 16),
+// X_TAGW its weight to the sums and to both ends' rows of the FP64 table (tg
+// holds the tags)
 #define X_NONE 0
 #define X_W 1
 #define X_TAG 2
+#define X_TAGW 3
 template <int X>
-__device__ __forceinline__ void sink_add(const WSink &s, int b, int m, float w) {
+__device__ __forceinline__ void sink_add(const WSink &s, int b, int m, float w, int tg = 0) {
     if (X == X_W) w2_add(s, b, m == 2 ? 2.0f * w : w);
     if (X == X_TAG) {
         const int t = __float_as_int(w);
         atomicAdd(&s.tab[(t & 0xffff) * s.tstride + b], (unsigned long long)m);
         atomicAdd(&s.tab[(t >> 16) * s.tstride + b], (unsigned long long)m);
     }
+    if (X == X_TAGW) {
+        const float x = m == 2 ? 2.0f * w : w;
+        w2_add(s, b, x);
+        double *t = reinterpret_cast<double *>(s.tab);
+        atomicAdd(&t[(tg & 0xffff) * s.tstride + b], (double)x);
+        atomicAdd(&t[(tg >> 16) * s.tstride + b], (double)x);
+    }
+}
+
+// ---------------- stage 2: weighted jackknife, 3-D ----------------
+// w_i w_j to the sums and to both ends' table rows, per ordered pair
+// (npairs_jackknife_3d_engine.pyx: jweight with weights)
+__device__ __forceinline__ void bin_3dw(const PairV &p, const WSink &ws, const AxisSm &A,
+                                        const Ix &ix, const CountArgs &a) {
+    const float v = p.v0;
+    const float4 t = lut_entry_c<false>(v, A);
+    int b = __float_as_int(t.x) + (v > t.y ? 1 : 0);
+    if ((v > t.z) & !(v > t.y)) {
+        int k[2];
+        const int n = slow_3d(v, __float_as_int(t.x), ix.ui[p.iu], ix.jw[p.jj], p.sym, k, A, a);
+        if (n == 0) {
+            b = k[0];
+        } else {
+            for (int q = 0; q < n; q++)
+                if (k[q] < A.nb) sink_add<X_TAGW>(ws, k[q], 1, p.w, p.tg);
+            return;
+        }
+    }
+    if (b < A.nb) sink_add<X_TAGW>(ws, b, p.sym ? 2 : 1, p.w, p.tg);
 }
 
 // ---------------- deferred FP64 rechecks (s, mu') ----------------
@@ -217,14 +250,15 @@ __device__ __forceinline__ bool rq_push(const RQ &q, int4 e) {
 // own).  CNT: integer counts into hw; X: what else the pair adds (sink_add).
 template <class HT, bool CNT, int X>
 __device__ __noinline__ void slow_xyz(float v0, float v1, int b0a, int b0b, int is, int js,
-                                      bool sym, float wt, HT *hw, const WSink ws, int stride,
-                                      const AxisSm &A, const AxisSm &Bx, const CountArgs &a) {
+                                      bool sym, float wt, int tg, HT *hw, const WSink ws,
+                                      int stride, const AxisSm &A, const AxisSm &Bx,
+                                      const CountArgs &a) {
     int ka = walk_bin(v0, b0a, A);
     int kb = walk_bin(v1, b0b, Bx);
     if (ka >= 0 && kb >= 0) {
         if (ka < A.nb && kb < Bx.nb) {
             if (CNT) atomicAdd(&hw[ka * stride + kb], (HT)(sym ? 2 : 1));
-            sink_add<X>(ws, ka * stride + kb, sym ? 2 : 1, wt);
+            sink_add<X>(ws, ka * stride + kb, sym ? 2 : 1, wt, tg);
         }
         return;
     }
@@ -241,7 +275,7 @@ __device__ __noinline__ void slow_xyz(float v0, float v1, int b0a, int b0b, int 
         const int eb = kb >= 0 ? kb : exact_bin(r.dz2, b0b, Bx);
         if (ea < A.nb && eb < Bx.nb) {
             if (CNT) atomicAdd(&hw[ea * stride + eb], (HT)1);
-            sink_add<X>(ws, ea * stride + eb, 1, wt);
+            sink_add<X>(ws, ea * stride + eb, 1, wt, tg);
         }
     }
 }
@@ -259,12 +293,12 @@ __device__ __forceinline__ void bin_xyz(const PairV &p, HT *hw, const WSink &ws,
     bool amb = ((v0 > e0.z) & !(v0 > e0.y)) | ((v1 > e1.z) & !(v1 > e1.y));
     if (amb) {
         slow_xyz<HT, CNT, X>(v0, v1, __float_as_int(e0.x), __float_as_int(e1.x), ix.ui[p.iu],
-                              ix.jw[p.jj], sym, p.w, hw, ws, stride, A, Bx, a);
+                              ix.jw[p.jj], sym, p.w, p.tg, hw, ws, stride, A, Bx, a);
         return;
     }
     if ((ba < A.nb) & (bb < Bx.nb)) {
         if (CNT) atomicAdd(&hw[ba * stride + bb], (HT)(sym ? 2 : 1));
-        sink_add<X>(ws, ba * stride + bb, sym ? 2 : 1, p.w);
+        sink_add<X>(ws, ba * stride + bb, sym ? 2 : 1, p.w, p.tg);
     }
 }
 
@@ -430,20 +464,26 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
     constexpr bool TWO = XYZF || SMUF;
     // weighted 2-D: a marking function's value per pair into the CTA's (hi, lo)
     // sums; weighted s_mu also counts
-    constexpr bool W2 = (MODE == MODE_XYZW || MODE == MODE_SMUW);
-    constexpr bool CNT2 = (MODE != MODE_XYZW);
+    // weighted jackknife (3-D, (rp, pi)): rows {w, tag} per point, w_i w_j to the
+    // sums and to both ends' FP64 table rows
+    constexpr bool JW = (MODE == MODE_JACKW || MODE == MODE_JACKXYZW);
+    constexpr bool W2 = (MODE == MODE_XYZW || MODE == MODE_SMUW || JW);
+    constexpr bool MW2 = (MODE == MODE_XYZW || MODE == MODE_SMUW);  // marking-function sums
+    constexpr bool CNT2 = (MODE != MODE_XYZW && !JW);
     constexpr bool MARK = (MODE == MODE_MARK);
-    constexpr bool MW = MARK || W2;  // per-pair marking function of staged weights
-    constexpr int XS = W2 ? X_W : JACK2 ? X_TAG : X_NONE;  // what 2-D bins add besides counts
+    constexpr bool MW = MARK || MW2;  // per-pair marking function of staged weights
+    // what 2-D bins add besides counts
+    constexpr int XS = JW ? X_TAGW : W2 ? X_W : JACK2 ? X_TAG : X_NONE;
     constexpr bool MARKC = (MODE == MODE_MARKC);  // nw = channels of product marks
+    constexpr bool COLS = MARKC || JW;  // nw FP32 columns staged per point
     constexpr unsigned FULL = 0xffffffffu;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nb0 = a.ax[0].nb, nb1 = TWO ? a.ax[1].nb : 0;
     const int T0 = a.ax[0].T, T1 = TWO ? a.ax[1].T : 0;
     const int copies = a.hist_copies;  // 2-D / wide: GBP_WARPS (one per warp) or 0 (global)
     constexpr bool JACK = (MODE == MODE_JACK);    // w1 / w2 hold the subsample tags
-    const int nw = (MW || MARKC || JACK || JACK2) ? a.nw : 0;
-    const int jwb = MW ? (WF == 0 ? 8 * nw : 4) : MARKC ? 4 * nw : (JACK || JACK2) ? 4 : 0;
+    const int nw = (MW || COLS || JACK || JACK2) ? a.nw : 0;
+    const int jwb = MW ? (WF == 0 ? 8 * nw : 4) : COLS ? 4 * nw : (JACK || JACK2) ? 4 : 0;
     const SmemLayout L = gbp_smem_layout(MODE, T0, T1, nb0, nb1, a.nsten, copies, jwb, a.ntag);
     if (gbp_smem_too_small(L.total, a.err)) return;
     unsigned *s_l0 = (unsigned *)(smem + L.off_lut0);
@@ -458,7 +498,7 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
     // the same j-points with each coordinate twice, for the packed stage 1
     ulonglong2 *jxy = (ulonglong2 *)(smem + L.off_j2) + warp * 32;
     unsigned long long *jzz = (unsigned long long *)(smem + L.off_j2 + GBP_JCAP * 16) + warp * 32;
-    float *jw = (float *)(smem + L.off_jw) + warp * 32 * (MARKC ? nw : 1);
+    float *jw = (float *)(smem + L.off_jw) + warp * 32 * (COLS ? nw : 1);
     double *jw64 = (double *)(smem + L.off_jw) + warp * 32 * (nw > 0 ? nw : 1);
     float4 *s_D = (float4 *)(smem + L.off_D);
     double *s_E0 = (double *)(smem + L.off_E0);
@@ -474,7 +514,7 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
     float *uy = ux + GBP_USLOTS, *uz = ux + 2 * GBP_USLOTS;
     int *uix = (int *)(ux + 3 * GBP_USLOTS);
     float *s_uw = (float *)(smem + L.off_q + GBP_WARPS * GBP_USLOTS * 16) +
-                  warp * GBP_USLOTS * (MARKC ? nw : 1);
+                  warp * GBP_USLOTS * (COLS ? nw : 1);
     // MARKC: this warp's binned pairs of one round {bin | multiplicity << 16, second bin, i, j}
     int4 *s_rec = (int4 *)(smem + L.off_rec) + warp * 32;
     // (s, mu'): this warp's ring of deferred FP64 rechecks and its tail
@@ -564,6 +604,7 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
             if (copies) bin_smu<unsigned, CNT2, XS>(e, wh, wsink, stride2, A0, A1, ix, rq, a);
             else bin_smu<unsigned long long, CNT2, XS>(e, gh, wsink, stride2, A0, A1, ix, rq, a);
         } else if (MARK) bin_mark(e, hs, hc, A0, ix, a);
+        else if (MODE == MODE_JACKW) bin_3dw(e, wsink, A0, ix, a);
     };
     // Bin the rest of the queue, add this warp's histogram to mock mk and clear it.
     // Re-evaluate queued rechecks in FP64, 32 at a time, until fewer than
@@ -700,7 +741,7 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                 s_uw[lane + 48] = w1;
             }
         }
-        if (MARKC) {
+        if (COLS) {
             for (int k = 0; k < nw; k++) {
                 s_uw[lane * nw + k] = lane < icnt ? a.w1[(int64_t)(ifirst + lane) * nw + k] : 0.f;
                 s_uw[(lane + 48) * nw + k] =
@@ -763,7 +804,7 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                             jw[lane] = a.w2[j];
                         }
                     }
-                    if (MARKC)
+                    if (COLS)
                         for (int q = 0; q < nw; q++) jw[lane * nw + q] = a.w2[(int64_t)j * nw + q];
                     if (JACK || JACK2) jw[lane] = a.w2[j];
                 } else {
@@ -840,10 +881,15 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                                                  : (float)wfunc64(a.wfunc, wa, jw64 + jj * nw);
                                 kahan_add(hs, hc, a.self_bin, ws);
                             }
-                            if (W2 && a.self_bin >= 0) {
+                            if (MW2 && a.self_bin >= 0) {
                                 const float ws = WF == 1 ? w0 * jw[jj] : WF == 2 ? w0 + jw[jj]
                                                  : (float)wfunc64(a.wfunc, wa, jw64 + jj * nw);
                                 w2_add(wsink, a.self_bin, ws);
+                            }
+                            if (JW && a.self_bin >= 0) {
+                                const int t = (int)jw[jj * 2 + 1];
+                                sink_add<X_TAGW>(wsink, a.self_bin, 1, jw[jj * 2] * jw[jj * 2],
+                                                 t | (t << 16));
                             }
                         }
                         if (jt == is1) {
@@ -853,10 +899,15 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                                                  : (float)wfunc64(a.wfunc, wb, jw64 + jj * nw);
                                 kahan_add(hs, hc, a.self_bin, ws);
                             }
-                            if (W2 && a.self_bin >= 0) {
+                            if (MW2 && a.self_bin >= 0) {
                                 const float ws = WF == 1 ? w1 * jw[jj] : WF == 2 ? w1 + jw[jj]
                                                  : (float)wfunc64(a.wfunc, wb, jw64 + jj * nw);
                                 w2_add(wsink, a.self_bin, ws);
+                            }
+                            if (JW && a.self_bin >= 0) {
+                                const int t = (int)jw[jj * 2 + 1];
+                                sink_add<X_TAGW>(wsink, a.self_bin, 1, jw[jj * 2] * jw[jj * 2],
+                                                 t | (t << 16));
                             }
                         }
                     }
@@ -920,7 +971,12 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                         }
                         // jackknife (rp, pi): both ends' tags (exact small integers)
                         if (JACK2) wt = __int_as_float((int)s_uw[iu] | ((int)jw[jj] << 16));
-                        return PairV{v0, v1, iu, jj, ((sym_bits >> jj) & 1u) != 0u, wt};
+                        int tg = 0;
+                        if (JW) {
+                            wt = s_uw[iu * 2] * jw[jj * 2];
+                            tg = (int)s_uw[iu * 2 + 1] | ((int)jw[jj * 2 + 1] << 16);
+                        }
+                        return PairV{v0, v1, iu, jj, ((sym_bits >> jj) & 1u) != 0u, wt, tg};
                     };
                     if (MARKC) {
                         // each lane bins one pair per round; then lane (g, c) adds channel
@@ -1006,7 +1062,7 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                                                                    ka * stride2 + ga],
                                                            ea.sym ? 2ull : 1ull);
                                         }
-                                        sink_add<XS>(wsink, ka * stride2 + ga, ea.sym ? 2 : 1, ea.w);
+                                        sink_add<XS>(wsink, ka * stride2 + ga, ea.sym ? 2 : 1, ea.w, ea.tg);
                                     }
                                 }
                                 if (hb) {
@@ -1018,7 +1074,7 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                                                                    kb * stride2 + gb],
                                                            eb.sym ? 2ull : 1ull);
                                         }
-                                        sink_add<XS>(wsink, kb * stride2 + gb, eb.sym ? 2 : 1, eb.w);
+                                        sink_add<XS>(wsink, kb * stride2 + gb, eb.sym ? 2 : 1, eb.w, eb.tg);
                                     }
                                 }
                             } else if (MARK) {
@@ -1154,6 +1210,10 @@ cudaError_t gbp_launch_count(int mode, int wf, const CountArgs &a, int grid, siz
         return launch_t<MODE_SMUW, 1>(a, grid, smem, st);
     case MODE_JACKXYZ:
         return launch_t<MODE_JACKXYZ, 1>(a, grid, smem, st);
+    case MODE_JACKW:
+        return launch_t<MODE_JACKW, 1>(a, grid, smem, st);
+    case MODE_JACKXYZW:
+        return launch_t<MODE_JACKXYZW, 1>(a, grid, smem, st);
     case MODE_XYZW:
         if (wf == 1) return launch_t<MODE_XYZW, 1>(a, grid, smem, st);
         if (wf == 2) return launch_t<MODE_XYZW, 2>(a, grid, smem, st);
@@ -1180,6 +1240,10 @@ int gbp_count_occupancy(int mode, int wf, size_t smem) {
         return occ_t<MODE_SMUW, 1>(smem);
     case MODE_JACKXYZ:
         return occ_t<MODE_JACKXYZ, 1>(smem);
+    case MODE_JACKW:
+        return occ_t<MODE_JACKW, 1>(smem);
+    case MODE_JACKXYZW:
+        return occ_t<MODE_JACKXYZW, 1>(smem);
     case MODE_XYZW:
         if (wf == 1) return occ_t<MODE_XYZW, 1>(smem);
         if (wf == 2) return occ_t<MODE_XYZW, 2>(smem);

@@ -31,12 +31,14 @@ enum { MODE_3D = 0, MODE_XYZ = 1, MODE_SMU = 2, MODE_MARK = 3, MODE_ADJ = 4, MOD
        MODE_XYZW = 9,     // (rp, pi) sums of a marking function (marked_npairs_xy_z)
        MODE_SMUW = 10,    // (s, mu') counts and w1 * w2 sums (weighted_npairs_s_mu)
        MODE_JACKXYZ = 11,    // (rp, pi) counts plus a global (tag, bin) table of pair ends
-       MODE_NEIGH = 12 };    // per-object neighbours in per-point spheres / cylinders
+       MODE_NEIGH = 12,      // per-object neighbours in per-point spheres / cylinders
+       MODE_JACKW = 13,      // weighted jackknife, 3-D: w1 w2 sums plus an FP64 (tag, bin) table
+       MODE_JACKXYZW = 14 }; // weighted jackknife, (rp, pi)
 
 // Pair geometry of a count mode: (rp, pi) cylinders or (s, mu') cones; every
 // other mode measures 3-D separations
 __host__ __device__ constexpr bool gbp_mode_xyz(int m) {
-    return m == MODE_XYZ || m == MODE_XYZW || m == MODE_JACKXYZ;
+    return m == MODE_XYZ || m == MODE_XYZW || m == MODE_JACKXYZ || m == MODE_JACKXYZW;
 }
 __host__ __device__ constexpr bool gbp_mode_smu(int m) { return m == MODE_SMU || m == MODE_SMUW; }
 
@@ -204,7 +206,8 @@ __host__ __device__ inline SmemLayout gbp_smem_layout(int mode, int T0, int T1, 
         hist_bytes = copies * (nb0 + 1) * 4;                  // shared u32 copies (wide 1-D)
     } else {
         hist_bytes = copies * (nb0 + 1) * (nb1 + 1) * 4;      // shared u32 copies (2-D)
-        if (mode == MODE_XYZW || mode == MODE_SMUW)           // then the CTA's weighted sums
+        if (mode == MODE_XYZW || mode == MODE_SMUW || mode == MODE_JACKW ||
+            mode == MODE_JACKXYZW)                            // then the CTA's weighted sums
             hist_bytes = gbp_align(hist_bytes, 16) + gbp_w2_bytes((nb0 + 1) * (nb1 + 1));
     }
     o += gbp_align(hist_bytes, 16);

@@ -497,18 +497,18 @@ def marked_npairs_3d_channels(sample1, sample2, rbins, period=None, weights1=Non
 
 def _jackknife_inputs(sample1, sample2, jtags1, jtags2, N_samples, weights1, weights2):
     """npairs_jackknife_3d.py / npairs_jackknife_xy_z.py weight and tag checks
-    (_npairs_jackknife_xy_z_process_weights_jtags); non-unit weights are refused."""
+    (_npairs_jackknife_xy_z_process_weights_jtags).  Returns the samples, tags and
+    float64 weights (None when every weight is 1: the exact integer path)."""
     s1 = _columns(sample1)
     s2 = s1 if sample2 is sample1 else _columns(sample2)
+    ws = []
     for w, s, name in ((weights1, s1, "weights1"), (weights2, s2, "weights2")):
         if w is not None:
             w = np.asarray(w).astype("float64")
             if np.shape(w)[0] != np.shape(s)[0]:
                 raise HalotoolsError("%s should have same len as %s" % (name, name.replace(
                     "weights", "sample")))
-            if np.any(w != 1.0):
-                raise NotImplementedError("weighted jackknife counts are not supported on the "
-                                          "GPU; pass unit weights")
+        ws.append(w)
     t1 = np.asarray(jtags1).astype("int")
     t2 = np.asarray(jtags2).astype("int")
     if np.shape(t1)[0] != np.shape(s1)[0]:
@@ -525,16 +525,31 @@ def _jackknife_inputs(sample1, sample2, jtags1, jtags2, N_samples, weights1, wei
         raise HalotoolsError("jtags2 must be <= N_samples")
     if not np.array_equal(np.unique(t1), np.arange(1, N_samples + 1)):
         warnings.warn("Warning: sample1 does not contain points in every jackknife sample.")
-    return s1, s2, t1, t2
+    w1, w2 = ws
+    if (w1 is None or np.all(w1 == 1.0)) and (w2 is None or np.all(w2 == 1.0)):
+        return s1, s2, t1, t2, None
+    w1 = np.ones(len(s1)) if w1 is None else np.ascontiguousarray(w1.reshape(len(s1)))
+    w2 = np.ones(len(s2)) if w2 is None else np.ascontiguousarray(w2.reshape(len(s2)))
+    return s1, s2, t1, t2, (w1, w2)
 
 
-def _jackknife_tags(x1, x2, t1, t2):
-    """int32 tag arrays; the same points with different tags count as a cross-correlation."""
+def _jackknife_tags(x1, x2, t1, t2, wts=None):
+    """int32 tag arrays; the same points with different tags (or weights) count as a
+    cross-correlation."""
     j1 = np.ascontiguousarray(t1, dtype=np.int32)
-    j2 = j1 if (x2 is x1 and np.array_equal(t1, t2)) else np.ascontiguousarray(t2, dtype=np.int32)
+    same_w = wts is None or np.array_equal(wts[0], wts[1])
+    j2 = j1 if (x2 is x1 and np.array_equal(t1, t2) and same_w) else \
+        np.ascontiguousarray(t2, dtype=np.int32)
     if x2 is x1 and j2 is not j1:
         x2 = x1.copy()
     return x1, x2, j1, j2
+
+
+def _jackknife_weights(x1, x2, wts):
+    """float64 weight arrays, shared when the auto-correlation shares its samples."""
+    wa = np.ascontiguousarray(wts[0], dtype=np.float64)
+    wb = wa if x2 is x1 else np.ascontiguousarray(wts[1], dtype=np.float64)
+    return wa, wb
 
 
 def npairs_jackknife_3d(sample1, sample2, rbins, jtags1, jtags2, N_samples, period=None,
@@ -546,8 +561,8 @@ def npairs_jackknife_3d(sample1, sample2, rbins, jtags1, jtags2, N_samples, peri
     (npairs_jackknife_3d.py:29-31): row 0 is the cumulative count of all pairs,
     row s the count with subsample s removed, where a pair with one end in s
     counts one half (npairs_jackknife_3d_engine.pyx:238-289). Exact for unit
-    weights (the ``tpcf_jackknife`` case); other weights are not supported on
-    the GPU and raise ``NotImplementedError``.
+    weights (the ``tpcf_jackknife`` case); other weights are summed per pair as
+    w1 w2, within 1e-6 relative of the FP64 reference.
     """
     _check_num_threads(num_threads)
     rbins = _bins(rbins, "Input ``rbins`` must be a monotonically increasing 1D array with at "
@@ -555,13 +570,21 @@ def npairs_jackknife_3d(sample1, sample2, rbins, jtags1, jtags2, N_samples, peri
     rmax = np.max(rbins)
     _approx_cells(approx_cell1_size, [rmax] * 3, "approx_cell1_size")
     _approx_cells(approx_cell2_size, [rmax] * 3, "approx_cell2_size")
-    s1, s2, t1, t2 = _jackknife_inputs(sample1, sample2, jtags1, jtags2, N_samples, weights1,
-                                       weights2)
+    s1, s2, t1, t2, wts = _jackknife_inputs(sample1, sample2, jtags1, jtags2, N_samples,
+                                            weights1, weights2)
     _nonneg(rbins, "rbins")
     x1, x2, box, pbc = _positions(s1, s2, period, [rmax] * 3, [rmax * 3.0] * 3)
-    x1, x2, j1, j2 = _jackknife_tags(x1, x2, t1, t2)
+    x1, x2, j1, j2 = _jackknife_tags(x1, x2, t1, t2, wts)
     plan = _native.default_plan()
     out = np.zeros((int(N_samples) + 1, len(rbins)), dtype=np.float64)
+    if wts is not None:
+        wa, wb = _jackknife_weights(x1, x2, wts)
+        plan.check(plan.lib.gbp_npairs_jackknife_3d_weighted(
+            plan.handle, _native.dptr(x1), len(x1), _native.dptr(x2), len(x2),
+            _native.dptr(wa), _native.dptr(wb), _native.dptr(j1), _native.dptr(j2),
+            int(N_samples), _native.pd(rbins), len(rbins), _native.pd(box), pbc, GBP_MEM_HOST,
+            _native.pd(out)))
+        return out
     plan.check(plan.lib.gbp_npairs_jackknife_3d(
         plan.handle, _native.dptr(x1), len(x1), _native.dptr(x2), len(x2), _native.dptr(j1),
         _native.dptr(j2), int(N_samples), _native.pd(rbins), len(rbins), _native.pd(box), pbc,
@@ -579,7 +602,8 @@ def npairs_jackknife_xy_z(sample1, sample2, rp_bins, pi_bins, jtags1, jtags2, N_
     (npairs_jackknife_xy_z.py:23-26): row 0 counts all pairs, row s the pairs
     without subsample s, a pair with one end in s counting one half
     (npairs_jackknife_xy_z_engine.pyx:250-281).  Exact for unit weights; other
-    weights raise ``NotImplementedError``.
+    weights are summed per pair as w1 w2, within 1e-6 relative of the FP64
+    reference.
     """
     _check_num_threads(num_threads)
     rp_bins = _bins(rp_bins, "Input ``rp_bins`` must be a monotonically increasing 1D array "
@@ -589,15 +613,23 @@ def npairs_jackknife_xy_z(sample1, sample2, rp_bins, pi_bins, jtags1, jtags2, N_
     rpm, pim = np.max(rp_bins), np.max(pi_bins)
     _approx_cells(approx_cell1_size, [rpm, rpm, pim], "approx_cell1_size")
     _approx_cells(approx_cell2_size, [rpm, rpm, pim], "approx_cell2_size")
-    s1, s2, t1, t2 = _jackknife_inputs(sample1, sample2, jtags1, jtags2, N_samples, weights1,
-                                       weights2)
+    s1, s2, t1, t2, wts = _jackknife_inputs(sample1, sample2, jtags1, jtags2, N_samples,
+                                            weights1, weights2)
     _nonneg(rp_bins, "rp_bins")
     _nonneg(pi_bins, "pi_bins")
     x1, x2, box, pbc = _positions(s1, s2, period, [rpm, rpm, pim],
                                   [rpm * 3.0, rpm * 3.0, pim * 3.0])
-    x1, x2, j1, j2 = _jackknife_tags(x1, x2, t1, t2)
+    x1, x2, j1, j2 = _jackknife_tags(x1, x2, t1, t2, wts)
     plan = _native.default_plan()
     out = np.zeros((int(N_samples) + 1, len(rp_bins), len(pi_bins)), dtype=np.float64)
+    if wts is not None:
+        wa, wb = _jackknife_weights(x1, x2, wts)
+        plan.check(plan.lib.gbp_npairs_jackknife_xy_z_weighted(
+            plan.handle, _native.dptr(x1), len(x1), _native.dptr(x2), len(x2),
+            _native.dptr(wa), _native.dptr(wb), _native.dptr(j1), _native.dptr(j2),
+            int(N_samples), _native.pd(rp_bins), len(rp_bins), _native.pd(pi_bins),
+            len(pi_bins), _native.pd(box), pbc, GBP_MEM_HOST, _native.pd(out)))
+        return out
     plan.check(plan.lib.gbp_npairs_jackknife_xy_z(
         plan.handle, _native.dptr(x1), len(x1), _native.dptr(x2), len(x2), _native.dptr(j1),
         _native.dptr(j2), int(N_samples), _native.pd(rp_bins), len(rp_bins),

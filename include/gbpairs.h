@@ -227,6 +227,31 @@ int gbp_npairs_jackknife_xy_z(gbp_plan *plan, const double *xyz1, int64_t n1, co
                               int32_t pbc, int32_t mem, double *out);
 
 /*
+ * Weighted jackknife counts, as npairs_jackknife_3d / npairs_jackknife_xy_z with
+ * weights (jweight in npairs_jackknife_3d_engine.pyx and
+ * npairs_jackknife_xy_z_engine.pyx:250-281): row 0 sums w1_i w2_j over the
+ * ordered pairs in each cumulative bin, row s leaves out the pairs with both
+ * ends in subsample s and counts those with one end there at one half.  One FP64
+ * weight and one tag per point; host memory; out (n_samples + 1, nbins) or
+ * (n_samples + 1, n_rp, n_pi).  Sums in FP32 with an exact-error companion and an
+ * FP64 (tag, bin) table: within 1e-6 relative of the FP64 reference for
+ * non-negative weights.
+ */
+int gbp_npairs_jackknife_3d_weighted(gbp_plan *plan, const double *xyz1, int64_t n1,
+                                     const double *xyz2, int64_t n2, const double *w1,
+                                     const double *w2, const int32_t *jtags1,
+                                     const int32_t *jtags2, int32_t n_samples,
+                                     const double *rbins, int32_t nb, const double *period3,
+                                     int32_t pbc, int32_t mem, double *out);
+int gbp_npairs_jackknife_xy_z_weighted(gbp_plan *plan, const double *xyz1, int64_t n1,
+                                       const double *xyz2, int64_t n2, const double *w1,
+                                       const double *w2, const int32_t *jtags1,
+                                       const int32_t *jtags2, int32_t n_samples,
+                                       const double *rp_bins, int32_t n_rp, const double *pi_bins,
+                                       int32_t n_pi, const double *period3, int32_t pbc,
+                                       int32_t mem, double *out);
+
+/*
  * Cumulative (r_p, pi) sums of marking function `wfunc_id` (1..17), row-major
  * [n_rp][n_pi]: out[k][g] adds wfunc(w1_i, w2_j) over ordered pairs with
  * dxy^2 <= rp_bins[k]^2 and dz^2 <= pi_bins[g]^2.  Weights (N, nw) row-major

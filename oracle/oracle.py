@@ -50,6 +50,8 @@ def lib():
                                                pd, pd, i, pi64, pd]
         L.orc_npairs_jackknife_xy_z.argtypes = [pd, i64, pd, i64, pd, pd, pi64, pi64, i, pd, i,
                                                 pd, i, pd, i, pd, pd, i, pd]
+        L.orc_npairs_jackknife_3d.argtypes = [pd, i64, pd, i64, pd, pd, pi64, pi64, i, pd, i,
+                                              pd, i, pd, pd, i, pd]
         L.orc_neighbours.argtypes = [pd, i64, pd, i64, pd, pd, pd, pd, i, i, i, d, d, i, i, i,
                                      pd, i, pd, pd, i, pi64]
         L.orc_bf_npairs_3d.argtypes = [pd, i64, pd, i64, pd, i, pd, i, pi64]
@@ -243,6 +245,29 @@ def npairs_jackknife_xy_z(sample1, sample2, rp_bins, pi_bins, jtags1, jtags2, N_
                                            _pi(t2), int(N_samples), _p(rp), len(rp), _p(pi),
                                            len(pi), _p(lbox), pbc, _p(a1), _p(a2),
                                            int(num_threads), _p(out)))
+    return out
+
+
+def npairs_jackknife_3d(sample1, sample2, rbins, jtags1, jtags2, N_samples, period=None,
+                        weights1=None, weights2=None, num_threads=1, approx_cell1_size=None,
+                        approx_cell2_size=None):
+    """npairs_jackknife_3d.py:29-160 driving npairs_jackknife_3d_engine.pyx:
+    (N_samples + 1, len(rbins)) float64."""
+    rb = np.ascontiguousarray(np.atleast_1d(rbins), dtype=np.float64)
+    rmax = np.max(rb)
+    n1, n2 = len(sample1), len(sample2)
+    w1 = np.ones(n1) if weights1 is None else np.asarray(weights1, dtype=np.float64)
+    w2 = np.ones(n2) if weights2 is None else np.asarray(weights2, dtype=np.float64)
+    w1, w2 = np.ascontiguousarray(w1), np.ascontiguousarray(w2)
+    t1 = np.ascontiguousarray(jtags1, dtype=np.int64)
+    t2 = np.ascontiguousarray(jtags2, dtype=np.int64)
+    x1, x2, lbox, pbc = _geometry(sample1, sample2, [rmax] * 3, period)
+    a1 = _approx(approx_cell1_size, [rmax] * 3)
+    a2 = _approx(approx_cell2_size, [rmax] * 3)
+    out = np.zeros((int(N_samples) + 1, len(rb)), dtype=np.float64)
+    _check(lib().orc_npairs_jackknife_3d(_p(x1), n1, _p(x2), n2, _p(w1), _p(w2), _pi(t1), _pi(t2),
+                                         int(N_samples), _p(rb), len(rb), _p(lbox), pbc, _p(a1),
+                                         _p(a2), int(num_threads), _p(out)))
     return out
 
 

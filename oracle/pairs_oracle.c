@@ -129,7 +129,7 @@ static void mesh_free(mesh_t *m) {
 }
 
 enum { K_3D = 0, K_XYZ = 1, K_SMU = 2, K_MARKED = 3, K_XYZ_MARKED = 4, K_SMU_WEIGHTED = 5,
-       K_XYZ_JACK = 6, K_NEIGH = 7 };
+       K_XYZ_JACK = 6, K_NEIGH = 7, K_3D_JACK = 8 };
 
 typedef struct {
     int kind;
@@ -334,6 +334,19 @@ static void walk_range(const walk_t *w, int64_t c0, int64_t c1, int64_t *ic, dou
                                         if (k < 0) break;
                                     }
                                 }
+                            } else if (w->kind == K_3D_JACK) {
+                                /* npairs_jackknife_3d_engine.pyx: per row s, walk the
+                                   cumulative bins from the top adding jweight */
+                                double dsq = dx * dx + dy * dy + dz * dz;
+                                for (int sidx = 0; sidx <= w->nsamp; sidx++) {
+                                    int k = w->n1e - 1;
+                                    while (dsq <= w->e1[k]) {
+                                        dc[sidx * (int64_t)w->n1e + k] +=
+                                            jweight(sidx, w->t1[i], w->t2[j], w->w1[i], w->w2[j]);
+                                        k--;
+                                        if (k < 0) break;
+                                    }
+                                }
                             } else if (w->kind == K_NEIGH) {
                                 /* counts_in_cylinders_engine.pyx:262-281,
                                    spherical_isolation_engine.pyx:190-199,
@@ -442,7 +455,7 @@ static int run_walk(int kind, const double *xyz1, int64_t n1, const double *xyz2
     }
     double *wb = NULL;
     int64_t *tb = NULL;
-    if (kind == K_XYZ_JACK) {
+    if (kind == K_XYZ_JACK || kind == K_3D_JACK) {
         tb = (int64_t *)malloc(sizeof(int64_t) * (s1 + s2));
         if (!tb) { free(buf); mesh_free(&w.m1); mesh_free(&w.m2); return -1; }
         w.t1 = tb; w.t2 = tb + s1;
@@ -451,7 +464,7 @@ static int run_walk(int kind, const double *xyz1, int64_t n1, const double *xyz2
         w.nsamp = nsamp;
     }
     if (kind == K_MARKED || kind == K_XYZ_MARKED || kind == K_SMU_WEIGHTED || kind == K_XYZ_JACK ||
-        kind == K_NEIGH) {
+        kind == K_NEIGH || kind == K_3D_JACK) {
         wb = (double *)malloc(sizeof(double) * (size_t)nw * (s1 + s2));
         if (!wb) { free(buf); mesh_free(&w.m1); mesh_free(&w.m2); return -1; }
         w.w1 = wb; w.w2 = wb + (size_t)nw * s1;
@@ -467,6 +480,7 @@ static int run_walk(int kind, const double *xyz1, int64_t n1, const double *xyz2
 
     int64_t nout = (kind == K_3D || kind == K_MARKED) ? n1e : (int64_t)n1e * n2e;
     if (kind == K_XYZ_JACK) nout *= (int64_t)(nsamp + 1);
+    if (kind == K_3D_JACK) nout = (int64_t)n1e * (nsamp + 1);
     if (kind == K_NEIGH) nout = n1 > 0 ? n1 : 1;  /* one count per sorted sample-1 point */
     double *dsum = NULL;
     if (nthreads < 1) nthreads = 1;
@@ -684,6 +698,25 @@ int orc_npairs_jackknife_xy_z(const double *xyz1, int64_t n1, const double *xyz2
     int rc = run_walk(K_XYZ_JACK, xyz1, n1, xyz2, n2, w1, w2, 1, 0, tags1, tags2, nsamp, e1, nrp,
                       e2, npi, 0, 0, period, pbc, search, approx1, approx2, nthreads, NULL, out, NULL);
     free(e1);
+    return rc;
+}
+
+/* npairs_jackknife_3d_engine: out[s][k] = sum of jweight(s, ...) over ordered pairs
+   with dsq <= rbins[k]^2; w1, w2 one weight per point */
+int orc_npairs_jackknife_3d(const double *xyz1, int64_t n1, const double *xyz2, int64_t n2,
+                            const double *w1, const double *w2, const int64_t *tags1,
+                            const int64_t *tags2, int nsamp, const double *rbins, int nb,
+                            const double period[3], int pbc, const double approx1[3],
+                            const double approx2[3], int nthreads, double *out) {
+    double *e = (double *)malloc(sizeof(double) * (size_t)nb);
+    if (!e) return -1;
+    double rmax = rbins[0];
+    for (int k = 0; k < nb; k++) { e[k] = rbins[k] * rbins[k]; if (rbins[k] > rmax) rmax = rbins[k]; }
+    double search[3] = {rmax, rmax, rmax};
+    int rc = run_walk(K_3D_JACK, xyz1, n1, xyz2, n2, w1, w2, 1, 0, tags1, tags2, nsamp, e, nb,
+                      NULL, 0, 0, 0, period, pbc, search, approx1, approx2, nthreads, NULL, out,
+                      NULL);
+    free(e);
     return rc;
 }
 

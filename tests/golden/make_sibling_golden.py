@@ -127,6 +127,18 @@ CASES = {
     "marked_xy_z_threes_auto_pbc": ("marked_npairs_xy_z", lambda m, s1, s2, t1, t2: m.marked_npairs_xy_z(
         s1, s1, RP, PI, weights1=np.full(len(s1), 3.0), weights2=np.full(len(s1), 3.0),
         weight_func_id=1, period=L)),
+    "jackknife_w_auto_pbc": ("npairs_jackknife_3d", lambda m, s1, s2, t1, t2:
+                             m.npairs_jackknife_3d(s1, s1, RBINS, t1, t1, 5, period=L,
+                                                   weights1=_wt()[2][:, 0],
+                                                   weights2=_wt()[2][:, 0])),
+    "jackknife_w_cross_nopbc": ("npairs_jackknife_3d", lambda m, s1, s2, t1, t2:
+                                m.npairs_jackknife_3d(s1, s2, RBINS, t1, t2, 5,
+                                                      weights1=_wt()[2][:, 0],
+                                                      weights2=_wt()[3][:, 0])),
+    "jackknife_xy_z_w_auto_pbc": ("npairs_jackknife_xy_z", lambda m, s1, s2, t1, t2:
+                                  m.npairs_jackknife_xy_z(s1, s1, RP, PI, t1, t1, 5, period=L,
+                                                          weights1=_wt()[2][:, 1],
+                                                          weights2=_wt()[2][:, 1])),
     "jackknife_xy_z_auto_pbc": ("npairs_jackknife_xy_z", lambda m, s1, s2, t1, t2:
                                 m.npairs_jackknife_xy_z(s1, s1, RP, PI, t1, t1, 5, period=L)),
     "jackknife_xy_z_cross_pbc": ("npairs_jackknife_xy_z", lambda m, s1, s2, t1, t2:

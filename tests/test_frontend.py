@@ -125,9 +125,6 @@ def test_jackknife_xy_z_messages():
         h.npairs_jackknife_xy_z(S, S, [0.1, 0.2], [0.1, 0.2], t, t, 1, period=1,
                                 weights1=np.ones(49))
     assert "weights1 should have same len as sample1" in str(err.value)
-    with pytest.raises(NotImplementedError):
-        h.npairs_jackknife_xy_z(S, S, [0.1, 0.2], [0.1, 0.2], t, t, 1, period=1,
-                                weights1=np.full(50, 2.0))
 
 
 def test_neighbour_messages():

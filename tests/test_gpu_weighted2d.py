@@ -211,3 +211,59 @@ def test_jackknife_xy_z_cross_and_blocks(gpu):
         got = gpu.npairs_jackknife_xy_z(s1, s2, rp, pi, t1, t2, 27, period=L)
         assert plan.stats()["block"] == 2
     assert np.array_equal(got, want)
+
+
+# ---------------- weighted jackknife (3-D and (rp, pi)) ----------------
+@pytest.mark.parametrize("pbc", [True, False])
+def test_weighted_jackknife_3d_matches_oracle(gpu, pbc):
+    rng = np.random.default_rng(90)
+    L = 300.0
+    s = clustered(rng, 30000, L, 1500)
+    t = _cuboid_tags(s, L)
+    w = rng.uniform(0.2, 2.0, len(s))
+    rb = np.logspace(-1, np.log10(20), 12)
+    per = L if pbc else None
+    want = oracle.npairs_jackknife_3d(s, s, rb, t, t, 27, period=per, weights1=w, weights2=w,
+                                      num_threads=8)
+    got = gpu.npairs_jackknife_3d(s, s, rb, t, t, 27, period=per, weights1=w, weights2=w)
+    assert got.shape == (28, 12)
+    _close(got, want)
+
+
+def test_weighted_jackknife_cross_and_integer_weights(gpu):
+    rng = np.random.default_rng(91)
+    L = 250.0
+    s1 = clustered(rng, 20000, L, 1000)
+    s2 = rng.uniform(0, L, (15000, 3))
+    t1, t2 = _cuboid_tags(s1, L), _cuboid_tags(s2, L)
+    w1, w2 = rng.uniform(0.2, 2.0, len(s1)), rng.uniform(0.2, 2.0, len(s2))
+    rb = np.logspace(-1, np.log10(15), 10)
+    rp, pi = np.logspace(-1, np.log10(15), 10), np.linspace(0, 20, 11)
+    _close(gpu.npairs_jackknife_3d(s1, s2, rb, t1, t2, 27, period=L, weights1=w1, weights2=w2),
+           oracle.npairs_jackknife_3d(s1, s2, rb, t1, t2, 27, period=L, weights1=w1,
+                                      weights2=w2, num_threads=8))
+    _close(gpu.npairs_jackknife_xy_z(s1, s2, rp, pi, t1, t2, 27, period=L, weights1=w1,
+                                     weights2=w2),
+           oracle.npairs_jackknife_xy_z(s1, s2, rp, pi, t1, t2, 27, period=L, weights1=w1,
+                                        weights2=w2, num_threads=8))
+    # weights of 2: every product is 4, so the weighted rows are exactly 4x the counts
+    two1, two2 = np.full(len(s1), 2.0), np.full(len(s2), 2.0)
+    assert np.array_equal(
+        gpu.npairs_jackknife_3d(s1, s1, rb, t1, t1, 27, period=L, weights1=two1, weights2=two1),
+        4.0 * gpu.npairs_jackknife_3d(s1, s1, rb, t1, t1, 27, period=L))
+    assert np.array_equal(
+        gpu.npairs_jackknife_xy_z(s1, s2, rp, pi, t1, t2, 27, period=L, weights1=two1,
+                                  weights2=two2),
+        4.0 * gpu.npairs_jackknife_xy_z(s1, s2, rp, pi, t1, t2, 27, period=L))
+
+
+def test_weighted_jackknife_xy_z_auto_matches_oracle(gpu):
+    rng = np.random.default_rng(92)
+    L = 300.0
+    s = clustered(rng, 25000, L, 1200)
+    t = _cuboid_tags(s, L)
+    w = rng.lognormal(0.0, 0.5, len(s))
+    rp, pi = np.logspace(-1, np.log10(20), 12), np.linspace(0, 25, 11)
+    _close(gpu.npairs_jackknife_xy_z(s, s, rp, pi, t, t, 27, period=L, weights1=w, weights2=w),
+           oracle.npairs_jackknife_xy_z(s, s, rp, pi, t, t, 27, period=L, weights1=w,
+                                        weights2=w, num_threads=8))

@@ -73,7 +73,8 @@ from tests.golden import make_sibling_golden as S  # noqa: E402
 # (the oracle has no pair list: the index cases are checked on the GPU only)
 _W2_CASES = sorted(n for n in S.CASES
                    if S.CASES[n][0] in ("marked_npairs_xy_z", "weighted_npairs_s_mu",
-                                        "npairs_jackknife_xy_z", "counts_in_cylinders",
+                                        "npairs_jackknife_xy_z", "npairs_jackknife_3d",
+                                        "counts_in_cylinders",
                                         "spherical_isolation", "cylindrical_isolation",
                                         "conditional_spherical_isolation",
                                         "conditional_cylindrical_isolation")
