@@ -268,6 +268,74 @@ def extra_differentiable(dev, reps=3):
             "dC_dtheta_last_bin": [float(v) for v in g.cpu().numpy()]}
 
 
+def extra_batched_adjoint(dev, reps=3, m=16):
+    """Batched + adjoint (the configurations' target): 16 Zheng07 parameter draws on the
+    config-4 halo table (2M halos, L = 1000; draws as config 3: logMmin ~ U[11.8, 12.4],
+    sigma_logM ~ U[0.2, 0.5], logM0 = logMmin, logM1 = logMmin + 1.3, alpha ~ U[0.9, 1.1]),
+    weighted npairs_3d over 20 log bins 0.1-30 and dC/dtheta for every draw: one forward
+    pass over all draws and one adjoint pass per 8 draws, against the same 16 forward +
+    backward steps run one draw at a time on the same GPU."""
+    import torch
+    from halotools_gb300 import differentiable as D, mocks
+    L = 1000.0
+    pos, mass, _ = mocks.halo_table(2_000_000, L, seed=21)
+    rb = np.logspace(-1, np.log10(30), 20)
+    rng = np.random.default_rng(31)
+    lmin = rng.uniform(11.8, 12.4, m)
+    th = np.stack([lmin, rng.uniform(0.2, 0.5, m), lmin, lmin + 1.3, rng.uniform(0.9, 1.1, m)],
+                  axis=1)
+    xd = torch.from_numpy(pos).cuda(dev)
+    md = torch.from_numpy(mass).cuda(dev)
+    gbar = torch.ones((m, len(rb)), dtype=torch.float64, device=f"cuda:{dev}")
+    stream = torch.cuda.current_stream(dev)
+
+    def batched():
+        T = torch.tensor(th, dtype=torch.float64, device=f"cuda:{dev}", requires_grad=True)
+        C = D.hod_pair_counts_batched(T, xd, md, rb, L)
+        (C * gbar).sum().backward()
+        return C, T.grad
+
+    def single():
+        out = []
+        for k in range(m):
+            t1 = torch.tensor(th[k], dtype=torch.float64, device=f"cuda:{dev}",
+                              requires_grad=True)
+            c1 = D.hod_pair_counts(t1, xd, md, rb, L)
+            (c1 * gbar[k]).sum().backward()
+            out.append(t1.grad)
+        return out
+
+    def timed(fn):
+        fn()
+        t = []
+        for _ in range(reps):
+            a, b = _events()
+            a.record(stream)
+            r = fn()
+            b.record(stream)
+            torch.cuda.synchronize()
+            t.append(a.elapsed_time(b) / 1e3)
+        return float(np.median(t)), r
+    tb, (C, G) = timed(batched)
+    ts, g1 = timed(single)
+
+    def forward_only():
+        with torch.no_grad():
+            T = torch.tensor(th, dtype=torch.float64, device=f"cuda:{dev}")
+            return D.hod_pair_counts_batched(T, xd, md, rb, L)
+    tf, _ = timed(forward_only)
+    import halotools_gb300 as H
+    pairs = int(H.npairs_3d(pos, pos, rb, period=L)[-1])
+    gerr = max(float(np.max(np.abs(G[k].cpu().numpy() - g1[k].cpu().numpy()) /
+                            np.abs(g1[k].cpu().numpy()).max())) for k in range(m))
+    return {"halos": len(pos), "draws": m, "in_range_pairs_per_draw": pairs,
+            "batched_ms": tb * 1e3, "batched_forward_ms": tf * 1e3, "single_draws_ms": ts * 1e3,
+            "speedup": ts / tb,
+            "batched_pair_evals_per_s": 2 * m * pairs / tb,
+            "single_pair_evals_per_s": 2 * m * pairs / ts,
+            "max_rel_dtheta_diff_vs_single": gerr, "passes": 2}
+
+
 _POINTS_10M = []
 
 
@@ -511,6 +579,7 @@ def extra_siblings_10m(dev, threads):
 EXTRAS = {
     "batched_hod64": lambda dev, threads: extra_batched(dev),
     "differentiable_2m": lambda dev, threads: extra_differentiable(dev),
+    "batched_adjoint_2m": lambda dev, threads: extra_batched_adjoint(dev),
     "npairs_3d_10m": extra_npairs_3d_10m,
     "marked_10m": extra_marked_10m,
     "s_mu_10m": extra_s_mu_10m,

@@ -32,7 +32,8 @@ EXPORTED = (
     "gbp_npairs_per_object_3d", "gbp_marked_npairs_xy_z", "gbp_weighted_npairs_s_mu",
     "gbp_npairs_jackknife_xy_z", "gbp_counts_in_cylinders", "gbp_cylinder_pairs",
     "gbp_isolation", "gbp_hod_mocks", "gbp_npairs_jackknife_3d_weighted",
-    "gbp_npairs_jackknife_xy_z_weighted",
+    "gbp_npairs_jackknife_xy_z_weighted", "gbp_weighted_adjoint_3d_channels",
+    "gbp_zheng07_weights_batched", "gbp_zheng07_vjp_batched",
     "gbp_weighted_adjoint_3d", "gbp_zheng07_weights", "gbp_zheng07_vjp",
 )
 
@@ -138,6 +139,10 @@ def load(build_if_missing: bool = True):
                                                        pd, i32, pd, i32, i32, pd]
         L.gbp_npairs_jackknife_xy_z_weighted.argtypes = [vp, vp, i64, vp, i64, vp, vp, vp, vp,
                                                          i32, pd, i32, pd, i32, pd, i32, i32, pd]
+        L.gbp_weighted_adjoint_3d_channels.argtypes = [vp, vp, i64, vp, i32, pd, i32, pd, i32,
+                                                       i32, pd, vp]
+        L.gbp_zheng07_weights_batched.argtypes = [vp, vp, i64, pd, i32, i32, vp]
+        L.gbp_zheng07_vjp_batched.argtypes = [vp, vp, i64, pd, i32, vp, i32, pd]
         L.gbp_hod_mocks.argtypes = [vp, vp, vp, vp, vp, i64, pd, i32, ctypes.c_double,
                                     ctypes.c_uint64, i32, vp, i64, pi64]
         pcond = P(NeighCond)

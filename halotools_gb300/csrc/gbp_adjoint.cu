@@ -236,6 +236,213 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_gather(const CountArgs a) {
     if (lane == 0 && cand) atomicAdd(a.nrecheck + 1, cand);
 }
 
+// Bins of one pair in both orders (k1 == k2 when FP32 decides), as slow_adj forms
+// its mean over the two orders
+__device__ __noinline__ int2 slow_adj_bins(float v, int b0, int is, int js, const AxisSm &A,
+                                           const CountArgs &a) {
+    int k = walk_bin(v, b0, A);
+    if (k >= 0) return make_int2(k, k);
+    if (is < 0 || js < 0) return make_int2(A.nb, A.nb);  // never a real pair
+    atomicAdd(a.nrecheck, 1ull);
+    double p[3], q[3];
+    ref_pos(a, 0, is, p);
+    ref_pos(a, 1, js, q);
+    return make_int2(exact_bin(exact_pair(p, q, a).s2, b0, A),
+                     exact_bin(exact_pair(q, p, a).s2, b0, A));
+}
+
+// k_gather_ch: the adjoint gather over up to NCH weight channels at once (one
+// parameter draw per channel): each in-range pair is binned once, then channel c
+// adds w_j^c G^c(bin) to the i-point's compensated sum in registers, so the
+// distance work is shared by all channels.
+template <int NCH>
+__global__ void __launch_bounds__(GBP_BLOCK, 2) k_gather_ch(const CountArgs a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    constexpr unsigned FULL = 0xffffffffu;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nb0 = a.ax[0].nb, T0 = a.ax[0].T, nch = a.nw;
+    const SmemLayout L = gbp_smem_layout(MODE_ADJC, T0, 0, nb0, 0, a.nsten, 0, 4 * NCH);
+    if (gbp_smem_too_small(L.total, a.err)) return;
+    float4 *s_lut0 = (float4 *)(smem + L.off_lut0);
+    float4 *jb = (float4 *)(smem + L.off_j) + warp * 32;
+    ulonglong2 *jxy = (ulonglong2 *)(smem + L.off_j2) + warp * 32;
+    unsigned long long *jzz = (unsigned long long *)(smem + L.off_j2 + GBP_JCAP * 16) + warp * 32;
+    float *jw = (float *)(smem + L.off_jw) + warp * 32 * NCH;
+    float4 *s_D = (float4 *)(smem + L.off_D);
+    double *s_E0 = (double *)(smem + L.off_E0);
+    float *s_hi0 = (float *)(smem + L.off_hi0);
+    float *s_lo0 = (float *)(smem + L.off_lo0);
+    int *s_off = (int *)(smem + L.off_off);
+    const int nbc = nb0 + 1;
+    float *s_gt = (float *)(smem + L.off_hist);  // [channel][bin]
+    for (int i = tid; i < T0; i += GBP_BLOCK) s_lut0[i] = a.ax[0].lut[i];
+    for (int i = tid; i < nb0; i += GBP_BLOCK) {
+        s_E0[i] = a.ax[0].E[i];
+        s_hi0[i] = a.ax[0].hi[i];
+        s_lo0[i] = a.ax[0].lo[i];
+    }
+    for (int i = tid; i < NCH * nbc; i += GBP_BLOCK) s_gt[i] = i < nch * nbc ? a.gt[i] : 0.f;
+    for (int i = tid; i < a.nsten; i += GBP_BLOCK) {
+        s_off[i] = a.sten[i];
+        s_D[i] = a.stenD[i];
+    }
+    AxisSm A0{s_lut0, s_hi0, s_lo0, s_E0, nb0, a.ax[0].S, a.ax[0].B, a.ax[0].vlo, a.ax[0].vhi};
+    const int nitems = *a.nitems;
+    const int n1 = a.n[1], n2 = a.n[2];
+    const float R0 = fmaf(a.top0, 0x1p-18f, a.top0) + 1.0e-30f;
+    const unsigned long long RR0 = pk2(R0, R0);
+    unsigned long long cand = 0;
+    __syncthreads();
+
+    while (true) {
+        int it = 0;
+        if (lane == 0) it = atomicAdd(a.counter, 1);
+        it = __shfl_sync(FULL, it, 0);
+        if (it >= nitems) break;
+        const int4 item = a.items[it];
+        const int cell = item.x, ifirst = item.y;
+        const int icnt = item.z & 127, s0 = (item.z >> 7) & 1023, s1 = (item.z >> 17) & 1023;
+        const int cz = cell % n2, cy = (cell / n2) % n1, cx = cell / (n1 * n2);
+        float4 u0 = make_float4(GBP_FAR, GBP_FAR, GBP_FAR, __int_as_float(0));
+        float4 u1 = u0;
+        if (lane < icnt) u0 = a.pos1[ifirst + lane];
+        if (lane + 32 < icnt) u1 = a.pos1[ifirst + 32 + lane];
+        const unsigned long long UX = pk2(u0.x, u1.x), UY = pk2(u0.y, u1.y), UZ = pk2(u0.z, u1.z);
+        float acc0[NCH], cmp0[NCH], acc1[NCH], cmp1[NCH];  // Kahan: sum ~ acc - cmp
+#pragma unroll
+        for (int c = 0; c < NCH; c++) acc0[c] = cmp0[c] = acc1[c] = cmp1[c] = 0.f;
+        for (int sb = s0; sb < s1; sb += 32) {
+            const int s = sb + lane;
+            int st = 0, cn = 0;
+            float4 D = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (s < s1) {
+                D = s_D[s];
+                const int key = gbp_run_key(s_off[s], cx, cy, cz, a.n, a.pbc, 0, a.bf3);
+                if (key >= 0) {
+                    st = a.start2[key];
+                    cn = a.start2[key + __float_as_int(D.w)] - st;
+                }
+            }
+            int incl = cn;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(FULL, incl, o);
+                if (lane >= o) incl += t;
+            }
+            const int T = __shfl_sync(FULL, incl, 31);
+            cand += (unsigned long long)icnt * (unsigned long long)T;
+            for (int f0 = 0; f0 < T; f0 += 32) {
+                const int f = f0 + lane;
+                int k = 0;
+#pragma unroll
+                for (int step = 16; step > 0; step >>= 1) {
+                    const int v = __shfl_sync(FULL, incl, k + step - 1);
+                    if (v <= f) k += step;
+                }
+                k &= 31;
+                const int stk = __shfl_sync(FULL, st, k);
+                const int exk = __shfl_sync(FULL, incl - cn, k);
+                const float Dx = __shfl_sync(FULL, D.x, k), Dy = __shfl_sync(FULL, D.y, k),
+                            Dz = __shfl_sync(FULL, D.z, k);
+                if (f < T) {
+                    const int j = stk + (f - exk);
+                    const float4 p = a.pos2[j];
+                    const float tx = p.x + Dx, ty = p.y + Dy, tz = p.z + Dz;
+                    jb[lane] = make_float4(tx, ty, tz, p.w);
+                    jxy[lane] = make_ulonglong2(pk2(tx, tx), pk2(ty, ty));
+                    jzz[lane] = pk2(tz, tz);
+#pragma unroll
+                    for (int c = 0; c < NCH; c++)
+                        jw[lane * NCH + c] = c < nch ? a.w2[(int64_t)j * nch + c] : 0.f;
+                }
+                __syncwarp();
+                const int nj = min(32, T - f0);
+                unsigned o0 = 0u, o1 = 0u;
+#pragma unroll 8
+                for (int jj = 0; jj < 32; jj++) {
+                    const ulonglong2 txy = jxy[jj];
+                    const unsigned long long dX = f2_sub(UX, txy.x), dY = f2_sub(UY, txy.y),
+                                             dZ = f2_sub(UZ, jzz[jj]);
+                    const unsigned long long d =
+                        f2_sub(RR0, f2_fma(dZ, dZ, f2_fma(dY, dY, f2_mul(dX, dX))));
+                    o0 = __funnelshift_l((unsigned)d, o0, 1);
+                    o1 = __funnelshift_l((unsigned)(d >> 32), o1, 1);
+                }
+                const unsigned valid = nj >= 32 ? 0xffffffffu : ((1u << nj) - 1u);
+                unsigned m0 = __brev(~o0) & valid, m1 = __brev(~o1) & valid;
+                while (m0 | m1) {
+                    const bool first = m0 != 0u;
+                    const int jj = 31 - __clz(first ? m0 : m1);
+                    if (first) m0 ^= 1u << jj;
+                    else m1 ^= 1u << jj;
+                    const float4 u = first ? u0 : u1;
+                    const float4 t = jb[jj];
+                    const float dx = u.x - t.x, dy = u.y - t.y, dz = u.z - t.z;
+                    const float v = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+                    const float4 e = lut_entry(v, A0);
+                    int2 kk;
+                    if ((v > e.z) & !(v > e.y)) {
+                        kk = slow_adj_bins(v, __float_as_int(e.x), __float_as_int(u.w),
+                                           __float_as_int(t.w), A0, a);
+                    } else {
+                        const int b = __float_as_int(e.x) + (v > e.y ? 1 : 0);
+                        kk = make_int2(b, b);
+                    }
+                    const float *wj = jw + jj * NCH;
+                    if (first) {
+#pragma unroll
+                        for (int c = 0; c < NCH; c++) {
+                            const float g = 0.5f * (s_gt[c * nbc + kk.x] + s_gt[c * nbc + kk.y]);
+                            const float y = fmaf(wj[c], g, -cmp0[c]), s2 = acc0[c] + y;
+                            cmp0[c] = (s2 - acc0[c]) - y;
+                            acc0[c] = s2;
+                        }
+                    } else {
+#pragma unroll
+                        for (int c = 0; c < NCH; c++) {
+                            const float g = 0.5f * (s_gt[c * nbc + kk.x] + s_gt[c * nbc + kk.y]);
+                            const float y = fmaf(wj[c], g, -cmp1[c]), s2 = acc1[c] + y;
+                            cmp1[c] = (s2 - acc1[c]) - y;
+                            acc1[c] = s2;
+                        }
+                    }
+                }
+                __syncwarp();
+            }
+        }
+        // this item's sums of the lane's two points: dL/dw rows (caller's order)
+#pragma unroll
+        for (int c = 0; c < NCH; c++) {
+            if (c < nch && lane < icnt)
+                atomicAdd(&a.grad[(int64_t)a.orig[ifirst + lane] * nch + c],
+                          2.0 * ((double)acc0[c] - (double)cmp0[c]));
+            if (c < nch && lane + 32 < icnt)
+                atomicAdd(&a.grad[(int64_t)a.orig[ifirst + 32 + lane] * nch + c],
+                          2.0 * ((double)acc1[c] - (double)cmp1[c]));
+        }
+    }
+    if (lane == 0 && cand) atomicAdd(a.nrecheck + 1, cand);
+}
+
+cudaError_t gbp_launch_adjoint_ch(const CountArgs &a, int grid, size_t smem, cudaStream_t st) {
+    cudaError_t e = cudaFuncSetAttribute(k_gather_ch<GBP_ADJ_CH>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k_gather_ch<GBP_ADJ_CH><<<grid, GBP_BLOCK, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+int gbp_adjoint_ch_occupancy(size_t smem) {
+    int nblk = 0;
+    if (cudaFuncSetAttribute(k_gather_ch<GBP_ADJ_CH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem) != cudaSuccess)
+        return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nblk, k_gather_ch<GBP_ADJ_CH>, GBP_BLOCK,
+                                                      smem) != cudaSuccess)
+        return 0;
+    return nblk;
+}
+
 template <bool POBJ>
 static cudaError_t gather_launch(const CountArgs &a, int grid, size_t smem, cudaStream_t st) {
     cudaError_t e = cudaFuncSetAttribute(k_gather<POBJ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -319,6 +526,99 @@ __global__ void k_zheng07_vjp(const double *__restrict__ mass, int64_t n, Zheng0
         for (int w = 0; w < GBP_WARPS; w++) v += red[threadIdx.x][w];
         atomicAdd(&out5[threadIdx.x], v);
     }
+}
+
+// ---------------- Zheng07 weights for many parameter vectors ----------------
+// The occupations in FP32 (the counting kernels multiply the weights in FP32
+// anyway, and GB300's FP64 units are slow) from an FP64 log10 M computed once per
+// halo; W is (n, M) row-major: halo i, draw m.
+__global__ void k_log10(const double *__restrict__ mass, int64_t n, double *__restrict__ lm) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        lm[i] = log10(mass[i]);
+}
+
+__device__ __forceinline__ void zheng07_terms_f(double M, double lm, const Zheng07 &t,
+                                                float *ncen, float *nsat, float *x, float *r) {
+    *x = (float)((lm - t.logMmin) * t.inv_sigma);
+    *ncen = 0.5f * (1.0f + erff(*x));
+    *r = (float)((M - t.M0) * t.inv_M1);
+    *nsat = M > t.M0 ? powf(*r, (float)t.alpha) : 0.0f;
+}
+
+__global__ void k_zheng07_wb(const double *__restrict__ mass, const double *__restrict__ lm,
+                             int64_t n, const Zheng07 *__restrict__ th, int nth,
+                             double *__restrict__ W) {
+    const int64_t total = n * nth;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = e / nth;
+        const int m = (int)(e - i * nth);
+        float nc, ns, x, r;
+        zheng07_terms_f(mass[i], lm[i], th[m], &nc, &ns, &x, &r);
+        W[e] = (double)nc + (double)ns;
+    }
+}
+
+// out[m][5] += sum_i gW[i][m] dw_i/dtheta_m: warp gw keeps draw m = gw % nth and
+// strides over 32-halo chunks, so its terms reduce by shuffles to one add each
+__global__ void k_zheng07_vjpb(const double *__restrict__ mass, const double *__restrict__ lm,
+                               int64_t n, const Zheng07 *__restrict__ th, int nth,
+                               const double *__restrict__ gW, int nwarps, double *out) {
+    const int gw = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (gw >= nwarps) return;  // (whole warps)
+    const int m = gw % nth, wstep = nwarps / nth;
+    const Zheng07 t = th[m];
+    const float ln10 = 2.302585093f;
+    const float c2 = (float)(-t.M0 * 2.30258509299404568402 * t.inv_M1);
+    double d[5] = {0, 0, 0, 0, 0};
+    for (int64_t c = gw / nth; c * 32 < n; c += wstep) {
+        const int64_t i = c * 32 + lane;
+        if (i >= n) continue;
+        const double g = gW[i * nth + m];
+        float nc, ns, x, r;
+        zheng07_terms_f(mass[i], lm[i], t, &nc, &ns, &x, &r);
+        // d/dx of (1 + erf x)/2 is exp(-x^2)/sqrt(pi)
+        const float dphi = expf(-x * x) * 0.5641895835f;
+        d[0] += g * (double)(-dphi * (float)t.inv_sigma);      // logMmin
+        d[1] += g * (double)(-dphi * x * (float)t.inv_sigma);  // sigma_logM
+        if (ns > 0.0f) {
+            d[2] += g * (double)((float)t.alpha * ns / r * c2);  // logM0
+            d[3] += g * (double)(-(float)t.alpha * ln10 * ns);   // logM1
+            d[4] += g * (double)(ns * logf(r));                  // alpha
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 5; k++) {
+        double v = d[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0 && v != 0.0) atomicAdd(&out[m * 5 + k], v);
+    }
+}
+
+cudaError_t gbp_launch_zheng07_wb(const double *mass, double *lm, int64_t n, const Zheng07 *th,
+                                  int nth, double *W, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    k_log10<<<(unsigned)std::min<int64_t>((n + 255) / 256, 152 * 16), 256, 0, st>>>(mass, n, lm);
+    const int64_t total = n * nth;
+    const unsigned g = (unsigned)std::min<int64_t>((total + 255) / 256, 152 * 16);
+    k_zheng07_wb<<<g, 256, 0, st>>>(mass, lm, n, th, nth, W);
+    return cudaGetLastError();
+}
+
+cudaError_t gbp_launch_zheng07_vjpb(const double *mass, double *lm, int64_t n, const Zheng07 *th,
+                                    int nth, const double *gW, double *out, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    k_log10<<<(unsigned)std::min<int64_t>((n + 255) / 256, 152 * 16), 256, 0, st>>>(mass, n, lm);
+    // a whole number of warps per draw
+    const int64_t chunks = (n + 31) / 32;
+    const int per = (int)std::max<int64_t>(1, std::min<int64_t>(chunks, (152 * 16 * 8) / nth));
+    const int nwarps = per * nth;
+    k_zheng07_vjpb<<<(unsigned)((nwarps + 7) / 8), 256, 0, st>>>(mass, lm, n, th, nth, gW, nwarps,
+                                                                  out);
+    return cudaGetLastError();
 }
 
 cudaError_t gbp_launch_zheng07_w(const double *mass, int64_t n, Zheng07 th, double *w,

@@ -241,7 +241,10 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
     size_t o_items = cv.take<int4>(max_items);
     size_t o_itmp = cv.take<int>(2 * ((size_t)nkeys + 2));
     size_t o_offs = cv.take<int64_t>((size_t)nm + 1);
-    const bool adj = c.mode == MODE_ADJ;
+    const bool adjc = c.mode == MODE_ADJC;  // several weight channels
+    const bool adj = c.mode == MODE_ADJ || adjc;
+    const size_t ngrad = (size_t)c.n1 * (size_t)(adjc ? c.nw : 1);  // dL/dw entries
+    const size_t ngt = adj ? c.gt.size() : (size_t)nb0 + 1;         // gradient-table floats
     const bool pobj = c.mode == MODE_POBJ;
     const bool neigh = c.mode == MODE_NEIGH;
     const size_t npobj = pobj ? (size_t)c.n1 * (size_t)(nb0 + 1) : neigh ? (size_t)c.n1 : 0;
@@ -250,8 +253,8 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
     size_t o_poff = cv.take<long long>(plist ? (size_t)c.n1 + 1 : 1);
     size_t o_pcur = cv.take<unsigned>(plist ? (size_t)std::max<int64_t>(c.n1, 1) : 1);
     size_t o_pairs = cv.take<unsigned>(plist ? 2 * (size_t)std::max<int64_t>(c.npairs, 1) : 1);
-    size_t o_gt = cv.take<float>((size_t)nb0 + 1);
-    size_t o_grad = cv.take<double>(adj && c.mem == GBP_MEM_HOST ? (size_t)c.n1 : 1);
+    size_t o_gt = cv.take<float>(std::max<size_t>(ngt, 1));
+    size_t o_grad = cv.take<double>(adj && c.mem == GBP_MEM_HOST ? std::max<size_t>(ngrad, 1) : 1);
     size_t o_pobj = cv.take<unsigned>(npobj > 0 ? npobj : 1);
     size_t o_lut0 = cv.take<float4>(T0), o_lut1 = cv.take<float4>(std::max(T1, 1));
     size_t o_E0 = cv.take<double>(nb0), o_E1 = cv.take<double>(std::max(nb1, 1));
@@ -277,7 +280,7 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
     size_t h_hi1 = hv.take<float>(std::max(nb1, 1)), h_lo1 = hv.take<float>(std::max(nb1, 1));
     size_t h_sten = hv.take<int>(nsten), h_stenD = hv.take<float4>(nsten);
     size_t h_offs = hv.take<int64_t>((size_t)nm + 1);
-    size_t h_gt = hv.take<float>((size_t)nb0 + 1);
+    size_t h_gt = hv.take<float>(std::max<size_t>(ngt, 1));
     size_t h_end = hv.take<char>(0);
     size_t h_hist = hv.take<unsigned long long>(nhist * nm);
     size_t h_histd = hv.take<double>(nhist * nm);
@@ -299,7 +302,7 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
     std::memcpy(at<char>(H, h_sten), c.g.sten, sizeof(int) * nsten);
     std::memcpy(at<char>(H, h_stenD), c.g.stenD, sizeof(float4) * nsten);
     if (nm > 1) std::memcpy(at<char>(H, h_offs), c.offsets.data(), sizeof(int64_t) * (nm + 1));
-    if (adj) std::memcpy(at<char>(H, h_gt), c.gt.data(), sizeof(float) * (nb0 + 1));
+    if (adj) std::memcpy(at<char>(H, h_gt), c.gt.data(), sizeof(float) * ngt);
 
     int launches = 0;
     int64_t h2d = 0, d2h = 0;
@@ -328,8 +331,8 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
         CK(cudaMemcpyAsync(at<char>(W, o_sten), at<char>(H, h_sten), sizeof(int) * nsten, cudaMemcpyHostToDevice, st));
         CK(cudaMemcpyAsync(at<char>(W, o_stenD), at<char>(H, h_stenD), sizeof(float4) * nsten, cudaMemcpyHostToDevice, st));
         if (adj) {
-            CK(cudaMemcpyAsync(at<char>(W, o_gt), at<char>(H, h_gt), sizeof(float) * (nb0 + 1), cudaMemcpyHostToDevice, st));
-            h2d += (int64_t)(sizeof(float) * (nb0 + 1));
+            CK(cudaMemcpyAsync(at<char>(W, o_gt), at<char>(H, h_gt), sizeof(float) * ngt, cudaMemcpyHostToDevice, st));
+            h2d += (int64_t)(sizeof(float) * ngt);
         }
         if (nm > 1) {
             CK(cudaMemcpyAsync(at<char>(W, o_offs), at<char>(H, h_offs), sizeof(int64_t) * (nm + 1), cudaMemcpyHostToDevice, st));
@@ -486,6 +489,7 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
                         : (c.mode == MODE_MARK || w2) ? (c.wf == 0 ? 8 * c.nw : 4)
                         : c.mode == MODE_MARKC ? 4 * c.nw
                         : c.mode == MODE_ADJ   ? 4
+                        : c.mode == MODE_ADJC  ? 4 * GBP_ADJ_CH  // the kernel's fixed stride
                         : c.mode == MODE_POBJ  ? 4   // the gather kernel's fixed stride
                         : (c.mode == MODE_JACK || c.mode == MODE_JACKXYZ) ? 4
                         : neigh                ? 4   // the j-slots' sorted indices
@@ -534,19 +538,21 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
                 h2d += (int64_t)(sizeof(long long) * (c.n1 + 1));
             }
         }
-        int occ = (adj || pobj) ? gbp_adjoint_occupancy(smem, pobj)
+        int occ = adjc            ? gbp_adjoint_ch_occupancy(smem)
+                  : (adj || pobj) ? gbp_adjoint_occupancy(smem, pobj)
                   : neigh       ? gbp_neigh_occupancy(smem)
                                 : gbp_count_occupancy(c.mode, c.wf, smem);
         if (occ <= 0) return fail(plan, GBP_ERR_INVALID, "count kernel does not fit (smem %zu B)", smem);
         int grid = plan->nsm * occ;
-        if (adj) CK(cudaMemsetAsync(a.grad, 0, sizeof(double) * (size_t)c.n1, st));
+        if (adj) CK(cudaMemsetAsync(a.grad, 0, sizeof(double) * ngrad, st));
         if (pobj || neigh) CK(cudaMemsetAsync(a.pobj, 0, sizeof(unsigned) * npobj, st));
-        if (adj || pobj) CK(gbp_launch_adjoint(a, grid, smem, st, pobj));
+        if (adjc) CK(gbp_launch_adjoint_ch(a, grid, smem, st));
+        else if (adj || pobj) CK(gbp_launch_adjoint(a, grid, smem, st, pobj));
         else if (neigh) CK(gbp_launch_neigh(a, (int)c.n1, c.nout, grid, smem, st));
         else CK(gbp_launch_count(c.mode, c.wf, a, grid, smem, st));
         if (adj && c.mem == GBP_MEM_HOST && c.n1 > 0) {
-            CK(cudaMemcpyAsync(c.grad_out, a.grad, sizeof(double) * c.n1, cudaMemcpyDeviceToHost, st));
-            d2h += (int64_t)(sizeof(double) * c.n1);
+            CK(cudaMemcpyAsync(c.grad_out, a.grad, sizeof(double) * ngrad, cudaMemcpyDeviceToHost, st));
+            d2h += (int64_t)(sizeof(double) * ngrad);
         }
         if (plist && c.npairs > 0) {
             CK(cudaMemcpyAsync(c.pairs_out, a.pairs, 2 * sizeof(unsigned) * (size_t)c.npairs,
@@ -1691,6 +1697,52 @@ int gbp_weighted_adjoint_3d(gbp_plan *plan, const double *xyz, int64_t n, const 
     return run_call(plan, c, h);
 }
 
+int gbp_weighted_adjoint_3d_channels(gbp_plan *plan, const double *xyz, int64_t n,
+                                     const double *w, int32_t nch, const double *rbins,
+                                     int32_t nb, const double *period3, int32_t pbc, int32_t mem,
+                                     const double *gbar, double *grad_w) {
+    int rc = check_common(plan, xyz, n, xyz, n, period3, pbc, mem);
+    if (rc) return rc;
+    if (nch < 1 || nch > GBP_ADJ_CH)
+        return fail(plan, GBP_ERR_INVALID, "nch must be 1..%d, got %d", GBP_ADJ_CH, nch);
+    if ((n > 0 && (!w || !grad_w)) || !gbar) return fail(plan, GBP_ERR_INVALID, "null weights or gradients");
+    if (!rbins || nb < 2 || nb > GBP_NB_MAX)
+        return fail(plan, GBP_ERR_INVALID, "rbins must have 2..%d entries", GBP_NB_MAX);
+    double rmax = max_nan(rbins, nb);
+    double search[3] = {rmax, rmax, rmax};
+    if ((rc = check_search(plan, search, period3))) return rc;
+    if (n == 0) return GBP_OK;
+    Call c;
+    c.mode = MODE_ADJC;
+    c.xyz1 = c.xyz2 = xyz;
+    c.n1 = c.n2 = n;
+    c.autocorr = true;  // one sorted copy; the walk is a gather
+    c.mem = mem;
+    c.w1 = c.w2 = w;
+    c.nw = nch;
+    c.wfunc = 1;
+    c.naxes = 1;
+    c.grad_out = grad_w;
+    choose_grid(c.g, period3, search, pbc, n, plan->reach, MAX_CELLS_PER_DIM, 0.0, plan->block);
+    build_stencil(c.g, search, 0, false);  // the full stencil: a gather, no scatter to j
+    ErrModel em = err_model(c.g);
+    std::vector<double> E(nb);
+    edges_top_walk(rbins, nb, E.data());
+    c.ax[0].set(E, &em, 3);
+    c.ax[0].make_lut(no_qband);
+    // per channel: G(bin b) = sum of the upstream gradient over cumulative bins >= b
+    c.gt.assign((size_t)nch * (nb + 1), 0.f);
+    for (int ch = 0; ch < nch; ch++) {
+        double run = 0.0;
+        for (int k = nb - 1; k >= 0; k--) {
+            run += gbar[(size_t)ch * nb + k];
+            c.gt[(size_t)ch * (nb + 1) + k] = (float)run;
+        }
+    }
+    std::vector<unsigned long long> h;
+    return run_call(plan, c, h);
+}
+
 static int zheng07_args(gbp_plan *plan, const double *theta, Zheng07 *th) {
     if (!theta) return fail(plan, GBP_ERR_INVALID, "null theta");
     th->logMmin = theta[0];
@@ -1703,6 +1755,87 @@ static int zheng07_args(gbp_plan *plan, const double *theta, Zheng07 *th) {
     th->M1 = std::pow(10.0, th->logM1);
     th->inv_sigma = 1.0 / th->sigma;
     th->inv_M1 = 1.0 / th->M1;
+    return GBP_OK;
+}
+
+// Zheng07 weights / VJP for nth parameter vectors at once: the derived constants
+// of every vector on the device, then one launch over (halo, vector)
+static int zheng07_batched_args(gbp_plan *plan, const double *thetas, int32_t nth,
+                                std::vector<Zheng07> &th) {
+    if (!thetas || nth < 1) return fail(plan, GBP_ERR_INVALID, "no parameter vector");
+    th.resize((size_t)nth);
+    for (int m = 0; m < nth; m++) {
+        int rc = zheng07_args(plan, thetas + 5 * (size_t)m, &th[(size_t)m]);
+        if (rc) return rc;
+    }
+    return GBP_OK;
+}
+
+int gbp_zheng07_weights_batched(gbp_plan *plan, const double *mass, int64_t n,
+                                const double *thetas, int32_t nth, int32_t mem, double *W) {
+    if (!plan) return GBP_ERR_INVALID;
+    std::vector<Zheng07> th;
+    int rc = zheng07_batched_args(plan, thetas, nth, th);
+    if (rc) return rc;
+    if (n < 0 || (n > 0 && (!mass || !W))) return fail(plan, GBP_ERR_INVALID, "null arrays");
+    if (n == 0) return GBP_OK;
+    CK(cudaSetDevice(plan->device));
+    cudaStream_t st = plan->stream;
+    Carve cv;
+    size_t o_th = cv.take<Zheng07>((size_t)nth);
+    size_t o_lm = cv.take<double>((size_t)n);
+    size_t o_m = mem == GBP_MEM_HOST ? cv.take<double>((size_t)n) : 0;
+    size_t o_w = mem == GBP_MEM_HOST ? cv.take<double>((size_t)n * nth) : 0;
+    if ((rc = ensure_work(plan, cv.take<char>(0) + 256))) return rc;
+    void *Wk = plan->work.p;
+    CK(cudaMemcpyAsync(at<char>(Wk, o_th), th.data(), sizeof(Zheng07) * nth, cudaMemcpyHostToDevice, st));
+    const double *dm = mass;
+    double *dw = W;
+    if (mem == GBP_MEM_HOST) {
+        dm = at<double>(Wk, o_m);
+        dw = at<double>(Wk, o_w);
+        CK(cudaMemcpyAsync((void *)dm, mass, n * sizeof(double), cudaMemcpyHostToDevice, st));
+    }
+    CK(gbp_launch_zheng07_wb(dm, at<double>(Wk, o_lm), n, at<Zheng07>(Wk, o_th), nth, dw, st));
+    if (mem == GBP_MEM_HOST)
+        CK(cudaMemcpyAsync(W, dw, (size_t)n * nth * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    return GBP_OK;
+}
+
+int gbp_zheng07_vjp_batched(gbp_plan *plan, const double *mass, int64_t n, const double *thetas,
+                            int32_t nth, const double *grad_W, int32_t mem, double *grad_theta) {
+    if (!plan) return GBP_ERR_INVALID;
+    std::vector<Zheng07> th;
+    int rc = zheng07_batched_args(plan, thetas, nth, th);
+    if (rc) return rc;
+    if (!grad_theta || n < 0 || (n > 0 && (!mass || !grad_W)))
+        return fail(plan, GBP_ERR_INVALID, "null arrays");
+    for (int k = 0; k < 5 * nth; k++) grad_theta[k] = 0.0;
+    if (n == 0) return GBP_OK;
+    CK(cudaSetDevice(plan->device));
+    cudaStream_t st = plan->stream;
+    Carve cv;
+    size_t o_th = cv.take<Zheng07>((size_t)nth);
+    size_t o_out = cv.take<double>(5 * (size_t)nth);
+    size_t o_lm = cv.take<double>((size_t)n);
+    size_t o_m = mem == GBP_MEM_HOST ? cv.take<double>((size_t)n) : 0;
+    size_t o_g = mem == GBP_MEM_HOST ? cv.take<double>((size_t)n * nth) : 0;
+    if ((rc = ensure_work(plan, cv.take<char>(0) + 256))) return rc;
+    void *Wk = plan->work.p;
+    CK(cudaMemcpyAsync(at<char>(Wk, o_th), th.data(), sizeof(Zheng07) * nth, cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(at<char>(Wk, o_out), 0, sizeof(double) * 5 * nth, st));
+    const double *dm = mass, *dg = grad_W;
+    if (mem == GBP_MEM_HOST) {
+        dm = at<double>(Wk, o_m);
+        dg = at<double>(Wk, o_g);
+        CK(cudaMemcpyAsync((void *)dm, mass, n * sizeof(double), cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync((void *)dg, grad_W, (size_t)n * nth * sizeof(double), cudaMemcpyHostToDevice, st));
+    }
+    CK(gbp_launch_zheng07_vjpb(dm, at<double>(Wk, o_lm), n, at<Zheng07>(Wk, o_th), nth, dg,
+                               at<double>(Wk, o_out), st));
+    CK(cudaMemcpyAsync(grad_theta, at<double>(Wk, o_out), sizeof(double) * 5 * nth, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
     return GBP_OK;
 }
 

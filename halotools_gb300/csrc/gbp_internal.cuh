@@ -33,7 +33,11 @@ enum { MODE_3D = 0, MODE_XYZ = 1, MODE_SMU = 2, MODE_MARK = 3, MODE_ADJ = 4, MOD
        MODE_JACKXYZ = 11,    // (rp, pi) counts plus a global (tag, bin) table of pair ends
        MODE_NEIGH = 12,      // per-object neighbours in per-point spheres / cylinders
        MODE_JACKW = 13,      // weighted jackknife, 3-D: w1 w2 sums plus an FP64 (tag, bin) table
-       MODE_JACKXYZW = 14 }; // weighted jackknife, (rp, pi)
+       MODE_JACKXYZW = 14,   // weighted jackknife, (rp, pi)
+       MODE_ADJC = 15 };     // adjoint over several weight channels (parameter draws)
+
+// channels of one batched adjoint launch
+#define GBP_ADJ_CH 8
 
 // Pair geometry of a count mode: (rp, pi) cylinders or (s, mu') cones; every
 // other mode measures 3-D separations
@@ -161,7 +165,8 @@ __host__ __device__ inline SmemLayout gbp_smem_layout(int mode, int T0, int T1, 
     int o = 0;
     // adjoint: float4 tables {b0, thr, lo, qband}; count kernels: u32 table
     // {b0 | threshold-pair index << 16} and the threshold pairs (hi, lo)
-    const bool adj = mode == MODE_ADJ || mode == MODE_POBJ || mode == MODE_NEIGH;  // gather kernels
+    const bool adj = mode == MODE_ADJ || mode == MODE_POBJ || mode == MODE_NEIGH ||
+                     mode == MODE_ADJC;  // gather kernels
     L.off_lut0 = o; o += adj ? T0 * 16 : gbp_align(T0 * 4, 16);
     L.off_lut1 = o; o += adj ? T1 * 16 : gbp_align(T1 * 4, 16);
     const bool smu = gbp_mode_smu(mode);
@@ -198,6 +203,8 @@ __host__ __device__ inline SmemLayout gbp_smem_layout(int mode, int T0, int T1, 
         hist_bytes = GBP_WARPS * (nb0 + 1) * 32 * 4 * 2;      // lane-private FP32 sum + compensation
     } else if (mode == MODE_ADJ) {
         hist_bytes = GBP_BLOCK * 8 + gbp_align((nb0 + 1) * 4, 16);  // partial sums + gt table
+    } else if (mode == MODE_ADJC) {
+        hist_bytes = gbp_align(GBP_ADJ_CH * (nb0 + 1) * 4, 16);     // gt table per channel
     } else if (mode == MODE_NEIGH) {
         hist_bytes = 0;                                       // counters live in registers
     } else if (mode == MODE_POBJ) {
@@ -298,6 +305,9 @@ cudaError_t gbp_count_set_smem(size_t smem);
 cudaError_t gbp_launch_adjoint(const CountArgs &a, int grid, size_t smem, cudaStream_t st,
                                bool per_object = false);
 int gbp_adjoint_occupancy(size_t smem, bool per_object = false);
+// batched adjoint: up to GBP_ADJ_CH weight channels (a.nw) per launch
+cudaError_t gbp_launch_adjoint_ch(const CountArgs &a, int grid, size_t smem, cudaStream_t st);
+int gbp_adjoint_ch_occupancy(size_t smem);
 // per-object neighbours: thresholds pre-pass then k_neigh<geometry, out>
 // (out 0 counts, 1 has-neighbour flags, 2 pair list)
 cudaError_t gbp_launch_neigh(const CountArgs &a, int n1, int out, int grid, size_t smem,
@@ -312,6 +322,12 @@ cudaError_t gbp_launch_zheng07_w(const double *mass, int64_t n, Zheng07 th, doub
                                  cudaStream_t st);
 cudaError_t gbp_launch_zheng07_vjp(const double *mass, int64_t n, Zheng07 th, const double *gw,
                                    double *out5, cudaStream_t st);
+// many parameter vectors (th: nth device structs): W (n, nth) and out (nth, 5)
+// (lm: n doubles of scratch for log10 M)
+cudaError_t gbp_launch_zheng07_wb(const double *mass, double *lm, int64_t n, const Zheng07 *th,
+                                  int nth, double *W, cudaStream_t st);
+cudaError_t gbp_launch_zheng07_vjpb(const double *mass, double *lm, int64_t n, const Zheng07 *th,
+                                    int nth, const double *gW, double *out, cudaStream_t st);
 // Zheng07 mocks on the GPU (gbp_hod.cu): thetas as (n, 5) rows converted by
 // gbp_hod_thetas into gbp_hod_theta_bytes() each
 cudaError_t gbp_hod_count(const double *mass, double *logm, int64_t nh, const void *thetas,

@@ -22,7 +22,8 @@ from . import _native
 from .pair_counters import _bins, _nonneg, _period, _search_check
 
 __all__ = ("WeightedPairCounts", "Zheng07Weights", "weighted_pair_counts", "zheng07_weights",
-           "hod_pair_counts")
+           "hod_pair_counts", "WeightedPairCountsBatched", "Zheng07WeightsBatched",
+           "weighted_pair_counts_batched", "zheng07_weights_batched", "hod_pair_counts_batched")
 
 
 def _plan():
@@ -126,3 +127,103 @@ def zheng07_weights(theta, mass):
 def hod_pair_counts(theta, halo_xyz, halo_mass, rbins, period):
     """Expected weighted pair counts of a Zheng07 HOD on a halo catalogue, C(theta)."""
     return weighted_pair_counts(zheng07_weights(theta, halo_mass), halo_xyz, rbins, period)
+
+
+# ---------------- many parameter draws at once ----------------
+_ADJ_CH = 8  # channels of one batched adjoint launch (gbp_weighted_adjoint_3d_channels)
+
+
+class WeightedPairCountsBatched(torch.autograd.Function):
+    """C[m] = sum_ij W_im W_jm [d_ij <= r_k] for the M columns of W (N, M), M <= 32:
+    one forward pass over all columns (gbp_marked_npairs_3d_channels) and one
+    adjoint pass per 8 columns (gbp_weighted_adjoint_3d_channels)."""
+
+    @staticmethod
+    def forward(ctx, W, xyz, rbins, box):
+        plan = _plan()
+        plan.set_stream(torch.cuda.current_stream(W.device).cuda_stream)
+        Wd, xd = _cuda_f64(W), _cuda_f64(xyz)
+        n, m = Wd.shape
+        out = np.zeros((m, len(rbins)), dtype=np.float64)
+        plan.check(plan.lib.gbp_marked_npairs_3d_channels(
+            plan.handle, _native.dptr_int(xd.data_ptr()), n, _native.dptr_int(xd.data_ptr()), n,
+            _native.dptr_int(Wd.data_ptr()), _native.dptr_int(Wd.data_ptr()), m,
+            _native.pd(rbins), len(rbins), _native.pd(box), 1, _native.GBP_MEM_DEVICE,
+            _native.pd(out)))
+        ctx.save_for_backward(Wd, xd)
+        ctx.rbins, ctx.box = rbins, box
+        return torch.from_numpy(out).to(W.device)
+
+    @staticmethod
+    def backward(ctx, gC):
+        Wd, xd = ctx.saved_tensors
+        plan = _plan()
+        plan.set_stream(torch.cuda.current_stream(Wd.device).cuda_stream)
+        g = gC.detach().to("cpu", torch.float64).numpy()
+        n, m = Wd.shape
+        grad = torch.empty_like(Wd)
+        for c0 in range(0, m, _ADJ_CH):
+            c1 = min(m, c0 + _ADJ_CH)
+            wg = Wd[:, c0:c1].contiguous()
+            gg = torch.empty_like(wg)
+            gb = np.ascontiguousarray(g[c0:c1])
+            plan.check(plan.lib.gbp_weighted_adjoint_3d_channels(
+                plan.handle, _native.dptr_int(xd.data_ptr()), n, _native.dptr_int(wg.data_ptr()),
+                c1 - c0, _native.pd(ctx.rbins), len(ctx.rbins), _native.pd(ctx.box), 1,
+                _native.GBP_MEM_DEVICE, _native.pd(gb), _native.dptr_int(gg.data_ptr())))
+            grad[:, c0:c1] = gg
+        return grad, None, None, None
+
+
+class Zheng07WeightsBatched(torch.autograd.Function):
+    """W[:, m] = <Ncen>(M_i; theta_m) + <Nsat>(M_i; theta_m) for thetas (M, 5): one
+    launch over (halo, draw) each way (occupations in FP32, the VJP summed in FP64)."""
+
+    @staticmethod
+    def forward(ctx, thetas, mass):
+        plan = _plan()
+        plan.set_stream(torch.cuda.current_stream(mass.device).cuda_stream)
+        md = _cuda_f64(mass)
+        th = np.ascontiguousarray(thetas.detach().to("cpu", torch.float64).numpy())
+        W = torch.empty((md.shape[0], len(th)), dtype=torch.float64, device=md.device)
+        plan.check(plan.lib.gbp_zheng07_weights_batched(
+            plan.handle, _native.dptr_int(md.data_ptr()), md.shape[0], _native.pd(th), len(th),
+            _native.GBP_MEM_DEVICE, _native.dptr_int(W.data_ptr())))
+        ctx.save_for_backward(md)
+        ctx.thetas = th
+        ctx.theta_dtype, ctx.theta_device = thetas.dtype, thetas.device
+        return W
+
+    @staticmethod
+    def backward(ctx, gW):
+        (md,) = ctx.saved_tensors
+        plan = _plan()
+        plan.set_stream(torch.cuda.current_stream(md.device).cuda_stream)
+        g = gW.detach().to(torch.float64).contiguous()
+        out = np.zeros(ctx.thetas.shape, dtype=np.float64)
+        plan.check(plan.lib.gbp_zheng07_vjp_batched(
+            plan.handle, _native.dptr_int(md.data_ptr()), md.shape[0], _native.pd(ctx.thetas),
+            len(ctx.thetas), _native.dptr_int(g.data_ptr()), _native.GBP_MEM_DEVICE,
+            _native.pd(out)))
+        return torch.from_numpy(out).to(ctx.theta_device, ctx.theta_dtype), None
+
+
+def weighted_pair_counts_batched(W, xyz, rbins, period):
+    """Differentiable C[m, k] = sum_ij W_im W_jm [d_ij <= rbins[k]] for each column m of
+    W (N, M), M <= 32: marked_npairs_3d(xyz, xyz, rbins, 1, period, W[:, m], W[:, m])."""
+    rbins, box = _geometry(rbins, period)
+    if W.dim() != 2 or W.shape[1] < 1 or W.shape[1] > 32:
+        raise ValueError("W must be (N, M) with 1 <= M <= 32 weight columns")
+    return WeightedPairCountsBatched.apply(W, xyz, rbins, box)
+
+
+def zheng07_weights_batched(thetas, mass):
+    """Per-halo Zheng07 mean occupations for each parameter vector: (N, M)."""
+    return Zheng07WeightsBatched.apply(thetas, mass)
+
+
+def hod_pair_counts_batched(thetas, halo_xyz, halo_mass, rbins, period):
+    """Expected weighted pair counts C(theta_m) of a Zheng07 HOD for M parameter
+    vectors at once (M <= 32): (M, nbins), differentiable in thetas (M, 5)."""
+    return weighted_pair_counts_batched(zheng07_weights_batched(thetas, halo_mass), halo_xyz,
+                                        rbins, period)

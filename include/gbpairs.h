@@ -135,6 +135,29 @@ int gbp_marked_npairs_3d(gbp_plan *plan, const double *xyz1, int64_t n1, const d
                          const double *period3, int32_t pbc, int32_t mem, double *out);
 
 /*
+ * gbp_weighted_adjoint_3d for nch <= 8 weight channels at once (parameter draws
+ * of an occupation model): w is (n, nch) row-major, gbar (nch, nbins), grad_w
+ * (n, nch) with grad_w[m][c] = dL/dw_m of channel c for the forward counts
+ * gbp_marked_npairs_3d_channels(x, x, w, w).  Each pair is binned once for all
+ * channels.
+ */
+int gbp_weighted_adjoint_3d_channels(gbp_plan *plan, const double *xyz, int64_t n,
+                                     const double *w, int32_t nch, const double *rbins,
+                                     int32_t nb, const double *period3, int32_t pbc, int32_t mem,
+                                     const double *gbar, double *grad_w);
+
+/*
+ * gbp_zheng07_weights and gbp_zheng07_vjp for nth parameter vectors at once
+ * (thetas (nth, 5)): W (n, nth) row-major, grad_W likewise, grad_theta (nth, 5)
+ * on the host.  The occupations are evaluated in FP32 (the counting kernels
+ * multiply weights in FP32), the VJP sums in FP64.
+ */
+int gbp_zheng07_weights_batched(gbp_plan *plan, const double *mass, int64_t n,
+                                const double *thetas, int32_t nth, int32_t mem, double *W);
+int gbp_zheng07_vjp_batched(gbp_plan *plan, const double *mass, int64_t n, const double *thetas,
+                            int32_t nth, const double *grad_W, int32_t mem, double *grad_theta);
+
+/*
  * Zheng07 HOD mocks on the GPU, one per parameter vector thetas[m] =
  * (logMmin, sigma_logM, logM0, logM1, alpha), (n_theta, 5) row-major: a
  * Bernoulli central with <Ncen> = (1 + erf((log10 M - logMmin) / sigma_logM)) / 2

@@ -102,3 +102,76 @@ def test_hod_gradient_matches_central_differences(gpu):
     h = 1e-4
     fd = np.array([(loss(THETA + h * e) - loss(THETA - h * e)) / (2 * h) for e in np.eye(5)])
     np.testing.assert_allclose(got, fd, rtol=2e-4, atol=1e-6 * np.abs(fd).max())
+
+
+# ---------------- many parameter draws in one forward and one adjoint pass ----------------
+def _thetas(m, seed):
+    rng = np.random.default_rng(seed)
+    lmin = rng.uniform(11.8, 12.4, m)
+    return np.stack([lmin, rng.uniform(0.2, 0.5, m), lmin, lmin + 1.3, rng.uniform(0.9, 1.1, m)],
+                    axis=1)
+
+
+def test_batched_forward_and_dw_match_fp64(gpu):
+    import torch
+    from halotools_gb300 import differentiable as D
+    L = 120.0
+    pos, mass, _ = halos(8000, L, 21)
+    th = _thetas(11, 22)  # 11 draws: adjoint groups of 8 and 3
+    W = np.stack([zheng07_np(t, mass) for t in th], axis=1)
+    rb = np.logspace(-1, np.log10(15), 10)
+    Wt = torch.from_numpy(W).cuda().requires_grad_(True)
+    C = D.weighted_pair_counts_batched(Wt, torch.from_numpy(pos).cuda(), rb, L)
+    assert C.shape == (11, len(rb))
+    gbar = np.random.default_rng(23).normal(size=(11, len(rb)))
+    (C * torch.from_numpy(gbar).cuda()).sum().backward()
+    got_w = Wt.grad.cpu().numpy()
+    for m in range(11):
+        want = oracle.marked_npairs_3d(pos, pos, rb, 1, period=L, weights1=W[:, m],
+                                       weights2=W[:, m], num_threads=8)
+        np.testing.assert_allclose(C[m].detach().cpu().numpy(), want, rtol=1e-6)
+        wg = oracle.weighted_adjoint_3d(pos, W[:, m], rb, L, gbar[m])
+        assert np.max(np.abs(got_w[:, m] - wg)) / np.abs(wg).max() < 2e-6, m
+
+
+def test_batched_theta_gradient_matches_single_draws(gpu):
+    import torch
+    from halotools_gb300 import differentiable as D
+    L = 150.0
+    pos, mass, _ = halos(20000, L, 24)
+    th = _thetas(5, 25)
+    rb = np.logspace(-1, np.log10(20), 12)
+    x, m = torch.from_numpy(pos).cuda(), torch.from_numpy(mass).cuda()
+    T = torch.tensor(th, dtype=torch.float64, device="cuda", requires_grad=True)
+    gbar = torch.from_numpy(np.random.default_rng(26).normal(size=(5, len(rb)))).cuda()
+    C = D.hod_pair_counts_batched(T, x, m, rb, L)
+    (C * gbar).sum().backward()
+    for k in range(5):
+        t1 = torch.tensor(th[k], dtype=torch.float64, device="cuda", requires_grad=True)
+        c1 = D.hod_pair_counts(t1, x, m, rb, L)
+        (c1 * gbar[k]).sum().backward()
+        np.testing.assert_allclose(C[k].detach().cpu().numpy(), c1.detach().cpu().numpy(),
+                                   rtol=1e-6)
+        g1 = t1.grad.cpu().numpy()
+        np.testing.assert_allclose(T.grad[k].cpu().numpy(), g1, rtol=1e-5,
+                                   atol=1e-6 * np.abs(g1).max())
+
+
+def test_batched_zheng07_weights_and_vjp(gpu):
+    import torch
+    from halotools_gb300 import differentiable as D
+    pos, mass, _ = halos(50000, 200.0, 27)
+    th = _thetas(6, 28)
+    T = torch.tensor(th, dtype=torch.float64, device="cuda", requires_grad=True)
+    W = D.zheng07_weights_batched(T, torch.from_numpy(mass).cuda())
+    want = np.stack([zheng07_np(t, mass) for t in th], axis=1)
+    # FP32 occupations from an FP64 log10 M: 1e-6 relative (absolute near 0)
+    np.testing.assert_allclose(W.detach().cpu().numpy(), want, rtol=1e-6, atol=1e-7)
+    g = torch.from_numpy(np.random.default_rng(29).normal(size=W.shape)).cuda()
+    (W * g).sum().backward()
+    for k in range(6):
+        t1 = torch.tensor(th[k], dtype=torch.float64, device="cuda", requires_grad=True)
+        (D.zheng07_weights(t1, torch.from_numpy(mass).cuda()) * g[:, k]).sum().backward()
+        g1 = t1.grad.cpu().numpy()
+        np.testing.assert_allclose(T.grad[k].cpu().numpy(), g1, rtol=1e-5,
+                                   atol=1e-6 * np.abs(g1).max())
