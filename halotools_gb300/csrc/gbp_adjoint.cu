@@ -254,7 +254,9 @@ __device__ __noinline__ int2 slow_adj_bins(float v, int b0, int is, int js, cons
 // k_gather_ch: the adjoint gather over up to NCH weight channels at once (one
 // parameter draw per channel): each in-range pair is binned once, then channel c
 // adds w_j^c G^c(bin) to the i-point's compensated sum in registers, so the
-// distance work is shared by all channels.
+// distance work is shared by all channels.  The G table is bin-major and the
+// channels go in packed f32x2 pairs: a pair costs 16-byte loads of G and w_j and
+// one packed compensated add per two channels, into registers.
 template <int NCH>
 __global__ void __launch_bounds__(GBP_BLOCK, 2) k_gather_ch(const CountArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -274,14 +276,17 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_gather_ch(const CountArgs a) {
     float *s_lo0 = (float *)(smem + L.off_lo0);
     int *s_off = (int *)(smem + L.off_off);
     const int nbc = nb0 + 1;
-    float *s_gt = (float *)(smem + L.off_hist);  // [channel][bin]
+    float *s_gt = (float *)(smem + L.off_hist);  // [bin][channel]
     for (int i = tid; i < T0; i += GBP_BLOCK) s_lut0[i] = a.ax[0].lut[i];
     for (int i = tid; i < nb0; i += GBP_BLOCK) {
         s_E0[i] = a.ax[0].E[i];
         s_hi0[i] = a.ax[0].hi[i];
         s_lo0[i] = a.ax[0].lo[i];
     }
-    for (int i = tid; i < NCH * nbc; i += GBP_BLOCK) s_gt[i] = i < nch * nbc ? a.gt[i] : 0.f;
+    for (int i = tid; i < NCH * nbc; i += GBP_BLOCK) {
+        const int k = i / NCH, c = i - k * NCH;
+        s_gt[i] = c < nch ? a.gt[c * nbc + k] : 0.f;
+    }
     for (int i = tid; i < a.nsten; i += GBP_BLOCK) {
         s_off[i] = a.sten[i];
         s_D[i] = a.stenD[i];
@@ -308,9 +313,55 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_gather_ch(const CountArgs a) {
         if (lane < icnt) u0 = a.pos1[ifirst + lane];
         if (lane + 32 < icnt) u1 = a.pos1[ifirst + 32 + lane];
         const unsigned long long UX = pk2(u0.x, u1.x), UY = pk2(u0.y, u1.y), UZ = pk2(u0.z, u1.z);
-        float acc0[NCH], cmp0[NCH], acc1[NCH], cmp1[NCH];  // Kahan: sum ~ acc - cmp
+        // packed channel pairs (2q, 2q + 1) of the two points: sum ~ acc + ncm
+        constexpr int NH = NCH / 2;
+        unsigned long long acc0[NH], ncm0[NH], acc1[NH], ncm1[NH];
 #pragma unroll
-        for (int c = 0; c < NCH; c++) acc0[c] = cmp0[c] = acc1[c] = cmp1[c] = 0.f;
+        for (int q = 0; q < NH; q++) acc0[q] = ncm0[q] = acc1[q] = ncm1[q] = 0ull;
+        // the in-range pairs of one point in m, highest slot first
+        auto gather = [&](unsigned m, const float4 &u, unsigned long long *acc,
+                          unsigned long long *ncm) {
+            while (m) {
+                const int jj = 31 - __clz(m);
+                m ^= 1u << jj;
+                const float4 t = jb[jj];
+                const float dx = u.x - t.x, dy = u.y - t.y, dz = u.z - t.z;
+                const float v = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+                const float4 e = lut_entry(v, A0);
+                int2 kk;
+                if ((v > e.z) & !(v > e.y)) {
+                    kk = slow_adj_bins(v, __float_as_int(e.x), __float_as_int(u.w),
+                                       __float_as_int(t.w), A0, a);
+                } else {
+                    const int b = __float_as_int(e.x) + (v > e.y ? 1 : 0);
+                    kk = make_int2(b, b);
+                }
+                const ulonglong2 *wr = (const ulonglong2 *)(jw + jj * NCH);
+                const ulonglong2 *gr = (const ulonglong2 *)(s_gt + kk.x * NCH);
+                unsigned long long g[NH], w[NH];
+#pragma unroll
+                for (int q = 0; q < NH / 2; q++) {
+                    const ulonglong2 gq = gr[q], wq = wr[q];
+                    g[2 * q] = gq.x;
+                    g[2 * q + 1] = gq.y;
+                    w[2 * q] = wq.x;
+                    w[2 * q + 1] = wq.y;
+                }
+                if (kk.x != kk.y) {
+                    // the mean over the two orders: 0.5 (G[k1] + G[k2])
+                    const ulonglong2 *hr = (const ulonglong2 *)(s_gt + kk.y * NCH);
+                    const unsigned long long half = pk2(0.5f, 0.5f);
+#pragma unroll
+                    for (int q = 0; q < NH / 2; q++) {
+                        const ulonglong2 hq = hr[q];
+                        g[2 * q] = f2_mul(half, f2_add(g[2 * q], hq.x));
+                        g[2 * q + 1] = f2_mul(half, f2_add(g[2 * q + 1], hq.y));
+                    }
+                }
+#pragma unroll
+                for (int q = 0; q < NH; q++) kahan_f2(acc[q], ncm[q], w[q], g[q]);
+            }
+        };
         for (int sb = s0; sb < s1; sb += 32) {
             const int s = sb + lane;
             int st = 0, cn = 0;
@@ -344,16 +395,31 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_gather_ch(const CountArgs a) {
                 const int exk = __shfl_sync(FULL, incl - cn, k);
                 const float Dx = __shfl_sync(FULL, D.x, k), Dy = __shfl_sync(FULL, D.y, k),
                             Dz = __shfl_sync(FULL, D.z, k);
+                int jg = -1;  // the slot's sorted j index (-1: padding)
                 if (f < T) {
                     const int j = stk + (f - exk);
+                    jg = j;
                     const float4 p = a.pos2[j];
                     const float tx = p.x + Dx, ty = p.y + Dy, tz = p.z + Dz;
                     jb[lane] = make_float4(tx, ty, tz, p.w);
                     jxy[lane] = make_ulonglong2(pk2(tx, tx), pk2(ty, ty));
                     jzz[lane] = pk2(tz, tz);
+                }
+                {
+                    // the slots' weight rows: lanes over (slot, channel), coalesced
+                    // read-only loads all issued before the contiguous stores
 #pragma unroll
-                    for (int c = 0; c < NCH; c++)
-                        jw[lane * NCH + c] = c < nch ? a.w2[(int64_t)j * nch + c] : 0.f;
+                    for (int u0 = 0; u0 < NCH; u0 += 4) {
+                        float v[4];
+#pragma unroll
+                        for (int u = 0; u < 4; u++) {
+                            const int t = 32 * (u0 + u) + lane, c = t % NCH;
+                            const int js = __shfl_sync(FULL, jg, t / NCH);
+                            v[u] = (js >= 0 && c < nch) ? __ldg(&a.w2[(int64_t)js * nch + c]) : 0.f;
+                        }
+#pragma unroll
+                        for (int u = 0; u < 4; u++) jw[32 * (u0 + u) + lane] = v[u];
+                    }
                 }
                 __syncwarp();
                 const int nj = min(32, T - f0);
@@ -369,56 +435,27 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_gather_ch(const CountArgs a) {
                     o1 = __funnelshift_l((unsigned)(d >> 32), o1, 1);
                 }
                 const unsigned valid = nj >= 32 ? 0xffffffffu : ((1u << nj) - 1u);
-                unsigned m0 = __brev(~o0) & valid, m1 = __brev(~o1) & valid;
-                while (m0 | m1) {
-                    const bool first = m0 != 0u;
-                    const int jj = 31 - __clz(first ? m0 : m1);
-                    if (first) m0 ^= 1u << jj;
-                    else m1 ^= 1u << jj;
-                    const float4 u = first ? u0 : u1;
-                    const float4 t = jb[jj];
-                    const float dx = u.x - t.x, dy = u.y - t.y, dz = u.z - t.z;
-                    const float v = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-                    const float4 e = lut_entry(v, A0);
-                    int2 kk;
-                    if ((v > e.z) & !(v > e.y)) {
-                        kk = slow_adj_bins(v, __float_as_int(e.x), __float_as_int(u.w),
-                                           __float_as_int(t.w), A0, a);
-                    } else {
-                        const int b = __float_as_int(e.x) + (v > e.y ? 1 : 0);
-                        kk = make_int2(b, b);
-                    }
-                    const float *wj = jw + jj * NCH;
-                    if (first) {
-#pragma unroll
-                        for (int c = 0; c < NCH; c++) {
-                            const float g = 0.5f * (s_gt[c * nbc + kk.x] + s_gt[c * nbc + kk.y]);
-                            const float y = fmaf(wj[c], g, -cmp0[c]), s2 = acc0[c] + y;
-                            cmp0[c] = (s2 - acc0[c]) - y;
-                            acc0[c] = s2;
-                        }
-                    } else {
-#pragma unroll
-                        for (int c = 0; c < NCH; c++) {
-                            const float g = 0.5f * (s_gt[c * nbc + kk.x] + s_gt[c * nbc + kk.y]);
-                            const float y = fmaf(wj[c], g, -cmp1[c]), s2 = acc1[c] + y;
-                            cmp1[c] = (s2 - acc1[c]) - y;
-                            acc1[c] = s2;
-                        }
-                    }
-                }
+                gather(__brev(~o0) & valid, u0, acc0, ncm0);
+                gather(__brev(~o1) & valid, u1, acc1, ncm1);
                 __syncwarp();
             }
         }
         // this item's sums of the lane's two points: dL/dw rows (caller's order)
+        auto lo = [](unsigned long long v) { return (double)__uint_as_float((unsigned)v); };
+        auto hi = [](unsigned long long v) { return (double)__uint_as_float((unsigned)(v >> 32)); };
 #pragma unroll
-        for (int c = 0; c < NCH; c++) {
-            if (c < nch && lane < icnt)
-                atomicAdd(&a.grad[(int64_t)a.orig[ifirst + lane] * nch + c],
-                          2.0 * ((double)acc0[c] - (double)cmp0[c]));
-            if (c < nch && lane + 32 < icnt)
-                atomicAdd(&a.grad[(int64_t)a.orig[ifirst + 32 + lane] * nch + c],
-                          2.0 * ((double)acc1[c] - (double)cmp1[c]));
+        for (int q = 0; q < NH; q++) {
+            const int c = 2 * q;
+            if (lane < icnt) {
+                double *row = a.grad + (int64_t)a.orig[ifirst + lane] * nch;
+                if (c < nch) atomicAdd(&row[c], 2.0 * (lo(acc0[q]) + lo(ncm0[q])));
+                if (c + 1 < nch) atomicAdd(&row[c + 1], 2.0 * (hi(acc0[q]) + hi(ncm0[q])));
+            }
+            if (lane + 32 < icnt) {
+                double *row = a.grad + (int64_t)a.orig[ifirst + 32 + lane] * nch;
+                if (c < nch) atomicAdd(&row[c], 2.0 * (lo(acc1[q]) + lo(ncm1[q])));
+                if (c + 1 < nch) atomicAdd(&row[c + 1], 2.0 * (hi(acc1[q]) + hi(ncm1[q])));
+            }
         }
     }
     if (lane == 0 && cand) atomicAdd(a.nrecheck + 1, cand);

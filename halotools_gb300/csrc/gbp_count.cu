@@ -483,7 +483,12 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
     const int copies = a.hist_copies;  // 2-D / wide: GBP_WARPS (one per warp) or 0 (global)
     constexpr bool JACK = (MODE == MODE_JACK);    // w1 / w2 hold the subsample tags
     const int nw = (MW || COLS || JACK || JACK2) ? a.nw : 0;
-    const int jwb = MW ? (WF == 0 ? 8 * nw : 4) : COLS ? 4 * nw : (JACK || JACK2) ? 4 : 0;
+    // MARKC: channel pairs and the staged column count (zero columns pad to 2 mP)
+    const int mP = MARKC ? gbp_markc_pairs(nw) : 1;
+    const int ncol = MARKC ? 2 * mP : nw;
+    const int lcol = 31 - __clz(ncol > 0 ? ncol : 1);  // ncol is a power of two when COLS
+    const bool msort = MARKC && mP >= GBP_MARKC_SORTED;
+    const int jwb = MW ? (WF == 0 ? 8 * nw : 4) : COLS ? 4 * ncol : (JACK || JACK2) ? 4 : 0;
     const SmemLayout L = gbp_smem_layout(MODE, T0, T1, nb0, nb1, a.nsten, copies, jwb, a.ntag);
     if (gbp_smem_too_small(L.total, a.err)) return;
     unsigned *s_l0 = (unsigned *)(smem + L.off_lut0);
@@ -498,7 +503,7 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
     // the same j-points with each coordinate twice, for the packed stage 1
     ulonglong2 *jxy = (ulonglong2 *)(smem + L.off_j2) + warp * 32;
     unsigned long long *jzz = (unsigned long long *)(smem + L.off_j2 + GBP_JCAP * 16) + warp * 32;
-    float *jw = (float *)(smem + L.off_jw) + warp * 32 * (COLS ? nw : 1);
+    float *jw = (float *)(smem + L.off_jw) + warp * 32 * (COLS ? ncol : 1);
     double *jw64 = (double *)(smem + L.off_jw) + warp * 32 * (nw > 0 ? nw : 1);
     float4 *s_D = (float4 *)(smem + L.off_D);
     double *s_E0 = (double *)(smem + L.off_E0);
@@ -514,9 +519,15 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
     float *uy = ux + GBP_USLOTS, *uz = ux + 2 * GBP_USLOTS;
     int *uix = (int *)(ux + 3 * GBP_USLOTS);
     float *s_uw = (float *)(smem + L.off_q + GBP_WARPS * GBP_USLOTS * 16) +
-                  warp * GBP_USLOTS * (COLS ? nw : 1);
-    // MARKC: this warp's binned pairs of one round {bin | multiplicity << 16, second bin, i, j}
+                  warp * GBP_USLOTS * (COLS ? ncol : 1);
+    // MARKC, few channels: this warp's binned pairs of one round {bin | multiplicity
+    // << 16, second bin, i, j}
     int4 *s_rec = (int4 *)(smem + L.off_rec) + warp * 32;
+    // MARKC sorted, per warp and code batch: each code's bin, the codes sorted by
+    // bin, and per bin its count and (after the scatter) its end
+    unsigned char *s_bin = (unsigned char *)(smem + L.off_rec) + warp * gbp_markc_sort_bytes(nb0);
+    unsigned short *s_rec2 = (unsigned short *)(s_bin + 1024);
+    int *s_cnt = (int *)(s_bin + 3072), *s_cur = s_cnt + (nb0 + 1);
     // (s, mu'): this warp's ring of deferred FP64 rechecks and its tail
     constexpr bool RQM = SMUF;
     RQ rq{(int4 *)(smem + L.off_rq) + warp * GBP_RQCAP,
@@ -549,9 +560,13 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
     const int nbin = (nb0 + 1) * (TWO ? nb1 + 1 : 1);
     // this warp's histogram words: lane-private (3-D, marked) or its own copy
     const int warp_words = (MODE == MODE_3D || JACK) ? (nb0 + 1) * 32
-                           : (MARK || MARKC) ? (nb0 + 1) * 32 * 2 : (copies ? nbin : 0);
+                           : (MARK || (MARKC && !msort)) ? (nb0 + 1) * 32 * 2
+                           : MARKC ? (nb0 + 1) * mP * 4
+                           : (copies ? nbin : 0);
     unsigned *wh = s_hist + warp * warp_words;
     for (int i = lane; i < warp_words; i += 32) wh[i] = 0u;
+    if (msort)
+        for (int i = lane; i <= nb0; i += 32) s_cnt[i] = 0;
     if (RQM && lane == 0) *rq.tail = 0u;
     // jackknife: the CTA's (tag, bin) table of pair ends, after the warps' counts
     unsigned long long *s_tab =
@@ -578,6 +593,8 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
     unsigned *hl = wh + lane;                       // 1-D: lane-private column
     float *hs = (float *)wh + lane;                 // marked: sums
     float *hc = hs + (nb0 + 1) * 32;                // marked: compensations
+    // MARKC: (bin, channel pair) packed sums and negated compensations
+    unsigned long long *hs2 = (unsigned long long *)wh, *hc2 = hs2 + (nb0 + 1) * mP;
     const int nitems = *a.nitems;
     const int n0 = a.n[0], n1 = a.n[1], n2 = a.n[2];
     // stage-1 thresholds: top * (1 + 2^-18) + 1e-30 covers the rounding of the
@@ -657,7 +674,7 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                 for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(FULL, v, o);
                 if (lane == 0 && v) atomicAdd(&gh[b], v);
             }
-        } else if (MARKC) {
+        } else if (MARKC && !msort) {
             // lane = (pair group g, channel c): channel c sums lanes c, c + nw, ...
             double *gd = a.histd + (size_t)mk * a.hist_stride;
             const int G = 32 / nw, c = lane % nw;
@@ -668,6 +685,21 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                 double tot = 0.0;
                 for (int g = 0; g < G; g++) tot += __shfl_sync(FULL, v, g * nw + c);
                 if (lane < nw && tot != 0.0) atomicAdd(&gd[lane * (nb0 + 1) + b], tot);
+            }
+        } else if (MARKC) {
+            // one (bin, channel pair) per lane: its two channels' sums in FP64
+            double *gd = a.histd + (size_t)mk * a.hist_stride;
+            for (int i = lane; i < nb0 * mP; i += 32) {
+                const int b = i / mP, c = 2 * (i - b * mP);
+                const unsigned long long sv = hs2[i], cv = hc2[i];
+                hs2[i] = 0ull;
+                hc2[i] = 0ull;
+                const double v0 = (double)__uint_as_float((unsigned)sv) +
+                                  (double)__uint_as_float((unsigned)cv);
+                const double v1 = (double)__uint_as_float((unsigned)(sv >> 32)) +
+                                  (double)__uint_as_float((unsigned)(cv >> 32));
+                if (c < nw && v0 != 0.0) atomicAdd(&gd[c * (nb0 + 1) + b], v0);
+                if (c + 1 < nw && v1 != 0.0) atomicAdd(&gd[(c + 1) * (nb0 + 1) + b], v1);
             }
         } else if (MARK) {
             double *gd = a.histd + (size_t)mk * a.hist_stride;
@@ -742,10 +774,21 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
             }
         }
         if (COLS) {
-            for (int k = 0; k < nw; k++) {
-                s_uw[lane * nw + k] = lane < icnt ? a.w1[(int64_t)(ifirst + lane) * nw + k] : 0.f;
-                s_uw[(lane + 48) * nw + k] =
-                    lane + 32 < icnt ? a.w1[(int64_t)(ifirst + 32 + lane) * nw + k] : 0.f;
+            // lanes over (point, column): whole rows read, contiguous stores; the
+            // read-only loads of a batch are all issued before its stores
+            for (int t0 = 0; t0 < 64 * ncol; t0 += 256) {
+                float v[8];
+#pragma unroll
+                for (int u = 0; u < 8; u++) {
+                    const int t = t0 + 32 * u + lane, sp = t >> lcol, q = t & (ncol - 1);
+                    v[u] = (t < 64 * ncol && sp < icnt && q < nw)
+                               ? __ldg(&a.w1[(int64_t)(ifirst + sp) * nw + q]) : 0.f;
+                }
+#pragma unroll
+                for (int u = 0; u < 8; u++) {
+                    const int t = t0 + 32 * u + lane, sp = t >> lcol, q = t & (ncol - 1);
+                    if (t < 64 * ncol) s_uw[gbp_uslot(sp) * ncol + q] = v[u];
+                }
             }
         }
         __syncwarp();
@@ -789,8 +832,10 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                             Dz = __shfl_sync(FULL, D.z, k);
                 // this lane's j-slot in registers too (the transposed stage 1)
                 float jtx = -GBP_FAR, jty = -GBP_FAR, jtz = -GBP_FAR;
+                int jg = -1;  // the slot's sorted j index (-1: padding)
                 if (f < T) {
                     const int j = stk + (f - exk);
+                    jg = j;
                     const float4 p = a.pos2[j];
                     const float tx = p.x + Dx, ty = p.y + Dy, tz = p.z + Dz;
                     jtx = tx; jty = ty; jtz = tz;
@@ -804,8 +849,6 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                             jw[lane] = a.w2[j];
                         }
                     }
-                    if (COLS)
-                        for (int q = 0; q < nw; q++) jw[lane * nw + q] = a.w2[(int64_t)j * nw + q];
                     if (JACK || JACK2) jw[lane] = a.w2[j];
                 } else {
                     // padding slot: at -FAR, so it is 2*FAR from an idle i-lane (+FAR)
@@ -813,6 +856,23 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                     jx[lane] = -GBP_FAR; jy[lane] = -GBP_FAR; jz[lane] = -GBP_FAR; jix[lane] = -2;
                     jxy[lane] = make_ulonglong2(pk2(-GBP_FAR, -GBP_FAR), pk2(-GBP_FAR, -GBP_FAR));
                     jzz[lane] = pk2(-GBP_FAR, -GBP_FAR);
+                }
+                if (COLS) {
+                    // lanes over (slot, column): whole rows read, contiguous stores;
+                    // a batch's read-only loads are all issued before its stores
+                    for (int t0 = 0; t0 < 32 * ncol; t0 += 256) {
+                        float v[8];
+#pragma unroll
+                        for (int u = 0; u < 8; u++) {
+                            const int t = t0 + 32 * u + lane, q = t & (ncol - 1);
+                            const int js = __shfl_sync(FULL, jg, (t >> lcol) & 31);
+                            v[u] = (t < 32 * ncol && js >= 0 && q < nw)
+                                       ? __ldg(&a.w2[(int64_t)js * nw + q]) : 0.f;
+                        }
+#pragma unroll
+                        for (int u = 0; u < 8; u++)
+                            if (t0 + 32 * u < 32 * ncol) jw[t0 + 32 * u + lane] = v[u];
+                    }
                 }
                 __syncwarp();
                 const int nj = min(32, T - f0);
@@ -978,7 +1038,7 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                         }
                         return PairV{v0, v1, iu, jj, ((sym_bits >> jj) & 1u) != 0u, wt, tg};
                     };
-                    if (MARKC) {
+                    if (MARKC && !msort) {
                         // each lane bins one pair per round; then lane (g, c) adds channel
                         // c's product for pairs g, g + G, ... of the round to its own
                         // Kahan column, so no two lanes touch one column
@@ -995,8 +1055,8 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                                 b0 = __float_as_int(t.x) + (e.v0 > t.y ? 1 : 0);
                                 if ((e.v0 > t.z) & !(e.v0 > t.y)) {
                                     int k[2];
-                                    const int n = slow_3d(e.v0, __float_as_int(t.x), ix.ui[iu], ix.jw[jj],
-                                                          e.sym, k, A0, a);
+                                    const int n = slow_3d(e.v0, __float_as_int(t.x), ix.ui[iu],
+                                                          ix.jw[jj], e.sym, k, A0, a);
                                     b0 = k[0];
                                     if (n == 2) {
                                         b1 = k[1];
@@ -1010,13 +1070,133 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                             for (int p = g; p < np; p += G) {
                                 if (g >= G) break;
                                 const int4 r = s_rec[p];
-                                const float val = s_uw[r.z * nw + ch] * jw[r.w * nw + ch];
+                                const float val = s_uw[r.z * ncol + ch] * jw[r.w * ncol + ch];
                                 const int rb0 = r.x & 0xffff;
                                 if (rb0 < nb0) kahan_add(hs, hc, rb0, (r.x >> 16) == 2 ? 2.0f * val : val);
                                 if (r.y < nb0) kahan_add(hs, hc, r.y, val);
                             }
                             __syncwarp();
                         }
+                    } else if (MARKC) {
+                        // (1) each lane bins one code per round: its bin (nb0: none) to
+                        // s_bin, the symmetric multiplicity into the code's bit 12, the
+                        // bin's count up by the lanes that share it
+                        const unsigned long long *W1 = (const unsigned long long *)s_uw;
+                        const unsigned long long *W2 = (const unsigned long long *)jw;
+                        for (int r0 = 0; r0 < C; r0 += 32) {
+                            const int sa = r0 + lane;
+                            int b0 = nb0, b1 = nb0;
+                            unsigned code = 0u;
+                            if (sa < C) {
+                                code = s_code[sa];
+                                const PairV e = entry((int)code);
+                                bool two = e.sym;
+                                const float4 t = lut_entry_c<false>(e.v0, A0);
+                                b0 = __float_as_int(t.x) + (e.v0 > t.y ? 1 : 0);
+                                if ((e.v0 > t.z) & !(e.v0 > t.y)) {
+                                    int k[2];
+                                    const int n = slow_3d(e.v0, __float_as_int(t.x), ix.ui[e.iu],
+                                                          ix.jw[e.jj], e.sym, k, A0, a);
+                                    b0 = k[0];
+                                    if (n == 2) {
+                                        b1 = min(k[1], nb0);
+                                        two = false;
+                                    }
+                                }
+                                b0 = min(b0, nb0);
+                                s_bin[sa] = (unsigned char)b0;
+                                s_code[sa] = (unsigned short)(code | (two ? 0x1000u : 0u));
+                            }
+                            // a pair whose two orders fall in different bins: its second
+                            // bin right away, one channel pair per lane (rare)
+                            unsigned split = __ballot_sync(FULL, b1 < nb0);
+                            while (split) {
+                                const int l = __ffs(split) - 1;
+                                split &= split - 1u;
+                                const int bl = __shfl_sync(FULL, b1, l);
+                                const unsigned cl = __shfl_sync(FULL, code, l);
+                                if (lane < mP) {
+                                    const unsigned long long v = f2_mul(W1[(cl & 127u) * mP + lane],
+                                                                        W2[((cl >> 7) & 31u) * mP + lane]);
+                                    kahan_f2(hs2[bl * mP + lane], hc2[bl * mP + lane],
+                                             pk2(1.f, 1.f), v);
+                                }
+                            }
+                            const unsigned peers = __match_any_sync(FULL, b0);
+                            if (b0 < nb0 && lane == __ffs(peers) - 1) s_cnt[b0] += __popc(peers);
+                            __syncwarp();
+                        }
+                        // (2) each bin's first record (exclusive scan of the counts)
+                        unsigned nz[2] = {0u, 0u};  // bins holding records, 32 per word
+                        {
+                            int run = 0;
+                            for (int bs = 0; bs < nb0; bs += 32) {
+                                const int b = bs + lane;
+                                const int c = b < nb0 ? s_cnt[b] : 0;
+                                int incl = c;
+#pragma unroll
+                                for (int o = 1; o < 32; o <<= 1) {
+                                    const int t = __shfl_up_sync(FULL, incl, o);
+                                    if (lane >= o) incl += t;
+                                }
+                                if (b < nb0) s_cur[b] = run + incl - c;
+                                run += __shfl_sync(FULL, incl, 31);
+                                nz[bs >> 5] = __ballot_sync(FULL, c > 0);
+                            }
+                        }
+                        __syncwarp();
+                        // (3) the codes scattered by bin, in code order within a bin;
+                        // s_cur[b] ends at the bin's end
+                        for (int r0 = 0; r0 < C; r0 += 32) {
+                            const int sa = r0 + lane;
+                            const int b = sa < C ? (int)s_bin[sa] : nb0;
+                            const unsigned peers = __match_any_sync(FULL, b);
+                            const int rank = __popc(peers & ((1u << lane) - 1u));
+                            const int base = b < nb0 ? s_cur[b] : 0;
+                            __syncwarp();
+                            if (b < nb0) {
+                                s_rec2[base + rank] = s_code[sa];
+                                if (rank == 0) s_cur[b] = base + __popc(peers);
+                            }
+                            __syncwarp();
+                        }
+                        // (4) per bin, lane (g, cp) sums the products of channel pair cp
+                        // over records g, g + G, ...: runs of 8 in packed FP32, the runs
+                        // compensated in registers, the G groups' totals by a shuffle
+                        // tree, then one compensated add to the warp's (bin, pair) sums
+                        const int G = 32 / mP, g = lane / mP, cp = lane - g * mP;
+                        const unsigned long long ONE2 = pk2(1.f, 1.f);
+                        for (int w = 0; w < 2; w++) {
+                            unsigned bits = nz[w];
+                            while (bits) {
+                                const int b = 32 * w + __ffs(bits) - 1;
+                                bits &= bits - 1u;
+                                const int end = s_cur[b], st = end - s_cnt[b];
+                                unsigned long long S = 0ull, NC = 0ull;
+                                for (int p = st + g; p < end; p += 8 * G) {
+                                    unsigned long long r = 0ull;
+#pragma unroll
+                                    for (int k = 0; k < 8; k++) {
+                                        const int q = p + k * G;
+                                        if (q < end) {
+                                            const unsigned rec = s_rec2[q];
+                                            unsigned long long v = f2_mul(W1[(rec & 127u) * mP + cp],
+                                                                          W2[((rec >> 7) & 31u) * mP + cp]);
+                                            if (rec & 0x1000u) v = f2_add(v, v);
+                                            r = f2_add(r, v);
+                                        }
+                                    }
+                                    kahan_f2(S, NC, ONE2, r);
+                                }
+                                unsigned long long v = f2_add(S, NC);
+                                for (int o = 16; o >= mP; o >>= 1)
+                                    v = f2_add(v, __shfl_xor_sync(FULL, v, o));
+                                if (g == 0) kahan_f2(hs2[b * mP + cp], hc2[b * mP + cp], ONE2, v);
+                            }
+                        }
+                        __syncwarp();
+                        for (int b = lane; b < nb0; b += 32) s_cnt[b] = 0;
+                        __syncwarp();
                     } else {
                         for (int r0 = 0; r0 < C; r0 += 64) {
                             const int sa = r0 + lane, sb = sa + 32;

@@ -126,6 +126,11 @@ __device__ __forceinline__ unsigned long long f2_sub(unsigned long long a, unsig
     asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
     return d;
 }
+__device__ __forceinline__ unsigned long long f2_add(unsigned long long a, unsigned long long b) {
+    unsigned long long d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
 __device__ __forceinline__ unsigned long long f2_mul(unsigned long long a, unsigned long long b) {
     unsigned long long d;
     asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
@@ -137,3 +142,13 @@ __device__ __forceinline__ unsigned long long f2_fma(unsigned long long a, unsig
     asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
     return d;
 }
+// Compensated (Kahan) add of the packed pair w * g to the packed sums s, with the
+// compensation kept negated (nc = -c): y = w g - c, t = s + y, c = (t - s) - y,
+// each element rounded as the scalar sum would be.
+__device__ __forceinline__ void kahan_f2(unsigned long long &s, unsigned long long &nc,
+                                         unsigned long long w, unsigned long long g) {
+    const unsigned long long y = f2_fma(w, g, nc), t = f2_add(s, y);
+    nc = f2_sub(y, f2_sub(t, s));
+    s = t;
+}
+

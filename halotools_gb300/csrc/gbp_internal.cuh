@@ -158,6 +158,24 @@ __host__ __device__ inline int gbp_uslot(int iu) { return iu + ((iu >> 5) << 4);
 
 __host__ __device__ inline int gbp_align(int x, int a) { return (x + a - 1) / a * a; }
 
+// Product marks over several channels (MODE_MARKC): the channels are staged and
+// summed in packed FP32 pairs, the number of pairs a power of two (zero columns
+// pad the last ones), so that 32 lanes split into (pair group, channel pair).
+__host__ __device__ inline int gbp_markc_pairs(int nw) {
+    int p = 1;
+    while (2 * p < nw) p <<= 1;
+    return p;
+}
+// From this many channel pairs on, MARKC sorts each code batch by bin and sums
+// the products bin by bin; with fewer, each lane adds its own channel's products
+// round by round to lane-private columns.
+#define GBP_MARKC_SORTED 4
+// MARKC per-warp scratch of one code batch (sorted form): each code's bin (u8),
+// the codes sorted by bin (u16), and two counters per bin
+__host__ __device__ inline int gbp_markc_sort_bytes(int nb0) {
+    return gbp_align(1024 + 2048 + 8 * (nb0 + 1), 16);
+}
+
 __host__ __device__ inline SmemLayout gbp_smem_layout(int mode, int T0, int T1, int nb0, int nb1,
                                                       int nsten, int copies, int jw,
                                                       int ntag = 0) {
@@ -182,7 +200,11 @@ __host__ __device__ inline SmemLayout gbp_smem_layout(int mode, int T0, int T1, 
     // codes of one 32-point j batch: 64 x 32 (marked modes: one i-point at a time, 32 x 32)
     L.off_code = o;
     o += adj ? 0 : GBP_WARPS * ((mode == MODE_MARK || mode == MODE_MARKC) ? 1024 : 2048) * 2;
-    L.off_rec = o; o += (mode == MODE_MARKC) ? GBP_WARPS * 32 * 16 : 0;  // binned pairs of a round
+    const bool msort = mode == MODE_MARKC && jw / 8 >= GBP_MARKC_SORTED;
+    L.off_rec = o;
+    o += mode != MODE_MARKC ? 0
+         : msort ? GBP_WARPS * gbp_markc_sort_bytes(nb0)
+                 : GBP_WARPS * 32 * 16;  // binned pairs of one round {bin, second bin, i, j}
     L.off_rq = o; o += smu ? GBP_WARPS * (GBP_RQCAP * 16 + 16) : 0;
     L.off_D = o; o += nsten * 16;
     L.off_E0 = o; o += gbp_align(nb0 * 8, 16);
@@ -199,8 +221,11 @@ __host__ __device__ inline SmemLayout gbp_smem_layout(int mode, int T0, int T1, 
     } else if (mode == MODE_JACK) {
         // lane-private u32 counts, then the CTA's u64 (tag, bin) table
         hist_bytes = gbp_align(GBP_WARPS * (nb0 + 1) * 32 * 4, 16) + ntag * (nb0 + 1) * 8;
-    } else if (mode == MODE_MARK || mode == MODE_MARKC) {
+    } else if (mode == MODE_MARK || (mode == MODE_MARKC && !msort)) {
         hist_bytes = GBP_WARPS * (nb0 + 1) * 32 * 4 * 2;      // lane-private FP32 sum + compensation
+    } else if (mode == MODE_MARKC) {
+        // per warp, (bin, channel pair): packed FP32 sums + packed compensations
+        hist_bytes = GBP_WARPS * (nb0 + 1) * (jw / 8) * 16;
     } else if (mode == MODE_ADJ) {
         hist_bytes = GBP_BLOCK * 8 + gbp_align((nb0 + 1) * 4, 16);  // partial sums + gt table
     } else if (mode == MODE_ADJC) {

@@ -117,16 +117,17 @@ def test_batched_forward_and_dw_match_fp64(gpu):
     from halotools_gb300 import differentiable as D
     L = 120.0
     pos, mass, _ = halos(8000, L, 21)
-    th = _thetas(11, 22)  # 11 draws: adjoint groups of 8 and 3
+    m_draws = 19  # adjoint groups of 8, 8 and 3
+    th = _thetas(m_draws, 22)
     W = np.stack([zheng07_np(t, mass) for t in th], axis=1)
     rb = np.logspace(-1, np.log10(15), 10)
     Wt = torch.from_numpy(W).cuda().requires_grad_(True)
     C = D.weighted_pair_counts_batched(Wt, torch.from_numpy(pos).cuda(), rb, L)
-    assert C.shape == (11, len(rb))
-    gbar = np.random.default_rng(23).normal(size=(11, len(rb)))
+    assert C.shape == (m_draws, len(rb))
+    gbar = np.random.default_rng(23).normal(size=(m_draws, len(rb)))
     (C * torch.from_numpy(gbar).cuda()).sum().backward()
     got_w = Wt.grad.cpu().numpy()
-    for m in range(11):
+    for m in range(m_draws):
         want = oracle.marked_npairs_3d(pos, pos, rb, 1, period=L, weights1=W[:, m],
                                        weights2=W[:, m], num_threads=8)
         np.testing.assert_allclose(C[m].detach().cpu().numpy(), want, rtol=1e-6)
