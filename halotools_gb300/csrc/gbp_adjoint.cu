@@ -253,10 +253,12 @@ __device__ __noinline__ int2 slow_adj_bins(float v, int b0, int is, int js, cons
 
 // k_gather_ch: the adjoint gather over up to NCH weight channels at once (one
 // parameter draw per channel): each in-range pair is binned once, then channel c
-// adds w_j^c G^c(bin) to the i-point's compensated sum in registers, so the
-// distance work is shared by all channels.  The G table is bin-major and the
-// channels go in packed f32x2 pairs: a pair costs 16-byte loads of G and w_j and
-// one packed compensated add per two channels, into registers.
+// adds w_j^c G^c(bin) to the i-point's sum in registers, so the distance work is
+// shared by all channels.  The G table is bin-major and the channels go in packed
+// f32x2 pairs: a pair costs 16-byte loads of G and w_j and one packed FMA per two
+// channels into a run of at most 8 pairs; each run is then one packed
+// compensated (Kahan) add.  Error bound per point and item for same-sign terms:
+// 7u per run plus about 2u for the compensated sum of the runs.
 template <int NCH>
 __global__ void __launch_bounds__(GBP_BLOCK, 2) k_gather_ch(const CountArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -318,9 +320,14 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_gather_ch(const CountArgs a) {
         unsigned long long acc0[NH], ncm0[NH], acc1[NH], ncm1[NH];
 #pragma unroll
         for (int q = 0; q < NH; q++) acc0[q] = ncm0[q] = acc1[q] = ncm1[q] = 0ull;
-        // the in-range pairs of one point in m, highest slot first
+        // the in-range pairs of one point in m, highest slot first: runs of up to 8
+        // products summed by packed FMA, each run then one compensated add
         auto gather = [&](unsigned m, const float4 &u, unsigned long long *acc,
                           unsigned long long *ncm) {
+            unsigned long long run[NH];
+#pragma unroll
+            for (int q = 0; q < NH; q++) run[q] = 0ull;
+            int nr = 0;
             while (m) {
                 const int jj = 31 - __clz(m);
                 m ^= 1u << jj;
@@ -359,7 +366,19 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_gather_ch(const CountArgs a) {
                     }
                 }
 #pragma unroll
-                for (int q = 0; q < NH; q++) kahan_f2(acc[q], ncm[q], w[q], g[q]);
+                for (int q = 0; q < NH; q++) run[q] = f2_fma(w[q], g[q], run[q]);
+                if (++nr == 8) {
+#pragma unroll
+                    for (int q = 0; q < NH; q++) {
+                        kahan_f2(acc[q], ncm[q], pk2(1.f, 1.f), run[q]);
+                        run[q] = 0ull;
+                    }
+                    nr = 0;
+                }
+            }
+            if (nr) {
+#pragma unroll
+                for (int q = 0; q < NH; q++) kahan_f2(acc[q], ncm[q], pk2(1.f, 1.f), run[q]);
             }
         };
         for (int sb = s0; sb < s1; sb += 32) {
@@ -569,92 +588,120 @@ __global__ void k_zheng07_vjp(const double *__restrict__ mass, int64_t n, Zheng0
 // The occupations in FP32 (the counting kernels multiply the weights in FP32
 // anyway, and GB300's FP64 units are slow) from an FP64 log10 M computed once per
 // halo; W is (n, M) row-major: halo i, draw m.
-__global__ void k_log10(const double *__restrict__ mass, int64_t n, double *__restrict__ lm) {
+// Per halo, once per call: log10 M (FP64) and M, each split into the nearest
+// float and the float nearest the remainder (0 beside an infinite part, so that
+// M = 0 gives log10 M = -inf and <Ncen> = 0 as in FP64)
+__global__ void k_zheng07_prep(const double *__restrict__ mass, int64_t n,
+                               float4 *__restrict__ hl) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-         i += (int64_t)gridDim.x * blockDim.x)
-        lm[i] = log10(mass[i]);
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const double M = mass[i], lm = log10(M);
+        const float lh = (float)lm, mh = (float)M;
+        hl[i] = make_float4(lh, isfinite(lh) ? (float)(lm - (double)lh) : 0.f, mh,
+                            isfinite(mh) ? (float)(M - (double)mh) : 0.f);
+    }
 }
 
-__device__ __forceinline__ void zheng07_terms_f(double M, double lm, const Zheng07 &t,
-                                                float *ncen, float *nsat, float *x, float *r) {
-    *x = (float)((lm - t.logMmin) * t.inv_sigma);
+// x = (log10 M - logMmin) / sigma_logM, r = (M - M0) / M1 and the FP32 mean
+// occupations of one (halo, draw); d = M - M0 decides M > M0 with the sign of
+// the FP64 difference
+__device__ __forceinline__ void zheng07_terms_f(const float4 &h, const Zheng07F &t, float *ncen,
+                                                float *nsat, float *x, float *r) {
+    *x = ((h.x - t.lmin_hi) + (h.y - t.lmin_lo)) * t.inv_sigma;
     *ncen = 0.5f * (1.0f + erff(*x));
-    *r = (float)((M - t.M0) * t.inv_M1);
-    *nsat = M > t.M0 ? powf(*r, (float)t.alpha) : 0.0f;
+    const float d = (h.z - t.m0_hi) + (h.w - t.m0_lo);
+    *r = d * t.inv_m1;
+    *nsat = d > 0.0f ? powf(*r, t.alpha) : 0.0f;
 }
 
-__global__ void k_zheng07_wb(const double *__restrict__ mass, const double *__restrict__ lm,
-                             int64_t n, const Zheng07 *__restrict__ th, int nth,
-                             double *__restrict__ W) {
-    const int64_t total = n * nth;
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
-         e += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t i = e / nth;
-        const int m = (int)(e - i * nth);
+__device__ __forceinline__ Zheng07F zheng07_f_load(const Zheng07F *th, int m) {
+    const float4 *p = (const float4 *)(th + m);
+    const float4 a = __ldg(p), b = __ldg(p + 1);
+    return Zheng07F{a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+}
+
+// W[i][m] for every (halo i, draw m): one element per thread, 32-bit indices
+// while n * nth fits
+template <class I>
+__global__ void k_zheng07_wb(const float4 *__restrict__ hl, I total, int nth,
+                             const Zheng07F *__restrict__ th, double *__restrict__ W) {
+    for (I e = blockIdx.x * (I)blockDim.x + threadIdx.x; e < total;
+         e += (I)gridDim.x * blockDim.x) {
+        const I i = e / (I)nth;
+        const int m = (int)(e - i * (I)nth);
         float nc, ns, x, r;
-        zheng07_terms_f(mass[i], lm[i], th[m], &nc, &ns, &x, &r);
+        zheng07_terms_f(hl[i], zheng07_f_load(th, m), &nc, &ns, &x, &r);
         W[e] = (double)nc + (double)ns;
     }
 }
 
 // out[m][5] += sum_i gW[i][m] dw_i/dtheta_m: warp gw keeps draw m = gw % nth and
-// strides over 32-halo chunks, so its terms reduce by shuffles to one add each
-__global__ void k_zheng07_vjpb(const double *__restrict__ mass, const double *__restrict__ lm,
-                               int64_t n, const Zheng07 *__restrict__ th, int nth,
+// strides over 32-halo chunks.  Each lane sums its terms in FP32 with Kahan
+// compensation; the lanes' totals reduce in FP64 by shuffles to one add each.
+__global__ void k_zheng07_vjpb(const float4 *__restrict__ hl, int64_t n,
+                               const Zheng07F *__restrict__ th, int nth,
                                const double *__restrict__ gW, int nwarps, double *out) {
     const int gw = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
     if (gw >= nwarps) return;  // (whole warps)
     const int m = gw % nth, wstep = nwarps / nth;
-    const Zheng07 t = th[m];
+    const Zheng07F t = zheng07_f_load(th, m);
     const float ln10 = 2.302585093f;
-    const float c2 = (float)(-t.M0 * 2.30258509299404568402 * t.inv_M1);
-    double d[5] = {0, 0, 0, 0, 0};
-    for (int64_t c = gw / nth; c * 32 < n; c += wstep) {
-        const int64_t i = c * 32 + lane;
+    float s[5] = {0, 0, 0, 0, 0}, c[5] = {0, 0, 0, 0, 0};
+    auto add = [&](int k, float v) {
+        const float y = v - c[k], u = s[k] + y;
+        c[k] = (u - s[k]) - y;
+        s[k] = u;
+    };
+    for (int64_t ch = gw / nth; ch * 32 < n; ch += wstep) {
+        const int64_t i = ch * 32 + lane;
         if (i >= n) continue;
-        const double g = gW[i * nth + m];
+        const float g = (float)gW[i * nth + m];
         float nc, ns, x, r;
-        zheng07_terms_f(mass[i], lm[i], t, &nc, &ns, &x, &r);
+        zheng07_terms_f(hl[i], t, &nc, &ns, &x, &r);
         // d/dx of (1 + erf x)/2 is exp(-x^2)/sqrt(pi)
         const float dphi = expf(-x * x) * 0.5641895835f;
-        d[0] += g * (double)(-dphi * (float)t.inv_sigma);      // logMmin
-        d[1] += g * (double)(-dphi * x * (float)t.inv_sigma);  // sigma_logM
+        add(0, g * (-dphi * t.inv_sigma));      // logMmin
+        add(1, g * (-dphi * x * t.inv_sigma));  // sigma_logM
         if (ns > 0.0f) {
-            d[2] += g * (double)((float)t.alpha * ns / r * c2);  // logM0
-            d[3] += g * (double)(-(float)t.alpha * ln10 * ns);   // logM1
-            d[4] += g * (double)(ns * logf(r));                  // alpha
+            add(2, g * (t.alpha * ns / r * t.c2));  // logM0
+            add(3, g * (-t.alpha * ln10 * ns));     // logM1
+            add(4, g * (ns * logf(r)));             // alpha
         }
     }
 #pragma unroll
     for (int k = 0; k < 5; k++) {
-        double v = d[k];
+        double v = (double)s[k] - (double)c[k];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
         if (lane == 0 && v != 0.0) atomicAdd(&out[m * 5 + k], v);
     }
 }
 
-cudaError_t gbp_launch_zheng07_wb(const double *mass, double *lm, int64_t n, const Zheng07 *th,
+cudaError_t gbp_launch_zheng07_wb(const double *mass, float4 *hl, int64_t n, const Zheng07F *th,
                                   int nth, double *W, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    k_log10<<<(unsigned)std::min<int64_t>((n + 255) / 256, 152 * 16), 256, 0, st>>>(mass, n, lm);
+    k_zheng07_prep<<<(unsigned)std::min<int64_t>((n + 255) / 256, 152 * 16), 256, 0, st>>>(mass, n,
+                                                                                           hl);
     const int64_t total = n * nth;
     const unsigned g = (unsigned)std::min<int64_t>((total + 255) / 256, 152 * 16);
-    k_zheng07_wb<<<g, 256, 0, st>>>(mass, lm, n, th, nth, W);
+    if (total < ((int64_t)1 << 31))
+        k_zheng07_wb<int><<<g, 256, 0, st>>>(hl, (int)total, nth, th, W);
+    else
+        k_zheng07_wb<int64_t><<<g, 256, 0, st>>>(hl, total, nth, th, W);
     return cudaGetLastError();
 }
 
-cudaError_t gbp_launch_zheng07_vjpb(const double *mass, double *lm, int64_t n, const Zheng07 *th,
+cudaError_t gbp_launch_zheng07_vjpb(const double *mass, float4 *hl, int64_t n, const Zheng07F *th,
                                     int nth, const double *gW, double *out, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    k_log10<<<(unsigned)std::min<int64_t>((n + 255) / 256, 152 * 16), 256, 0, st>>>(mass, n, lm);
+    k_zheng07_prep<<<(unsigned)std::min<int64_t>((n + 255) / 256, 152 * 16), 256, 0, st>>>(mass, n,
+                                                                                           hl);
     // a whole number of warps per draw
     const int64_t chunks = (n + 31) / 32;
     const int per = (int)std::max<int64_t>(1, std::min<int64_t>(chunks, (152 * 16 * 8) / nth));
     const int nwarps = per * nth;
-    k_zheng07_vjpb<<<(unsigned)((nwarps + 7) / 8), 256, 0, st>>>(mass, lm, n, th, nth, gW, nwarps,
-                                                                  out);
+    k_zheng07_vjpb<<<(unsigned)((nwarps + 7) / 8), 256, 0, st>>>(hl, n, th, nth, gW, nwarps, out);
     return cudaGetLastError();
 }
 

@@ -1761,12 +1761,14 @@ static int zheng07_args(gbp_plan *plan, const double *theta, Zheng07 *th) {
 // Zheng07 weights / VJP for nth parameter vectors at once: the derived constants
 // of every vector on the device, then one launch over (halo, vector)
 static int zheng07_batched_args(gbp_plan *plan, const double *thetas, int32_t nth,
-                                std::vector<Zheng07> &th) {
+                                std::vector<Zheng07F> &th) {
     if (!thetas || nth < 1) return fail(plan, GBP_ERR_INVALID, "no parameter vector");
     th.resize((size_t)nth);
     for (int m = 0; m < nth; m++) {
-        int rc = zheng07_args(plan, thetas + 5 * (size_t)m, &th[(size_t)m]);
+        Zheng07 t;
+        int rc = zheng07_args(plan, thetas + 5 * (size_t)m, &t);
         if (rc) return rc;
+        th[(size_t)m] = gbp_zheng07_f(t);
     }
     return GBP_OK;
 }
@@ -1774,7 +1776,7 @@ static int zheng07_batched_args(gbp_plan *plan, const double *thetas, int32_t nt
 int gbp_zheng07_weights_batched(gbp_plan *plan, const double *mass, int64_t n,
                                 const double *thetas, int32_t nth, int32_t mem, double *W) {
     if (!plan) return GBP_ERR_INVALID;
-    std::vector<Zheng07> th;
+    std::vector<Zheng07F> th;
     int rc = zheng07_batched_args(plan, thetas, nth, th);
     if (rc) return rc;
     if (n < 0 || (n > 0 && (!mass || !W))) return fail(plan, GBP_ERR_INVALID, "null arrays");
@@ -1782,13 +1784,13 @@ int gbp_zheng07_weights_batched(gbp_plan *plan, const double *mass, int64_t n,
     CK(cudaSetDevice(plan->device));
     cudaStream_t st = plan->stream;
     Carve cv;
-    size_t o_th = cv.take<Zheng07>((size_t)nth);
-    size_t o_lm = cv.take<double>((size_t)n);
+    size_t o_th = cv.take<Zheng07F>((size_t)nth);
+    size_t o_lm = cv.take<float4>((size_t)n);
     size_t o_m = mem == GBP_MEM_HOST ? cv.take<double>((size_t)n) : 0;
     size_t o_w = mem == GBP_MEM_HOST ? cv.take<double>((size_t)n * nth) : 0;
     if ((rc = ensure_work(plan, cv.take<char>(0) + 256))) return rc;
     void *Wk = plan->work.p;
-    CK(cudaMemcpyAsync(at<char>(Wk, o_th), th.data(), sizeof(Zheng07) * nth, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(at<char>(Wk, o_th), th.data(), sizeof(Zheng07F) * nth, cudaMemcpyHostToDevice, st));
     const double *dm = mass;
     double *dw = W;
     if (mem == GBP_MEM_HOST) {
@@ -1796,7 +1798,7 @@ int gbp_zheng07_weights_batched(gbp_plan *plan, const double *mass, int64_t n,
         dw = at<double>(Wk, o_w);
         CK(cudaMemcpyAsync((void *)dm, mass, n * sizeof(double), cudaMemcpyHostToDevice, st));
     }
-    CK(gbp_launch_zheng07_wb(dm, at<double>(Wk, o_lm), n, at<Zheng07>(Wk, o_th), nth, dw, st));
+    CK(gbp_launch_zheng07_wb(dm, at<float4>(Wk, o_lm), n, at<Zheng07F>(Wk, o_th), nth, dw, st));
     if (mem == GBP_MEM_HOST)
         CK(cudaMemcpyAsync(W, dw, (size_t)n * nth * sizeof(double), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
@@ -1806,7 +1808,7 @@ int gbp_zheng07_weights_batched(gbp_plan *plan, const double *mass, int64_t n,
 int gbp_zheng07_vjp_batched(gbp_plan *plan, const double *mass, int64_t n, const double *thetas,
                             int32_t nth, const double *grad_W, int32_t mem, double *grad_theta) {
     if (!plan) return GBP_ERR_INVALID;
-    std::vector<Zheng07> th;
+    std::vector<Zheng07F> th;
     int rc = zheng07_batched_args(plan, thetas, nth, th);
     if (rc) return rc;
     if (!grad_theta || n < 0 || (n > 0 && (!mass || !grad_W)))
@@ -1816,14 +1818,14 @@ int gbp_zheng07_vjp_batched(gbp_plan *plan, const double *mass, int64_t n, const
     CK(cudaSetDevice(plan->device));
     cudaStream_t st = plan->stream;
     Carve cv;
-    size_t o_th = cv.take<Zheng07>((size_t)nth);
+    size_t o_th = cv.take<Zheng07F>((size_t)nth);
     size_t o_out = cv.take<double>(5 * (size_t)nth);
-    size_t o_lm = cv.take<double>((size_t)n);
+    size_t o_lm = cv.take<float4>((size_t)n);
     size_t o_m = mem == GBP_MEM_HOST ? cv.take<double>((size_t)n) : 0;
     size_t o_g = mem == GBP_MEM_HOST ? cv.take<double>((size_t)n * nth) : 0;
     if ((rc = ensure_work(plan, cv.take<char>(0) + 256))) return rc;
     void *Wk = plan->work.p;
-    CK(cudaMemcpyAsync(at<char>(Wk, o_th), th.data(), sizeof(Zheng07) * nth, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(at<char>(Wk, o_th), th.data(), sizeof(Zheng07F) * nth, cudaMemcpyHostToDevice, st));
     CK(cudaMemsetAsync(at<char>(Wk, o_out), 0, sizeof(double) * 5 * nth, st));
     const double *dm = mass, *dg = grad_W;
     if (mem == GBP_MEM_HOST) {
@@ -1832,7 +1834,7 @@ int gbp_zheng07_vjp_batched(gbp_plan *plan, const double *mass, int64_t n, const
         CK(cudaMemcpyAsync((void *)dm, mass, n * sizeof(double), cudaMemcpyHostToDevice, st));
         CK(cudaMemcpyAsync((void *)dg, grad_W, (size_t)n * nth * sizeof(double), cudaMemcpyHostToDevice, st));
     }
-    CK(gbp_launch_zheng07_vjpb(dm, at<double>(Wk, o_lm), n, at<Zheng07>(Wk, o_th), nth, dg,
+    CK(gbp_launch_zheng07_vjpb(dm, at<float4>(Wk, o_lm), n, at<Zheng07F>(Wk, o_th), nth, dg,
                                at<double>(Wk, o_out), st));
     CK(cudaMemcpyAsync(grad_theta, at<double>(Wk, o_out), sizeof(double) * 5 * nth, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));

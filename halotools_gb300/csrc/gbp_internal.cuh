@@ -347,11 +347,31 @@ cudaError_t gbp_launch_zheng07_w(const double *mass, int64_t n, Zheng07 th, doub
                                  cudaStream_t st);
 cudaError_t gbp_launch_zheng07_vjp(const double *mass, int64_t n, Zheng07 th, const double *gw,
                                    double *out5, cudaStream_t st);
+// Single-precision form of one parameter vector for the batched kernels.  The
+// per-draw differences log10 M - logMmin and M - M0 are formed from hi + lo
+// float splits of both sides: hi - hi is exact when the two lie within a factor
+// of 2 (Sterbenz), and the lo parts carry the rest, so the cancellation costs no
+// FP64 arithmetic per (halo, draw).
+struct Zheng07F {
+    float lmin_hi, lmin_lo, m0_hi, m0_lo, inv_sigma, inv_m1, alpha, c2;
+};
+inline Zheng07F gbp_zheng07_f(const Zheng07 &t) {
+    Zheng07F f;
+    f.lmin_hi = (float)t.logMmin;
+    f.lmin_lo = (float)(t.logMmin - (double)f.lmin_hi);
+    f.m0_hi = (float)t.M0;
+    f.m0_lo = (float)(t.M0 - (double)f.m0_hi);
+    f.inv_sigma = (float)t.inv_sigma;
+    f.inv_m1 = (float)t.inv_M1;
+    f.alpha = (float)t.alpha;
+    f.c2 = (float)(-t.M0 * 2.30258509299404568402 * t.inv_M1);  // d r / d logM0
+    return f;
+}
 // many parameter vectors (th: nth device structs): W (n, nth) and out (nth, 5)
-// (lm: n doubles of scratch for log10 M)
-cudaError_t gbp_launch_zheng07_wb(const double *mass, double *lm, int64_t n, const Zheng07 *th,
+// (hl: n float4 of scratch for the halos' hi + lo splits of log10 M and M)
+cudaError_t gbp_launch_zheng07_wb(const double *mass, float4 *hl, int64_t n, const Zheng07F *th,
                                   int nth, double *W, cudaStream_t st);
-cudaError_t gbp_launch_zheng07_vjpb(const double *mass, double *lm, int64_t n, const Zheng07 *th,
+cudaError_t gbp_launch_zheng07_vjpb(const double *mass, float4 *hl, int64_t n, const Zheng07F *th,
                                     int nth, const double *gW, double *out, cudaStream_t st);
 // Zheng07 mocks on the GPU (gbp_hod.cu): thetas as (n, 5) rows converted by
 // gbp_hod_thetas into gbp_hod_theta_bytes() each
