@@ -111,56 +111,6 @@ def hod_mock(pos, mass, conc, lbox, theta, seed=0):
     return np.mod(np.concatenate([cen, sat]), lbox)
 
 
-def hod_mocks_torch(pos, mass, conc, lbox, thetas, seed=0, dtype=None):
-    """Many Zheng07 realisations on the GPU (torch), concatenated.
-
-    pos (N, 3), mass, conc: halo table (numpy or torch).  thetas: (M, 5) array
-    of (logMmin, sigma_logM, logM0, logM1, alpha).  Bernoulli centrals at the
-    halo centre, Poisson satellites at NFW radii (bisection of the enclosed-mass
-    profile) in isotropic directions, wrapped into the box.  Returns (xyz, offsets):
-    a CUDA tensor (total, 3) and a numpy int64 array of M+1 row offsets.
-    """
-    import torch
-    dev = torch.device("cuda")
-    dtype = dtype or torch.float32
-    g = torch.Generator(device=dev)
-    g.manual_seed(int(seed))
-    P = torch.as_tensor(pos, dtype=torch.float64, device=dev)
-    M = torch.as_tensor(mass, dtype=torch.float64, device=dev)
-    C = torch.as_tensor(conc, dtype=torch.float64, device=dev)
-    logm = torch.log10(M)
-    rvir_all = (M / 1e14) ** (1.0 / 3.0)
-    parts, offsets = [], [0]
-    for th in np.asarray(thetas, dtype=np.float64):
-        logMmin, sig, logM0, logM1, alpha = (float(v) for v in th)
-        ncen = 0.5 * (1.0 + torch.erf((logm - logMmin) / sig))
-        m0, m1 = 10.0 ** logM0, 10.0 ** logM1
-        nsat = torch.where(M > m0, torch.clamp((M - m0) / m1, min=0.0) ** alpha,
-                           torch.zeros_like(M))
-        cen = P[torch.rand(M.shape, generator=g, device=dev, dtype=torch.float64) < ncen]
-        ns = torch.poisson(nsat, generator=g).to(torch.int64)
-        host = torch.repeat_interleave(torch.arange(len(M), device=dev), ns)
-        c = C[host]
-        u = torch.rand(host.shape, generator=g, device=dev, dtype=torch.float64)
-        target = u * (torch.log1p(c) - c / (1.0 + c))
-        lo, hi = torch.zeros_like(c), c.clone()
-        for _ in range(40):
-            mid = 0.5 * (lo + hi)
-            below = (torch.log1p(mid) - mid / (1.0 + mid)) < target
-            lo = torch.where(below, mid, lo)
-            hi = torch.where(below, hi, mid)
-        r = 0.5 * (lo + hi) / c * rvir_all[host]
-        d = torch.randn((len(host), 3), generator=g, device=dev, dtype=torch.float64)
-        d = d / torch.linalg.norm(d, dim=1, keepdim=True)
-        sat = P[host] + d * r[:, None]
-        gal = torch.remainder(torch.cat([cen, sat]), lbox)
-        # remainder can round up to exactly lbox for tiny negative inputs; keep [0, lbox)
-        gal = torch.where(gal >= lbox, gal - lbox, gal)
-        parts.append(gal.to(dtype))
-        offsets.append(offsets[-1] + len(gal))
-    return torch.cat(parts).contiguous(), np.asarray(offsets, dtype=np.int64)
-
-
 def hod_mocks_gpu(pos, mass, conc, lbox, thetas, seed=0, rvir=None, plan=None):
     """Many Zheng07 realisations drawn by the GPU kernels (``gbp_hod_mocks``).
 
