@@ -487,7 +487,7 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
         }
         const int jwb = jw ? 4 * c.nw   // {w, tag} columns
                         : (c.mode == MODE_MARK || w2) ? (c.wf == 0 ? 8 * c.nw : 4)
-                        : c.mode == MODE_MARKC ? 8 * gbp_markc_pairs(c.nw)
+                        : c.mode == MODE_MARKC ? 4 * gbp_markc_cols(c.nw)
                         : c.mode == MODE_ADJ   ? 4
                         : c.mode == MODE_ADJC  ? 4 * GBP_ADJ_CH  // the kernel's fixed stride
                         : c.mode == MODE_POBJ  ? 4   // the gather kernel's fixed stride

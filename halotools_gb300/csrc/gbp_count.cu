@@ -483,11 +483,15 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
     const int copies = a.hist_copies;  // 2-D / wide: GBP_WARPS (one per warp) or 0 (global)
     constexpr bool JACK = (MODE == MODE_JACK);    // w1 / w2 hold the subsample tags
     const int nw = (MW || COLS || JACK || JACK2) ? a.nw : 0;
-    // MARKC: channel pairs and the staged column count (zero columns pad to 2 mP)
+    // MARKC: channel pairs and the staged column count (sorted form: zero columns
+    // pad to 2 mP, a power of two)
     const int mP = MARKC ? gbp_markc_pairs(nw) : 1;
-    const int ncol = MARKC ? 2 * mP : nw;
-    const int lcol = 31 - __clz(ncol > 0 ? ncol : 1);  // ncol is a power of two when COLS
-    const bool msort = MARKC && mP >= GBP_MARKC_SORTED;
+    const int ncol = MARKC ? gbp_markc_cols(nw) : nw;
+    const bool cpow2 = ncol > 0 && (ncol & (ncol - 1)) == 0;
+    const int lcol = 31 - __clz(ncol > 0 ? ncol : 1);
+    const bool msort = MARKC && gbp_markc_sorted(nw);
+    // staged element t of a column table: its row
+    auto col_row = [&](int t) { return cpow2 ? t >> lcol : t / ncol; };
     const int jwb = MW ? (WF == 0 ? 8 * nw : 4) : COLS ? 4 * ncol : (JACK || JACK2) ? 4 : 0;
     const SmemLayout L = gbp_smem_layout(MODE, T0, T1, nb0, nb1, a.nsten, copies, jwb, a.ntag);
     if (gbp_smem_too_small(L.total, a.err)) return;
@@ -780,13 +784,13 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                 float v[8];
 #pragma unroll
                 for (int u = 0; u < 8; u++) {
-                    const int t = t0 + 32 * u + lane, sp = t >> lcol, q = t & (ncol - 1);
+                    const int t = t0 + 32 * u + lane, sp = col_row(t), q = t - sp * ncol;
                     v[u] = (t < 64 * ncol && sp < icnt && q < nw)
                                ? __ldg(&a.w1[(int64_t)(ifirst + sp) * nw + q]) : 0.f;
                 }
 #pragma unroll
                 for (int u = 0; u < 8; u++) {
-                    const int t = t0 + 32 * u + lane, sp = t >> lcol, q = t & (ncol - 1);
+                    const int t = t0 + 32 * u + lane, sp = col_row(t), q = t - sp * ncol;
                     if (t < 64 * ncol) s_uw[gbp_uslot(sp) * ncol + q] = v[u];
                 }
             }
@@ -864,8 +868,8 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                         float v[8];
 #pragma unroll
                         for (int u = 0; u < 8; u++) {
-                            const int t = t0 + 32 * u + lane, q = t & (ncol - 1);
-                            const int js = __shfl_sync(FULL, jg, (t >> lcol) & 31);
+                            const int t = t0 + 32 * u + lane, r = col_row(t), q = t - r * ncol;
+                            const int js = __shfl_sync(FULL, jg, r & 31);
                             v[u] = (t < 32 * ncol && js >= 0 && q < nw)
                                        ? __ldg(&a.w2[(int64_t)js * nw + q]) : 0.f;
                         }

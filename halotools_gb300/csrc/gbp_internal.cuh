@@ -166,10 +166,22 @@ __host__ __device__ inline int gbp_markc_pairs(int nw) {
     while (2 * p < nw) p <<= 1;
     return p;
 }
-// From this many channel pairs on, MARKC sorts each code batch by bin and sums
-// the products bin by bin; with fewer, each lane adds its own channel's products
-// round by round to lane-private columns.
+// With GBP_MARKC_SORTED to GBP_MARKC_SORTED_MAX channel pairs (5 to 16
+// channels), MARKC sorts each code batch by bin and sums the products bin by
+// bin; otherwise each lane adds its own channel's products round by round to
+// lane-private columns (with 17 to 32 channels the sort scratch would push the
+// shared memory past the per-CTA limit at a few more bins).
 #define GBP_MARKC_SORTED 4
+#define GBP_MARKC_SORTED_MAX 8
+__host__ __device__ inline bool gbp_markc_sorted(int nw) {
+    const int p = gbp_markc_pairs(nw);
+    return p >= GBP_MARKC_SORTED && p <= GBP_MARKC_SORTED_MAX;
+}
+// MARKC staged columns per point: packed pairs (zero-padded) in the sorted form,
+// the channels themselves otherwise
+__host__ __device__ inline int gbp_markc_cols(int nw) {
+    return gbp_markc_sorted(nw) ? 2 * gbp_markc_pairs(nw) : nw;
+}
 // MARKC per-warp scratch of one code batch (sorted form): each code's bin (u8),
 // the codes sorted by bin (u16), and two counters per bin
 __host__ __device__ inline int gbp_markc_sort_bytes(int nb0) {
@@ -200,7 +212,7 @@ __host__ __device__ inline SmemLayout gbp_smem_layout(int mode, int T0, int T1, 
     // codes of one 32-point j batch: 64 x 32 (marked modes: one i-point at a time, 32 x 32)
     L.off_code = o;
     o += adj ? 0 : GBP_WARPS * ((mode == MODE_MARK || mode == MODE_MARKC) ? 1024 : 2048) * 2;
-    const bool msort = mode == MODE_MARKC && jw / 8 >= GBP_MARKC_SORTED;
+    const bool msort = mode == MODE_MARKC && gbp_markc_sorted(jw / 4);
     L.off_rec = o;
     o += mode != MODE_MARKC ? 0
          : msort ? GBP_WARPS * gbp_markc_sort_bytes(nb0)
