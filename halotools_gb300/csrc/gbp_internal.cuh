@@ -170,7 +170,7 @@ __host__ __device__ inline int gbp_markc_pairs(int nw) {
 // channels), MARKC sorts each code batch by bin and sums the products bin by
 // bin; otherwise each lane adds its own channel's products round by round to
 // lane-private columns (with 17 to 32 channels the sort scratch would push the
-// shared memory past the per-CTA limit at a few more bins).
+// shared memory past the per-CTA limit from about 23 bins on).
 #define GBP_MARKC_SORTED 4
 #define GBP_MARKC_SORTED_MAX 8
 __host__ __device__ inline bool gbp_markc_sorted(int nw) {
