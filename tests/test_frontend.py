@@ -152,3 +152,20 @@ def test_neighbour_messages():
     with pytest.raises(ValueError) as err:
         h.spherical_isolation(S, S, 0.5, period=1)
     assert "cannot be larger than Lbox/3" in str(err.value)
+
+
+def test_marked_channels_messages():
+    # (N, nch) marks, 1 <= nch <= 32, the same channel count on both sides
+    rb = [0.1, 0.2]
+    with pytest.raises(ValueError, match="1 to 32 mark channels"):
+        h.marked_npairs_3d_channels(S, S, rb, period=1, weights1=np.ones((50, 33)),
+                                    weights2=np.ones((50, 33)))
+    with pytest.raises(h.HalotoolsError, match="same number of channels"):
+        h.marked_npairs_3d_channels(S, S, rb, period=1, weights1=np.ones((50, 2)),
+                                    weights2=np.ones((50, 3)))
+    with pytest.raises(h.HalotoolsError, match="must have shape"):
+        h.marked_npairs_3d_channels(S, S, rb, period=1, weights1=np.ones((49, 2)))
+    with pytest.raises(h.HalotoolsError, match="must have shape"):
+        h.marked_npairs_3d_channels(S, S, rb, period=1, weights1=np.ones((50, 2, 1)))
+    with pytest.raises(ValueError, match="monotonically increasing"):
+        h.marked_npairs_3d_channels(S, S, [0.2, 0.1, 0.05], period=1)
