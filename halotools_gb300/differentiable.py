@@ -177,7 +177,9 @@ class WeightedPairCountsBatched(torch.autograd.Function):
 
 class Zheng07WeightsBatched(torch.autograd.Function):
     """W[:, m] = <Ncen>(M_i; theta_m) + <Nsat>(M_i; theta_m) for thetas (M, 5): one
-    launch over (halo, draw) each way (occupations in FP32, the VJP summed in FP64)."""
+    launch over (halo, draw) each way (occupations and VJP terms in FP32 from hi/lo
+    float splits of log10 M and M; each lane's VJP sums compensated in FP32, the
+    lanes reduced in FP64)."""
 
     @staticmethod
     def forward(ctx, thetas, mass):

@@ -169,3 +169,15 @@ def test_marked_channels_messages():
         h.marked_npairs_3d_channels(S, S, rb, period=1, weights1=np.ones((50, 2, 1)))
     with pytest.raises(ValueError, match="monotonically increasing"):
         h.marked_npairs_3d_channels(S, S, [0.2, 0.1, 0.05], period=1)
+
+
+def test_batched_weight_columns_message():
+    torch = pytest.importorskip("torch")
+    from halotools_gb300 import differentiable as D
+    x = torch.zeros((10, 3), dtype=torch.float64)
+    for W in (torch.ones((10, 33), dtype=torch.float64), torch.ones(10, dtype=torch.float64)):
+        with pytest.raises(ValueError, match="1 <= M <= 32"):
+            D.weighted_pair_counts_batched(W, x, [0.1, 0.2], 1.0)
+    with pytest.raises(ValueError, match="Lbox/3"):
+        D.weighted_pair_counts_batched(torch.ones((10, 2), dtype=torch.float64), x, [0.1, 0.5],
+                                       1.0)
