@@ -621,7 +621,7 @@ __device__ __forceinline__ Zheng07F zheng07_f_load(const Zheng07F *th, int m) {
 }
 
 // W[i][m] for every (halo i, draw m): one element per thread, 32-bit indices
-// while n * nth fits
+// while n * nth stays below 2^30
 template <class I>
 __global__ void k_zheng07_wb(const float4 *__restrict__ hl, I total, int nth,
                              const Zheng07F *__restrict__ th, double *__restrict__ W) {
@@ -685,7 +685,8 @@ cudaError_t gbp_launch_zheng07_wb(const double *mass, float4 *hl, int64_t n, con
                                                                                            hl);
     const int64_t total = n * nth;
     const unsigned g = (unsigned)std::min<int64_t>((total + 255) / 256, 152 * 16);
-    if (total < ((int64_t)1 << 31))
+    // 32-bit indices while the last grid stride cannot pass INT_MAX (stride < 2^20)
+    if (total < ((int64_t)1 << 30))
         k_zheng07_wb<int><<<g, 256, 0, st>>>(hl, (int)total, nth, th, W);
     else
         k_zheng07_wb<int64_t><<<g, 256, 0, st>>>(hl, total, nth, th, W);
