@@ -1900,7 +1900,26 @@ int gbp_hod_mocks(gbp_plan *plan, const double *halo_xyz, const double *mass, co
     for (int m = 0; m <= n_theta; m++)
         CK(cudaMemcpyAsync(&hoff[(size_t)m], off + (int64_t)m * n_halo, sizeof(int),
                            cudaMemcpyDeviceToHost, st));
+    // the total in int64 from the scan's parts: the int32 offsets are only valid
+    // while it stays below 2^31 and no count is negative
+    const int *parts = nullptr;
+    int64_t nparts = 0;
+    gbp_scan_parts(cnt, items, at<int>(W, o_scan), &parts, &nparts);
+    std::vector<int> hparts((size_t)std::max<int64_t>(nparts, 1));
+    if (nparts > 0)
+        CK(cudaMemcpyAsync(hparts.data(), parts, (size_t)nparts * sizeof(int),
+                           cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
+    int64_t sum = 0;
+    bool neg = false;
+    for (int64_t k = 0; k < nparts; k++) {
+        neg |= hparts[(size_t)k] < 0;
+        sum += hparts[(size_t)k];
+    }
+    if (neg || sum >= (int64_t)INT32_MAX)
+        return fail(plan, GBP_ERR_INVALID,
+                    "the draws give %lld galaxies in all, beyond the 2^31 - 1 the offsets hold",
+                    (long long)sum);
     for (int m = 0; m <= n_theta; m++) offsets[m] = hoff[(size_t)m];
     const int64_t total = offsets[n_theta];
     if (!gal_xyz || cap < total || total == 0) return GBP_OK;  // offsets only

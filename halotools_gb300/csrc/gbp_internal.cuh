@@ -332,6 +332,8 @@ cudaError_t gbp_build_items(const ItemPlan &ip, int4 *d_items, int cap, int *d_n
 cudaError_t gbp_scan_exclusive(const int *d_in, int *d_out, int64_t n, int *d_tmp,
                                cudaStream_t st, int *launches);
 size_t gbp_scan_tmp_ints(int64_t n);
+void gbp_scan_parts(const int *d_in, int64_t n, const int *d_tmp, const int **parts,
+                    int64_t *nparts);
 
 // mode: MODE_*; wf: marking-function template (1 product, 2 sum, 0 any id in FP64)
 cudaError_t gbp_launch_count(int mode, int wf, const CountArgs &a, int grid, size_t smem,

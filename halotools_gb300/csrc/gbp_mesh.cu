@@ -183,6 +183,17 @@ __global__ void k_scan_add(int *__restrict__ out, int64_t n, const int *__restri
     }
 }
 
+// The device array whose entries add up to the total of the n counts that
+// gbp_scan_exclusive just summed: the counts themselves when they fit one tile,
+// else the per-tile sums it leaves at the start of its scratch (a few KB).  The
+// caller adds them in int64 to check that the int32 prefix did not wrap.
+void gbp_scan_parts(const int *d_in, int64_t n, const int *d_tmp, const int **parts,
+                    int64_t *nparts) {
+    const int64_t tiles = (n + 1 + SCAN_TILE - 1) / SCAN_TILE;
+    *parts = tiles == 1 ? d_in : d_tmp;
+    *nparts = tiles == 1 ? n : tiles;
+}
+
 size_t gbp_scan_tmp_ints(int64_t n) {
     size_t total = 0;
     int64_t m = n + 1;
