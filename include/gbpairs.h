@@ -150,7 +150,9 @@ int gbp_weighted_adjoint_3d_channels(gbp_plan *plan, const double *xyz, int64_t 
  * gbp_zheng07_weights and gbp_zheng07_vjp for nth parameter vectors at once
  * (thetas (nth, 5)): W (n, nth) row-major, grad_W likewise, grad_theta (nth, 5)
  * on the host.  The occupations are evaluated in FP32 (the counting kernels
- * multiply weights in FP32), the VJP sums in FP64.
+ * multiply weights in FP32) from hi + lo float splits of the FP64 log10 M and M;
+ * the VJP terms are FP32, summed with compensation per lane and in FP64 across
+ * lanes.
  */
 int gbp_zheng07_weights_batched(gbp_plan *plan, const double *mass, int64_t n,
                                 const double *thetas, int32_t nth, int32_t mem, double *W);
@@ -170,7 +172,8 @@ int gbp_zheng07_vjp_batched(gbp_plan *plan, const double *mass, int64_t n, const
  * of gal_xyz, (offsets[n_theta], 3) float32.  With gal_xyz NULL or cap (rows)
  * below the total, only offsets are written: call again with a buffer of
  * offsets[n_theta] rows.  mem: all arrays on the host or all on the device
- * (offsets always on the host).
+ * (offsets always on the host).  GBP_ERR_INVALID (offsets left 0) when the
+ * draws give 2^31 - 1 galaxies or more in all.
  */
 int gbp_hod_mocks(gbp_plan *plan, const double *halo_xyz, const double *mass, const double *conc,
                   const double *rvir, int64_t n_halo, const double *thetas, int32_t n_theta,
