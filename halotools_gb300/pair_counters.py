@@ -73,22 +73,31 @@ def _columns(sample):
     return s
 
 
-def _enclose_in_box(s1, s2, min_size):
-    # mesh_helpers.py:17-64: shift by the smallest coordinate over both samples
-    # and all three dimensions, in the input dtype; box = largest extent,
-    # padded to min_size.
-    x1, x2 = s1[:, :3], s2[:, :3]
-    xyzmin = np.min([np.min(x1[:, 0]), np.min(x2[:, 0]), np.min(x1[:, 1]), np.min(x2[:, 1]),
-                     np.min(x1[:, 2]), np.min(x2[:, 2])])
-    xyzmax = np.max([np.max(x1[:, 0]), np.max(x2[:, 0]), np.max(x1[:, 1]), np.max(x2[:, 1]),
-                     np.max(x1[:, 2]), np.max(x2[:, 2])]) - xyzmin
-    x1 = x1 - xyzmin
-    x2 = x2 - xyzmin
+def _enclosing_box(s1, s2, min_size, same=False):
+    # mesh_helpers.py:17-64: the smallest coordinate over both samples and all
+    # three dimensions (in the input dtype) and the box = largest extent, padded
+    # to min_size.  One reduction over each sample's three columns gives the same
+    # minimum and maximum as the reference's six per-column reductions.
+    x1 = s1[:, :3]
+    x2 = x1 if same else s2[:, :3]
+    lo = [np.min(x1)] if same else [np.min(x1), np.min(x2)]
+    hi = [np.max(x1)] if same else [np.max(x1), np.max(x2)]
+    xyzmin = np.min(lo)
+    xyzmax = np.max(hi) - xyzmin
     lbox = np.array([xyzmax, xyzmax, xyzmax])
     min_size = np.atleast_1d(min_size)
     if np.any(lbox < min_size):
         lbox[(lbox < min_size)] = min_size[(lbox < min_size)]
-    return x1, x2, lbox.astype(np.float64)
+    return xyzmin, lbox.astype(np.float64)
+
+
+def _enclose_in_box(s1, s2, min_size, same=False):
+    # mesh_helpers.py:17-64: both samples shifted by the smallest coordinate, in
+    # the input dtype (a sample given twice is shifted once), and the box
+    xyzmin, lbox = _enclosing_box(s1, s2, min_size, same)
+    x1 = s1[:, :3] - xyzmin
+    x2 = x1 if same else s2[:, :3] - xyzmin
+    return x1, x2, lbox
 
 
 def _period(period):
@@ -132,7 +141,7 @@ def _positions(sample1, sample2, period, search, pbc_min_size):
     s2 = s1 if same else _columns(sample2)
     if period is None:
         pbc = 0
-        x1, x2, box = _enclose_in_box(s1, s2, pbc_min_size)
+        x1, x2, box = _enclose_in_box(s1, s2, pbc_min_size, same)
     else:
         pbc = 1
         box = _period(period)
@@ -222,8 +231,8 @@ def npairs_projected(sample1, sample2, rp_bins, pi_max, period=None, num_threads
     msg = "Input ``pi_max`` must be a positive scalar less than period[2]/3"
     if period is None:
         pi_max_f = float(pi_max)
-        x1, _, box = _enclose_in_box(_columns(sample1), _columns(sample2),
-                                     [rpm * 3.0, rpm * 3.0, pi_max_f * 3.0])
+        _, box = _enclosing_box(_columns(sample1), _columns(sample2),
+                                [rpm * 3.0, rpm * 3.0, pi_max_f * 3.0], sample2 is sample1)
     else:
         box = _period(period)
     if not (pi_max > 0.0 and pi_max < box[2] / 3.0):

@@ -181,3 +181,31 @@ def test_batched_weight_columns_message():
     with pytest.raises(ValueError, match="Lbox/3"):
         D.weighted_pair_counts_batched(torch.ones((10, 2), dtype=torch.float64), x, [0.1, 0.5],
                                        1.0)
+
+
+def _enclose_per_column(s1, s2, min_size):
+    # the reference's form (mesh_helpers.py:17-64): six per-column minima and
+    # maxima, both samples shifted in their input dtype
+    x1, x2 = s1[:, :3], s2[:, :3]
+    cols = [x1[:, 0], x2[:, 0], x1[:, 1], x2[:, 1], x1[:, 2], x2[:, 2]]
+    xyzmin = np.min([np.min(c) for c in cols])
+    xyzmax = np.max([np.max(c) for c in cols]) - xyzmin
+    lbox = np.array([xyzmax] * 3)
+    min_size = np.atleast_1d(min_size)
+    lbox[lbox < min_size] = min_size[lbox < min_size]
+    return x1 - xyzmin, x2 - xyzmin, lbox.astype(np.float64)
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+@pytest.mark.parametrize("ncol", [3, 4])
+def test_enclose_in_box_matches_per_column_form(dtype, ncol):
+    from halotools_gb300.pair_counters import _enclose_in_box
+    g = np.random.default_rng(ncol)
+    a = (g.uniform(-40, 60, (500, ncol)) * [1.0, 0.5, 2.0, 1.0][:ncol]).astype(dtype)
+    b = g.uniform(-10, 90, (300, ncol)).astype(dtype)
+    for s1, s2, same in ((a, b, False), (a, a, True), (b, a, False)):
+        for min_size in ([1.0, 1.0, 1.0], [500.0, 1.0, 300.0]):
+            got = _enclose_in_box(s1, s2, min_size, same)
+            want = _enclose_per_column(s1, s2, min_size)
+            for x, y in zip(got, want):
+                assert x.dtype == y.dtype and np.array_equal(x, y)
