@@ -40,24 +40,29 @@ __all__ = ("counts_in_cylinders", "spherical_isolation", "cylindrical_isolation"
 
 
 def _per_point(values, n1, msg):
-    # counts_in_cylinders.py:207-223: a scalar or one value per sample-1 point
+    # counts_in_cylinders.py:207-223: a scalar or one value per sample-1 point;
+    # a scalar is broadcast in one pass (v + 0.0, the bits of zeros(n1) + v)
     v = np.atleast_1d(values).astype("f8")
     if len(v) == 1:
-        return np.zeros(n1) + v[0]
+        return np.full(n1, v[0] + 0.0)
     if len(v) == n1:
         return v
     raise ValueError(msg)
 
 
 def _get_r_max(n1, r_max):
-    # isolation_functions_helpers.py:11-35
+    # isolation_functions_helpers.py:11-35; a scalar is checked once, then
+    # broadcast (with no points every value passes, as the empty array does)
     r = np.atleast_1d(r_max).astype(float)
+    msg = "Input ``r_max`` must be an array of bounded positive numbers."
     if len(r) == 1:
-        r = np.full(n1, r[0])
-    elif len(r) != n1:
+        if n1 > 0 and not (r[0] < np.inf and r[0] > 0):
+            raise ValueError(msg)
+        return np.full(n1, r[0])
+    if len(r) != n1:
         raise ValueError("Input ``r_max`` must be the same length as ``sample1``.")
     if not (np.all(r < np.inf) and np.all(r > 0)):
-        raise ValueError("Input ``r_max`` must be an array of bounded positive numbers.")
+        raise ValueError(msg)
     return r
 
 

@@ -209,3 +209,25 @@ def test_enclose_in_box_matches_per_column_form(dtype, ncol):
             want = _enclose_per_column(s1, s2, min_size)
             for x, y in zip(got, want):
                 assert x.dtype == y.dtype and np.array_equal(x, y)
+
+
+def test_per_point_radii_match_broadcast_forms():
+    from halotools_gb300.neighbours import _get_r_max, _per_point
+    for v in (2.5, -0.0, 0.0, np.nan, np.inf):
+        got = _per_point(v, 7, "m")
+        want = np.zeros(7) + np.atleast_1d(v).astype("f8")[0]
+        assert got.dtype == want.dtype and np.array_equal(got.view(np.int64), want.view(np.int64))
+    arr = np.linspace(1.0, 2.0, 7)
+    assert np.array_equal(_per_point(arr, 7, "m"), arr)
+    with pytest.raises(ValueError, match="m"):
+        _per_point(arr, 6, "m")
+    # isolation_functions_helpers.py:11-35
+    assert np.array_equal(_get_r_max(5, 1.5), np.array([1.5] * 5))
+    for bad in (0.0, -1.0, np.inf, np.nan):
+        with pytest.raises(ValueError, match="bounded positive"):
+            _get_r_max(5, bad)
+        assert len(_get_r_max(0, bad)) == 0
+    with pytest.raises(ValueError, match="same length"):
+        _get_r_max(5, [1.0, 2.0])
+    with pytest.raises(ValueError, match="bounded positive"):
+        _get_r_max(2, [1.0, 0.0])
