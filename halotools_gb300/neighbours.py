@@ -42,7 +42,7 @@ __all__ = ("counts_in_cylinders", "spherical_isolation", "cylindrical_isolation"
 def _per_point(values, n1, msg):
     # counts_in_cylinders.py:207-223: a scalar or one value per sample-1 point;
     # a scalar is broadcast in one pass (v + 0.0, the bits of zeros(n1) + v)
-    v = np.atleast_1d(values).astype("f8")
+    v = np.atleast_1d(values).astype("f8", copy=False)  # read only
     if len(v) == 1:
         return np.full(n1, v[0] + 0.0)
     if len(v) == n1:
@@ -53,7 +53,7 @@ def _per_point(values, n1, msg):
 def _get_r_max(n1, r_max):
     # isolation_functions_helpers.py:11-35; a scalar is checked once, then
     # broadcast (with no points every value passes, as the empty array does)
-    r = np.atleast_1d(r_max).astype(float)
+    r = np.atleast_1d(r_max).astype(float, copy=False)  # read only
     msg = "Input ``r_max`` must be an array of bounded positive numbers."
     if len(r) == 1:
         if n1 > 0 and not (r[0] < np.inf and r[0] > 0):
@@ -221,7 +221,7 @@ def _reshape_input_marks(marks, npts, nm, cond_func):
     # isolation_functions_helpers.py:110-139
     if marks is None:
         return np.ones((npts, nm), dtype=np.float64)
-    marks = np.atleast_1d(marks).astype(np.float64)
+    marks = np.atleast_1d(marks).astype(np.float64, copy=False)  # read only
     if len(marks.shape) == 1:
         marks = np.reshape(marks, (len(marks), 1))
     if marks.shape[0] != npts:

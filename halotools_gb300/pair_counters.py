@@ -304,7 +304,7 @@ def _process_weights(sample1, sample2, weights1, weights2, weight_func_id, known
         if w is None:
             w = np.ones(shape, dtype=np.float64)
         else:
-            w = np.atleast_1d(w).astype("float64")
+            w = np.atleast_1d(w).astype("float64", copy=False)  # read only
             if w.ndim == 1:
                 conv = True
                 w = w.reshape((len(w), 1))
@@ -513,26 +513,38 @@ def _jackknife_inputs(sample1, sample2, jtags1, jtags2, N_samples, weights1, wei
     ws = []
     for w, s, name in ((weights1, s1, "weights1"), (weights2, s2, "weights2")):
         if w is not None:
-            w = np.asarray(w).astype("float64")
+            w = np.asarray(w).astype("float64", copy=False)  # read only
             if np.shape(w)[0] != np.shape(s)[0]:
                 raise HalotoolsError("%s should have same len as %s" % (name, name.replace(
                     "weights", "sample")))
         ws.append(w)
-    t1 = np.asarray(jtags1).astype("int")
-    t2 = np.asarray(jtags2).astype("int")
+    # (read only; one array given for both sides is converted and checked once)
+    t1 = np.asarray(jtags1).astype("int", copy=False)
+    t2 = t1 if jtags2 is jtags1 else np.asarray(jtags2).astype("int", copy=False)
     if np.shape(t1)[0] != np.shape(s1)[0]:
         raise HalotoolsError("jtags1 should have same len as sample1")
     if np.shape(t2)[0] != np.shape(s2)[0]:
         raise HalotoolsError("jtags2 should have same len as sample2")
-    if len(t1) and np.min(t1) < 1:
+    lo1 = np.min(t1) if len(t1) else None
+    hi1 = np.max(t1) if len(t1) else None
+    lo2, hi2 = (lo1, hi1) if t2 is t1 else ((np.min(t2), np.max(t2)) if len(t2) else (None, None))
+    if lo1 is not None and lo1 < 1:
         raise HalotoolsError("jtags1 must be >= 1")
-    if len(t2) and np.min(t2) < 1:
+    if lo2 is not None and lo2 < 1:
         raise HalotoolsError("jtags2 must be >= 1")
-    if len(t1) and np.max(t1) > N_samples:
+    if hi1 is not None and hi1 > N_samples:
         raise HalotoolsError("jtags1 must be <= N_samples")
-    if len(t2) and np.max(t2) > N_samples:
+    if hi2 is not None and hi2 > N_samples:
         raise HalotoolsError("jtags2 must be <= N_samples")
-    if not np.array_equal(np.unique(t1), np.arange(1, N_samples + 1)):
+    # np.unique(t1) == arange(1, N_samples + 1): with the tags checked to lie in
+    # [1, N_samples], every subsample present (a count per tag when N_samples is
+    # a whole number)
+    if float(N_samples).is_integer():
+        present = np.bincount(t1, minlength=int(N_samples) + 1)[1:] > 0
+        every = len(present) == int(N_samples) and bool(np.all(present))
+    else:
+        every = np.array_equal(np.unique(t1), np.arange(1, N_samples + 1))
+    if not every:
         warnings.warn("Warning: sample1 does not contain points in every jackknife sample.")
     w1, w2 = ws
     if (w1 is None or np.all(w1 == 1.0)) and (w2 is None or np.all(w2 == 1.0)):
@@ -547,7 +559,7 @@ def _jackknife_tags(x1, x2, t1, t2, wts=None):
     cross-correlation."""
     j1 = np.ascontiguousarray(t1, dtype=np.int32)
     same_w = wts is None or np.array_equal(wts[0], wts[1])
-    j2 = j1 if (x2 is x1 and np.array_equal(t1, t2) and same_w) else \
+    j2 = j1 if (x2 is x1 and (t2 is t1 or np.array_equal(t1, t2)) and same_w) else \
         np.ascontiguousarray(t2, dtype=np.int32)
     if x2 is x1 and j2 is not j1:
         x2 = x1.copy()

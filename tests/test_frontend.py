@@ -231,3 +231,25 @@ def test_per_point_radii_match_broadcast_forms():
         _get_r_max(5, [1.0, 2.0])
     with pytest.raises(ValueError, match="bounded positive"):
         _get_r_max(2, [1.0, 0.0])
+
+
+def test_jackknife_tag_checks_and_coverage_warning():
+    import warnings as w
+    from halotools_gb300.pair_counters import _jackknife_inputs
+    t = np.arange(50) % 5 + 1  # every subsample 1..5 present
+    with w.catch_warnings():
+        w.simplefilter("error")
+        _jackknife_inputs(S, S, t, t, 5, None, None)
+        _jackknife_inputs(S, S, t.astype(float), t, 5.0, None, None)
+    for tags, n in ((np.minimum(t, 4), 5), (t, 6)):  # subsample 5, or 6, has no point
+        with pytest.warns(UserWarning, match="every jackknife sample"):
+            _jackknife_inputs(S, S, tags, tags, n, None, None)
+    with pytest.warns(UserWarning, match="every jackknife sample"):
+        _jackknife_inputs(S, S, t, t, 5.5, None, None)  # np.unique form for a fractional count
+    # one array for both sides is still checked against each sample
+    with pytest.raises(h.HalotoolsError, match="jtags1 must be >= 1"):
+        _jackknife_inputs(S, S, t - 1, t - 1, 5, None, None)
+    with pytest.raises(h.HalotoolsError, match="jtags2 should have same len as sample2"):
+        _jackknife_inputs(S, S[:40], t, t, 5, None, None)
+    with pytest.raises(h.HalotoolsError, match="jtags2 must be <= N_samples"):
+        _jackknife_inputs(S, S, t, t + 1, 5, None, None)
