@@ -524,8 +524,8 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
     int *uix = (int *)(ux + 3 * GBP_USLOTS);
     float *s_uw = (float *)(smem + L.off_q + GBP_WARPS * GBP_USLOTS * 16) +
                   warp * GBP_USLOTS * (COLS ? ncol : 1);
-    // MARKC, few channels: this warp's binned pairs of one round {bin | multiplicity
-    // << 16, second bin, i, j}
+    // MARKC per-round form (up to 4 or over 16 channels): this warp's binned pairs
+    // of one round {bin | multiplicity << 16, second bin, i, j}
     int4 *s_rec = (int4 *)(smem + L.off_rec) + warp * 32;
     // MARKC sorted, per warp and code batch: each code's bin, the codes sorted by
     // bin, and per bin its count and (after the scatter) its end
