@@ -41,12 +41,13 @@ __all__ = ("counts_in_cylinders", "spherical_isolation", "cylindrical_isolation"
 
 def _per_point(values, n1, msg):
     # counts_in_cylinders.py:207-223: a scalar or one value per sample-1 point;
-    # a scalar is broadcast in one pass (v + 0.0, the bits of zeros(n1) + v)
+    # a scalar is broadcast in one pass (v + 0.0, the bits of zeros(n1) + v).
+    # Returns the per-point array and its maximum (0.0 with no points).
     v = np.atleast_1d(values).astype("f8", copy=False)  # read only
     if len(v) == 1:
-        return np.full(n1, v[0] + 0.0)
+        return np.full(n1, v[0] + 0.0), (v[0] + 0.0 if n1 else 0.0)
     if len(v) == n1:
-        return v
+        return v, (np.max(v) if n1 else 0.0)
     raise ValueError(msg)
 
 
@@ -107,12 +108,10 @@ def counts_in_cylinders(sample1, sample2, proj_search_radius, cylinder_half_leng
     if return_indexes and (len(s1) > 2 ** 32 or len(s2) > 2 ** 32):
         raise ValueError("Return indexes uses a uint32 and so can only handle inputs shorter "
                          "than 2^32 (~4 Billion).")
-    rp = _per_point(proj_search_radius, n1,
-                    "Input ``proj_search_radius`` must be a scalar or length-Npts1 array")
-    pi = _per_point(cylinder_half_length, n1,
-                    "Input ``cylinder_half_length`` must be a scalar or length-Npts1 array")
-    rpm = np.max(rp) if n1 else 0.0
-    pim = np.max(pi) if n1 else 0.0
+    rp, rpm = _per_point(proj_search_radius, n1,
+                         "Input ``proj_search_radius`` must be a scalar or length-Npts1 array")
+    pi, pim = _per_point(cylinder_half_length, n1,
+                         "Input ``cylinder_half_length`` must be a scalar or length-Npts1 array")
     _approx_cells(approx_cell1_size, [rpm, rpm, pim], "approx_cell1_size")
     _approx_cells(approx_cell2_size, [rpm, rpm, pim], "approx_cell2_size")
     # conditions.pyx choose_condition

@@ -214,11 +214,14 @@ def test_enclose_in_box_matches_per_column_form(dtype, ncol):
 def test_per_point_radii_match_broadcast_forms():
     from halotools_gb300.neighbours import _get_r_max, _per_point
     for v in (2.5, -0.0, 0.0, np.nan, np.inf):
-        got = _per_point(v, 7, "m")
+        got, gmax = _per_point(v, 7, "m")
         want = np.zeros(7) + np.atleast_1d(v).astype("f8")[0]
         assert got.dtype == want.dtype and np.array_equal(got.view(np.int64), want.view(np.int64))
+        assert np.array_equal(np.float64(gmax).view(np.int64), np.max(want).view(np.int64))
+        assert _per_point(v, 0, "m")[1] == 0.0
     arr = np.linspace(1.0, 2.0, 7)
-    assert np.array_equal(_per_point(arr, 7, "m"), arr)
+    got, gmax = _per_point(arr, 7, "m")
+    assert np.array_equal(got, arr) and gmax == 2.0
     with pytest.raises(ValueError, match="m"):
         _per_point(arr, 6, "m")
     # isolation_functions_helpers.py:11-35
