@@ -540,7 +540,7 @@ def _jackknife_inputs(sample1, sample2, jtags1, jtags2, N_samples, weights1, wei
     # [1, N_samples], every subsample present (a count per tag when N_samples is
     # a whole number)
     if float(N_samples).is_integer():
-        present = np.bincount(t1, minlength=int(N_samples) + 1)[1:] > 0
+        present = np.bincount(np.ravel(t1), minlength=int(N_samples) + 1)[1:] > 0
         every = len(present) == int(N_samples) and bool(np.all(present))
     else:
         every = np.array_equal(np.unique(t1), np.arange(1, N_samples + 1))

@@ -244,6 +244,7 @@ def test_jackknife_tag_checks_and_coverage_warning():
         w.simplefilter("error")
         _jackknife_inputs(S, S, t, t, 5, None, None)
         _jackknife_inputs(S, S, t.astype(float), t, 5.0, None, None)
+        _jackknife_inputs(S, S, t[:, None], t[:, None], 5, None, None)  # (N, 1) tags
     for tags, n in ((np.minimum(t, 4), 5), (t, 6)):  # subsample 5, or 6, has no point
         with pytest.warns(UserWarning, match="every jackknife sample"):
             _jackknife_inputs(S, S, tags, tags, n, None, None)
