@@ -34,7 +34,7 @@ EXPORTED = (
     "gbp_isolation", "gbp_hod_mocks", "gbp_npairs_jackknife_3d_weighted",
     "gbp_npairs_jackknife_xy_z_weighted", "gbp_weighted_adjoint_3d_channels",
     "gbp_zheng07_weights_batched", "gbp_zheng07_vjp_batched",
-    "gbp_weighted_adjoint_3d", "gbp_zheng07_weights", "gbp_zheng07_vjp",
+    "gbp_weighted_adjoint_3d", "gbp_zheng07_weights", "gbp_zheng07_vjp", "gbp_plan_set_limits",
 )
 
 
@@ -166,6 +166,7 @@ def load(build_if_missing: bool = True):
         L.gbp_zheng07_vjp.argtypes = [vp, vp, i64, pd, vp, i32, pd]
         L.gbp_plan_set_autotune.argtypes = [vp, ctypes.c_int]
         L.gbp_plan_set_block.argtypes = [vp, ctypes.c_int]
+        L.gbp_plan_set_limits.argtypes = [vp, i64, i64]
         _lib = L
         return L
 
@@ -226,6 +227,12 @@ class Plan:
 
     def set_reach(self, reach: int):
         self.check(self.lib.gbp_plan_set_reach(self.handle, int(reach)))
+
+    def set_limits(self, first_item_cap: int = 0, flush_after: int = 0):
+        """Small capacities that make a small call take the item-overflow retry
+        and the early histogram flush (0 = the defaults)."""
+        self.check(self.lib.gbp_plan_set_limits(self.handle, int(first_item_cap),
+                                                int(flush_after)))
 
     def set_block(self, block: int):
         """Fine cells per block edge of the two-level grid (1..4); 0 = automatic."""

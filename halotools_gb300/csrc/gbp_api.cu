@@ -43,6 +43,8 @@ struct gbp_plan {
     bool graph_mode = false;          // capture each call into a CUDA graph and replay it
     bool autotune = false;            // time the feasible reaches on a new workload shape
     size_t item_cap = 0;              // work-item capacity learned from an overflow
+    size_t first_item_cap = 0;        // gbp_plan_set_limits: room for the next call's items
+    unsigned long long flush_after = 1ull << 24;  // gbp_plan_set_limits: early histogram flush
     std::vector<std::pair<std::string, int>> tuned;  // workload signature -> best reach
     cudaGraphExec_t gexec = nullptr;  // reused (updated in place) across calls
     gbp_stats stats;
@@ -238,6 +240,10 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
         plan->item_cap,
         2 * ((size_t)nkeys + (size_t)(c.n1 / GBP_TI)) +
             (size_t)nsten * (size_t)(c.n2 / GBP_JCAP_ITEM) + 65536);
+    if (plan->first_item_cap) {
+        max_items = plan->first_item_cap;  // once: an overflow sets item_cap for the retry
+        plan->first_item_cap = 0;
+    }
     size_t o_items = cv.take<int4>(max_items);
     size_t o_itmp = cv.take<int>(2 * ((size_t)nkeys + 2));
     size_t o_offs = cv.take<int64_t>((size_t)nm + 1);
@@ -436,6 +442,7 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
         a.items = at<int4>(W, o_items);
         a.nitems = d_nitems;
         a.counter = d_counter;
+        a.flush_after = plan->flush_after;
         a.sten = at<int>(W, o_sten);
         a.stenD = at<float4>(W, o_stenD);
         a.nsten = nsten;
@@ -747,6 +754,15 @@ int gbp_plan_set_graph(gbp_plan *plan, int enable) {
 int gbp_plan_set_autotune(gbp_plan *plan, int enable) {
     if (!plan) return GBP_ERR_INVALID;
     plan->autotune = enable != 0;
+    return GBP_OK;
+}
+
+int gbp_plan_set_limits(gbp_plan *plan, int64_t first_item_cap, int64_t flush_after) {
+    if (!plan || first_item_cap < 0 || first_item_cap > INT32_MAX / 2 || flush_after < 0)
+        return GBP_ERR_INVALID;
+    plan->first_item_cap = (size_t)first_item_cap;
+    plan->item_cap = 0;
+    plan->flush_after = flush_after ? (unsigned long long)flush_after : (1ull << 24);
     return GBP_OK;
 }
 

@@ -1338,7 +1338,7 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
         }
         // a lane adds at most 2 per pair of its own and a warp copy at most 64
         // per lane: flush long before a u32 could wrap
-        if (!MARK && !MARKC && drained > (1ull << 24)) warp_flush(cur_mock);
+        if (!MARK && !MARKC && drained > a.flush_after) warp_flush(cur_mock);
     }
     if (cur_mock >= 0) warp_flush(cur_mock);
     if (lane == 0 && cand) atomicAdd(a.nrecheck + 1, cand);

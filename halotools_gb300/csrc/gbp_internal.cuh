@@ -85,6 +85,7 @@ struct CountArgs {
     const int4 *items;
     const int *nitems;      // device scalar (written by the item builder)
     int *counter;           // work-item cursor, zero before launch
+    unsigned long long flush_after;  // early flush of the u32 histogram words (j-batches x 64)
     const int *sten;        // runs: block offset (ox+64) | (oy+64)<<8 | (oz+64)<<16 | first cell<<24
     const float4 *stenD;    // FP32 block offsets o*bf*c and (bits of) the run length
     int nsten;

@@ -20,8 +20,13 @@
 // work cursor, error word) on its own stream.  Calls whose work overlaps on the
 // GPU (different streams, or different host threads on one device) race on the
 // array and give wrong counts: serialise them.
+//
+// Each call copies its bin and stencil tables from host stack memory into the
+// array; a stream that is being captured would record copies from memory that
+// no longer exists when the graph replays, so such a stream is refused.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstring>
 
 #include "../../include/gbpairs.h"
@@ -69,25 +74,31 @@ static __device__ __align__(256) unsigned char g_gbp_scratch[GBP_STATIC_SCRATCH_
 namespace {
 
 const int MAX_DEVICES = 64;
-unsigned char *g_scratch_ptr[MAX_DEVICES];  // device address per device, set once
+// device address per device, looked up once (first calls from several host
+// threads may each look it up; they store the same value)
+std::atomic<unsigned char *> g_scratch_ptr[MAX_DEVICES];
 
 // Once per device, with that device current: look up the array's address.
+// It stays valid for the life of the device's primary context; calls after a
+// cudaDeviceReset are not supported.
 cudaError_t scratch_for_device(int dev, unsigned char **out) {
     if (dev < 0 || dev >= MAX_DEVICES) return cudaErrorInvalidDevice;
-    if (!g_scratch_ptr[dev]) {
-        void *p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_gbp_scratch);
+    unsigned char *p = g_scratch_ptr[dev].load(std::memory_order_acquire);
+    if (!p) {
+        void *q = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&q, g_gbp_scratch);
         if (e != cudaSuccess) return e;
-        g_scratch_ptr[dev] = static_cast<unsigned char *>(p);
+        p = static_cast<unsigned char *>(q);
+        g_scratch_ptr[dev].store(p, std::memory_order_release);
     }
-    *out = g_scratch_ptr[dev];
+    *out = p;
     return cudaSuccess;
 }
 
 // Cumulative counts from the differential histogram, plus the n self-pairs
 // (separation exactly 0) in bin `self_bin`; every count is -1 if the
-// digitiser flagged a position outside the box or the work items overflowed
-// the scratch (an input far denser than the point limit suggests).
+// digitiser flagged a position outside the box or not finite (misc word 2),
+// or the work items overflowed their part of the scratch (misc word 3).
 __global__ void k_static_finalize(const unsigned long long *hist, const unsigned long long *misc,
                                   int nb, int self_bin, long long nself, long long *counts) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
@@ -117,6 +128,9 @@ extern "C" int gbp_npairs_3d_static(const double *xyz, int64_t n, const double *
         if (!(search[d] > 0)) return GBP_ERR_INVALID;
     }
     cudaStream_t st = static_cast<cudaStream_t>(stream);
+    cudaStreamCaptureStatus cap_status = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cap_status) != cudaSuccess) return GBP_ERR_CUDA;
+    if (cap_status != cudaStreamCaptureStatusNone) return GBP_ERR_INVALID;
     int dev = 0, nsm = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return GBP_ERR_CUDA;
     unsigned char *W = nullptr;
@@ -224,14 +238,14 @@ extern "C" int gbp_npairs_3d_static(const double *xyz, int64_t n, const double *
     ad.vlo = li.vlo;
     ad.vhi = li.vhi;
     a.hist_stride = nbins + 1;
-    a.hist_copies = GBP_WARPS;
+    a.hist_copies = GBP_WARPS;  // as gbp_npairs_3d; MODE_3D keeps lane-private counts
     a.ncells_mock = (int)g.nblocks;
-    a.hist_copies = 1;
+    a.flush_after = 1ull << 24;
     a.hist = reinterpret_cast<unsigned long long *>(W + O_HIST);
     a.nrecheck = misc + 2;
     a.top0 = std::min(hi[nbins - 1], 1.0e30f);
     a.self_bin = self_bin;
-    SmemLayout L = gbp_smem_layout(MODE_3D, li.T, 0, nbins, 0, g.nsten, GBP_WARPS, 0);
+    SmemLayout L = gbp_smem_layout(MODE_3D, li.T, 0, nbins, 0, g.nsten, a.hist_copies, 0);
     size_t smem = (size_t)L.total;
     int occ = gbp_count_occupancy(MODE_3D, 1, smem);
     if (occ <= 0) return GBP_ERR_INVALID;

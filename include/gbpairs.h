@@ -75,6 +75,15 @@ int gbp_plan_set_graph(gbp_plan *plan, int enable);
 /* 1: on the first call of a new workload shape, time every feasible reach and
  * keep the fastest for later calls of that shape; 0: density heuristic. */
 int gbp_plan_set_autotune(gbp_plan *plan, int enable);
+/* Capacity limits, for exercising rare paths on small inputs (no reference
+ * counterpart).  first_item_cap > 0: the next call starts with room for that
+ * many work items, so a denser workload overflows it and the call repeats with
+ * room for its estimate (the path a large clustered sample takes); 0 = the
+ * estimate.  flush_after > 0: a warp of the count kernel moves its 32-bit
+ * histogram words to the 64-bit totals at the end of the first work item
+ * after it has binned more than flush_after / 64 j-batches since its last
+ * move (default 2^24, long before a word could wrap); 0 = default. */
+int gbp_plan_set_limits(gbp_plan *plan, int64_t first_item_cap, int64_t flush_after);
 const char *gbp_plan_last_error(const gbp_plan *plan);
 int gbp_plan_stats(const gbp_plan *plan, gbp_stats *stats);
 
@@ -377,15 +386,26 @@ int gbp_zheng07_vjp(gbp_plan *plan, const double *mass, int64_t n, const double 
  * device array of GBP_STATIC_SCRATCH_BYTES that each GPU loading this
  * library holds until exit; the call allocates nothing, device or host.
  *   xyz     device pointer, (n, 3) row-major float64, 1 <= n <= GBP_STATIC_MAX_POINTS
- *   rbins   host array of 2..64 edges; period3 host array; pbc 0 or 1
+ *   rbins   host array of 2..64 edges; period3 host array
+ *   pbc     1: periodic box of sides period3; 0: no wrap, the points lie in
+ *           the box [0, period3] (not shifted by their minimum as the
+ *           period=None front-ends do); either way the largest edge must be
+ *           at most period3 / 3
  *   counts  device pointer to n_bins int64, written by the last kernel of the
- *           call (all -1 if a position lies outside [0, period] or is not
- *           finite)
+ *           call.  All counts are -1 (the call still returns GBP_OK, since
+ *           it does not wait for its kernels) when a position lies outside
+ *           [0, period3] or is not finite, or when the input needs more work
+ *           items than the array holds (a sample far more clustered than
+ *           GBP_STATIC_MAX_POINTS points spread over GBP_STATIC_MAX_CELLS
+ *           cells can produce)
  *   stream  cudaStream_t (NULL = legacy default stream); the call does not
  *           synchronise it
- * Larger inputs return GBP_ERR_INVALID.  The first call on a device looks up
- * the array's device address (cudaGetSymbolAddress) with that device
- * current; make that first call before any stream capture.  All calls share
+ * Larger inputs return GBP_ERR_INVALID, and so does a stream that is being
+ * captured (each call copies its bin tables from host memory).  The first
+ * call on a device looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current; make that first call
+ * before any stream capture.  The address is kept for the life of the
+ * process: calls after a cudaDeviceReset are not supported.  All calls share
  * the array: calls that overlap on the GPU race and must be serialised.
  */
 #define GBP_STATIC_MAX_POINTS 131072

@@ -6,9 +6,15 @@ compiled file under ``oracle/_ref/`` (git-ignored).  The reference flags are
 kept: ``language="c++"`` and ``-Ofast`` (halotools
 ``mock_observables/pair_counters/cpairs/setup_package.py:22-27``).
 
-Cython is needed, so this runs only where Cython is installed; machines
-without it (or without the halotools tree) skip it and the repository's own
-C restatement of the engines (``oracle/pairs_oracle.c``) is used instead.
+Generating the C++ needs Cython and the halotools tree.  Compiling the
+generated C++ needs neither: ``build_generated`` compiles whatever
+``oracle/_ref`` already holds for the running platform (g++, the Python and
+numpy headers), which is how the engines are built on a machine that has the
+generated files but no halotools checkout.  Where neither works, the
+repository's own C restatement (``oracle/pairs_oracle.c``) stands in.
+
+The halotools checkout is read from ``$HALOTOOLS_SRC``, else from
+``DEFAULT_SRC``.
 
 Usage::
 
@@ -25,7 +31,7 @@ from concurrent.futures import ThreadPoolExecutor
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
-DEFAULT_SRC = "/root/reference"
+DEFAULT_SRC = os.environ.get("HALOTOOLS_SRC", "/root/reference")
 
 PC = os.path.join("halotools", "mock_observables", "pair_counters")
 CIC = os.path.join("halotools", "mock_observables", "counts_in_cells")
@@ -55,9 +61,19 @@ ENGINES = [
 ]
 
 
-def _build_one(src_root: str, subdir: str, name: str) -> str:
+def _compile(cpp: str, so: str) -> str:
+    """g++ with the reference flags (-Ofast, C++), into a temporary name first."""
     import numpy as np
 
+    inc = sysconfig.get_paths()["include"]
+    tmp = so + ".tmp%d" % os.getpid()
+    subprocess.run(["g++", "-Ofast", "-shared", "-fPIC", "-I", inc, "-I", np.get_include(),
+                    cpp, "-o", tmp], check=True, capture_output=True)
+    os.replace(tmp, so)
+    return so
+
+
+def _build_one(src_root: str, subdir: str, name: str) -> str:
     pyx = os.path.join(src_root, subdir, name + ".pyx")
     outdir = os.path.join(OUT, subdir)
     os.makedirs(outdir, exist_ok=True)
@@ -68,10 +84,35 @@ def _build_one(src_root: str, subdir: str, name: str) -> str:
         return so
     subprocess.run([sys.executable, "-m", "cython", "--cplus", "-o", cpp, pyx],
                    check=True, capture_output=True)
-    inc = sysconfig.get_paths()["include"]
-    subprocess.run(["g++", "-Ofast", "-shared", "-fPIC", "-I", inc, "-I", np.get_include(),
-                    cpp, "-o", so], check=True, capture_output=True)
-    return so
+    return _compile(cpp, so)
+
+
+# the engines the CPU reference of the benchmark runs (oracle/ref_driver.py)
+DRIVER_ENGINES = ("npairs_3d_engine", "npairs_xy_z_engine")
+
+
+def build_generated(names=DRIVER_ENGINES) -> bool:
+    """Compile the already generated C++ of the ``cpairs`` engines ``names`` for
+    this platform where no up-to-date module exists; True when all are there."""
+    outdir = os.path.join(OUT, PC, "cpairs")
+    ext = sysconfig.get_config_var("EXT_SUFFIX")
+    todo = []
+    for name in names:
+        cpp = os.path.join(outdir, name + ".cpp")
+        so = os.path.join(outdir, name + ext)
+        if os.path.exists(so) and (not os.path.exists(cpp) or
+                                   os.path.getmtime(so) >= os.path.getmtime(cpp)):
+            continue
+        if not os.path.exists(cpp):
+            return False
+        todo.append((cpp, so))
+    if todo:
+        try:
+            with ThreadPoolExecutor(max_workers=len(todo)) as ex:
+                list(ex.map(lambda t: _compile(*t), todo))
+        except (subprocess.CalledProcessError, OSError):
+            return False
+    return True
 
 
 def build(src_root: str = DEFAULT_SRC) -> bool:

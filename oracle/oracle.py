@@ -56,6 +56,7 @@ def lib():
                                      pd, i, pd, pd, i, pi64]
         L.orc_bf_npairs_3d.argtypes = [pd, i64, pd, i64, pd, i, pd, i, pi64]
         L.orc_weighted_adjoint_3d.argtypes = [pd, i64, pd, pd, i, pd, i, pd, i, pd]
+        L.orc_weighted_per_object_3d.argtypes = [pd, i64, pd, i64, pd, pd, i, pd, i, i, pd]
         _lib = L
     return _lib
 
@@ -376,4 +377,18 @@ def weighted_adjoint_3d(xyz, w, rbins, period, gbar, num_threads=8):
     out = np.zeros(len(xyz), dtype=np.float64)
     _check(lib().orc_weighted_adjoint_3d(_p(xyz), len(xyz), _p(w), _p(rbins), len(rbins), _p(box),
                                          1, _p(gbar), int(num_threads), _p(out)))
+    return out
+
+
+def weighted_per_object_3d(xyz, w, rbins, period, num_threads=8):
+    """FP64 (N, nb) table S[m, k] = sum_j w_j [d_mj <= r_k] over the cell walk
+    (j = m included), auto-correlation of ``xyz`` in a periodic box.  From it:
+    C_k = sum_m w_m S[m, k], dL/dw_m = 2 sum_k gbar_k S[m, k] and
+    dC_k/dtheta = 2 sum_m S[m, k] dw_m/dtheta."""
+    rbins = np.ascontiguousarray(np.atleast_1d(rbins), dtype=np.float64)
+    x, _, lbox, pbc = _geometry(xyz, xyz, [np.max(rbins)] * 3, period)
+    w = np.ascontiguousarray(w, dtype=np.float64)
+    out = np.zeros((len(x), len(rbins)), dtype=np.float64)
+    _check(lib().orc_weighted_per_object_3d(_p(x), len(x), _p(x), len(x), _p(w), _p(rbins),
+                                            len(rbins), _p(lbox), pbc, int(num_threads), _p(out)))
     return out

@@ -129,7 +129,7 @@ static void mesh_free(mesh_t *m) {
 }
 
 enum { K_3D = 0, K_XYZ = 1, K_SMU = 2, K_MARKED = 3, K_XYZ_MARKED = 4, K_SMU_WEIGHTED = 5,
-       K_XYZ_JACK = 6, K_NEIGH = 7, K_3D_JACK = 8 };
+       K_XYZ_JACK = 6, K_NEIGH = 7, K_3D_JACK = 8, K_WPOBJ = 9 };
 
 typedef struct {
     int kind;
@@ -347,6 +347,20 @@ static void walk_range(const walk_t *w, int64_t c0, int64_t c1, int64_t *ic, dou
                                         if (k < 0) break;
                                     }
                                 }
+                            } else if (w->kind == K_WPOBJ) {
+                                /* per-point FP64 sums of the neighbours' weights by
+                                   cumulative bin (no reference counterpart; the bin
+                                   walk of npairs_3d_engine.pyx:173-182).  Rows are
+                                   sorted sample-1 points: each thread owns its cells'
+                                   rows of the one shared table. */
+                                double dsq = dx * dx + dy * dy + dz * dz;
+                                double *row = dc + i * (int64_t)w->n1e;
+                                int k = w->n1e - 1;
+                                while (dsq <= w->e1[k]) {
+                                    row[k] += w->w2[j];
+                                    k--;
+                                    if (k < 0) break;
+                                }
                             } else if (w->kind == K_NEIGH) {
                                 /* counts_in_cylinders_engine.pyx:262-281,
                                    spherical_isolation_engine.pyx:190-199,
@@ -464,7 +478,7 @@ static int run_walk(int kind, const double *xyz1, int64_t n1, const double *xyz2
         w.nsamp = nsamp;
     }
     if (kind == K_MARKED || kind == K_XYZ_MARKED || kind == K_SMU_WEIGHTED || kind == K_XYZ_JACK ||
-        kind == K_NEIGH || kind == K_3D_JACK) {
+        kind == K_NEIGH || kind == K_3D_JACK || kind == K_WPOBJ) {
         wb = (double *)malloc(sizeof(double) * (size_t)nw * (s1 + s2));
         if (!wb) { free(buf); mesh_free(&w.m1); mesh_free(&w.m2); return -1; }
         w.w1 = wb; w.w2 = wb + (size_t)nw * s1;
@@ -482,6 +496,12 @@ static int run_walk(int kind, const double *xyz1, int64_t n1, const double *xyz2
     if (kind == K_XYZ_JACK) nout *= (int64_t)(nsamp + 1);
     if (kind == K_3D_JACK) nout = (int64_t)n1e * (nsamp + 1);
     if (kind == K_NEIGH) nout = n1 > 0 ? n1 : 1;  /* one count per sorted sample-1 point */
+    double *wshared = NULL;  /* K_WPOBJ: one (n1, n1e) table of sorted rows, shared */
+    if (kind == K_WPOBJ) {
+        nout = 1;
+        wshared = (double *)calloc(s1 * (size_t)n1e, sizeof(double));
+        if (!wshared) { free(buf); free(wb); mesh_free(&w.m1); mesh_free(&w.m2); return -1; }
+    }
     double *dsum = NULL;
     if (nthreads < 1) nthreads = 1;
     if (nthreads > w.m1.ncells) nthreads = (int)w.m1.ncells;
@@ -500,7 +520,7 @@ static int run_walk(int kind, const double *xyz1, int64_t n1, const double *xyz2
             jobs[t].c0 = c;
             jobs[t].c1 = c + len;
             jobs[t].icounts = ipart + (size_t)t * nout;
-            jobs[t].dcounts = dpart + (size_t)t * nout;
+            jobs[t].dcounts = wshared ? wshared : dpart + (size_t)t * nout;
             c += len;
         }
     }
@@ -524,6 +544,12 @@ static int run_walk(int kind, const double *xyz1, int64_t n1, const double *xyz2
         }
         if (icounts) icounts[k] = si;
         if (dcounts) dcounts[k] = sd;
+    }
+    if (kind == K_WPOBJ) {
+        /* sorted rows -> the caller's order */
+        for (int64_t k = 0; k < n1; k++)
+            memcpy(dcounts + w.m1.order[k] * (int64_t)n1e, wshared + k * (int64_t)n1e,
+                   sizeof(double) * (size_t)n1e);
     }
     if (kind == K_NEIGH && icounts) {
         /* per sorted point -> caller's order */
@@ -559,7 +585,7 @@ static int run_walk(int kind, const double *xyz1, int64_t n1, const double *xyz2
             }
     }
 done:
-    free(jobs); free(th); free(ipart); free(dpart); free(dsum);
+    free(jobs); free(th); free(ipart); free(dpart); free(dsum); free(wshared);
     free(wb); free(tb); free(buf);
     mesh_free(&w.m1); mesh_free(&w.m2);
     return rc;
@@ -633,6 +659,28 @@ int orc_marked_npairs_3d(const double *xyz1, int64_t n1, const double *xyz2, int
     double search[3] = {rmax, rmax, rmax};
     int rc = run_walk(K_MARKED, xyz1, n1, xyz2, n2, w1, w2, nw, wfunc, NULL, NULL, 0, e, nb, NULL, 0, 0, 0,
                       period, pbc, search, approx1, approx2, nthreads, NULL, out, NULL);
+    free(e);
+    return rc;
+}
+
+/*
+ * FP64 per-point neighbour weight sums, the oracle of the adjoint at full size
+ * (halotools has no gradients): out[m][k] = sum over j of w2[j] for the
+ * ordered pairs (m, j) with dsq <= rbins[k]^2, j = m included when the samples
+ * are the same.  With sample 2 = sample 1 and weights w, C_k = sum_m w_m
+ * out[m][k], dL/dw_m = 2 sum_k gbar_k out[m][k] and dC_k/dtheta =
+ * 2 sum_m out[m][k] dw_m/dtheta.  out is (n1, nb), the caller's row order.
+ */
+int orc_weighted_per_object_3d(const double *xyz1, int64_t n1, const double *xyz2, int64_t n2,
+                               const double *w2, const double *rbins, int nb,
+                               const double period[3], int pbc, int nthreads, double *out) {
+    double *e = (double *)malloc(sizeof(double) * (size_t)nb);
+    if (!e) return -1;
+    double rmax = rbins[0];
+    for (int k = 0; k < nb; k++) { e[k] = rbins[k] * rbins[k]; if (rbins[k] > rmax) rmax = rbins[k]; }
+    double search[3] = {rmax, rmax, rmax};
+    int rc = run_walk(K_WPOBJ, xyz1, n1, xyz2, n2, w2, w2, 1, 1, NULL, NULL, 0, e, nb, NULL, 0, 0, 0,
+                      period, pbc, search, search, search, nthreads, NULL, out, NULL);
     free(e);
     return rc;
 }

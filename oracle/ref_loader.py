@@ -20,7 +20,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_ref")
-DEFAULT_SRC = "/root/reference"
+from oracle.build_ref import DEFAULT_SRC  # noqa: E402  (the one place the checkout path is set)
 
 
 class NumpyRNGContext:

@@ -25,6 +25,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "estimators")
 sys.path.insert(0, os.path.abspath(os.path.join(HERE, "..", "..")))
+from oracle import build_ref  # noqa: E402
 warnings.filterwarnings("ignore")
 
 L = 100.0
@@ -155,7 +156,7 @@ def load_reference(src):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--src", default="/root/reference")
+    ap.add_argument("--src", default=build_ref.DEFAULT_SRC)
     args = ap.parse_args()
     mods = load_reference(args.src)
     sha = input_sha()

@@ -26,6 +26,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.abspath(os.path.join(HERE, "..", "..")))
+from oracle import build_ref  # noqa: E402
 
 warnings.filterwarnings("ignore", category=SyntaxWarning)
 
@@ -241,5 +242,5 @@ def main(src):
 
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
-    ap.add_argument("--src", default="/root/reference")
+    ap.add_argument("--src", default=build_ref.DEFAULT_SRC)
     main(ap.parse_args().src)

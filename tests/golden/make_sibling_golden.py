@@ -24,6 +24,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "siblings")
 sys.path.insert(0, os.path.abspath(os.path.join(HERE, "..", "..")))
+from oracle import build_ref  # noqa: E402
 warnings.filterwarnings("ignore")
 
 L = 120.0
@@ -204,7 +205,7 @@ def run_case(mod, name):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--src", default="/root/reference")
+    ap.add_argument("--src", default=build_ref.DEFAULT_SRC)
     args = ap.parse_args()
     from oracle import ref_loader
     ns = ref_loader.load(args.src)
