@@ -75,19 +75,35 @@ _BINDINGS = tuple([
 ])
 
 
-def install_into_halotools():
+def install_into_halotools(strict=True):
     """Point halotools' estimators at the GB300 counters; returns the rebound names.
 
-    Modules that are not importable (halotools absent) are skipped.
+    Without halotools (``import halotools`` fails) nothing is rebound and the
+    list is empty.  With halotools importable, every module of the binding
+    table is imported and its name rebound; a module that fails to import is
+    reported: ``strict=True`` raises ImportError naming each such module and
+    its error (after rebinding the others), ``strict=False`` warns instead.
     """
     import importlib
-    done = []
+    import warnings
+    try:
+        importlib.import_module("halotools")
+    except ImportError:
+        return []
+    done, failed = [], {}
     for mod_name, attr, fn in _BINDINGS:
         try:
             mod = importlib.import_module(mod_name)
-        except Exception:
+        except Exception as exc:  # reported below, never dropped
+            failed.setdefault(mod_name, "%s: %s" % (type(exc).__name__, exc))
             continue
         if hasattr(mod, attr):
             setattr(mod, attr, fn)
             done.append("%s.%s" % (mod_name, attr))
+    if failed:
+        msg = ("halotools is importable, but these modules failed to import and keep their "
+               "CPU counters: " + "; ".join("%s (%s)" % kv for kv in sorted(failed.items())))
+        if strict:
+            raise ImportError(msg)
+        warnings.warn(msg)
     return done

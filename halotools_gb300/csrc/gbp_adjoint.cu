@@ -259,6 +259,9 @@ __device__ __noinline__ int2 slow_adj_bins(float v, int b0, int is, int js, cons
 // channels into a run of at most 8 pairs; each run is then one packed
 // compensated (Kahan) add.  Error bound per point and item for same-sign terms:
 // 7u per run plus about 2u for the compensated sum of the runs.
+// GBP_ADJC_BATCHES j batches are staged before the walk, and a lane walks the
+// in-range pairs of all of them in one loop: its trip count is then its total
+// over the batches, which varies far less between lanes than one batch's.
 template <int NCH>
 __global__ void __launch_bounds__(GBP_BLOCK, 2) k_gather_ch(const CountArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -268,10 +271,12 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_gather_ch(const CountArgs a) {
     const SmemLayout L = gbp_smem_layout(MODE_ADJC, T0, 0, nb0, 0, a.nsten, 0, 4 * NCH);
     if (gbp_smem_too_small(L.total, a.err)) return;
     float4 *s_lut0 = (float4 *)(smem + L.off_lut0);
-    float4 *jb = (float4 *)(smem + L.off_j) + warp * 32;
+    constexpr int NB = GBP_ADJC_BATCHES;
+    static_assert(NB == 4, "the walk keeps the slots' masks in two 64-bit words");
+    float4 *jb = (float4 *)(smem + L.off_j) + warp * 32 * NB;
     ulonglong2 *jxy = (ulonglong2 *)(smem + L.off_j2) + warp * 32;
     unsigned long long *jzz = (unsigned long long *)(smem + L.off_j2 + GBP_JCAP * 16) + warp * 32;
-    float *jw = (float *)(smem + L.off_jw) + warp * 32 * NCH;
+    float *jw = (float *)(smem + L.off_jw) + warp * 32 * NB * NCH;
     float4 *s_D = (float4 *)(smem + L.off_D);
     double *s_E0 = (double *)(smem + L.off_E0);
     float *s_hi0 = (float *)(smem + L.off_hi0);
@@ -320,17 +325,21 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_gather_ch(const CountArgs a) {
         unsigned long long acc0[NH], ncm0[NH], acc1[NH], ncm1[NH];
 #pragma unroll
         for (int q = 0; q < NH; q++) acc0[q] = ncm0[q] = acc1[q] = ncm1[q] = 0ull;
-        // the in-range pairs of one point in m, highest slot first: runs of up to 8
+        // the in-range pairs of one point over the staged slots (ma: slots 0-63,
+        // mb: slots 64-127), highest slot of each word first: runs of up to 8
         // products summed by packed FMA, each run then one compensated add
-        auto gather = [&](unsigned m, const float4 &u, unsigned long long *acc,
-                          unsigned long long *ncm) {
+        auto gather = [&](unsigned long long ma, unsigned long long mb, const float4 &u,
+                          unsigned long long *acc, unsigned long long *ncm) {
             unsigned long long run[NH];
 #pragma unroll
             for (int q = 0; q < NH; q++) run[q] = 0ull;
             int nr = 0;
-            while (m) {
-                const int jj = 31 - __clz(m);
-                m ^= 1u << jj;
+            while (ma | mb) {
+                const bool first = ma != 0ull;
+                const int bit = 63 - __clzll(first ? ma : mb);
+                if (first) ma ^= 1ull << bit;
+                else mb ^= 1ull << bit;
+                const int jj = bit + (first ? 0 : 64);
                 const float4 t = jb[jj];
                 const float dx = u.x - t.x, dy = u.y - t.y, dz = u.z - t.z;
                 const float v = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
@@ -401,7 +410,13 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_gather_ch(const CountArgs a) {
             }
             const int T = __shfl_sync(FULL, incl, 31);
             cand += (unsigned long long)icnt * (unsigned long long)T;
-            for (int f0 = 0; f0 < T; f0 += 32) {
+            for (int f00 = 0; f00 < T; f00 += 32 * NB) {
+                // masks of the NB batches' slots: bits 0-63 in *a, 64-127 in *b
+                unsigned long long m0a = 0ull, m0b = 0ull, m1a = 0ull, m1b = 0ull;
+#pragma unroll
+                for (int bt = 0; bt < NB; bt++) {
+                const int f0 = f00 + 32 * bt;
+                if (f0 >= T) break;  // warp-uniform
                 const int f = f0 + lane;
                 int k = 0;
 #pragma unroll
@@ -420,7 +435,7 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_gather_ch(const CountArgs a) {
                     jg = j;
                     const float4 p = a.pos2[j];
                     const float tx = p.x + Dx, ty = p.y + Dy, tz = p.z + Dz;
-                    jb[lane] = make_float4(tx, ty, tz, p.w);
+                    jb[32 * bt + lane] = make_float4(tx, ty, tz, p.w);
                     jxy[lane] = make_ulonglong2(pk2(tx, tx), pk2(ty, ty));
                     jzz[lane] = pk2(tz, tz);
                 }
@@ -437,7 +452,7 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_gather_ch(const CountArgs a) {
                             v[u] = (js >= 0 && c < nch) ? __ldg(&a.w2[(int64_t)js * nch + c]) : 0.f;
                         }
 #pragma unroll
-                        for (int u = 0; u < 4; u++) jw[32 * (u0 + u) + lane] = v[u];
+                        for (int u = 0; u < 4; u++) jw[32 * NCH * bt + 32 * (u0 + u) + lane] = v[u];
                     }
                 }
                 __syncwarp();
@@ -454,8 +469,19 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_gather_ch(const CountArgs a) {
                     o1 = __funnelshift_l((unsigned)(d >> 32), o1, 1);
                 }
                 const unsigned valid = nj >= 32 ? 0xffffffffu : ((1u << nj) - 1u);
-                gather(__brev(~o0) & valid, u0, acc0, ncm0);
-                gather(__brev(~o1) & valid, u1, acc1, ncm1);
+                const unsigned long long w0 = __brev(~o0) & valid, w1 = __brev(~o1) & valid;
+                const int sh = 32 * (bt & 1);
+                if (bt < 2) {
+                    m0a |= w0 << sh;
+                    m1a |= w1 << sh;
+                } else {
+                    m0b |= w0 << sh;
+                    m1b |= w1 << sh;
+                }
+                __syncwarp();  // the next batch restages the stage-1 slots
+                }
+                gather(m0a, m0b, u0, acc0, ncm0);
+                gather(m1a, m1b, u1, acc1, ncm1);
                 __syncwarp();
             }
         }

@@ -217,6 +217,11 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
     Carve cv;
     size_t o_xyz[2] = {0, 0}, o_cellid[2], o_rank[2], o_count[2], o_start[2], o_orig[2],
            o_pos32[2], o_w32[2] = {0, 0}, o_w64[2] = {0, 0}, o_win[2] = {0, 0};
+    // sorted FP64 weights: only the FP64 marking functions and the per-object
+    // neighbour conditions read them; the FP32 kernels read the FP32 copy
+    const bool need_w64 = c.mode == MODE_NEIGH ||
+                          (c.wf == 0 && (c.mode == MODE_MARK || c.mode == MODE_XYZW ||
+                                         c.mode == MODE_SMUW));
     for (int s = 0; s < nsamp; s++) {
         size_t n = (size_t)std::max<int64_t>(ns[s], 1);
         if (c.mem == GBP_MEM_HOST) o_xyz[s] = cv.take<double>(3 * n);
@@ -229,7 +234,7 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
         if (c.nw > 0) {
             if (c.mem == GBP_MEM_HOST) o_win[s] = cv.take<double>(n * c.nw);
             o_w32[s] = cv.take<float>(n * c.nw);
-            o_w64[s] = cv.take<double>(n * c.nw);
+            if (need_w64) o_w64[s] = cv.take<double>(n * c.nw);
         }
     }
     size_t scan_ints = gbp_scan_tmp_ints(nkeys + 1);
@@ -374,7 +379,7 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
                     h2d += (int64_t)(n * c.nw * sizeof(double));
                 }
                 sd[s].w32 = at<float>(W, o_w32[s]);
-                sd[s].w64 = at<double>(W, o_w64[s]);
+                sd[s].w64 = need_w64 ? at<double>(W, o_w64[s]) : nullptr;
                 wsrc = wd;
             }
             if (s == 0) c.w1 = wsrc; else c.w2 = wsrc;

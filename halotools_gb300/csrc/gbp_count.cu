@@ -530,8 +530,8 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
     // MARKC sorted, per warp and code batch: each code's bin, the codes sorted by
     // bin, and per bin its count and (after the scatter) its end
     unsigned char *s_bin = (unsigned char *)(smem + L.off_rec) + warp * gbp_markc_sort_bytes(nb0);
-    unsigned short *s_rec2 = (unsigned short *)(s_bin + 1024);
-    int *s_cnt = (int *)(s_bin + 3072), *s_cur = s_cnt + (nb0 + 1);
+    unsigned short *s_rec2 = (unsigned short *)(s_bin + GBP_MARKC_CODES);
+    int *s_cnt = (int *)(s_bin + 3 * GBP_MARKC_CODES), *s_cur = s_cnt + (nb0 + 1);
     // (s, mu'): this warp's ring of deferred FP64 rechecks and its tail
     constexpr bool RQM = SMUF;
     RQ rq{(int4 *)(smem + L.off_rq) + warp * GBP_RQCAP,
@@ -540,9 +540,10 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                      warp * GBP_USLOTS * (nw > 0 ? nw : 1);
     const Ix ix{uix, jix};
     // this warp's pair codes of one 32-point j batch: at most 64 x 32 (marked
-    // modes: one i-point at a time, 32 x 32)
+    // modes other than the sorted channel form: one i-point at a time, 32 x 32)
     unsigned short *s_code =
-        (unsigned short *)(smem + L.off_code) + warp * ((MARK || MARKC) ? 1024 : 2048);
+        (unsigned short *)(smem + L.off_code) +
+        warp * ((MARK || (MARKC && !msort)) ? 1024 : msort ? GBP_MARKC_CODES : 2048);
 
     lut_compact(a.ax[0].lut, T0, a.ax[0].hi, a.ax[0].lo, nb0, s_l0, s_hl0, s_qb, tid, GBP_BLOCK);
     if (TWO) lut_compact(a.ax[1].lut, T1, a.ax[1].hi, a.ax[1].lo, nb1, s_l1, s_hl1, nullptr, tid,
@@ -1178,17 +1179,16 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                                 const int end = s_cur[b], st = end - s_cnt[b];
                                 unsigned long long S = 0ull, NC = 0ull;
                                 for (int p = st + g; p < end; p += 8 * G) {
+                                    // this group's records of the run: as many
+                                    // iterations as records, at most 8
+                                    const int nk = min(8, (end - p + G - 1) / G);
                                     unsigned long long r = 0ull;
-#pragma unroll
-                                    for (int k = 0; k < 8; k++) {
-                                        const int q = p + k * G;
-                                        if (q < end) {
-                                            const unsigned rec = s_rec2[q];
-                                            unsigned long long v = f2_mul(W1[(rec & 127u) * mP + cp],
-                                                                          W2[((rec >> 7) & 31u) * mP + cp]);
-                                            if (rec & 0x1000u) v = f2_add(v, v);
-                                            r = f2_add(r, v);
-                                        }
+                                    for (int k = 0; k < nk; k++) {
+                                        const unsigned rec = s_rec2[p + k * G];
+                                        unsigned long long v = f2_mul(W1[(rec & 127u) * mP + cp],
+                                                                      W2[((rec >> 7) & 31u) * mP + cp]);
+                                        if (rec & 0x1000u) v = f2_add(v, v);
+                                        r = f2_add(r, v);
                                     }
                                     kahan_f2(S, NC, ONE2, r);
                                 }
@@ -1326,7 +1326,7 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                     }
                     __syncwarp();
                 };
-                if (MARK || MARKC) {
+                if (MARK || (MARKC && (!msort || GBP_MARKC_CODES < 2048))) {
                     stage2(m0, 0u);
                     stage2(0u, m1);
                 } else {

@@ -38,6 +38,9 @@ enum { MODE_3D = 0, MODE_XYZ = 1, MODE_SMU = 2, MODE_MARK = 3, MODE_ADJ = 4, MOD
 
 // channels of one batched adjoint launch
 #define GBP_ADJ_CH 8
+// batched adjoint: 32-point j batches staged per pass; a lane walks the in-range
+// pairs of all of them in one loop, which evens out the lanes' trip counts
+#define GBP_ADJC_BATCHES 4
 
 // Pair geometry of a count mode: (rp, pi) cylinders or (s, mu') cones; every
 // other mode measures 3-D separations
@@ -183,10 +186,15 @@ __host__ __device__ inline bool gbp_markc_sorted(int nw) {
 __host__ __device__ inline int gbp_markc_cols(int nw) {
     return gbp_markc_sorted(nw) ? 2 * gbp_markc_pairs(nw) : nw;
 }
+// MARKC sorted form: a code batch holds the pairs of both i-halves of a 32-point
+// j batch (64 x 32 codes), so a sort spreads its per-bin cost over twice the pairs
+#ifndef GBP_MARKC_CODES
+#define GBP_MARKC_CODES 2048
+#endif
 // MARKC per-warp scratch of one code batch (sorted form): each code's bin (u8),
 // the codes sorted by bin (u16), and two counters per bin
 __host__ __device__ inline int gbp_markc_sort_bytes(int nb0) {
-    return gbp_align(1024 + 2048 + 8 * (nb0 + 1), 16);
+    return gbp_align(GBP_MARKC_CODES * 3 + 8 * (nb0 + 1), 16);
 }
 
 __host__ __device__ inline SmemLayout gbp_smem_layout(int mode, int T0, int T1, int nb0, int nb1,
@@ -204,16 +212,20 @@ __host__ __device__ inline SmemLayout gbp_smem_layout(int mode, int T0, int T1, 
     L.off_qb = o; o += smu ? gbp_align(T0 * 4, 16) : 0;
     L.off_hl0 = o; o += adj ? 0 : gbp_align((nb0 + 2) * 8, 16);
     L.off_hl1 = o; o += adj ? 0 : gbp_align((nb1 + 2) * 8, 16);
-    L.off_j = o; o += GBP_JCAP * 16;   // adjoint: float4 per j; count: x, y, z, index arrays
+    const int jb = mode == MODE_ADJC ? GBP_ADJC_BATCHES : 1;  // j batches staged at once
+    L.off_j = o; o += jb * GBP_JCAP * 16;   // adjoint: float4 per j; count: x, y, z, index arrays
     L.off_j2 = o; o += GBP_JCAP * 24;   // (x,x,y,y), (z,z) per j
-    L.off_jw = o; o += gbp_align(GBP_JCAP * jw, 16);
+    L.off_jw = o; o += gbp_align(jb * GBP_JCAP * jw, 16);
     L.off_q = o;
     o += adj ? 0 : GBP_WARPS * GBP_USLOTS * 16 +
                        gbp_align(GBP_WARPS * GBP_USLOTS * (jw > 4 ? jw : 4), 16);
-    // codes of one 32-point j batch: 64 x 32 (marked modes: one i-point at a time, 32 x 32)
-    L.off_code = o;
-    o += adj ? 0 : GBP_WARPS * ((mode == MODE_MARK || mode == MODE_MARKC) ? 1024 : 2048) * 2;
+    // codes of one 32-point j batch: 64 x 32 (marked modes other than the sorted
+    // channel form: one i-point at a time, 32 x 32)
     const bool msort = mode == MODE_MARKC && gbp_markc_sorted(jw / 4);
+    L.off_code = o;
+    o += adj ? 0
+             : GBP_WARPS * ((mode == MODE_MARK || (mode == MODE_MARKC && !msort)) ? 1024
+                            : msort ? GBP_MARKC_CODES : 2048) * 2;
     L.off_rec = o;
     o += mode != MODE_MARKC ? 0
          : msort ? GBP_WARPS * gbp_markc_sort_bytes(nb0)

@@ -7,7 +7,9 @@
 // scan         exclusive prefix sum of the cell counts (three-kernel tile scan)
 // k_scatter    one thread per point: writes the sorted FP32 record and the
 //              sorted -> caller's row map (the FP64 recheck reads the caller's
-//              positions through it).
+//              positions through it); the warp then copies its points' weight
+//              rows with lanes over (point, column), so that reads and writes
+//              are whole rows.
 // items        one work item per (block, chunk of <= GBP_TI points).
 //
 // Roofline: HBM-bound, about 12-24 B (positions) + 24 B read and 44 B written
@@ -114,18 +116,28 @@ __global__ void k_scatter(int64_t npts, const int *__restrict__ cellid, const in
                           float4 *__restrict__ pos32, int *__restrict__ orig,
                           const double *__restrict__ w, int nw, float *__restrict__ w32,
                           double *__restrict__ w64) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= npts) return;
-    int dst = start[cellid[i]] + rank[i];
-    float4 r = rel[i];
-    r.w = __int_as_float(dst);
-    pos32[dst] = r;
-    orig[dst] = (int)i;
+    // launched with whole warps (blocks of 256): every lane stays for the shuffles
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    int dst = -1;
+    if (i < npts) {
+        dst = start[cellid[i]] + rank[i];
+        float4 r = rel[i];
+        r.w = __int_as_float(dst);
+        pos32[dst] = r;
+        orig[dst] = (int)i;
+    }
     if (w) {
-        for (int k = 0; k < nw; k++) {
-            double v = w[i * nw + k];
-            w32[(int64_t)dst * nw + k] = __double2float_rn(v);
-            w64[(int64_t)dst * nw + k] = v;
+        // the warp's 32 rows: element t = (point t / nw, column t % nw)
+        const int64_t i0 = i - lane;
+        for (int t0 = 0; t0 < 32 * nw; t0 += 32) {
+            const int t = t0 + lane, p = t / nw, k = t - p * nw;
+            const int d = __shfl_sync(0xffffffffu, dst, p & 31);
+            if (p < 32 && i0 + p < npts) {
+                const double v = w[(i0 + p) * nw + k];
+                w32[(int64_t)d * nw + k] = __double2float_rn(v);
+                if (w64) w64[(int64_t)d * nw + k] = v;
+            }
         }
     }
 }

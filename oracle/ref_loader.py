@@ -146,3 +146,15 @@ def _namespace():
     ns.pairs = importlib.import_module(base + ".pairs")
     ns.HalotoolsError = importlib.import_module("halotools.custom_exceptions").HalotoolsError
     return ns
+
+
+def load_estimators(src_root: str = DEFAULT_SRC):
+    """halotools' own estimator modules (``tpcf``, ``rp_pi_tpcf``, ``wp``,
+    ``s_mu_tpcf``, ``marked_tpcf``) over the reference's counters, loaded
+    without ``two_point_clustering/__init__.py`` (which reaches astropy through
+    the jackknife helpers).  Returns {name: module}."""
+    load(src_root)
+    name = "halotools.mock_observables.two_point_clustering"
+    _pkg(name, [os.path.join(src_root, "halotools", "mock_observables", "two_point_clustering")])
+    return {m: importlib.import_module(name + "." + m)
+            for m in ("tpcf", "rp_pi_tpcf", "wp", "s_mu_tpcf", "marked_tpcf")}

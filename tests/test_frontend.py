@@ -109,9 +109,6 @@ def test_weighted_s_mu_messages():
     assert "Input ``rbins`` must be a monotonically increasing" in str(err.value)
 
 
-def test_install_into_halotools_without_halotools_is_a_noop():
-    assert isinstance(h.install_into_halotools(), list)
-
 
 def test_jackknife_xy_z_messages():
     t = np.ones(50, dtype=int)
