@@ -207,6 +207,13 @@ struct Geometry {
 };
 
 const int64_t MAX_CELLS_PER_DIM = 256;
+// Mean points per reach-K cell from which choose_grid takes reach K >= 2.  The
+// unweighted 3-D and (s, mu') counts, whose cost is mostly per binned pair,
+// take finer cells earlier than the marked and (rp, pi) ones: on 10M clustered
+// points (19.5 per reach-2 cell) reach 2 cut the 3-D count 22.2 -> 20.8 ms and
+// the (s, mu') count 32.6 -> 30.4 ms, while the 2-channel marked count went
+// 48.2 -> 85.9 ms and the (rp, pi) count on 2M points (9 per cell) 3.6 -> 3.9 ms.
+const double GBP_DENSE_REACH2 = 16.0;
 
 // Cells per dimension for reach K: as many as keep K*c >= search, capped;
 // with periodic wrap every offset in [-K, K] must reach a distinct cell.
@@ -234,7 +241,7 @@ inline bool grid_for_reach(int K, const double L[3], const double search[3], int
 // bf_hint > 0 forces the block factor (when the grid allows it).
 inline void choose_grid(Geometry &g, const double L[3], const double search[3], int pbc,
                         int64_t n2, int reach_hint, int64_t cap_per_dim, double ppc = 0.0,
-                        int bf_hint = 0) {
+                        int bf_hint = 0, double dense = 28.0) {
     for (int d = 0; d < 3; d++) g.L[d] = L[d];
     g.pbc = pbc;
     double vol = L[0] * L[1] * L[2];
@@ -248,7 +255,7 @@ inline void choose_grid(Geometry &g, const double L[3], const double search[3], 
             if (K <= reach_hint) best = K;
             continue;
         }
-        if (rho * cvol >= 28.0) best = K;
+        if (rho * cvol >= dense) best = K;
     }
     int64_t n[3];
     grid_for_reach(best, L, search, pbc, n, cap_per_dim);
