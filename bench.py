@@ -554,6 +554,36 @@ def extra_batched_adjoint(dev, threads, check, reps=3, m=16):
     return res
 
 
+def batched_step_only(k, m=16):
+    """The batched step of batched_adjoint_2m alone, ``k`` times: 16 Zheng07 draws
+    on 2M halos, forward over all draws and dC/dtheta; CUDA-event times of the
+    weights, the forward and the backward of each step."""
+    import torch
+    from halotools_gb300 import differentiable as D, mocks
+    L = 1000.0
+    pos, mass, _ = mocks.halo_table(2_000_000, L, seed=21)
+    rb = np.logspace(-1, np.log10(30), 20)
+    th = _hod_theta_draws(m)
+    xd = torch.from_numpy(pos).cuda()
+    md = torch.from_numpy(mass).cuda()
+    gbar = torch.ones((m, len(rb)), dtype=torch.float64, device="cuda")
+    steps = []
+    for _ in range(k):
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        e[0].record()
+        T = torch.tensor(th, dtype=torch.float64, device="cuda", requires_grad=True)
+        W = D.zheng07_weights_batched(T, md)
+        e[1].record()
+        C = D.weighted_pair_counts_batched(W, xd, rb, L)
+        e[2].record()
+        (C * gbar).sum().backward()
+        e[3].record()
+        torch.cuda.synchronize()
+        steps.append({"weights_ms": e[0].elapsed_time(e[1]), "forward_ms": e[1].elapsed_time(e[2]),
+                      "backward_ms": e[2].elapsed_time(e[3]), "step_ms": e[0].elapsed_time(e[3])})
+    return {"path": "batched_adjoint_2m step", "draws": m, "steps": steps}
+
+
 _POINTS_10M = []
 
 
@@ -763,6 +793,9 @@ def main():
                     help="skip the full-size oracle checks")
     ap.add_argument("--only-path", choices=sorted(EXTRAS),
                     help="run one comparison path alone and print its JSON (profiling)")
+    ap.add_argument("--batched-step", type=int, default=0, metavar="K",
+                    help="run only the batched + adjoint step of batched_adjoint_2m K times "
+                         "and print its timings (profiling)")
     # the reference arm's own options
     ap.add_argument("--slabs", type=int, default=0,
                     help="reference arm: slabs of cell1 ids (default: --steps, at most 64)")
@@ -772,6 +805,11 @@ def main():
     ap.add_argument("--counts-file", help="reference arm: save the whole workload's counts")
     args = ap.parse_args()
     threads = os.cpu_count() or 1
+    if args.batched_step:
+        import torch
+        torch.cuda.set_device(0)
+        print(json.dumps(batched_step_only(args.batched_step)))
+        return 0
     if args.only_path:
         import torch
         torch.cuda.set_device(0)
@@ -899,6 +937,11 @@ def main():
             roofline["traffic"] = json.load(open(tf)).get(args.workload)
         except Exception:
             pass
+    # diagnostics: the FP64 recheck rate, and the count kernel's DRAM rate from the
+    # ncu traffic figure over its live time (far below HBM: the kernel is issue-bound)
+    roofline["recheck_fraction"] = st["recheck_pairs"] / pairs_step if pairs_step else None
+    if roofline["traffic"]:
+        roofline["hbm_gbs"] = roofline["traffic"] / (cnt_ms * 1e-3) / 1e9
 
     line = {"metric": metric, "value": value, "unit": "pairs/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_s / args.steps * 1e3,
