@@ -77,3 +77,23 @@ def test_mesh_and_counts_match_the_reference_front_end():
     pi = np.linspace(0, 40, 11)
     assert np.array_equal(R.full_call("xyz", x, x, rb, pi, 300.0, 4),
                           ns.npairs_xy_z(x, x, rb, pi, period=300.0, num_threads=4))
+
+
+def test_bench_reference_arm_counts_the_whole_workload():
+    """bench.py --impl reference on config 1: its K slabs count the workload once
+    (21,542,180 in-range ordered pairs, the reference's own count) and the line
+    carries the contract's keys."""
+    import json
+    import os
+    import subprocess
+    import sys
+    root = os.path.abspath(os.path.join(os.path.dirname(__file__), ".."))
+    r = subprocess.run([sys.executable, os.path.join(root, "bench.py"), "--impl", "reference",
+                        "--workload", "3d100k", "--steps", "3", "--warmup", "1"],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["cpu_baseline"]["kind"] == "reference"
+    assert line["pairs_counted"] == 21542180 and line["slabs"] == 3
+    assert line["full_call"]["same_counts_as_slabs"] is True
+    assert line["value"] > 0 and line["e2e"]["h2d_bytes_per_step"] == 0
