@@ -506,7 +506,267 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_gather_ch(const CountArgs a) {
     if (lane == 0 && cand) atomicAdd(a.nrecheck + 1, cand);
 }
 
+// k_gather_c1: the batched adjoint over up to NCH (16) channels in one pass, one
+// i-point per lane (items of at most 32 points), so that the 16 channels' sums
+// fit in registers.  The two 8-channel passes of k_gather_ch each repeat the
+// staging, the range tests and the binning of every pair; here they are done
+// once.  Stage 1 packs two consecutive j-slots into each f32x2 operation.  The
+// per-pair channel work, the runs of 8 and their compensated sums are those of
+// k_gather_ch (error bound per point and item for same-sign terms: 7u per run
+// plus about 2u for the compensated sum of the runs).
+template <int NCH>
+__global__ void __launch_bounds__(GBP_BLOCK, 2) k_gather_c1(const CountArgs a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    constexpr unsigned FULL = 0xffffffffu;
+    constexpr int NB = GBP_ADJC_BATCHES;
+    static_assert(NB == 4, "the walk keeps the slots' masks in two 64-bit words");
+    static_assert(NCH % 8 == 0, "channels go in groups of 8 (two 16-byte loads)");
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nb0 = a.ax[0].nb, T0 = a.ax[0].T, nch = a.nw;
+    const SmemLayout L = gbp_smem_layout(MODE_ADJC, T0, 0, nb0, 0, a.nsten, 0, 4 * NCH);
+    if (gbp_smem_too_small(L.total, a.err)) return;
+    float4 *s_lut0 = (float4 *)(smem + L.off_lut0);
+    float4 *jb = (float4 *)(smem + L.off_j) + warp * 32 * NB;
+    // the current batch's slots for stage 1: x, y, z arrays, read as pairs
+    float *jx = (float *)(smem + L.off_j2) + warp * 96;
+    float *jy = jx + 32, *jz = jx + 64;
+    float *jw = (float *)(smem + L.off_jw) + warp * 32 * NB * NCH;
+    float4 *s_D = (float4 *)(smem + L.off_D);
+    double *s_E0 = (double *)(smem + L.off_E0);
+    float *s_hi0 = (float *)(smem + L.off_hi0);
+    float *s_lo0 = (float *)(smem + L.off_lo0);
+    int *s_off = (int *)(smem + L.off_off);
+    const int nbc = nb0 + 1;
+    float *s_gt = (float *)(smem + L.off_hist);  // [bin][channel]
+    for (int i = tid; i < T0; i += GBP_BLOCK) s_lut0[i] = a.ax[0].lut[i];
+    for (int i = tid; i < nb0; i += GBP_BLOCK) {
+        s_E0[i] = a.ax[0].E[i];
+        s_hi0[i] = a.ax[0].hi[i];
+        s_lo0[i] = a.ax[0].lo[i];
+    }
+    for (int i = tid; i < NCH * nbc; i += GBP_BLOCK) {
+        const int k = i / NCH, c = i - k * NCH;
+        s_gt[i] = c < nch ? a.gt[c * nbc + k] : 0.f;
+    }
+    for (int i = tid; i < a.nsten; i += GBP_BLOCK) {
+        s_off[i] = a.sten[i];
+        s_D[i] = a.stenD[i];
+    }
+    AxisSm A0{s_lut0, s_hi0, s_lo0, s_E0, nb0, a.ax[0].S, a.ax[0].B, a.ax[0].vlo, a.ax[0].vhi};
+    const int nitems = *a.nitems;
+    const int n1 = a.n[1], n2 = a.n[2];
+    const float R0 = fmaf(a.top0, 0x1p-18f, a.top0) + 1.0e-30f;
+    const unsigned long long RR0 = pk2(R0, R0);
+    unsigned long long cand = 0;
+    __syncthreads();
+
+    while (true) {
+        int it = 0;
+        if (lane == 0) it = atomicAdd(a.counter, 1);
+        it = __shfl_sync(FULL, it, 0);
+        if (it >= nitems) break;
+        const int4 item = a.items[it];
+        const int cell = item.x, ifirst = item.y;
+        const int icnt = item.z & 127, s0 = (item.z >> 7) & 1023, s1 = (item.z >> 17) & 1023;
+        const int cz = cell % n2, cy = (cell / n2) % n1, cx = cell / (n1 * n2);
+        float4 u = make_float4(GBP_FAR, GBP_FAR, GBP_FAR, __int_as_float(0));
+        if (lane < icnt) u = a.pos1[ifirst + lane];
+        const unsigned long long UX = pk2(u.x, u.x), UY = pk2(u.y, u.y), UZ = pk2(u.z, u.z);
+        constexpr int NH = NCH / 2;  // packed channel pairs
+        unsigned long long acc[NH], ncm[NH];
+#pragma unroll
+        for (int q = 0; q < NH; q++) acc[q] = ncm[q] = 0ull;
+        // the lane's in-range pairs over the staged slots (ma: slots 0-63, mb:
+        // 64-127), highest slot of each word first
+        auto gather = [&](unsigned long long ma, unsigned long long mb) {
+            unsigned long long run[NH];
+#pragma unroll
+            for (int q = 0; q < NH; q++) run[q] = 0ull;
+            int nr = 0;
+            while (ma | mb) {
+                const bool first = ma != 0ull;
+                const int bit = 63 - __clzll(first ? ma : mb);
+                if (first) ma ^= 1ull << bit;
+                else mb ^= 1ull << bit;
+                const int jj = bit + (first ? 0 : 64);
+                const float4 t = jb[jj];
+                const float dx = u.x - t.x, dy = u.y - t.y, dz = u.z - t.z;
+                const float v = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+                const float4 e = lut_entry(v, A0);
+                int2 kk;
+                if ((v > e.z) & !(v > e.y)) {
+                    kk = slow_adj_bins(v, __float_as_int(e.x), __float_as_int(u.w),
+                                       __float_as_int(t.w), A0, a);
+                } else {
+                    const int b = __float_as_int(e.x) + (v > e.y ? 1 : 0);
+                    kk = make_int2(b, b);
+                }
+                // channels in groups of 8: two 16-byte loads of G and of w_j each
+#pragma unroll
+                for (int h = 0; h < NCH / 8; h++) {
+                    const ulonglong2 *wr = (const ulonglong2 *)(jw + jj * NCH + 8 * h);
+                    const ulonglong2 *gr = (const ulonglong2 *)(s_gt + kk.x * NCH + 8 * h);
+                    unsigned long long g[4], w[4];
+#pragma unroll
+                    for (int q = 0; q < 2; q++) {
+                        const ulonglong2 gq = gr[q], wq = wr[q];
+                        g[2 * q] = gq.x;
+                        g[2 * q + 1] = gq.y;
+                        w[2 * q] = wq.x;
+                        w[2 * q + 1] = wq.y;
+                    }
+                    if (kk.x != kk.y) {
+                        // the mean over the two orders: 0.5 (G[k1] + G[k2])
+                        const ulonglong2 *hr = (const ulonglong2 *)(s_gt + kk.y * NCH + 8 * h);
+                        const unsigned long long half = pk2(0.5f, 0.5f);
+#pragma unroll
+                        for (int q = 0; q < 2; q++) {
+                            const ulonglong2 hq = hr[q];
+                            g[2 * q] = f2_mul(half, f2_add(g[2 * q], hq.x));
+                            g[2 * q + 1] = f2_mul(half, f2_add(g[2 * q + 1], hq.y));
+                        }
+                    }
+#pragma unroll
+                    for (int q = 0; q < 4; q++) run[4 * h + q] = f2_fma(w[q], g[q], run[4 * h + q]);
+                }
+                if (++nr == 8) {
+#pragma unroll
+                    for (int q = 0; q < NH; q++) {
+                        kahan_f2(acc[q], ncm[q], pk2(1.f, 1.f), run[q]);
+                        run[q] = 0ull;
+                    }
+                    nr = 0;
+                }
+            }
+            if (nr) {
+#pragma unroll
+                for (int q = 0; q < NH; q++) kahan_f2(acc[q], ncm[q], pk2(1.f, 1.f), run[q]);
+            }
+        };
+        for (int sb = s0; sb < s1; sb += 32) {
+            const int s = sb + lane;
+            int st = 0, cn = 0;
+            float4 D = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (s < s1) {
+                D = s_D[s];
+                const int key = gbp_run_key(s_off[s], cx, cy, cz, a.n, a.pbc, 0, a.bf3);
+                if (key >= 0) {
+                    st = a.start2[key];
+                    cn = a.start2[key + __float_as_int(D.w)] - st;
+                }
+            }
+            int incl = cn;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(FULL, incl, o);
+                if (lane >= o) incl += t;
+            }
+            const int T = __shfl_sync(FULL, incl, 31);
+            cand += (unsigned long long)icnt * (unsigned long long)T;
+            for (int f00 = 0; f00 < T; f00 += 32 * NB) {
+                unsigned long long ma = 0ull, mb = 0ull;
+#pragma unroll
+                for (int bt = 0; bt < NB; bt++) {
+                    const int f0 = f00 + 32 * bt;
+                    if (f0 >= T) break;  // warp-uniform
+                    const int f = f0 + lane;
+                    int k = 0;
+#pragma unroll
+                    for (int step = 16; step > 0; step >>= 1) {
+                        const int vv = __shfl_sync(FULL, incl, k + step - 1);
+                        if (vv <= f) k += step;
+                    }
+                    k &= 31;
+                    const int stk = __shfl_sync(FULL, st, k);
+                    const int exk = __shfl_sync(FULL, incl - cn, k);
+                    const float Dx = __shfl_sync(FULL, D.x, k), Dy = __shfl_sync(FULL, D.y, k),
+                                Dz = __shfl_sync(FULL, D.z, k);
+                    int jg = -1;  // the slot's sorted j index (-1: padding)
+                    if (f < T) {
+                        const int j = stk + (f - exk);
+                        jg = j;
+                        const float4 p = a.pos2[j];
+                        const float tx = p.x + Dx, ty = p.y + Dy, tz = p.z + Dz;
+                        jb[32 * bt + lane] = make_float4(tx, ty, tz, p.w);
+                        jx[lane] = tx;
+                        jy[lane] = ty;
+                        jz[lane] = tz;
+                    } else {
+                        // padding: at -FAR, 2 FAR from an idle lane's point, and masked
+                        jx[lane] = -GBP_FAR;
+                        jy[lane] = -GBP_FAR;
+                        jz[lane] = -GBP_FAR;
+                    }
+                    {
+                        // the slots' weight rows: lanes over (slot, channel), coalesced
+                        // read-only loads all issued before the contiguous stores
+#pragma unroll
+                        for (int u0 = 0; u0 < NCH; u0 += 4) {
+                            float vw[4];
+#pragma unroll
+                            for (int q = 0; q < 4; q++) {
+                                const int t = 32 * (u0 + q) + lane, c = t % NCH;
+                                const int js = __shfl_sync(FULL, jg, t / NCH);
+                                vw[q] = (js >= 0 && c < nch) ? __ldg(&a.w2[(int64_t)js * nch + c]) : 0.f;
+                            }
+#pragma unroll
+                            for (int q = 0; q < 4; q++) jw[32 * NCH * bt + 32 * (u0 + q) + lane] = vw[q];
+                        }
+                    }
+                    __syncwarp();
+                    // stage 1: slots 2k and 2k + 1 in one packed operation; v as the
+                    // gather forms it, then R - v, whose sign bits are appended to o
+                    const int nj = min(32, T - f0);
+                    unsigned o = 0u;
+                    const unsigned long long *jx2 = (const unsigned long long *)jx;
+                    const unsigned long long *jy2 = (const unsigned long long *)jy;
+                    const unsigned long long *jz2 = (const unsigned long long *)jz;
+#pragma unroll 8
+                    for (int kk2 = 0; kk2 < 16; kk2++) {
+                        const unsigned long long dX = f2_sub(UX, jx2[kk2]), dY = f2_sub(UY, jy2[kk2]),
+                                                 dZ = f2_sub(UZ, jz2[kk2]);
+                        const unsigned long long d =
+                            f2_sub(RR0, f2_fma(dZ, dZ, f2_fma(dY, dY, f2_mul(dX, dX))));
+                        o = __funnelshift_l((unsigned)d, o, 1);
+                        o = __funnelshift_l((unsigned)(d >> 32), o, 1);
+                    }
+                    const unsigned valid = nj >= 32 ? 0xffffffffu : ((1u << nj) - 1u);
+                    const unsigned long long w0 = __brev(~o) & valid;
+                    const int sh = 32 * (bt & 1);
+                    if (bt < 2) ma |= w0 << sh;
+                    else mb |= w0 << sh;
+                    __syncwarp();  // the next batch restages the stage-1 slots
+                }
+                gather(ma, mb);
+                __syncwarp();
+            }
+        }
+        // this item's sums of the lane's point: its dL/dw row (caller's order)
+        if (lane < icnt) {
+            double *row = a.grad + (int64_t)a.orig[ifirst + lane] * nch;
+#pragma unroll
+            for (int q = 0; q < NH; q++) {
+                const int c = 2 * q;
+                const double lo = (double)__uint_as_float((unsigned)acc[q]) +
+                                  (double)__uint_as_float((unsigned)ncm[q]);
+                const double hi = (double)__uint_as_float((unsigned)(acc[q] >> 32)) +
+                                  (double)__uint_as_float((unsigned)(ncm[q] >> 32));
+                if (c < nch) atomicAdd(&row[c], 2.0 * lo);
+                if (c + 1 < nch) atomicAdd(&row[c + 1], 2.0 * hi);
+            }
+        }
+    }
+    if (lane == 0 && cand) atomicAdd(a.nrecheck + 1, cand);
+}
+
 cudaError_t gbp_launch_adjoint_ch(const CountArgs &a, int grid, size_t smem, cudaStream_t st) {
+    if (a.nw > GBP_ADJ_CH) {
+        cudaError_t e = cudaFuncSetAttribute(k_gather_c1<GBP_ADJ_CH_MAX>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        k_gather_c1<GBP_ADJ_CH_MAX><<<grid, GBP_BLOCK, smem, st>>>(a);
+        return cudaGetLastError();
+    }
     cudaError_t e = cudaFuncSetAttribute(k_gather_ch<GBP_ADJ_CH>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -514,15 +774,20 @@ cudaError_t gbp_launch_adjoint_ch(const CountArgs &a, int grid, size_t smem, cud
     return cudaGetLastError();
 }
 
-int gbp_adjoint_ch_occupancy(size_t smem) {
+template <class K>
+static int occupancy_of(K kernel, size_t smem) {
     int nblk = 0;
-    if (cudaFuncSetAttribute(k_gather_ch<GBP_ADJ_CH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem) != cudaSuccess)
+    if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        cudaSuccess)
         return 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nblk, k_gather_ch<GBP_ADJ_CH>, GBP_BLOCK,
-                                                      smem) != cudaSuccess)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nblk, kernel, GBP_BLOCK, smem) != cudaSuccess)
         return 0;
     return nblk;
+}
+
+int gbp_adjoint_ch_occupancy(size_t smem, int nw) {
+    return nw > GBP_ADJ_CH ? occupancy_of(k_gather_c1<GBP_ADJ_CH_MAX>, smem)
+                           : occupancy_of(k_gather_ch<GBP_ADJ_CH>, smem);
 }
 
 template <bool POBJ>

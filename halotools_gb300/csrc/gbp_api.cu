@@ -241,9 +241,11 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
     size_t o_scan = cv.take<int>(scan_ints);
     // work items: i-chunks of GBP_TI times stencil groups of <= GBP_JCAP_ITEM
     // j-points; the builder flags an overflow and the call is repeated larger
+    // the 16-channel adjoint holds one point per lane: items of 32
+    const int item_ti = (c.mode == MODE_ADJC && c.nw > GBP_ADJ_CH) ? 32 : GBP_TI;
     size_t max_items = std::max<size_t>(
         plan->item_cap,
-        2 * ((size_t)nkeys + (size_t)(c.n1 / GBP_TI)) +
+        2 * ((size_t)nkeys + (size_t)(c.n1 / item_ti)) +
             (size_t)nsten * (size_t)(c.n2 / GBP_JCAP_ITEM) + 65536);
     if (plan->first_item_cap) {
         max_items = plan->first_item_cap;  // once: an overflow sets item_cap for the retry
@@ -424,6 +426,7 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
         ip.stenD = at<float4>(W, o_stenD);
         ip.nsten = nsten;
         ip.jcap = GBP_JCAP_ITEM;
+        ip.ti = item_ti;
         CK(gbp_build_items(ip, at<int4>(W, o_items), (int)std::min<size_t>(max_items, INT32_MAX),
                            d_nitems, reinterpret_cast<int *>(misc) + 3, at<int>(W, o_itmp),
                            at<int>(W, o_scan), st, &launches));
@@ -501,7 +504,7 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
                         : (c.mode == MODE_MARK || w2) ? (c.wf == 0 ? 8 * c.nw : 4)
                         : c.mode == MODE_MARKC ? 4 * gbp_markc_cols(c.nw)
                         : c.mode == MODE_ADJ   ? 4
-                        : c.mode == MODE_ADJC  ? 4 * GBP_ADJ_CH  // the kernel's fixed stride
+                        : c.mode == MODE_ADJC  ? 4 * gbp_adjc_nch(c.nw)  // the kernel's fixed stride
                         : c.mode == MODE_POBJ  ? 4   // the gather kernel's fixed stride
                         : (c.mode == MODE_JACK || c.mode == MODE_JACKXYZ) ? 4
                         : neigh                ? 4   // the j-slots' sorted indices
@@ -550,7 +553,7 @@ int run_call(gbp_plan *plan, Call &c, std::vector<unsigned long long> &hist_host
                 h2d += (int64_t)(sizeof(long long) * (c.n1 + 1));
             }
         }
-        int occ = adjc            ? gbp_adjoint_ch_occupancy(smem)
+        int occ = adjc            ? gbp_adjoint_ch_occupancy(smem, c.nw)
                   : (adj || pobj) ? gbp_adjoint_occupancy(smem, pobj)
                   : neigh       ? gbp_neigh_occupancy(smem)
                                 : gbp_count_occupancy(c.mode, c.wf, smem);
@@ -1726,8 +1729,8 @@ int gbp_weighted_adjoint_3d_channels(gbp_plan *plan, const double *xyz, int64_t 
                                      const double *gbar, double *grad_w) {
     int rc = check_common(plan, xyz, n, xyz, n, period3, pbc, mem);
     if (rc) return rc;
-    if (nch < 1 || nch > GBP_ADJ_CH)
-        return fail(plan, GBP_ERR_INVALID, "nch must be 1..%d, got %d", GBP_ADJ_CH, nch);
+    if (nch < 1 || nch > GBP_ADJ_CH_MAX)
+        return fail(plan, GBP_ERR_INVALID, "nch must be 1..%d, got %d", GBP_ADJ_CH_MAX, nch);
     if ((n > 0 && (!w || !grad_w)) || !gbar) return fail(plan, GBP_ERR_INVALID, "null weights or gradients");
     if (!rbins || nb < 2 || nb > GBP_NB_MAX)
         return fail(plan, GBP_ERR_INVALID, "rbins must have 2..%d entries", GBP_NB_MAX);

@@ -38,6 +38,10 @@ enum { MODE_3D = 0, MODE_XYZ = 1, MODE_SMU = 2, MODE_MARK = 3, MODE_ADJ = 4, MOD
 
 // channels of one batched adjoint launch
 #define GBP_ADJ_CH 8
+// ... and up to GBP_ADJ_CH_MAX in one pass with one i-point per lane (items of 32)
+#define GBP_ADJ_CH_MAX 16
+// channels a batched adjoint launch stages per j-point: 8, or 16 past 8
+__host__ __device__ inline int gbp_adjc_nch(int nw) { return nw <= GBP_ADJ_CH ? GBP_ADJ_CH : GBP_ADJ_CH_MAX; }
 // batched adjoint: 32-point j batches staged per pass; a lane walks the in-range
 // pairs of all of them in one loop, which evens out the lanes' trip counts
 #define GBP_ADJC_BATCHES 4
@@ -254,7 +258,7 @@ __host__ __device__ inline SmemLayout gbp_smem_layout(int mode, int T0, int T1, 
     } else if (mode == MODE_ADJ) {
         hist_bytes = GBP_BLOCK * 8 + gbp_align((nb0 + 1) * 4, 16);  // partial sums + gt table
     } else if (mode == MODE_ADJC) {
-        hist_bytes = gbp_align(GBP_ADJ_CH * (nb0 + 1) * 4, 16);     // gt table per channel
+        hist_bytes = gbp_align((jw / 4) * (nb0 + 1) * 4, 16);      // gt table per channel
     } else if (mode == MODE_NEIGH) {
         hist_bytes = 0;                                       // counters live in registers
     } else if (mode == MODE_POBJ) {
@@ -338,6 +342,7 @@ struct ItemPlan {
     const float4 *stenD;  // device (run lengths in .w)
     int nsten;
     int jcap;
+    int ti = GBP_TI;      // i-points per item (at most GBP_TI)
 };
 cudaError_t gbp_build_items(const ItemPlan &ip, int4 *d_items, int cap, int *d_nitems,
                             int *d_overflow, int *d_tmp, int *d_scan_tmp, cudaStream_t st,
@@ -359,7 +364,7 @@ cudaError_t gbp_launch_adjoint(const CountArgs &a, int grid, size_t smem, cudaSt
 int gbp_adjoint_occupancy(size_t smem, bool per_object = false);
 // batched adjoint: up to GBP_ADJ_CH weight channels (a.nw) per launch
 cudaError_t gbp_launch_adjoint_ch(const CountArgs &a, int grid, size_t smem, cudaStream_t st);
-int gbp_adjoint_ch_occupancy(size_t smem);
+int gbp_adjoint_ch_occupancy(size_t smem, int nw);
 // per-object neighbours: thresholds pre-pass then k_neigh<geometry, out>
 // (out 0 counts, 1 has-neighbour flags, 2 pair list)
 cudaError_t gbp_launch_neigh(const CountArgs &a, int n1, int out, int grid, size_t smem,

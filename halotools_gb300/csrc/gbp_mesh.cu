@@ -270,9 +270,9 @@ cudaError_t gbp_build_cells(const void *d_xyz, int xyz_f32, int64_t npts, const 
     return cudaSuccess;
 }
 
-// Work items: (block key, first i-point, packed {i count <= GBP_TI, first and
+// Work items: (block key, first i-point, packed {i count <= ti, first and
 // one-past-last stencil entry}).  A block's i-points are cut into chunks of
-// GBP_TI; its stencil runs are cut into consecutive groups of at most `jcap`
+// ti (GBP_TI, or fewer for kernels that hold one point per lane); its stencil runs are cut into consecutive groups of at most `jcap`
 // j-points (a group closes before the run that would overflow it), so every
 // item costs at most GBP_TI * jcap pair evaluations plus one run.
 struct ItemPlanDev {
@@ -286,6 +286,7 @@ struct ItemPlanDev {
     const float4 *stenD;
     int nsten;
     int jcap;
+    int ti;  // i-points per item
 };
 
 __device__ __forceinline__ int stencil_count(const ItemPlanDev &P, int keybase, int cx, int cy,
@@ -305,7 +306,7 @@ __global__ void k_items(ItemPlanDev P, int *__restrict__ nitem, const int *__res
     if (EMIT && k == 0 && off[P.nkeys] > cap) *overflow = 1;
     if (k >= P.nkeys) return;
     const int first = P.start1[k * P.bf3], cnt = P.start1[(k + 1) * P.bf3] - first;
-    const int q = (cnt + GBP_TI - 1) / GBP_TI;
+    const int q = (cnt + P.ti - 1) / P.ti;
     const int mock = (int)(k / P.ncm), cell = (int)(k - (int64_t)mock * P.ncm);
     const int cz = cell % P.n[2], cy = (cell / P.n[2]) % P.n[1], cx = cell / (P.n[1] * P.n[2]);
     const int keybase = mock * P.ncm;
@@ -318,9 +319,9 @@ __global__ void k_items(ItemPlanDev P, int *__restrict__ nitem, const int *__res
             if (close) {
                 if (EMIT) {
                     for (int c = 0; c < q; c++) {
-                        const int num = min(GBP_TI, cnt - c * GBP_TI);
+                        const int num = min(P.ti, cnt - c * P.ti);
                         if (o < cap)
-                            items[o] = make_int4((int)k, first + c * GBP_TI,
+                            items[o] = make_int4((int)k, first + c * P.ti,
                                                  num | (s0 << 7) | (s << 17), 0);
                         o++;
                     }
@@ -350,6 +351,7 @@ cudaError_t gbp_build_items(const ItemPlan &ip, int4 *d_items, int cap, int *d_n
     P.stenD = ip.stenD;
     P.nsten = ip.nsten;
     P.jcap = ip.jcap;
+    P.ti = ip.ti > 0 && ip.ti <= GBP_TI ? ip.ti : GBP_TI;
     unsigned g = (unsigned)((ip.nkeys + 255) / 256);
     int *nitem = d_tmp;
     int *off = d_tmp + ip.nkeys + 1;

@@ -130,13 +130,13 @@ def hod_pair_counts(theta, halo_xyz, halo_mass, rbins, period):
 
 
 # ---------------- many parameter draws at once ----------------
-_ADJ_CH = 8  # channels of one batched adjoint launch (gbp_weighted_adjoint_3d_channels)
+_ADJ_CH = 16  # channels of one batched adjoint launch (gbp_weighted_adjoint_3d_channels)
 
 
 class WeightedPairCountsBatched(torch.autograd.Function):
     """C[m] = sum_ij W_im W_jm [d_ij <= r_k] for the M columns of W (N, M), M <= 32:
     one forward pass over all columns (gbp_marked_npairs_3d_channels) and one
-    adjoint pass per 8 columns (gbp_weighted_adjoint_3d_channels)."""
+    adjoint pass per 16 columns (gbp_weighted_adjoint_3d_channels)."""
 
     @staticmethod
     def forward(ctx, W, xyz, rbins, box):

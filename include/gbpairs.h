@@ -144,11 +144,11 @@ int gbp_marked_npairs_3d(gbp_plan *plan, const double *xyz1, int64_t n1, const d
                          const double *period3, int32_t pbc, int32_t mem, double *out);
 
 /*
- * gbp_weighted_adjoint_3d for nch <= 8 weight channels at once (parameter draws
- * of an occupation model): w is (n, nch) row-major, gbar (nch, nbins), grad_w
- * (n, nch) with grad_w[m][c] = dL/dw_m of channel c for the forward counts
- * gbp_marked_npairs_3d_channels(x, x, w, w).  Each pair is binned once for all
- * channels.
+ * gbp_weighted_adjoint_3d for nch <= 16 weight channels at once (parameter
+ * draws of an occupation model): w is (n, nch) row-major, gbar (nch, nbins),
+ * grad_w (n, nch) with grad_w[m][c] = dL/dw_m of channel c for the forward
+ * counts gbp_marked_npairs_3d_channels(x, x, w, w).  Each pair is binned once
+ * for all channels (up to 8 channels: two i-points per lane; 9-16: one).
  */
 int gbp_weighted_adjoint_3d_channels(gbp_plan *plan, const double *xyz, int64_t n,
                                      const double *w, int32_t nch, const double *rbins,

@@ -117,7 +117,7 @@ def test_batched_forward_and_dw_match_fp64(gpu):
     from halotools_gb300 import differentiable as D
     L = 120.0
     pos, mass, _ = halos(8000, L, 21)
-    m_draws = 19  # adjoint groups of 8, 8 and 3
+    m_draws = 19  # adjoint groups of 16 (one point per lane) and 3 (two per lane)
     th = _thetas(m_draws, 22)
     W = np.stack([zheng07_np(t, mass) for t in th], axis=1)
     rb = np.logspace(-1, np.log10(15), 10)
@@ -133,6 +133,36 @@ def test_batched_forward_and_dw_match_fp64(gpu):
         np.testing.assert_allclose(C[m].detach().cpu().numpy(), want, rtol=1e-6)
         wg = oracle.weighted_adjoint_3d(pos, W[:, m], rb, L, gbar[m])
         assert np.max(np.abs(got_w[:, m] - wg)) / np.abs(wg).max() < 2e-6, m
+
+
+def test_batched_dw_twelve_channels_on_finer_grids(gpu):
+    """12 draws (the one-point-per-lane adjoint with 4 padded channels) against the
+    FP64 brute-force gradient, on the automatic grid and on forced finer ones."""
+    import torch
+    from halotools_gb300 import _native
+    from halotools_gb300 import differentiable as D
+    L = 90.0
+    pos, mass, _ = halos(6000, L, 31)
+    th = _thetas(12, 32)
+    W = np.stack([zheng07_np(t, mass) for t in th], axis=1)
+    rb = np.logspace(-1, np.log10(12), 9)
+    gbar = np.random.default_rng(33).normal(size=(12, len(rb)))
+    want = [oracle.weighted_adjoint_3d(pos, W[:, m], rb, L, gbar[m]) for m in range(12)]
+    plan = _native.default_plan()
+    try:
+        for reach, block in ((0, 0), (2, 2), (3, 1)):
+            plan.set_reach(reach)
+            plan.set_block(block)
+            Wt = torch.from_numpy(W).cuda().requires_grad_(True)
+            C = D.weighted_pair_counts_batched(Wt, torch.from_numpy(pos).cuda(), rb, L)
+            (C * torch.from_numpy(gbar).cuda()).sum().backward()
+            got = Wt.grad.cpu().numpy()
+            for m in range(12):
+                err = np.max(np.abs(got[:, m] - want[m])) / np.abs(want[m]).max()
+                assert err < 2e-6, (reach, block, m, err)
+    finally:
+        plan.set_reach(0)
+        plan.set_block(0)
 
 
 def test_batched_theta_gradient_matches_single_draws(gpu):
