@@ -537,6 +537,10 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_gather_c1(const CountArgs a) {
     float *s_lo0 = (float *)(smem + L.off_lo0);
     int *s_off = (int *)(smem + L.off_off);
     const int nbc = nb0 + 1;
+    // The staged weight rows go chunk-major: 16-byte chunk q (channels 4q..4q+3)
+    // of slot r at (q * 128 + r), so that lanes reading chunk q of different
+    // slots fall in different banks (64-byte rows put every row's chunk q in
+    // the same two bank groups).
     float *s_gt = (float *)(smem + L.off_hist);  // [bin][channel]
     for (int i = tid; i < T0; i += GBP_BLOCK) s_lut0[i] = a.ax[0].lut[i];
     for (int i = tid; i < nb0; i += GBP_BLOCK) {
@@ -604,12 +608,12 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_gather_c1(const CountArgs a) {
                 // channels in groups of 8: two 16-byte loads of G and of w_j each
 #pragma unroll
                 for (int h = 0; h < NCH / 8; h++) {
-                    const ulonglong2 *wr = (const ulonglong2 *)(jw + jj * NCH + 8 * h);
-                    const ulonglong2 *gr = (const ulonglong2 *)(s_gt + kk.x * NCH + 8 * h);
                     unsigned long long g[4], w[4];
 #pragma unroll
                     for (int q = 0; q < 2; q++) {
-                        const ulonglong2 gq = gr[q], wq = wr[q];
+                        const int cq = 2 * h + q;
+                        const ulonglong2 gq = *(const ulonglong2 *)(s_gt + kk.x * NCH + 4 * cq);
+                        const ulonglong2 wq = *(const ulonglong2 *)(jw + (cq * 32 * NB + jj) * 4);
                         g[2 * q] = gq.x;
                         g[2 * q + 1] = gq.y;
                         w[2 * q] = wq.x;
@@ -617,11 +621,11 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_gather_c1(const CountArgs a) {
                     }
                     if (kk.x != kk.y) {
                         // the mean over the two orders: 0.5 (G[k1] + G[k2])
-                        const ulonglong2 *hr = (const ulonglong2 *)(s_gt + kk.y * NCH + 8 * h);
                         const unsigned long long half = pk2(0.5f, 0.5f);
 #pragma unroll
                         for (int q = 0; q < 2; q++) {
-                            const ulonglong2 hq = hr[q];
+                            const ulonglong2 hq =
+                                *(const ulonglong2 *)(s_gt + kk.y * NCH + 4 * (2 * h + q));
                             g[2 * q] = f2_mul(half, f2_add(g[2 * q], hq.x));
                             g[2 * q + 1] = f2_mul(half, f2_add(g[2 * q + 1], hq.y));
                         }
@@ -710,7 +714,11 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_gather_c1(const CountArgs a) {
                                 vw[q] = (js >= 0 && c < nch) ? __ldg(&a.w2[(int64_t)js * nch + c]) : 0.f;
                             }
 #pragma unroll
-                            for (int q = 0; q < 4; q++) jw[32 * NCH * bt + 32 * (u0 + q) + lane] = vw[q];
+                            for (int q = 0; q < 4; q++) {
+                                const int t = 32 * (u0 + q) + lane, c = t % NCH;
+                                const int r = 32 * bt + t / NCH;  // the slot's row
+                                jw[((c >> 2) * 32 * NB + r) * 4 + (c & 3)] = vw[q];
+                            }
                         }
                     }
                     __syncwarp();
