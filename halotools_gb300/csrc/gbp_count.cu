@@ -374,14 +374,11 @@ __device__ __forceinline__ void bin_smu(const PairV &p, HT *hw, const WSink &ws,
     if (bs >= A.nb) return;  // beyond the s gate
     float q = __fdividef(dxy, v);
     float qb = e0.w;
-    float4 e1 = lut_entry_c<false>(q, Q);
-    int bq = __float_as_int(e1.x) + (q > e1.y ? 1 : 0);
     // nearest edges around q must be farther than qb
-    float below = bq > 0 ? Q.hi[bq - 1] : -3.0e38f;
-    float above = bq < Q.nb ? Q.lo[bq] : 3.0e38f;
-    // (e1.z = -inf marks a slot where several mu' edges may be crossed)
-    bool amb = ((v > e0.z) & !(v > e0.y)) | !(q - below > qb) | !(above - q > qb) |
-               (e1.z < -3.0e38f);
+    const QBin e1 = lut_q(q, Q);
+    const int bq = e1.b;
+    bool amb = ((v > e0.z) & !(v > e0.y)) | !(q - e1.below > qb) | !(e1.above - q > qb) |
+               e1.walk;
     if (amb) {
         slow_smu<HT, CNT, X>(v, q, qb, __float_as_int(e0.x), ix.ui[p.iu], ix.jw[p.jj], sym, p.w,
                               hw, ws, stride, A, Q, rq, a);
@@ -502,9 +499,9 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
     if (gbp_smem_too_small(L.total, a.err)) return;
     unsigned *s_l0 = (unsigned *)(smem + L.off_lut0);
     unsigned *s_l1 = (unsigned *)(smem + L.off_lut1);
-    float *s_qb = SMUF ? (float *)(smem + L.off_qb) : nullptr;
     float2 *s_hl0 = (float2 *)(smem + L.off_hl0);
     float2 *s_hl1 = (float2 *)(smem + L.off_hl1);
+    float4 *s_hq = SMUF ? (float4 *)(smem + L.off_hl1) : nullptr;
     // this warp's 32 staged j-points: x, y, z (cell offset added) and sorted index
     float *jx = (float *)(smem + L.off_j) + warp * 128;
     float *jy = jx + 32, *jz = jx + 64;
@@ -550,9 +547,10 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
         (unsigned short *)(smem + L.off_code) +
         warp * ((MARK || (MARKC && !msort)) ? 1024 : msort ? GBP_MARKC_CODES : 2048);
 
-    lut_compact(a.ax[0].lut, T0, a.ax[0].hi, a.ax[0].lo, nb0, s_l0, s_hl0, s_qb, tid, GBP_BLOCK);
-    if (TWO) lut_compact(a.ax[1].lut, T1, a.ax[1].hi, a.ax[1].lo, nb1, s_l1, s_hl1, nullptr, tid,
-                         GBP_BLOCK);
+    lut_compact(a.ax[0].lut, T0, a.ax[0].hi, a.ax[0].lo, nb0, s_l0, s_hl0, SMUF, nullptr, tid,
+                GBP_BLOCK);
+    if (TWO) lut_compact(a.ax[1].lut, T1, a.ax[1].hi, a.ax[1].lo, nb1, s_l1, s_hl1, false, s_hq,
+                         tid, GBP_BLOCK);
     for (int i = tid; i < nb0; i += GBP_BLOCK) {
         s_E0[i] = a.ax[0].E[i];
         s_hi0[i] = a.ax[0].hi[i];
@@ -596,9 +594,9 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
         }
     unsigned w2_binned = 0;  // pairs this warp binned since it last moved (hi, lo) to FP64
     AxisSm A0{nullptr, s_hi0, s_lo0, s_E0, nb0, a.ax[0].S, a.ax[0].B, a.ax[0].vlo, a.ax[0].vhi,
-              s_l0, s_hl0, s_qb};
+              s_l0, s_hl0, nullptr};
     AxisSm A1{nullptr, s_hi1, s_lo1, s_E1, nb1, TWO ? a.ax[1].S : 0, TWO ? a.ax[1].B : 0,
-              TWO ? a.ax[1].vlo : 0.f, TWO ? a.ax[1].vhi : 0.f, s_l1, s_hl1, nullptr};
+              TWO ? a.ax[1].vlo : 0.f, TWO ? a.ax[1].vhi : 0.f, s_l1, s_hl1, s_hq};
     const int stride2 = nb1 + 1;
     unsigned *hl = wh + lane;                       // 1-D: lane-private column
     float *hs = (float *)wh + lane;                 // marked: sums
@@ -1304,22 +1302,16 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                                 const float4 sa4 = lut_entry_c<true>(ea.v0, A0);
                                 const float4 sb4 = lut_entry_c<true>(eb.v0, A0);
                                 const float qa = __fdividef(ea.v1, ea.v0), qb = __fdividef(eb.v1, eb.v0);
-                                const float4 qa4 = lut_entry_c<false>(qa, A1);
-                                const float4 qb4 = lut_entry_c<false>(qb, A1);
+                                const QBin qa4 = lut_q(qa, A1), qb4 = lut_q(qb, A1);
                                 const int bsa = __float_as_int(sa4.x) + (ea.v0 > sa4.y ? 1 : 0);
                                 const int bsb = __float_as_int(sb4.x) + (eb.v0 > sb4.y ? 1 : 0);
-                                const int bqa = __float_as_int(qa4.x) + (qa > qa4.y ? 1 : 0);
-                                const int bqb = __float_as_int(qb4.x) + (qb > qb4.y ? 1 : 0);
-                                const float lwa = bqa > 0 ? A1.hi[bqa - 1] : -3.0e38f;
-                                const float upa = bqa < nb1 ? A1.lo[bqa] : 3.0e38f;
-                                const float lwb = bqb > 0 ? A1.hi[bqb - 1] : -3.0e38f;
-                                const float upb = bqb < nb1 ? A1.lo[bqb] : 3.0e38f;
+                                const int bqa = qa4.b, bqb = qb4.b;
                                 const bool amba = ((ea.v0 > sa4.z) & !(ea.v0 > sa4.y)) |
-                                                  !(qa - lwa > sa4.w) | !(upa - qa > sa4.w) |
-                                                  (qa4.z < -3.0e38f);
+                                                  !(qa - qa4.below > sa4.w) |
+                                                  !(qa4.above - qa > sa4.w) | qa4.walk;
                                 const bool ambb = ((eb.v0 > sb4.z) & !(eb.v0 > sb4.y)) |
-                                                  !(qb - lwb > sb4.w) | !(upb - qb > sb4.w) |
-                                                  (qb4.z < -3.0e38f);
+                                                  !(qb - qb4.below > sb4.w) |
+                                                  !(qb4.above - qb > sb4.w) | qb4.walk;
                                 // (as bin_smu: past the s gate first, then the guard bands)
                                 if (ha && bsa < nb0) {
                                     if (amba) bin_entry(ea, cur_mock);

@@ -11,9 +11,10 @@ struct AxisSm {
     const double *E;
     int nb, S, B;
     float vlo, vhi;
-    const unsigned *l32;    // count kernels: b0 | (threshold-pair index << 16) per slot
+    const unsigned *l32;    // count kernels: b0 | (threshold-pair index << 16) per slot;
+                            // s of (s, mu'): pairs {that word, the slot's q error bound}
     const float2 *hl;       // threshold pairs (thr, lo): nb edges, the top, the always-walk pair
-    const float *qb;        // s_mu: q error bound per slot
+    const float4 *hq;       // q of (s, mu'): {thr, lo, hi of the edge below, lo of the edge above}
 };
 
 __device__ __forceinline__ int lut_slot(float v, const AxisSm &a) {
@@ -27,25 +28,63 @@ __device__ __forceinline__ float4 lut_entry(float v, const AxisSm &a) {
 
 // The same entry from the compact tables: a 4-byte slot word and a shared
 // threshold pair (few distinct addresses, so few bank conflicts).
+// QB: the s table of (s, mu'), whose slot words sit beside the q error bounds.
 template <bool QB>
 __device__ __forceinline__ float4 lut_entry_c(float v, const AxisSm &a) {
     const int s = lut_slot(v, a);
-    const unsigned w = a.l32[s];
+    unsigned w;
+    float qb = 0.f;
+    if (QB) {
+        const uint2 e = ((const uint2 *)a.l32)[s];
+        w = e.x;
+        qb = __uint_as_float(e.y);
+    } else {
+        w = a.l32[s];
+    }
     const float2 t = a.hl[w >> 16];
-    return make_float4(__int_as_float((int)(w & 0xffffu)), t.x, t.y, QB ? a.qb[s] : 0.f);
+    return make_float4(__int_as_float((int)(w & 0xffffu)), t.x, t.y, qb);
 }
 
-// Build the compact tables in shared memory from the float4 table.
+// The q axis of (s, mu'): q's bin, the guard values that q must keep clear of
+// (the upper guard of its bin's lower edge, the lower guard of its upper edge;
+// -3e38 / 3e38 where the bin has none), and whether its slot holds several edges.
+struct QBin {
+    int b;
+    float below, above;
+    bool walk;
+};
+__device__ __forceinline__ QBin lut_q(float q, const AxisSm &Q) {
+    const unsigned w = Q.l32[lut_slot(q, Q)];
+    const float4 t = Q.hq[w >> 16];
+    const bool up = q > t.x;
+    return QBin{(int)(w & 0xffffu) + (up ? 1 : 0), up ? t.x : t.z, up ? t.w : t.y,
+                t.y < -3.0e38f};
+}
+
+// Build the compact tables in shared memory from the float4 table.  With qb
+// the slot words are written as pairs {word, q error bound} (the s table of
+// (s, mu')); with hq the threshold table is the q table's float4 form.
 __device__ __forceinline__ void lut_compact(const float4 *lut, int T, const float *hi,
                                             const float *lo, int nb, unsigned *l32, float2 *hl,
-                                            float *qb, int tid, int nthr) {
+                                            bool qb, float4 *hq, int tid, int nthr) {
     for (int s = tid; s < T; s += nthr) {
         const float4 e = lut[s];
         const int b0 = __float_as_int(e.x);
         // simple slot: (hi[b0], lo[b0]); top: (inf, inf) at nb; always-walk: (inf, -inf) at nb + 1
-        const int h = (b0 < nb && e.z == -INFINITY) ? nb + 1 : b0;
-        l32[s] = (unsigned)b0 | ((unsigned)h << 16);
-        if (qb) qb[s] = e.w;
+        const unsigned h = (b0 < nb && e.z == -INFINITY) ? nb + 1 : b0;
+        const unsigned word = (unsigned)b0 | (h << 16);
+        if (qb) ((uint2 *)l32)[s] = make_uint2(word, __float_as_uint(e.w));
+        else l32[s] = word;
+    }
+    if (hq) {
+        for (int k = tid; k < nb; k += nthr)
+            hq[k] = make_float4(hi[k], lo[k], k > 0 ? hi[k - 1] : -3.0e38f,
+                                k + 1 < nb ? lo[k + 1] : 3.0e38f);
+        if (tid == 0) {
+            hq[nb] = make_float4(INFINITY, 3.0e38f, nb > 0 ? hi[nb - 1] : -3.0e38f, 3.0e38f);
+            hq[nb + 1] = make_float4(INFINITY, -INFINITY, -3.0e38f, 3.0e38f);
+        }
+        return;
     }
     for (int k = tid; k < nb; k += nthr) hl[k] = make_float2(hi[k], lo[k]);
     if (tid == 0) {

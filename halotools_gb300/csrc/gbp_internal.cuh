@@ -144,7 +144,7 @@ struct CountArgs {
 // jw: bytes of staged weights per j-point (marked mode), copies: shared
 // histogram copies (2-D and wide 1-D modes).
 struct SmemLayout {
-    int off_lut0, off_lut1, off_qb, off_hl0, off_hl1, off_j, off_j2, off_jw, off_q, off_code, off_rec, off_rq,
+    int off_lut0, off_lut1, off_hl0, off_hl1, off_j, off_j2, off_jw, off_q, off_code, off_rec, off_rq,
         off_D, off_E0, off_E1, off_hi0, off_lo0, off_hi1, off_lo1, off_off, off_hist, total;
 };
 
@@ -210,12 +210,13 @@ __host__ __device__ inline SmemLayout gbp_smem_layout(int mode, int T0, int T1, 
     // {b0 | threshold-pair index << 16} and the threshold pairs (hi, lo)
     const bool adj = mode == MODE_ADJ || mode == MODE_POBJ || mode == MODE_NEIGH ||
                      mode == MODE_ADJC;  // gather kernels
-    L.off_lut0 = o; o += adj ? T0 * 16 : gbp_align(T0 * 4, 16);
-    L.off_lut1 = o; o += adj ? T1 * 16 : gbp_align(T1 * 4, 16);
+    // ((s, mu'): the s words paired with the q error bounds; the q thresholds as
+    // float4 {thr, lo, hi below, lo above})
     const bool smu = gbp_mode_smu(mode);
-    L.off_qb = o; o += smu ? gbp_align(T0 * 4, 16) : 0;
+    L.off_lut0 = o; o += adj ? T0 * 16 : gbp_align(T0 * (smu ? 8 : 4), 16);
+    L.off_lut1 = o; o += adj ? T1 * 16 : gbp_align(T1 * 4, 16);
     L.off_hl0 = o; o += adj ? 0 : gbp_align((nb0 + 2) * 8, 16);
-    L.off_hl1 = o; o += adj ? 0 : gbp_align((nb1 + 2) * 8, 16);
+    L.off_hl1 = o; o += adj ? 0 : gbp_align((nb1 + 2) * (smu ? 16 : 8), 16);
     const int jb = mode == MODE_ADJC ? GBP_ADJC_BATCHES : 1;  // j batches staged at once
     L.off_j = o; o += jb * GBP_JCAP * 16;   // adjoint: float4 per j; count: x, y, z, index arrays
     L.off_j2 = o; o += GBP_JCAP * 24;   // (x,x,y,y), (z,z) per j
