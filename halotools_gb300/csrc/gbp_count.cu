@@ -46,8 +46,9 @@ struct PairV {
     int tg;   // weighted jackknife: tag_i | tag_j << 16
 };
 struct Ix {
-    const int *ui;  // sorted index of each i-slot
-    const int *jw;  // sorted index of each j-slot
+    const float4 *u;  // i-slots {x, y, z, sorted index bits}
+    const int *jw;    // sorted index of each j-slot
+    __device__ __forceinline__ int ui(int s) const { return __float_as_int(u[s].w); }
 };
 
 // ---------------- stage 2: 1-D (3-D separation) ----------------
@@ -85,7 +86,7 @@ __device__ __forceinline__ void bin_3d(const PairV &p, HT *h, const AxisSm &A, c
     int b = __float_as_int(t.x) + (v > t.y ? 1 : 0);
     if ((v > t.z) & !(v > t.y)) {
         int k[2];
-        int n = slow_3d(v, __float_as_int(t.x), ix.ui[p.iu], ix.jw[p.jj], sym, k, A, a);
+        int n = slow_3d(v, __float_as_int(t.x), ix.ui(p.iu), ix.jw[p.jj], sym, k, A, a);
         if (n == 0) {
             b = k[0];
         } else {
@@ -113,7 +114,7 @@ __device__ __forceinline__ void bin_jack(const PairV &p, int ti, int tj, unsigne
     int b = __float_as_int(t.x) + (v > t.y ? 1 : 0);
     if ((v > t.z) & !(v > t.y)) {
         int k[2];
-        const int n = slow_3d(v, __float_as_int(t.x), ix.ui[p.iu], ix.jw[p.jj], p.sym, k, A, a);
+        const int n = slow_3d(v, __float_as_int(t.x), ix.ui(p.iu), ix.jw[p.jj], p.sym, k, A, a);
         if (n == 0) {
             b = k[0];
         } else {
@@ -148,7 +149,7 @@ __device__ __forceinline__ void bin_mark(const PairV &p, float *hs, float *hc, c
     int b = __float_as_int(t.x) + (v > t.y ? 1 : 0);
     if ((v > t.z) & !(v > t.y)) {
         int k[2];
-        int n = slow_3d(v, __float_as_int(t.x), ix.ui[p.iu], ix.jw[p.jj], sym, k, A, a);
+        int n = slow_3d(v, __float_as_int(t.x), ix.ui(p.iu), ix.jw[p.jj], sym, k, A, a);
         if (n == 0) {
             b = k[0];
         } else {
@@ -213,7 +214,7 @@ __device__ __forceinline__ void bin_3dw(const PairV &p, const WSink &ws, const A
     int b = __float_as_int(t.x) + (v > t.y ? 1 : 0);
     if ((v > t.z) & !(v > t.y)) {
         int k[2];
-        const int n = slow_3d(v, __float_as_int(t.x), ix.ui[p.iu], ix.jw[p.jj], p.sym, k, A, a);
+        const int n = slow_3d(v, __float_as_int(t.x), ix.ui(p.iu), ix.jw[p.jj], p.sym, k, A, a);
         if (n == 0) {
             b = k[0];
         } else {
@@ -292,7 +293,7 @@ __device__ __forceinline__ void bin_xyz(const PairV &p, HT *hw, const WSink &ws,
     int bb = __float_as_int(e1.x) + (v1 > e1.y ? 1 : 0);
     bool amb = ((v0 > e0.z) & !(v0 > e0.y)) | ((v1 > e1.z) & !(v1 > e1.y));
     if (amb) {
-        slow_xyz<HT, CNT, X>(v0, v1, __float_as_int(e0.x), __float_as_int(e1.x), ix.ui[p.iu],
+        slow_xyz<HT, CNT, X>(v0, v1, __float_as_int(e0.x), __float_as_int(e1.x), ix.ui(p.iu),
                               ix.jw[p.jj], sym, p.w, p.tg, hw, ws, stride, A, Bx, a);
         return;
     }
@@ -380,7 +381,7 @@ __device__ __forceinline__ void bin_smu(const PairV &p, HT *hw, const WSink &ws,
     bool amb = ((v > e0.z) & !(v > e0.y)) | !(q - e1.below > qb) | !(e1.above - q > qb) |
                e1.walk;
     if (amb) {
-        slow_smu<HT, CNT, X>(v, q, qb, __float_as_int(e0.x), ix.ui[p.iu], ix.jw[p.jj], sym, p.w,
+        slow_smu<HT, CNT, X>(v, q, qb, __float_as_int(e0.x), ix.ui(p.iu), ix.jw[p.jj], sym, p.w,
                               hw, ws, stride, A, Q, rq, a);
         return;
     }
@@ -521,9 +522,8 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
     int *s_off = (int *)(smem + L.off_off);
     unsigned *s_hist = (unsigned *)(smem + L.off_hist);
     // this warp's 64 i-points (and their weights) for stage 2, at slots gbp_uslot(iu)
-    float *ux = (float *)(smem + L.off_q) + warp * 4 * GBP_USLOTS;
-    float *uy = ux + GBP_USLOTS, *uz = ux + 2 * GBP_USLOTS;
-    int *uix = (int *)(ux + 3 * GBP_USLOTS);
+    // this warp's i-slots {x, y, z, sorted index bits}: one 16-byte load per pair end
+    float4 *u4 = (float4 *)(smem + L.off_q) + warp * GBP_USLOTS;
     float *s_uw = (float *)(smem + L.off_q + GBP_WARPS * GBP_USLOTS * 16) +
                   warp * GBP_USLOTS * (COLS ? ncol : 1);
     // MARKC per-round form (up to 4 or over 16 channels): this warp's binned pairs
@@ -540,7 +540,7 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
           (unsigned *)(smem + L.off_rq + GBP_WARPS * GBP_RQCAP * 16) + warp, 0u};
     double *s_uw64 = (double *)(smem + L.off_q + GBP_WARPS * GBP_USLOTS * 16) +
                      warp * GBP_USLOTS * (nw > 0 ? nw : 1);
-    const Ix ix{uix, jix};
+    const Ix ix{u4, jix};
     // this warp's pair codes of one 32-point j batch: at most 64 x 32 (marked
     // modes other than the sorted channel form: one i-point at a time, 32 x 32)
     unsigned short *s_code =
@@ -753,8 +753,8 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
         if (lane + 32 < icnt) u1 = a.pos1[ifirst + 32 + lane];
         const int is0 = __float_as_int(u0.w), is1 = __float_as_int(u1.w);
         const unsigned long long UX = pk2(u0.x, u1.x), UY = pk2(u0.y, u1.y), UZ = pk2(u0.z, u1.z);
-        ux[lane] = u0.x; uy[lane] = u0.y; uz[lane] = u0.z; uix[lane] = is0;
-        ux[lane + 48] = u1.x; uy[lane + 48] = u1.y; uz[lane + 48] = u1.z; uix[lane + 48] = is1;
+        u4[lane] = u0;
+        u4[lane + 48] = u1;
         float w0 = 0.f, w1 = 0.f;
         double wa[5] = {0, 0, 0, 0, 0}, wb[5] = {0, 0, 0, 0, 0};
         if (JACK || JACK2) {
@@ -915,7 +915,7 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                     const float4 tj = make_float4(jtx, jty, jtz, 0.f);
                     unsigned mine = 0u;
                     for (int i = 0; i < icnt; i++) {
-                        const float4 ui = make_float4(ux[i], uy[i], uz[i], 0.f);
+                        const float4 ui = u4[i];
                         const unsigned in = __ballot_sync(FULL, (int)out_bits<MODE>(ui, tj, R0, R1) >= 0);
                         if (lane == i) mine = in;
                     }
@@ -1034,7 +1034,8 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                     __syncwarp();
                     auto entry = [&](int code) {
                         const int iu = code & 127, jj = code >> 7;
-                        const float dx = ux[iu] - jx[jj], dy = uy[iu] - jy[jj], dz = uz[iu] - jz[jj];
+                        const float4 ui = u4[iu];
+                        const float dx = ui.x - jx[jj], dy = ui.y - jy[jj], dz = ui.z - jz[jj];
                         float v0, v1 = 0.f, wt = 0.f;
                         if (XYZF) {
                             v0 = fmaf(dy, dy, dx * dx);
@@ -1080,7 +1081,7 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                                 b0 = __float_as_int(t.x) + (e.v0 > t.y ? 1 : 0);
                                 if ((e.v0 > t.z) & !(e.v0 > t.y)) {
                                     int k[2];
-                                    const int n = slow_3d(e.v0, __float_as_int(t.x), ix.ui[iu],
+                                    const int n = slow_3d(e.v0, __float_as_int(t.x), ix.ui(iu),
                                                           ix.jw[jj], e.sym, k, A0, a);
                                     b0 = k[0];
                                     if (n == 2) {
@@ -1120,7 +1121,7 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                                 b0 = __float_as_int(t.x) + (e.v0 > t.y ? 1 : 0);
                                 if ((e.v0 > t.z) & !(e.v0 > t.y)) {
                                     int k[2];
-                                    const int n = slow_3d(e.v0, __float_as_int(t.x), ix.ui[e.iu],
+                                    const int n = slow_3d(e.v0, __float_as_int(t.x), ix.ui(e.iu),
                                                           ix.jw[e.jj], e.sym, k, A0, a);
                                     b0 = k[0];
                                     if (n == 2) {
