@@ -1223,9 +1223,23 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                         for (int b = lane; b < nb0; b += 32) s_cnt[b] = 0;
                         __syncwarp();
                     } else {
-                        for (int r0 = 0; r0 < C; r0 += 64) {
-                            const int sa = r0 + lane, sb = sa + 32;
-                            const bool ha = sa < C, hb = sb < C;
+                        // lanes in GR regions of WL: lane (g, o) bins codes
+                        // g * R / GR + t * WL + o at steps t (R = C rounded up to 32), so
+                        // one instruction's lanes hold pairs of GR distant i-points
+                        // (GR = 1: 32 consecutive codes).  The weighted 2-D sums add into
+                        // the CTA's shared (hi, lo) pairs, where lanes of one i-point
+                        // (same direction, so often the same bin) serialise: spread out,
+                        // weighted (s, mu') took 65.7 -> 63.2 ms and weighted (rp, pi)
+                        // 67.5 -> 66.4 ms on 10M points.  The plain counts lose (the
+                        // 10M (s, mu') count 30.1 -> 30.9-31.3 ms at 2-32 regions): there
+                        // one i-point's table and position loads are broadcasts.
+                        constexpr int GR = MODE == MODE_SMUW ? 32 : MODE == MODE_XYZW ? 4 : 1;
+                        constexpr int WL = 32 / GR;
+                        const int rend = GR == 1 ? C : ((C + 31) & ~31);
+                        const int rbase = GR == 1 ? lane : (lane / WL) * (rend / GR) + (lane % WL);
+                        for (int r0 = 0; r0 < rend; r0 += 64) {
+                            const int sa = rbase + r0 / GR, sb = sa + WL;
+                            const bool ha = sa < C, hb = (GR == 1 || r0 + 32 < rend) && sb < C;
                             const PairV ea = entry(ha ? s_code[sa] : 0);
                             const PairV eb = entry(hb ? s_code[sb] : 0);
                             if (MODE == MODE_3D) {
