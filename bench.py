@@ -931,17 +931,34 @@ def main():
                 "candidate_pairs": st["candidate_pairs"], "recheck_pairs": st["recheck_pairs"],
                 "grid_cells": st["cells"], "reach": st["reach"], "block": st["block"],
                 "stencil_cells": st["stencil_cells"]}
-    tf = os.path.join(ROOT, "profiles", "k_count_dram_traffic.json")
+    # figures of one ncu capture of the count kernel per workload (profiles/*.md)
+    tf = os.path.join(ROOT, "profiles", "k_count_ncu.json")
+    ncu_fig = {}
     if os.path.exists(tf):
         try:
-            roofline["traffic"] = json.load(open(tf)).get(args.workload)
+            ncu_fig = json.load(open(tf)).get(args.workload) or {}
         except Exception:
-            pass
+            ncu_fig = {}
+    roofline["traffic"] = ncu_fig.get("dram_bytes")
     # diagnostics: the FP64 recheck rate, and the count kernel's DRAM rate from the
     # ncu traffic figure over its live time (far below HBM: the kernel is issue-bound)
     roofline["recheck_fraction"] = st["recheck_pairs"] / pairs_step if pairs_step else None
     if roofline["traffic"]:
         roofline["hbm_gbs"] = roofline["traffic"] / (cnt_ms * 1e-3) / 1e9
+    # the limit the kernel actually meets: instruction issue (one warp instruction
+    # per scheduler per cycle, 4 schedulers per SM, at the SM clock sampled during
+    # the timed region); warp instructions per launch from the ncu capture
+    sm_mhz = clk.summary().get("sm_mhz")
+    wi = ncu_fig.get("warp_instructions")
+    if wi and sm_mhz:
+        nsm = torch.cuda.get_device_properties(dev).multi_processor_count
+        peak_issue = nsm * 4 * sm_mhz * 1e6
+        roofline["issue"] = {"warp_instructions_per_launch": wi,
+                             "achieved": wi / (cnt_ms * 1e-3), "peak": peak_issue,
+                             "unit": "warp instructions/s",
+                             "frac": wi / (cnt_ms * 1e-3) / peak_issue,
+                             "source": "smsp__inst_executed.sum of one ncu capture "
+                                       "(profiles/k_count_ncu.json)"}
 
     line = {"metric": metric, "value": value, "unit": "pairs/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_s / args.steps * 1e3,
