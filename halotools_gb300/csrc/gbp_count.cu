@@ -547,6 +547,15 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
         (unsigned short *)(smem + L.off_code) +
         warp * ((MARK || (MARKC && !msort)) ? 1024 : msort ? GBP_MARKC_CODES : 2048);
 
+    // 3-D: each slot's threshold pair beside its word, so that the two loads of
+    // a lookup are independent (the shared pair of the compact form is read
+    // through the word: 20.49 -> 20.30 ms on the 10M-point count)
+    float2 *s_t0 = (float2 *)(smem + L.off_lut0 + gbp_align(T0 * 4, 16));
+    if (MODE == MODE_3D)
+        for (int i = tid; i < T0; i += GBP_BLOCK) {
+            const float4 e = a.ax[0].lut[i];
+            s_t0[i] = make_float2(e.y, e.z);
+        }
     lut_compact(a.ax[0].lut, T0, a.ax[0].hi, a.ax[0].lo, nb0, s_l0, s_hl0, SMUF, nullptr, tid,
                 GBP_BLOCK);
     if (TWO) lut_compact(a.ax[1].lut, T1, a.ax[1].hi, a.ax[1].lo, nb1, s_l1, s_hl1, false, s_hq,
@@ -1245,8 +1254,11 @@ __global__ void __launch_bounds__(GBP_BLOCK, 2) k_count(const CountArgs a) {
                             if (MODE == MODE_3D) {
                                 // both pairs' table lookups first (independent chains
                                 // the scheduler can overlap), then the updates
-                                const float4 ta = lut_entry_c<false>(ea.v0, A0);
-                                const float4 tb = lut_entry_c<false>(eb.v0, A0);
+                                const int qa = lut_slot(ea.v0, A0), qb = lut_slot(eb.v0, A0);
+                                const unsigned wa = s_l0[qa], wb = s_l0[qb];
+                                const float2 pa = s_t0[qa], pb = s_t0[qb];
+                                const float4 ta = make_float4(__int_as_float((int)(wa & 0xffffu)), pa.x, pa.y, 0.f);
+                                const float4 tb = make_float4(__int_as_float((int)(wb & 0xffffu)), pb.x, pb.y, 0.f);
                                 const bool sla = (ea.v0 > ta.z) & !(ea.v0 > ta.y);
                                 const bool slb = (eb.v0 > tb.z) & !(eb.v0 > tb.y);
                                 const int ba = __float_as_int(ta.x) + (ea.v0 > ta.y ? 1 : 0);

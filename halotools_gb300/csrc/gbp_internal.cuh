@@ -213,7 +213,11 @@ __host__ __device__ inline SmemLayout gbp_smem_layout(int mode, int T0, int T1, 
     // ((s, mu'): the s words paired with the q error bounds; the q thresholds as
     // float4 {thr, lo, hi below, lo above})
     const bool smu = gbp_mode_smu(mode);
-    L.off_lut0 = o; o += adj ? T0 * 16 : gbp_align(T0 * (smu ? 8 : 4), 16);
+    // (3-D counts: the slot words, then each slot's own threshold pair)
+    const bool lutd = mode == MODE_3D;
+    L.off_lut0 = o;
+    o += adj ? T0 * 16 : lutd ? gbp_align(T0 * 4, 16) + gbp_align(T0 * 8, 16)
+                              : gbp_align(T0 * (smu ? 8 : 4), 16);
     L.off_lut1 = o; o += adj ? T1 * 16 : gbp_align(T1 * 4, 16);
     L.off_hl0 = o; o += adj ? 0 : gbp_align((nb0 + 2) * 8, 16);
     L.off_hl1 = o; o += adj ? 0 : gbp_align((nb1 + 2) * (smu ? 16 : 8), 16);
