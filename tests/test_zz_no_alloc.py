@@ -4,12 +4,12 @@ gbp_npairs_3d_static serves callers that cannot allocate device memory while
 they count (their device memory belongs to another framework's caching
 allocator, or a cudaMalloc/cudaFree would stall a latency-critical loop): all
 its scratch is one static device array inside the library.  These tests call
-it through the C ABI: twice in a row on different samples (periodic and not),
-each against the oracle's integer counts, so a call must not see the previous
-call's leftovers; with a point outside the box (every count -1, and the next
-call clean again); checking that free device memory does not move across a
-call; and on a stream being captured (refused).  The file is collected last
-on purpose.
+it through the C ABI: three times in a row on different samples (periodic and
+not), each against the oracle's integer counts and the allocating entry
+point's, so a call must not see the previous call's leftovers; with a point
+outside the box (every count -1, and the next call clean again); checking
+that free device memory does not move across a call; and on a stream being
+captured (refused).  The file is collected last on purpose.
 """
 import ctypes
 
@@ -57,6 +57,8 @@ def test_static_entry_matches_oracle_twice(gpu):
         want = oracle.npairs_3d(x, x, rb, period=L if pbc else None, num_threads=8)
         got = _static_counts(lib, torch.from_numpy(x).cuda(), rb, [L] * 3, pbc, stream)
         assert np.array_equal(got, want), (pbc, got, want)
+        # and the allocating entry point (gbp_npairs_3d behind npairs_3d) agrees
+        assert np.array_equal(got, gpu.npairs_3d(x, x, rb, period=L if pbc else None))
 
 
 def test_static_entry_out_of_box_gives_minus_one_then_recovers(gpu):
