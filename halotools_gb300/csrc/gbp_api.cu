@@ -802,7 +802,7 @@ int gbp_npairs_3d(gbp_plan *plan, const double *xyz1, int64_t n1, const double *
     c.mem = mem;
     c.naxes = 1;
     choose_grid(c.g, period3, search, pbc, n2, plan->reach, MAX_CELLS_PER_DIM, 0.0, plan->block,
-                GBP_DENSE_REACH2);
+                GBP_DENSE_REACH2, c.mode == MODE_3D);
     build_stencil(c.g, search, 0, c.autocorr);
     ErrModel em = err_model(c.g);
     std::vector<double> E(nb);
@@ -1039,7 +1039,7 @@ static int setup_smu(gbp_plan *plan, Call &c, const double *xyz1, int64_t n1, co
     c.mem = mem;
     c.naxes = 2;
     choose_grid(c.g, period3, search, pbc, n2, plan->reach, MAX_CELLS_PER_DIM, 0.0, plan->block,
-                c.mode == MODE_SMU ? GBP_DENSE_REACH2 : 28.0);
+                c.mode == MODE_SMU ? GBP_DENSE_REACH2 : 28.0, c.mode == MODE_SMU);
     build_stencil(c.g, search, 0, c.autocorr);
     ErrModel em = err_model(c.g);
     std::vector<double> Es(n_s), Em(n_mu), Eps(n_s), Epm(n_mu);

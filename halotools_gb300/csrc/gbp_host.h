@@ -238,10 +238,15 @@ inline bool grid_for_reach(int K, const double L[3], const double search[3], int
 // occupancy)), at most 4), so that an item's i-points come from a block while
 // its j-cells hug the block's search region; with ppc > 0, single cells larger
 // than the search holding about ppc points instead.  ppc < 0 disables both.
-// bf_hint > 0 forces the block factor (when the grid allows it).
+// bf_hint > 0 forces the block factor (when the grid allows it).  With split,
+// an automatic choice of reach 2 becomes reach 4 in blocks of 2^3 cells: the
+// items' i-points come from the same reach-2-sized blocks, while the j side is
+// pruned at half the cell size (on 10M clustered points 12.7e9 -> 11.1e9
+// candidates, the 3-D count 20.30 -> 19.47 ms and the (s, mu') count 30.1 ->
+// 29.0 ms; reach 3 in blocks of 2, 20.25 ms; reach 4 in blocks of 4, 20.21 ms).
 inline void choose_grid(Geometry &g, const double L[3], const double search[3], int pbc,
                         int64_t n2, int reach_hint, int64_t cap_per_dim, double ppc = 0.0,
-                        int bf_hint = 0, double dense = 28.0) {
+                        int bf_hint = 0, double dense = 28.0, bool split = false) {
     for (int d = 0; d < 3; d++) g.L[d] = L[d];
     g.pbc = pbc;
     double vol = L[0] * L[1] * L[2];
@@ -256,6 +261,17 @@ inline void choose_grid(Geometry &g, const double L[3], const double search[3], 
             continue;
         }
         if (rho * cvol >= dense) best = K;
+    }
+    bool split4 = false;
+    if (split && reach_hint <= 0 && bf_hint <= 0 && best == 2) {
+        // reach 4 in blocks of 2: feasible when the blocks tile the grid, the
+        // stencil's block offsets (DB = 2) reach distinct blocks and its runs fit
+        int64_t n4[3];
+        split4 = grid_for_reach(4, L, search, pbc, n4, cap_per_dim) &&
+                 5 * 5 * 5 * 2 * 2 <= GBP_STEN_CAP;
+        for (int d = 0; d < 3 && split4; d++)
+            if (n4[d] / 2 < 1 || (pbc && n4[d] / 2 < 5)) split4 = false;
+        if (split4) best = 4;
     }
     int64_t n[3];
     grid_for_reach(best, L, search, pbc, n, cap_per_dim);
@@ -276,6 +292,8 @@ inline void choose_grid(Geometry &g, const double L[3], const double search[3], 
         }
     } else if (bf_hint > 0) {
         bf = bf_hint;
+    } else if (split4) {
+        bf = 2;
     }
     bf = std::max(1, std::min(bf, 4));
     // blocks must tile the grid and, with periodic wrap, every block offset of
