@@ -753,6 +753,33 @@ int gbp_plan_set_block(gbp_plan *plan, int block) {
     return GBP_OK;
 }
 
+int gbp_grid_describe(const double *period3, int32_t pbc, const double *search3, int64_t n2,
+                      int32_t kind, int32_t reach, int32_t block, int32_t *out) {
+    if (!period3 || !search3 || !out || n2 < 0 || kind < 0 || kind > 2 || reach < 0 || reach > 4 ||
+        block < 0 || block > 4)
+        return GBP_ERR_INVALID;
+    for (int d = 0; d < 3; d++)
+        if (!(period3[d] > 0.0) || !std::isfinite(period3[d]) || !(search3[d] > 0.0) ||
+            !(search3[d] * 3.0 <= period3[d]))
+            return GBP_ERR_RANGE;
+    // the choices of the entry points: npairs_3d (up to GBP_NB_LANE edges) and
+    // npairs_s_mu take finer grids for dense samples, npairs_xy_z the default
+    Geometry g;
+    if (kind == 2) {
+        choose_grid(g, period3, search3, pbc, n2, reach, MAX_CELLS_PER_DIM, 0.0, block);
+    } else {
+        choose_grid(g, period3, search3, pbc, n2, reach, MAX_CELLS_PER_DIM, 0.0, block,
+                    GBP_DENSE_REACH2, true);
+    }
+    build_stencil(g, search3, kind == 2 ? 1 : 0, true);
+    out[0] = g.K;
+    out[1] = g.bf;
+    for (int d = 0; d < 3; d++) out[2 + d] = g.n[d];
+    out[5] = g.nsten;
+    out[6] = g.DB;
+    return GBP_OK;
+}
+
 int gbp_plan_set_graph(gbp_plan *plan, int enable) {
     if (!plan) return GBP_ERR_INVALID;
     plan->graph_mode = enable != 0;

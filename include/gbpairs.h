@@ -67,8 +67,19 @@ int gbp_plan_set_stream(gbp_plan *plan, void *cuda_stream);
 /* Force the stencil reach (1..4 cells per search length); 0 = automatic. */
 int gbp_plan_set_reach(gbp_plan *plan, int reach);
 /* Force the block factor of the two-level grid (1..4 fine cells per block
- * edge; 1 = plain cell list); 0 = automatic (blocks for sparse samples). */
+ * edge; 1 = plain cell list); 0 = automatic (blocks for sparse samples; for
+ * dense npairs_3d and npairs_s_mu samples, reach 4 in blocks of 2). */
 int gbp_plan_set_block(gbp_plan *plan, int block);
+/* The cell grid a call would choose, computed on the host without a GPU (no
+ * reference counterpart: the reference's mesh is RectangularDoubleMesh,
+ * rectangular_mesh.py:228, which the GPU grid replaces).  kind: 0 npairs_3d
+ * (up to 64 edges), 1 npairs_s_mu, 2 npairs_xy_z; search3: the largest
+ * separation searched per dimension (each at most a third of the period);
+ * n2: points of sample 2; reach, block: the plan's hints (0 = automatic).
+ * out[0..6] = reach, block factor, fine cells per dimension (3), stencil runs,
+ * block reach.  GBP_ERR_RANGE for a search longer than a third of the box. */
+int gbp_grid_describe(const double *period3, int32_t pbc, const double *search3, int64_t n2,
+                      int32_t kind, int32_t reach, int32_t block, int32_t *out);
 /* 1: capture each call's stream work into one CUDA graph (instantiated once,
  * updated in place on later calls) and launch that; 0: launch directly. */
 int gbp_plan_set_graph(gbp_plan *plan, int enable);
