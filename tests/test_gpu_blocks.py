@@ -179,3 +179,39 @@ def test_marked_channels_cross_nonperiodic_and_ones(gpu):
                                          weights2=np.ones((len(s2), 2)))
     cnt = gpu.npairs_3d(s1, s2, rb).astype(np.float64)
     assert np.array_equal(ones[0], cnt) and np.array_equal(ones[1], cnt)
+
+
+@pytest.mark.parametrize("pbc", [True, False])
+def test_dense_sample_takes_reach_4_blocks_by_default(gpu, pbc):
+    # 37 points per reach-2 cell: npairs_3d and npairs_s_mu choose reach 4 in
+    # blocks of 2 on their own (periodic, and over the enclosing box)
+    rng = np.random.default_rng(15)
+    L = 100.0
+    s = clustered(rng, 300000, L, 6000, mhi=13.5)
+    rb = np.logspace(-1, 1, 12)
+    per = L if pbc else None
+    got = gpu.npairs_3d(s, s, rb, period=per)
+    st = gpu.default_plan().stats()
+    assert (st["reach"], st["block"]) == (4, 2)
+    assert np.array_equal(got, oracle.npairs_3d(s, s, rb, period=per, num_threads=8))
+    sb = np.logspace(np.log10(0.5), 1, 11)
+    mu = np.linspace(0, 1, 11)
+    got = gpu.npairs_s_mu(s, s, sb, mu, period=per)
+    st = gpu.default_plan().stats()
+    assert (st["reach"], st["block"]) == (4, 2)
+    assert np.array_equal(got, oracle.npairs_s_mu(s, s, sb, mu, period=per, num_threads=8))
+
+
+def test_reach_4_blocks_cross_counts(gpu):
+    # two samples: the stencil covers the whole neighbourhood of each block
+    rng = np.random.default_rng(16)
+    L = 120.0
+    s1 = clustered(rng, 40000, L, 2000)
+    s2 = rng.uniform(0, L, (70000, 3))
+    rb = np.logspace(-1, np.log10(12), 14)
+    want = oracle.npairs_3d(s1, s2, rb, period=L, num_threads=8)
+    with forced(gpu, 2, 4) as plan:
+        got = gpu.npairs_3d(s1, s2, rb, period=L)
+        st = plan.stats()
+    assert (st["reach"], st["block"]) == (4, 2)
+    assert np.array_equal(got, want)
