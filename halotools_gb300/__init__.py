@@ -58,10 +58,18 @@ _BINDINGS = tuple([
     ("halotools.mock_observables.isolation_functions", "conditional_cylindrical_isolation",
      conditional_cylindrical_isolation),
 ] + [
-    # the intrinsic-alignment estimators bind marked_npairs_xy_z at import time
-    ("halotools.mock_observables.ia_correlations." + m, "marked_npairs_xy_z", marked_npairs_xy_z)
+    # the intrinsic-alignment estimators bind their plain and marked counters at
+    # import time (their positional marked counters have no GPU form here and
+    # stay halotools' own); a name a module does not import is left alone
+    ("halotools.mock_observables.ia_correlations." + m, attr, fn)
     for m in ("ee_projected", "ed_projected", "ii_plus_projected", "ii_minus_projected",
               "gi_plus_projected", "gi_minus_projected")
+    for attr, fn in (("marked_npairs_xy_z", marked_npairs_xy_z), ("npairs_xy_z", npairs_xy_z))
+] + [
+    ("halotools.mock_observables.ia_correlations." + m, attr, fn)
+    for m in ("ee_3d", "ed_3d", "ee_3d_one_two_halo_decomp", "ed_3d_one_two_halo_decomp",
+              "ii_plus_3d", "ii_minus_3d", "gi_plus_3d", "gi_minus_3d")
+    for attr, fn in (("marked_npairs_3d", marked_npairs_3d), ("npairs_3d", npairs_3d))
 ] + [
     ("halotools.mock_observables", "npairs_3d", npairs_3d),
     ("halotools.mock_observables", "npairs_xy_z", npairs_xy_z),
