@@ -148,6 +148,20 @@ def _namespace():
     return ns
 
 
+def load_alignments(src_root: str = DEFAULT_SRC):
+    """halotools' own intrinsic-alignment modules whose counters are the plain and
+    marked ones (``ee_3d``, ``ee_projected``), over the reference's counters,
+    loaded without ``ia_correlations/__init__.py`` (whose other modules need the
+    positional marked engines).  Returns {name: module}."""
+    ns = load(src_root)
+    pc = sys.modules["halotools.mock_observables.pair_counters"]
+    for name in ("npairs_3d", "npairs_xy_z", "marked_npairs_3d", "marked_npairs_xy_z"):
+        setattr(pc, name, getattr(ns, name))
+    name = "halotools.mock_observables.ia_correlations"
+    _pkg(name, [os.path.join(src_root, "halotools", "mock_observables", "ia_correlations")])
+    return {m: importlib.import_module(name + "." + m) for m in ("ee_3d", "ee_projected")}
+
+
 def load_estimators(src_root: str = DEFAULT_SRC):
     """halotools' own estimator modules (``tpcf``, ``rp_pi_tpcf``, ``wp``,
     ``s_mu_tpcf``, ``marked_tpcf``) over the reference's counters, loaded

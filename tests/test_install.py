@@ -68,3 +68,52 @@ def test_install_rebinds_halotools_estimators():
 
 def test_install_without_halotools_is_a_noop():
     assert h.install_into_halotools() == []
+
+
+IA_SCRIPT = r"""
+import sys, warnings
+sys.path.insert(0, %(root)r)
+warnings.simplefilter("ignore", SyntaxWarning)
+import numpy as np
+from oracle import ref_loader
+try:
+    ia = ref_loader.load_alignments()
+except Exception as exc:
+    print("SKIP", repr(exc)); sys.exit(0)
+import halotools_gb300 as h
+rng = np.random.default_rng(0)
+x = rng.uniform(0, 100.0, (300, 3))
+o = rng.normal(size=(300, 3))
+rb = np.logspace(-1, 1, 5)
+# before: halotools' own ee_3d over its own engines
+before = ia["ee_3d"].ee_3d(x, o, x, o, rb, period=100.0)
+assert len(before) == len(rb) - 1
+with warnings.catch_warnings(record=True):
+    warnings.simplefilter("always")
+    done = h.install_into_halotools(strict=False)
+pre = "halotools.mock_observables.ia_correlations."
+for m, names in (("ee_3d", ("marked_npairs_3d", "npairs_3d")),
+                 ("ee_projected", ("marked_npairs_xy_z", "npairs_xy_z"))):
+    for a in names:
+        assert getattr(ia[m], a) is getattr(h, a), (m, a)
+        assert pre + m + "." + a in done, (m, a)
+# after: halotools' own ee_3d reaches the GPU counters
+try:
+    ia["ee_3d"].ee_3d(x, o, x, o, rb, period=100.0)
+except h.GBPairsUnavailable:
+    print("ROUTED")
+else:
+    import torch
+    print("ROUTED" if torch.cuda.is_available() else "NOT ROUTED")
+"""
+
+
+def test_install_rebinds_alignment_estimators():
+    # halotools' ee_3d / ee_projected bind their plain and marked counters at
+    # import time (ee_3d.py:15, ee_projected.py:15)
+    r = subprocess.run([sys.executable, "-c", IA_SCRIPT % {"root": ROOT}], capture_output=True,
+                       text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    if r.stdout.startswith("SKIP"):
+        pytest.skip(r.stdout.strip())
+    assert "ROUTED" in r.stdout.split(), r.stdout
