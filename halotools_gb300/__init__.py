@@ -80,6 +80,22 @@ _BINDINGS = tuple([
     ("halotools.mock_observables.two_point_clustering.s_mu_tpcf", "npairs_s_mu", npairs_s_mu),
     ("halotools.mock_observables.two_point_clustering.marked_tpcf", "marked_npairs_3d",
      marked_npairs_3d),
+    ("halotools.mock_observables.two_point_clustering.marked_tpcf", "npairs_3d", npairs_3d),
+    ("halotools.mock_observables.two_point_clustering.angular_tpcf", "npairs_3d", npairs_3d),
+    ("halotools.mock_observables.two_point_clustering.tpcf_one_two_halo_decomp", "npairs_3d",
+     npairs_3d),
+    ("halotools.mock_observables.two_point_clustering.tpcf_one_two_halo_decomp",
+     "marked_npairs_3d", marked_npairs_3d),
+    ("halotools.mock_observables.two_point_clustering.wp_jackknife", "npairs_jackknife_xy_z",
+     npairs_jackknife_xy_z),
+    ("halotools.mock_observables.two_point_clustering.rp_pi_tpcf_jackknife",
+     "npairs_jackknife_xy_z", npairs_jackknife_xy_z),
+    ("halotools.mock_observables.large_scale_density.large_scale_density_spherical_volume",
+     "npairs_per_object_3d", npairs_per_object_3d),
+    ("halotools.mock_observables.large_scale_density.large_scale_density_spherical_annulus",
+     "npairs_per_object_3d", npairs_per_object_3d),
+    ("halotools.mock_observables.void_statistics.underdensity_prob_func",
+     "npairs_per_object_3d", npairs_per_object_3d),
 ])
 
 

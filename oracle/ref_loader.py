@@ -162,6 +162,27 @@ def load_alignments(src_root: str = DEFAULT_SRC):
     return {m: importlib.import_module(name + "." + m) for m in ("ee_3d", "ee_projected")}
 
 
+def load_counter_users(src_root: str = DEFAULT_SRC):
+    """The other halotools modules that bind a counter at import time and load
+    without astropy: ``angular_tpcf`` and ``tpcf_one_two_halo_decomp`` (both over
+    ``npairs_3d``; the latter also ``marked_npairs_3d``), the two large-scale
+    density functions and ``underdensity_prob_func`` (over
+    ``npairs_per_object_3d``).  Returns {name: module}."""
+    load_estimators(src_root)
+    mods = {}
+    tpc = "halotools.mock_observables.two_point_clustering"
+    for m in ("angular_tpcf", "tpcf_one_two_halo_decomp"):
+        mods[m] = importlib.import_module(tpc + "." + m)
+    for pkg, names in (("large_scale_density", ("large_scale_density_spherical_volume",
+                                                "large_scale_density_spherical_annulus")),
+                       ("void_statistics", ("underdensity_prob_func",))):
+        name = "halotools.mock_observables." + pkg
+        _pkg(name, [os.path.join(src_root, "halotools", "mock_observables", pkg)])
+        for m in names:
+            mods[m] = importlib.import_module(name + "." + m)
+    return mods
+
+
 def load_estimators(src_root: str = DEFAULT_SRC):
     """halotools' own estimator modules (``tpcf``, ``rp_pi_tpcf``, ``wp``,
     ``s_mu_tpcf``, ``marked_tpcf``) over the reference's counters, loaded

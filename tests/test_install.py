@@ -117,3 +117,51 @@ def test_install_rebinds_alignment_estimators():
     if r.stdout.startswith("SKIP"):
         pytest.skip(r.stdout.strip())
     assert "ROUTED" in r.stdout.split(), r.stdout
+
+
+USERS_SCRIPT = r"""
+import sys, warnings
+sys.path.insert(0, %(root)r)
+warnings.simplefilter("ignore", SyntaxWarning)
+import numpy as np
+from oracle import ref_loader
+try:
+    mods = ref_loader.load_counter_users()
+except Exception as exc:
+    print("SKIP", repr(exc)); sys.exit(0)
+import halotools_gb300 as h
+with warnings.catch_warnings(record=True):
+    warnings.simplefilter("always")
+    done = h.install_into_halotools(strict=False)
+want = {"angular_tpcf": ("npairs_3d",),
+        "tpcf_one_two_halo_decomp": ("npairs_3d", "marked_npairs_3d"),
+        "large_scale_density_spherical_volume": ("npairs_per_object_3d",),
+        "large_scale_density_spherical_annulus": ("npairs_per_object_3d",),
+        "underdensity_prob_func": ("npairs_per_object_3d",)}
+for m, names in want.items():
+    for a in names:
+        assert getattr(mods[m], a) is getattr(h, a), (m, a)
+        assert any(d.endswith("." + m + "." + a) for d in done), (m, a)
+# halotools' own large-scale density function reaches the GPU per-object counter
+x = np.random.default_rng(0).uniform(0, 100.0, (400, 3))
+try:
+    mods["large_scale_density_spherical_volume"].large_scale_density_spherical_volume(
+        x, x, 5.0, period=100.0)
+except h.GBPairsUnavailable:
+    print("ROUTED")
+else:
+    import torch
+    print("ROUTED" if torch.cuda.is_available() else "NOT ROUTED")
+"""
+
+
+def test_install_rebinds_other_counter_users():
+    # angular_tpcf.py:15, tpcf_one_two_halo_decomp.py:24-25,
+    # large_scale_density_spherical_volume.py:12, ..._annulus.py:12,
+    # underdensity_prob_func.py:12 bind their counters at import time
+    r = subprocess.run([sys.executable, "-c", USERS_SCRIPT % {"root": ROOT}],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    if r.stdout.startswith("SKIP"):
+        pytest.skip(r.stdout.strip())
+    assert "ROUTED" in r.stdout.split(), r.stdout
