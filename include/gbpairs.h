@@ -80,6 +80,17 @@ int gbp_plan_set_block(gbp_plan *plan, int block);
  * block reach.  GBP_ERR_RANGE for a search longer than a third of the box. */
 int gbp_grid_describe(const double *period3, int32_t pbc, const double *search3, int64_t n2,
                       int32_t kind, int32_t reach, int32_t block, int32_t *out);
+/* The FP32 guard thresholds an npairs_3d call (up to 64 edges) compares its
+ * FP32 squared separations with, computed on the host without a GPU (no
+ * reference counterpart; for tests of the error bound).  The grid is the one
+ * gbp_grid_describe gives for kind 0 with search = max(rbins); the squared
+ * edges are walked from the top as npairs_3d_engine.pyx:178-182 does; then
+ * v32 <= lo[k] proves v64 <= rbins[k]^2 and v32 > hi[k] proves v64 > rbins[k]^2
+ * for the FP32 value v32 the count kernel forms from the grid's cell offsets.
+ * cell3: the fine cell size per dimension. */
+int gbp_npairs_3d_thresholds(const double *period3, int32_t pbc, const double *rbins, int32_t nb,
+                             int64_t n2, int32_t reach, int32_t block, float *hi, float *lo,
+                             double *cell3);
 /* 1: capture each call's stream work into one CUDA graph (instantiated once,
  * updated in place on later calls) and launch that; 0: launch directly. */
 int gbp_plan_set_graph(gbp_plan *plan, int enable);

@@ -1,0 +1,159 @@
+"""The FP32 guard band of the count kernels, checked on the host (no GPU).
+
+A pair is counted in bin k iff its FP64 squared separation, formed as
+npairs_3d_engine.pyx:167-176 does ((x1 - shift) - x2 per coordinate, squared
+and summed left to right), is <= fl(rbins[k]^2).  The count kernel decides that
+from an FP32 value instead and sends only pairs between two FP32 thresholds to
+an FP64 recheck: v32 <= lo[k] must prove v64 <= E[k] and v32 > hi[k] must
+prove v64 > E[k].  These tests form v32 exactly as the kernel does (each
+coordinate as an FP32 offset from its block corner, the neighbour block's FP32
+offset added to the j point, the differences squared with fused multiply-adds)
+for adversarial pairs within a few parts per million of every edge, on the
+grids the library chooses, and check both implications against the thresholds
+the library computes (gbp_npairs_3d_thresholds)."""
+import ctypes
+from fractions import Fraction
+
+import numpy as np
+import pytest
+
+from halotools_gb300 import _native as N
+
+LD = np.longdouble
+pytestmark = pytest.mark.skipif(np.finfo(LD).nmant < 60,
+                                reason="needs an extended long double to emulate FMA")
+
+
+def _p(a, t):
+    return a.ctypes.data_as(ctypes.POINTER(t))
+
+
+def grid_and_thresholds(L, rbins, n2, reach=0, block=0):
+    lib = N.load()
+    per = np.array([L] * 3)
+    rb = np.ascontiguousarray(rbins, dtype=np.float64)
+    out = (ctypes.c_int32 * 7)()
+    search = np.array([rb.max()] * 3)
+    assert lib.gbp_grid_describe(_p(per, ctypes.c_double), 1, _p(search, ctypes.c_double), n2,
+                                 0, reach, block, out) == 0
+    hi = np.zeros(len(rb), np.float32)
+    lo = np.zeros(len(rb), np.float32)
+    c = np.zeros(3)
+    assert lib.gbp_npairs_3d_thresholds(_p(per, ctypes.c_double), 1, _p(rb, ctypes.c_double),
+                                        len(rb), n2, reach, block, _p(hi, ctypes.c_float),
+                                        _p(lo, ctypes.c_float), _p(c, ctypes.c_double)) == 0
+    return {"reach": out[0], "bf": out[1], "n": out[2], "DB": out[6], "c": c[0]}, hi, lo
+
+
+def fma32(a, b, c):
+    """fmaf(a, b, c) for float32 arrays: one rounding of a*b + c to float32."""
+    p = a.astype(LD) * b.astype(LD)          # exact: 24 + 24 bits
+    cl = c.astype(LD)
+    s = p + cl
+    z = s - p
+    e = (p - (s - z)) + (cl - z)             # s + e == a*b + c exactly
+    r = s.astype(np.float32)
+    # s exactly halfway between two floats with a nonzero remainder: the
+    # remainder's sign decides (a rare case, settled exactly)
+    d = s - r.astype(LD)
+    half = np.spacing(np.abs(r)).astype(LD) / 2
+    tie = (np.abs(d) == half) & (e != 0)
+    for i in np.flatnonzero(tie):
+        q = Fraction(float(a[i])) * Fraction(float(b[i])) + Fraction(float(c[i]))
+        cand = [r[i], np.nextafter(r[i], np.float32(np.inf)), np.nextafter(r[i], np.float32(-np.inf))]
+        r[i] = min(cand, key=lambda f: abs(Fraction(float(f)) - q))
+    return r
+
+
+def v32_of(xi, xj, g, L, f32_input):
+    """The kernel's FP32 squared separation of i-point xi and j-point xj."""
+    c, bf, n, DB = g["c"], g["bf"], g["n"], g["DB"]
+    nbk = n // bf
+    dv = []
+    for d in range(3):
+        def rel(x):
+            k = np.clip(np.floor(x * (1.0 / c)).astype(np.int64), 0, n - 1)
+            ib = k // bf
+            C = (ib * bf) * c
+            if f32_input:
+                chi = C.astype(np.float32)
+                clo = (C - chi.astype(np.float64)).astype(np.float32)
+                return ((x.astype(np.float32) - chi) - clo).astype(np.float32), ib
+            return (x - C).astype(np.float32), ib
+        ui, bi = rel(xi[:, d])
+        uj, bj = rel(xj[:, d])
+        ox = bj - bi
+        ox = np.where(ox > nbk // 2, ox - nbk, np.where(ox < -(nbk // 2), ox + nbk, ox))
+        assert np.all(np.abs(ox) <= DB)
+        D = (ox * bf * c).astype(np.float32)
+        t = (uj + D).astype(np.float32)
+        dv.append((ui - t).astype(np.float32))
+    dx, dy, dz = dv
+    return fma32(dz, dz, fma32(dy, dy, (dx * dx).astype(np.float32)))
+
+
+def v64_of(xi, xj, L):
+    """npairs_3d_engine.pyx:167-176: (x1 - shift) - x2, squared, summed left to right."""
+    s = np.zeros(len(xi))
+    for d in range(3):
+        best = None
+        for shift in (0.0, L, -L):
+            dd = (xi[:, d] - shift) - xj[:, d]
+            best = dd if best is None else np.where(np.abs(dd) < np.abs(best), dd, best)
+        s = s + best * best if d < 2 else s + best * best
+    return s
+
+
+def adversarial_pairs(rng, L, rbins, npairs, rel, f32_input):
+    """Pairs whose separation lies within `rel` (relative) of a random edge."""
+    k = rng.integers(0, len(rbins), npairs)
+    r = rbins[k] * (1.0 + rng.uniform(-rel, rel, npairs))
+    d = rng.normal(size=(npairs, 3))
+    d /= np.linalg.norm(d, axis=1)[:, None]
+    xi = rng.uniform(0, L, (npairs, 3))
+    xj = np.mod(xi + r[:, None] * d, L)
+    if f32_input:  # the engines upcast float32 exactly
+        xi = xi.astype(np.float32).astype(np.float64)
+        xj = np.minimum(xj.astype(np.float32).astype(np.float64), np.nextafter(L, 0))
+    return xi, xj
+
+
+CASES = [
+    # (box, rbins, points of sample 2, reach hint, block hint, float32 input)
+    (2000.0, np.logspace(np.log10(0.5), np.log10(50), 30), 10_000_000, 0, 0, False),
+    (250.0, np.logspace(-1, np.log10(20), 15), 100_000, 0, 0, False),
+    (1000.0, np.logspace(-1, np.log10(30), 20), 10_000, 0, 0, False),
+    (1000.0, np.logspace(-1, np.log10(20), 15), 2_000_000, 3, 2, True),
+    (420.0, np.logspace(-1, np.log10(20), 15), 30_000, 2, 1, False),
+]
+
+
+@pytest.mark.parametrize("L,rbins,n2,reach,block,f32", CASES)
+def test_fp32_thresholds_bracket_the_fp64_edges(L, rbins, n2, reach, block, f32):
+    g, hi, lo = grid_and_thresholds(L, rbins, n2, reach, block)
+    E = rbins * rbins
+    rng = np.random.default_rng(int(L) + n2 % 1000 + reach)
+    decided = 0
+    for rel in (3e-5, 3e-6, 4e-7):
+        xi, xj = adversarial_pairs(rng, L, rbins, 100_000, rel, f32)
+        for a, b in ((xi, xj), (xj, xi)):  # both orders, as the kernel's symmetric walk
+            v32 = v32_of(a, b, g, L, f32)
+            v64 = v64_of(a, b, L)
+            for k in range(len(E)):
+                inside = v32 <= lo[k]
+                outside = v32 > hi[k]
+                assert np.all(v64[inside] <= E[k]), (k, "inside")
+                assert np.all(v64[outside] > E[k]), (k, "outside")
+                decided += int(np.count_nonzero(inside | outside))
+    assert decided > 0
+
+
+def test_headline_grid_is_the_blocked_one():
+    g, hi, lo = grid_and_thresholds(2000.0, np.logspace(np.log10(0.5), np.log10(50), 30),
+                                    10_000_000)
+    assert (g["reach"], g["bf"], g["n"]) == (4, 2, 160)
+    E = np.logspace(np.log10(0.5), np.log10(50), 30) ** 2
+    assert np.all(lo <= E) and np.all(E <= hi)
+    # the band is narrow at the outer edges, where most pairs lie: a few parts
+    # per million (at the inner edges the offsets' absolute error dominates)
+    assert np.all(((hi - lo) / E)[-5:] < 1e-5)
