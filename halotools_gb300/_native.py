@@ -35,7 +35,7 @@ EXPORTED = (
     "gbp_npairs_jackknife_xy_z_weighted", "gbp_weighted_adjoint_3d_channels",
     "gbp_zheng07_weights_batched", "gbp_zheng07_vjp_batched",
     "gbp_weighted_adjoint_3d", "gbp_zheng07_weights", "gbp_zheng07_vjp", "gbp_plan_set_limits",
-    "gbp_grid_describe", "gbp_npairs_3d_thresholds",
+    "gbp_grid_describe", "gbp_npairs_3d_thresholds", "gbp_npairs_xy_z_thresholds",
 )
 
 
@@ -171,6 +171,9 @@ def load(build_if_missing: bool = True):
         L.gbp_grid_describe.argtypes = [pd, i32, pd, i64, i32, i32, i32, P(ctypes.c_int32)]
         L.gbp_npairs_3d_thresholds.argtypes = [pd, i32, pd, i32, i64, i32, i32,
                                                P(ctypes.c_float), P(ctypes.c_float), pd]
+        pf = P(ctypes.c_float)
+        L.gbp_npairs_xy_z_thresholds.argtypes = [pd, i32, pd, i32, pd, i32, i64, i32, i32,
+                                                 pf, pf, pf, pf, pd]
         _lib = L
         return L
 

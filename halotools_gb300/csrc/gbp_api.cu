@@ -804,6 +804,33 @@ int gbp_npairs_3d_thresholds(const double *period3, int32_t pbc, const double *r
     return GBP_OK;
 }
 
+int gbp_npairs_xy_z_thresholds(const double *period3, int32_t pbc, const double *rp_bins,
+                               int32_t n_rp, const double *pi_bins, int32_t n_pi, int64_t n2,
+                               int32_t reach, int32_t block, float *hi_rp, float *lo_rp,
+                               float *hi_pi, float *lo_pi, double *cell3) {
+    if (!period3 || !rp_bins || !pi_bins || !hi_rp || !lo_rp || !hi_pi || !lo_pi || !cell3 ||
+        n_rp < 2 || n_pi < 2 || n_rp > GBP_NB_MAX || n_pi > GBP_NB_MAX || n2 < 0 || reach < 0 ||
+        reach > 4 || block < 0 || block > 4)
+        return GBP_ERR_INVALID;
+    const double rpm = max_nan(rp_bins, n_rp), pim = max_nan(pi_bins, n_pi);
+    const double search[3] = {rpm, rpm, pim};
+    for (int d = 0; d < 3; d++)
+        if (!(period3[d] > 0.0) || !std::isfinite(period3[d]) || !(search[d] > 0.0) ||
+            !(search[d] * 3.0 <= period3[d]))
+            return GBP_ERR_RANGE;
+    // as setup_xyz: its grid, its error model, its edges and thresholds
+    Geometry g;
+    choose_grid(g, period3, search, pbc, n2, reach, MAX_CELLS_PER_DIM, 0.0, block);
+    ErrModel em = err_model(g);
+    std::vector<double> E0(n_rp), E1(n_pi);
+    edges_top_walk(rp_bins, n_rp, E0.data());
+    edges_top_walk(pi_bins, n_pi, E1.data());
+    thresholds(n_rp, E0.data(), &em, 2, hi_rp, lo_rp);
+    thresholds(n_pi, E1.data(), &em, 1, hi_pi, lo_pi);
+    for (int d = 0; d < 3; d++) cell3[d] = g.c[d];
+    return GBP_OK;
+}
+
 int gbp_plan_set_graph(gbp_plan *plan, int enable) {
     if (!plan) return GBP_ERR_INVALID;
     plan->graph_mode = enable != 0;

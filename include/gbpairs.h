@@ -91,6 +91,14 @@ int gbp_grid_describe(const double *period3, int32_t pbc, const double *search3,
 int gbp_npairs_3d_thresholds(const double *period3, int32_t pbc, const double *rbins, int32_t nb,
                              int64_t n2, int32_t reach, int32_t block, float *hi, float *lo,
                              double *cell3);
+/* The same for npairs_xy_z (no reference counterpart): the grid of
+ * gbp_grid_describe for kind 2, and the thresholds of the rp axis (v = dx^2 +
+ * dy^2 against rp_bins^2) and of the pi axis (v = dz^2 against pi_bins^2), the
+ * edges walked from the top as npairs_xy_z_engine.pyx:183-194 does. */
+int gbp_npairs_xy_z_thresholds(const double *period3, int32_t pbc, const double *rp_bins,
+                               int32_t n_rp, const double *pi_bins, int32_t n_pi, int64_t n2,
+                               int32_t reach, int32_t block, float *hi_rp, float *lo_rp,
+                               float *hi_pi, float *lo_pi, double *cell3);
 /* 1: capture each call's stream work into one CUDA graph (instantiated once,
  * updated in place on later calls) and launch that; 0: launch directly. */
 int gbp_plan_set_graph(gbp_plan *plan, int enable);

@@ -42,7 +42,29 @@ def grid_and_thresholds(L, rbins, n2, reach=0, block=0):
     assert lib.gbp_npairs_3d_thresholds(_p(per, ctypes.c_double), 1, _p(rb, ctypes.c_double),
                                         len(rb), n2, reach, block, _p(hi, ctypes.c_float),
                                         _p(lo, ctypes.c_float), _p(c, ctypes.c_double)) == 0
-    return {"reach": out[0], "bf": out[1], "n": out[2], "DB": out[6], "c": c[0]}, hi, lo
+    return {"reach": out[0], "bf": out[1], "n": out[2], "DB": out[6], "c": c[0],
+            "n3": [out[2], out[3], out[4]], "c3": list(c)}, hi, lo
+
+
+def grid_and_thresholds_xy_z(L, rp, pi, n2, reach=0, block=0):
+    lib = N.load()
+    per = np.array([L] * 3)
+    rp = np.ascontiguousarray(rp, dtype=np.float64)
+    pi = np.ascontiguousarray(pi, dtype=np.float64)
+    out = (ctypes.c_int32 * 7)()
+    search = np.array([rp.max(), rp.max(), pi.max()])
+    assert lib.gbp_grid_describe(_p(per, ctypes.c_double), 1, _p(search, ctypes.c_double), n2,
+                                 2, reach, block, out) == 0
+    t = [np.zeros(len(a), np.float32) for a in (rp, rp, pi, pi)]
+    c = np.zeros(3)
+    fp = ctypes.c_float
+    assert lib.gbp_npairs_xy_z_thresholds(_p(per, ctypes.c_double), 1, _p(rp, ctypes.c_double),
+                                          len(rp), _p(pi, ctypes.c_double), len(pi), n2, reach,
+                                          block, _p(t[0], fp), _p(t[1], fp), _p(t[2], fp),
+                                          _p(t[3], fp), _p(c, ctypes.c_double)) == 0
+    g = {"reach": out[0], "bf": out[1], "DB": out[6], "n3": [out[2], out[3], out[4]],
+         "c3": list(c)}
+    return g, t
 
 
 def fma32(a, b, c):
@@ -65,12 +87,14 @@ def fma32(a, b, c):
     return r
 
 
-def v32_of(xi, xj, g, L, f32_input):
-    """The kernel's FP32 squared separation of i-point xi and j-point xj."""
-    c, bf, n, DB = g["c"], g["bf"], g["n"], g["DB"]
-    nbk = n // bf
+def deltas32(xi, xj, g, f32_input):
+    """The kernel's FP32 coordinate differences of i-point xi and j-point xj."""
+    bf, DB = g["bf"], g["DB"]
     dv = []
     for d in range(3):
+        c, n = g["c3"][d], g["n3"][d]
+        nbk = n // bf
+
         def rel(x):
             k = np.clip(np.floor(x * (1.0 / c)).astype(np.int64), 0, n - 1)
             ib = k // bf
@@ -88,20 +112,31 @@ def v32_of(xi, xj, g, L, f32_input):
         D = (ox * bf * c).astype(np.float32)
         t = (uj + D).astype(np.float32)
         dv.append((ui - t).astype(np.float32))
-    dx, dy, dz = dv
+    return dv
+
+
+def v32_of(xi, xj, g, L, f32_input):
+    """The 3-D count's FP32 squared separation: fma(dz, dz, fma(dy, dy, dx * dx))."""
+    dx, dy, dz = deltas32(xi, xj, g, f32_input)
     return fma32(dz, dz, fma32(dy, dy, (dx * dx).astype(np.float32)))
 
 
-def v64_of(xi, xj, L):
-    """npairs_3d_engine.pyx:167-176: (x1 - shift) - x2, squared, summed left to right."""
-    s = np.zeros(len(xi))
+def deltas64(xi, xj, L):
+    """npairs_*_engine.pyx: (x1 - shift) - x2 with the shift in {-L, 0, L} of the visit."""
+    out = []
     for d in range(3):
         best = None
         for shift in (0.0, L, -L):
             dd = (xi[:, d] - shift) - xj[:, d]
             best = dd if best is None else np.where(np.abs(dd) < np.abs(best), dd, best)
-        s = s + best * best if d < 2 else s + best * best
-    return s
+        out.append(best)
+    return out
+
+
+def v64_of(xi, xj, L):
+    """npairs_3d_engine.pyx:167-176: the differences squared and summed left to right."""
+    dx, dy, dz = deltas64(xi, xj, L)
+    return (dx * dx + dy * dy) + dz * dz
 
 
 def adversarial_pairs(rng, L, rbins, npairs, rel, f32_input):
@@ -157,3 +192,39 @@ def test_headline_grid_is_the_blocked_one():
     # the band is narrow at the outer edges, where most pairs lie: a few parts
     # per million (at the inner edges the offsets' absolute error dominates)
     assert np.all(((hi - lo) / E)[-5:] < 1e-5)
+
+
+@pytest.mark.parametrize("f32", [False, True])
+def test_fp32_thresholds_bracket_the_fp64_edges_xy_z(f32):
+    # the xyz2m geometry: rp 20 log edges 0.1-30, pi 40 linear edges 0-40
+    L = 1000.0
+    rp = np.logspace(-1, np.log10(30), 20)
+    pi = np.linspace(0.0, 40.0, 40)
+    g, (hr, lr, hp, lp) = grid_and_thresholds_xy_z(L, rp, pi, 2_000_000)
+    E0, E1 = rp * rp, pi * pi
+    rng = np.random.default_rng(21 + f32)
+    for rel in (3e-5, 3e-6, 4e-7):
+        n = 100_000
+        # half the pairs near an rp edge, half near a pi edge
+        k = rng.integers(0, len(rp), n)
+        q = rng.integers(1, len(pi), n)
+        near_rp = np.arange(n) < n // 2
+        r = np.where(near_rp, rp[k] * (1 + rng.uniform(-rel, rel, n)), rng.uniform(0, 30.0, n))
+        z = np.where(near_rp, rng.uniform(-40.0, 40.0, n),
+                     pi[q] * (1 + rng.uniform(-rel, rel, n)) * rng.choice([-1.0, 1.0], n))
+        phi = rng.uniform(0, 2 * np.pi, n)
+        xi = rng.uniform(0, L, (n, 3))
+        xj = np.mod(xi + np.stack([r * np.cos(phi), r * np.sin(phi), z], axis=1), L)
+        if f32:
+            xi = xi.astype(np.float32).astype(np.float64)
+            xj = np.minimum(xj.astype(np.float32).astype(np.float64), np.nextafter(L, 0))
+        for a, b in ((xi, xj), (xj, xi)):
+            dx, dy, dz = deltas32(a, b, g, f32)
+            v0 = fma32(dy, dy, (dx * dx).astype(np.float32))
+            v1 = (dz * dz).astype(np.float32)
+            ex, ey, ez = deltas64(a, b, L)
+            w0, w1 = ex * ex + ey * ey, ez * ez
+            for kk in range(len(E0)):
+                assert np.all(w0[v0 <= lr[kk]] <= E0[kk]) and np.all(w0[v0 > hr[kk]] > E0[kk]), kk
+            for kk in range(len(E1)):
+                assert np.all(w1[v1 <= lp[kk]] <= E1[kk]) and np.all(w1[v1 > hp[kk]] > E1[kk]), kk
