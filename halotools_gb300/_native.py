@@ -36,6 +36,7 @@ EXPORTED = (
     "gbp_zheng07_weights_batched", "gbp_zheng07_vjp_batched",
     "gbp_weighted_adjoint_3d", "gbp_zheng07_weights", "gbp_zheng07_vjp", "gbp_plan_set_limits",
     "gbp_grid_describe", "gbp_npairs_3d_thresholds", "gbp_npairs_xy_z_thresholds",
+    "gbp_npairs_3d_lut",
 )
 
 
@@ -174,6 +175,8 @@ def load(build_if_missing: bool = True):
         pf = P(ctypes.c_float)
         L.gbp_npairs_xy_z_thresholds.argtypes = [pd, i32, pd, i32, pd, i32, i64, i32, i32,
                                                  pf, pf, pf, pf, pd]
+        L.gbp_npairs_3d_lut.argtypes = [pd, i32, pd, i32, i64, i32, i32, pf,
+                                        P(ctypes.c_int32), pf]
         _lib = L
         return L
 

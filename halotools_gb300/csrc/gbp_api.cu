@@ -831,6 +831,37 @@ int gbp_npairs_xy_z_thresholds(const double *period3, int32_t pbc, const double 
     return GBP_OK;
 }
 
+int gbp_npairs_3d_lut(const double *period3, int32_t pbc, const double *rbins, int32_t nb,
+                      int64_t n2, int32_t reach, int32_t block, float *lut, int32_t *info,
+                      float *vrange) {
+    if (!period3 || !rbins || !lut || !info || !vrange || nb < 2 || nb > GBP_NB_LANE || n2 < 0 ||
+        reach < 0 || reach > 4 || block < 0 || block > 4)
+        return GBP_ERR_INVALID;
+    const double rmax = max_nan(rbins, nb);
+    const double search[3] = {rmax, rmax, rmax};
+    for (int d = 0; d < 3; d++)
+        if (!(period3[d] > 0.0) || !std::isfinite(period3[d]) || !(rmax > 0.0) ||
+            !(rmax * 3.0 <= period3[d]))
+            return GBP_ERR_RANGE;
+    // as gbp_npairs_3d: its grid, thresholds and float-bit table
+    Geometry g;
+    choose_grid(g, period3, search, pbc, n2, reach, MAX_CELLS_PER_DIM, 0.0, block,
+                GBP_DENSE_REACH2, true);
+    ErrModel em = err_model(g);
+    AxisHost ax;
+    std::vector<double> E(nb);
+    edges_top_walk(rbins, nb, E.data());
+    ax.set(E, &em, 3);
+    ax.make_lut(no_qband);
+    std::memcpy(lut, ax.lut.data(), sizeof(float4) * ax.T);
+    info[0] = ax.T;
+    info[1] = ax.S;
+    info[2] = ax.B;
+    vrange[0] = ax.vlo;
+    vrange[1] = ax.vhi;
+    return GBP_OK;
+}
+
 int gbp_plan_set_graph(gbp_plan *plan, int enable) {
     if (!plan) return GBP_ERR_INVALID;
     plan->graph_mode = enable != 0;

@@ -99,6 +99,16 @@ int gbp_npairs_xy_z_thresholds(const double *period3, int32_t pbc, const double 
                                int32_t n_rp, const double *pi_bins, int32_t n_pi, int64_t n2,
                                int32_t reach, int32_t block, float *hi_rp, float *lo_rp,
                                float *hi_pi, float *lo_pi, double *cell3);
+/* The float-bit lookup table an npairs_3d call bins with (no reference
+ * counterpart; for tests of the table): lut receives info[0] = T slots of 4
+ * floats {first bin (int bits), upper threshold, lower threshold, unused}
+ * (room for 1024 slots), info[1..2] = the right shift S and the first slot's
+ * shifted bits B, vrange = the clamp range {vlo, vhi}.  A value v falls in slot
+ * (bits(clamp(v)) >> S) - B; its bin is b0 + (v > upper), and the pair is
+ * rechecked when lower < v <= upper. */
+int gbp_npairs_3d_lut(const double *period3, int32_t pbc, const double *rbins, int32_t nb,
+                      int64_t n2, int32_t reach, int32_t block, float *lut, int32_t *info,
+                      float *vrange);
 /* 1: capture each call's stream work into one CUDA graph (instantiated once,
  * updated in place on later calls) and launch that; 0: launch directly. */
 int gbp_plan_set_graph(gbp_plan *plan, int enable);

@@ -228,3 +228,48 @@ def test_fp32_thresholds_bracket_the_fp64_edges_xy_z(f32):
                 assert np.all(w0[v0 <= lr[kk]] <= E0[kk]) and np.all(w0[v0 > hr[kk]] > E0[kk]), kk
             for kk in range(len(E1)):
                 assert np.all(w1[v1 <= lp[kk]] <= E1[kk]) and np.all(w1[v1 > hp[kk]] > E1[kk]), kk
+
+
+def lut_of(L, rbins, n2, reach=0, block=0):
+    lib = N.load()
+    per = np.array([L] * 3)
+    rb = np.ascontiguousarray(rbins, dtype=np.float64)
+    lut = np.zeros((1024, 4), np.float32)
+    info = np.zeros(3, np.int32)
+    vr = np.zeros(2, np.float32)
+    assert lib.gbp_npairs_3d_lut(_p(per, ctypes.c_double), 1, _p(rb, ctypes.c_double), len(rb),
+                                 n2, reach, block, _p(lut, ctypes.c_float),
+                                 _p(info, ctypes.c_int32), _p(vr, ctypes.c_float)) == 0
+    T, S, B = (int(v) for v in info)
+    return lut[:T], S, B, vr
+
+
+@pytest.mark.parametrize("L,rbins,n2", [c[:3] for c in CASES])
+def test_bin_table_agrees_with_the_thresholds(L, rbins, n2):
+    # the kernel bins v by one table slot: b0 + (v > upper), rechecked when
+    # lower < v <= upper.  Where that does not ask for a recheck, the bin must be
+    # the one the per-edge thresholds prove: every edge below it provably
+    # exceeded (v > hi), its own edge provably not (v <= lo), or past the top
+    lut, S, B, (vlo, vhi) = lut_of(L, rbins, n2)
+    _, hi, lo = grid_and_thresholds(L, rbins, n2)
+    rng = np.random.default_rng(int(L))
+    # values log-uniform over the table's range and beyond, plus every threshold
+    # and its float neighbours
+    v = np.exp(rng.uniform(np.log(vlo) - 2, np.log(vhi) + 2, 400_000)).astype(np.float32)
+    th = np.concatenate([hi, lo, [vlo, vhi, 0.0]]).astype(np.float32)
+    v = np.concatenate([v, th, np.nextafter(th, np.float32(np.inf)),
+                        np.nextafter(th, np.float32(-np.inf)), [np.float32(0.0)]])
+    v = v[np.isfinite(v) & (v >= 0)]
+    vc = np.clip(v, vlo, vhi)
+    slot = (vc.view(np.uint32) >> np.uint32(S)).astype(np.int64) - B
+    assert np.all((slot >= 0) & (slot < len(lut)))
+    e = lut[slot]
+    b0 = e[:, 0].view(np.int32)
+    up, low = e[:, 1], e[:, 2]
+    b = b0 + (v > up)
+    walk = (v > low) & ~(v > up)
+    nb = len(hi)
+    for i in np.flatnonzero(~walk):
+        k = b[i]
+        assert np.all(v[i] > hi[:k]), (v[i], k)
+        assert k == nb or v[i] <= lo[k], (v[i], k)
