@@ -862,6 +862,39 @@ int gbp_npairs_3d_lut(const double *period3, int32_t pbc, const double *rbins, i
     return GBP_OK;
 }
 
+int gbp_stencil_describe(const double *period3, int32_t pbc, const double *search3, int64_t n2,
+                         int32_t kind, int32_t reach, int32_t block, int32_t autocorr,
+                         int32_t *runs, int32_t *nruns) {
+    if (!period3 || !search3 || !runs || !nruns || n2 < 0 || kind < 0 || kind > 2 || reach < 0 ||
+        reach > 4 || block < 0 || block > 4)
+        return GBP_ERR_INVALID;
+    for (int d = 0; d < 3; d++)
+        if (!(period3[d] > 0.0) || !std::isfinite(period3[d]) || !(search3[d] > 0.0) ||
+            !(search3[d] * 3.0 <= period3[d]))
+            return GBP_ERR_RANGE;
+    // the grid and stencil of gbp_grid_describe
+    Geometry g;
+    if (kind == 2) {
+        choose_grid(g, period3, search3, pbc, n2, reach, MAX_CELLS_PER_DIM, 0.0, block);
+    } else {
+        choose_grid(g, period3, search3, pbc, n2, reach, MAX_CELLS_PER_DIM, 0.0, block,
+                    GBP_DENSE_REACH2, true);
+    }
+    build_stencil(g, search3, kind == 2 ? 1 : 0, autocorr != 0);
+    for (int s = 0; s < g.nsten; s++) {
+        const int w = g.sten[s];
+        int span;
+        std::memcpy(&span, &g.stenD[s].w, 4);
+        runs[5 * s + 0] = (w & 0xff) - 64;
+        runs[5 * s + 1] = ((w >> 8) & 0xff) - 64;
+        runs[5 * s + 2] = ((w >> 16) & 0xff) - 64;
+        runs[5 * s + 3] = (w >> 24) & 0xff;
+        runs[5 * s + 4] = span;
+    }
+    *nruns = g.nsten;
+    return GBP_OK;
+}
+
 int gbp_plan_set_graph(gbp_plan *plan, int enable) {
     if (!plan) return GBP_ERR_INVALID;
     plan->graph_mode = enable != 0;

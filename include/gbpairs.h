@@ -109,6 +109,15 @@ int gbp_npairs_xy_z_thresholds(const double *period3, int32_t pbc, const double 
 int gbp_npairs_3d_lut(const double *period3, int32_t pbc, const double *rbins, int32_t nb,
                       int64_t n2, int32_t reach, int32_t block, float *lut, int32_t *info,
                       float *vrange);
+/* The stencil of the grid gbp_grid_describe gives (no reference counterpart;
+ * for tests of its pruning): per run 5 ints {block offset x, y, z, first fine
+ * cell, fine cells} into runs (room for 729 runs), their number into nruns.
+ * A fine cell (lx, ly, lz) of a block is (lx * bf + ly) * bf + lz.  With
+ * autocorr only the own block and the lexicographically positive block offsets
+ * are listed (each unordered block pair once). */
+int gbp_stencil_describe(const double *period3, int32_t pbc, const double *search3, int64_t n2,
+                         int32_t kind, int32_t reach, int32_t block, int32_t autocorr,
+                         int32_t *runs, int32_t *nruns);
 /* 1: capture each call's stream work into one CUDA graph (instantiated once,
  * updated in place on later calls) and launch that; 0: launch directly. */
 int gbp_plan_set_graph(gbp_plan *plan, int enable);
