@@ -36,7 +36,7 @@ EXPORTED = (
     "gbp_zheng07_weights_batched", "gbp_zheng07_vjp_batched",
     "gbp_weighted_adjoint_3d", "gbp_zheng07_weights", "gbp_zheng07_vjp", "gbp_plan_set_limits",
     "gbp_grid_describe", "gbp_npairs_3d_thresholds", "gbp_npairs_xy_z_thresholds",
-    "gbp_npairs_3d_lut", "gbp_stencil_describe",
+    "gbp_npairs_3d_lut", "gbp_stencil_describe", "gbp_npairs_s_mu_tables",
 )
 
 
@@ -179,6 +179,8 @@ def load(build_if_missing: bool = True):
                                         P(ctypes.c_int32), pf]
         L.gbp_stencil_describe.argtypes = [pd, i32, pd, i64, i32, i32, i32, i32,
                                            P(ctypes.c_int32), P(ctypes.c_int32)]
+        L.gbp_npairs_s_mu_tables.argtypes = [pd, i32, pd, i32, pd, i32, i64, i32, i32, pf, pf, pf,
+                                             pf, pf, pf, P(ctypes.c_int32), pf, pd]
         _lib = L
         return L
 

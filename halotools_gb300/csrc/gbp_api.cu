@@ -1160,27 +1160,14 @@ int gbp_marked_npairs_xy_z(gbp_plan *plan, const double *xyz1, int64_t n1, const
     return GBP_OK;
 }
 
-// (s, mu') geometry shared by npairs_s_mu and weighted_npairs_s_mu: differential
-// bins found by the strict walks of npairs_s_mu_engine.pyx:200-226, the FP32
-// guard bands, and the per-slot error bound of q = dxy / s^2
-static int setup_smu(gbp_plan *plan, Call &c, const double *xyz1, int64_t n1, const double *xyz2,
-                     int64_t n2, const double *s_bins, int32_t n_s, const double *mu_prime,
-                     int32_t n_mu, const double *period3, int32_t pbc, int32_t mem) {
-    int rc = check_common(plan, xyz1, n1, xyz2, n2, period3, pbc, mem);
-    if (rc) return rc;
-    if (!s_bins || !mu_prime || n_s < 2 || n_mu < 2 || n_s > GBP_NB_MAX || n_mu > GBP_NB_MAX)
-        return fail(plan, GBP_ERR_INVALID, "bin arrays must have 2..%d entries", GBP_NB_MAX);
-    double smax = max_nan(s_bins, n_s);
-    double search[3] = {smax, smax, smax};
-    if ((rc = check_search(plan, search, period3))) return rc;
-    c.xyz1 = xyz1;
-    c.xyz2 = xyz2;
-    c.n1 = n1;
-    c.n2 = n2;
-    c.autocorr = (xyz1 == xyz2 && n1 == n2 && c.w1 == c.w2);
-    c.mem = mem;
-    c.naxes = 2;
-    choose_grid(c.g, period3, search, pbc, n2, plan->reach, MAX_CELLS_PER_DIM, 0.0, plan->block,
+// The (s, mu') grid, stencil and tables of a call: the differential bins of
+// the strict walks (edges_smu), the s thresholds with the per-slot bound of q,
+// and the tight FP32 bracket of each mu'^2 edge (the band of q is per pair)
+static void smu_tables(Call &c, const double *period3, int32_t pbc, int64_t n2, int reach, int block,
+                       const double *s_bins, int32_t n_s, const double *mu_prime, int32_t n_mu) {
+    const double smax = max_nan(s_bins, n_s);
+    const double search[3] = {smax, smax, smax};
+    choose_grid(c.g, period3, search, pbc, n2, reach, MAX_CELLS_PER_DIM, 0.0, block,
                 c.mode == MODE_SMU ? GBP_DENSE_REACH2 : 28.0, c.mode == MODE_SMU);
     build_stencil(c.g, search, 0, c.autocorr);
     ErrModel em = err_model(c.g);
@@ -1207,6 +1194,67 @@ static int setup_smu(gbp_plan *plan, Call &c, const double *xyz1, int64_t n1, co
         return f_up(2.0 * qb);
     });
     c.ax[1].make_lut(no_qband);
+}
+
+// (s, mu') geometry shared by npairs_s_mu and weighted_npairs_s_mu: differential
+// bins found by the strict walks of npairs_s_mu_engine.pyx:200-226, the FP32
+// guard bands, and the per-slot error bound of q = dxy / s^2
+static int setup_smu(gbp_plan *plan, Call &c, const double *xyz1, int64_t n1, const double *xyz2,
+                     int64_t n2, const double *s_bins, int32_t n_s, const double *mu_prime,
+                     int32_t n_mu, const double *period3, int32_t pbc, int32_t mem) {
+    int rc = check_common(plan, xyz1, n1, xyz2, n2, period3, pbc, mem);
+    if (rc) return rc;
+    if (!s_bins || !mu_prime || n_s < 2 || n_mu < 2 || n_s > GBP_NB_MAX || n_mu > GBP_NB_MAX)
+        return fail(plan, GBP_ERR_INVALID, "bin arrays must have 2..%d entries", GBP_NB_MAX);
+    double smax = max_nan(s_bins, n_s);
+    double search[3] = {smax, smax, smax};
+    if ((rc = check_search(plan, search, period3))) return rc;
+    c.xyz1 = xyz1;
+    c.xyz2 = xyz2;
+    c.n1 = n1;
+    c.n2 = n2;
+    c.autocorr = (xyz1 == xyz2 && n1 == n2 && c.w1 == c.w2);
+    c.mem = mem;
+    c.naxes = 2;
+    smu_tables(c, period3, pbc, n2, plan->reach, plan->block, s_bins, n_s, mu_prime, n_mu);
+    return GBP_OK;
+}
+
+int gbp_npairs_s_mu_tables(const double *period3, int32_t pbc, const double *s_bins, int32_t n_s,
+                           const double *mu_prime, int32_t n_mu, int64_t n2, int32_t reach,
+                           int32_t block, float *s_lut, float *s_hi, float *s_lo, float *q_lut,
+                           float *q_hi, float *q_lo, int32_t *info, float *vrange, double *cell3) {
+    if (!period3 || !s_bins || !mu_prime || !s_lut || !s_hi || !s_lo || !q_lut || !q_hi ||
+        !q_lo || !info || !vrange || !cell3 || n_s < 2 || n_mu < 2 || n_s > GBP_NB_MAX ||
+        n_mu > GBP_NB_MAX || n2 < 0 || reach < 0 || reach > 4 || block < 0 || block > 4)
+        return GBP_ERR_INVALID;
+    const double smax = max_nan(s_bins, n_s);
+    for (int d = 0; d < 3; d++)
+        if (!(period3[d] > 0.0) || !std::isfinite(period3[d]) || !(smax > 0.0) ||
+            !(smax * 3.0 <= period3[d]))
+            return GBP_ERR_RANGE;
+    // the tables an npairs_s_mu auto-correlation builds (smu_tables)
+    Call c;
+    c.mode = MODE_SMU;
+    c.autocorr = true;
+    smu_tables(c, period3, pbc, n2, reach, block, s_bins, n_s, mu_prime, n_mu);
+    std::memcpy(s_lut, c.ax[0].lut.data(), sizeof(float4) * c.ax[0].T);
+    std::memcpy(q_lut, c.ax[1].lut.data(), sizeof(float4) * c.ax[1].T);
+    for (int k = 0; k < n_s; k++) {
+        s_hi[k] = c.ax[0].hi[k];
+        s_lo[k] = c.ax[0].lo[k];
+    }
+    for (int k = 0; k < n_mu; k++) {
+        q_hi[k] = c.ax[1].hi[k];
+        q_lo[k] = c.ax[1].lo[k];
+    }
+    const int vals[6] = {c.ax[0].T, c.ax[0].S, c.ax[0].B, c.ax[1].T, c.ax[1].S, c.ax[1].B};
+    for (int k = 0; k < 6; k++) info[k] = vals[k];
+    vrange[0] = c.ax[0].vlo;
+    vrange[1] = c.ax[0].vhi;
+    vrange[2] = c.ax[1].vlo;
+    vrange[3] = c.ax[1].vhi;
+    for (int d = 0; d < 3; d++) cell3[d] = c.g.c[d];
     return GBP_OK;
 }
 

@@ -118,6 +118,19 @@ int gbp_npairs_3d_lut(const double *period3, int32_t pbc, const double *rbins, i
 int gbp_stencil_describe(const double *period3, int32_t pbc, const double *search3, int64_t n2,
                          int32_t kind, int32_t reach, int32_t block, int32_t autocorr,
                          int32_t *runs, int32_t *nruns);
+/* The binning tables of an npairs_s_mu auto-correlation, computed on the host
+ * without a GPU (no reference counterpart; for tests of the (s, mu') error
+ * bounds).  s_lut / q_lut receive the float-bit tables of s^2 and of
+ * q = mu'^2 = dxy / s^2 as gbp_npairs_3d_lut does (the s slots carry, in their
+ * 4th float, the bound on the error of the FP32 quotient q for every s^2 of the
+ * slot); s_hi / s_lo (n_s) and q_hi / q_lo (n_mu) the thresholds of the
+ * differential edges that the strict walks of npairs_s_mu_engine.pyx:198-226
+ * define; info = {T, S, B} of s, then of q; vrange = {vlo, vhi} of s, then of
+ * q; cell3 the fine cell size per dimension. */
+int gbp_npairs_s_mu_tables(const double *period3, int32_t pbc, const double *s_bins, int32_t n_s,
+                           const double *mu_prime, int32_t n_mu, int64_t n2, int32_t reach,
+                           int32_t block, float *s_lut, float *s_hi, float *s_lo, float *q_lut,
+                           float *q_hi, float *q_lo, int32_t *info, float *vrange, double *cell3);
 /* 1: capture each call's stream work into one CUDA graph (instantiated once,
  * updated in place on later calls) and launch that; 0: launch directly. */
 int gbp_plan_set_graph(gbp_plan *plan, int enable);

@@ -273,3 +273,127 @@ def test_bin_table_agrees_with_the_thresholds(L, rbins, n2):
         k = b[i]
         assert np.all(v[i] > hi[:k]), (v[i], k)
         assert k == nb or v[i] <= lo[k], (v[i], k)
+
+
+def smu_tables(L, sb, mup, n2):
+    lib = N.load()
+    per = np.array([L] * 3)
+    sb = np.ascontiguousarray(sb, dtype=np.float64)
+    mup = np.ascontiguousarray(mup, dtype=np.float64)
+    fp = ctypes.c_float
+    s_lut = np.zeros((1024, 4), np.float32)
+    q_lut = np.zeros((1024, 4), np.float32)
+    s_hi, s_lo = np.zeros(len(sb), np.float32), np.zeros(len(sb), np.float32)
+    q_hi, q_lo = np.zeros(len(mup), np.float32), np.zeros(len(mup), np.float32)
+    info = np.zeros(6, np.int32)
+    vr = np.zeros(4, np.float32)
+    c = np.zeros(3)
+    assert lib.gbp_npairs_s_mu_tables(
+        _p(per, ctypes.c_double), 1, _p(sb, ctypes.c_double), len(sb), _p(mup, ctypes.c_double),
+        len(mup), n2, 0, 0, _p(s_lut, fp), _p(s_hi, fp), _p(s_lo, fp), _p(q_lut, fp),
+        _p(q_hi, fp), _p(q_lo, fp), _p(info, ctypes.c_int32), _p(vr, fp),
+        _p(c, ctypes.c_double)) == 0
+    T0, S0, B0, T1, S1, B1 = (int(v) for v in info)
+    out = (ctypes.c_int32 * 7)()
+    search = np.array([sb.max()] * 3)
+    assert lib.gbp_grid_describe(_p(per, ctypes.c_double), 1, _p(search, ctypes.c_double), n2, 1,
+                                 0, 0, out) == 0
+    g = {"bf": out[1], "DB": out[6], "n3": [out[2], out[3], out[4]], "c3": list(c)}
+    return g, dict(s_lut=s_lut[:T0], S0=S0, B0=B0, s_hi=s_hi, s_lo=s_lo, q_lut=q_lut[:T1], S1=S1,
+                   B1=B1, q_hi=q_hi, q_lo=q_lo, vr=vr)
+
+
+def slot_of(v, vlo, vhi, S, B):
+    return (np.clip(v, vlo, vhi).view(np.uint32) >> np.uint32(S)).astype(np.int64) - B
+
+
+def smu_kernel_bins(v0, v1, q, t):
+    """The (s, mu') kernel's binning of FP32 s^2 = v0, dxy = v1 and quotient q:
+    (s bin, mu' bin, settled).  A pair not settled goes to the FP64 recheck."""
+    ns, nq = len(t["s_hi"]), len(t["q_hi"])
+    e0 = t["s_lut"][slot_of(v0, t["vr"][0], t["vr"][1], t["S0"], t["B0"])]
+    b0 = e0[:, 0].view(np.int32)
+    bs = b0 + (v0 > e0[:, 1])
+    amb = (v0 > e0[:, 2]) & ~(v0 > e0[:, 1])
+    qb = e0[:, 3]
+    # the q thresholds as the kernel lays them out: {thr, lo, hi below, lo above}
+    hq = np.zeros((nq + 2, 4), np.float32)
+    for k in range(nq):
+        hq[k] = (t["q_hi"][k], t["q_lo"][k], t["q_hi"][k - 1] if k > 0 else -3.0e38,
+                 t["q_lo"][k + 1] if k + 1 < nq else 3.0e38)
+    hq[nq] = (np.inf, 3.0e38, t["q_hi"][nq - 1], 3.0e38)
+    hq[nq + 1] = (np.inf, -np.inf, -3.0e38, 3.0e38)
+    e1 = t["q_lut"][slot_of(q, t["vr"][2], t["vr"][3], t["S1"], t["B1"])]
+    bq0 = e1[:, 0].view(np.int32)
+    h = np.where((bq0 < nq) & (e1[:, 2] == -np.inf), nq + 1, bq0)
+    th = hq[h]
+    up = q > th[:, 0]
+    bq = bq0 + up
+    below = np.where(up, th[:, 0], th[:, 2])
+    above = np.where(up, th[:, 3], th[:, 1])
+    walk = th[:, 1] < -3.0e38
+    amb |= ~(q - below > qb) | ~(above - q > qb) | walk
+    return bs, bq, ~amb
+
+
+@pytest.mark.parametrize("f32", [False, True])
+def test_s_mu_bins_settled_in_fp32_are_the_fp64_bins(f32):
+    # config 5's (s, mu') geometry: 30 log s bins 0.5-50, 21 linear mu edges 0-1
+    L = 2000.0
+    sb = np.logspace(np.log10(0.5), np.log10(50), 30)
+    mu = np.linspace(0.0, 1.0, 21)
+    mup = np.sort(np.sin(np.arccos(mu)))
+    g, t = smu_tables(L, sb, mup, 10_000_000)
+    Es, Eq = sb * sb, mup * mup
+    rng = np.random.default_rng(31 + f32)
+    settled = 0
+    for rel in (3e-5, 3e-6, 4e-7):
+        n = 100_000
+        # half near an s edge (random direction), half near a mu' edge (random s)
+        k = rng.integers(0, len(sb), n)
+        qk = rng.integers(0, len(mup), n)
+        s = np.where(np.arange(n) < n // 2, sb[k] * (1 + rng.uniform(-rel, rel, n)),
+                     sb[-1] * rng.uniform(0.02, 1.0, n) ** (1 / 3))
+        qq = np.where(np.arange(n) < n // 2, rng.uniform(0, 1, n),
+                      np.clip(Eq[qk] * (1 + rng.uniform(-rel, rel, n)), 0, 1))
+        phi = rng.uniform(0, 2 * np.pi, n)
+        rxy = s * np.sqrt(qq)
+        dz = s * np.sqrt(1 - qq) * rng.choice([-1.0, 1.0], n)
+        xi = rng.uniform(0, L, (n, 3))
+        xj = np.mod(xi + np.stack([rxy * np.cos(phi), rxy * np.sin(phi), dz], axis=1), L)
+        if f32:
+            xi = xi.astype(np.float32).astype(np.float64)
+            xj = np.minimum(xj.astype(np.float32).astype(np.float64), np.nextafter(L, 0))
+        for a, b in ((xi, xj), (xj, xi)):
+            dx, dy, dzz = deltas32(a, b, g, f32)
+            v1 = fma32(dy, dy, (dx * dx).astype(np.float32))
+            v0 = fma32(dzz, dzz, v1)
+            ex, ey, ez = deltas64(a, b, L)
+            dxy = ex * ex + ey * ey
+            s2 = ez * ez + dxy
+            mu2 = np.where(s2 > 0, dxy / np.where(s2 > 0, s2, 1.0), 0.0)
+            ms = np.searchsorted(Es, s2, side="left")
+            mq = np.searchsorted(Eq, mu2, side="left")
+            ok = v0 > 0
+            qrn = np.zeros_like(v0)
+            qrn[ok] = v1[ok] / v0[ok]
+            # the FP32 quotient is within 2 ulp of the exact one: every float
+            # within 2 ulp of the rounded quotient
+            for step in (-2, -1, 0, 1, 2):
+                q = qrn.copy()
+                for _ in range(abs(step)):
+                    q = np.nextafter(q, np.float32(np.inf if step > 0 else -np.inf))
+                bs, bq, settled_k = smu_kernel_bins(v0, v1, q, t)
+                sel = ok & settled_k & (bs < len(sb))
+                # a settled pair lands in the reference's (s, mu') bin, or both
+                # leave it out beyond the top mu' edge
+                assert np.all(ms[sel] == bs[sel]), "s bin"
+                cnt = sel & (bq < len(mup))
+                assert np.all(mq[cnt] == bq[cnt]), "mu bin"
+                drop = sel & (bq >= len(mup))
+                assert np.all(mq[drop] >= len(mup)), "mu gate"
+                # s beyond the top edge, settled in FP32: the reference skips it too
+                gate = ok & (bs >= len(sb))
+                assert np.all(ms[gate] >= len(sb)), "s gate"
+                settled += int(np.count_nonzero(sel))
+    assert settled > 0
