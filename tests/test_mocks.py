@@ -5,7 +5,6 @@ Zheng07 mean occupations, zheng07_components.py:149-153, 455-470)."""
 import math
 
 import numpy as np
-import pytest
 
 from halotools_gb300 import mocks
 
